@@ -1,0 +1,3 @@
+"""CPU oracle for the hypervector encode / cosine top-k / propagate path.
+
+Test infrastructure only (the checker): the product never imports this."""

@@ -1,0 +1,548 @@
+/*
+ * hdc_oracle.c -- CPU oracle for the k-mer hypervector encode / cosine top-k /
+ * propagate-children path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker: only the test suite,
+ * the smoke check and the CPU-baseline leg of the benchmark load it.  The
+ * product library never links or calls it.
+ *
+ * It is a plain C restatement of the reference's CPU algorithm (citations are
+ * to files of benlaflen/bacterial-classification):
+ *
+ *   base hypervectors   src/HV.cpp:20-41 (make_hv: mt19937_64(seed), one draw
+ *                       per 64-bit word, tail bits masked; A,C,T,G use seeds
+ *                       0,1,2,3; src/HV.cpp:43-51 get_base_hv)
+ *   permute + bind      src/HV.cpp:98-147 (mult: out_j = l_j ^ r_{(j+s) mod 64W})
+ *   k-mer binder        src/encoder.cpp:47-74 (canonical = min(s, revcomp(s)) in
+ *                       std::string order; binder = ~0 ^ rot_0(b0) ^ ... ^
+ *                       rot_{k-1}(b_{k-1}) over the canonical k-mer's bases)
+ *   bundle              src/HV.cpp:156-216 (superpose_batch: +1 per set bit,
+ *                       -1 per clear bit, int16 accumulator)
+ *   sequence encode     src/encoder.cpp:106-132 (HVCache::compute: every k-mer
+ *                       position 0..len-k, k-mers holding a byte outside
+ *                       "ACGT" are skipped)
+ *   cosine              src/HV.cpp:219-252 (int64 dot and norms; NORM_COSINE
+ *                       returns float(2*(dot/(sqrt(nl)*sqrt(nr)) - 0.5)), -1 when
+ *                       a norm is zero; without NORM_COSINE returns float(dot))
+ *   greedy propagate    targets/propogate-children.cpp:60-73
+ *
+ * The mt19937_64 generator below follows the published MT19937-64 algorithm
+ * (Matsumoto & Nishimura), whose parameters the C++ standard fixes for
+ * std::mt19937_64.
+ *
+ * Ranking rule used everywhere: descending float score, ties broken by the
+ * lower reference index (the first maximum wins, as in the reference's
+ * brute-force CPU argmax, tests/cosine_comparison_test.cpp:146-156).
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------ */
+/* MT19937-64                                                          */
+/* ------------------------------------------------------------------ */
+#define MT_N 312
+#define MT_M 156
+#define MT_A 0xB5026F5AA96619E9ULL
+#define MT_UPPER 0xFFFFFFFF80000000ULL
+#define MT_LOWER 0x000000007FFFFFFFULL
+
+typedef struct {
+    uint64_t s[MT_N];
+    int i;
+} orc_mt64;
+
+static void mt_seed(orc_mt64* g, uint64_t seed) {
+    g->s[0] = seed;
+    for (int i = 1; i < MT_N; ++i)
+        g->s[i] = 6364136223846793005ULL * (g->s[i - 1] ^ (g->s[i - 1] >> 62)) + (uint64_t)i;
+    g->i = MT_N;
+}
+
+static uint64_t mt_next(orc_mt64* g) {
+    if (g->i >= MT_N) {
+        for (int j = 0; j < MT_N; ++j) {
+            uint64_t y = (g->s[j] & MT_UPPER) | (g->s[(j + 1) % MT_N] & MT_LOWER);
+            uint64_t v = g->s[(j + MT_M) % MT_N] ^ (y >> 1);
+            if (y & 1ULL) v ^= MT_A;
+            g->s[j] = v;
+        }
+        g->i = 0;
+    }
+    uint64_t x = g->s[g->i++];
+    x ^= (x >> 29) & 0x5555555555555555ULL;
+    x ^= (x << 17) & 0x71D67FFFEDA60000ULL;
+    x ^= (x << 37) & 0xFFF7EEE000000000ULL;
+    x ^= (x >> 43);
+    return x;
+}
+
+/* First n outputs of mt19937_64(seed); used to pin the generator. */
+void orc_mt64_stream(uint64_t seed, int n, uint64_t* out) {
+    orc_mt64 g;
+    mt_seed(&g, seed);
+    for (int i = 0; i < n; ++i) out[i] = mt_next(&g);
+}
+
+/* ------------------------------------------------------------------ */
+/* Hypervector primitives                                              */
+/* ------------------------------------------------------------------ */
+static int words64(int dim) { return (dim + 63) / 64; }
+
+static uint64_t tail_mask(int dim) {
+    int excess = words64(dim) * 64 - dim;
+    return excess ? (~0ULL >> excess) : ~0ULL;
+}
+
+/* code: A=0 C=1 G=2 T=3 (std::string order); anything else is invalid. */
+static int base_code(char c) {
+    switch (c) {
+        case 'A': return 0;
+        case 'C': return 1;
+        case 'G': return 2;
+        case 'T': return 3;
+        default: return -1;
+    }
+}
+
+/* Seeds per code, from get_base_hv: A->0, C->1, G->3, T->2. */
+static const int SEED_OF_CODE[4] = {0, 1, 3, 2};
+
+/* out: [4][W] words, indexed by base code (A,C,G,T). */
+int orc_base_hvs(int dim, uint64_t* out) {
+    int W = words64(dim);
+    for (int c = 0; c < 4; ++c) {
+        orc_mt64 g;
+        mt_seed(&g, (uint64_t)SEED_OF_CODE[c]);
+        for (int w = 0; w < W; ++w) out[c * W + w] = mt_next(&g);
+        out[c * W + W - 1] &= tail_mask(dim);
+    }
+    return W;
+}
+
+/* mult(l, r, out, s): out_j = l_j ^ r_{(j+s) mod 64W} for s < 64, tail masked. */
+static void mult(const uint64_t* l, const uint64_t* r, uint64_t* out, int W, int s, uint64_t tmask) {
+    uint64_t tmp[W];
+    for (int w = 0; w < W; ++w) {
+        uint64_t rw;
+        if (s == 0)
+            rw = r[w];
+        else
+            rw = (r[w] >> s) | (r[(w + 1) % W] << (64 - s));
+        tmp[w] = l[w] ^ rw;
+    }
+    memcpy(out, tmp, sizeof(uint64_t) * (size_t)W);
+    out[W - 1] &= tmask;
+}
+
+/* Lexicographic code of a k-mer (first base most significant), or -1. */
+static int64_t lex_code(const char* s, int k) {
+    int64_t v = 0;
+    for (int i = 0; i < k; ++i) {
+        int c = base_code(s[i]);
+        if (c < 0) return -1;
+        v = (v << 2) | c;
+    }
+    return v;
+}
+
+/* canonical = min(s, revcomp(s)) under std::string ordering (A<C<G<T). */
+int64_t orc_canonical(const char* kmer, int k) {
+    int64_t f = lex_code(kmer, k);
+    if (f < 0) return -1;
+    int64_t r = 0;
+    for (int i = k - 1; i >= 0; --i) r = (r << 2) | (3 - base_code(kmer[i]));
+    return f < r ? f : r;
+}
+
+/* binder of a canonical k-mer code: start from all-ones, then mult by the
+ * base of digit i rotated by i, for i = 0 (first base) .. k-1. */
+void orc_binder(int dim, int k, int64_t canon, uint64_t* out) {
+    int W = words64(dim);
+    uint64_t tm = tail_mask(dim);
+    uint64_t* base = (uint64_t*)malloc(sizeof(uint64_t) * 4 * (size_t)W);
+    orc_base_hvs(dim, base);
+    for (int w = 0; w < W; ++w) out[w] = ~0ULL;
+    out[W - 1] &= tm;
+    for (int i = 0; i < k; ++i) {
+        int c = (int)((canon >> (2 * (k - 1 - i))) & 3);
+        mult(out, base + (size_t)c * W, out, W, i, tm);
+    }
+    free(base);
+}
+
+/* Rotated base table R[i][c][W] = rot_i(base[c]); lets a binder be built as
+ * ~0 ^ XOR_i R[i][c_i] (equal to the chain of mult calls: each output bit
+ * depends only on the same bit of l, and the tail is masked at the end). */
+typedef struct {
+    int dim, k, W;
+    uint64_t tmask;
+    uint64_t* rot; /* [k][4][W] */
+} orc_tables;
+
+static void tables_init(orc_tables* t, int dim, int k) {
+    t->dim = dim;
+    t->k = k;
+    t->W = words64(dim);
+    t->tmask = tail_mask(dim);
+    uint64_t* base = (uint64_t*)malloc(sizeof(uint64_t) * 4 * (size_t)t->W);
+    orc_base_hvs(dim, base);
+    t->rot = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)k * 4 * (size_t)t->W);
+    uint64_t* zero = (uint64_t*)calloc((size_t)t->W, sizeof(uint64_t));
+    for (int i = 0; i < k; ++i)
+        for (int c = 0; c < 4; ++c)
+            mult(zero, base + (size_t)c * t->W, t->rot + ((size_t)i * 4 + c) * t->W, t->W, i, ~0ULL);
+    free(zero);
+    free(base);
+}
+
+static void tables_free(orc_tables* t) { free(t->rot); }
+
+static void tables_binder(const orc_tables* t, int64_t canon, uint64_t* out) {
+    int W = t->W, k = t->k;
+    for (int w = 0; w < W; ++w) out[w] = ~0ULL;
+    for (int i = 0; i < k; ++i) {
+        int c = (int)((canon >> (2 * (k - 1 - i))) & 3);
+        const uint64_t* r = t->rot + ((size_t)i * 4 + c) * W;
+        for (int w = 0; w < W; ++w) out[w] ^= r[w];
+    }
+    out[W - 1] &= t->tmask;
+}
+
+/* HVCache::compute: counts in int32, returned modulo 2^16 like the int16
+ * accumulator of superpose_batch.  Returns the number of k-mers bundled. */
+static int64_t encode_one(const orc_tables* t, const char* seq, int64_t len, int32_t* acc, uint64_t* scratch) {
+    int dim = t->dim, k = t->k;
+    memset(acc, 0, sizeof(int32_t) * (size_t)dim);
+    int64_t n = 0;
+    for (int64_t p = 0; p + k <= len; ++p) {
+        int64_t canon = orc_canonical(seq + p, k);
+        if (canon < 0) continue;
+        tables_binder(t, canon, scratch);
+        for (int d = 0; d < dim; ++d) acc[d] += ((scratch[d >> 6] >> (d & 63)) & 1ULL) ? 1 : -1;
+        ++n;
+    }
+    return n;
+}
+
+/* Encode one sequence (whole-sequence semantics) into int16[dim]. */
+int64_t orc_encode(int dim, int k, const char* seq, int64_t len, int16_t* out) {
+    orc_tables t;
+    tables_init(&t, dim, k);
+    int32_t* acc = (int32_t*)malloc(sizeof(int32_t) * (size_t)dim);
+    uint64_t* tmp = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)t.W);
+    int64_t n = encode_one(&t, seq, len, acc, tmp);
+    for (int d = 0; d < dim; ++d) out[d] = (int16_t)(uint16_t)(uint32_t)acc[d];
+    free(tmp);
+    free(acc);
+    tables_free(&t);
+    return n;
+}
+
+/* ------------------------------------------------------------------ */
+/* Threaded batch helpers                                              */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    const orc_tables* t;
+    const char* buf;
+    const int64_t* off; /* segment starts */
+    const int64_t* len; /* segment lengths */
+    int64_t n;
+    int out_kind; /* 0: int16 counts, 1: int32 counts, 2: bipolar int8 (ties -> +1) */
+    void* out;
+    int64_t* nk;
+    int tid, nthreads;
+} enc_job;
+
+static void* enc_worker(void* arg) {
+    enc_job* j = (enc_job*)arg;
+    int dim = j->t->dim;
+    int32_t* acc = (int32_t*)malloc(sizeof(int32_t) * (size_t)dim);
+    uint64_t* tmp = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)j->t->W);
+    for (int64_t s = j->tid; s < j->n; s += j->nthreads) {
+        int64_t n = encode_one(j->t, j->buf + j->off[s], j->len[s], acc, tmp);
+        if (j->nk) j->nk[s] = n;
+        if (j->out_kind == 0) {
+            int16_t* o = (int16_t*)j->out + (size_t)s * dim;
+            for (int d = 0; d < dim; ++d) o[d] = (int16_t)(uint16_t)(uint32_t)acc[d];
+        } else if (j->out_kind == 1) {
+            memcpy((int32_t*)j->out + (size_t)s * dim, acc, sizeof(int32_t) * (size_t)dim);
+        } else {
+            int8_t* o = (int8_t*)j->out + (size_t)s * dim;
+            for (int d = 0; d < dim; ++d) o[d] = acc[d] >= 0 ? 1 : -1;
+        }
+    }
+    free(tmp);
+    free(acc);
+    return NULL;
+}
+
+/* Encode n segments buf[off[i] .. off[i]+len[i]) (whole-segment semantics). */
+int orc_encode_segments(int dim, int k, const char* buf, const int64_t* off, const int64_t* len, int64_t n,
+                        int out_kind, void* out, int64_t* nk, int nthreads) {
+    if (nthreads < 1) nthreads = 1;
+    orc_tables t;
+    tables_init(&t, dim, k);
+    pthread_t th[256];
+    enc_job jobs[256];
+    if (nthreads > 256) nthreads = 256;
+    for (int i = 0; i < nthreads; ++i) {
+        jobs[i] = (enc_job){&t, buf, off, len, n, out_kind, out, nk, i, nthreads};
+        pthread_create(&th[i], NULL, enc_worker, &jobs[i]);
+    }
+    for (int i = 0; i < nthreads; ++i) pthread_join(th[i], NULL);
+    tables_free(&t);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Cosine and ranking                                                  */
+/* ------------------------------------------------------------------ */
+enum { ORC_SCORE_NORM = 0, ORC_SCORE_COS = 1, ORC_SCORE_DOT = 2 };
+
+/* Score from exact integer dot and squared norms. */
+static float score_from(int64_t dot, int64_t nl, int64_t nr, int mode) {
+    if (mode == ORC_SCORE_DOT) return (float)dot;
+    if (nl == 0 || nr == 0) return -1.0f;
+    double c = (double)dot / (sqrt((double)nl) * sqrt((double)nr));
+    if (mode == ORC_SCORE_NORM) return (float)(2.0 * (c - 0.5));
+    return (float)c;
+}
+
+static double cos_from(int64_t dot, int64_t nl, int64_t nr) {
+    if (nl == 0 || nr == 0) return 0.0;
+    return (double)dot / (sqrt((double)nl) * sqrt((double)nr));
+}
+
+float orc_cosine_i32(const int32_t* l, const int32_t* r, int dim, int mode) {
+    int64_t dot = 0, nl = 0, nr = 0;
+    for (int i = 0; i < dim; ++i) {
+        int64_t a = l[i], b = r[i];
+        dot += a * b;
+        nl += a * a;
+        nr += b * b;
+    }
+    return score_from(dot, nl, nr, mode);
+}
+
+/* ordering key: larger is better; score descending then index ascending */
+static int better(float sa, int32_t ia, float sb, int32_t ib) {
+    if (sa != sb) return sa > sb;
+    return ia < ib;
+}
+
+typedef struct {
+    const int32_t *q, *r;
+    const int64_t *qn, *rn;
+    int64_t nq, nr;
+    int dim, k, mode;
+    float* out_s;
+    int32_t* out_i;
+    double* out_c;
+    int64_t* out_dot;
+    int tid, nthreads;
+} topk_job;
+
+static void* topk_worker(void* arg) {
+    topk_job* j = (topk_job*)arg;
+    int k = j->k, dim = j->dim;
+    float* bs = (float*)malloc(sizeof(float) * (size_t)k);
+    int32_t* bi = (int32_t*)malloc(sizeof(int32_t) * (size_t)k);
+    int64_t* bd = (int64_t*)malloc(sizeof(int64_t) * (size_t)k);
+    for (int64_t qi = j->tid; qi < j->nq; qi += j->nthreads) {
+        const int32_t* q = j->q + (size_t)qi * dim;
+        int filled = 0;
+        for (int64_t ri = 0; ri < j->nr; ++ri) {
+            const int32_t* r = j->r + (size_t)ri * dim;
+            int64_t dot = 0;
+            for (int d = 0; d < dim; ++d) dot += (int64_t)q[d] * (int64_t)r[d];
+            float s = score_from(dot, j->qn[qi], j->rn[ri], j->mode);
+            if (filled == k && !better(s, (int32_t)ri, bs[k - 1], bi[k - 1])) continue;
+            int pos = filled < k ? filled : k - 1;
+            while (pos > 0 && better(s, (int32_t)ri, bs[pos - 1], bi[pos - 1])) {
+                bs[pos] = bs[pos - 1];
+                bi[pos] = bi[pos - 1];
+                bd[pos] = bd[pos - 1];
+                --pos;
+            }
+            bs[pos] = s;
+            bi[pos] = (int32_t)ri;
+            bd[pos] = dot;
+            if (filled < k) ++filled;
+        }
+        for (int t = 0; t < k; ++t) {
+            int ok = t < filled;
+            j->out_s[qi * k + t] = ok ? bs[t] : -INFINITY;
+            j->out_i[qi * k + t] = ok ? bi[t] : -1;
+            if (j->out_c) j->out_c[qi * k + t] = ok ? cos_from(bd[t], j->qn[qi], j->rn[bi[t]]) : 0.0;
+            if (j->out_dot) j->out_dot[qi * k + t] = ok ? bd[t] : 0;
+        }
+    }
+    free(bd);
+    free(bi);
+    free(bs);
+    return NULL;
+}
+
+static void norms_i32(const int32_t* v, int64_t n, int dim, int64_t* out) {
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t s = 0;
+        for (int d = 0; d < dim; ++d) s += (int64_t)v[(size_t)i * dim + d] * v[(size_t)i * dim + d];
+        out[i] = s;
+    }
+}
+
+/* Brute-force top-k of every query against every reference. */
+int orc_topk_i32(const int32_t* q, int64_t nq, const int32_t* r, int64_t nr, int dim, int k, int mode,
+                 float* out_s, int32_t* out_i, double* out_c, int64_t* out_dot, int nthreads) {
+    if (k < 1) return -1;
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    int64_t* qn = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nq > 0 ? nq : 1));
+    int64_t* rn = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nr > 0 ? nr : 1));
+    norms_i32(q, nq, dim, qn);
+    norms_i32(r, nr, dim, rn);
+    pthread_t th[256];
+    topk_job jobs[256];
+    for (int i = 0; i < nthreads; ++i) {
+        jobs[i] = (topk_job){q, r, qn, rn, nq, nr, dim, k, mode, out_s, out_i, out_c, out_dot, i, nthreads};
+        pthread_create(&th[i], NULL, topk_worker, &jobs[i]);
+    }
+    for (int i = 0; i < nthreads; ++i) pthread_join(th[i], NULL);
+    free(rn);
+    free(qn);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Classification: encode reads then rank them against references.     */
+/* This is the CPU baseline: HVCache::compute per read followed by a    */
+/* brute-force cosine over every reference (encode + top-k search).     */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    const orc_tables* t;
+    const char* buf;
+    const int64_t *off, *len;
+    int64_t n;
+    const int32_t* refs;
+    const int64_t* rn;
+    int64_t nr;
+    int k, mode, bipolar;
+    float* out_s;
+    int32_t* out_i;
+    int tid, nthreads;
+} cls_job;
+
+static void* cls_worker(void* arg) {
+    cls_job* j = (cls_job*)arg;
+    int dim = j->t->dim, k = j->k;
+    int32_t* acc = (int32_t*)malloc(sizeof(int32_t) * (size_t)dim);
+    uint64_t* tmp = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)j->t->W);
+    float* bs = (float*)malloc(sizeof(float) * (size_t)k);
+    int32_t* bi = (int32_t*)malloc(sizeof(int32_t) * (size_t)k);
+    for (int64_t s = j->tid; s < j->n; s += j->nthreads) {
+        encode_one(j->t, j->buf + j->off[s], j->len[s], acc, tmp);
+        int64_t qn = 0;
+        for (int d = 0; d < dim; ++d) {
+            int32_t v = j->bipolar ? (acc[d] >= 0 ? 1 : -1) : (int32_t)(int16_t)(uint16_t)(uint32_t)acc[d];
+            acc[d] = v;
+            qn += (int64_t)v * v;
+        }
+        int filled = 0;
+        for (int64_t ri = 0; ri < j->nr; ++ri) {
+            const int32_t* r = j->refs + (size_t)ri * dim;
+            int64_t dot = 0;
+            for (int d = 0; d < dim; ++d) dot += (int64_t)acc[d] * r[d];
+            float sc = score_from(dot, qn, j->rn[ri], j->mode);
+            if (filled == k && !better(sc, (int32_t)ri, bs[k - 1], bi[k - 1])) continue;
+            int pos = filled < k ? filled : k - 1;
+            while (pos > 0 && better(sc, (int32_t)ri, bs[pos - 1], bi[pos - 1])) {
+                bs[pos] = bs[pos - 1];
+                bi[pos] = bi[pos - 1];
+                --pos;
+            }
+            bs[pos] = sc;
+            bi[pos] = (int32_t)ri;
+            if (filled < k) ++filled;
+        }
+        for (int t = 0; t < k; ++t) {
+            j->out_s[s * k + t] = t < filled ? bs[t] : -INFINITY;
+            j->out_i[s * k + t] = t < filled ? bi[t] : -1;
+        }
+    }
+    free(bi);
+    free(bs);
+    free(tmp);
+    free(acc);
+    return NULL;
+}
+
+int orc_classify(int dim, int kmer, const char* buf, const int64_t* off, const int64_t* len, int64_t n,
+                 const int32_t* refs, int64_t nr, int k, int mode, int bipolar, float* out_s, int32_t* out_i,
+                 int nthreads) {
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    orc_tables t;
+    tables_init(&t, dim, kmer);
+    int64_t* rn = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nr > 0 ? nr : 1));
+    norms_i32(refs, nr, dim, rn);
+    pthread_t th[256];
+    cls_job jobs[256];
+    for (int i = 0; i < nthreads; ++i) {
+        jobs[i] = (cls_job){&t, buf, off, len, n, refs, rn, nr, k, mode, bipolar, out_s, out_i, i, nthreads};
+        pthread_create(&th[i], NULL, cls_worker, &jobs[i]);
+    }
+    for (int i = 0; i < nthreads; ++i) pthread_join(th[i], NULL);
+    free(rn);
+    tables_free(&t);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Propagate-children                                                  */
+/* ------------------------------------------------------------------ */
+
+/* Bundling: parent[p] = sum of rows of its children (CSR: child_ptr[p] ..
+ * child_ptr[p+1] index into child_idx), exact int32. */
+int orc_bundle(const int32_t* rows, int dim, const int64_t* child_ptr, const int32_t* child_idx, int64_t nparents,
+               int32_t* out) {
+    for (int64_t p = 0; p < nparents; ++p) {
+        int32_t* o = out + (size_t)p * dim;
+        memset(o, 0, sizeof(int32_t) * (size_t)dim);
+        for (int64_t c = child_ptr[p]; c < child_ptr[p + 1]; ++c) {
+            const int32_t* r = rows + (size_t)child_idx[c] * dim;
+            for (int d = 0; d < dim; ++d) o[d] += r[d];
+        }
+    }
+    return 0;
+}
+
+/* Greedy representative selection for one parent
+ * (targets/propogate-children.cpp:60-73): candidates are visited in order;
+ * best = max(0, max score vs the parent's existing representatives and the
+ * candidates already added); a candidate is added when best < threshold.
+ * reps/cands are int32 rows; selected[i] = 1 if candidate i was added. */
+int orc_propagate_greedy(const int32_t* reps, int64_t nreps, const int32_t* cands, int64_t ncands, int dim,
+                         double threshold, int mode, uint8_t* selected, float* best_out) {
+    int64_t* added = (int64_t*)malloc(sizeof(int64_t) * (size_t)(ncands > 0 ? ncands : 1));
+    int64_t nadded = 0;
+    for (int64_t i = 0; i < ncands; ++i) {
+        const int32_t* x = cands + (size_t)i * dim;
+        float best = 0.0f;
+        for (int64_t r = 0; r < nreps; ++r) {
+            float s = orc_cosine_i32(x, reps + (size_t)r * dim, dim, mode);
+            if (s > best) best = s;
+        }
+        for (int64_t a = 0; a < nadded; ++a) {
+            float s = orc_cosine_i32(x, cands + (size_t)added[a] * dim, dim, mode);
+            if (s > best) best = s;
+        }
+        if (best_out) best_out[i] = best;
+        selected[i] = (double)best < threshold;
+        if (selected[i]) added[nadded++] = i;
+    }
+    free(added);
+    return (int)nadded;
+}

@@ -1,0 +1,165 @@
+"""ctypes front end of the CPU oracle (oracle/hdc_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as
+the checker and by bench.py's CPU-baseline leg; never by the product path.
+Every function restates the reference CPU algorithm (see hdc_oracle.c for
+the file:line citations into benlaflen/bacterial-classification).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+SCORE_NORM, SCORE_COS, SCORE_DOT = 0, 1, 2
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        L = ctypes.CDLL(path)
+        P = ctypes.c_void_p
+        i64, i32 = ctypes.c_int64, ctypes.c_int
+        L.orc_mt64_stream.argtypes = [ctypes.c_uint64, i32, P]
+        L.orc_base_hvs.argtypes = [i32, P]
+        L.orc_base_hvs.restype = i32
+        L.orc_canonical.argtypes = [ctypes.c_char_p, i32]
+        L.orc_canonical.restype = i64
+        L.orc_binder.argtypes = [i32, i32, i64, P]
+        L.orc_encode.argtypes = [i32, i32, ctypes.c_char_p, i64, P]
+        L.orc_encode.restype = i64
+        L.orc_encode_segments.argtypes = [i32, i32, P, P, P, i64, i32, P, P, i32]
+        L.orc_cosine_i32.argtypes = [P, P, i32, i32]
+        L.orc_cosine_i32.restype = ctypes.c_float
+        L.orc_topk_i32.argtypes = [P, i64, P, i64, i32, i32, i32, P, P, P, P, i32]
+        L.orc_classify.argtypes = [i32, i32, P, P, P, i64, P, i64, i32, i32, i32, P, P, i32]
+        L.orc_bundle.argtypes = [P, i32, P, P, i64, P]
+        L.orc_propagate_greedy.argtypes = [P, i64, P, i64, i32, ctypes.c_double, i32, P, P]
+        L.orc_propagate_greedy.restype = i32
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def nthreads_default():
+    return max(1, os.cpu_count() or 1)
+
+
+def mt64_stream(seed, n):
+    out = np.zeros(n, np.uint64)
+    lib().orc_mt64_stream(seed, n, _p(out))
+    return out
+
+
+def base_hvs(dim):
+    W = (dim + 63) // 64
+    out = np.zeros((4, W), np.uint64)
+    lib().orc_base_hvs(dim, _p(out))
+    return out
+
+
+def canonical(kmer):
+    return lib().orc_canonical(kmer.encode(), len(kmer))
+
+
+def binder(dim, k, canon):
+    out = np.zeros((dim + 63) // 64, np.uint64)
+    lib().orc_binder(dim, k, canon, _p(out))
+    return out
+
+
+def pack_segments(seqs):
+    """Concatenate byte strings; returns (buffer, offsets, lengths)."""
+    bs = [s.encode() if isinstance(s, str) else bytes(s) for s in seqs]
+    lens = np.array([len(b) for b in bs], np.int64)
+    offs = np.zeros(len(bs), np.int64)
+    if len(bs) > 1:
+        offs[1:] = np.cumsum(lens)[:-1]
+    buf = np.frombuffer(b"".join(bs) + b"\0", np.uint8).copy()
+    return buf, offs, lens
+
+
+def encode(seqs, dim, k, out="int16", nthreads=None):
+    """HVCache::compute of every sequence. out: 'int16' | 'int32' | 'bipolar'."""
+    buf, offs, lens = pack_segments(seqs)
+    n = len(lens)
+    kind = {"int16": 0, "int32": 1, "bipolar": 2}[out]
+    dt = {0: np.int16, 1: np.int32, 2: np.int8}[kind]
+    res = np.zeros((n, dim), dt)
+    nk = np.zeros(n, np.int64)
+    lib().orc_encode_segments(dim, k, _p(buf), _p(offs), _p(lens), n, kind, _p(res), _p(nk),
+                              nthreads or nthreads_default())
+    return res, nk
+
+
+def window_segments(seqs, window, step):
+    """Windows of every sequence: (len-window)//step+1 of them (none when
+    len < window), window w covering [w*step, w*step+window)."""
+    out = []
+    for s in seqs:
+        if len(s) < window:
+            continue
+        for w in range((len(s) - window) // step + 1):
+            out.append(s[w * step: w * step + window])
+    return out
+
+
+def cosine(a, b, mode=SCORE_NORM):
+    a = np.ascontiguousarray(a, np.int32)
+    b = np.ascontiguousarray(b, np.int32)
+    return lib().orc_cosine_i32(_p(a), _p(b), a.shape[-1], mode)
+
+
+def topk(q, r, k, mode=SCORE_NORM, nthreads=None):
+    """Brute-force top-k: returns (scores f32, idx i32, cos f64, dot i64), each [nq, k]."""
+    q = np.ascontiguousarray(q, np.int32)
+    r = np.ascontiguousarray(r, np.int32)
+    nq, dim = q.shape
+    nr = r.shape[0]
+    s = np.zeros((nq, k), np.float32)
+    i = np.zeros((nq, k), np.int32)
+    c = np.zeros((nq, k), np.float64)
+    d = np.zeros((nq, k), np.int64)
+    lib().orc_topk_i32(_p(q), nq, _p(r), nr, dim, k, mode, _p(s), _p(i), _p(c), _p(d),
+                       nthreads or nthreads_default())
+    return s, i, c, d
+
+
+def classify(reads, refs, dim, kmer, k, mode=SCORE_NORM, bipolar=False, nthreads=None):
+    """Encode every read and rank it against int32 refs [nr, dim]: the CPU path."""
+    buf, offs, lens = pack_segments(reads)
+    refs = np.ascontiguousarray(refs, np.int32)
+    n = len(lens)
+    s = np.zeros((n, k), np.float32)
+    i = np.zeros((n, k), np.int32)
+    lib().orc_classify(dim, kmer, _p(buf), _p(offs), _p(lens), n, _p(refs), refs.shape[0], k, mode,
+                       int(bipolar), _p(s), _p(i), nthreads or nthreads_default())
+    return s, i
+
+
+def bundle(rows, child_ptr, child_idx):
+    rows = np.ascontiguousarray(rows, np.int32)
+    child_ptr = np.ascontiguousarray(child_ptr, np.int64)
+    child_idx = np.ascontiguousarray(child_idx, np.int32)
+    npar = len(child_ptr) - 1
+    out = np.zeros((npar, rows.shape[1]), np.int32)
+    lib().orc_bundle(_p(rows), rows.shape[1], _p(child_ptr), _p(child_idx), npar, _p(out))
+    return out
+
+
+def propagate_greedy(reps, cands, threshold=0.75, mode=SCORE_NORM):
+    reps = np.ascontiguousarray(reps, np.int32).reshape(-1, cands.shape[1]) if len(reps) else \
+        np.zeros((0, cands.shape[1]), np.int32)
+    cands = np.ascontiguousarray(cands, np.int32)
+    sel = np.zeros(cands.shape[0], np.uint8)
+    best = np.zeros(cands.shape[0], np.float32)
+    lib().orc_propagate_greedy(_p(reps), reps.shape[0], _p(cands), cands.shape[0], cands.shape[1],
+                               threshold, mode, _p(sel), _p(best))
+    return sel.astype(bool), best
