@@ -1,0 +1,180 @@
+// extern "C" entry points of libhdc_gb300 (declared in include/hdc_gb300.h).
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <random>
+#include <string>
+
+#include "hdc_internal.cuh"
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+namespace hdc {
+
+int fail(int status, const std::string& msg) {
+    g_last_error = msg;
+    return status;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? HDC_ERR_NOMEM : HDC_ERR_CUDA;
+}
+
+}  // namespace hdc
+
+using hdc::fail;
+
+extern "C" {
+
+const char* hdc_last_error(void) { return g_last_error.c_str(); }
+
+const char* hdc_status_string(int status) {
+    switch (status) {
+        case HDC_OK: return "ok";
+        case HDC_ERR_INVALID: return "invalid argument";
+        case HDC_ERR_RANGE: return "value range";
+        case HDC_ERR_CUDA: return "CUDA error";
+        case HDC_ERR_NOMEM: return "out of device memory";
+        case HDC_ERR_UNSUPPORTED: return "unsupported device";
+        case HDC_ERR_TIMEOUT: return "device wait timed out";
+        default: return "unknown status";
+    }
+}
+
+// Base hypervectors exactly as src/HV.cpp:20-41: mt19937_64(seed), one draw per
+// 64-bit word, bits at and above HV_DIM cleared; seeds A=0, C=1, T=2, G=3
+// (src/HV.cpp:37-40).  Stored in code order A,C,G,T.
+int hdc_context_create(int dim, int kmer, int window, int step, hdc_context** out) {
+    if (!out) return fail(HDC_ERR_INVALID, "context: null output pointer");
+    *out = nullptr;
+    if (dim < 1 || dim > (1 << 20)) return fail(HDC_ERR_INVALID, "context: dim must be in 1..2^20");
+    if (kmer < 1 || kmer > 16) return fail(HDC_ERR_INVALID, "context: kmer must be in 1..16");
+    if (window < 1 || step < 1) return fail(HDC_ERR_INVALID, "context: window and step must be positive");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return hdc::cuda_fail(e, "context: cudaGetDevice");
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, dev);
+    if (e != cudaSuccess) return hdc::cuda_fail(e, "context: cudaGetDeviceProperties");
+    auto* c = new hdc_context();
+    c->dim = dim;
+    c->kmer = kmer;
+    c->window = window;
+    c->step = step;
+    c->words64 = (dim + 63) / 64;
+    c->words32 = 2 * c->words64;
+    c->device = dev;
+    c->num_sms = prop.multiProcessorCount;
+    c->host_base = new uint64_t[4 * (size_t)c->words64];
+    const int seed_of_code[4] = {0, 1, 3, 2};
+    const int excess = c->words64 * 64 - dim;
+    for (int code = 0; code < 4; ++code) {
+        std::mt19937_64 rng((uint64_t)seed_of_code[code]);
+        uint64_t* w = c->host_base + (size_t)code * c->words64;
+        for (int i = 0; i < c->words64; ++i) w[i] = rng();
+        if (excess > 0) w[c->words64 - 1] &= (~uint64_t(0)) >> excess;
+    }
+    e = cudaMalloc(&c->d_base32, sizeof(uint64_t) * 4 * (size_t)c->words64);
+    if (e != cudaSuccess) {
+        delete[] c->host_base;
+        delete c;
+        return hdc::cuda_fail(e, "context: cudaMalloc");
+    }
+    // little-endian: 64-bit word i is 32-bit words 2i (low) and 2i+1 (high)
+    e = cudaMemcpy(c->d_base32, c->host_base, sizeof(uint64_t) * 4 * (size_t)c->words64, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(c->d_base32);
+        delete[] c->host_base;
+        delete c;
+        return hdc::cuda_fail(e, "context: upload");
+    }
+    *out = c;
+    return HDC_OK;
+}
+
+void hdc_context_destroy(hdc_context* ctx) {
+    if (!ctx) return;
+    cudaFree(ctx->d_base32);
+    delete[] ctx->host_base;
+    delete ctx;
+}
+
+int hdc_context_base_hvs(const hdc_context* ctx, uint64_t* host_out) {
+    if (!ctx || !host_out) return fail(HDC_ERR_INVALID, "base_hvs: null argument");
+    std::memcpy(host_out, ctx->host_base, sizeof(uint64_t) * 4 * (size_t)ctx->words64);
+    return HDC_OK;
+}
+
+int hdc_encode_segments(hdc_context* ctx, const char* d_bytes, const int64_t* d_seg_off, const int32_t* d_seg_len,
+                        int64_t n_segs, int32_t max_len, int out_kind, void* d_out, int64_t out_stride,
+                        int32_t* d_nkmers, void* stream) {
+    if (!ctx) return fail(HDC_ERR_INVALID, "encode: null context");
+    if (n_segs < 0) return fail(HDC_ERR_INVALID, "encode: negative segment count");
+    if (n_segs == 0) return HDC_OK;
+    if (!d_bytes || !d_seg_off || !d_seg_len || !d_out) return fail(HDC_ERR_INVALID, "encode: null pointer");
+    if (out_kind < HDC_OUT_I16 || out_kind > HDC_OUT_BIPOLAR_I16) return fail(HDC_ERR_INVALID, "encode: bad out_kind");
+    if (out_stride < ctx->dim) return fail(HDC_ERR_INVALID, "encode: out_stride < dim");
+    if (max_len < 0) return fail(HDC_ERR_INVALID, "encode: negative max_len");
+    return hdc::launch_encode(ctx, d_bytes, d_seg_off, d_seg_len, nullptr, nullptr, 0, n_segs, out_kind, d_out,
+                              out_stride, d_nkmers, max_len, static_cast<cudaStream_t>(stream));
+}
+
+int64_t hdc_num_windows(const hdc_context* ctx, int64_t len) {
+    if (!ctx || len < ctx->window) return 0;
+    return (len - ctx->window) / ctx->step + 1;
+}
+
+int hdc_encode_windows(hdc_context* ctx, const char* d_bytes, const int64_t* d_seq_off, const int64_t* d_win_off,
+                       int64_t n_seqs, int64_t n_windows, int16_t* d_out, void* stream) {
+    if (!ctx) return fail(HDC_ERR_INVALID, "encode_windows: null context");
+    if (n_seqs < 0 || n_windows < 0) return fail(HDC_ERR_INVALID, "encode_windows: negative count");
+    if (n_seqs == 0 || n_windows == 0) return HDC_OK;
+    if (!d_bytes || !d_seq_off || !d_win_off || !d_out) return fail(HDC_ERR_INVALID, "encode_windows: null pointer");
+    return hdc::launch_encode(ctx, d_bytes, nullptr, nullptr, d_seq_off, d_win_off, n_seqs, n_windows, HDC_OUT_I16,
+                              d_out, ctx->dim, nullptr, ctx->window, static_cast<cudaStream_t>(stream));
+}
+
+int hdc_norms(hdc_context* ctx, const void* d_hv, int elem_bytes, int64_t n, int64_t* d_norm2, int32_t* d_maxabs,
+              void* stream) {
+    if (!ctx) return fail(HDC_ERR_INVALID, "norms: null context");
+    if (elem_bytes != 2 && elem_bytes != 4) return fail(HDC_ERR_INVALID, "norms: elem_bytes must be 2 or 4");
+    if (n < 0) return fail(HDC_ERR_INVALID, "norms: negative count");
+    if (n > 0 && (!d_hv || !d_norm2)) return fail(HDC_ERR_INVALID, "norms: null pointer");
+    return hdc::launch_norms(ctx, d_hv, elem_bytes, n, d_norm2, d_maxabs, static_cast<cudaStream_t>(stream));
+}
+
+size_t hdc_search_workspace_bytes(const hdc_context* ctx, int64_t nq, int64_t nr, int k) {
+    if (!ctx || nq <= 0 || nr <= 0 || k <= 0) return 0;
+    return hdc::plain_workspace_bytes(ctx, nq, nr, k);
+}
+
+int hdc_search_plain(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qnorm2, int64_t nq, int32_t max_abs_q,
+                     const int16_t* d_r, const int64_t* d_rnorm2, int64_t nr, int32_t max_abs_r, int k,
+                     int score_mode, float* d_score, int32_t* d_idx, double* d_cos, int64_t* d_dot, void* d_work,
+                     size_t work_bytes, void* stream) {
+    if (!ctx) return fail(HDC_ERR_INVALID, "search: null context");
+    if (nq < 0 || nr < 0) return fail(HDC_ERR_INVALID, "search: negative count");
+    if (nq == 0) return HDC_OK;
+    if (!hdc::valid_score_mode(score_mode)) return fail(HDC_ERR_INVALID, "search: bad score mode");
+    if (!d_q || !d_qnorm2 || !d_r || !d_rnorm2 || !d_score || !d_idx)
+        return fail(HDC_ERR_INVALID, "search: null pointer");
+    return hdc::launch_search_plain(ctx, d_q, d_qnorm2, nq, max_abs_q, d_r, d_rnorm2, nr, max_abs_r, k, score_mode,
+                                    d_score, d_idx, d_cos, d_dot, d_work, work_bytes,
+                                    static_cast<cudaStream_t>(stream));
+}
+
+int hdc_bundle(hdc_context* ctx, const void* d_rows, int elem_bytes, const int64_t* d_child_ptr,
+               const int32_t* d_child_idx, int64_t n_parents, int32_t* d_out, void* stream) {
+    if (!ctx) return fail(HDC_ERR_INVALID, "bundle: null context");
+    if (elem_bytes != 2 && elem_bytes != 4) return fail(HDC_ERR_INVALID, "bundle: elem_bytes must be 2 or 4");
+    if (n_parents < 0) return fail(HDC_ERR_INVALID, "bundle: negative count");
+    if (n_parents == 0) return HDC_OK;
+    if (!d_rows || !d_child_ptr || !d_child_idx || !d_out) return fail(HDC_ERR_INVALID, "bundle: null pointer");
+    return hdc::launch_bundle(ctx, d_rows, elem_bytes, d_child_ptr, d_child_idx, n_parents, d_out,
+                              static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,382 @@
+// (a) k-mer hypervector encoding on sm_103a.
+//
+// Semantics (bit-exact with the reference CPU encoder):
+//   out[d] = sum over k-mer positions p of (2*bit_d(binder(canon(seq[p..p+k)))) - 1)
+// where canon() is min(kmer, revcomp(kmer)) in A<C<G<T order and
+//   binder(c)_j = 1 ^ XOR_i base[c_i][(j + i) mod 64*W]
+// (src/encoder.cpp:47-74 builds binders with mult(), src/HV.cpp:98-147;
+// src/encoder.cpp:106-132 bundles every position and skips k-mers holding a
+// byte outside "ACGT"; src/HV.cpp:156-216 accumulates +1/-1 per bit).
+//
+// GB300 design
+//   * One warp owns 32 consecutive 32-bit words of the hypervector (a 1024-dim
+//     "slab"); lane l owns word l.  A CTA serves one slab for many segments,
+//     so the slab's lookup tables are built once per CTA and reused.
+//   * The canonical k-mer's digits are split into parts of <= 4 digits.  For
+//     each part the CTA keeps in shared memory a table of all 4^len
+//     pre-rotated, pre-XORed binder fragments restricted to the slab; part 0
+//     also carries the all-ones start value.  A binder word is the XOR of
+//     one 128-byte table row per part (conflict-free: the 32 lanes read the
+//     32 words of one row).
+//   * Per chunk of 256 positions each lane computes 8 canonical k-mers with
+//     a rolling 2-bit code (revcomp = bitwise NOT of the little-endian code,
+//     forward = digit reversal), and writes one packed entry of table row
+//     offsets per position.  Invalid k-mers and the chunk tail point at an
+//     all-zero row, which contributes nothing.
+//   * Bundling never unpacks bits: 16 binder words are reduced by a
+//     carry-save adder tree into bit-sliced counters (ones/twos/fours/eights
+//     plus NH higher planes), ~2 logic ops per word; counts are extracted
+//     once per segment.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
+#include "hdc_internal.cuh"
+
+namespace hdc {
+namespace {
+
+constexpr int kWarps = 8;
+constexpr int kThreads = kWarps * 32;
+constexpr int kChunk = 256;  // positions per staged chunk: 8 per lane
+constexpr int kMaxParts = 4;
+
+struct EncodeArgs {
+    const uint32_t* base32;  // [4][W32], A,C,G,T
+    int dim, k, W32;
+    int nparts;
+    int part_first[kMaxParts];  // first digit (0 = first base of the canonical k-mer)
+    int part_len[kMaxParts];
+    int part_row0[kMaxParts];
+    int zero_row;
+    int table_rows;
+    const unsigned char* bytes;
+    const int64_t* seg_off;  // explicit segments
+    const int32_t* seg_len;
+    const int64_t* seq_off;  // window segments: [n_seqs+1]
+    const int64_t* win_off;  // [n_seqs+1]
+    int64_t n_seqs;
+    int window, step;
+    int64_t n_segs;
+    int out_kind;
+    void* out;
+    int64_t out_stride;
+    int32_t* nkmers;
+};
+
+__device__ __forceinline__ void csa(uint32_t& h, uint32_t& l, uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t u = a ^ b;
+    h = (a & b) | (u & c);
+    l = u ^ c;
+}
+
+__device__ __forceinline__ void get_segment(const EncodeArgs& a, int64_t g, int64_t& start, int& len) {
+    if (a.seg_off) {
+        start = a.seg_off[g];
+        len = a.seg_len[g];
+        return;
+    }
+    // window mode: find s with win_off[s] <= g < win_off[s+1]
+    int64_t lo = 0, hi = a.n_seqs;  // invariant win_off[lo] <= g < win_off[hi]
+    while (hi - lo > 1) {
+        int64_t mid = (lo + hi) >> 1;
+        if (a.win_off[mid] <= g)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    start = a.seq_off[lo] + (g - a.win_off[lo]) * (int64_t)a.step;
+    len = a.window;
+}
+
+// 2-bit code of an ASCII byte (A=0 C=1 G=2 T=3) and whether it is a base.
+__device__ __forceinline__ uint32_t base_code(uint32_t c) { return ((c >> 1) ^ (c >> 2)) & 3u; }
+__device__ __forceinline__ uint32_t is_base(uint32_t c) {
+    return (c == 'A') | (c == 'C') | (c == 'G') | (c == 'T');
+}
+
+template <int NP>
+__device__ __forceinline__ uint64_t pack_entry(const EncodeArgs& a, uint32_t canon) {
+    uint64_t e = 0;
+#pragma unroll
+    for (int p = 0; p < kMaxParts; ++p) {
+        uint32_t row;
+        if (p < NP) {
+            int len = a.part_len[p];
+            int shift = 2 * (a.k - a.part_first[p] - len);
+            uint32_t sub = (canon >> shift) & ((1u << (2 * len)) - 1u);
+            row = (uint32_t)a.part_row0[p] + sub;
+        } else {
+            row = (uint32_t)a.zero_row;
+        }
+        e |= (uint64_t)(row * 32u) << (16 * p);
+    }
+    return e;
+}
+
+template <int NP, int NH>
+__global__ void __launch_bounds__(kThreads) encode_kernel(const EncodeArgs a) {
+    extern __shared__ __align__(16) uint32_t smem[];
+    uint32_t* table = smem;  // [table_rows][32]
+    uint64_t* lists = reinterpret_cast<uint64_t*>(smem + a.table_rows * 32);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int slab = blockIdx.y;
+
+    // ---- lookup tables for this slab ----
+    for (int e = threadIdx.x; e < a.table_rows * 32; e += kThreads) {
+        const int row = e >> 5, w = slab * 32 + (e & 31);
+        uint32_t v = 0;
+        if (row < a.zero_row && w < a.W32) {
+            int p = 0;
+            while (p + 1 < a.nparts && row >= a.part_row0[p + 1]) ++p;
+            const int sub = row - a.part_row0[p], len = a.part_len[p], first = a.part_first[p];
+            v = p == 0 ? ~0u : 0u;
+            const int wn = (w + 1 == a.W32) ? 0 : w + 1;
+            for (int t = 0; t < len; ++t) {
+                const int digit = (sub >> (2 * (len - 1 - t))) & 3;
+                const uint32_t* b = a.base32 + digit * a.W32;
+                v ^= __funnelshift_r(b[w], b[wn], first + t);  // rot_{first+t}
+            }
+        }
+        table[e] = v;
+    }
+    __syncthreads();
+
+    const uint32_t* trow = table + lane;
+    uint64_t* list = lists + warp * kChunk;
+    const uint64_t zero_entry = pack_entry<0>(a, 0);
+    const int k = a.k;
+    const uint32_t mask2k = k == 16 ? 0xffffffffu : ((1u << (2 * k)) - 1u);
+    const int64_t gw = (int64_t)blockIdx.x * kWarps + warp, nw = (int64_t)gridDim.x * kWarps;
+    const int w32 = slab * 32 + lane;
+
+    for (int64_t seg = gw; seg < a.n_segs; seg += nw) {
+        int64_t start;
+        int len;
+        get_segment(a, seg, start, len);
+        const unsigned char* s = a.bytes + start;
+        const int npos = len >= k ? len - k + 1 : 0;
+        uint32_t ones = 0, twos = 0, fours = 0, eights = 0;
+        uint32_t hi[NH];
+#pragma unroll
+        for (int h = 0; h < NH; ++h) hi[h] = 0;
+        int nvalid = 0;
+
+        for (int c0 = 0; c0 < npos; c0 += kChunk) {
+            // ---- stage 8 canonical k-mers per lane ----
+            const int p0 = c0 + lane * 8;
+            uint32_t x = 0, m = 0;
+            auto push = [&](int pos) {
+                uint32_t c = pos < len ? (uint32_t)__ldg(s + pos) : 0u;
+                uint32_t inv = pos < len ? (is_base(c) ^ 1u) : 1u;
+                x = (x >> 2) | (base_code(c) << (2 * (k - 1)));
+                m = (m >> 1) | (inv << (k - 1));
+            };
+            for (int j = 0; j < k - 1; ++j) push(p0 + j);
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                push(p0 + r + k - 1);
+                uint64_t e = zero_entry;
+                if (p0 + r < npos && m == 0) {
+                    uint32_t rc = ~x & mask2k;
+                    uint32_t y = __brev(x) >> (32 - 2 * k);
+                    uint32_t fw = ((y & 0x55555555u) << 1) | ((y >> 1) & 0x55555555u);
+                    e = pack_entry<NP>(a, fw < rc ? fw : rc);
+                    ++nvalid;
+                }
+                list[lane * 8 + r] = e;
+            }
+            __syncwarp();
+
+            // ---- bundle: binder words through a carry-save adder tree ----
+            const int groups = (min(kChunk, npos - c0) + 15) >> 4;
+            for (int g = 0; g < groups; ++g) {
+                uint32_t xw[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const uint64_t e = list[g * 16 + j];
+                    const uint32_t lo = (uint32_t)e, hw = (uint32_t)(e >> 32);
+                    uint32_t v = trow[lo & 0xffffu];
+                    if (NP > 1) v ^= trow[lo >> 16];
+                    if (NP > 2) v ^= trow[hw & 0xffffu];
+                    if (NP > 3) v ^= trow[hw >> 16];
+                    xw[j] = v;
+                }
+                uint32_t twosA, twosB, foursA, foursB, eightsA, eightsB, sixteens;
+                csa(twosA, ones, ones, xw[0], xw[1]);
+                csa(twosB, ones, ones, xw[2], xw[3]);
+                csa(foursA, twos, twos, twosA, twosB);
+                csa(twosA, ones, ones, xw[4], xw[5]);
+                csa(twosB, ones, ones, xw[6], xw[7]);
+                csa(foursB, twos, twos, twosA, twosB);
+                csa(eightsA, fours, fours, foursA, foursB);
+                csa(twosA, ones, ones, xw[8], xw[9]);
+                csa(twosB, ones, ones, xw[10], xw[11]);
+                csa(foursA, twos, twos, twosA, twosB);
+                csa(twosA, ones, ones, xw[12], xw[13]);
+                csa(twosB, ones, ones, xw[14], xw[15]);
+                csa(foursB, twos, twos, twosA, twosB);
+                csa(eightsB, fours, fours, foursA, foursB);
+                csa(sixteens, eights, eights, eightsA, eightsB);
+                uint32_t carry = sixteens;
+#pragma unroll
+                for (int h = 0; h < NH; ++h) {
+                    const uint32_t t = hi[h] & carry;
+                    hi[h] ^= carry;
+                    carry = t;
+                }
+            }
+            __syncwarp();
+        }
+        nvalid = __reduce_add_sync(0xffffffffu, nvalid);
+        if (a.nkmers && lane == 0 && slab == 0) a.nkmers[seg] = nvalid;
+        if (w32 >= a.W32) continue;
+
+        // ---- counts -> output values, dims b and b+16 in 16-bit fields ----
+        uint32_t val[32];
+#pragma unroll
+        for (int b = 0; b < 16; ++b) {
+            const uint32_t M = 0x00010001u;
+            uint32_t v = ((ones >> b) & M) + (((twos >> b) & M) << 1) + (((fours >> b) & M) << 2) +
+                         (((eights >> b) & M) << 3);
+#pragma unroll
+            for (int h = 0; h < NH; ++h) v += ((hi[h] >> b) & M) << (4 + h);
+            val[b] = v & 0xffffu;
+            val[b + 16] = v >> 16;
+        }
+        const int dbase = w32 * 32;
+        const int nd = min(32, a.dim - dbase);
+        char* rowp = static_cast<char*>(a.out);
+        if (a.out_kind == HDC_OUT_I32) {
+            int32_t* o = reinterpret_cast<int32_t*>(rowp) + seg * a.out_stride + dbase;
+            if (nd == 32 && ((reinterpret_cast<uintptr_t>(o) & 15) == 0)) {
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    int4 v4;
+                    v4.x = 2 * (int)val[4 * q + 0] - nvalid;
+                    v4.y = 2 * (int)val[4 * q + 1] - nvalid;
+                    v4.z = 2 * (int)val[4 * q + 2] - nvalid;
+                    v4.w = 2 * (int)val[4 * q + 3] - nvalid;
+                    reinterpret_cast<int4*>(o)[q] = v4;
+                }
+            } else {
+#pragma unroll
+                for (int b = 0; b < 32; ++b)
+                    if (b < nd) o[b] = 2 * (int)val[b] - nvalid;
+            }
+        } else {
+            uint16_t* o = reinterpret_cast<uint16_t*>(rowp) + seg * a.out_stride + dbase;
+            uint32_t pk[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+                uint32_t h2[2];
+#pragma unroll
+                for (int t = 0; t < 2; ++t) {
+                    const int v = 2 * (int)val[2 * q + t] - nvalid;
+                    if (a.out_kind == HDC_OUT_I16)
+                        h2[t] = (uint32_t)v & 0xffffu;
+                    else if (a.out_kind == HDC_OUT_BIPOLAR_I16)
+                        h2[t] = v >= 0 ? 0x0001u : 0xffffu;
+                    else
+                        h2[t] = v >= 0 ? 0x3f80u : 0xbf80u;  // bf16 +1 / -1
+                }
+                pk[q] = h2[0] | (h2[1] << 16);
+            }
+            if (nd == 32 && ((reinterpret_cast<uintptr_t>(o) & 15) == 0)) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    reinterpret_cast<uint4*>(o)[q] = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
+            } else {
+#pragma unroll
+                for (int b = 0; b < 32; ++b)
+                    if (b < nd) o[b] = (uint16_t)(pk[b >> 1] >> (16 * (b & 1)));
+            }
+        }
+    }
+}
+
+template <int NP, int NH>
+int launch_np_nh(const EncodeArgs& a, int grid_x, int n_slabs, size_t smem, cudaStream_t stream) {
+    auto kern = encode_kernel<NP, NH>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail(e, "encode: cudaFuncSetAttribute");
+    kern<<<dim3(grid_x, n_slabs), kThreads, smem, stream>>>(a);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? HDC_OK : cuda_fail(e, "encode: launch");
+}
+
+template <int NP>
+int launch_np(const EncodeArgs& a, int nh, int grid_x, int n_slabs, size_t smem, cudaStream_t stream) {
+    if (nh <= 4) return launch_np_nh<NP, 4>(a, grid_x, n_slabs, smem, stream);
+    if (nh <= 8) return launch_np_nh<NP, 8>(a, grid_x, n_slabs, smem, stream);
+    return launch_np_nh<NP, 12>(a, grid_x, n_slabs, smem, stream);
+}
+
+}  // namespace
+
+int launch_encode(hdc_context* ctx, const char* d_bytes, const int64_t* d_seg_off, const int32_t* d_seg_len,
+                  const int64_t* d_seq_off, const int64_t* d_win_off, int64_t n_seqs, int64_t n_segs, int out_kind,
+                  void* d_out, int64_t out_stride, int32_t* d_nkmers, int max_seg_len, cudaStream_t stream) {
+    if (n_segs == 0) return HDC_OK;
+    EncodeArgs a{};
+    a.base32 = ctx->d_base32;
+    a.dim = ctx->dim;
+    a.k = ctx->kmer;
+    a.W32 = ctx->words32;
+    // digit parts of <= 4 digits, as even as possible, longer parts first
+    const int np = (a.k + 3) / 4;
+    a.nparts = np;
+    int first = 0, row0 = 0;
+    for (int p = 0; p < np; ++p) {
+        const int len = a.k / np + (p < a.k % np ? 1 : 0);
+        a.part_first[p] = first;
+        a.part_len[p] = len;
+        a.part_row0[p] = row0;
+        first += len;
+        row0 += 1 << (2 * len);
+    }
+    a.zero_row = row0;
+    a.table_rows = row0 + 1;
+    a.bytes = reinterpret_cast<const unsigned char*>(d_bytes);
+    a.seg_off = d_seg_off;
+    a.seg_len = d_seg_len;
+    a.seq_off = d_seq_off;
+    a.win_off = d_win_off;
+    a.n_seqs = n_seqs;
+    a.window = ctx->window;
+    a.step = ctx->step;
+    a.n_segs = n_segs;
+    a.out_kind = out_kind;
+    a.out = d_out;
+    a.out_stride = out_stride;
+    a.nkmers = d_nkmers;
+
+    // counters: ones..eights hold 0..15, NH higher planes hold multiples of 16
+    const int64_t max_nk = max_seg_len > 0 ? std::max<int64_t>(0, (int64_t)max_seg_len - a.k + 1) : (int64_t)1 << 40;
+    int nh;
+    if (max_nk <= 255)
+        nh = 4;
+    else if (max_nk <= 4095)
+        nh = 8;
+    else
+        nh = 12;  // counts modulo 2^16
+    if (out_kind != HDC_OUT_I16 && max_nk > 65535)
+        return fail(HDC_ERR_RANGE, "encode: segments longer than 65535 k-mers need HDC_OUT_I16 (counts wrap)");
+
+    const int n_slabs = (a.W32 + 31) / 32;
+    const size_t smem = (size_t)a.table_rows * 32 * 4 + (size_t)kWarps * kChunk * 8;
+    // occupancy-sized grid: every SM busy, each slab served by the same number of CTAs
+    const int per_sm = std::max(1, std::min(8, (int)((227 * 1024) / (smem + 1024))));
+    const int64_t want = ((int64_t)ctx->num_sms * per_sm + n_slabs - 1) / n_slabs;
+    const int64_t need = (n_segs + kWarps - 1) / kWarps;
+    const int grid_x = (int)std::max<int64_t>(1, std::min<int64_t>(want, need));
+
+    switch (np) {
+        case 1: return launch_np<1>(a, nh, grid_x, n_slabs, smem, stream);
+        case 2: return launch_np<2>(a, nh, grid_x, n_slabs, smem, stream);
+        case 3: return launch_np<3>(a, nh, grid_x, n_slabs, smem, stream);
+        default: return launch_np<4>(a, nh, grid_x, n_slabs, smem, stream);
+    }
+}
+
+}  // namespace hdc

@@ -1,0 +1,51 @@
+// Internal definitions shared by the translation units of libhdc_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "hdc_gb300.h"
+
+struct hdc_context {
+    int dim = 0;      // HV_DIM
+    int kmer = 0;     // KMER_SIZE
+    int window = 0;   // SEQUENCE_LENGTH
+    int step = 0;     // SIM_STEP
+    int words64 = 0;  // ceil(dim / 64): the reference's HV_WORDS
+    int words32 = 0;  // 2 * words64: the 64*HV_WORDS-bit ring in 32-bit words
+    int device = 0;
+    int num_sms = 0;
+    uint64_t* host_base = nullptr;  // [4][words64], A,C,G,T
+    uint32_t* d_base32 = nullptr;   // [4][words32] on the device
+};
+
+namespace hdc {
+
+// Records a message for hdc_last_error() and returns the status.
+int fail(int status, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+inline bool valid_score_mode(int m) { return m == HDC_SCORE_NORM || m == HDC_SCORE_COS || m == HDC_SCORE_DOT; }
+
+// Launchers implemented in the kernel translation units.
+int launch_encode(hdc_context* ctx, const char* d_bytes, const int64_t* d_seg_off, const int32_t* d_seg_len,
+                  const int64_t* d_seq_off, const int64_t* d_win_off, int64_t n_seqs, int64_t n_segs,
+                  int out_kind, void* d_out, int64_t out_stride, int32_t* d_nkmers, int max_seg_len,
+                  cudaStream_t stream);
+
+int launch_norms(hdc_context* ctx, const void* d_hv, int elem_bytes, int64_t n, int64_t* d_norm2,
+                 int32_t* d_maxabs, cudaStream_t stream);
+
+size_t plain_workspace_bytes(const hdc_context* ctx, int64_t nq, int64_t nr, int k);
+
+int launch_search_plain(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qn, int64_t nq, int32_t maxq,
+                        const int16_t* d_r, const int64_t* d_rn, int64_t nr, int32_t maxr, int k, int mode,
+                        float* d_score, int32_t* d_idx, double* d_cos, int64_t* d_dot, void* d_work,
+                        size_t work_bytes, cudaStream_t stream);
+
+int launch_bundle(hdc_context* ctx, const void* d_rows, int elem_bytes, const int64_t* d_child_ptr,
+                  const int32_t* d_child_idx, int64_t n_parents, int32_t* d_out, cudaStream_t stream);
+
+}  // namespace hdc

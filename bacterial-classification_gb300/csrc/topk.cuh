@@ -1,0 +1,78 @@
+// Ranking keys and exact scores shared by the plain and tensor-core searches.
+//
+// Ranking rule: descending float score, ties to the lower reference index
+// (the reference CPU argmax keeps the first maximum,
+// tests/cosine_comparison_test.cpp:146-156).  A candidate is packed into a
+// 64-bit key that orders exactly like that rule:
+//     key = orderable(score bits) << 32 | (0xffffffff - ref index)
+// so "larger key" means "ranks earlier" and key 0 is below every real key.
+#pragma once
+
+#include <stdint.h>
+
+#include "hdc_gb300.h"
+
+namespace hdc {
+
+__host__ __device__ __forceinline__ uint32_t ord_float(float f) {
+    uint32_t b;
+    memcpy(&b, &f, 4);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+__host__ __device__ __forceinline__ float unord_float(uint32_t o) {
+    uint32_t b = (o & 0x80000000u) ? (o & 0x7fffffffu) : ~o;
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+}
+
+__host__ __device__ __forceinline__ uint64_t make_key(float score, uint32_t idx) {
+    return ((uint64_t)ord_float(score) << 32) | (uint64_t)(0xffffffffu - idx);
+}
+
+__host__ __device__ __forceinline__ uint32_t key_idx(uint64_t key) { return 0xffffffffu - (uint32_t)key; }
+__host__ __device__ __forceinline__ float key_score(uint64_t key) { return unord_float((uint32_t)(key >> 32)); }
+
+// The reference's float score from the exact dot and squared norms:
+//   NORM: (float)(2.0 * (dot / (sqrt(nq) * sqrt(nr)) - 0.5)), -1 on a zero norm
+//         (src/HV.cpp:219-242; the float literal 0.5f is exactly 0.5)
+//   COS:  (float)(dot / (sqrt(nq) * sqrt(nr))), -1 on a zero norm
+//   DOT:  (float)dot (src/HV.cpp:244-252)
+// Every double operation is IEEE round-to-nearest, written with explicit
+// intrinsics so no contraction or reassociation can change the rounding.
+__device__ __forceinline__ double exact_cos(int64_t dot, int64_t nq, int64_t nr) {
+    if (nq == 0 || nr == 0) return 0.0;
+    double den = __dmul_rn(__dsqrt_rn((double)nq), __dsqrt_rn((double)nr));
+    return __ddiv_rn((double)dot, den);
+}
+
+__device__ __forceinline__ float exact_score(int64_t dot, int64_t nq, int64_t nr, int mode) {
+    if (mode == HDC_SCORE_DOT) return __ll2float_rn(dot);
+    if (nq == 0 || nr == 0) return -1.0f;
+    double c = exact_cos(dot, nq, nr);
+    if (mode == HDC_SCORE_NORM) return __double2float_rn(__dmul_rn(2.0, __dadd_rn(c, -0.5)));
+    return __double2float_rn(c);
+}
+
+// Width of the fp32 pre-filter guard band, in score units.  The fp32
+// estimate  fl(fl(dot) * fl(1/sqrt(nq)) * fl(1/sqrt(nr)))  is within about
+// 5 * 2^-24 (relative, i.e. < 3.5e-7 absolute for |cos| <= 1) of the exact
+// cosine, and the reference's float score is the double result rounded to
+// float (another <= 6e-8); a score that can reach the current k-th best is
+// therefore never rejected with a margin of 4e-6 (NORM doubles the cosine
+// error, still < 1e-6).  DOT scores are exact and need no margin.
+constexpr float kFilterMargin = 4e-6f;
+
+__device__ __forceinline__ float approx_score(float dotf, float rq, float rr, int mode) {
+    if (mode == HDC_SCORE_DOT) return dotf;
+    const float c = dotf * rq * rr;  // rq/rr are 0 for zero norms
+    return mode == HDC_SCORE_NORM ? fmaf(2.0f, c, -1.0f) : c;
+}
+
+// fp32 reciprocal square root of a squared norm, rounded from FP64
+__device__ __forceinline__ float rsqrt_norm(int64_t n2) {
+    return n2 == 0 ? 0.0f : __double2float_rn(__drcp_rn(__dsqrt_rn((double)n2)));
+}
+
+}  // namespace hdc

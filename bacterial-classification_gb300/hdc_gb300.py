@@ -1,0 +1,237 @@
+"""ctypes binding of libhdc_gb300.so (the C ABI in include/hdc_gb300.h).
+
+This is the Python side used by the tests, the smoke check and the benchmark;
+device memory and streams come from torch (plumbing only: every computation
+runs in the library's own CUDA kernels).  Loading fails loudly when the
+library has not been built: there is no CPU fallback.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libhdc_gb300.so")
+
+HDC_OK = 0
+ERR = {1: "HDC_ERR_INVALID", 2: "HDC_ERR_RANGE", 3: "HDC_ERR_CUDA", 4: "HDC_ERR_NOMEM",
+       5: "HDC_ERR_UNSUPPORTED", 6: "HDC_ERR_TIMEOUT"}
+SCORE_NORM, SCORE_COS, SCORE_DOT = 0, 1, 2
+OUT_I16, OUT_I32, OUT_BIPOLAR_BF16, OUT_BIPOLAR_I16 = 0, 1, 2, 3
+
+# (name, restype, argtypes) of every exported entry point
+P, I32, I64, SZ = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_size_t
+SIGNATURES = [
+    ("hdc_last_error", ctypes.c_char_p, []),
+    ("hdc_status_string", ctypes.c_char_p, [I32]),
+    ("hdc_context_create", I32, [I32, I32, I32, I32, ctypes.POINTER(P)]),
+    ("hdc_context_destroy", None, [P]),
+    ("hdc_context_base_hvs", I32, [P, P]),
+    ("hdc_encode_segments", I32, [P, P, P, P, I64, ctypes.c_int32, I32, P, I64, P, P]),
+    ("hdc_num_windows", I64, [P, I64]),
+    ("hdc_encode_windows", I32, [P, P, P, P, I64, I64, P, P]),
+    ("hdc_norms", I32, [P, P, I32, I64, P, P, P]),
+    ("hdc_search_workspace_bytes", SZ, [P, I64, I64, I32]),
+    ("hdc_search_plain", I32, [P, P, P, I64, ctypes.c_int32, P, P, I64, ctypes.c_int32, I32, I32, P, P, P, P, P,
+                               SZ, P]),
+    ("hdc_bundle", I32, [P, P, I32, P, P, I64, P, P]),
+    ("hdc_synth_tree", I32, [ctypes.c_uint64, I64, I32, P, I32, I32, I32, P, I64, P, P, P, I32]),
+    ("hdc_synth_copies", I32, [ctypes.c_uint64, P, P, P, I64, I32, ctypes.c_double, P, I64, P, P, I32]),
+    ("hdc_synth_reads", I32, [ctypes.c_uint64, P, P, P, I64, I64, I32, ctypes.c_double, I32, I32, ctypes.c_double,
+                              ctypes.c_double, ctypes.c_double, P, I64, P, P, P, I32]),
+]
+
+_lib = None
+
+
+class HDCError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (ERR.get(status, status), msg))
+        self.status = status
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libhdc_gb300.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status):
+    if status != HDC_OK:
+        raise HDCError(status, lib().hdc_last_error().decode())
+
+
+def ptr(t):
+    """Device (or host) address of a torch tensor, or None."""
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def stream_ptr(stream=None):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+class Context:
+    """One hypervector configuration (dim, kmer, window, step) on the current device."""
+
+    def __init__(self, dim, kmer, window=150, step=10):
+        self.dim, self.kmer, self.window, self.step = dim, kmer, window, step
+        h = ctypes.c_void_p()
+        check(lib().hdc_context_create(dim, kmer, window, step, ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().hdc_context_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def base_hvs(self):
+        import numpy as np
+        out = np.zeros((4, (self.dim + 63) // 64), np.uint64)
+        check(lib().hdc_context_base_hvs(self.h, out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    # ---------------------------------------------------------------- encode
+    def encode_segments(self, d_bytes, d_off, d_len, out, out_kind=OUT_I16, max_len=0, nkmers=None, stream=None):
+        n = d_off.numel()
+        check(lib().hdc_encode_segments(self.h, ptr(d_bytes), ptr(d_off), ptr(d_len), n, int(max_len), out_kind,
+                                        ptr(out), out.stride(0), ptr(nkmers), stream_ptr(stream)))
+        return out
+
+    def num_windows(self, length):
+        return lib().hdc_num_windows(self.h, length)
+
+    def encode_windows(self, d_bytes, d_seq_off, d_win_off, n_windows, out, stream=None):
+        check(lib().hdc_encode_windows(self.h, ptr(d_bytes), ptr(d_seq_off), ptr(d_win_off), d_seq_off.numel() - 1,
+                                       n_windows, ptr(out), stream_ptr(stream)))
+        return out
+
+    # ---------------------------------------------------------------- search
+    def norms(self, hv, maxabs=None, stream=None):
+        import torch
+        n2 = torch.empty(hv.shape[0], dtype=torch.int64, device=hv.device)
+        check(lib().hdc_norms(self.h, ptr(hv), hv.element_size(), hv.shape[0], ptr(n2), ptr(maxabs),
+                              stream_ptr(stream)))
+        return n2
+
+    def workspace_bytes(self, nq, nr, k):
+        return lib().hdc_search_workspace_bytes(self.h, nq, nr, k)
+
+    def search_plain(self, q, qn, maxq, r, rn, maxr, k, mode=SCORE_NORM, work=None, out=None, stream=None):
+        import torch
+        nq, nr = q.shape[0], r.shape[0]
+        kk = min(k, nr)
+        dev = q.device
+        if out is None:
+            out = (torch.empty((nq, kk), dtype=torch.float32, device=dev),
+                   torch.empty((nq, kk), dtype=torch.int32, device=dev),
+                   torch.empty((nq, kk), dtype=torch.float64, device=dev),
+                   torch.empty((nq, kk), dtype=torch.int64, device=dev))
+        wb = self.workspace_bytes(nq, nr, k)
+        if work is None or work.numel() < wb:
+            work = torch.empty(max(wb, 16), dtype=torch.uint8, device=dev)
+        s, i, c, d = out
+        check(lib().hdc_search_plain(self.h, ptr(q), ptr(qn), nq, int(maxq), ptr(r), ptr(rn), nr, int(maxr), k, mode,
+                                     ptr(s), ptr(i), ptr(c), ptr(d), ptr(work), work.numel(), stream_ptr(stream)))
+        return out
+
+    # ---------------------------------------------------------------- propagate
+    def bundle(self, rows, child_ptr, child_idx, out=None, stream=None):
+        import torch
+        npar = child_ptr.numel() - 1
+        if out is None:
+            out = torch.empty((npar, self.dim), dtype=torch.int32, device=rows.device)
+        check(lib().hdc_bundle(self.h, ptr(rows), rows.element_size(), ptr(child_ptr), ptr(child_idx), npar,
+                               ptr(out), stream_ptr(stream)))
+        return out
+
+
+def pack_sequences(seqs):
+    """Host packing of ASCII sequences: (bytes uint8[total+16], offsets int64[n], lengths int32[n])."""
+    import numpy as np
+    bs = [s.encode() if isinstance(s, str) else bytes(s) for s in seqs]
+    lens = np.fromiter((len(b) for b in bs), np.int64, len(bs))
+    offs = np.zeros(len(bs), np.int64)
+    if len(bs) > 1:
+        offs[1:] = np.cumsum(lens)[:-1]
+    buf = np.frombuffer(b"".join(bs) + b"\0" * 16, np.uint8)
+    return buf, offs, lens.astype(np.int32)
+
+
+# ---------------------------------------------------------------- synthetic workloads
+class Seqs:
+    """Concatenated ASCII sequences on the host: buf uint8, off int64, len int32."""
+
+    def __init__(self, buf, off, ln, label=None):
+        self.buf, self.off, self.len, self.label = buf, off, ln, label
+
+    def __len__(self):
+        return len(self.off)
+
+    def get(self, i):
+        o = int(self.off[i])
+        return bytes(self.buf[o:o + int(self.len[i])]).decode()
+
+    def max_len(self):
+        return int(self.len.max()) if len(self.len) else 0
+
+
+def _np_ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def synth_tree(seed, n_leaves, root_len=1500, subst=(0.04, 0.03, 0.02, 0.015, 0.01, 0.005), jitter=20,
+               min_len=1400, max_len=1600, threads=0):
+    import numpy as np
+    sub = np.array(subst, np.float64)
+    buf = np.zeros(n_leaves * max_len + 16, np.uint8)
+    off = np.zeros(n_leaves, np.int64)
+    ln = np.zeros(n_leaves, np.int32)
+    ranks = np.zeros(7, np.int64)
+    if lib().hdc_synth_tree(seed, n_leaves, root_len, _np_ptr(sub), jitter, min_len, max_len, _np_ptr(buf),
+                            buf.size, _np_ptr(off), _np_ptr(ln), _np_ptr(ranks), threads) != 0:
+        raise ValueError("hdc_synth_tree failed")
+    s = Seqs(buf, off, ln)
+    s.nodes_per_rank = ranks
+    return s
+
+
+def synth_copies(seed, src, n_copies, subst, threads=0):
+    import numpy as np
+    n = len(src) * n_copies
+    buf = np.zeros(int(src.len.astype(np.int64).sum()) * n_copies + 16, np.uint8)
+    off = np.zeros(n, np.int64)
+    ln = np.zeros(n, np.int32)
+    if lib().hdc_synth_copies(seed, _np_ptr(src.buf), _np_ptr(src.off), _np_ptr(src.len), len(src), n_copies,
+                              subst, _np_ptr(buf), buf.size, _np_ptr(off), _np_ptr(ln), threads) != 0:
+        raise ValueError("hdc_synth_copies failed")
+    return Seqs(buf, off, ln)
+
+
+def synth_reads(seed, src, n_reads, read_len, subst=0.01, sigma=0.0, min_read=100, max_read=1600,
+                mixed_frac=0.0, mixed_rate=0.0, threads=0):
+    import numpy as np
+    cap_len = max(read_len, max_read if sigma > 0 else read_len)
+    cap = n_reads * (cap_len + cap_len // 4 + 8) + 16
+    buf = np.zeros(cap, np.uint8)
+    off = np.zeros(n_reads, np.int64)
+    ln = np.zeros(n_reads, np.int32)
+    lab = np.zeros(n_reads, np.int32)
+    if lib().hdc_synth_reads(seed, _np_ptr(src.buf), _np_ptr(src.off), _np_ptr(src.len), len(src), n_reads,
+                             read_len, sigma, min_read, max_read, subst, mixed_frac, mixed_rate, _np_ptr(buf),
+                             buf.size, _np_ptr(off), _np_ptr(ln), _np_ptr(lab), threads) != 0:
+        raise ValueError("hdc_synth_reads failed")
+    return Seqs(buf, off, ln, lab)

@@ -1,0 +1,388 @@
+"""Benchmark of the hypervector classification hot path on GB300.
+
+A step is one batch of synthetic reads pushed through the hot path with the
+reference database resident in HBM: encode every read (kernel a), then
+exact cosine top-k against every reference (kernel b).  Prints one JSON line.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config c2|c3]
+                    [--form plain|tc] [--batch B] [--impl ours|reference]
+
+Workloads (seeded synthetic data standing in for real 16S data, none of
+which is available here):
+  c2  plain GPU drop-in at scale: 50,000 leaf references of a 6-rank tree,
+      D=8192, k=8, reads of 150 bp with 1% substitutions, top-5, NORM score
+  c3  precision form: 200,000 leaf references, each the bundle of 8 noisy
+      copies (1% substitutions) of its leaf, D=10240, k=10; reads of 250 bp
+      with 1% substitutions, bipolar queries, top-5
+
+--impl reference times the reference CPU algorithm (the C restatement in
+oracle/, the reference's own sources being unavailable on the GPU host) on
+the host cores, on a bounded sample of the same workload.
+With torchrun (N > 1) every rank runs an independent replica on its own GPU
+(reads shard with no exchange); the step time is the max over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "bacterial-classification_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+CONFIGS = {
+    "c2": dict(n_leaves=50000, dim=8192, kmer=8, read_len=150, subst=0.01, topk=5, copies=0, bipolar=False,
+               tree_seed=2, read_seed=102, copy_seed=0),
+    "c3": dict(n_leaves=200000, dim=10240, kmer=10, read_len=250, subst=0.01, topk=5, copies=8, bipolar=True,
+               tree_seed=3, read_seed=103, copy_seed=203),
+}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "sm_max_mhz": 2070.0}, \
+        "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# ---------------------------------------------------------------------------- workload
+def build_database(H, ctx, cfg, dev):
+    """Reference hypervectors resident in HBM: leaves (c2) or bundles of noisy copies (c3)."""
+    import torch
+    t0 = time.time()
+    tree = H.synth_tree(cfg["tree_seed"], cfg["n_leaves"])
+    nr, dim = cfg["n_leaves"], cfg["dim"]
+    refs = torch.empty((nr, dim), dtype=torch.int16, device=dev)
+    d_tree = torch.from_numpy(tree.buf).to(dev)
+    chunk = 8192
+    for a in range(0, nr, chunk):
+        b = min(nr, a + chunk)
+        sub = H.Seqs(tree.buf, tree.off[a:b], tree.len[a:b])
+        if cfg["copies"]:
+            cp = H.synth_copies(cfg["copy_seed"] + a, sub, cfg["copies"], 0.01)
+            d_b = torch.from_numpy(cp.buf).to(dev)
+            n = len(cp)
+            tmp = torch.empty((n, dim), dtype=torch.int32, device=dev)
+            ctx.encode_segments(d_b, torch.from_numpy(cp.off).to(dev), torch.from_numpy(cp.len).to(dev), tmp,
+                                H.OUT_I32, cp.max_len())
+            ptr = torch.arange(0, n + 1, cfg["copies"], dtype=torch.int64, device=dev)
+            idx = torch.arange(n, dtype=torch.int32, device=dev)
+            summed = ctx.bundle(tmp, ptr, idx)
+            refs[a:b] = summed.to(torch.int16)  # |sum| <= 8 * 1600 fits int16
+        else:
+            off = torch.from_numpy(np.ascontiguousarray(tree.off[a:b])).to(dev)
+            ln = torch.from_numpy(np.ascontiguousarray(tree.len[a:b])).to(dev)
+            ctx.encode_segments(d_tree, off, ln, refs[a:b], H.OUT_I16, int(tree.len[a:b].max()))
+    maxr = torch.zeros(1, dtype=torch.int32, device=dev)
+    rn = ctx.norms(refs, maxr)
+    torch.cuda.synchronize()
+    log("database: %d references x %d dims built in %.1f s" % (nr, dim, time.time() - t0))
+    return tree, refs, rn, int(maxr.item())
+
+
+def make_reads(H, tree, cfg, n, seed):
+    return H.synth_reads(seed, tree, n, cfg["read_len"], subst=cfg["subst"])
+
+
+# ---------------------------------------------------------------------------- our arm
+def run_ours(args, cfg, rank, world):
+    import torch
+    import hdc_gb300 as H
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    ctx = H.Context(cfg["dim"], cfg["kmer"], cfg["read_len"], 10)
+    tree, refs, rn, maxr = build_database(H, ctx, cfg, dev)
+    B, K, dim = args.batch, cfg["topk"], cfg["dim"]
+    n_pool = 2
+    reads = make_reads(H, tree, cfg, B * n_pool, cfg["read_seed"] + 1000 * rank)
+    maxq = cfg["read_len"] - cfg["kmer"] + 1 if not cfg["bipolar"] else 1
+    kind = H.OUT_BIPOLAR_I16 if cfg["bipolar"] else H.OUT_I16
+    # device-resident read batches
+    d_buf = torch.from_numpy(reads.buf).to(dev)
+    batches = []
+    for p in range(n_pool):
+        off = torch.from_numpy(np.ascontiguousarray(reads.off[p * B:(p + 1) * B])).to(dev)
+        ln = torch.from_numpy(np.ascontiguousarray(reads.len[p * B:(p + 1) * B])).to(dev)
+        batches.append((off, ln))
+    q = torch.empty((B, dim), dtype=torch.int16, device=dev)
+    work = torch.empty(ctx.workspace_bytes(B, refs.shape[0], K), dtype=torch.uint8, device=dev)
+    out = (torch.empty((B, K), dtype=torch.float32, device=dev), torch.empty((B, K), dtype=torch.int32, device=dev),
+           torch.empty((B, K), dtype=torch.float64, device=dev), torch.empty((B, K), dtype=torch.int64, device=dev))
+    stream = torch.cuda.current_stream()
+    ev_s = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    search_ms = []
+
+    def step(i, time_search=False):
+        off, ln = batches[i % n_pool]
+        ctx.encode_segments(d_buf, off, ln, q, kind, cfg["read_len"])
+        qn = ctx.norms(q)
+        if time_search:
+            ev_s[0].record(stream)
+        ctx.search_plain(q, qn, maxq, refs, rn, maxr, K, H.SCORE_NORM, work=work, out=out)
+        if time_search:
+            ev_s[1].record(stream)
+        return out
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        torch.cuda.synchronize()
+        t0.record(stream)
+        for i in range(args.steps):
+            step(i)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / args.steps
+    # dominant kernel, timed alone inside a step (same stream)
+    for i in range(3):
+        step(i, time_search=True)
+        torch.cuda.synchronize()
+        search_ms.append(ev_s[0].elapsed_time(ev_s[1]))
+    search_ms = float(np.median(search_ms))
+
+    # end to end through the C ABI with host buffers (pinned), copies inside the timed region
+    h_bufs = []
+    for p in range(n_pool):
+        o0 = int(reads.off[p * B])
+        o1 = int(reads.off[(p + 1) * B - 1] + reads.len[(p + 1) * B - 1])
+        hb = torch.from_numpy(reads.buf[o0:o1].copy()).pin_memory()
+        ho = torch.from_numpy(reads.off[p * B:(p + 1) * B] - o0).pin_memory()
+        hl = torch.from_numpy(reads.len[p * B:(p + 1) * B].copy()).pin_memory()
+        h_bufs.append((hb, ho, hl))
+    cap = max(x[0].numel() for x in h_bufs)
+    e_buf = torch.empty(cap + 16, dtype=torch.uint8, device=dev)
+    e_off = torch.empty(B, dtype=torch.int64, device=dev)
+    e_len = torch.empty(B, dtype=torch.int32, device=dev)
+    h_s = torch.empty((B, K), dtype=torch.float32).pin_memory()
+    h_i = torch.empty((B, K), dtype=torch.int32).pin_memory()
+    h2d = d2h = 0
+
+    def e2e_step(i):
+        nonlocal h2d, d2h
+        hb, ho, hl = h_bufs[i % n_pool]
+        e_buf[:hb.numel()].copy_(hb, non_blocking=True)
+        e_off.copy_(ho, non_blocking=True)
+        e_len.copy_(hl, non_blocking=True)
+        ctx.encode_segments(e_buf, e_off, e_len, q, kind, cfg["read_len"])
+        qn = ctx.norms(q)
+        ctx.search_plain(q, qn, maxq, refs, rn, maxr, K, H.SCORE_NORM, work=work, out=out)
+        h_s.copy_(out[0], non_blocking=True)
+        h_i.copy_(out[1], non_blocking=True)
+        h2d = hb.numel() + ho.numel() * 8 + hl.numel() * 4
+        d2h = h_s.numel() * 4 + h_i.numel() * 4
+
+    for i in range(args.warmup):
+        e2e_step(i)
+    torch.cuda.synchronize()
+    t0.record(stream)
+    for i in range(args.steps):
+        e2e_step(i)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = t0.elapsed_time(t1) / args.steps
+
+    if world > 1:
+        t = torch.tensor([ms, e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms, e2e_ms = float(t[0]), float(t[1])
+    return dict(ms=ms, e2e_ms=e2e_ms, search_ms=search_ms, clocks=clk.summary(), h2d=h2d, d2h=d2h,
+                refs=refs.shape[0], launches=4 * args.steps, tree=tree,
+                refs_host=refs.cpu().numpy().astype(np.int32) if rank == 0 else None)
+
+
+def oracle_database(cfg, threads):
+    """Reference hypervectors built by the CPU oracle (no GPU involved)."""
+    import hdc_gb300 as H
+    from oracle import oracle as O
+    tree = H.synth_tree(cfg["tree_seed"], cfg["n_leaves"])
+    nr = cfg["n_leaves"]
+    refs = np.zeros((nr, cfg["dim"]), np.int32)
+    step = 4096
+    for a in range(0, nr, step):
+        sub = H.Seqs(tree.buf, tree.off[a:a + step], tree.len[a:a + step])
+        if cfg["copies"]:
+            cp = H.synth_copies(cfg["copy_seed"] + a, sub, cfg["copies"], 0.01)
+            enc, _ = O.encode([cp.get(i) for i in range(len(cp))], cfg["dim"], cfg["kmer"], "int32", threads)
+            refs[a:a + len(sub)] = enc.reshape(len(sub), cfg["copies"], -1).sum(1)
+        else:
+            enc, _ = O.encode([sub.get(i) for i in range(len(sub))], cfg["dim"], cfg["kmer"], "int32", threads)
+            refs[a:a + len(sub)] = enc
+    return tree, refs
+
+
+def cpu_baseline(cfg, tree, refs, seconds=12.0, threads=None):
+    """The reference CPU algorithm (oracle restatement: HVCache::compute per read
+    then brute-force cosine over every reference) on a bounded sample of reads."""
+    import hdc_gb300 as H
+    from oracle import oracle as O
+    threads = threads or (os.cpu_count() or 1)
+    reads = make_reads(H, tree, cfg, 4096, cfg["read_seed"] + 999)
+    n = max(threads, 1)
+    done = 0
+    t_total = 0.0
+    while t_total < seconds and done < len(reads):
+        batch = [reads.get(i) for i in range(done, min(len(reads), done + n))]
+        t0 = time.time()
+        O.classify(batch, refs, cfg["dim"], cfg["kmer"], cfg["topk"], O.SCORE_NORM, cfg["bipolar"], threads)
+        t_total += time.time() - t0
+        done += len(batch)
+        n = min(4 * n, 1024)
+    return done / t_total, threads, done
+
+
+def run_reference(args, cfg):
+    """Reference arm: the reference CPU path on the host cores, per step a bounded sample."""
+    threads = os.cpu_count() or 1
+    t0 = time.time()
+    tree, refs = oracle_database(cfg, threads)
+    log("oracle database built in %.1f s" % (time.time() - t0))
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, threads, done = cpu_baseline(cfg, tree, refs, seconds=2.0 if i < args.warmup else 6.0, threads=threads)
+        if i >= args.warmup:
+            vals.append(v)
+    v = float(np.median(vals))
+    return v, threads, done
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
+    ap.add_argument("--form", default="plain", choices=["plain"])
+    ap.add_argument("--batch", type=int, default=32768)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("warmup raised to 3")
+        args.warmup = 3
+    cfg = CONFIGS[args.config]
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    workload = "%s: %d refs D=%d k=%d, %d bp reads, top-%d" % (args.config, cfg["n_leaves"], cfg["dim"], cfg["kmer"],
+                                                               cfg["read_len"], cfg["topk"])
+    metric = "reads/s encode+top-%d search" % cfg["topk"]
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        v, threads, done = run_reference(args, cfg)
+        line = {"impl": "reference", "metric": metric, "value": v, "unit": "reads/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "int64",
+                "data": "synthetic", "config": {"workload": workload},
+                "cpu_baseline": {"value": v, "unit": "reads/s", "cores": threads, "kind": "port",
+                                 "sample": "%d reads per step, same database" % done},
+                "e2e": {"value": v, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    r = run_ours(args, cfg, rank, world)
+    if rank != 0:
+        torch.distributed.destroy_process_group()
+        return
+    pk, src = peaks()
+    B = args.batch
+    value = B * world / (r["ms"] / 1e3)
+    # roofline of the dominant kernel (the plain search): 2*D*R ops per read on the FP32 pipe
+    ops = 2.0 * cfg["dim"] * r["refs"] * B
+    achieved = ops / (r["search_ms"] / 1e3) / 1e12
+    sm_mhz = r["clocks"].get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    line = {
+        "metric": metric, "value": value, "unit": "reads/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int16 (exact integer dot, fp32-pipe chunks)", "data": "synthetic",
+        "config": {"workload": workload, "form": args.form, "batch_reads": B,
+                   "l2": "inputs larger than L2: %.0f MB reference database read every step" %
+                         (r["refs"] * cfg["dim"] * 2 / 1e6)},
+        "e2e": {"value": B * world / (r["e2e_ms"] / 1e3), "unit": "reads/s", "h2d_bytes_per_step": r["h2d"],
+                "d2h_bytes_per_step": r["d2h"]},
+        "roofline": {"bound": "fp32-pipe", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak, "traffic": None,
+                     "note": "plain search on CUDA cores; peak = 152 SMs x 128 FFMA x 2 x median SM clock"},
+        "clocks": r["clocks"], "gpu_launches": r["launches"],
+    }
+    if not args.no_cpu_baseline:
+        v, threads, done = cpu_baseline(cfg, r["tree"], r["refs_host"])
+        line["cpu_baseline"] = {"value": v, "unit": "reads/s", "cores": threads, "kind": "port",
+                                "sample": "%d reads of the same workload (encode + brute-force top-%d against "
+                                          "all %d references; database hypervectors from the GPU encoder, "
+                                          "bit-identical to the oracle's)" % (done, cfg["topk"], r["refs"])}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,137 @@
+/*
+ * hdc_gb300.h -- C ABI of the GB300 (sm_103a) k-mer hypervector classifier
+ * hot path: (a) k-mer hypervector encoding, (b) query x reference cosine
+ * top-k search, (c) propagate-children bundling and greedy selection.
+ *
+ * Conventions
+ *   - Every function returns an int status (HDC_OK = 0); no exception crosses
+ *     this boundary.  hdc_last_error() gives a message for the calling thread.
+ *   - Pointers named d_* are device pointers owned by the caller; outputs are
+ *     caller-allocated.  Work is enqueued on the given CUDA stream (a
+ *     cudaStream_t passed as void*; NULL is the legacy default stream) and is
+ *     asynchronous unless stated otherwise.
+ *   - Sizes are runtime parameters (the reference fixes them at compile time
+ *     in src/config.h:5-8): dim = HV_DIM, kmer = KMER_SIZE (1..16),
+ *     window = SEQUENCE_LENGTH, step = SIM_STEP.
+ *   - Sequences are raw ASCII bytes.  Exactly the bytes 'A','C','G','T' are
+ *     bases; a k-mer holding any other byte (N, lowercase, IUPAC codes) is
+ *     skipped, as the reference CPU encoder does (src/encoder.cpp:115-117).
+ *
+ * Score modes (the ranking key is the float score, ties -> lower ref index)
+ *   HDC_SCORE_NORM  float(2*(cos - 0.5)), -1 for a zero norm: the reference
+ *                   cosine() built with NORM_COSINE (src/HV.cpp:219-242)
+ *   HDC_SCORE_COS   float(cos), -1 for a zero norm: the scale the reference
+ *                   GPU search reports (src/cosine.cu:270-271), but computed
+ *                   from the exact integer dot and norms in FP64
+ *   HDC_SCORE_DOT   float(dot): cosine() built without NORM_COSINE
+ *                   (src/HV.cpp:244-252)
+ */
+#ifndef HDC_GB300_H
+#define HDC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HDC_OK 0
+#define HDC_ERR_INVALID 1     /* bad argument or unsupported size */
+#define HDC_ERR_RANGE 2       /* values outside the exactly-representable range */
+#define HDC_ERR_CUDA 3        /* CUDA runtime error */
+#define HDC_ERR_NOMEM 4       /* device allocation failed */
+#define HDC_ERR_UNSUPPORTED 5 /* device is not sm_103 or lacks a feature */
+#define HDC_ERR_TIMEOUT 6     /* a bounded device-side wait gave up */
+
+#define HDC_SCORE_NORM 0
+#define HDC_SCORE_COS 1
+#define HDC_SCORE_DOT 2
+
+/* Output element kinds of the encoder. */
+#define HDC_OUT_I16 0          /* int16 bundle, wraps modulo 2^16 like the reference */
+#define HDC_OUT_I32 1          /* int32 bundle, exact (segments of <= 65535 k-mers) */
+#define HDC_OUT_BIPOLAR_BF16 2 /* bf16 +1/-1 sign of the bundle, 0 -> +1 */
+#define HDC_OUT_BIPOLAR_I16 3  /* int16 +1/-1 sign of the bundle, 0 -> +1 */
+
+typedef struct hdc_context hdc_context;
+typedef struct hdc_refdb hdc_refdb;
+
+const char* hdc_last_error(void);
+const char* hdc_status_string(int status);
+
+/* Create a context on the current device: base hypervectors (src/HV.cpp:20-41,
+ * mt19937_64 seeds A=0 C=1 T=2 G=3) are generated and uploaded. */
+int hdc_context_create(int dim, int kmer, int window, int step, hdc_context** out);
+void hdc_context_destroy(hdc_context* ctx);
+/* The four base hypervectors in A,C,G,T order, [4][ceil(dim/64)] uint64 words (host). */
+int hdc_context_base_hvs(const hdc_context* ctx, uint64_t* host_out);
+
+/* ---------------------------------------------------------------- (a) encode */
+
+/* Encode n_segs byte segments d_bytes[d_seg_off[i] .. d_seg_off[i]+d_seg_len[i])
+ * with the whole-segment semantics of HVCache::compute (src/encoder.cpp:106-132):
+ * sum over every k-mer position of the +1/-1 binder of the canonical k-mer.
+ * Row i of d_out (row stride out_stride elements, >= dim) receives segment i.
+ * max_len is an upper bound on the segment lengths (0: unknown), used to size
+ * the device counters.  d_nkmers (optional, int32[n_segs]) receives the
+ * number of k-mers bundled.  Replaces the per-window kernel hdc_encode /
+ * launch_hdc_encode (src/encode.cu:69-165). */
+int hdc_encode_segments(hdc_context* ctx, const char* d_bytes, const int64_t* d_seg_off,
+                        const int32_t* d_seg_len, int64_t n_segs, int32_t max_len, int out_kind,
+                        void* d_out, int64_t out_stride, int32_t* d_nkmers, void* stream);
+
+/* Number of windows of a sequence of length len: (len - window)/step + 1, or 0
+ * when len < window (src/encode.cu:258 without its negative-length case). */
+int64_t hdc_num_windows(const hdc_context* ctx, int64_t len);
+
+/* Window form of the encoder, the drop-in for launch_hdc_encode
+ * (src/encode.cu:136-165): sequence s is d_bytes[d_seq_off[s] .. d_seq_off[s+1]),
+ * its windows start at w*step and span `window` bytes, and window w of
+ * sequence s is written to row d_win_off[s] + w of d_out (int16, row stride
+ * dim).  d_win_off[s+1] - d_win_off[s] must equal hdc_num_windows(len s).
+ * Each window gets HVCache::compute of its substring (the sequence offsets
+ * are byte offsets, so every sequence of a batch is read from its own bases). */
+int hdc_encode_windows(hdc_context* ctx, const char* d_bytes, const int64_t* d_seq_off,
+                       const int64_t* d_win_off, int64_t n_seqs, int64_t n_windows, int16_t* d_out,
+                       void* stream);
+
+/* ---------------------------------------------------------------- (b) search */
+
+/* Squared L2 norms (int64) and optional max |v| (int32 atomic max into
+ * *d_maxabs, which the caller zeroes) of n rows of int16 (elem_bytes 2) or
+ * int32 (elem_bytes 4) hypervectors, row stride dim. */
+int hdc_norms(hdc_context* ctx, const void* d_hv, int elem_bytes, int64_t n, int64_t* d_norm2,
+              int32_t* d_maxabs, void* stream);
+
+/* Workspace the plain search needs for nq queries and top-k. */
+size_t hdc_search_workspace_bytes(const hdc_context* ctx, int64_t nq, int64_t nr, int k);
+
+/* Plain form: exact integer cosine top-k of int16 queries against int16
+ * references on CUDA cores, the drop-in for launch_cosine_topk
+ * (src/cosine.cu:441-496) and, with k = 1, launch_cosine_argmax
+ * (src/cosine.cu:172-222).  For every query: the k best references by the
+ * float score of score_mode (descending), ties to the lower reference index.
+ * k is clamped to nr (src/cosine.cu:451).  Outputs are [nq][k]: d_score
+ * (float), d_idx (int32), d_cos (double, FP64 cosine from the exact dot;
+ * optional), d_dot (int64 exact dot; optional).  max_abs_q / max_abs_r bound
+ * |element| of queries / references (from hdc_norms); products must satisfy
+ * max_abs_q * max_abs_r <= 2^22.  d_qnorm2 / d_rnorm2 come from hdc_norms.
+ * d_work must hold hdc_search_workspace_bytes(nq, nr, k) bytes. */
+int hdc_search_plain(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qnorm2, int64_t nq,
+                     int32_t max_abs_q, const int16_t* d_r, const int64_t* d_rnorm2, int64_t nr,
+                     int32_t max_abs_r, int k, int score_mode, float* d_score, int32_t* d_idx,
+                     double* d_cos, int64_t* d_dot, void* d_work, size_t work_bytes, void* stream);
+
+/* ---------------------------------------------------------------- (c) propagate */
+
+/* Bundling of taxonomy nodes: parent p = sum of its children's rows
+ * (child_ptr[p] .. child_ptr[p+1] index child_idx, which indexes d_rows),
+ * exact int32.  Rows are int16 (elem_bytes 2) or int32 (4); out is int32. */
+int hdc_bundle(hdc_context* ctx, const void* d_rows, int elem_bytes, const int64_t* d_child_ptr,
+               const int32_t* d_child_idx, int64_t n_parents, int32_t* d_out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HDC_GB300_H */

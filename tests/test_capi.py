@@ -1,0 +1,55 @@
+"""CPU checks of the C-ABI library: it builds, loads, and exports every
+symbol include/hdc_gb300.h declares (no compute call needs a GPU here)."""
+import os
+import re
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if not h.endswith(".h"):
+            continue
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names += re.findall(r"^[A-Za-z_][\w \*]*?\b(hdc_\w+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert "hdc_encode_segments" in names and "hdc_search_plain" in names and "hdc_bundle" in names
+
+
+def test_library_exports_every_declared_symbol(hdc):
+    lib = hdc.lib()
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_binding_covers_header(hdc):
+    bound = {name for name, _, _ in hdc.SIGNATURES}
+    assert set(declared_functions()) <= bound
+
+
+def test_status_strings(hdc):
+    lib = hdc.lib()
+    assert lib.hdc_status_string(0) == b"ok"
+    assert lib.hdc_status_string(2) == b"value range"
+
+
+def test_context_rejects_bad_sizes_without_gpu(hdc):
+    import ctypes
+    h = ctypes.c_void_p()
+    assert hdc.lib().hdc_context_create(0, 8, 150, 10, ctypes.byref(h)) == 1
+    assert b"dim" in hdc.lib().hdc_last_error()
+    assert hdc.lib().hdc_context_create(1024, 17, 150, 10, ctypes.byref(h)) == 1
+    assert hdc.lib().hdc_context_create(1024, 8, 0, 10, ctypes.byref(h)) == 1
+
+
+def test_null_context_is_an_error(hdc):
+    lib = hdc.lib()
+    assert lib.hdc_norms(None, None, 2, 0, None, None, None) == 1
+    assert lib.hdc_search_workspace_bytes(None, 1, 1, 1) == 0
+    assert lib.hdc_num_windows(None, 500) == 0
