@@ -45,6 +45,12 @@ int launch_search_plain(hdc_context* ctx, const int16_t* d_q, const int64_t* d_q
                         float* d_score, int32_t* d_idx, double* d_cos, int64_t* d_dot, void* d_work,
                         size_t work_bytes, cudaStream_t stream);
 
+// Merge n_lists partial top-k lists per query ([n_lists][nq][k] keys and dots)
+// into the final outputs.
+int launch_merge(const uint64_t* ws_key, const int64_t* ws_dot, int n_lists, int64_t nq, int k, const int64_t* d_qn,
+                 const int64_t* d_rn, float* d_score, int32_t* d_idx, double* d_cos, int64_t* d_dot,
+                 cudaStream_t stream);
+
 int launch_bundle(hdc_context* ctx, const void* d_rows, int elem_bytes, const int64_t* d_child_ptr,
                   const int32_t* d_child_idx, int64_t n_parents, int32_t* d_out, cudaStream_t stream);
 

@@ -69,7 +69,7 @@ struct PlainArgs {
     const int64_t* rn;
     int64_t nr;
     int dim, k, mode;
-    int chunk_tiles;   // K tiles per exact fp32 chunk (>= 1)
+    int fold_groups;   // 4-dim groups per exact fp32 chunk (>= 1)
     int n_splits;      // reference ranges per query tile
     int64_t split_len;  // references per range (multiple of kBR)
     uint64_t* ws_key;   // [n_splits][nq][k]
@@ -78,18 +78,6 @@ struct PlainArgs {
 
 __device__ __forceinline__ int32_t fold_bits(float acc) { return __float_as_int(acc + 12582912.0f); }
 constexpr int32_t kMagicBits = 0x4B400000;
-
-// Insert (key, dot) into a descending list of length k held in local memory.
-__device__ __forceinline__ void list_insert(uint64_t* keys, int64_t* dots, int k, uint64_t key, int64_t dot) {
-    int pos = k - 1;
-    while (pos > 0 && keys[pos - 1] < key) {
-        keys[pos] = keys[pos - 1];
-        dots[pos] = dots[pos - 1];
-        --pos;
-    }
-    keys[pos] = key;
-    dots[pos] = dot;
-}
 
 template <int TQ, bool WIDE, bool VEC>
 __global__ void __launch_bounds__(kThreadsP, 1) plain_kernel(const PlainArgs a) {
@@ -180,7 +168,7 @@ __global__ void __launch_bounds__(kThreadsP, 1) plain_kernel(const PlainArgs a) 
                 acc[i][j] = 0.f;
                 mid[i][j] = 0;
             }
-        int nfold = 0;
+        int nfold = 0, groups_since_fold = 0;
         if (t < kBR) {
             const int64_t g = rb + t;
             const int64_t n2 = g < rend ? a.rn[g] : 0;
@@ -201,38 +189,45 @@ __global__ void __launch_bounds__(kThreadsP, 1) plain_kernel(const PlainArgs a) 
             }
             const float* qb = qs + buf * kKT * QLD + ty * TQ;
             const float* rb0 = rs + buf * kKT * RLD + tx * 4;
-#pragma unroll 8
-            for (int d = 0; d < kKT; ++d) {
-                float qv[TQ], rv[8];
 #pragma unroll
-                for (int u = 0; u < TQ / 4; ++u) {
-                    const float4 f = *reinterpret_cast<const float4*>(qb + d * QLD + 4 * u);
-                    qv[4 * u] = f.x;
-                    qv[4 * u + 1] = f.y;
-                    qv[4 * u + 2] = f.z;
-                    qv[4 * u + 3] = f.w;
-                }
-                const float4 r0 = *reinterpret_cast<const float4*>(rb0 + d * RLD);
-                const float4 r1 = *reinterpret_cast<const float4*>(rb0 + d * RLD + 64);
-                rv[0] = r0.x; rv[1] = r0.y; rv[2] = r0.z; rv[3] = r0.w;
-                rv[4] = r1.x; rv[5] = r1.y; rv[6] = r1.z; rv[7] = r1.w;
+            for (int g = 0; g < kKT / 4; ++g) {
 #pragma unroll
-                for (int i = 0; i < TQ; ++i)
+                for (int dd = 0; dd < 4; ++dd) {
+                    const int d = 4 * g + dd;
+                    float qv[TQ], rv[8];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(qv[i], rv[j], acc[i][j]);
-            }
-            if ((kt + 1) % a.chunk_tiles == 0 || kt + 1 == nkt) {
-#pragma unroll
-                for (int i = 0; i < TQ; ++i)
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        if (WIDE)
-                            mid[i][j] += (int64_t)(fold_bits(acc[i][j]) - kMagicBits);
-                        else
-                            mid[i][j] = (Mid)((uint32_t)mid[i][j] + (uint32_t)fold_bits(acc[i][j]));
-                        acc[i][j] = 0.f;
+                    for (int u = 0; u < TQ / 4; ++u) {
+                        const float4 f = *reinterpret_cast<const float4*>(qb + d * QLD + 4 * u);
+                        qv[4 * u] = f.x;
+                        qv[4 * u + 1] = f.y;
+                        qv[4 * u + 2] = f.z;
+                        qv[4 * u + 3] = f.w;
                     }
-                ++nfold;
+                    const float4 r0 = *reinterpret_cast<const float4*>(rb0 + d * RLD);
+                    const float4 r1 = *reinterpret_cast<const float4*>(rb0 + d * RLD + 64);
+                    rv[0] = r0.x; rv[1] = r0.y; rv[2] = r0.z; rv[3] = r0.w;
+                    rv[4] = r1.x; rv[5] = r1.y; rv[6] = r1.z; rv[7] = r1.w;
+#pragma unroll
+                    for (int i = 0; i < TQ; ++i)
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(qv[i], rv[j], acc[i][j]);
+                }
+                // fold the exact fp32 partials into the integer accumulator
+                // every fold_groups groups of 4 dims, and after the last tile
+                if (++groups_since_fold == a.fold_groups || (kt + 1 == nkt && g == kKT / 4 - 1)) {
+                    groups_since_fold = 0;
+#pragma unroll
+                    for (int i = 0; i < TQ; ++i)
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            if (WIDE)
+                                mid[i][j] += (int64_t)(fold_bits(acc[i][j]) - kMagicBits);
+                            else
+                                mid[i][j] = (Mid)((uint32_t)mid[i][j] + (uint32_t)fold_bits(acc[i][j]));
+                            acc[i][j] = 0.f;
+                        }
+                    ++nfold;
+                }
             }
             if (kt + 1 < nkt) {
                 store_q(buf ^ 1, sq);
@@ -403,13 +398,11 @@ int launch_search_plain(hdc_context* ctx, const int16_t* d_q, const int64_t* d_q
     if (nr > 0x7fffffffLL) return fail(HDC_ERR_INVALID, "search: more than 2^31-1 references");
     if (maxq < 0 || maxr < 0) return fail(HDC_ERR_INVALID, "search: negative bound");
     const int64_t prod = (int64_t)std::max(maxq, 1) * std::max(maxr, 1);
-    const int64_t lim = (int64_t)1 << 22;
-    if (prod >= lim)
-        return fail(HDC_ERR_RANGE, "search: max|q|*max|r| must stay below 2^22 for exact fp32 products");
-    const int64_t chunk_dims = (lim - 1) / prod;  // fp32 partials stay below 2^22
-    const int chunk_tiles = (int)std::max<int64_t>(1, std::min<int64_t>(chunk_dims / kKT, 1 << 20));
-    if (chunk_dims < kKT)
-        return fail(HDC_ERR_RANGE, "search: max|q|*max|r| too large for a 32-dim exact fp32 chunk");
+    const int64_t lim = (int64_t)1 << 22;  // |fp32 partial| < 2^22 keeps FFMA chains and the fold exact
+    const int64_t chunk_dims = (lim - 1) / prod;
+    if (chunk_dims < 4)
+        return fail(HDC_ERR_RANGE, "search: max|q|*max|r| must not exceed 2^20 (exact fp32 chunks of 4 dims)");
+    const int fold_groups = (int)std::min<int64_t>(chunk_dims / 4, 1 << 24);
     const bool wide = prod * (int64_t)ctx->dim >= ((int64_t)1 << 31);
     const bool vec = (ctx->dim % 8 == 0) && ((reinterpret_cast<uintptr_t>(d_q) & 15) == 0) &&
                      ((reinterpret_cast<uintptr_t>(d_r) & 15) == 0);
@@ -424,7 +417,7 @@ int launch_search_plain(hdc_context* ctx, const int16_t* d_q, const int64_t* d_q
     a.dim = ctx->dim;
     a.k = k;
     a.mode = mode;
-    a.chunk_tiles = chunk_tiles;
+    a.fold_groups = fold_groups;
     a.n_splits = plain_splits(ctx, nq, nr, tq);
     const int64_t rtiles = (nr + kBR - 1) / kBR;
     a.split_len = ((rtiles + a.n_splits - 1) / a.n_splits) * kBR;
@@ -439,9 +432,15 @@ int launch_search_plain(hdc_context* ctx, const int16_t* d_q, const int64_t* d_q
     else
         st = vec ? launch_plain_t<8, false, true>(a, nq, stream) : launch_plain_t<8, false, false>(a, nq, stream);
     if (st != HDC_OK) return st;
+    return launch_merge(a.ws_key, a.ws_dot, a.n_splits, nq, k, d_qn, d_rn, d_score, d_idx, d_cos, d_dot, stream);
+}
+
+int launch_merge(const uint64_t* ws_key, const int64_t* ws_dot, int n_lists, int64_t nq, int k, const int64_t* d_qn,
+                 const int64_t* d_rn, float* d_score, int32_t* d_idx, double* d_cos, int64_t* d_dot,
+                 cudaStream_t stream) {
     const int mt = 128;
-    merge_kernel<<<(unsigned)((nq + mt - 1) / mt), mt, 0, stream>>>(a.ws_key, a.ws_dot, a.n_splits, nq, k, d_qn,
-                                                                  d_rn, d_score, d_idx, d_cos, d_dot);
+    merge_kernel<<<(unsigned)((nq + mt - 1) / mt), mt, 0, stream>>>(ws_key, ws_dot, n_lists, nq, k, d_qn, d_rn,
+                                                                  d_score, d_idx, d_cos, d_dot);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? HDC_OK : cuda_fail(e, "search: merge launch");
 }

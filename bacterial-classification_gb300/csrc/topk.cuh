@@ -75,4 +75,16 @@ __device__ __forceinline__ float rsqrt_norm(int64_t n2) {
     return n2 == 0 ? 0.0f : __double2float_rn(__drcp_rn(__dsqrt_rn((double)n2)));
 }
 
+// Insert (key, dot) into a descending list of length k held in local memory.
+__device__ __forceinline__ void list_insert(uint64_t* keys, int64_t* dots, int k, uint64_t key, int64_t dot) {
+    int pos = k - 1;
+    while (pos > 0 && keys[pos - 1] < key) {
+        keys[pos] = keys[pos - 1];
+        dots[pos] = dots[pos - 1];
+        --pos;
+    }
+    keys[pos] = key;
+    dots[pos] = dot;
+}
+
 }  // namespace hdc

@@ -116,7 +116,7 @@ size_t hdc_search_workspace_bytes(const hdc_context* ctx, int64_t nq, int64_t nr
  * (float), d_idx (int32), d_cos (double, FP64 cosine from the exact dot;
  * optional), d_dot (int64 exact dot; optional).  max_abs_q / max_abs_r bound
  * |element| of queries / references (from hdc_norms); products must satisfy
- * max_abs_q * max_abs_r <= 2^22.  d_qnorm2 / d_rnorm2 come from hdc_norms.
+ * max_abs_q * max_abs_r <= 2^20 (else HDC_ERR_RANGE).  d_qnorm2 / d_rnorm2 come from hdc_norms.
  * d_work must hold hdc_search_workspace_bytes(nq, nr, k) bytes. */
 int hdc_search_plain(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qnorm2, int64_t nq,
                      int32_t max_abs_q, const int16_t* d_r, const int64_t* d_rnorm2, int64_t nr,

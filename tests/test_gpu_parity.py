@@ -103,6 +103,16 @@ def test_encode_random_all_kinds(hdc, orc, cuda, dim, k):
     assert np.array_equal(outbf.float().numpy(), bip.astype(np.float32))
 
 
+def test_search_rejects_inexact_range(hdc, cuda):
+    import torch
+    ctx = hdc.Context(256, 8, 150, 10)
+    q = torch.zeros((4, 256), dtype=torch.int16, device=cuda)
+    n = ctx.norms(q)
+    with pytest.raises(hdc.HDCError) as e:
+        ctx.search_plain(q, n, 1100, q, n, 1000, 1)  # 1.1e6 > 2^20
+    assert e.value.status == 2
+
+
 def test_encode_max_len_hint_is_checked(hdc, cuda):
     ctx = hdc.Context(1024, 8, 150, 10)
     with pytest.raises(hdc.HDCError):
@@ -147,9 +157,10 @@ def test_search_plain_vs_oracle(hdc, orc, cuda, dim, nq, nr, k, mode, vmax):
     g = np.random.default_rng(dim + nq + nr + k)
     r = g.integers(-vmax, vmax + 1, (nr, dim)).astype(np.int16)
     q = g.integers(-vmax, vmax + 1, (nq, dim)).astype(np.int16)
-    r[5] = r[3]                      # duplicates: ties to the lower index
+    if nr > 5:
+        r[5] = r[3]                  # duplicates: ties to the lower index
     r[min(7, nr - 1)] = 0            # zero norm: score -1
-    q[1] = r[3]                      # exact matches
+    q[1] = r[min(3, nr - 1)]         # exact matches
     q[2] = 0
     ctx = hdc.Context(dim, 8, 150, 10)
     s, i, c, d = _search(hdc, ctx, q, r, k, mode, cuda)
@@ -208,7 +219,7 @@ def test_self_retrieval_full_size(hdc, cuda):
     import torch
     g = torch.Generator(device=cuda).manual_seed(11)
     nr, dim = 50000, 8192
-    r = torch.randint(-1500, 1501, (nr, dim), dtype=torch.int16, device=cuda, generator=g)
+    r = torch.randint(-1000, 1001, (nr, dim), dtype=torch.int16, device=cuda, generator=g)
     ctx = hdc.Context(dim, 8, 150, 10)
     mr = torch.zeros(1, dtype=torch.int32, device=cuda)
     rn = ctx.norms(r, mr)
