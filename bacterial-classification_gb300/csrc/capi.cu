@@ -78,7 +78,11 @@ int hdc_context_create(int dim, int kmer, int window, int step, hdc_context** ou
         if (excess > 0) w[c->words64 - 1] &= (~uint64_t(0)) >> excess;
     }
     e = cudaMalloc(&c->d_base32, sizeof(uint64_t) * 4 * (size_t)c->words64);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, sizeof(int));
     if (e != cudaSuccess) {
+        cudaFree(c->d_base32);
+        cudaFree(c->d_status);
         delete[] c->host_base;
         delete c;
         return hdc::cuda_fail(e, "context: cudaMalloc");
@@ -98,6 +102,7 @@ int hdc_context_create(int dim, int kmer, int window, int step, hdc_context** ou
 void hdc_context_destroy(hdc_context* ctx) {
     if (!ctx) return;
     cudaFree(ctx->d_base32);
+    cudaFree(ctx->d_status);
     delete[] ctx->host_base;
     delete ctx;
 }
@@ -115,7 +120,7 @@ int hdc_encode_segments(hdc_context* ctx, const char* d_bytes, const int64_t* d_
     if (n_segs < 0) return fail(HDC_ERR_INVALID, "encode: negative segment count");
     if (n_segs == 0) return HDC_OK;
     if (!d_bytes || !d_seg_off || !d_seg_len || !d_out) return fail(HDC_ERR_INVALID, "encode: null pointer");
-    if (out_kind < HDC_OUT_I16 || out_kind > HDC_OUT_BIPOLAR_I16) return fail(HDC_ERR_INVALID, "encode: bad out_kind");
+    if (out_kind < HDC_OUT_I16 || out_kind > HDC_OUT_BIPOLAR_F16) return fail(HDC_ERR_INVALID, "encode: bad out_kind");
     if (out_stride < ctx->dim) return fail(HDC_ERR_INVALID, "encode: out_stride < dim");
     if (max_len < 0) return fail(HDC_ERR_INVALID, "encode: negative max_len");
     return hdc::launch_encode(ctx, d_bytes, d_seg_off, d_seg_len, nullptr, nullptr, 0, n_segs, out_kind, d_out,
@@ -164,6 +169,46 @@ int hdc_search_plain(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qnor
     return hdc::launch_search_plain(ctx, d_q, d_qnorm2, nq, max_abs_q, d_r, d_rnorm2, nr, max_abs_r, k, score_mode,
                                     d_score, d_idx, d_cos, d_dot, d_work, work_bytes,
                                     static_cast<cudaStream_t>(stream));
+}
+
+int hdc_context_status(hdc_context* ctx, int* status) {
+    if (!ctx || !status) return fail(HDC_ERR_INVALID, "status: null argument");
+    cudaError_t e = cudaMemcpy(status, ctx->d_status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemset(ctx->d_status, 0, sizeof(int));
+    if (e != cudaSuccess) return hdc::cuda_fail(e, "status: read");
+    return HDC_OK;
+}
+
+int hdc_refdb_create(hdc_context* ctx, const void* d_ref, int elem_bytes, int64_t nr, int32_t max_abs,
+                     hdc_refdb** out, void* stream) {
+    if (!ctx || !out) return fail(HDC_ERR_INVALID, "refdb: null argument");
+    *out = nullptr;
+    if (elem_bytes != 2 && elem_bytes != 4) return fail(HDC_ERR_INVALID, "refdb: elem_bytes must be 2 or 4");
+    if (nr < 1 || !d_ref) return fail(HDC_ERR_INVALID, "refdb: empty reference set");
+    if (max_abs < 0) return fail(HDC_ERR_INVALID, "refdb: negative max_abs");
+    return hdc::refdb_create(ctx, d_ref, elem_bytes, nr, max_abs, out, static_cast<cudaStream_t>(stream));
+}
+
+void hdc_refdb_destroy(hdc_refdb* db) { hdc::refdb_destroy(db); }
+
+int hdc_refdb_limbs(const hdc_refdb* db) { return db ? db->L : 0; }
+
+size_t hdc_search_tc_workspace_bytes(const hdc_context* ctx, const hdc_refdb* db, int64_t nq, int k) {
+    if (!ctx || !db || nq <= 0 || k <= 0) return 0;
+    return hdc::tc_workspace_bytes(ctx, nq, db, k);
+}
+
+int hdc_search_tc(hdc_context* ctx, const hdc_refdb* db, const void* d_q, const int64_t* d_qnorm2, int64_t nq,
+                  int32_t max_abs_q, int k, int score_mode, float* d_score, int32_t* d_idx, double* d_cos,
+                  int64_t* d_dot, void* d_work, size_t work_bytes, void* stream) {
+    if (!ctx || !db) return fail(HDC_ERR_INVALID, "tc search: null context or database");
+    if (nq < 0) return fail(HDC_ERR_INVALID, "tc search: negative count");
+    if (nq == 0) return HDC_OK;
+    if (!hdc::valid_score_mode(score_mode)) return fail(HDC_ERR_INVALID, "tc search: bad score mode");
+    if (!d_q || !d_qnorm2 || !d_score || !d_idx) return fail(HDC_ERR_INVALID, "tc search: null pointer");
+    return hdc::launch_search_tc(ctx, db, static_cast<const __half*>(d_q), d_qnorm2, nq, max_abs_q, k, score_mode,
+                                 d_score, d_idx, d_cos, d_dot, d_work, work_bytes, ctx->d_status,
+                                 static_cast<cudaStream_t>(stream));
 }
 
 int hdc_bundle(hdc_context* ctx, const void* d_rows, int elem_bytes, const int64_t* d_child_ptr,

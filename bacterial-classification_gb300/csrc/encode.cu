@@ -277,6 +277,8 @@ __global__ void __launch_bounds__(kThreads) encode_kernel(const EncodeArgs a) {
                         h2[t] = (uint32_t)v & 0xffffu;
                     else if (a.out_kind == HDC_OUT_BIPOLAR_I16)
                         h2[t] = v >= 0 ? 0x0001u : 0xffffu;
+                    else if (a.out_kind == HDC_OUT_BIPOLAR_F16)
+                        h2[t] = v >= 0 ? 0x3c00u : 0xbc00u;  // fp16 +1 / -1
                     else
                         h2[t] = v >= 0 ? 0x3f80u : 0xbf80u;  // bf16 +1 / -1
                 }

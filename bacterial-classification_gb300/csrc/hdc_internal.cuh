@@ -1,6 +1,8 @@
 // Internal definitions shared by the translation units of libhdc_gb300.
 #pragma once
 
+#include <cuda.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -19,6 +21,19 @@ struct hdc_context {
     int num_sms = 0;
     uint64_t* host_base = nullptr;  // [4][words64], A,C,G,T
     uint32_t* d_base32 = nullptr;   // [4][words32] on the device
+    int* d_status = nullptr;        // device status word written by kernels that can give up
+};
+
+// A tensor-core reference database (hdc_refdb_create).
+struct hdc_refdb {
+    int64_t nr = 0, r_pad = 0;
+    int dim = 0, L = 0;
+    __half* d_limbs = nullptr;  // [L][r_pad][dim]
+    int64_t* d_norm2 = nullptr; // [nr]
+    float* d_rsq = nullptr;     // [nr]
+    int32_t limb_max[4] = {0, 0, 0, 0};
+    int32_t max_abs = 0;
+    CUtensorMap tmB;  // TMA descriptor of the limbs, [L*r_pad][dim] fp16
 };
 
 namespace hdc {
@@ -50,6 +65,14 @@ int launch_search_plain(hdc_context* ctx, const int16_t* d_q, const int64_t* d_q
 int launch_merge(const uint64_t* ws_key, const int64_t* ws_dot, int n_lists, int64_t nq, int k, const int64_t* d_qn,
                  const int64_t* d_rn, float* d_score, int32_t* d_idx, double* d_cos, int64_t* d_dot,
                  cudaStream_t stream);
+
+int refdb_create(hdc_context* ctx, const void* d_ref, int elem_bytes, int64_t nr, int32_t max_abs, hdc_refdb** out,
+                 cudaStream_t stream);
+void refdb_destroy(hdc_refdb* db);
+size_t tc_workspace_bytes(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int k);
+int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, const int64_t* d_qn, int64_t nq,
+                     int32_t maxq, int k, int mode, float* d_score, int32_t* d_idx, double* d_cos, int64_t* d_dot,
+                     void* d_work, size_t work_bytes, int* d_status, cudaStream_t stream);
 
 int launch_bundle(hdc_context* ctx, const void* d_rows, int elem_bytes, const int64_t* d_child_ptr,
                   const int32_t* d_child_idx, int64_t n_parents, int32_t* d_out, cudaStream_t stream);

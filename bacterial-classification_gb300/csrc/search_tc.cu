@@ -1,0 +1,519 @@
+// (b) precision form of the cosine search: a dense Q x R^T contraction on the
+// sm_103a tensor cores (tcgen05.mma kind::f16, fp32 accumulators in TMEM,
+// operands staged by TMA), exact in every dot product.
+//
+// Exactness.  fp16 holds every integer of magnitude <= 2048 exactly, and an
+// fp32 accumulator holds every integer of magnitude <= 2^24 exactly, so
+//   * queries are +1/-1 (the bipolar read hypervectors) or small integers,
+//   * every reference count v is split into balanced base-2048 limbs
+//     v = sum_l 2048^l * limb_l with limb_l in [-1024, 1023] (the top limb in
+//     [-2048, 2048]), each an exact fp16,
+//   * each limb gets its own accumulator, and the host checks
+//     dim * max|q| * max|limb_l| <= 2^24 so that no partial sum can round;
+//   * the epilogue recombines dot = sum_l 2048^l * acc_l in int64.
+// GB300's dense fp16/bf16 tensor rate is far above its INT8 rate, so integer
+// limbs on fp16 tensor cores are the fast exact path here.
+//
+// Kernel shape (one CTA per SM, persistent): M = 128 queries x N = 128
+// references per tile, K in blocks of 64 dims (one 128-byte swizzled row per
+// operand row), a multi-stage TMA ring, one MMA-issuing thread, and four
+// epilogue warps that read the accumulators with tcgen05.ld.  Each epilogue
+// thread owns one query (one TMEM lane) and keeps that query's running top-k
+// in registers/local memory: an fp32 estimate of every score filters
+// candidates, and only those near the current k-th best get the exact FP64
+// score of the reference CPU cosine (src/HV.cpp:219-242).  Work units are
+// (reference chunk, query tile) pairs handed out chunk-major, so the CTAs
+// running at the same time stream the same references through L2.
+#include <cuda.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "hdc_internal.cuh"
+#include "tc_ptx.cuh"
+#include "topk.cuh"
+
+namespace hdc {
+namespace {
+
+constexpr int kBM = 128;  // queries per tile (TMEM lanes)
+constexpr int kBN = 128;  // references per tile
+constexpr int kBK = 64;   // dims per K block (128 bytes of fp16)
+constexpr int kTileBytes = kBM * kBK * 2;  // 16 KB, same for A and each B limb
+constexpr int kThreadsTC = 192;            // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+constexpr int kMaxLimbs = 4;
+constexpr int kMaxKTC = 32;
+
+__host__ __device__ constexpr int tc_stages(int L) { return std::min(8, 196608 / (kTileBytes * (1 + L))); }
+__host__ __device__ constexpr int tc_acc_bufs(int L) { return L <= 2 ? 2 : 1; }
+__host__ __device__ constexpr int tc_tmem_cols(int L) {
+    return tc_acc_bufs(L) * L * kBN <= 256 ? 256 : 512;
+}
+
+struct TcArgs {
+    int64_t nq, nr;
+    int dim, k, mode, n_kblocks;
+    int64_t r_pad;        // rows per limb in the B tensor
+    int n_qtiles, n_rtiles, tiles_per_unit, n_chunks;
+    int64_t n_units;
+    const int64_t* qn;    // [nq] squared norms of the queries
+    const int64_t* rn;    // [nr] squared norms of the references
+    const float* rr;      // [nr] fp32 1/sqrt(norm)
+    uint64_t* ws_key;     // [n_chunks][nq][k]
+    int64_t* ws_dot;
+    int* status;          // device status word (0 = ok)
+};
+
+__device__ __forceinline__ float approx_tc(float af, float rq, float rr, int mode) {
+    if (mode == HDC_SCORE_DOT) return af;
+    const float c = af * rq * rr;
+    return mode == HDC_SCORE_NORM ? fmaf(2.0f, c, -1.0f) : c;
+}
+
+template <int L>
+__global__ void __launch_bounds__(kThreadsTC, 1)
+    tc_search_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcArgs a) {
+    constexpr int STAGES = tc_stages(L);
+    constexpr int ACC = tc_acc_bufs(L);
+    constexpr int TCOLS = tc_tmem_cols(L);
+    constexpr uint32_t kStageBytes = (uint32_t)kTileBytes * (1 + L);
+    constexpr uint32_t IDESC = tc::idesc_f16_f32(kBM, kBN);
+
+    extern __shared__ uint8_t smem_raw[];
+    // 1024-byte aligned tile ring (required by the 128-byte swizzle atoms)
+    const uint32_t raw_addr = tc::smem_u32(smem_raw);
+    uint8_t* ring = smem_raw + ((1024 - (raw_addr & 1023)) & 1023);
+    __shared__ uint64_t full_bar[STAGES], empty_bar[STAGES], accf_bar[ACC], acce_bar[ACC];
+    __shared__ uint32_t tmem_base_s;
+    __shared__ volatile int err_s;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        err_s = 0;
+        for (int s = 0; s < STAGES; ++s) {
+            tc::mbar_init(&full_bar[s], 1);
+            tc::mbar_init(&empty_bar[s], 1);
+        }
+        for (int b = 0; b < ACC; ++b) {
+            tc::mbar_init(&accf_bar[b], 1);
+            tc::mbar_init(&acce_bar[b], 128);
+        }
+        tc::fence_mbar_init();
+        tc::prefetch_tmap(&tmA);
+        tc::prefetch_tmap(&tmB);
+    }
+    if (warp == 1) {
+        tc::tmem_alloc(&tmem_base_s, TCOLS);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = tmem_base_s;
+
+    if (warp == 0) {
+        // ------------------------------------------------ TMA producer
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            int64_t issued = 0;
+            bool ok = true;
+            for (int64_t u = blockIdx.x; ok && u < a.n_units; u += gridDim.x) {
+                const int chunk = (int)(u / a.n_qtiles), qt = (int)(u % a.n_qtiles);
+                const int t0 = chunk * a.tiles_per_unit, t1 = min(a.n_rtiles, t0 + a.tiles_per_unit);
+                for (int t = t0; ok && t < t1; ++t) {
+                    for (int kb = 0; kb < a.n_kblocks; ++kb) {
+                        if (!tc::mbar_wait(&empty_bar[stage], phase ^ 1, &err_s, 1)) {
+                            ok = false;
+                            break;
+                        }
+                        uint8_t* st = ring + (size_t)stage * kStageBytes;
+                        tc::mbar_arrive_expect_tx(&full_bar[stage], kStageBytes);
+                        tc::tma_load_2d(st, &tmA, &full_bar[stage], kb * kBK, qt * kBM);
+#pragma unroll
+                        for (int l = 0; l < L; ++l)
+                            tc::tma_load_2d(st + (size_t)kTileBytes * (1 + l), &tmB, &full_bar[stage], kb * kBK,
+                                            (int)(l * a.r_pad + (int64_t)t * kBN));
+                        ++issued;
+                        if (++stage == STAGES) {
+                            stage = 0;
+                            phase ^= 1;
+                        }
+                    }
+                }
+            }
+            // before leaving, let the last loads land (bounded)
+            int s = stage;
+            uint32_t ph = phase;
+            for (int64_t i = 0; i < (issued < STAGES ? issued : (int64_t)STAGES); ++i) {
+                if (--s < 0) {
+                    s = STAGES - 1;
+                    ph ^= 1;
+                }
+                const long long c0 = clock64();
+                while (!tc::mbar_try_wait(tc::smem_u32(&full_bar[s]), ph) && clock64() - c0 < tc::kWaitCycles) {
+                }
+            }
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            int stage = 0, acc = 0;
+            uint32_t phase = 0, acc_phase = 0;
+            bool ok = true;
+            for (int64_t u = blockIdx.x; ok && u < a.n_units; u += gridDim.x) {
+                const int chunk = (int)(u / a.n_qtiles);
+                const int t0 = chunk * a.tiles_per_unit, t1 = min(a.n_rtiles, t0 + a.tiles_per_unit);
+                for (int t = t0; ok && t < t1; ++t) {
+                    if (!tc::mbar_wait(&acce_bar[acc], acc_phase ^ 1, &err_s, 2)) {
+                        ok = false;
+                        break;
+                    }
+                    tc::fence_after();
+                    const uint32_t d0 = tmem + (uint32_t)(acc * L * kBN);
+                    for (int kb = 0; kb < a.n_kblocks; ++kb) {
+                        if (!tc::mbar_wait(&full_bar[stage], phase, &err_s, 3)) {
+                            ok = false;
+                            break;
+                        }
+                        tc::fence_after();
+                        const uint32_t sa = tc::smem_u32(ring + (size_t)stage * kStageBytes);
+                        const uint64_t adesc = tc::sw128_kmajor_desc(sa);
+#pragma unroll
+                        for (int l = 0; l < L; ++l) {
+                            const uint64_t bdesc = tc::sw128_kmajor_desc(sa + (uint32_t)kTileBytes * (1 + l));
+#pragma unroll
+                            for (int kk = 0; kk < kBK / 16; ++kk)  // K = 16 fp16 per MMA = 32 bytes
+                                tc::mma_f16(d0 + l * kBN, adesc + 2 * kk, bdesc + 2 * kk, IDESC,
+                                            (kb | kk) != 0 ? 1u : 0u);
+                        }
+                        tc::mma_commit(&empty_bar[stage]);  // frees the stage when these MMAs finish
+                        if (++stage == STAGES) {
+                            stage = 0;
+                            phase ^= 1;
+                        }
+                    }
+                    if (!ok) break;
+                    tc::mma_commit(&accf_bar[acc]);  // accumulators of this tile are complete
+                    if (++acc == ACC) {
+                        acc = 0;
+                        acc_phase ^= 1;
+                    }
+                }
+            }
+        }
+    } else {
+        // ------------------------------------------------ epilogue: warps 2..5
+        const int quarter = warp & 3;  // TMEM lane quarter this warp may access
+        const int row = quarter * 32 + lane;
+        const uint32_t lane_addr = (uint32_t)(quarter * 32) << 16;
+        const int k = a.k;
+        int acc = 0;
+        uint32_t acc_phase = 0;
+        bool ok = true;
+        uint64_t keys[kMaxKTC];
+        int64_t dots[kMaxKTC];
+        for (int64_t u = blockIdx.x; ok && u < a.n_units; u += gridDim.x) {
+            const int chunk = (int)(u / a.n_qtiles), qt = (int)(u % a.n_qtiles);
+            const int t0 = chunk * a.tiles_per_unit, t1 = min(a.n_rtiles, t0 + a.tiles_per_unit);
+            const int64_t gq = (int64_t)qt * kBM + row;
+            const bool live = gq < a.nq;
+            const int64_t my_qn = live ? a.qn[gq] : 0;
+            const float my_rq = rsqrt_norm(my_qn);
+            for (int i = 0; i < k; ++i) {
+                keys[i] = 0;
+                dots[i] = 0;
+            }
+            float thr = -INFINITY;
+            for (int t = t0; t < t1; ++t) {
+                if (!tc::mbar_wait(&accf_bar[acc], acc_phase, &err_s, 4)) {
+                    ok = false;
+                    break;
+                }
+                tc::fence_after();
+                const uint32_t d0 = tmem + lane_addr + (uint32_t)(acc * L * kBN);
+                for (int c0 = 0; c0 < kBN; c0 += 32) {
+                    uint32_t v[L][32];
+#pragma unroll
+                    for (int l = 0; l < L; ++l) tc::tmem_ld32(d0 + l * kBN + c0, v[l]);
+                    tc::tmem_ld_wait();
+                    const int64_t rbase = (int64_t)t * kBN + c0;
+                    const float rr_lane = (rbase + lane < a.nr) ? __ldg(a.rr + rbase + lane) : 0.0f;
+#pragma unroll
+                    for (int c = 0; c < 32; ++c) {
+                        const float rrc = __shfl_sync(0xffffffffu, rr_lane, c);
+                        float af = __uint_as_float(v[0][c]);
+                        float scale = 1.0f;
+#pragma unroll
+                        for (int l = 1; l < L; ++l) {
+                            scale *= 2048.0f;
+                            af = fmaf(__uint_as_float(v[l][c]), scale, af);
+                        }
+                        const float ap = approx_tc(af, my_rq, rrc, a.mode);
+                        if (!(ap >= thr) || !live || rbase + c >= a.nr) continue;
+                        int64_t dot = 0;
+#pragma unroll
+                        for (int l = 0; l < L; ++l)
+                            dot += (int64_t)__float2ll_rn(__uint_as_float(v[l][c])) * ((int64_t)1 << (11 * l));
+                        const int64_t gr = rbase + c;
+                        const float s = exact_score(dot, my_qn, __ldg(a.rn + gr), a.mode);
+                        const uint64_t key = make_key(s, (uint32_t)gr);
+                        if (key <= keys[k - 1]) continue;
+                        list_insert(keys, dots, k, key, dot);
+                        if (keys[k - 1] != 0) {
+                            const float sk = key_score(keys[k - 1]);
+                            thr = a.mode == HDC_SCORE_DOT ? sk - (fabsf(sk) * 4e-6f + 1.0f) : sk - kFilterMargin;
+                        }
+                    }
+                }
+                tc::fence_before();
+                tc::mbar_arrive(&acce_bar[acc]);
+                if (++acc == ACC) {
+                    acc = 0;
+                    acc_phase ^= 1;
+                }
+            }
+            if (!ok) break;
+            if (live) {
+                uint64_t* ok_ = a.ws_key + ((int64_t)chunk * a.nq + gq) * k;
+                int64_t* od = a.ws_dot + ((int64_t)chunk * a.nq + gq) * k;
+                for (int i = 0; i < k; ++i) {
+                    ok_[i] = keys[i];
+                    od[i] = dots[i];
+                }
+            }
+        }
+    }
+
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc::fence_after();
+        tc::tmem_dealloc(tmem, TCOLS);
+    }
+    if (threadIdx.x == 0 && err_s) atomicCAS(a.status, 0, 100 + err_s);
+}
+
+// ---------------------------------------------------------------- database build
+// limbs[l][r][d] (fp16) of ref[r][d]; rows r >= nr of each limb are zero.
+template <typename T>
+__global__ void limbs_kernel(const T* __restrict__ ref, int64_t nr, int dim, int L, int64_t r_pad,
+                             __half* __restrict__ limbs, int32_t* __restrict__ limb_max) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t total = r_pad * dim;
+    int32_t mx[kMaxLimbs] = {0, 0, 0, 0};
+    if (i < total) {
+        const int64_t r = i / dim;
+        int64_t v = r < nr ? (int64_t)ref[i] : 0;
+        for (int l = 0; l < L; ++l) {
+            int64_t digit;
+            if (l == L - 1) {
+                digit = v;
+            } else {
+                digit = ((v + 1024) & 2047) - 1024;
+                v = (v - digit) / 2048;
+            }
+            limbs[(int64_t)l * total + i] = __int2half_rn((int)digit);
+            mx[l] = (int32_t)(digit < 0 ? -digit : digit);
+        }
+    }
+    for (int l = 0; l < L; ++l) {
+        int32_t m = mx[l];
+        for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if ((threadIdx.x & 31) == 0 && m) atomicMax(limb_max + l, m);
+    }
+}
+
+__global__ void rsqrt_kernel(const int64_t* __restrict__ n2, int64_t n, float* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = rsqrt_norm(n2[i]);
+}
+
+// cuTensorMapEncodeTiled resolved through the runtime, so the library does not
+// link libcuda (it must load on hosts without a driver).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled_fn() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+bool make_tmap(CUtensorMap* map, const void* base, int64_t rows, int dim) {
+    EncodeTiledFn encode = encode_tiled_fn();
+    if (!encode) return false;
+    cuuint64_t gdim[2] = {(cuuint64_t)dim, (cuuint64_t)rows};
+    cuuint64_t gstride[1] = {(cuuint64_t)dim * 2};
+    cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)kBM};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base), gdim,
+                                        gstride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+int refdb_create(hdc_context* ctx, const void* d_ref, int elem_bytes, int64_t nr, int32_t max_abs,
+                 hdc_refdb** out, cudaStream_t stream) {
+    *out = nullptr;
+    const int dim = ctx->dim;
+    if (dim % 8 != 0) return fail(HDC_ERR_INVALID, "refdb: dim must be a multiple of 8 (TMA row stride)");
+    if (nr < 1) return fail(HDC_ERR_INVALID, "refdb: empty reference set");
+    // limbs needed for |v| <= max_abs: L-1 balanced digits of 11 bits, then a top digit within 2048
+    int L = 1;
+    int64_t cover = 2048;
+    while ((int64_t)max_abs > cover) {
+        ++L;
+        cover = cover * 2048 + 1023;
+        if (L > kMaxLimbs) return fail(HDC_ERR_RANGE, "refdb: values need more than 4 limbs");
+    }
+    auto* db = new hdc_refdb();
+    db->nr = nr;
+    db->dim = dim;
+    db->L = L;
+    db->max_abs = max_abs;
+    db->r_pad = (nr + kBN - 1) / kBN * kBN;
+    const size_t nl = (size_t)L * db->r_pad * dim;
+    cudaError_t e = cudaMalloc(&db->d_limbs, nl * sizeof(__half));
+    if (e == cudaSuccess) e = cudaMalloc(&db->d_norm2, nr * sizeof(int64_t));
+    if (e == cudaSuccess) e = cudaMalloc(&db->d_rsq, nr * sizeof(float));
+    int32_t* d_lmax = nullptr;
+    if (e == cudaSuccess) e = cudaMalloc(&d_lmax, sizeof(int32_t) * kMaxLimbs);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_lmax, 0, sizeof(int32_t) * kMaxLimbs, stream);
+    if (e != cudaSuccess) {
+        cudaFree(db->d_limbs);
+        cudaFree(db->d_norm2);
+        cudaFree(db->d_rsq);
+        cudaFree(d_lmax);
+        delete db;
+        return cuda_fail(e, "refdb: allocation");
+    }
+    const int64_t total = db->r_pad * dim;
+    const unsigned grid = (unsigned)((total + 255) / 256);
+    if (elem_bytes == 2)
+        limbs_kernel<int16_t><<<grid, 256, 0, stream>>>(static_cast<const int16_t*>(d_ref), nr, dim, L, db->r_pad,
+                                                        db->d_limbs, d_lmax);
+    else
+        limbs_kernel<int32_t><<<grid, 256, 0, stream>>>(static_cast<const int32_t*>(d_ref), nr, dim, L, db->r_pad,
+                                                        db->d_limbs, d_lmax);
+    int st = launch_norms(ctx, d_ref, elem_bytes, nr, db->d_norm2, nullptr, stream);
+    if (st == HDC_OK) {
+        rsqrt_kernel<<<(unsigned)((nr + 255) / 256), 256, 0, stream>>>(db->d_norm2, nr, db->d_rsq);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(db->limb_max, d_lmax, sizeof(int32_t) * kMaxLimbs,
+                                                  cudaMemcpyDeviceToHost, stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+        if (e != cudaSuccess) st = cuda_fail(e, "refdb: build");
+    }
+    cudaFree(d_lmax);
+    if (st == HDC_OK && !make_tmap(&db->tmB, db->d_limbs, (int64_t)L * db->r_pad, dim))
+        st = fail(HDC_ERR_CUDA, "refdb: cuTensorMapEncodeTiled failed");
+    if (st != HDC_OK) {
+        cudaFree(db->d_limbs);
+        cudaFree(db->d_norm2);
+        cudaFree(db->d_rsq);
+        delete db;
+        return st;
+    }
+    *out = db;
+    return HDC_OK;
+}
+
+void refdb_destroy(hdc_refdb* db) {
+    if (!db) return;
+    cudaFree(db->d_limbs);
+    cudaFree(db->d_norm2);
+    cudaFree(db->d_rsq);
+    delete db;
+}
+
+static void tc_plan(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int& n_qtiles, int& n_rtiles,
+                    int& tiles_per_unit, int& n_chunks) {
+    n_qtiles = (int)((nq + kBM - 1) / kBM);
+    n_rtiles = (int)(db->r_pad / kBN);
+    // enough units for ~4 per SM, whole reference chunks streamed chunk-major
+    const int64_t pairs = (int64_t)n_qtiles * n_rtiles;
+    int64_t tpu = std::max<int64_t>(1, pairs / (4 * (int64_t)ctx->num_sms));
+    tpu = std::min<int64_t>(tpu, n_rtiles);
+    tiles_per_unit = (int)tpu;
+    n_chunks = (n_rtiles + tiles_per_unit - 1) / tiles_per_unit;
+}
+
+size_t tc_workspace_bytes(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int k) {
+    int qt, rt, tpu, nc;
+    tc_plan(ctx, nq, db, qt, rt, tpu, nc);
+    k = (int)std::min<int64_t>(k, db->nr);
+    return (size_t)nc * nq * std::max(k, 1) * (sizeof(uint64_t) + sizeof(int64_t));
+}
+
+template <int L>
+static int launch_tc_t(const CUtensorMap& tmA, const hdc_refdb* db, const TcArgs& a, int grid, cudaStream_t stream) {
+    const size_t smem = (size_t)tc_stages(L) * kTileBytes * (1 + L) + 1024;
+    auto kern = tc_search_kernel<L>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_fail(e, "tc search: cudaFuncSetAttribute");
+    kern<<<grid, kThreadsTC, smem, stream>>>(tmA, db->tmB, a);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? HDC_OK : cuda_fail(e, "tc search: launch");
+}
+
+int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, const int64_t* d_qn, int64_t nq,
+                     int32_t maxq, int k, int mode, float* d_score, int32_t* d_idx, double* d_cos, int64_t* d_dot,
+                     void* d_work, size_t work_bytes, int* d_status, cudaStream_t stream) {
+    if (nq == 0) return HDC_OK;
+    if (db->dim != ctx->dim) return fail(HDC_ERR_INVALID, "tc search: database and context dims differ");
+    if (k > db->nr) k = (int)db->nr;
+    if (k < 1 || k > kMaxKTC) return fail(HDC_ERR_INVALID, "tc search: k must be in 1..32");
+    if (maxq < 0 || maxq > 2048) return fail(HDC_ERR_RANGE, "tc search: queries must be integers with |q| <= 2048");
+    for (int l = 0; l < db->L; ++l) {
+        const double bound = (double)ctx->dim * std::max(maxq, 1) * std::max(db->limb_max[l], 1);
+        if (bound > 16777216.0)
+            return fail(HDC_ERR_RANGE, "tc search: dim * max|q| * max|limb| exceeds 2^24 (fp32 accumulators inexact)");
+    }
+    if ((reinterpret_cast<uintptr_t>(d_q) & 15) != 0) return fail(HDC_ERR_INVALID, "tc search: queries not 16B aligned");
+    CUtensorMap tmA;
+    if (!make_tmap(&tmA, d_q, nq, ctx->dim)) return fail(HDC_ERR_CUDA, "tc search: cuTensorMapEncodeTiled failed");
+    TcArgs a{};
+    a.nq = nq;
+    a.nr = db->nr;
+    a.dim = ctx->dim;
+    a.k = k;
+    a.mode = mode;
+    a.n_kblocks = (ctx->dim + kBK - 1) / kBK;
+    a.r_pad = db->r_pad;
+    tc_plan(ctx, nq, db, a.n_qtiles, a.n_rtiles, a.tiles_per_unit, a.n_chunks);
+    a.n_units = (int64_t)a.n_qtiles * a.n_chunks;
+    a.qn = d_qn;
+    a.rn = db->d_norm2;
+    a.rr = db->d_rsq;
+    const size_t need = (size_t)a.n_chunks * nq * k * (sizeof(uint64_t) + sizeof(int64_t));
+    if (!d_work || work_bytes < need) return fail(HDC_ERR_INVALID, "tc search: workspace too small");
+    a.ws_key = static_cast<uint64_t*>(d_work);
+    a.ws_dot = reinterpret_cast<int64_t*>(a.ws_key + (size_t)a.n_chunks * nq * k);
+    a.status = d_status;
+    const int grid = (int)std::min<int64_t>(a.n_units, ctx->num_sms);
+    int st;
+    switch (db->L) {
+        case 1: st = launch_tc_t<1>(tmA, db, a, grid, stream); break;
+        case 2: st = launch_tc_t<2>(tmA, db, a, grid, stream); break;
+        case 3: st = launch_tc_t<3>(tmA, db, a, grid, stream); break;
+        default: st = launch_tc_t<4>(tmA, db, a, grid, stream); break;
+    }
+    if (st != HDC_OK) return st;
+    return launch_merge(a.ws_key, a.ws_dot, a.n_chunks, nq, k, d_qn, db->d_norm2, d_score, d_idx, d_cos, d_dot,
+                        stream);
+}
+
+}  // namespace hdc

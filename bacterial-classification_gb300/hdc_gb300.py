@@ -15,7 +15,7 @@ HDC_OK = 0
 ERR = {1: "HDC_ERR_INVALID", 2: "HDC_ERR_RANGE", 3: "HDC_ERR_CUDA", 4: "HDC_ERR_NOMEM",
        5: "HDC_ERR_UNSUPPORTED", 6: "HDC_ERR_TIMEOUT"}
 SCORE_NORM, SCORE_COS, SCORE_DOT = 0, 1, 2
-OUT_I16, OUT_I32, OUT_BIPOLAR_BF16, OUT_BIPOLAR_I16 = 0, 1, 2, 3
+OUT_I16, OUT_I32, OUT_BIPOLAR_BF16, OUT_BIPOLAR_I16, OUT_BIPOLAR_F16 = 0, 1, 2, 3, 4
 
 # (name, restype, argtypes) of every exported entry point
 P, I32, I64, SZ = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_size_t
@@ -33,6 +33,12 @@ SIGNATURES = [
     ("hdc_search_plain", I32, [P, P, P, I64, ctypes.c_int32, P, P, I64, ctypes.c_int32, I32, I32, P, P, P, P, P,
                                SZ, P]),
     ("hdc_bundle", I32, [P, P, I32, P, P, I64, P, P]),
+    ("hdc_context_status", I32, [P, ctypes.POINTER(ctypes.c_int)]),
+    ("hdc_refdb_create", I32, [P, P, I32, I64, ctypes.c_int32, ctypes.POINTER(P), P]),
+    ("hdc_refdb_destroy", None, [P]),
+    ("hdc_refdb_limbs", I32, [P]),
+    ("hdc_search_tc_workspace_bytes", SZ, [P, P, I64, I32]),
+    ("hdc_search_tc", I32, [P, P, P, P, I64, ctypes.c_int32, I32, I32, P, P, P, P, P, SZ, P]),
     ("hdc_synth_tree", I32, [ctypes.c_uint64, I64, I32, P, I32, I32, I32, P, I64, P, P, P, I32]),
     ("hdc_synth_copies", I32, [ctypes.c_uint64, P, P, P, I64, I32, ctypes.c_double, P, I64, P, P, I32]),
     ("hdc_synth_reads", I32, [ctypes.c_uint64, P, P, P, I64, I64, I32, ctypes.c_double, I32, I32, ctypes.c_double,
@@ -148,6 +154,32 @@ class Context:
                                      ptr(s), ptr(i), ptr(c), ptr(d), ptr(work), work.numel(), stream_ptr(stream)))
         return out
 
+    def status(self):
+        st = ctypes.c_int(0)
+        check(lib().hdc_context_status(self.h, ctypes.byref(st)))
+        return st.value
+
+    def refdb(self, refs, max_abs, stream=None):
+        return RefDB(self, refs, max_abs, stream)
+
+    def search_tc(self, db, q, qn, maxq, k, mode=SCORE_NORM, work=None, out=None, stream=None):
+        import torch
+        nq = q.shape[0]
+        kk = min(k, db.nr)
+        dev = q.device
+        if out is None:
+            out = (torch.empty((nq, kk), dtype=torch.float32, device=dev),
+                   torch.empty((nq, kk), dtype=torch.int32, device=dev),
+                   torch.empty((nq, kk), dtype=torch.float64, device=dev),
+                   torch.empty((nq, kk), dtype=torch.int64, device=dev))
+        wb = lib().hdc_search_tc_workspace_bytes(self.h, db.h, nq, k)
+        if work is None or work.numel() < wb:
+            work = torch.empty(max(wb, 16), dtype=torch.uint8, device=dev)
+        s, i, c, d = out
+        check(lib().hdc_search_tc(self.h, db.h, ptr(q), ptr(qn), nq, int(maxq), k, mode, ptr(s), ptr(i), ptr(c),
+                                  ptr(d), ptr(work), work.numel(), stream_ptr(stream)))
+        return out
+
     # ---------------------------------------------------------------- propagate
     def bundle(self, rows, child_ptr, child_idx, out=None, stream=None):
         import torch
@@ -157,6 +189,28 @@ class Context:
         check(lib().hdc_bundle(self.h, ptr(rows), rows.element_size(), ptr(child_ptr), ptr(child_idx), npar,
                                ptr(out), stream_ptr(stream)))
         return out
+
+
+class RefDB:
+    """Tensor-core reference database (fp16 limbs + exact norms) built from int16/int32 rows."""
+
+    def __init__(self, ctx, refs, max_abs, stream=None):
+        h = ctypes.c_void_p()
+        check(lib().hdc_refdb_create(ctx.h, ptr(refs), refs.element_size(), refs.shape[0], int(max_abs),
+                                     ctypes.byref(h), stream_ptr(stream)))
+        self.h, self.nr = h, refs.shape[0]
+        self.limbs = lib().hdc_refdb_limbs(h)
+
+    def close(self):
+        if self.h:
+            lib().hdc_refdb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def pack_sequences(seqs):

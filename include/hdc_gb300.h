@@ -53,6 +53,7 @@ extern "C" {
 #define HDC_OUT_I32 1          /* int32 bundle, exact (segments of <= 65535 k-mers) */
 #define HDC_OUT_BIPOLAR_BF16 2 /* bf16 +1/-1 sign of the bundle, 0 -> +1 */
 #define HDC_OUT_BIPOLAR_I16 3  /* int16 +1/-1 sign of the bundle, 0 -> +1 */
+#define HDC_OUT_BIPOLAR_F16 4  /* fp16 +1/-1 sign of the bundle, 0 -> +1 (tensor-core queries) */
 
 typedef struct hdc_context hdc_context;
 typedef struct hdc_refdb hdc_refdb;
@@ -122,6 +123,36 @@ int hdc_search_plain(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qnor
                      int32_t max_abs_q, const int16_t* d_r, const int64_t* d_rnorm2, int64_t nr,
                      int32_t max_abs_r, int k, int score_mode, float* d_score, int32_t* d_idx,
                      double* d_cos, int64_t* d_dot, void* d_work, size_t work_bytes, void* stream);
+
+/* Read and clear the device status word of the context (synchronizes the
+ * device): 0, or 100 + the code of a bounded device-side wait that gave up
+ * in a tensor-core search (the search then returned partial results). */
+int hdc_context_status(hdc_context* ctx, int* status);
+
+/* Precision form, reference side: build a tensor-core database from int16
+ * (elem_bytes 2) or int32 (4) reference hypervectors [nr][dim] with
+ * max |v| <= max_abs.  Each value is split into balanced base-2048 fp16
+ * limbs (1 limb for |v| <= 2048, 2 for |v| <= 2048*2048+1023, ...), and the
+ * exact squared norms are kept.  Synchronizes the stream.  dim must be a
+ * multiple of 8.  No reference counterpart (the reference re-uploads and
+ * re-normalises the database on every cosine_search call, src/cosine.cu:
+ * 512-533). */
+int hdc_refdb_create(hdc_context* ctx, const void* d_ref, int elem_bytes, int64_t nr, int32_t max_abs,
+                     hdc_refdb** out, void* stream);
+void hdc_refdb_destroy(hdc_refdb* db);
+int hdc_refdb_limbs(const hdc_refdb* db);
+size_t hdc_search_tc_workspace_bytes(const hdc_context* ctx, const hdc_refdb* db, int64_t nq, int k);
+
+/* Precision form: exact cosine top-k of fp16 integer queries (normally the
+ * +1/-1 read hypervectors of HDC_OUT_BIPOLAR_F16, max_abs_q = 1) against a
+ * tensor-core database, on tcgen05 tensor cores with fp32 accumulators per
+ * limb (exact while dim * max|q| * max|limb| <= 2^24, else HDC_ERR_RANGE).
+ * Same ranking rule, outputs and score modes as hdc_search_plain, whose
+ * results it reproduces exactly; the replacement for launch_cosine_topk
+ * (src/cosine.cu:441-496) at scale. */
+int hdc_search_tc(hdc_context* ctx, const hdc_refdb* db, const void* d_q, const int64_t* d_qnorm2,
+                  int64_t nq, int32_t max_abs_q, int k, int score_mode, float* d_score, int32_t* d_idx,
+                  double* d_cos, int64_t* d_dot, void* d_work, size_t work_bytes, void* stream);
 
 /* ---------------------------------------------------------------- (c) propagate */
 

@@ -1,0 +1,135 @@
+"""Precision form: the tcgen05 tensor-core search against the CPU oracle and
+the plain CUDA-core search.  Dots must be exact (int64 equal), labels and
+order identical, float scores equal, FP64 cosines equal (the cosine error
+against the FP64 oracle is therefore zero; the stated bound is 1e-12
+relative)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(hdc, dev, refs, q_bipolar, dim):
+    import torch
+    ctx = hdc.Context(dim, 10, 250, 10)
+    tr = torch.from_numpy(refs).to(dev)
+    db = ctx.refdb(tr, int(np.abs(refs).max()))
+    q16 = torch.from_numpy(q_bipolar.astype(np.float16)).to(dev)
+    qi = torch.from_numpy(q_bipolar.astype(np.int16)).to(dev)
+    qn = ctx.norms(qi)
+    return ctx, db, tr, q16, qi, qn
+
+
+def _run_tc(ctx, db, q16, qn, maxq, k, mode):
+    import torch
+    s, i, c, d = ctx.search_tc(db, q16, qn, maxq, k, mode)
+    torch.cuda.synchronize()
+    assert ctx.status() == 0
+    return s.cpu().numpy(), i.cpu().numpy(), c.cpu().numpy(), d.cpu().numpy()
+
+
+@pytest.mark.parametrize("dim,nq,nr,k,mode,vmax,dtype", [
+    (1024, 200, 1000, 5, 0, 2000, np.int16),     # one fp16 limb (|v| <= 2048)
+    (2048, 130, 3000, 10, 0, 12000, np.int16),   # two limbs (bundle of 8 copies)
+    (1024, 300, 777, 1, 1, 12000, np.int16),     # argmax, COS scale, ragged sizes
+    (512, 64, 500, 32, 2, 3000, np.int16),       # DOT scale, largest k
+    (1024, 100, 600, 5, 0, 3000000, np.int32),   # two limbs, the top one above 1024
+    (1024, 100, 600, 5, 0, 20000000, np.int32),  # three limbs (int32 internal-node sums)
+    (640, 50, 400, 5, 0, 100000000, np.int32),   # three limbs, top limb ~ 24
+    (10240, 129, 300, 5, 0, 12728, np.int16),    # precision-form dimension
+])
+def test_tc_vs_oracle(hdc, orc, cuda, dim, nq, nr, k, mode, vmax, dtype):
+    g = np.random.default_rng(dim + nq + nr)
+    refs = g.integers(-vmax, vmax + 1, (nr, dim)).astype(dtype)
+    refs[3] = refs[1]                       # tie: lower index first
+    refs[4] = 0                             # zero norm
+    refs[5, :] = vmax                       # extreme limbs
+    refs[6, ::2] = -vmax
+    q = np.where(g.random((nq, dim)) < 0.5, -1, 1).astype(np.int8)
+    q[0] = np.where(refs[1] >= 0, 1, -1)    # a query aligned with reference 1
+    ctx, db, tr, q16, qi, qn = _setup(hdc, cuda, refs, q, dim)
+    s, i, c, d = _run_tc(ctx, db, q16, qn, 1, k, mode)
+    os_, oi, oc, od = orc.topk(q.astype(np.int32), refs.astype(np.int32), min(k, nr), mode)
+    assert np.array_equal(i, oi)
+    assert np.array_equal(d, od)
+    assert np.array_equal(s, os_)
+    assert np.array_equal(c, oc)
+
+
+def test_tc_matches_plain_form(hdc, cuda):
+    """Same bipolar queries and references through both GPU forms."""
+    import torch
+    g = np.random.default_rng(1)
+    dim, nq, nr = 2048, 500, 4000
+    refs = g.integers(-12000, 12001, (nr, dim)).astype(np.int16)
+    q = np.where(g.random((nq, dim)) < 0.5, -1, 1).astype(np.int8)
+    ctx, db, tr, q16, qi, qn = _setup(hdc, cuda, refs, q, dim)
+    rn = ctx.norms(tr)
+    a = ctx.search_plain(qi, qn, 1, tr, rn, 12000, 5, hdc.SCORE_NORM)
+    b = ctx.search_tc(db, q16, qn, 1, 5, hdc.SCORE_NORM)
+    torch.cuda.synchronize()
+    for x, y in zip(a, b):
+        assert torch.equal(x, y)
+
+
+def test_tc_exact_worst_case_accumulators(hdc, orc, cuda):
+    """Every query element +1 against limbs at their extremes: each per-limb
+    accumulator reaches dim * 1024 (= 2^23 at dim 8192) with no rounding."""
+    dim, nq, nr = 8192, 4, 130
+    refs = np.full((nr, dim), -1024 + 2048 * 7, np.int16)   # low limb -1024, high limb 7
+    refs[1] = 1023
+    refs[2] = -1024
+    refs[3] = 2047 * 5 + 1023
+    q = np.ones((nq, dim), np.int8)
+    q[1] = -1
+    ctx, db, tr, q16, qi, qn = _setup(hdc, cuda, refs, q, dim)
+    s, i, c, d = _run_tc(ctx, db, q16, qn, 1, 5, hdc.SCORE_DOT)
+    os_, oi, oc, od = orc.topk(q.astype(np.int32), refs.astype(np.int32), 5, orc.SCORE_DOT)
+    assert np.array_equal(d, od) and np.array_equal(i, oi)
+
+
+def test_tc_rejects_inexact_range(hdc, cuda):
+    import torch
+    dim = 16384 + 64
+    refs = np.full((8, dim), 2000, np.int16)    # one limb of 2000: 16448 * 2000 > 2^24
+    q = np.ones((2, dim), np.int8)
+    ctx, db, tr, q16, qi, qn = _setup(hdc, cuda, refs, q, dim)
+    with pytest.raises(hdc.HDCError) as e:
+        ctx.search_tc(db, q16, qn, 1, 1)
+    assert e.value.status == 2
+
+
+def test_tc_encoded_bipolar_reads(hdc, orc, cuda):
+    """End to end: bundled references (8 noisy copies) and bipolar reads encoded
+    on the GPU, searched on the tensor cores, checked against the oracle's
+    encode + brute-force ranking of the same sequences."""
+    import torch
+    H = hdc
+    dim, kmer = 2048, 10
+    tree = H.synth_tree(7, 64)
+    copies = H.synth_copies(8, tree, 8, 0.01)
+    reads = H.synth_reads(9, tree, 100, 250, subst=0.01)
+    ctx = H.Context(dim, kmer, 250, 10)
+
+    def enc(seqs, kind, dt):
+        out = torch.empty((len(seqs), dim), dtype=dt, device=cuda)
+        ctx.encode_segments(torch.from_numpy(seqs.buf).to(cuda), torch.from_numpy(seqs.off).to(cuda),
+                            torch.from_numpy(seqs.len).to(cuda), out, kind, seqs.max_len())
+        return out
+
+    cp = enc(copies, H.OUT_I32, torch.int32)
+    ptr = torch.arange(0, len(copies) + 1, 8, dtype=torch.int64, device=cuda)
+    refs = ctx.bundle(cp, ptr, torch.arange(len(copies), dtype=torch.int32, device=cuda))
+    q16 = enc(reads, H.OUT_BIPOLAR_F16, torch.float16)
+    qi = enc(reads, H.OUT_BIPOLAR_I16, torch.int16)
+    qn = ctx.norms(qi)
+    db = ctx.refdb(refs, int(refs.abs().max().item()))
+    s, i, c, d = ctx.search_tc(db, q16, qn, 1, 5, H.SCORE_NORM)
+    torch.cuda.synchronize()
+    ref_np = orc.encode([copies.get(j) for j in range(len(copies))], dim, kmer, "int32")[0]
+    ref_np = ref_np.reshape(64, 8, dim).sum(1)
+    assert np.array_equal(refs.cpu().numpy(), ref_np)
+    os_, oi = orc.classify([reads.get(j) for j in range(len(reads))], ref_np, dim, kmer, 5, orc.SCORE_NORM,
+                           bipolar=True)
+    assert np.array_equal(i.cpu().numpy(), oi)
+    assert np.array_equal(s.cpu().numpy(), os_)
