@@ -146,6 +146,94 @@ def make_reads(H, tree, cfg, n, seed):
 
 
 # ---------------------------------------------------------------------------- our arm
+class Form:
+    """One GPU form of the hot path for a fixed batch size: encode the batch of
+    reads, then top-k search against the resident database.
+      plain: int16 queries (counts, or +1/-1 when the workload is bipolar),
+             exact search on CUDA cores (hdc_search_plain)
+      tc:    fp16 +1/-1 queries, exact search on tcgen05 tensor cores
+             (hdc_search_tc against an fp16-limb database)"""
+
+    def __init__(self, H, ctx, cfg, name, refs, rn, maxr, B, dev):
+        import torch
+        self.H, self.ctx, self.cfg, self.name, self.B = H, ctx, cfg, name, B
+        self.refs, self.rn, self.maxr = refs, rn, maxr
+        K, dim = cfg["topk"], cfg["dim"]
+        self.K = K
+        if name == "tc":
+            self.db = ctx.refdb(refs, maxr)
+            self.kind, self.q = H.OUT_BIPOLAR_F16, torch.empty((B, dim), dtype=torch.float16, device=dev)
+            self.maxq = 1
+            self.work = torch.empty(max(16, H.lib().hdc_search_tc_workspace_bytes(ctx.h, self.db.h, B, K)),
+                                    dtype=torch.uint8, device=dev)
+        else:
+            self.db = None
+            self.kind = H.OUT_BIPOLAR_I16 if cfg["bipolar"] else H.OUT_I16
+            self.q = torch.empty((B, dim), dtype=torch.int16, device=dev)
+            self.maxq = 1 if cfg["bipolar"] else cfg["read_len"] - cfg["kmer"] + 1
+            self.work = torch.empty(max(16, ctx.workspace_bytes(B, refs.shape[0], K)), dtype=torch.uint8,
+                                    device=dev)
+        # +1/-1 rows have squared norm dim exactly; count rows are normed per batch
+        self.qn = torch.full((B,), dim, dtype=torch.int64, device=dev) if cfg["bipolar"] else None
+        self.out = (torch.empty((B, K), dtype=torch.float32, device=dev),
+                    torch.empty((B, K), dtype=torch.int32, device=dev),
+                    torch.empty((B, K), dtype=torch.float64, device=dev),
+                    torch.empty((B, K), dtype=torch.int64, device=dev))
+        self.launches = 3 if cfg["bipolar"] else 4  # encode, [norms], search, merge
+
+    def run(self, buf, off, ln, ev=None, stream=None):
+        H, ctx = self.H, self.ctx
+        ctx.encode_segments(buf, off, ln, self.q, self.kind, self.cfg["read_len"])
+        qn = self.qn if self.qn is not None else ctx.norms(self.q)
+        if ev is not None:
+            ev[0].record(stream)
+        if self.name == "tc":
+            ctx.search_tc(self.db, self.q, qn, 1, self.K, H.SCORE_NORM, work=self.work, out=self.out)
+        else:
+            ctx.search_plain(self.q, qn, self.maxq, self.refs, self.rn, self.maxr, self.K, H.SCORE_NORM,
+                             work=self.work, out=self.out)
+        if ev is not None:
+            ev[1].record(stream)
+        return self.out
+
+
+def time_form(form, batches, d_buf, steps, warmup, world, sampler=None):
+    """Device-timed steps of one form on resident batches; also the median
+    duration of its search kernel (+ merge) alone, on the same stream."""
+    import torch
+    stream = torch.cuda.current_stream()
+    for i in range(warmup):
+        form.run(d_buf, *batches[i % len(batches)])
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctxm = sampler if sampler is not None else _Null()
+    with ctxm:
+        torch.cuda.synchronize()
+        t0.record(stream)
+        for i in range(steps):
+            form.run(d_buf, *batches[i % len(batches)])
+        t1.record(stream)
+        torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / steps
+    ev = [torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)]
+    search = []
+    for i in range(3):
+        form.run(d_buf, *batches[i % len(batches)], ev=ev, stream=stream)
+        torch.cuda.synchronize()
+        search.append(ev[0].elapsed_time(ev[1]))
+    return ms, float(np.median(search))
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
 def run_ours(args, cfg, rank, world):
     import torch
     import hdc_gb300 as H
@@ -153,60 +241,40 @@ def run_ours(args, cfg, rank, world):
     torch.cuda.set_device(dev)
     ctx = H.Context(cfg["dim"], cfg["kmer"], cfg["read_len"], 10)
     tree, refs, rn, maxr = build_database(H, ctx, cfg, dev)
-    B, K, dim = args.batch, cfg["topk"], cfg["dim"]
+    B = args.batch
     n_pool = 2
     reads = make_reads(H, tree, cfg, B * n_pool, cfg["read_seed"] + 1000 * rank)
-    maxq = cfg["read_len"] - cfg["kmer"] + 1 if not cfg["bipolar"] else 1
-    kind = H.OUT_BIPOLAR_I16 if cfg["bipolar"] else H.OUT_I16
-    # device-resident read batches
     d_buf = torch.from_numpy(reads.buf).to(dev)
     batches = []
     for p in range(n_pool):
         off = torch.from_numpy(np.ascontiguousarray(reads.off[p * B:(p + 1) * B])).to(dev)
         ln = torch.from_numpy(np.ascontiguousarray(reads.len[p * B:(p + 1) * B])).to(dev)
         batches.append((off, ln))
-    q = torch.empty((B, dim), dtype=torch.int16, device=dev)
-    work = torch.empty(ctx.workspace_bytes(B, refs.shape[0], K), dtype=torch.uint8, device=dev)
-    out = (torch.empty((B, K), dtype=torch.float32, device=dev), torch.empty((B, K), dtype=torch.int32, device=dev),
-           torch.empty((B, K), dtype=torch.float64, device=dev), torch.empty((B, K), dtype=torch.int64, device=dev))
+    form = Form(H, ctx, cfg, args.form, refs, rn, maxr, B, dev)
+    clk = ClockSampler(dev.index)
+    ms, search_ms = time_form(form, batches, d_buf, args.steps, args.warmup, world, clk)
+    res = dict(ms=ms, search_ms=search_ms, clocks=clk.summary(), launches=form.launches * args.steps,
+               refs=refs.shape[0], limbs=form.db.limbs if form.db is not None else 0)
+
+    # the plain drop-in on the same workload, for the tensor-core speed-up
+    if args.form == "tc" and not args.no_plain:
+        pb = min(B, args.plain_batch)
+        pbat = [(o[:pb], l[:pb]) for o, l in batches]
+        plain = Form(H, ctx, cfg, "plain", refs, rn, maxr, pb, dev)
+        pms, psearch = time_form(plain, pbat, d_buf, max(2, args.steps // 2), 3, world)
+        res["plain"] = dict(value=pb / (pms / 1e3), ms=pms, batch=pb, search_ms=psearch)
+        del plain
+        # identical labels: the first plain batch against the tensor-core result
+        form.run(d_buf, *pbat[0])
+        tc_idx = form.out[1][:pb].clone()
+        plain2 = Form(H, ctx, cfg, "plain", refs, rn, maxr, pb, dev)
+        plain2.run(d_buf, *pbat[0])
+        torch.cuda.synchronize()
+        res["labels_identical_to_plain"] = bool(torch.equal(tc_idx, plain2.out[1]))
+        del plain2
+
+    # end to end through the C ABI with pinned host buffers, copies inside the timed region
     stream = torch.cuda.current_stream()
-    ev_s = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-    search_ms = []
-
-    def step(i, time_search=False):
-        off, ln = batches[i % n_pool]
-        ctx.encode_segments(d_buf, off, ln, q, kind, cfg["read_len"])
-        qn = ctx.norms(q)
-        if time_search:
-            ev_s[0].record(stream)
-        ctx.search_plain(q, qn, maxq, refs, rn, maxr, K, H.SCORE_NORM, work=work, out=out)
-        if time_search:
-            ev_s[1].record(stream)
-        return out
-
-    for i in range(args.warmup):
-        step(i)
-    torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    with ClockSampler(dev.index) as clk:
-        torch.cuda.synchronize()
-        t0.record(stream)
-        for i in range(args.steps):
-            step(i)
-        t1.record(stream)
-        torch.cuda.synchronize()
-    ms = t0.elapsed_time(t1) / args.steps
-    # dominant kernel, timed alone inside a step (same stream)
-    for i in range(3):
-        step(i, time_search=True)
-        torch.cuda.synchronize()
-        search_ms.append(ev_s[0].elapsed_time(ev_s[1]))
-    search_ms = float(np.median(search_ms))
-
-    # end to end through the C ABI with host buffers (pinned), copies inside the timed region
     h_bufs = []
     for p in range(n_pool):
         o0 = int(reads.off[p * B])
@@ -219,41 +287,38 @@ def run_ours(args, cfg, rank, world):
     e_buf = torch.empty(cap + 16, dtype=torch.uint8, device=dev)
     e_off = torch.empty(B, dtype=torch.int64, device=dev)
     e_len = torch.empty(B, dtype=torch.int32, device=dev)
-    h_s = torch.empty((B, K), dtype=torch.float32).pin_memory()
-    h_i = torch.empty((B, K), dtype=torch.int32).pin_memory()
-    h2d = d2h = 0
+    h_s = torch.empty((B, form.K), dtype=torch.float32).pin_memory()
+    h_i = torch.empty((B, form.K), dtype=torch.int32).pin_memory()
+    io = {}
 
     def e2e_step(i):
-        nonlocal h2d, d2h
         hb, ho, hl = h_bufs[i % n_pool]
         e_buf[:hb.numel()].copy_(hb, non_blocking=True)
         e_off.copy_(ho, non_blocking=True)
         e_len.copy_(hl, non_blocking=True)
-        ctx.encode_segments(e_buf, e_off, e_len, q, kind, cfg["read_len"])
-        qn = ctx.norms(q)
-        ctx.search_plain(q, qn, maxq, refs, rn, maxr, K, H.SCORE_NORM, work=work, out=out)
+        out = form.run(e_buf, e_off, e_len)
         h_s.copy_(out[0], non_blocking=True)
         h_i.copy_(out[1], non_blocking=True)
-        h2d = hb.numel() + ho.numel() * 8 + hl.numel() * 4
-        d2h = h_s.numel() * 4 + h_i.numel() * 4
+        io["h2d"] = hb.numel() + ho.numel() * 8 + hl.numel() * 4
+        io["d2h"] = h_s.numel() * 4 + h_i.numel() * 4
 
     for i in range(args.warmup):
         e2e_step(i)
     torch.cuda.synchronize()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0.record(stream)
     for i in range(args.steps):
         e2e_step(i)
     t1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = t0.elapsed_time(t1) / args.steps
-
     if world > 1:
         t = torch.tensor([ms, e2e_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms, e2e_ms = float(t[0]), float(t[1])
-    return dict(ms=ms, e2e_ms=e2e_ms, search_ms=search_ms, clocks=clk.summary(), h2d=h2d, d2h=d2h,
-                refs=refs.shape[0], launches=4 * args.steps, tree=tree,
-                refs_host=refs.cpu().numpy().astype(np.int32) if rank == 0 else None)
+        res["ms"], e2e_ms = float(t[0]), float(t[1])
+    res.update(e2e_ms=e2e_ms, h2d=io["h2d"], d2h=io["d2h"], tree=tree)
+    res["refs_host"] = refs.cpu().numpy() if (rank == 0 and not args.no_cpu_baseline) else None
+    return res
 
 
 def oracle_database(cfg, threads):
@@ -316,9 +381,11 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
-    ap.add_argument("--form", default="plain", choices=["plain"])
+    ap.add_argument("--config", default="c3", choices=sorted(CONFIGS))
+    ap.add_argument("--form", default="tc", choices=["plain", "tc"])
     ap.add_argument("--batch", type=int, default=32768)
+    ap.add_argument("--plain-batch", type=int, default=4096)
+    ap.add_argument("--no-plain", action="store_true", help="skip timing the plain form beside the tc form")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -354,31 +421,47 @@ def main():
     pk, src = peaks()
     B = args.batch
     value = B * world / (r["ms"] / 1e3)
-    # roofline of the dominant kernel (the plain search): 2*D*R ops per read on the FP32 pipe
-    ops = 2.0 * cfg["dim"] * r["refs"] * B
-    achieved = ops / (r["search_ms"] / 1e3) / 1e12
-    sm_mhz = r["clocks"].get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
-    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    dim, nr = cfg["dim"], r["refs"]
+    if args.form == "tc":
+        # tensor work per read: one fp16 MMA pass per limb, 2*D*R*limbs flops
+        flops = 2.0 * dim * nr * r["limbs"] * B
+        achieved = flops / (r["search_ms"] / 1e3) / 1e12
+        roof = {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                "frac": achieved / pk["bf16_tflops"], "traffic": None,
+                "peak_source": "%s dense bf16/fp16 burst (MEASURED_PEAKS.json)" % src,
+                "kernel": "tc_search_kernel + merge, %d fp16 limbs; algorithmic 2*D*R*limbs per read" % r["limbs"]}
+        dtype = "fp16 integer limbs, fp32 accumulators (exact int64 dots), FP64 scores"
+    else:
+        flops = 2.0 * dim * nr * B
+        achieved = flops / (r["search_ms"] / 1e3) / 1e12
+        sm_mhz = r["clocks"].get("sm_mhz") or pk.get("sm_max_mhz", 2070.0)
+        fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+        roof = {"bound": "fp32-pipe", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp32_peak, "traffic": None,
+                "peak_source": "152 SMs x 128 FFMA x 2 x median SM clock",
+                "kernel": "plain_kernel + merge on CUDA cores; algorithmic 2*D*R per read"}
+        dtype = "int16 (exact integer dots on the fp32 pipe), FP64 scores"
     line = {
         "metric": metric, "value": value, "unit": "reads/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "int16 (exact integer dot, fp32-pipe chunks)", "data": "synthetic",
+        "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded 6-rank tree, see bench.py)",
         "config": {"workload": workload, "form": args.form, "batch_reads": B,
-                   "l2": "inputs larger than L2: %.0f MB reference database read every step" %
-                         (r["refs"] * cfg["dim"] * 2 / 1e6)},
+                   "l2": "inputs larger than L2: %.0f MB reference database streamed every step" %
+                         (nr * dim * 2 * max(1, r["limbs"]) / 1e6)},
         "e2e": {"value": B * world / (r["e2e_ms"] / 1e3), "unit": "reads/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"]},
-        "roofline": {"bound": "fp32-pipe", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": achieved / fp32_peak, "traffic": None,
-                     "note": "plain search on CUDA cores; peak = 152 SMs x 128 FFMA x 2 x median SM clock"},
-        "clocks": r["clocks"], "gpu_launches": r["launches"],
+        "roofline": roof, "clocks": r["clocks"], "gpu_launches": r["launches"],
     }
+    if "plain" in r:
+        line["plain_form"] = {"value": r["plain"]["value"], "unit": "reads/s", "batch_reads": r["plain"]["batch"],
+                              "speedup_tc_over_plain": value / r["plain"]["value"],
+                              "labels_identical": r["labels_identical_to_plain"]}
     if not args.no_cpu_baseline:
         v, threads, done = cpu_baseline(cfg, r["tree"], r["refs_host"])
         line["cpu_baseline"] = {"value": v, "unit": "reads/s", "cores": threads, "kind": "port",
                                 "sample": "%d reads of the same workload (encode + brute-force top-%d against "
                                           "all %d references; database hypervectors from the GPU encoder, "
-                                          "bit-identical to the oracle's)" % (done, cfg["topk"], r["refs"])}
+                                          "bit-identical to the oracle's)" % (done, cfg["topk"], nr)}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -426,7 +426,8 @@ typedef struct {
     const char* buf;
     const int64_t *off, *len;
     int64_t n;
-    const int32_t* refs;
+    const void* refs;
+    int ref_bytes; /* 2: int16 rows (HV_16), 4: int32 rows */
     const int64_t* rn;
     int64_t nr;
     int k, mode, bipolar;
@@ -452,9 +453,14 @@ static void* cls_worker(void* arg) {
         }
         int filled = 0;
         for (int64_t ri = 0; ri < j->nr; ++ri) {
-            const int32_t* r = j->refs + (size_t)ri * dim;
             int64_t dot = 0;
-            for (int d = 0; d < dim; ++d) dot += (int64_t)acc[d] * r[d];
+            if (j->ref_bytes == 2) {
+                const int16_t* r = (const int16_t*)j->refs + (size_t)ri * dim;
+                for (int d = 0; d < dim; ++d) dot += (int64_t)acc[d] * r[d];
+            } else {
+                const int32_t* r = (const int32_t*)j->refs + (size_t)ri * dim;
+                for (int d = 0; d < dim; ++d) dot += (int64_t)acc[d] * r[d];
+            }
             float sc = score_from(dot, qn, j->rn[ri], j->mode);
             if (filled == k && !better(sc, (int32_t)ri, bs[k - 1], bi[k - 1])) continue;
             int pos = filled < k ? filled : k - 1;
@@ -480,18 +486,27 @@ static void* cls_worker(void* arg) {
 }
 
 int orc_classify(int dim, int kmer, const char* buf, const int64_t* off, const int64_t* len, int64_t n,
-                 const int32_t* refs, int64_t nr, int k, int mode, int bipolar, float* out_s, int32_t* out_i,
-                 int nthreads) {
+                 const void* refs, int ref_bytes, int64_t nr, int k, int mode, int bipolar, float* out_s,
+                 int32_t* out_i, int nthreads) {
     if (nthreads < 1) nthreads = 1;
     if (nthreads > 256) nthreads = 256;
     orc_tables t;
     tables_init(&t, dim, kmer);
     int64_t* rn = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nr > 0 ? nr : 1));
-    norms_i32(refs, nr, dim, rn);
+    for (int64_t i = 0; i < nr; ++i) {
+        int64_t s = 0;
+        for (int d = 0; d < dim; ++d) {
+            int64_t v = ref_bytes == 2 ? ((const int16_t*)refs)[(size_t)i * dim + d]
+                                       : ((const int32_t*)refs)[(size_t)i * dim + d];
+            s += v * v;
+        }
+        rn[i] = s;
+    }
     pthread_t th[256];
     cls_job jobs[256];
     for (int i = 0; i < nthreads; ++i) {
-        jobs[i] = (cls_job){&t, buf, off, len, n, refs, rn, nr, k, mode, bipolar, out_s, out_i, i, nthreads};
+        jobs[i] = (cls_job){&t, buf, off, len, n, refs, ref_bytes, rn, nr, k, mode, bipolar, out_s, out_i, i,
+                            nthreads};
         pthread_create(&th[i], NULL, cls_worker, &jobs[i]);
     }
     for (int i = 0; i < nthreads; ++i) pthread_join(th[i], NULL);

@@ -36,7 +36,7 @@ def lib():
         L.orc_cosine_i32.argtypes = [P, P, i32, i32]
         L.orc_cosine_i32.restype = ctypes.c_float
         L.orc_topk_i32.argtypes = [P, i64, P, i64, i32, i32, i32, P, P, P, P, i32]
-        L.orc_classify.argtypes = [i32, i32, P, P, P, i64, P, i64, i32, i32, i32, P, P, i32]
+        L.orc_classify.argtypes = [i32, i32, P, P, P, i64, P, i32, i64, i32, i32, i32, P, P, i32]
         L.orc_bundle.argtypes = [P, i32, P, P, i64, P]
         L.orc_propagate_greedy.argtypes = [P, i64, P, i64, i32, ctypes.c_double, i32, P, P]
         L.orc_propagate_greedy.restype = i32
@@ -133,14 +133,16 @@ def topk(q, r, k, mode=SCORE_NORM, nthreads=None):
 
 
 def classify(reads, refs, dim, kmer, k, mode=SCORE_NORM, bipolar=False, nthreads=None):
-    """Encode every read and rank it against int32 refs [nr, dim]: the CPU path."""
+    """Encode every read and rank it against refs [nr, dim] (int16 or int32): the CPU path."""
     buf, offs, lens = pack_segments(reads)
-    refs = np.ascontiguousarray(refs, np.int32)
+    if refs.dtype != np.int16:
+        refs = np.ascontiguousarray(refs, np.int32)
+    refs = np.ascontiguousarray(refs)
     n = len(lens)
     s = np.zeros((n, k), np.float32)
     i = np.zeros((n, k), np.int32)
-    lib().orc_classify(dim, kmer, _p(buf), _p(offs), _p(lens), n, _p(refs), refs.shape[0], k, mode,
-                       int(bipolar), _p(s), _p(i), nthreads or nthreads_default())
+    lib().orc_classify(dim, kmer, _p(buf), _p(offs), _p(lens), n, _p(refs), refs.dtype.itemsize, refs.shape[0], k,
+                       mode, int(bipolar), _p(s), _p(i), nthreads or nthreads_default())
     return s, i
 
 
