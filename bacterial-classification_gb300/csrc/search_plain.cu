@@ -22,6 +22,8 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <mutex>
+#include <string>
 #include <type_traits>
 
 #include "hdc_internal.cuh"
@@ -470,3 +472,67 @@ int launch_bundle(hdc_context* ctx, const void* d_rows, int elem_bytes, const in
 }
 
 }  // namespace hdc
+
+// ---------------------------------------------------------------- search without device allocation
+// Fixed scratch of hdc_search_plain_noalloc: the per-range top-k lists that
+// hdc_search_plain keeps in the caller's workspace.  It is part of the
+// library's device image, so every GPU that loads the library holds these
+// HDC_NOALLOC_SCRATCH_BYTES until the process exits.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[HDC_NOALLOC_SCRATCH_BYTES];
+
+namespace hdc {
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[kMaxDevices] = {};
+}  // namespace
+
+// Device address of the fixed scratch on the current device.  In host code
+// the array's name only stands in for the symbol, so the address is asked of
+// the runtime once per device (with that device current) and then reused.
+static int noalloc_scratch(const hdc_context* ctx, void** out) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "search_plain_noalloc: cudaGetDevice");
+    if (dev != ctx->device)
+        return fail(HDC_ERR_INVALID, "search_plain_noalloc: the context's device must be the current device");
+    if (dev < 0 || dev >= kMaxDevices) return fail(HDC_ERR_INVALID, "search_plain_noalloc: device ordinal >= 64");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "search_plain_noalloc: cudaGetSymbolAddress");
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return HDC_OK;
+}
+
+}  // namespace hdc
+
+extern "C" int hdc_search_plain_noalloc(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qnorm2, int64_t nq,
+                                        int32_t max_abs_q, const int16_t* d_r, const int64_t* d_rnorm2, int64_t nr,
+                                        int32_t max_abs_r, int k, int score_mode, float* d_score, int32_t* d_idx,
+                                        double* d_cos, int64_t* d_dot, void* stream) {
+    using namespace hdc;
+    if (!ctx) return fail(HDC_ERR_INVALID, "search_plain_noalloc: null context");
+    if (nq < 0 || nr < 0) return fail(HDC_ERR_INVALID, "search_plain_noalloc: negative count");
+    if (nq == 0) return HDC_OK;
+    if (!valid_score_mode(score_mode)) return fail(HDC_ERR_INVALID, "search_plain_noalloc: bad score mode");
+    if (!d_q || !d_qnorm2 || !d_r || !d_rnorm2 || !d_score || !d_idx)
+        return fail(HDC_ERR_INVALID, "search_plain_noalloc: null pointer");
+    if (nr <= 0) return fail(HDC_ERR_INVALID, "search_plain_noalloc: empty reference set");
+    const size_t need = plain_workspace_bytes(ctx, nq, nr, k);
+    if (need > (size_t)HDC_NOALLOC_SCRATCH_BYTES)
+        return fail(HDC_ERR_RANGE, "search_plain_noalloc: this batch needs " + std::to_string(need) +
+                                       " bytes of scratch but the fixed scratch holds " +
+                                       std::to_string((size_t)HDC_NOALLOC_SCRATCH_BYTES) +
+                                       "; pass fewer queries per call");
+    void* scratch = nullptr;
+    int st = noalloc_scratch(ctx, &scratch);
+    if (st != HDC_OK) return st;
+    // The kernel writes every scratch entry the merge reads, so nothing is cleared.
+    return launch_search_plain(ctx, d_q, d_qnorm2, nq, max_abs_q, d_r, d_rnorm2, nr, max_abs_r, k, score_mode, d_score,
+                               d_idx, d_cos, d_dot, scratch, (size_t)HDC_NOALLOC_SCRATCH_BYTES,
+                               static_cast<cudaStream_t>(stream));
+}

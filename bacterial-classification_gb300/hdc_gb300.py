@@ -34,6 +34,8 @@ SIGNATURES = [
                                SZ, P]),
     ("hdc_bundle", I32, [P, P, I32, P, P, I64, P, P]),
     ("hdc_context_status", I32, [P, ctypes.POINTER(ctypes.c_int)]),
+    ("hdc_search_plain_noalloc", I32, [P, P, P, I64, ctypes.c_int32, P, P, I64, ctypes.c_int32, I32, I32, P, P, P,
+                                       P, P]),
     ("hdc_refdb_create", I32, [P, P, I32, I64, ctypes.c_int32, ctypes.POINTER(P), P]),
     ("hdc_refdb_destroy", None, [P]),
     ("hdc_refdb_limbs", I32, [P]),

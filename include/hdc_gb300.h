@@ -154,6 +154,40 @@ int hdc_search_tc(hdc_context* ctx, const hdc_refdb* db, const void* d_q, const 
                   int64_t nq, int32_t max_abs_q, int k, int score_mode, float* d_score, int32_t* d_idx,
                   double* d_cos, int64_t* d_dot, void* d_work, size_t work_bytes, void* stream);
 
+/* Size of the fixed device scratch used by hdc_search_plain_noalloc (16 MiB). */
+#define HDC_NOALLOC_SCRATCH_BYTES (16u << 20)
+
+/* hdc_search_plain without any device allocation, by this library or by the
+ * caller: the same search, arguments, results and errors, except that the
+ * workspace is a fixed HDC_NOALLOC_SCRATCH_BYTES array that the library
+ * places in device memory once, when the GPU loads it.  It has no
+ * counterpart in the reference (whose launch_cosine_topk allocates and frees
+ * its buffers on every call, src/cosine.cu:455-494).
+ *
+ * For callers that cannot allocate device memory: a host application or
+ * framework that owns the device memory through its own pool and does not
+ * let plug-in code call cudaMalloc; code whose memory budget is already
+ * reserved in full; loops that cannot afford the device-wide
+ * synchronisation cudaMalloc / cudaFree imply.
+ *
+ * Limits and behaviour:
+ *   - a batch whose workspace (hdc_search_workspace_bytes) exceeds
+ *     HDC_NOALLOC_SCRATCH_BYTES is rejected with HDC_ERR_RANGE and a message
+ *     naming both sizes; pass fewer queries per call;
+ *   - the context's device must be the current device; the first call on a
+ *     device looks up the scratch's device address there (once per device),
+ *     so make that first call before any stream capture;
+ *   - every call on a device uses the same scratch, which keeps the previous
+ *     call's contents (the search overwrites every entry it reads, so
+ *     nothing needs clearing); calls that overlap on the GPU (other streams,
+ *     other threads) race on it: serialise them;
+ *   - the scratch stays allocated on every GPU that has loaded the library
+ *     until the process exits. */
+int hdc_search_plain_noalloc(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qnorm2, int64_t nq,
+                             int32_t max_abs_q, const int16_t* d_r, const int64_t* d_rnorm2, int64_t nr,
+                             int32_t max_abs_r, int k, int score_mode, float* d_score, int32_t* d_idx,
+                             double* d_cos, int64_t* d_dot, void* stream);
+
 /* ---------------------------------------------------------------- (c) propagate */
 
 /* Bundling of taxonomy nodes: parent p = sum of its children's rows
