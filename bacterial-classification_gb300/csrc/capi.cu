@@ -211,6 +211,16 @@ int hdc_search_tc(hdc_context* ctx, const hdc_refdb* db, const void* d_q, const 
                                  static_cast<cudaStream_t>(stream));
 }
 
+int hdc_search_tc_tuning(hdc_context* ctx, int group_tiles, int l2_policy, int tile_n) {
+    if (!ctx) return fail(HDC_ERR_INVALID, "tc tuning: null context");
+    if (group_tiles < 0 || l2_policy < -1 || l2_policy > 2 || (tile_n != 0 && tile_n != 128 && tile_n != 256))
+        return fail(HDC_ERR_INVALID, "tc tuning: bad value");
+    ctx->tc_group = group_tiles;
+    ctx->tc_policy = l2_policy;
+    ctx->tc_tile_n = tile_n;
+    return HDC_OK;
+}
+
 int hdc_bundle(hdc_context* ctx, const void* d_rows, int elem_bytes, const int64_t* d_child_ptr,
                const int32_t* d_child_idx, int64_t n_parents, int32_t* d_out, void* stream) {
     if (!ctx) return fail(HDC_ERR_INVALID, "bundle: null context");

@@ -22,6 +22,9 @@ struct hdc_context {
     uint64_t* host_base = nullptr;  // [4][words64], A,C,G,T
     uint32_t* d_base32 = nullptr;   // [4][words32] on the device
     int* d_status = nullptr;        // device status word written by kernels that can give up
+    int tc_group = 0;               // tensor-core search: query tiles per group (0: automatic)
+    int tc_policy = -1;             // tensor-core search: L2 policy (-1: automatic, see hdc_search_tc_tuning)
+    int tc_tile_n = 0;              // tensor-core search: references per tile, 128 or 256 (0: automatic)
 };
 
 // A tensor-core reference database (hdc_refdb_create).
@@ -33,7 +36,6 @@ struct hdc_refdb {
     float* d_rsq = nullptr;     // [nr]
     int32_t limb_max[4] = {0, 0, 0, 0};
     int32_t max_abs = 0;
-    CUtensorMap tmB;  // TMA descriptor of the limbs, [L*r_pad][dim] fp16
 };
 
 namespace hdc {
@@ -70,6 +72,9 @@ int refdb_create(hdc_context* ctx, const void* d_ref, int elem_bytes, int64_t nr
                  cudaStream_t stream);
 void refdb_destroy(hdc_refdb* db);
 size_t tc_workspace_bytes(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int k);
+int tc_default_group();
+int tc_default_policy();
+int tc_default_tile_n();
 int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, const int64_t* d_qn, int64_t nq,
                      int32_t maxq, int k, int mode, float* d_score, int32_t* d_idx, double* d_cos, int64_t* d_dot,
                      void* d_work, size_t work_bytes, int* d_status, cudaStream_t stream);

@@ -21,9 +21,17 @@
 // thread owns one query (one TMEM lane) and keeps that query's running top-k
 // in registers/local memory: an fp32 estimate of every score filters
 // candidates, and only those near the current k-th best get the exact FP64
-// score of the reference CPU cosine (src/HV.cpp:219-242).  Work units are
-// (reference chunk, query tile) pairs handed out chunk-major, so the CTAs
-// running at the same time stream the same references through L2.
+// score of the reference CPU cosine (src/HV.cpp:219-242).
+//
+// Schedule.  With D in the thousands neither operand tile fits in shared
+// memory for the whole K loop, so both are streamed from L2 for every
+// (query tile, reference tile) pair.  The persistent grid is G x S CTAs:
+// for each group of G query tiles, CTA (g, j) takes query tile g and the
+// reference tiles j, j+S, j+2S, ...  All CTAs advance in lockstep, so at any
+// moment G query tiles are each read by S CTAs and S reference tiles are each
+// read by G CTAs; query tiles are loaded with an L2 evict-last policy and
+// reference tiles with evict-first, so DRAM sees each reference tile about
+// once per group instead of each query tile once per pair.
 #include <cuda.h>
 #include <cuda_fp16.h>
 
@@ -38,29 +46,46 @@ namespace hdc {
 namespace {
 
 constexpr int kBM = 128;  // queries per tile (TMEM lanes)
-constexpr int kBN = 128;  // references per tile
-constexpr int kBK = 64;   // dims per K block (128 bytes of fp16)
-constexpr int kTileBytes = kBM * kBK * 2;  // 16 KB, same for A and each B limb
-constexpr int kThreadsTC = 192;            // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
+constexpr int kRowPad = 256;    // database rows are padded to a multiple of the largest N
+constexpr int kThreadsTC = 192;  // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 constexpr int kMaxLimbs = 4;
 constexpr int kMaxKTC = 32;
 
-__host__ __device__ constexpr int tc_stages(int L) { return std::min(8, 196608 / (kTileBytes * (1 + L))); }
-__host__ __device__ constexpr int tc_acc_bufs(int L) { return L <= 2 ? 2 : 1; }
-__host__ __device__ constexpr int tc_tmem_cols(int L) {
-    return tc_acc_bufs(L) * L * kBN <= 256 ? 256 : 512;
+// Tile shapes: N references per tile.  N = 128 streams K blocks of 64 dims
+// (128-byte rows, 128-byte swizzle); N = 256 uses K blocks of 32 dims
+// (64-byte rows, 64-byte swizzle) so that a stage stays small enough for a
+// deep ring.  Swizzle atoms are 8 rows, so the descriptor stride between
+// 8-row groups is 8 * row bytes.
+template <int N>
+struct Tile {
+    static constexpr int BK = N == 256 ? 32 : 64;
+    static constexpr int ROWB = BK * 2;
+    static constexpr int A_BYTES = kBM * ROWB;
+    static constexpr int B_BYTES = N * ROWB;  // per limb
+    static constexpr uint32_t SBO = 8 * ROWB;
+    static constexpr uint32_t LAYOUT = N == 256 ? 4u : 2u;  // descriptor swizzle code: 64B : 128B
+};
+
+template <int N>
+__host__ __device__ constexpr int tc_stage_bytes(int L) { return Tile<N>::A_BYTES + L * Tile<N>::B_BYTES; }
+template <int N>
+__host__ __device__ constexpr int tc_stages(int L) {
+    return 204800 / tc_stage_bytes<N>(L) < 8 ? 204800 / tc_stage_bytes<N>(L) : 8;
 }
+__host__ __device__ constexpr int tc_acc_bufs(int L, int N) { return L * N <= 256 ? 2 : 1; }
+__host__ __device__ constexpr int tc_tmem_cols(int L, int N) { return tc_acc_bufs(L, N) * L * N <= 256 ? 256 : 512; }
 
 struct TcArgs {
     int64_t nq, nr;
     int dim, k, mode, n_kblocks;
     int64_t r_pad;        // rows per limb in the B tensor
-    int n_qtiles, n_rtiles, tiles_per_unit, n_chunks;
-    int64_t n_units;
+    int n_qtiles, n_rtiles;
+    int G, S, n_groups;   // query tiles per group, reference lanes, groups
+    int policy;           // 0: no L2 hint, 1: queries evict-last, 2: + references evict-first
     const int64_t* qn;    // [nq] squared norms of the queries
     const int64_t* rn;    // [nr] squared norms of the references
     const float* rr;      // [nr] fp32 1/sqrt(norm)
-    uint64_t* ws_key;     // [n_chunks][nq][k]
+    uint64_t* ws_key;     // [S][nq][k]
     int64_t* ws_dot;
     int* status;          // device status word (0 = ok)
 };
@@ -71,13 +96,15 @@ __device__ __forceinline__ float approx_tc(float af, float rq, float rr, int mod
     return mode == HDC_SCORE_NORM ? fmaf(2.0f, c, -1.0f) : c;
 }
 
-template <int L>
+template <int L, int kBN>
 __global__ void __launch_bounds__(kThreadsTC, 1)
     tc_search_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcArgs a) {
-    constexpr int STAGES = tc_stages(L);
-    constexpr int ACC = tc_acc_bufs(L);
-    constexpr int TCOLS = tc_tmem_cols(L);
-    constexpr uint32_t kStageBytes = (uint32_t)kTileBytes * (1 + L);
+    using T = Tile<kBN>;
+    constexpr int kBK = T::BK;
+    constexpr int STAGES = tc_stages<kBN>(L);
+    constexpr int ACC = tc_acc_bufs(L, kBN);
+    constexpr int TCOLS = tc_tmem_cols(L, kBN);
+    constexpr uint32_t kStageBytes = (uint32_t)tc_stage_bytes<kBN>(L);
     constexpr uint32_t IDESC = tc::idesc_f16_f32(kBM, kBN);
 
     extern __shared__ uint8_t smem_raw[];
@@ -119,10 +146,12 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             uint32_t phase = 0;
             int64_t issued = 0;
             bool ok = true;
-            for (int64_t u = blockIdx.x; ok && u < a.n_units; u += gridDim.x) {
-                const int chunk = (int)(u / a.n_qtiles), qt = (int)(u % a.n_qtiles);
-                const int t0 = chunk * a.tiles_per_unit, t1 = min(a.n_rtiles, t0 + a.tiles_per_unit);
-                for (int t = t0; ok && t < t1; ++t) {
+            const uint64_t pol_q = tc::make_policy_evict_last(), pol_r = tc::make_policy_evict_first();
+            const bool hint_q = a.policy >= 1, hint_r = a.policy >= 2;
+            for (int grp = 0; ok && grp < a.n_groups; ++grp) {
+                const int qt = grp * a.G + (int)(blockIdx.x % a.G);
+                if (qt >= a.n_qtiles) continue;
+                for (int t = (int)(blockIdx.x / a.G); ok && t < a.n_rtiles; t += a.S) {
                     for (int kb = 0; kb < a.n_kblocks; ++kb) {
                         if (!tc::mbar_wait(&empty_bar[stage], phase ^ 1, &err_s, 1)) {
                             ok = false;
@@ -130,11 +159,19 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         }
                         uint8_t* st = ring + (size_t)stage * kStageBytes;
                         tc::mbar_arrive_expect_tx(&full_bar[stage], kStageBytes);
-                        tc::tma_load_2d(st, &tmA, &full_bar[stage], kb * kBK, qt * kBM);
+                        if (hint_q)
+                            tc::tma_load_2d_hint(st, &tmA, &full_bar[stage], kb * kBK, qt * kBM, pol_q);
+                        else
+                            tc::tma_load_2d(st, &tmA, &full_bar[stage], kb * kBK, qt * kBM);
 #pragma unroll
-                        for (int l = 0; l < L; ++l)
-                            tc::tma_load_2d(st + (size_t)kTileBytes * (1 + l), &tmB, &full_bar[stage], kb * kBK,
-                                            (int)(l * a.r_pad + (int64_t)t * kBN));
+                        for (int l = 0; l < L; ++l) {
+                            void* dst = st + (size_t)T::A_BYTES + (size_t)T::B_BYTES * l;
+                            const int y = (int)(l * a.r_pad + (int64_t)t * kBN);
+                            if (hint_r)
+                                tc::tma_load_2d_hint(dst, &tmB, &full_bar[stage], kb * kBK, y, pol_r);
+                            else
+                                tc::tma_load_2d(dst, &tmB, &full_bar[stage], kb * kBK, y);
+                        }
                         ++issued;
                         if (++stage == STAGES) {
                             stage = 0;
@@ -162,10 +199,10 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             int stage = 0, acc = 0;
             uint32_t phase = 0, acc_phase = 0;
             bool ok = true;
-            for (int64_t u = blockIdx.x; ok && u < a.n_units; u += gridDim.x) {
-                const int chunk = (int)(u / a.n_qtiles);
-                const int t0 = chunk * a.tiles_per_unit, t1 = min(a.n_rtiles, t0 + a.tiles_per_unit);
-                for (int t = t0; ok && t < t1; ++t) {
+            for (int grp = 0; ok && grp < a.n_groups; ++grp) {
+                const int qt = grp * a.G + (int)(blockIdx.x % a.G);
+                if (qt >= a.n_qtiles) continue;
+                for (int t = (int)(blockIdx.x / a.G); ok && t < a.n_rtiles; t += a.S) {
                     if (!tc::mbar_wait(&acce_bar[acc], acc_phase ^ 1, &err_s, 2)) {
                         ok = false;
                         break;
@@ -179,10 +216,11 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         }
                         tc::fence_after();
                         const uint32_t sa = tc::smem_u32(ring + (size_t)stage * kStageBytes);
-                        const uint64_t adesc = tc::sw128_kmajor_desc(sa);
+                        const uint64_t adesc = tc::kmajor_desc(sa, T::SBO, T::LAYOUT);
 #pragma unroll
                         for (int l = 0; l < L; ++l) {
-                            const uint64_t bdesc = tc::sw128_kmajor_desc(sa + (uint32_t)kTileBytes * (1 + l));
+                            const uint64_t bdesc =
+                                tc::kmajor_desc(sa + (uint32_t)T::A_BYTES + (uint32_t)T::B_BYTES * l, T::SBO, T::LAYOUT);
 #pragma unroll
                             for (int kk = 0; kk < kBK / 16; ++kk)  // K = 16 fp16 per MMA = 32 bytes
                                 tc::mma_f16(d0 + l * kBN, adesc + 2 * kk, bdesc + 2 * kk, IDESC,
@@ -214,9 +252,10 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         bool ok = true;
         uint64_t keys[kMaxKTC];
         int64_t dots[kMaxKTC];
-        for (int64_t u = blockIdx.x; ok && u < a.n_units; u += gridDim.x) {
-            const int chunk = (int)(u / a.n_qtiles), qt = (int)(u % a.n_qtiles);
-            const int t0 = chunk * a.tiles_per_unit, t1 = min(a.n_rtiles, t0 + a.tiles_per_unit);
+        const int lane_j = (int)(blockIdx.x / a.G);
+        for (int grp = 0; ok && grp < a.n_groups; ++grp) {
+            const int qt = grp * a.G + (int)(blockIdx.x % a.G);
+            if (qt >= a.n_qtiles) continue;
             const int64_t gq = (int64_t)qt * kBM + row;
             const bool live = gq < a.nq;
             const int64_t my_qn = live ? a.qn[gq] : 0;
@@ -226,7 +265,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 dots[i] = 0;
             }
             float thr = -INFINITY;
-            for (int t = t0; t < t1; ++t) {
+            for (int t = lane_j; t < a.n_rtiles; t += a.S) {
                 if (!tc::mbar_wait(&accf_bar[acc], acc_phase, &err_s, 4)) {
                     ok = false;
                     break;
@@ -276,8 +315,8 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             }
             if (!ok) break;
             if (live) {
-                uint64_t* ok_ = a.ws_key + ((int64_t)chunk * a.nq + gq) * k;
-                int64_t* od = a.ws_dot + ((int64_t)chunk * a.nq + gq) * k;
+                uint64_t* ok_ = a.ws_key + ((int64_t)lane_j * a.nq + gq) * k;
+                int64_t* od = a.ws_dot + ((int64_t)lane_j * a.nq + gq) * k;
                 for (int i = 0; i < k; ++i) {
                     ok_[i] = keys[i];
                     od[i] = dots[i];
@@ -349,17 +388,18 @@ EncodeTiledFn encode_tiled_fn() {
     return fn;
 }
 
-bool make_tmap(CUtensorMap* map, const void* base, int64_t rows, int dim) {
+// Tensor map of a row-major [rows][dim] fp16 matrix read in boxes of
+// box_rows x bk elements with the swizzle matching the row bytes (bk * 2).
+bool make_tmap(CUtensorMap* map, const void* base, int64_t rows, int dim, int bk, int box_rows) {
     EncodeTiledFn encode = encode_tiled_fn();
     if (!encode) return false;
     cuuint64_t gdim[2] = {(cuuint64_t)dim, (cuuint64_t)rows};
     cuuint64_t gstride[1] = {(cuuint64_t)dim * 2};
-    cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)kBM};
+    cuuint32_t box[2] = {(cuuint32_t)bk, (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base), gdim,
-                                        gstride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base), gdim, gstride, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, bk == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS;
 }
 
@@ -384,7 +424,7 @@ int refdb_create(hdc_context* ctx, const void* d_ref, int elem_bytes, int64_t nr
     db->dim = dim;
     db->L = L;
     db->max_abs = max_abs;
-    db->r_pad = (nr + kBN - 1) / kBN * kBN;
+    db->r_pad = (nr + kRowPad - 1) / kRowPad * kRowPad;
     const size_t nl = (size_t)L * db->r_pad * dim;
     cudaError_t e = cudaMalloc(&db->d_limbs, nl * sizeof(__half));
     if (e == cudaSuccess) e = cudaMalloc(&db->d_norm2, nr * sizeof(int64_t));
@@ -418,8 +458,6 @@ int refdb_create(hdc_context* ctx, const void* d_ref, int elem_bytes, int64_t nr
         if (e != cudaSuccess) st = cuda_fail(e, "refdb: build");
     }
     cudaFree(d_lmax);
-    if (st == HDC_OK && !make_tmap(&db->tmB, db->d_limbs, (int64_t)L * db->r_pad, dim))
-        st = fail(HDC_ERR_CUDA, "refdb: cuTensorMapEncodeTiled failed");
     if (st != HDC_OK) {
         cudaFree(db->d_limbs);
         cudaFree(db->d_norm2);
@@ -439,32 +477,46 @@ void refdb_destroy(hdc_refdb* db) {
     delete db;
 }
 
-static void tc_plan(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int& n_qtiles, int& n_rtiles,
-                    int& tiles_per_unit, int& n_chunks) {
+int tc_default_group() { return 1 << 30; }  // every SM on its own query tile, references shared
+int tc_default_policy() { return 0; }
+int tc_default_tile_n() { return 128; }
+
+// G query tiles per group (fewer for small batches) and S = SMs / G lanes.
+// N = 256 needs L * 256 TMEM columns for one accumulator set: 3 and 4 limbs use N = 128.
+static int tc_tile_n(const hdc_context* ctx, const hdc_refdb* db) {
+    const int n = ctx->tc_tile_n > 0 ? ctx->tc_tile_n : tc_default_tile_n();
+    return db->L > 2 ? 128 : n;
+}
+
+static void tc_plan(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int& n_qtiles, int& n_rtiles, int& G,
+                    int& S, int& n_groups) {
     n_qtiles = (int)((nq + kBM - 1) / kBM);
-    n_rtiles = (int)(db->r_pad / kBN);
-    // enough units for ~4 per SM, whole reference chunks streamed chunk-major
-    const int64_t pairs = (int64_t)n_qtiles * n_rtiles;
-    int64_t tpu = std::max<int64_t>(1, pairs / (4 * (int64_t)ctx->num_sms));
-    tpu = std::min<int64_t>(tpu, n_rtiles);
-    tiles_per_unit = (int)tpu;
-    n_chunks = (n_rtiles + tiles_per_unit - 1) / tiles_per_unit;
+    n_rtiles = (int)(db->r_pad / tc_tile_n(ctx, db));
+    const int want = ctx->tc_group > 0 ? ctx->tc_group : tc_default_group();
+    G = std::max(1, std::min(std::min(want, ctx->num_sms), n_qtiles));
+    S = std::max(1, ctx->num_sms / G);
+    S = std::min(S, n_rtiles);
+    n_groups = (n_qtiles + G - 1) / G;
 }
 
 size_t tc_workspace_bytes(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int k) {
-    int qt, rt, tpu, nc;
-    tc_plan(ctx, nq, db, qt, rt, tpu, nc);
+    int qt, rt, G, S, ng;
+    tc_plan(ctx, nq, db, qt, rt, G, S, ng);
     k = (int)std::min<int64_t>(k, db->nr);
-    return (size_t)nc * nq * std::max(k, 1) * (sizeof(uint64_t) + sizeof(int64_t));
+    return (size_t)S * nq * std::max(k, 1) * (sizeof(uint64_t) + sizeof(int64_t));
 }
 
-template <int L>
-static int launch_tc_t(const CUtensorMap& tmA, const hdc_refdb* db, const TcArgs& a, int grid, cudaStream_t stream) {
-    const size_t smem = (size_t)tc_stages(L) * kTileBytes * (1 + L) + 1024;
-    auto kern = tc_search_kernel<L>;
+template <int L, int N>
+static int launch_tc_t(const __half* d_q, const hdc_refdb* db, const TcArgs& a, int grid, cudaStream_t stream) {
+    CUtensorMap tmA, tmB;
+    if (!make_tmap(&tmA, d_q, a.nq, a.dim, Tile<N>::BK, kBM) ||
+        !make_tmap(&tmB, db->d_limbs, (int64_t)db->L * db->r_pad, a.dim, Tile<N>::BK, N))
+        return fail(HDC_ERR_CUDA, "tc search: cuTensorMapEncodeTiled failed");
+    const size_t smem = (size_t)tc_stages<N>(L) * tc_stage_bytes<N>(L) + 1024;
+    auto kern = tc_search_kernel<L, N>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_fail(e, "tc search: cudaFuncSetAttribute");
-    kern<<<grid, kThreadsTC, smem, stream>>>(tmA, db->tmB, a);
+    kern<<<grid, kThreadsTC, smem, stream>>>(tmA, tmB, a);
     e = cudaGetLastError();
     return e == cudaSuccess ? HDC_OK : cuda_fail(e, "tc search: launch");
 }
@@ -483,37 +535,44 @@ int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, c
             return fail(HDC_ERR_RANGE, "tc search: dim * max|q| * max|limb| exceeds 2^24 (fp32 accumulators inexact)");
     }
     if ((reinterpret_cast<uintptr_t>(d_q) & 15) != 0) return fail(HDC_ERR_INVALID, "tc search: queries not 16B aligned");
-    CUtensorMap tmA;
-    if (!make_tmap(&tmA, d_q, nq, ctx->dim)) return fail(HDC_ERR_CUDA, "tc search: cuTensorMapEncodeTiled failed");
+    const int N = tc_tile_n(ctx, db);
     TcArgs a{};
     a.nq = nq;
     a.nr = db->nr;
     a.dim = ctx->dim;
     a.k = k;
     a.mode = mode;
-    a.n_kblocks = (ctx->dim + kBK - 1) / kBK;
+    a.n_kblocks = (ctx->dim + (N == 256 ? Tile<256>::BK : Tile<128>::BK) - 1) / (N == 256 ? Tile<256>::BK : Tile<128>::BK);
     a.r_pad = db->r_pad;
-    tc_plan(ctx, nq, db, a.n_qtiles, a.n_rtiles, a.tiles_per_unit, a.n_chunks);
-    a.n_units = (int64_t)a.n_qtiles * a.n_chunks;
+    tc_plan(ctx, nq, db, a.n_qtiles, a.n_rtiles, a.G, a.S, a.n_groups);
     a.qn = d_qn;
     a.rn = db->d_norm2;
     a.rr = db->d_rsq;
-    const size_t need = (size_t)a.n_chunks * nq * k * (sizeof(uint64_t) + sizeof(int64_t));
+    const size_t need = (size_t)a.S * nq * k * (sizeof(uint64_t) + sizeof(int64_t));
     if (!d_work || work_bytes < need) return fail(HDC_ERR_INVALID, "tc search: workspace too small");
     a.ws_key = static_cast<uint64_t*>(d_work);
-    a.ws_dot = reinterpret_cast<int64_t*>(a.ws_key + (size_t)a.n_chunks * nq * k);
+    a.ws_dot = reinterpret_cast<int64_t*>(a.ws_key + (size_t)a.S * nq * k);
     a.status = d_status;
-    const int grid = (int)std::min<int64_t>(a.n_units, ctx->num_sms);
+    a.policy = ctx->tc_policy >= 0 ? ctx->tc_policy : tc_default_policy();
+    const int grid = a.G * a.S;
     int st;
-    switch (db->L) {
-        case 1: st = launch_tc_t<1>(tmA, db, a, grid, stream); break;
-        case 2: st = launch_tc_t<2>(tmA, db, a, grid, stream); break;
-        case 3: st = launch_tc_t<3>(tmA, db, a, grid, stream); break;
-        default: st = launch_tc_t<4>(tmA, db, a, grid, stream); break;
+    if (N == 256) {
+        switch (db->L) {
+            case 1: st = launch_tc_t<1, 256>(d_q, db, a, grid, stream); break;
+            case 2: st = launch_tc_t<2, 256>(d_q, db, a, grid, stream); break;
+            case 3: st = launch_tc_t<3, 256>(d_q, db, a, grid, stream); break;
+            default: st = launch_tc_t<4, 256>(d_q, db, a, grid, stream); break;
+        }
+    } else {
+        switch (db->L) {
+            case 1: st = launch_tc_t<1, 128>(d_q, db, a, grid, stream); break;
+            case 2: st = launch_tc_t<2, 128>(d_q, db, a, grid, stream); break;
+            case 3: st = launch_tc_t<3, 128>(d_q, db, a, grid, stream); break;
+            default: st = launch_tc_t<4, 128>(d_q, db, a, grid, stream); break;
+        }
     }
     if (st != HDC_OK) return st;
-    return launch_merge(a.ws_key, a.ws_dot, a.n_chunks, nq, k, d_qn, db->d_norm2, d_score, d_idx, d_cos, d_dot,
-                        stream);
+    return launch_merge(a.ws_key, a.ws_dot, a.S, nq, k, d_qn, db->d_norm2, d_score, d_idx, d_cos, d_dot, stream);
 }
 
 }  // namespace hdc

@@ -68,6 +68,28 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, u
         : "memory");
 }
 
+// Same, with an L2 eviction-priority policy (from make_policy_*).
+__device__ __forceinline__ void tma_load_2d_hint(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y,
+                                                 uint64_t policy) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint "
+        "[%0], [%1, {%3, %4}], [%2], %5;" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(smem_u32(bar)), "r"(x), "r"(y), "l"(policy)
+        : "memory");
+}
+
+__device__ __forceinline__ uint64_t make_policy_evict_last() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+__device__ __forceinline__ uint64_t make_policy_evict_first() {
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
 __device__ __forceinline__ void prefetch_tmap(const CUtensorMap* map) {
     asm volatile("prefetch.tensormap [%0];" ::"l"(map) : "memory");
 }
@@ -119,18 +141,19 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 }
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// Shared-memory matrix descriptor of a K-major tile written by TMA with the
-// 128-byte swizzle: rows of 128 bytes, 8-row (1024-byte) swizzle atoms, so
-// the stride between 8-row groups is 1024 bytes; the leading-byte offset is
-// unused for swizzled K-major layouts.  Advancing the start address by 32
-// bytes selects the next K=16 slice of fp16 elements within the atom.
-__device__ __forceinline__ uint64_t sw128_kmajor_desc(uint32_t smem_addr) {
+// Shared-memory matrix descriptor of a K-major tile written by TMA with a
+// 128-byte (layout code 2) or 64-byte (code 4) swizzle: rows of 128 or 64
+// bytes in 8-row swizzle atoms, so the stride between 8-row groups (sbo) is
+// 8 rows; the leading-byte offset is unused for swizzled K-major layouts.
+// Advancing the start address by 32 bytes selects the next K=16 slice of
+// fp16 elements within the atom.
+__device__ __forceinline__ uint64_t kmajor_desc(uint32_t smem_addr, uint32_t sbo, uint32_t layout) {
     uint64_t d = 0;
     d |= (uint64_t)((smem_addr & 0x3FFFFu) >> 4);  // start address, bits 0-13
     d |= (uint64_t)1 << 16;                         // leading byte offset (unused), bits 16-29
-    d |= (uint64_t)(1024 >> 4) << 32;               // stride byte offset, bits 32-45
+    d |= (uint64_t)(sbo >> 4) << 32;                // stride byte offset, bits 32-45
     d |= (uint64_t)1 << 46;                         // descriptor version for sm_10x, bits 46-47
-    d |= (uint64_t)2 << 61;                         // layout: 128-byte swizzle, bits 61-63
+    d |= (uint64_t)layout << 61;                    // swizzle layout, bits 61-63
     return d;
 }
 

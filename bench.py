@@ -388,11 +388,14 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain form beside the tc form")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--refs", type=int, default=0, help="override the number of references (small profiling cases)")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3")
         args.warmup = 3
-    cfg = CONFIGS[args.config]
+    cfg = dict(CONFIGS[args.config])
+    if args.refs:
+        cfg["n_leaves"] = args.refs
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     workload = "%s: %d refs D=%d k=%d, %d bp reads, top-%d" % (args.config, cfg["n_leaves"], cfg["dim"], cfg["kmer"],

@@ -188,6 +188,16 @@ int hdc_search_plain_noalloc(hdc_context* ctx, const int16_t* d_q, const int64_t
                              int32_t max_abs_r, int k, int score_mode, float* d_score, int32_t* d_idx,
                              double* d_cos, int64_t* d_dot, void* stream);
 
+/* Schedule of hdc_search_tc on this context (no reference counterpart; the
+ * knobs an autotuner varies): group_tiles = query tiles of 128 that run
+ * together (0: automatic), the persistent grid being group_tiles x
+ * (SMs / group_tiles) CTAs, each group's reference tiles dealt round-robin
+ * to the SMs / group_tiles lanes; l2_policy = 0 no L2 hint, 1 query tiles
+ * loaded evict-last, 2 also reference tiles evict-first (-1: automatic);
+ * tile_n = references per tile, 128 or 256 (0: automatic).  Results do not
+ * depend on these settings, only the speed does. */
+int hdc_search_tc_tuning(hdc_context* ctx, int group_tiles, int l2_policy, int tile_n);
+
 /* ---------------------------------------------------------------- (c) propagate */
 
 /* Bundling of taxonomy nodes: parent p = sum of its children's rows
