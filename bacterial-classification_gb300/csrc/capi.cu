@@ -211,10 +211,12 @@ int hdc_search_tc(hdc_context* ctx, const hdc_refdb* db, const void* d_q, const 
                                  static_cast<cudaStream_t>(stream));
 }
 
-int hdc_search_tc_tuning(hdc_context* ctx, int group_tiles, int l2_policy, int tile_n) {
+int hdc_search_tc_tuning(hdc_context* ctx, int group_tiles, int l2_policy, int tile_n, int m_blocks) {
     if (!ctx) return fail(HDC_ERR_INVALID, "tc tuning: null context");
-    if (group_tiles < 0 || l2_policy < -1 || l2_policy > 2 || (tile_n != 0 && tile_n != 128 && tile_n != 256))
+    if (group_tiles < 0 || l2_policy < -1 || l2_policy > 2 || (tile_n != 0 && tile_n != 128 && tile_n != 256) ||
+        m_blocks < 0 || m_blocks > 2)
         return fail(HDC_ERR_INVALID, "tc tuning: bad value");
+    ctx->tc_m_blocks = m_blocks;
     ctx->tc_group = group_tiles;
     ctx->tc_policy = l2_policy;
     ctx->tc_tile_n = tile_n;

@@ -25,6 +25,7 @@ struct hdc_context {
     int tc_group = 0;               // tensor-core search: query tiles per group (0: automatic)
     int tc_policy = -1;             // tensor-core search: L2 policy (-1: automatic, see hdc_search_tc_tuning)
     int tc_tile_n = 0;              // tensor-core search: references per tile, 128 or 256 (0: automatic)
+    int tc_m_blocks = 0;            // tensor-core search: 128-query M-blocks per CTA, 1 or 2 (0: automatic)
 };
 
 // A tensor-core reference database (hdc_refdb_create).
@@ -75,6 +76,7 @@ size_t tc_workspace_bytes(const hdc_context* ctx, int64_t nq, const hdc_refdb* d
 int tc_default_group();
 int tc_default_policy();
 int tc_default_tile_n();
+int tc_default_m_blocks();
 int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, const int64_t* d_qn, int64_t nq,
                      int32_t maxq, int k, int mode, float* d_score, int32_t* d_idx, double* d_cos, int64_t* d_dot,
                      void* d_work, size_t work_bytes, int* d_status, cudaStream_t stream);

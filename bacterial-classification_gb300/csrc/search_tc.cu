@@ -66,14 +66,18 @@ struct Tile {
     static constexpr uint32_t LAYOUT = N == 256 ? 4u : 2u;  // descriptor swizzle code: 64B : 128B
 };
 
+// A stage holds MB query tiles (M-blocks of 128 rows) and L reference-limb tiles.
 template <int N>
-__host__ __device__ constexpr int tc_stage_bytes(int L) { return Tile<N>::A_BYTES + L * Tile<N>::B_BYTES; }
+__host__ __device__ constexpr int tc_stage_bytes(int L, int MB) { return MB * Tile<N>::A_BYTES + L * Tile<N>::B_BYTES; }
 template <int N>
-__host__ __device__ constexpr int tc_stages(int L) {
-    return 204800 / tc_stage_bytes<N>(L) < 8 ? 204800 / tc_stage_bytes<N>(L) : 8;
+__host__ __device__ constexpr int tc_stages(int L, int MB) {
+    return 204800 / tc_stage_bytes<N>(L, MB) < 8 ? 204800 / tc_stage_bytes<N>(L, MB) : 8;
 }
-__host__ __device__ constexpr int tc_acc_bufs(int L, int N) { return L * N <= 256 ? 2 : 1; }
-__host__ __device__ constexpr int tc_tmem_cols(int L, int N) { return tc_acc_bufs(L, N) * L * N <= 256 ? 256 : 512; }
+// accumulator sets (TMEM columns MB * L * N each): two when they fit in 256 columns
+__host__ __device__ constexpr int tc_acc_bufs(int L, int N, int MB) { return MB * L * N <= 256 ? 2 : 1; }
+__host__ __device__ constexpr int tc_tmem_cols(int L, int N, int MB) {
+    return tc_acc_bufs(L, N, MB) * MB * L * N <= 256 ? 256 : 512;
+}
 
 struct TcArgs {
     int64_t nq, nr;
@@ -96,16 +100,19 @@ __device__ __forceinline__ float approx_tc(float af, float rq, float rr, int mod
     return mode == HDC_SCORE_NORM ? fmaf(2.0f, c, -1.0f) : c;
 }
 
-template <int L, int kBN>
+template <int L, int kBN, int MB>
 __global__ void __launch_bounds__(kThreadsTC, 1)
     tc_search_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcArgs a) {
     using T = Tile<kBN>;
     constexpr int kBK = T::BK;
-    constexpr int STAGES = tc_stages<kBN>(L);
-    constexpr int ACC = tc_acc_bufs(L, kBN);
-    constexpr int TCOLS = tc_tmem_cols(L, kBN);
-    constexpr uint32_t kStageBytes = (uint32_t)tc_stage_bytes<kBN>(L);
+    constexpr int STAGES = tc_stages<kBN>(L, MB);
+    constexpr int ACC = tc_acc_bufs(L, kBN, MB);
+    constexpr int TCOLS = tc_tmem_cols(L, kBN, MB);
+    constexpr int QT = MB * kBM;  // queries per query tile
+    constexpr uint32_t kStageBytes = (uint32_t)tc_stage_bytes<kBN>(L, MB);
+    constexpr uint32_t kAccCols = (uint32_t)(MB * L * kBN);
     constexpr uint32_t IDESC = tc::idesc_f16_f32(kBM, kBN);
+    static_assert(MB * L * kBN <= 512, "accumulators exceed TMEM");
 
     extern __shared__ uint8_t smem_raw[];
     // 1024-byte aligned tile ring (required by the 128-byte swizzle atoms)
@@ -159,13 +166,17 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         }
                         uint8_t* st = ring + (size_t)stage * kStageBytes;
                         tc::mbar_arrive_expect_tx(&full_bar[stage], kStageBytes);
-                        if (hint_q)
-                            tc::tma_load_2d_hint(st, &tmA, &full_bar[stage], kb * kBK, qt * kBM, pol_q);
-                        else
-                            tc::tma_load_2d(st, &tmA, &full_bar[stage], kb * kBK, qt * kBM);
+#pragma unroll
+                        for (int m = 0; m < MB; ++m) {
+                            void* dst = st + (size_t)T::A_BYTES * m;
+                            if (hint_q)
+                                tc::tma_load_2d_hint(dst, &tmA, &full_bar[stage], kb * kBK, qt * QT + m * kBM, pol_q);
+                            else
+                                tc::tma_load_2d(dst, &tmA, &full_bar[stage], kb * kBK, qt * QT + m * kBM);
+                        }
 #pragma unroll
                         for (int l = 0; l < L; ++l) {
-                            void* dst = st + (size_t)T::A_BYTES + (size_t)T::B_BYTES * l;
+                            void* dst = st + (size_t)T::A_BYTES * MB + (size_t)T::B_BYTES * l;
                             const int y = (int)(l * a.r_pad + (int64_t)t * kBN);
                             if (hint_r)
                                 tc::tma_load_2d_hint(dst, &tmB, &full_bar[stage], kb * kBK, y, pol_r);
@@ -208,7 +219,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         break;
                     }
                     tc::fence_after();
-                    const uint32_t d0 = tmem + (uint32_t)(acc * L * kBN);
+                    const uint32_t d0 = tmem + (uint32_t)acc * kAccCols;
                     for (int kb = 0; kb < a.n_kblocks; ++kb) {
                         if (!tc::mbar_wait(&full_bar[stage], phase, &err_s, 3)) {
                             ok = false;
@@ -216,15 +227,18 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         }
                         tc::fence_after();
                         const uint32_t sa = tc::smem_u32(ring + (size_t)stage * kStageBytes);
-                        const uint64_t adesc = tc::kmajor_desc(sa, T::SBO, T::LAYOUT);
 #pragma unroll
                         for (int l = 0; l < L; ++l) {
-                            const uint64_t bdesc =
-                                tc::kmajor_desc(sa + (uint32_t)T::A_BYTES + (uint32_t)T::B_BYTES * l, T::SBO, T::LAYOUT);
+                            const uint64_t bdesc = tc::kmajor_desc(
+                                sa + (uint32_t)T::A_BYTES * MB + (uint32_t)T::B_BYTES * l, T::SBO, T::LAYOUT);
 #pragma unroll
-                            for (int kk = 0; kk < kBK / 16; ++kk)  // K = 16 fp16 per MMA = 32 bytes
-                                tc::mma_f16(d0 + l * kBN, adesc + 2 * kk, bdesc + 2 * kk, IDESC,
-                                            (kb | kk) != 0 ? 1u : 0u);
+                            for (int m = 0; m < MB; ++m) {
+                                const uint64_t adesc = tc::kmajor_desc(sa + (uint32_t)T::A_BYTES * m, T::SBO, T::LAYOUT);
+#pragma unroll
+                                for (int kk = 0; kk < kBK / 16; ++kk)  // K = 16 fp16 per MMA = 32 bytes
+                                    tc::mma_f16(d0 + (uint32_t)((m * L + l) * kBN), adesc + 2 * kk, bdesc + 2 * kk,
+                                                IDESC, (kb | kk) != 0 ? 1u : 0u);
+                            }
                         }
                         tc::mma_commit(&empty_bar[stage]);  // frees the stage when these MMAs finish
                         if (++stage == STAGES) {
@@ -250,59 +264,69 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         int acc = 0;
         uint32_t acc_phase = 0;
         bool ok = true;
-        uint64_t keys[kMaxKTC];
-        int64_t dots[kMaxKTC];
+        uint64_t keys[MB][kMaxKTC];
+        int64_t dots[MB][kMaxKTC];
         const int lane_j = (int)(blockIdx.x / a.G);
         for (int grp = 0; ok && grp < a.n_groups; ++grp) {
             const int qt = grp * a.G + (int)(blockIdx.x % a.G);
             if (qt >= a.n_qtiles) continue;
-            const int64_t gq = (int64_t)qt * kBM + row;
-            const bool live = gq < a.nq;
-            const int64_t my_qn = live ? a.qn[gq] : 0;
-            const float my_rq = rsqrt_norm(my_qn);
-            for (int i = 0; i < k; ++i) {
-                keys[i] = 0;
-                dots[i] = 0;
+            // this thread owns query row `row` of each M-block
+            int64_t gq[MB], my_qn[MB];
+            float my_rq[MB], thr[MB];
+            bool live[MB];
+#pragma unroll
+            for (int m = 0; m < MB; ++m) {
+                gq[m] = (int64_t)qt * QT + m * kBM + row;
+                live[m] = gq[m] < a.nq;
+                my_qn[m] = live[m] ? a.qn[gq[m]] : 0;
+                my_rq[m] = rsqrt_norm(my_qn[m]);
+                thr[m] = -INFINITY;
+                for (int i = 0; i < k; ++i) {
+                    keys[m][i] = 0;
+                    dots[m][i] = 0;
+                }
             }
-            float thr = -INFINITY;
             for (int t = lane_j; t < a.n_rtiles; t += a.S) {
                 if (!tc::mbar_wait(&accf_bar[acc], acc_phase, &err_s, 4)) {
                     ok = false;
                     break;
                 }
                 tc::fence_after();
-                const uint32_t d0 = tmem + lane_addr + (uint32_t)(acc * L * kBN);
-                for (int c0 = 0; c0 < kBN; c0 += 32) {
-                    uint32_t v[L][32];
+                const uint32_t d0 = tmem + lane_addr + (uint32_t)acc * kAccCols;
 #pragma unroll
-                    for (int l = 0; l < L; ++l) tc::tmem_ld32(d0 + l * kBN + c0, v[l]);
-                    tc::tmem_ld_wait();
-                    const int64_t rbase = (int64_t)t * kBN + c0;
-                    const float rr_lane = (rbase + lane < a.nr) ? __ldg(a.rr + rbase + lane) : 0.0f;
+                for (int m = 0; m < MB; ++m) {
+                    for (int c0 = 0; c0 < kBN; c0 += 32) {
+                        uint32_t v[L][32];
 #pragma unroll
-                    for (int c = 0; c < 32; ++c) {
-                        const float rrc = __shfl_sync(0xffffffffu, rr_lane, c);
-                        float af = __uint_as_float(v[0][c]);
-                        float scale = 1.0f;
+                        for (int l = 0; l < L; ++l) tc::tmem_ld32(d0 + (uint32_t)((m * L + l) * kBN + c0), v[l]);
+                        tc::tmem_ld_wait();
+                        const int64_t rbase = (int64_t)t * kBN + c0;
+                        const float rr_lane = (rbase + lane < a.nr) ? __ldg(a.rr + rbase + lane) : 0.0f;
 #pragma unroll
-                        for (int l = 1; l < L; ++l) {
-                            scale *= 2048.0f;
-                            af = fmaf(__uint_as_float(v[l][c]), scale, af);
-                        }
-                        const float ap = approx_tc(af, my_rq, rrc, a.mode);
-                        if (!(ap >= thr) || !live || rbase + c >= a.nr) continue;
-                        int64_t dot = 0;
+                        for (int c = 0; c < 32; ++c) {
+                            const float rrc = __shfl_sync(0xffffffffu, rr_lane, c);
+                            float af = __uint_as_float(v[0][c]);
+                            float scale = 1.0f;
 #pragma unroll
-                        for (int l = 0; l < L; ++l)
-                            dot += (int64_t)__float2ll_rn(__uint_as_float(v[l][c])) * ((int64_t)1 << (11 * l));
-                        const int64_t gr = rbase + c;
-                        const float s = exact_score(dot, my_qn, __ldg(a.rn + gr), a.mode);
-                        const uint64_t key = make_key(s, (uint32_t)gr);
-                        if (key <= keys[k - 1]) continue;
-                        list_insert(keys, dots, k, key, dot);
-                        if (keys[k - 1] != 0) {
-                            const float sk = key_score(keys[k - 1]);
-                            thr = a.mode == HDC_SCORE_DOT ? sk - (fabsf(sk) * 4e-6f + 1.0f) : sk - kFilterMargin;
+                            for (int l = 1; l < L; ++l) {
+                                scale *= 2048.0f;
+                                af = fmaf(__uint_as_float(v[l][c]), scale, af);
+                            }
+                            const float ap = approx_tc(af, my_rq[m], rrc, a.mode);
+                            if (!(ap >= thr[m]) || !live[m] || rbase + c >= a.nr) continue;
+                            int64_t dot = 0;
+#pragma unroll
+                            for (int l = 0; l < L; ++l)
+                                dot += (int64_t)__float2ll_rn(__uint_as_float(v[l][c])) * ((int64_t)1 << (11 * l));
+                            const int64_t gr = rbase + c;
+                            const float s = exact_score(dot, my_qn[m], __ldg(a.rn + gr), a.mode);
+                            const uint64_t key = make_key(s, (uint32_t)gr);
+                            if (key <= keys[m][k - 1]) continue;
+                            list_insert(keys[m], dots[m], k, key, dot);
+                            if (keys[m][k - 1] != 0) {
+                                const float sk = key_score(keys[m][k - 1]);
+                                thr[m] = a.mode == HDC_SCORE_DOT ? sk - (fabsf(sk) * 4e-6f + 1.0f) : sk - kFilterMargin;
+                            }
                         }
                     }
                 }
@@ -314,12 +338,14 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 }
             }
             if (!ok) break;
-            if (live) {
-                uint64_t* ok_ = a.ws_key + ((int64_t)lane_j * a.nq + gq) * k;
-                int64_t* od = a.ws_dot + ((int64_t)lane_j * a.nq + gq) * k;
+#pragma unroll
+            for (int m = 0; m < MB; ++m) {
+                if (!live[m]) continue;
+                uint64_t* ok_ = a.ws_key + ((int64_t)lane_j * a.nq + gq[m]) * k;
+                int64_t* od = a.ws_dot + ((int64_t)lane_j * a.nq + gq[m]) * k;
                 for (int i = 0; i < k; ++i) {
-                    ok_[i] = keys[i];
-                    od[i] = dots[i];
+                    ok_[i] = keys[m][i];
+                    od[i] = dots[m][i];
                 }
             }
         }
@@ -480,6 +506,7 @@ void refdb_destroy(hdc_refdb* db) {
 int tc_default_group() { return 1 << 30; }  // every SM on its own query tile, references shared
 int tc_default_policy() { return 0; }
 int tc_default_tile_n() { return 128; }
+int tc_default_m_blocks() { return 2; }
 
 // G query tiles per group (fewer for small batches) and S = SMs / G lanes.
 // N = 256 needs L * 256 TMEM columns for one accumulator set: 3 and 4 limbs use N = 128.
@@ -488,9 +515,16 @@ static int tc_tile_n(const hdc_context* ctx, const hdc_refdb* db) {
     return db->L > 2 ? 128 : n;
 }
 
+// Two M-blocks per CTA need MB * L * N <= 512 TMEM columns: N = 128 and at most 2 limbs.
+static int tc_m_blocks(const hdc_context* ctx, const hdc_refdb* db) {
+    const int mb = ctx->tc_m_blocks > 0 ? ctx->tc_m_blocks : tc_default_m_blocks();
+    return (mb == 2 && db->L <= 2 && tc_tile_n(ctx, db) == 128) ? 2 : 1;
+}
+
 static void tc_plan(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int& n_qtiles, int& n_rtiles, int& G,
                     int& S, int& n_groups) {
-    n_qtiles = (int)((nq + kBM - 1) / kBM);
+    const int qt_rows = kBM * tc_m_blocks(ctx, db);
+    n_qtiles = (int)((nq + qt_rows - 1) / qt_rows);
     n_rtiles = (int)(db->r_pad / tc_tile_n(ctx, db));
     const int want = ctx->tc_group > 0 ? ctx->tc_group : tc_default_group();
     G = std::max(1, std::min(std::min(want, ctx->num_sms), n_qtiles));
@@ -506,14 +540,14 @@ size_t tc_workspace_bytes(const hdc_context* ctx, int64_t nq, const hdc_refdb* d
     return (size_t)S * nq * std::max(k, 1) * (sizeof(uint64_t) + sizeof(int64_t));
 }
 
-template <int L, int N>
+template <int L, int N, int MB>
 static int launch_tc_t(const __half* d_q, const hdc_refdb* db, const TcArgs& a, int grid, cudaStream_t stream) {
     CUtensorMap tmA, tmB;
     if (!make_tmap(&tmA, d_q, a.nq, a.dim, Tile<N>::BK, kBM) ||
         !make_tmap(&tmB, db->d_limbs, (int64_t)db->L * db->r_pad, a.dim, Tile<N>::BK, N))
         return fail(HDC_ERR_CUDA, "tc search: cuTensorMapEncodeTiled failed");
-    const size_t smem = (size_t)tc_stages<N>(L) * tc_stage_bytes<N>(L) + 1024;
-    auto kern = tc_search_kernel<L, N>;
+    const size_t smem = (size_t)tc_stages<N>(L, MB) * tc_stage_bytes<N>(L, MB) + 1024;
+    auto kern = tc_search_kernel<L, N, MB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_fail(e, "tc search: cudaFuncSetAttribute");
     kern<<<grid, kThreadsTC, smem, stream>>>(tmA, tmB, a);
@@ -556,19 +590,23 @@ int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, c
     a.policy = ctx->tc_policy >= 0 ? ctx->tc_policy : tc_default_policy();
     const int grid = a.G * a.S;
     int st;
+    const int MB = tc_m_blocks(ctx, db);
     if (N == 256) {
         switch (db->L) {
-            case 1: st = launch_tc_t<1, 256>(d_q, db, a, grid, stream); break;
-            case 2: st = launch_tc_t<2, 256>(d_q, db, a, grid, stream); break;
-            case 3: st = launch_tc_t<3, 256>(d_q, db, a, grid, stream); break;
-            default: st = launch_tc_t<4, 256>(d_q, db, a, grid, stream); break;
+            case 1: st = launch_tc_t<1, 256, 1>(d_q, db, a, grid, stream); break;
+            default: st = launch_tc_t<2, 256, 1>(d_q, db, a, grid, stream); break;
+        }
+    } else if (MB == 2) {
+        switch (db->L) {
+            case 1: st = launch_tc_t<1, 128, 2>(d_q, db, a, grid, stream); break;
+            default: st = launch_tc_t<2, 128, 2>(d_q, db, a, grid, stream); break;
         }
     } else {
         switch (db->L) {
-            case 1: st = launch_tc_t<1, 128>(d_q, db, a, grid, stream); break;
-            case 2: st = launch_tc_t<2, 128>(d_q, db, a, grid, stream); break;
-            case 3: st = launch_tc_t<3, 128>(d_q, db, a, grid, stream); break;
-            default: st = launch_tc_t<4, 128>(d_q, db, a, grid, stream); break;
+            case 1: st = launch_tc_t<1, 128, 1>(d_q, db, a, grid, stream); break;
+            case 2: st = launch_tc_t<2, 128, 1>(d_q, db, a, grid, stream); break;
+            case 3: st = launch_tc_t<3, 128, 1>(d_q, db, a, grid, stream); break;
+            default: st = launch_tc_t<4, 128, 1>(d_q, db, a, grid, stream); break;
         }
     }
     if (st != HDC_OK) return st;

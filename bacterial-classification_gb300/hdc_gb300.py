@@ -40,7 +40,7 @@ SIGNATURES = [
     ("hdc_refdb_destroy", None, [P]),
     ("hdc_refdb_limbs", I32, [P]),
     ("hdc_search_tc_workspace_bytes", SZ, [P, P, I64, I32]),
-    ("hdc_search_tc_tuning", I32, [P, I32, I32, I32]),
+    ("hdc_search_tc_tuning", I32, [P, I32, I32, I32, I32]),
     ("hdc_search_tc", I32, [P, P, P, P, I64, ctypes.c_int32, I32, I32, P, P, P, P, P, SZ, P]),
     ("hdc_synth_tree", I32, [ctypes.c_uint64, I64, I32, P, I32, I32, I32, P, I64, P, P, P, I32]),
     ("hdc_synth_copies", I32, [ctypes.c_uint64, P, P, P, I64, I32, ctypes.c_double, P, I64, P, P, I32]),
@@ -162,8 +162,8 @@ class Context:
         check(lib().hdc_context_status(self.h, ctypes.byref(st)))
         return st.value
 
-    def tc_tuning(self, group_tiles=0, l2_policy=-1, tile_n=0):
-        check(lib().hdc_search_tc_tuning(self.h, group_tiles, l2_policy, tile_n))
+    def tc_tuning(self, group_tiles=0, l2_policy=-1, tile_n=0, m_blocks=0):
+        check(lib().hdc_search_tc_tuning(self.h, group_tiles, l2_policy, tile_n, m_blocks))
 
     def refdb(self, refs, max_abs, stream=None):
         return RefDB(self, refs, max_abs, stream)

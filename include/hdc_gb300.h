@@ -194,9 +194,11 @@ int hdc_search_plain_noalloc(hdc_context* ctx, const int16_t* d_q, const int64_t
  * (SMs / group_tiles) CTAs, each group's reference tiles dealt round-robin
  * to the SMs / group_tiles lanes; l2_policy = 0 no L2 hint, 1 query tiles
  * loaded evict-last, 2 also reference tiles evict-first (-1: automatic);
- * tile_n = references per tile, 128 or 256 (0: automatic).  Results do not
- * depend on these settings, only the speed does. */
-int hdc_search_tc_tuning(hdc_context* ctx, int group_tiles, int l2_policy, int tile_n);
+ * tile_n = references per tile, 128 or 256 (0: automatic); m_blocks = query
+ * M-blocks of 128 rows per CTA sharing each reference tile, 1 or 2 (0:
+ * automatic; 2 needs tile_n 128 and at most 2 limbs).  Results do not depend
+ * on these settings, only the speed does. */
+int hdc_search_tc_tuning(hdc_context* ctx, int group_tiles, int l2_policy, int tile_n, int m_blocks);
 
 /* ---------------------------------------------------------------- (c) propagate */
 

@@ -20,16 +20,16 @@ def _setup(hdc, dev, refs, q_bipolar, dim):
     return ctx, db, tr, q16, qi, qn
 
 
-def _run_tc(ctx, db, q16, qn, maxq, k, mode, tile_n=0, group=0):
+def _run_tc(ctx, db, q16, qn, maxq, k, mode, tile_n=0, group=0, m_blocks=0):
     import torch
-    ctx.tc_tuning(group, -1, tile_n)
+    ctx.tc_tuning(group, -1, tile_n, m_blocks)
     s, i, c, d = ctx.search_tc(db, q16, qn, maxq, k, mode)
     torch.cuda.synchronize()
     assert ctx.status() == 0
     return s.cpu().numpy(), i.cpu().numpy(), c.cpu().numpy(), d.cpu().numpy()
 
 
-@pytest.mark.parametrize("tile_n,group", [(128, 0), (256, 0), (256, 3)])
+@pytest.mark.parametrize("tile_n,group,m_blocks", [(128, 0, 1), (128, 0, 2), (256, 0, 1), (128, 3, 2)])
 @pytest.mark.parametrize("dim,nq,nr,k,mode,vmax,dtype", [
     (1024, 200, 1000, 5, 0, 2000, np.int16),     # one fp16 limb (|v| <= 2048)
     (2048, 130, 3000, 10, 0, 12000, np.int16),   # two limbs (bundle of 8 copies)
@@ -40,7 +40,7 @@ def _run_tc(ctx, db, q16, qn, maxq, k, mode, tile_n=0, group=0):
     (640, 50, 400, 5, 0, 100000000, np.int32),   # three limbs, top limb ~ 24
     (10240, 129, 300, 5, 0, 12728, np.int16),    # precision-form dimension
 ])
-def test_tc_vs_oracle(hdc, orc, cuda, dim, nq, nr, k, mode, vmax, dtype, tile_n, group):
+def test_tc_vs_oracle(hdc, orc, cuda, dim, nq, nr, k, mode, vmax, dtype, tile_n, group, m_blocks):
     g = np.random.default_rng(dim + nq + nr)
     refs = g.integers(-vmax, vmax + 1, (nr, dim)).astype(dtype)
     refs[3] = refs[1]                       # tie: lower index first
@@ -50,7 +50,7 @@ def test_tc_vs_oracle(hdc, orc, cuda, dim, nq, nr, k, mode, vmax, dtype, tile_n,
     q = np.where(g.random((nq, dim)) < 0.5, -1, 1).astype(np.int8)
     q[0] = np.where(refs[1] >= 0, 1, -1)    # a query aligned with reference 1
     ctx, db, tr, q16, qi, qn = _setup(hdc, cuda, refs, q, dim)
-    s, i, c, d = _run_tc(ctx, db, q16, qn, 1, k, mode, tile_n, group)
+    s, i, c, d = _run_tc(ctx, db, q16, qn, 1, k, mode, tile_n, group, m_blocks)
     os_, oi, oc, od = orc.topk(q.astype(np.int32), refs.astype(np.int32), min(k, nr), mode)
     assert np.array_equal(i, oi)
     assert np.array_equal(d, od)
