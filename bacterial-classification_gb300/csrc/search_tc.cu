@@ -506,7 +506,7 @@ void refdb_destroy(hdc_refdb* db) {
 int tc_default_group() { return 1 << 30; }  // every SM on its own query tile, references shared
 int tc_default_policy() { return 0; }
 int tc_default_tile_n() { return 128; }
-int tc_default_m_blocks() { return 2; }
+int tc_default_m_blocks() { return 1; }
 
 // G query tiles per group (fewer for small batches) and S = SMs / G lanes.
 // N = 256 needs L * 256 TMEM columns for one accumulator set: 3 and 4 limbs use N = 128.

@@ -383,7 +383,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--config", default="c3", choices=sorted(CONFIGS))
     ap.add_argument("--form", default="tc", choices=["plain", "tc"])
-    ap.add_argument("--batch", type=int, default=32768)
+    ap.add_argument("--batch", type=int, default=0,
+                    help="reads per step; 0 = 2 x SMs x 128, whole waves of 128-query tensor-core tiles")
     ap.add_argument("--plain-batch", type=int, default=4096)
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain form beside the tc form")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -417,6 +418,9 @@ def main():
     import torch
     if world > 1:
         torch.distributed.init_process_group("nccl")
+    if args.batch <= 0:
+        sms = torch.cuda.get_device_properties(int(os.environ.get("LOCAL_RANK", 0))).multi_processor_count
+        args.batch = 2 * sms * 128
     r = run_ours(args, cfg, rank, world)
     if rank != 0:
         torch.distributed.destroy_process_group()
