@@ -59,5 +59,31 @@ def build(force=False, verbose=False):
     return LIB
 
 
+DROPIN = os.path.join(HERE, "dropin")
+
+
+def build_dropin(dim=1024, kmer=8, window=150, step=10, force=False):
+    """The GPU.cuh drop-in (dropin/gpu_dropin.cpp) and its self-check driver for
+    one compile-time configuration, linked against libhdc_gb300.so."""
+    lib = build(force=force)
+    out = os.path.join(OUT, "dropin_D%d_k%d_L%d_s%d" % (dim, kmer, window, step))
+    os.makedirs(out, exist_ok=True)
+    so = os.path.join(out, "libhdc_dropin.so")
+    exe = os.path.join(out, "selftest")
+    srcs = [os.path.join(DROPIN, f) for f in ("gpu_dropin.cpp", "selftest.cpp", "GPU.cuh", "config.h")]
+    newest = max([os.path.getmtime(x) for x in srcs] + [os.path.getmtime(lib)])
+    if not force and os.path.exists(exe) and os.path.getmtime(exe) >= newest:
+        return out
+    defs = ["-DHV_DIM=%d" % dim, "-DKMER_SIZE=%d" % kmer, "-DSEQUENCE_LENGTH=%d" % window, "-DSIM_STEP=%d" % step]
+    inc = ["-I" + DROPIN, "-I" + os.path.join(ROOT, "include")]
+    rpath = "-Wl,-rpath," + OUT + ":" + out
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared"] + defs + inc +
+                          [os.path.join(DROPIN, "gpu_dropin.cpp"), "-L" + OUT, "-lhdc_gb300", rpath, "-o", so])
+    subprocess.check_call(["g++", "-O2", "-std=c++17"] + defs + inc +
+                          [os.path.join(DROPIN, "selftest.cpp"), "-L" + out, "-lhdc_dropin", "-L" + OUT,
+                           "-lhdc_gb300", rpath, "-o", exe])
+    return out
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -234,4 +234,45 @@ int hdc_bundle(hdc_context* ctx, const void* d_rows, int elem_bytes, const int64
                               static_cast<cudaStream_t>(stream));
 }
 
+int hdc_propagate_greedy(hdc_context* ctx, const int16_t* d_hv, const int64_t* d_norm2, const int64_t* d_cand_ptr,
+                         const int32_t* d_cand_idx, const int64_t* d_rep_ptr, const int32_t* d_rep_idx,
+                         int64_t n_parents, double threshold, int score_mode, uint8_t* d_selected, float* d_best,
+                         int32_t* d_scratch, void* stream) {
+    if (!ctx) return fail(HDC_ERR_INVALID, "propagate: null context");
+    if (n_parents < 0) return fail(HDC_ERR_INVALID, "propagate: negative count");
+    if (n_parents == 0) return HDC_OK;
+    if (!hdc::valid_score_mode(score_mode)) return fail(HDC_ERR_INVALID, "propagate: bad score mode");
+    if (!d_hv || !d_norm2 || !d_cand_ptr || !d_cand_idx || !d_rep_ptr || !d_selected || !d_scratch)
+        return fail(HDC_ERR_INVALID, "propagate: null pointer");
+    return hdc::launch_propagate_greedy(ctx, d_hv, d_norm2, d_cand_ptr, d_cand_idx, d_rep_ptr, d_rep_idx, n_parents,
+                                        threshold, score_mode, d_selected, d_best, d_scratch,
+                                        static_cast<cudaStream_t>(stream));
+}
+
+int hdc_device_alloc(size_t bytes, void** out) {
+    if (!out) return fail(HDC_ERR_INVALID, "alloc: null output pointer");
+    *out = nullptr;
+    if (bytes == 0) return HDC_OK;
+    cudaError_t e = cudaMalloc(out, bytes);
+    return e == cudaSuccess ? HDC_OK : hdc::cuda_fail(e, "alloc: cudaMalloc");
+}
+
+int hdc_device_free(void* p) {
+    cudaError_t e = cudaFree(p);
+    return e == cudaSuccess ? HDC_OK : hdc::cuda_fail(e, "free: cudaFree");
+}
+
+int hdc_copy(void* dst, const void* src, size_t bytes, int to_device, void* stream) {
+    if (bytes == 0) return HDC_OK;
+    if (!dst || !src) return fail(HDC_ERR_INVALID, "copy: null pointer");
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, to_device ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost,
+                                    static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? HDC_OK : hdc::cuda_fail(e, "copy: cudaMemcpyAsync");
+}
+
+int hdc_stream_sync(void* stream) {
+    cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? HDC_OK : hdc::cuda_fail(e, "sync: cudaStreamSynchronize");
+}
+
 }  // extern "C"

@@ -81,6 +81,11 @@ int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, c
                      int32_t maxq, int k, int mode, float* d_score, int32_t* d_idx, double* d_cos, int64_t* d_dot,
                      void* d_work, size_t work_bytes, int* d_status, cudaStream_t stream);
 
+int launch_propagate_greedy(hdc_context* ctx, const int16_t* d_hv, const int64_t* d_norm2,
+                            const int64_t* d_cand_ptr, const int32_t* d_cand_idx, const int64_t* d_rep_ptr,
+                            const int32_t* d_rep_idx, int64_t n_parents, double threshold, int mode,
+                            uint8_t* d_selected, float* d_best, int32_t* d_scratch, cudaStream_t stream);
+
 int launch_bundle(hdc_context* ctx, const void* d_rows, int elem_bytes, const int64_t* d_child_ptr,
                   const int32_t* d_child_idx, int64_t n_parents, int32_t* d_out, cudaStream_t stream);
 

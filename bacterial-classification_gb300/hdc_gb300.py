@@ -25,6 +25,10 @@ SIGNATURES = [
     ("hdc_context_create", I32, [I32, I32, I32, I32, ctypes.POINTER(P)]),
     ("hdc_context_destroy", None, [P]),
     ("hdc_context_base_hvs", I32, [P, P]),
+    ("hdc_device_alloc", I32, [SZ, ctypes.POINTER(P)]),
+    ("hdc_device_free", I32, [P]),
+    ("hdc_copy", I32, [P, P, SZ, I32, P]),
+    ("hdc_stream_sync", I32, [P]),
     ("hdc_encode_segments", I32, [P, P, P, P, I64, ctypes.c_int32, I32, P, I64, P, P]),
     ("hdc_num_windows", I64, [P, I64]),
     ("hdc_encode_windows", I32, [P, P, P, P, I64, I64, P, P]),
@@ -33,6 +37,7 @@ SIGNATURES = [
     ("hdc_search_plain", I32, [P, P, P, I64, ctypes.c_int32, P, P, I64, ctypes.c_int32, I32, I32, P, P, P, P, P,
                                SZ, P]),
     ("hdc_bundle", I32, [P, P, I32, P, P, I64, P, P]),
+    ("hdc_propagate_greedy", I32, [P, P, P, P, P, P, P, I64, ctypes.c_double, I32, P, P, P, P]),
     ("hdc_context_status", I32, [P, ctypes.POINTER(ctypes.c_int)]),
     ("hdc_search_plain_noalloc", I32, [P, P, P, I64, ctypes.c_int32, P, P, I64, ctypes.c_int32, I32, I32, P, P, P,
                                        P, P]),
@@ -187,6 +192,18 @@ class Context:
         return out
 
     # ---------------------------------------------------------------- propagate
+    def propagate_greedy(self, hv, norm2, cand_ptr, cand_idx, rep_ptr, rep_idx, threshold=0.75, mode=SCORE_NORM,
+                         stream=None):
+        import torch
+        n = cand_idx.numel()
+        sel = torch.zeros(max(n, 1), dtype=torch.uint8, device=hv.device)
+        best = torch.zeros(max(n, 1), dtype=torch.float32, device=hv.device)
+        scratch = torch.empty(max(n, 1), dtype=torch.int32, device=hv.device)
+        check(lib().hdc_propagate_greedy(self.h, ptr(hv), ptr(norm2), ptr(cand_ptr), ptr(cand_idx), ptr(rep_ptr),
+                                         ptr(rep_idx), cand_ptr.numel() - 1, threshold, mode, ptr(sel), ptr(best),
+                                         ptr(scratch), stream_ptr(stream)))
+        return sel[:n], best[:n]
+
     def bundle(self, rows, child_ptr, child_idx, out=None, stream=None):
         import torch
         npar = child_ptr.numel() - 1

@@ -68,6 +68,14 @@ void hdc_context_destroy(hdc_context* ctx);
 /* The four base hypervectors in A,C,G,T order, [4][ceil(dim/64)] uint64 words (host). */
 int hdc_context_base_hvs(const hdc_context* ctx, uint64_t* host_out);
 
+/* Device memory and copies for callers without a CUDA runtime of their own
+ * (FFI bindings, the GPU.cuh drop-in).  hdc_copy copies host->device when
+ * to_device != 0, else device->host, asynchronously on `stream`. */
+int hdc_device_alloc(size_t bytes, void** out);
+int hdc_device_free(void* p);
+int hdc_copy(void* dst, const void* src, size_t bytes, int to_device, void* stream);
+int hdc_stream_sync(void* stream);
+
 /* ---------------------------------------------------------------- (a) encode */
 
 /* Encode n_segs byte segments d_bytes[d_seg_off[i] .. d_seg_off[i]+d_seg_len[i])
@@ -207,6 +215,22 @@ int hdc_search_tc_tuning(hdc_context* ctx, int group_tiles, int l2_policy, int t
  * exact int32.  Rows are int16 (elem_bytes 2) or int32 (4); out is int32. */
 int hdc_bundle(hdc_context* ctx, const void* d_rows, int elem_bytes, const int64_t* d_child_ptr,
                const int32_t* d_child_idx, int64_t n_parents, int32_t* d_out, void* stream);
+
+/* Greedy representative selection of propagate-children
+ * (targets/propogate-children.cpp:60-73), every parent of one rank at once.
+ * Parent p visits its candidates d_cand_idx[d_cand_ptr[p] .. d_cand_ptr[p+1])
+ * (indices into d_hv, the int16 whole-sequence hypervectors [n][dim] with
+ * squared norms d_norm2) in order; candidate x gets
+ *   best = max(0, max score(x, s) over the parent's existing sequences
+ *          d_rep_idx[d_rep_ptr[p] .. d_rep_ptr[p+1]) and the candidates
+ *          already appended)
+ * and is appended when (double)best < threshold (the reference uses 0.75 on
+ * the NORM scale).  d_selected[i] (uint8) and d_best[i] (float, optional)
+ * are per candidate slot; d_scratch holds one int32 per candidate slot. */
+int hdc_propagate_greedy(hdc_context* ctx, const int16_t* d_hv, const int64_t* d_norm2,
+                         const int64_t* d_cand_ptr, const int32_t* d_cand_idx, const int64_t* d_rep_ptr,
+                         const int32_t* d_rep_idx, int64_t n_parents, double threshold, int score_mode,
+                         uint8_t* d_selected, float* d_best, int32_t* d_scratch, void* stream);
 
 #ifdef __cplusplus
 }
