@@ -62,6 +62,10 @@ struct EncodeArgs {
     void* out;
     int64_t out_stride;
     int32_t* nkmers;
+    // length-binned work queue (optional): segments are taken in the order
+    // order[0], order[1], ... (longest first) from one counter per slab
+    const int32_t* order;
+    int* queue;  // [n_slabs] counters, zero at launch
 };
 
 __device__ __forceinline__ void csa(uint32_t& h, uint32_t& l, uint32_t a, uint32_t b, uint32_t c) {
@@ -150,7 +154,14 @@ __global__ void __launch_bounds__(kThreads) encode_kernel(const EncodeArgs a) {
     const int64_t gw = (int64_t)blockIdx.x * kWarps + warp, nw = (int64_t)gridDim.x * kWarps;
     const int w32 = slab * 32 + lane;
 
-    for (int64_t seg = gw; seg < a.n_segs; seg += nw) {
+    int64_t next = gw;
+    if (a.queue) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(a.queue + slab, 1);
+        next = __shfl_sync(0xffffffffu, t, 0);
+    }
+    for (int64_t pos_q = next; pos_q < a.n_segs;) {
+        const int64_t seg = a.order ? (int64_t)a.order[pos_q] : pos_q;
         int64_t start;
         int len;
         get_segment(a, seg, start, len);
@@ -230,6 +241,14 @@ __global__ void __launch_bounds__(kThreads) encode_kernel(const EncodeArgs a) {
         }
         nvalid = __reduce_add_sync(0xffffffffu, nvalid);
         if (a.nkmers && lane == 0 && slab == 0) a.nkmers[seg] = nvalid;
+        // next segment: from the queue, or a fixed stride over the grid
+        if (a.queue) {
+            int t = 0;
+            if (lane == 0) t = atomicAdd(a.queue + slab, 1);
+            pos_q = __shfl_sync(0xffffffffu, t, 0);
+        } else {
+            pos_q += nw;
+        }
         if (w32 >= a.W32) continue;
 
         // ---- counts -> output values, dims b and b+16 in 16-bit fields ----
@@ -316,9 +335,12 @@ int launch_np(const EncodeArgs& a, int nh, int grid_x, int n_slabs, size_t smem,
 
 }  // namespace
 
+int encode_slabs(const hdc_context* ctx) { return (ctx->words32 + 31) / 32; }
+
 int launch_encode(hdc_context* ctx, const char* d_bytes, const int64_t* d_seg_off, const int32_t* d_seg_len,
                   const int64_t* d_seq_off, const int64_t* d_win_off, int64_t n_seqs, int64_t n_segs, int out_kind,
-                  void* d_out, int64_t out_stride, int32_t* d_nkmers, int max_seg_len, cudaStream_t stream) {
+                  void* d_out, int64_t out_stride, int32_t* d_nkmers, int max_seg_len, cudaStream_t stream,
+                  const int32_t* d_order, int* d_queue) {
     if (n_segs == 0) return HDC_OK;
     EncodeArgs a{};
     a.base32 = ctx->d_base32;
@@ -352,6 +374,8 @@ int launch_encode(hdc_context* ctx, const char* d_bytes, const int64_t* d_seg_of
     a.out = d_out;
     a.out_stride = out_stride;
     a.nkmers = d_nkmers;
+    a.order = d_order;
+    a.queue = d_queue;
 
     // counters: ones..eights hold 0..15, NH higher planes hold multiples of 16
     const int64_t max_nk = max_seg_len > 0 ? std::max<int64_t>(0, (int64_t)max_seg_len - a.k + 1) : (int64_t)1 << 40;

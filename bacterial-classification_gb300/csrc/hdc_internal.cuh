@@ -51,7 +51,8 @@ inline bool valid_score_mode(int m) { return m == HDC_SCORE_NORM || m == HDC_SCO
 int launch_encode(hdc_context* ctx, const char* d_bytes, const int64_t* d_seg_off, const int32_t* d_seg_len,
                   const int64_t* d_seq_off, const int64_t* d_win_off, int64_t n_seqs, int64_t n_segs,
                   int out_kind, void* d_out, int64_t out_stride, int32_t* d_nkmers, int max_seg_len,
-                  cudaStream_t stream);
+                  cudaStream_t stream, const int32_t* d_order = nullptr, int* d_queue = nullptr);
+int encode_slabs(const hdc_context* ctx);
 
 int launch_norms(hdc_context* ctx, const void* d_hv, int elem_bytes, int64_t n, int64_t* d_norm2,
                  int32_t* d_maxabs, cudaStream_t stream);

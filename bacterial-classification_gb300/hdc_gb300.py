@@ -46,6 +46,13 @@ SIGNATURES = [
     ("hdc_refdb_limbs", I32, [P]),
     ("hdc_search_tc_workspace_bytes", SZ, [P, P, I64, I32]),
     ("hdc_search_tc_tuning", I32, [P, I32, I32, I32, I32]),
+    ("hdc_pipeline_create", I32, [P, P, I64, I64, ctypes.c_int32, I32, I32, ctypes.POINTER(P)]),
+    ("hdc_pipeline_destroy", None, [P]),
+    ("hdc_pipeline_run", I32, [P, P, P, P, I64, P, P]),
+    ("hdc_pipeline_launch_resident", I32, [P]),
+    ("hdc_pipeline_stream", P, [P]),
+    ("hdc_pipeline_autotune", I32, [P, ctypes.POINTER(I32), ctypes.POINTER(I32), ctypes.POINTER(I32),
+                                    ctypes.POINTER(I32), ctypes.POINTER(ctypes.c_float)]),
     ("hdc_search_tc", I32, [P, P, P, P, I64, ctypes.c_int32, I32, I32, P, P, P, P, P, SZ, P]),
     ("hdc_synth_tree", I32, [ctypes.c_uint64, I64, I32, P, I32, I32, I32, P, I64, P, P, P, I32]),
     ("hdc_synth_copies", I32, [ctypes.c_uint64, P, P, P, I64, I32, ctypes.c_double, P, I64, P, P, I32]),
@@ -227,6 +234,51 @@ class RefDB:
     def close(self):
         if self.h:
             lib().hdc_refdb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Pipeline:
+    """Batching form: CUDA-graph encode -> tensor-core search -> top-k over host batches."""
+
+    def __init__(self, ctx, db, max_reads, max_bytes, max_len, k, mode=SCORE_NORM):
+        import numpy as np
+        h = ctypes.c_void_p()
+        check(lib().hdc_pipeline_create(ctx.h, db.h, max_reads, max_bytes, max_len, k, mode, ctypes.byref(h)))
+        self.h, self.k, self.max_reads = h, min(k, db.nr), max_reads
+        self.ctx, self.db = ctx, db  # keep alive
+        self._np = np
+
+    def run(self, seqs, n=None):
+        np = self._np
+        n = len(seqs) if n is None else n
+        s = np.zeros((n, self.k), np.float32)
+        i = np.zeros((n, self.k), np.int32)
+        p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+        check(lib().hdc_pipeline_run(self.h, p(seqs.buf), p(seqs.off), p(seqs.len), n, p(s), p(i)))
+        return s, i
+
+    def launch_resident(self):
+        check(lib().hdc_pipeline_launch_resident(self.h))
+
+    def stream(self):
+        return lib().hdc_pipeline_stream(self.h)
+
+    def autotune(self):
+        g, pol, tn, mb = I32(), I32(), I32(), I32()
+        ms = ctypes.c_float()
+        check(lib().hdc_pipeline_autotune(self.h, ctypes.byref(g), ctypes.byref(pol), ctypes.byref(tn), ctypes.byref(mb),
+                                          ctypes.byref(ms)))
+        return dict(group_tiles=g.value, l2_policy=pol.value, tile_n=tn.value, m_blocks=mb.value, ms=ms.value)
+
+    def close(self):
+        if self.h:
+            lib().hdc_pipeline_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -42,6 +42,11 @@ CONFIGS = {
                tree_seed=2, read_seed=102, copy_seed=0),
     "c3": dict(n_leaves=200000, dim=10240, kmer=10, read_len=250, subst=0.01, topk=5, copies=8, bipolar=True,
                tree_seed=3, read_seed=103, copy_seed=203),
+    # batching form: the config-3 database, reads of log-normal length (median 250, sigma 0.5,
+    # clipped to 100-1600), 20 % of them with 6 % substitution:insertion:deletion = 3:1:1 errors
+    "c4": dict(n_leaves=200000, dim=10240, kmer=10, read_len=250, subst=0.01, topk=10, copies=8, bipolar=True,
+               tree_seed=3, read_seed=104, copy_seed=203, sigma=0.5, min_read=100, max_read=1600,
+               mixed_frac=0.2, mixed_rate=0.06),
 }
 
 
@@ -142,7 +147,9 @@ def build_database(H, ctx, cfg, dev):
 
 
 def make_reads(H, tree, cfg, n, seed):
-    return H.synth_reads(seed, tree, n, cfg["read_len"], subst=cfg["subst"])
+    return H.synth_reads(seed, tree, n, cfg["read_len"], subst=cfg["subst"], sigma=cfg.get("sigma", 0.0),
+                         min_read=cfg.get("min_read", 100), max_read=cfg.get("max_read", 1600),
+                         mixed_frac=cfg.get("mixed_frac", 0.0), mixed_rate=cfg.get("mixed_rate", 0.0))
 
 
 # ---------------------------------------------------------------------------- our arm
@@ -234,6 +241,52 @@ class _Null:
         return False
 
 
+def run_pipeline(args, cfg, rank, world, H, ctx, tree, refs, rn, maxr, dev):
+    """Batching form: the CUDA-graph pipeline over host batches of uneven reads."""
+    import torch
+    B, K = args.batch, cfg["topk"]
+    pool = [make_reads(H, tree, cfg, B, cfg["read_seed"] + 1000 * rank + p) for p in range(2)]
+    max_bytes = max(int(r.len.astype(np.int64).sum()) for r in pool) + 4096
+    db = ctx.refdb(refs, maxr)
+    pipe = H.Pipeline(ctx, db, B, max_bytes, cfg.get("max_read", cfg["read_len"]), K)
+    pipe.run(pool[0])
+    tuned = pipe.autotune()
+    # device-resident: replay encode + search on the staged batch, timed on the pipeline's stream
+    st = torch.cuda.ExternalStream(pipe.stream())
+    for _ in range(args.warmup):
+        pipe.launch_resident()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clk = ClockSampler(dev.index)
+    with clk:
+        e0.record(st)
+        for _ in range(args.steps):
+            pipe.launch_resident()
+        e1.record(st)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    # end to end: host batches through hdc_pipeline_run (host packing, copies, graph, copies back)
+    for i in range(args.warmup):
+        pipe.run(pool[i % 2])
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        pipe.run(pool[i % 2])
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    # the search kernel alone on the same batch, for the roofline
+    form = Form(H, ctx, cfg, "tc", refs, rn, maxr, B, dev)
+    d_buf = torch.from_numpy(pool[0].buf).to(dev)
+    bat = [(torch.from_numpy(pool[0].off).to(dev), torch.from_numpy(pool[0].len).to(dev))]
+    _, search_ms = time_form(form, bat, d_buf, 2, 3, 1)
+    if world > 1:
+        t = torch.tensor([ms, e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms, e2e_ms = float(t[0]), float(t[1])
+    return dict(ms=ms, e2e_ms=e2e_ms, search_ms=search_ms, clocks=clk.summary(), launches=4 * args.steps,
+                refs=refs.shape[0], limbs=db.limbs, h2d=max_bytes + B * 16, d2h=B * K * 8, tree=tree,
+                tuned=tuned, mean_len=float(np.mean(pool[0].len)),
+                refs_host=refs.cpu().numpy() if (rank == 0 and not args.no_cpu_baseline) else None)
+
+
 def run_ours(args, cfg, rank, world):
     import torch
     import hdc_gb300 as H
@@ -241,6 +294,8 @@ def run_ours(args, cfg, rank, world):
     torch.cuda.set_device(dev)
     ctx = H.Context(cfg["dim"], cfg["kmer"], cfg["read_len"], 10)
     tree, refs, rn, maxr = build_database(H, ctx, cfg, dev)
+    if args.form == "pipe":
+        return run_pipeline(args, cfg, rank, world, H, ctx, tree, refs, rn, maxr, dev)
     B = args.batch
     n_pool = 2
     reads = make_reads(H, tree, cfg, B * n_pool, cfg["read_seed"] + 1000 * rank)
@@ -382,7 +437,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--config", default="c3", choices=sorted(CONFIGS))
-    ap.add_argument("--form", default="tc", choices=["plain", "tc"])
+    ap.add_argument("--form", default="", choices=["", "plain", "tc", "pipe"],
+                    help="default: tc for c3, pipe for c4, plain for c2")
     ap.add_argument("--batch", type=int, default=0,
                     help="reads per step; 0 = 2 x SMs x 128, whole waves of 128-query tensor-core tiles")
     ap.add_argument("--plain-batch", type=int, default=4096)
@@ -395,12 +451,21 @@ def main():
         log("warmup raised to 3")
         args.warmup = 3
     cfg = dict(CONFIGS[args.config])
+    if not args.form:
+        args.form = {"c2": "plain", "c3": "tc", "c4": "pipe"}[args.config]
     if args.refs:
         cfg["n_leaves"] = args.refs
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
-    workload = "%s: %d refs D=%d k=%d, %d bp reads, top-%d" % (args.config, cfg["n_leaves"], cfg["dim"], cfg["kmer"],
-                                                               cfg["read_len"], cfg["topk"])
+    if cfg.get("sigma"):
+        reads_desc = "log-normal reads (median %d bp, sigma %.1f, %d-%d bp, %d%% with %d%% sub:ins:del 3:1:1)" % (
+            cfg["read_len"], cfg["sigma"], cfg["min_read"], cfg["max_read"], 100 * cfg["mixed_frac"],
+            100 * cfg["mixed_rate"])
+        workload = "%s: %d refs D=%d k=%d, %s, top-%d" % (args.config, cfg["n_leaves"], cfg["dim"], cfg["kmer"],
+                                                         reads_desc, cfg["topk"])
+    else:
+        workload = "%s: %d refs D=%d k=%d, %d bp reads, top-%d" % (args.config, cfg["n_leaves"], cfg["dim"], cfg["kmer"],
+                                                                   cfg["read_len"], cfg["topk"])
     metric = "reads/s encode+top-%d search" % cfg["topk"]
     if args.impl == "reference":
         if rank != 0:
@@ -429,7 +494,7 @@ def main():
     B = args.batch
     value = B * world / (r["ms"] / 1e3)
     dim, nr = cfg["dim"], r["refs"]
-    if args.form == "tc":
+    if args.form in ("tc", "pipe"):
         # tensor work per read: one fp16 MMA pass per limb, 2*D*R*limbs flops
         flops = 2.0 * dim * nr * r["limbs"] * B
         achieved = flops / (r["search_ms"] / 1e3) / 1e12
@@ -459,6 +524,9 @@ def main():
                 "d2h_bytes_per_step": r["d2h"]},
         "roofline": roof, "clocks": r["clocks"], "gpu_launches": r["launches"],
     }
+    if "tuned" in r:
+        line["config"]["autotuned_schedule"] = r["tuned"]
+        line["config"]["mean_read_len"] = r["mean_len"]
     if "plain" in r:
         line["plain_form"] = {"value": r["plain"]["value"], "unit": "reads/s", "batch_reads": r["plain"]["batch"],
                               "speedup_tc_over_plain": value / r["plain"]["value"],

@@ -57,6 +57,7 @@ extern "C" {
 
 typedef struct hdc_context hdc_context;
 typedef struct hdc_refdb hdc_refdb;
+typedef struct hdc_pipeline hdc_pipeline;
 
 const char* hdc_last_error(void);
 const char* hdc_status_string(int status);
@@ -207,6 +208,32 @@ int hdc_search_plain_noalloc(hdc_context* ctx, const int16_t* d_q, const int64_t
  * automatic; 2 needs tile_n 128 and at most 2 limbs).  Results do not depend
  * on these settings, only the speed does. */
 int hdc_search_tc_tuning(hdc_context* ctx, int group_tiles, int l2_policy, int tile_n, int m_blocks);
+
+/* ---------------------------------------------------------------- batching form */
+
+/* A reusable encode -> tensor-core search -> top-k pipeline for batches of up
+ * to max_reads reads of up to max_len bases (max_bytes in total) against a
+ * resident database, replayed as a CUDA graph: copies to the device, the
+ * encoder's length-binned work queue (longest read first), hdc_search_tc,
+ * copies back.  Reads are encoded to +1/-1 (ties to +1).  The encode()/
+ * cosine_search() pair of the reference (src/GPU.cuh) at stream scale; no
+ * single reference counterpart. */
+int hdc_pipeline_create(hdc_context* ctx, const hdc_refdb* db, int64_t max_reads, int64_t max_bytes,
+                        int32_t max_len, int k, int score_mode, hdc_pipeline** out);
+void hdc_pipeline_destroy(hdc_pipeline* p);
+/* Host reads bytes[off[i] .. off[i]+len[i]), i < n_reads <= max_reads; host
+ * outputs [n_reads][k].  Synchronous. */
+int hdc_pipeline_run(hdc_pipeline* p, const char* bytes, const int64_t* off, const int32_t* len, int64_t n_reads,
+                     float* scores, int32_t* idx);
+/* Replay encode + search on the batch already staged on the device, without
+ * copies, asynchronously on hdc_pipeline_stream(p). */
+int hdc_pipeline_launch_resident(hdc_pipeline* p);
+void* hdc_pipeline_stream(hdc_pipeline* p);
+/* Time the tensor-core schedules of hdc_search_tc_tuning on the pipeline's
+ * buffers, keep the fastest on the context and re-capture the graphs.
+ * Outputs (optional): the chosen knobs and the search time in ms. */
+int hdc_pipeline_autotune(hdc_pipeline* p, int* group_tiles, int* l2_policy, int* tile_n, int* m_blocks,
+                          float* ms);
 
 /* ---------------------------------------------------------------- (c) propagate */
 
