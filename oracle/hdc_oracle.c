@@ -298,6 +298,143 @@ int orc_encode_segments(int dim, int k, const char* buf, const int64_t* off, con
 }
 
 /* ------------------------------------------------------------------ */
+/* Fast CPU encoder for building large reference sets (the CPU-baseline  */
+/* database).  Same result as encode_one, checked bit for bit by the     */
+/* tests: binder words from per-part tables of pre-rotated, pre-XORed    */
+/* base fragments (parts of <= 4 digits), counts in 64-bit bit-sliced    */
+/* counters (ripple-carry add of each binder word).  Not used to time    */
+/* the reference path, which is encode_one.                              */
+/* ------------------------------------------------------------------ */
+typedef struct {
+    int dim, k, W, np;
+    int first[4], len[4];
+    uint64_t* tab[4]; /* [4^len][W] */
+} fast_tables;
+
+static void fast_init(fast_tables* f, const orc_tables* t) {
+    f->dim = t->dim;
+    f->k = t->k;
+    f->W = t->W;
+    f->np = (t->k + 3) / 4;
+    int first = 0;
+    for (int p = 0; p < f->np; ++p) {
+        int len = t->k / f->np + (p < t->k % f->np ? 1 : 0);
+        f->first[p] = first;
+        f->len[p] = len;
+        int rows = 1 << (2 * len);
+        f->tab[p] = (uint64_t*)calloc((size_t)rows * f->W, sizeof(uint64_t));
+        for (int r = 0; r < rows; ++r) {
+            uint64_t* o = f->tab[p] + (size_t)r * f->W;
+            if (p == 0)
+                for (int w = 0; w < f->W; ++w) o[w] = ~0ULL;
+            for (int d = 0; d < len; ++d) {
+                int c = (r >> (2 * (len - 1 - d))) & 3;
+                const uint64_t* rot = t->rot + ((size_t)(first + d) * 4 + c) * f->W;
+                for (int w = 0; w < f->W; ++w) o[w] ^= rot[w];
+            }
+        }
+        first += len;
+    }
+}
+
+static void fast_free(fast_tables* f) {
+    for (int p = 0; p < f->np; ++p) free(f->tab[p]);
+}
+
+/* counts[d] for d < dim into acc (int32), returns the number of k-mers */
+static int64_t fast_encode_one(const fast_tables* f, const char* seq, int64_t len, int32_t* acc, uint64_t* planes,
+                               int nplanes, uint64_t* word) {
+    const int W = f->W, k = f->k;
+    memset(planes, 0, sizeof(uint64_t) * (size_t)nplanes * W);
+    int64_t n = 0;
+    for (int64_t p = 0; p + k <= len; ++p) {
+        int64_t canon = orc_canonical(seq + p, k);
+        if (canon < 0) continue;
+        const uint64_t* rows[4];
+        for (int q = 0; q < f->np; ++q) {
+            int shift = 2 * (k - f->first[q] - f->len[q]);
+            rows[q] = f->tab[q] + (size_t)((canon >> shift) & ((1 << (2 * f->len[q])) - 1)) * W;
+        }
+        for (int w = 0; w < W; ++w) {
+            uint64_t x = rows[0][w];
+            for (int q = 1; q < f->np; ++q) x ^= rows[q][w];
+            word[w] = x;
+        }
+        for (int w = 0; w < W; ++w) { /* ripple-carry add into the bit-sliced counter */
+            uint64_t c = word[w];
+            for (int b = 0; b < nplanes && c; ++b) {
+                uint64_t t = planes[(size_t)b * W + w] & c;
+                planes[(size_t)b * W + w] ^= c;
+                c = t;
+            }
+        }
+        ++n;
+    }
+    for (int d = 0; d < f->dim; ++d) {
+        int32_t c = 0;
+        for (int b = 0; b < nplanes; ++b) c |= (int32_t)((planes[(size_t)b * W + (d >> 6)] >> (d & 63)) & 1) << b;
+        acc[d] = 2 * c - (int32_t)n;
+    }
+    return n;
+}
+
+typedef struct {
+    const fast_tables* f;
+    const char* buf;
+    const int64_t *off, *len;
+    int64_t n;
+    int group; /* rows summed per output row (bundles of noisy copies) */
+    int32_t* out;
+    int tid, nthreads;
+} fast_job;
+
+static void* fast_worker(void* arg) {
+    fast_job* j = (fast_job*)arg;
+    const int dim = j->f->dim, W = j->f->W;
+    const int nplanes = 17;
+    int32_t* acc = (int32_t*)malloc(sizeof(int32_t) * (size_t)dim);
+    uint64_t* planes = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)nplanes * W);
+    uint64_t* word = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)W);
+    const int64_t nout = j->n / j->group;
+    for (int64_t o = j->tid; o < nout; o += j->nthreads) {
+        int32_t* dst = j->out + (size_t)o * dim;
+        memset(dst, 0, sizeof(int32_t) * (size_t)dim);
+        for (int g = 0; g < j->group; ++g) {
+            int64_t s = o * j->group + g;
+            fast_encode_one(j->f, j->buf + j->off[s], j->len[s], acc, planes, nplanes, word);
+            for (int d = 0; d < dim; ++d) dst[d] += acc[d];
+        }
+    }
+    free(word);
+    free(planes);
+    free(acc);
+    return NULL;
+}
+
+/* Encode n segments (exact int32 counts; segments of < 2^17 k-mers) and sum
+ * them in consecutive groups of `group` into out [n/group][dim]. */
+int orc_encode_bundles(int dim, int k, const char* buf, const int64_t* off, const int64_t* len, int64_t n, int group,
+                       int32_t* out, int nthreads) {
+    if (group < 1 || n % group) return -1;
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    orc_tables t;
+    tables_init(&t, dim, k);
+    fast_tables f;
+    fast_init(&f, &t);
+    pthread_t th[256];
+    fast_job jobs[256];
+    for (int i = 0; i < nthreads; ++i) {
+        jobs[i] = (fast_job){&f, buf, off, len, n, group, out, i, nthreads};
+        pthread_create(&th[i], NULL, fast_worker, &jobs[i]);
+    }
+    for (int i = 0; i < nthreads; ++i) pthread_join(th[i], NULL);
+    fast_free(&f);
+    tables_free(&t);
+    return 0;
+}
+
+/* ------------------------------------------------------------------ */
 /* Cosine and ranking                                                  */
 /* ------------------------------------------------------------------ */
 enum { ORC_SCORE_NORM = 0, ORC_SCORE_COS = 1, ORC_SCORE_DOT = 2 };

@@ -38,6 +38,7 @@ def lib():
         L.orc_topk_i32.argtypes = [P, i64, P, i64, i32, i32, i32, P, P, P, P, i32]
         L.orc_classify.argtypes = [i32, i32, P, P, P, i64, P, i32, i64, i32, i32, i32, P, P, i32]
         L.orc_bundle.argtypes = [P, i32, P, P, i64, P]
+        L.orc_encode_bundles.argtypes = [i32, i32, P, P, P, i64, i32, P, i32]
         L.orc_propagate_greedy.argtypes = [P, i64, P, i64, i32, ctypes.c_double, i32, P, P]
         L.orc_propagate_greedy.restype = i32
         _lib = L
@@ -97,6 +98,20 @@ def encode(seqs, dim, k, out="int16", nthreads=None):
     lib().orc_encode_segments(dim, k, _p(buf), _p(offs), _p(lens), n, kind, _p(res), _p(nk),
                               nthreads or nthreads_default())
     return res, nk
+
+
+def encode_bundles(buf, off, lens, dim, k, group=1, nthreads=None):
+    """Fast CPU encoder for large reference sets: exact int32 encodings of the
+    segments buf[off[i]:off[i]+lens[i]], summed in consecutive groups."""
+    buf = np.ascontiguousarray(buf, np.uint8)
+    off = np.ascontiguousarray(off, np.int64)
+    lens = np.ascontiguousarray(lens, np.int64)
+    n = len(off)
+    out = np.zeros((n // group, dim), np.int32)
+    if lib().orc_encode_bundles(dim, k, _p(buf), _p(off), _p(lens), n, group, _p(out),
+                                nthreads or nthreads_default()) != 0:
+        raise ValueError("encode_bundles: bad group")
+    return out
 
 
 def window_segments(seqs, window, step):

@@ -92,3 +92,19 @@ def test_simtest_pairs(orc):
     assert np.array_equal(np.array(got, np.float32), np.array(meta["cosine"], np.float32))
     for i in range(n):  # self-similarity prints 1.000000 in the reference
         assert got[i * n + i] == np.float32(1.0)
+
+
+def test_fast_bundle_encoder_matches_oracle(orc):
+    """The fast CPU encoder used only to build large reference sets for the
+    CPU baseline equals the oracle's encoder bit for bit (and sums groups)."""
+    import random
+    rng = random.Random(9)
+    seqs = ["".join(rng.choice("ACGT") for _ in range(rng.randint(0, 900))) for _ in range(40)]
+    seqs += ["ACGTNNACGTacgtACGTACGTAGCTAGCTAGCT" * 5, "A" * 9, ""]
+    buf, off, ln = orc.pack_segments(seqs)
+    for dim, k in [(1024, 8), (200, 3), (2048, 10), (4096, 12), (512, 16)]:
+        ref, _ = orc.encode(seqs, dim, k, "int32")
+        assert np.array_equal(orc.encode_bundles(buf, off, ln, dim, k), ref), (dim, k)
+    ref, _ = orc.encode(seqs[:40], 1024, 8, "int32")
+    got = orc.encode_bundles(buf, off[:40], ln[:40], 1024, 8, group=8)
+    assert np.array_equal(got, ref.reshape(5, 8, -1).sum(1))
