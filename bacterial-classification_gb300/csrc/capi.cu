@@ -249,6 +249,22 @@ int hdc_propagate_greedy(hdc_context* ctx, const int16_t* d_hv, const int64_t* d
                                         static_cast<cudaStream_t>(stream));
 }
 
+int hdc_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qnorm2, int64_t nq, const int32_t* d_proto,
+                    const int64_t* d_proto_norm2, const int64_t* d_child_ptr, const int32_t* d_child_idx,
+                    const int32_t* d_roots, int n_roots, int levels, int beam, double threshold, int score_mode,
+                    int32_t* d_path, float* d_path_score, int32_t* d_depth, void* stream) {
+    if (!ctx) return fail(HDC_ERR_INVALID, "beam: null context");
+    if (nq < 0) return fail(HDC_ERR_INVALID, "beam: negative count");
+    if (nq == 0) return HDC_OK;
+    if (!hdc::valid_score_mode(score_mode)) return fail(HDC_ERR_INVALID, "beam: bad score mode");
+    if (!d_q || !d_qnorm2 || !d_proto || !d_proto_norm2 || !d_child_ptr || !d_child_idx || !d_roots || !d_path ||
+        !d_path_score || !d_depth)
+        return fail(HDC_ERR_INVALID, "beam: null pointer");
+    return hdc::launch_beam_search(ctx, d_q, d_qnorm2, nq, d_proto, d_proto_norm2, d_child_ptr, d_child_idx, d_roots,
+                                   n_roots, levels, beam, threshold, score_mode, d_path, d_path_score, d_depth,
+                                   static_cast<cudaStream_t>(stream));
+}
+
 int hdc_device_alloc(size_t bytes, void** out) {
     if (!out) return fail(HDC_ERR_INVALID, "alloc: null output pointer");
     *out = nullptr;

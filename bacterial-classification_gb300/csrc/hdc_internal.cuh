@@ -87,6 +87,11 @@ int launch_propagate_greedy(hdc_context* ctx, const int16_t* d_hv, const int64_t
                             const int32_t* d_rep_idx, int64_t n_parents, double threshold, int mode,
                             uint8_t* d_selected, float* d_best, int32_t* d_scratch, cudaStream_t stream);
 
+int launch_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn, int64_t nq, const int32_t* d_proto,
+                       const int64_t* d_pn, const int64_t* d_child_ptr, const int32_t* d_child_idx,
+                       const int32_t* d_roots, int n_roots, int levels, int beam, double threshold, int mode,
+                       int32_t* d_path, float* d_path_score, int32_t* d_depth, cudaStream_t stream);
+
 int launch_bundle(hdc_context* ctx, const void* d_rows, int elem_bytes, const int64_t* d_child_ptr,
                   const int32_t* d_child_idx, int64_t n_parents, int32_t* d_out, cudaStream_t stream);
 

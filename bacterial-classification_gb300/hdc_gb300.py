@@ -37,6 +37,7 @@ SIGNATURES = [
     ("hdc_search_plain", I32, [P, P, P, I64, ctypes.c_int32, P, P, I64, ctypes.c_int32, I32, I32, P, P, P, P, P,
                                SZ, P]),
     ("hdc_bundle", I32, [P, P, I32, P, P, I64, P, P]),
+    ("hdc_beam_search", I32, [P, P, P, I64, P, P, P, P, P, I32, I32, I32, ctypes.c_double, I32, P, P, P, P]),
     ("hdc_propagate_greedy", I32, [P, P, P, P, P, P, P, I64, ctypes.c_double, I32, P, P, P, P]),
     ("hdc_context_status", I32, [P, ctypes.POINTER(ctypes.c_int)]),
     ("hdc_search_plain_noalloc", I32, [P, P, P, I64, ctypes.c_int32, P, P, I64, ctypes.c_int32, I32, I32, P, P, P,
@@ -210,6 +211,18 @@ class Context:
                                          ptr(rep_idx), cand_ptr.numel() - 1, threshold, mode, ptr(sel), ptr(best),
                                          ptr(scratch), stream_ptr(stream)))
         return sel[:n], best[:n]
+
+    def beam_search(self, q, qn, proto, pn, child_ptr, child_idx, roots, levels=6, beam=5, threshold=0.0,
+                    mode=SCORE_NORM, stream=None):
+        import torch
+        nq = q.shape[0]
+        path = torch.empty((nq, levels), dtype=torch.int32, device=q.device)
+        score = torch.empty((nq, levels), dtype=torch.float32, device=q.device)
+        depth = torch.empty(nq, dtype=torch.int32, device=q.device)
+        check(lib().hdc_beam_search(self.h, ptr(q), ptr(qn), nq, ptr(proto), ptr(pn), ptr(child_ptr), ptr(child_idx),
+                                    ptr(roots), roots.numel(), levels, beam, threshold, mode, ptr(path), ptr(score),
+                                    ptr(depth), stream_ptr(stream)))
+        return path, score, depth
 
     def bundle(self, rows, child_ptr, child_idx, out=None, stream=None):
         import torch

@@ -209,6 +209,23 @@ int hdc_search_plain_noalloc(hdc_context* ctx, const int16_t* d_q, const int64_t
  * on these settings, only the speed does. */
 int hdc_search_tc_tuning(hdc_context* ctx, int group_tiles, int l2_policy, int tile_n, int m_blocks);
 
+/* Hierarchical descent (config 5; targets/identify.cpp:89-202 with one
+ * prototype hypervector per taxonomy node): beam search of +1/-1 int8 read
+ * hypervectors [nq][dim] down a tree whose nodes carry int32 prototypes
+ * d_proto [n_nodes][dim] (squared norms d_proto_norm2), children in CSR
+ * (d_child_ptr, d_child_idx).  Level 0 scores d_roots; every later level
+ * scores the children of the beam entries (a node without children scores
+ * itself again), ranks them by score (ties to the lower node index), stops
+ * when the best score is below threshold (the reference uses 0 on the NORM
+ * scale) and keeps the entries scoring >= threshold, at most `beam` (<= 8).
+ * Outputs per read: the best path d_path [nq][levels] (-1 past its depth),
+ * its per-level scores, and its depth.  levels <= 8; dim % 4 == 0. */
+int hdc_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qnorm2, int64_t nq,
+                    const int32_t* d_proto, const int64_t* d_proto_norm2, const int64_t* d_child_ptr,
+                    const int32_t* d_child_idx, const int32_t* d_roots, int n_roots, int levels, int beam,
+                    double threshold, int score_mode, int32_t* d_path, float* d_path_score, int32_t* d_depth,
+                    void* stream);
+
 /* ---------------------------------------------------------------- batching form */
 
 /* A reusable encode -> tensor-core search -> top-k pipeline for batches of up

@@ -453,6 +453,11 @@ static double cos_from(int64_t dot, int64_t nl, int64_t nr) {
     return (double)dot / (sqrt((double)nl) * sqrt((double)nr));
 }
 
+/* The reference float score for given exact dots and squared norms (vectorised). */
+void orc_scores_from(const int64_t* dot, const int64_t* nl, const int64_t* nr, int64_t n, int mode, float* out) {
+    for (int64_t i = 0; i < n; ++i) out[i] = score_from(dot[i], nl[i], nr[i], mode);
+}
+
 float orc_cosine_i32(const int32_t* l, const int32_t* r, int dim, int mode) {
     int64_t dot = 0, nl = 0, nr = 0;
     for (int i = 0; i < dim; ++i) {

@@ -39,6 +39,7 @@ def lib():
         L.orc_classify.argtypes = [i32, i32, P, P, P, i64, P, i32, i64, i32, i32, i32, P, P, i32]
         L.orc_bundle.argtypes = [P, i32, P, P, i64, P]
         L.orc_encode_bundles.argtypes = [i32, i32, P, P, P, i64, i32, P, i32]
+        L.orc_scores_from.argtypes = [P, P, P, i64, i32, P]
         L.orc_propagate_greedy.argtypes = [P, i64, P, i64, i32, ctypes.c_double, i32, P, P]
         L.orc_propagate_greedy.restype = i32
         _lib = L
@@ -180,3 +181,55 @@ def propagate_greedy(reps, cands, threshold=0.75, mode=SCORE_NORM):
     lib().orc_propagate_greedy(_p(reps), reps.shape[0], _p(cands), cands.shape[0], cands.shape[1],
                                threshold, mode, _p(sel), _p(best))
     return sel.astype(bool), best
+
+
+def scores_from(dot, nl, nr, mode=SCORE_NORM):
+    """Reference float scores from exact int64 dots and squared norms."""
+    dot = np.ascontiguousarray(dot, np.int64).ravel()
+    nl = np.ascontiguousarray(np.broadcast_to(nl, dot.shape), np.int64)
+    nr = np.ascontiguousarray(np.broadcast_to(nr, dot.shape), np.int64)
+    out = np.zeros(dot.shape, np.float32)
+    lib().orc_scores_from(_p(dot), _p(nl), _p(nr), dot.size, mode, _p(out))
+    return out
+
+
+def beam_search(q, proto, child_ptr, child_idx, roots, levels=6, beam=5, threshold=0.0, mode=SCORE_NORM):
+    """Beam descent of targets/identify.cpp:89-202 with one prototype per node:
+    level 0 scores `roots`; each later level expands every beam entry to its
+    children (a node without children to itself, :28-33); candidates are
+    ranked by score with ties to the lower node index; a read stops with its
+    best path when the best score is below threshold (:257-269), else keeps
+    the entries with score >= threshold, at most `beam` (:271-279).
+    Returns per read (path list, score list)."""
+    q = np.asarray(q, np.int64)
+    proto = np.asarray(proto, np.int64)
+    pn = (proto * proto).sum(1)
+    out = []
+    for r in range(q.shape[0]):
+        qn = int((q[r] * q[r]).sum())
+        beams = [([], [])]
+        result = None
+        for L in range(levels):
+            cands = []
+            for path, sc in beams:
+                if L == 0:
+                    kids = list(roots)
+                else:
+                    node = path[-1]
+                    kids = list(child_idx[child_ptr[node]:child_ptr[node + 1]]) or [node]
+                for c in kids:
+                    cands.append((path, sc, int(c)))
+            nodes = np.array([c[2] for c in cands], np.int64)
+            dots = proto[nodes] @ q[r]
+            s = scores_from(dots, qn, pn[nodes], mode)
+            order = sorted(range(len(cands)), key=lambda i: (-float(s[i]), int(nodes[i])))
+            ranked = [(cands[i][0] + [cands[i][2]], cands[i][1] + [float(s[i])]) for i in order]
+            if not ranked or ranked[0][1][-1] < threshold:
+                result = ranked[0] if ranked else beams[0]
+                break
+            keep = [e for e in ranked[:beam] if e[1][-1] >= threshold]
+            beams = keep
+            if L == levels - 1:
+                result = beams[0]
+        out.append(result)
+    return out

@@ -1,0 +1,70 @@
+"""Hierarchical descent (config 5 shape): beam search of bipolar reads down
+a bundled taxonomy (leaf encodings, internal nodes = exact int32 sums of
+their children) against the oracle's restatement of targets/identify.cpp's
+level loop: identical paths, per-level scores and stopping depths."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _tree_csr(n_leaves, b):
+    """Nodes of all ranks (rank 1..6) numbered level by level; the layout of
+    hdc_synth_tree (node j of rank r has parent j // b)."""
+    counts = []
+    for r in range(1, 7):
+        span = b ** (6 - r)
+        counts.append((n_leaves + span - 1) // span)
+    base = np.cumsum([0] + counts)
+    children = [[] for _ in range(base[-1])]
+    for r in range(1, 6):
+        for j in range(counts[r]):
+            children[base[r - 1] + j // b].append(base[r] + j)
+    ptr = np.zeros(base[-1] + 1, np.int64)
+    ptr[1:] = np.cumsum([len(c) for c in children])
+    idx = np.array([x for c in children for x in c], np.int32)
+    return base, counts, ptr, idx
+
+
+@pytest.mark.parametrize("dim,kmer,n_leaves,beam,threshold", [(1024, 10, 200, 5, 0.0), (2048, 12, 300, 3, 0.0),
+                                                              (1024, 8, 150, 5, 0.6)])
+def test_beam_descent_matches_oracle(hdc, orc, cuda, dim, kmer, n_leaves, beam, threshold):
+    import torch
+    H = hdc
+    b = 1
+    while b ** 6 < n_leaves:
+        b += 1
+    tree = H.synth_tree(41 + n_leaves, n_leaves)
+    reads = H.synth_reads(42, tree, 64, 250, subst=0.01, sigma=0.5, min_read=100, max_read=800,
+                          mixed_frac=0.2, mixed_rate=0.06)
+    ctx = H.Context(dim, kmer, 250, 10)
+    base, counts, ptr, idx = _tree_csr(n_leaves, b)
+    n_nodes = int(base[-1])
+    proto = torch.zeros((n_nodes, dim), dtype=torch.int32, device=cuda)
+    leaves = proto[int(base[5]):]
+    ctx.encode_segments(torch.from_numpy(tree.buf).to(cuda), torch.from_numpy(tree.off).to(cuda),
+                        torch.from_numpy(tree.len).to(cuda), leaves, H.OUT_I32, tree.max_len())
+    for r in range(4, -1, -1):  # internal nodes: bundles of their children, bottom-up
+        lo, hi = int(base[r]), int(base[r + 1])
+        cp = torch.from_numpy(ptr[lo:hi + 1].copy()).to(cuda)
+        proto[lo:hi] = ctx.bundle(proto, cp, torch.from_numpy(idx).to(cuda))
+    q16 = torch.empty((len(reads), dim), dtype=torch.int16, device=cuda)
+    ctx.encode_segments(torch.from_numpy(reads.buf).to(cuda), torch.from_numpy(reads.off).to(cuda),
+                        torch.from_numpy(reads.len).to(cuda), q16, H.OUT_BIPOLAR_I16, reads.max_len())
+    q8 = q16.to(torch.int8)
+    qn = ctx.norms(q16)
+    pn = ctx.norms(proto)
+    roots = torch.arange(0, counts[0], dtype=torch.int32, device=cuda)
+    path, score, depth = ctx.beam_search(q8, qn, proto, pn, torch.from_numpy(ptr).to(cuda),
+                                         torch.from_numpy(idx).to(cuda), roots, 6, beam, threshold)
+    torch.cuda.synchronize()
+    want = orc.beam_search(q8.cpu().numpy(), proto.cpu().numpy(), ptr, idx, list(range(counts[0])), 6, beam,
+                           threshold)
+    path, score, depth = path.cpu().numpy(), score.cpu().numpy(), depth.cpu().numpy()
+    for r, (wp, ws) in enumerate(want):
+        assert depth[r] == len(wp), r
+        assert list(path[r, :len(wp)]) == wp, r
+        assert np.array_equal(score[r, :len(wp)], np.array(ws, np.float32)), r
+    # most reads descend to a leaf of their own lineage
+    label_leaf = base[5] + reads.label
+    assert (path[:, 5] == label_leaf).mean() > 0.5 if threshold == 0.0 else True
