@@ -70,7 +70,8 @@ def build_dropin(dim=1024, kmer=8, window=150, step=10, force=False):
     os.makedirs(out, exist_ok=True)
     so = os.path.join(out, "libhdc_dropin.so")
     exe = os.path.join(out, "selftest")
-    srcs = [os.path.join(DROPIN, f) for f in ("gpu_dropin.cpp", "selftest.cpp", "GPU.cuh", "config.h")]
+    srcs = [os.path.join(DROPIN, f) for f in ("gpu_dropin.cpp", "selftest.cpp", "GPU.cuh", "config.h",
+                                             "hierarchy.cpp", "hierarchy.h", "propagate_gpu.cpp")]
     newest = max([os.path.getmtime(x) for x in srcs] + [os.path.getmtime(lib)])
     if not force and os.path.exists(exe) and os.path.getmtime(exe) >= newest:
         return out
@@ -82,6 +83,9 @@ def build_dropin(dim=1024, kmer=8, window=150, step=10, force=False):
     subprocess.check_call(["g++", "-O2", "-std=c++17"] + defs + inc +
                           [os.path.join(DROPIN, "selftest.cpp"), "-L" + out, "-lhdc_dropin", "-L" + OUT,
                            "-lhdc_gb300", rpath, "-o", exe])
+    subprocess.check_call(["g++", "-O2", "-std=c++20"] + defs + inc +
+                          [os.path.join(DROPIN, "propagate_gpu.cpp"), os.path.join(DROPIN, "hierarchy.cpp"),
+                           "-L" + OUT, "-lhdc_gb300", rpath, "-o", os.path.join(out, "propagate-children")])
     return out
 
 
