@@ -63,17 +63,19 @@ DROPIN = os.path.join(HERE, "dropin")
 
 
 def build_dropin(dim=1024, kmer=8, window=150, step=10, force=False):
-    """The GPU.cuh drop-in (dropin/gpu_dropin.cpp) and its self-check driver for
-    one compile-time configuration, linked against libhdc_gb300.so."""
+    """The GPU.cuh drop-in (dropin/gpu_dropin.cpp), its self-check driver and
+    the GPU propagate-children and identify applications for one compile-time
+    configuration, linked against libhdc_gb300.so."""
     lib = build(force=force)
     out = os.path.join(OUT, "dropin_D%d_k%d_L%d_s%d" % (dim, kmer, window, step))
     os.makedirs(out, exist_ok=True)
     so = os.path.join(out, "libhdc_dropin.so")
     exe = os.path.join(out, "selftest")
     srcs = [os.path.join(DROPIN, f) for f in ("gpu_dropin.cpp", "selftest.cpp", "GPU.cuh", "config.h",
-                                             "hierarchy.cpp", "hierarchy.h", "propagate_gpu.cpp")]
+                                             "hierarchy.cpp", "hierarchy.h", "propagate_gpu.cpp", "identify_gpu.cpp")]
     newest = max([os.path.getmtime(x) for x in srcs] + [os.path.getmtime(lib)])
-    if not force and os.path.exists(exe) and os.path.getmtime(exe) >= newest:
+    last = os.path.join(out, "identify")  # built last
+    if not force and os.path.exists(last) and os.path.getmtime(last) >= newest:
         return out
     defs = ["-DHV_DIM=%d" % dim, "-DKMER_SIZE=%d" % kmer, "-DSEQUENCE_LENGTH=%d" % window, "-DSIM_STEP=%d" % step]
     inc = ["-I" + DROPIN, "-I" + os.path.join(ROOT, "include")]
@@ -86,6 +88,9 @@ def build_dropin(dim=1024, kmer=8, window=150, step=10, force=False):
     subprocess.check_call(["g++", "-O2", "-std=c++20"] + defs + inc +
                           [os.path.join(DROPIN, "propagate_gpu.cpp"), os.path.join(DROPIN, "hierarchy.cpp"),
                            "-L" + OUT, "-lhdc_gb300", rpath, "-o", os.path.join(out, "propagate-children")])
+    subprocess.check_call(["g++", "-O2", "-std=c++20"] + defs + inc +
+                          [os.path.join(DROPIN, "identify_gpu.cpp"), os.path.join(DROPIN, "hierarchy.cpp"),
+                           "-L" + OUT, "-lhdc_gb300", rpath, "-o", os.path.join(out, "identify")])
     return out
 
 

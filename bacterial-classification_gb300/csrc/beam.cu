@@ -12,8 +12,8 @@
 //   score (ties to the lower node index, where the reference's std::sort
 //   leaves the order unspecified), and when the best score is below the
 //   threshold the read stops with that best path (targets/identify.cpp:
-//   257-269); otherwise the entries with score >= threshold, at most `beam`
-//   of them, go on.  After `levels` levels the best entry's path is returned.
+//   174-189); otherwise the entries with score >= threshold, at most `beam`
+//   of them, go on (:191-199).  After `levels` levels the best entry's path is returned.
 //
 // One warp per read: the read's +1/-1 hypervector stays in L1 while the warp
 // streams each candidate prototype with coalesced 16-byte loads; dots are

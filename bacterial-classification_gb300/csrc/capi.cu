@@ -265,6 +265,39 @@ int hdc_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qnorm2
                                    static_cast<cudaStream_t>(stream));
 }
 
+int hdc_similarity(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qnorm2, const int16_t* d_rows,
+                   const int64_t* d_row_norm2, const int64_t* d_ref_rows, const uint8_t* d_ref_whole,
+                   const int32_t* d_pair_q, const int32_t* d_pair_ref, int64_t n_pairs, int score_mode,
+                   float* d_score, int32_t* d_window, void* stream) {
+    if (!ctx) return fail(HDC_ERR_INVALID, "similarity: null context");
+    if (n_pairs < 0) return fail(HDC_ERR_INVALID, "similarity: negative count");
+    if (n_pairs == 0) return HDC_OK;
+    if (!hdc::valid_score_mode(score_mode)) return fail(HDC_ERR_INVALID, "similarity: bad score mode");
+    if (!d_q || !d_qnorm2 || !d_rows || !d_row_norm2 || !d_ref_rows || !d_pair_q || !d_pair_ref || !d_score ||
+        !d_window)
+        return fail(HDC_ERR_INVALID, "similarity: null pointer");
+    return hdc::launch_similarity(ctx, d_q, d_qnorm2, d_rows, d_row_norm2, d_ref_rows, d_ref_whole, d_pair_q,
+                                  d_pair_ref, n_pairs, score_mode, d_score, d_window,
+                                  static_cast<cudaStream_t>(stream));
+}
+
+int hdc_identify(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qnorm2, int64_t nq, const int16_t* d_rows,
+                 const int64_t* d_row_norm2, const int64_t* d_node_rows, const int64_t* d_child_ptr,
+                 const int32_t* d_child_idx, const int32_t* d_roots, int n_roots, int levels, int beam,
+                 double threshold, int score_mode, int32_t* d_path, float* d_path_score, int32_t* d_depth,
+                 int32_t* d_stop_level, void* stream) {
+    if (!ctx) return fail(HDC_ERR_INVALID, "identify: null context");
+    if (nq < 0) return fail(HDC_ERR_INVALID, "identify: negative count");
+    if (nq == 0) return HDC_OK;
+    if (!hdc::valid_score_mode(score_mode)) return fail(HDC_ERR_INVALID, "identify: bad score mode");
+    if (!d_q || !d_qnorm2 || !d_rows || !d_row_norm2 || !d_node_rows || !d_child_ptr || !d_child_idx ||
+        (n_roots > 0 && !d_roots) || !d_path || !d_path_score || !d_depth)
+        return fail(HDC_ERR_INVALID, "identify: null pointer");
+    return hdc::launch_identify(ctx, d_q, d_qnorm2, nq, d_rows, d_row_norm2, d_node_rows, d_child_ptr, d_child_idx,
+                                d_roots, n_roots, levels, beam, threshold, score_mode, d_path, d_path_score, d_depth,
+                                d_stop_level, static_cast<cudaStream_t>(stream));
+}
+
 int hdc_device_alloc(size_t bytes, void** out) {
     if (!out) return fail(HDC_ERR_INVALID, "alloc: null output pointer");
     *out = nullptr;

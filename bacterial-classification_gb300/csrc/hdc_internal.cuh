@@ -92,6 +92,17 @@ int launch_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn,
                        const int32_t* d_roots, int n_roots, int levels, int beam, double threshold, int mode,
                        int32_t* d_path, float* d_path_score, int32_t* d_depth, cudaStream_t stream);
 
+int launch_identify(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qn, int64_t nq, const int16_t* d_rows,
+                    const int64_t* d_rn, const int64_t* d_node_rows, const int64_t* d_child_ptr,
+                    const int32_t* d_child_idx, const int32_t* d_roots, int n_roots, int levels, int beam,
+                    double threshold, int mode, int32_t* d_path, float* d_path_score, int32_t* d_depth,
+                    int32_t* d_stop_level, cudaStream_t stream);
+
+int launch_similarity(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qn, const int16_t* d_rows,
+                      const int64_t* d_rn, const int64_t* d_ref_rows, const uint8_t* d_ref_whole,
+                      const int32_t* d_pair_q, const int32_t* d_pair_ref, int64_t n_pairs, int mode, float* d_score,
+                      int32_t* d_window, cudaStream_t stream);
+
 int launch_bundle(hdc_context* ctx, const void* d_rows, int elem_bytes, const int64_t* d_child_ptr,
                   const int32_t* d_child_idx, int64_t n_parents, int32_t* d_out, cudaStream_t stream);
 

@@ -38,6 +38,8 @@ SIGNATURES = [
                                SZ, P]),
     ("hdc_bundle", I32, [P, P, I32, P, P, I64, P, P]),
     ("hdc_beam_search", I32, [P, P, P, I64, P, P, P, P, P, I32, I32, I32, ctypes.c_double, I32, P, P, P, P]),
+    ("hdc_similarity", I32, [P, P, P, P, P, P, P, P, P, I64, I32, P, P, P]),
+    ("hdc_identify", I32, [P, P, P, I64, P, P, P, P, P, P, I32, I32, I32, ctypes.c_double, I32, P, P, P, P, P]),
     ("hdc_propagate_greedy", I32, [P, P, P, P, P, P, P, I64, ctypes.c_double, I32, P, P, P, P]),
     ("hdc_context_status", I32, [P, ctypes.POINTER(ctypes.c_int)]),
     ("hdc_search_plain_noalloc", I32, [P, P, P, I64, ctypes.c_int32, P, P, I64, ctypes.c_int32, I32, I32, P, P, P,
@@ -223,6 +225,33 @@ class Context:
                                     ptr(roots), roots.numel(), levels, beam, threshold, mode, ptr(path), ptr(score),
                                     ptr(depth), stream_ptr(stream)))
         return path, score, depth
+
+    def similarity(self, q, qn, rows, rn, ref_rows, ref_whole, pair_q, pair_ref, mode=SCORE_NORM, stream=None):
+        """HVCache::similarity for (query, reference) pairs; returns (scores,
+        first best window index within the reference or -1)."""
+        import torch
+        n = pair_q.numel()
+        score = torch.empty(max(n, 1), dtype=torch.float32, device=q.device)
+        win = torch.empty(max(n, 1), dtype=torch.int32, device=q.device)
+        check(lib().hdc_similarity(self.h, ptr(q), ptr(qn), ptr(rows), ptr(rn), ptr(ref_rows),
+                                   ptr(ref_whole) if ref_whole is not None else None, ptr(pair_q), ptr(pair_ref), n,
+                                   mode, ptr(score), ptr(win), stream_ptr(stream)))
+        return score[:n], win[:n]
+
+    def identify(self, q, qn, rows, rn, node_rows, child_ptr, child_idx, roots, levels=6, beam=5, threshold=0.0,
+                 mode=SCORE_NORM, stream=None):
+        """identify's descent with max-over-similarity-rows node scores;
+        returns (path, path scores, depth, stop level)."""
+        import torch
+        nq = q.shape[0]
+        path = torch.empty((nq, levels), dtype=torch.int32, device=q.device)
+        score = torch.empty((nq, levels), dtype=torch.float32, device=q.device)
+        depth = torch.empty(nq, dtype=torch.int32, device=q.device)
+        stop = torch.empty(nq, dtype=torch.int32, device=q.device)
+        check(lib().hdc_identify(self.h, ptr(q), ptr(qn), nq, ptr(rows), ptr(rn), ptr(node_rows), ptr(child_ptr),
+                                 ptr(child_idx), ptr(roots), roots.numel(), levels, beam, threshold, mode, ptr(path),
+                                 ptr(score), ptr(depth), ptr(stop), stream_ptr(stream)))
+        return path, score, depth, stop
 
     def bundle(self, rows, child_ptr, child_idx, out=None, stream=None):
         import torch

@@ -226,6 +226,39 @@ int hdc_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qnorm2
                     double threshold, int score_mode, int32_t* d_path, float* d_path_score, int32_t* d_depth,
                     void* stream);
 
+/* Windowed similarity, HVCache::similarity (src/encoder.cpp:198-215), for a
+ * list of (query, reference sequence) pairs.  A reference's "similarity rows"
+ * are the int16 hypervectors of its windows x = 0, step, ... while
+ * x + window < len (strict), in order, listed in CSR d_ref_rows [n_refs+1]
+ * over d_rows [n_rows][dim] (squared norms d_row_norm2); a reference with
+ * len <= window has one row, the whole sequence, flagged in d_ref_whole (may
+ * be NULL when there is none) and scored unclamped.  Otherwise the score is
+ * the best score over the rows starting from -1, and d_window the first row
+ * reaching it (-1 when none beat -1; the reference then reports position 0).
+ * Queries d_q [nq][dim] are whole-read int16 hypervectors (HVCache::get).
+ * dim % 8 == 0; rows and queries 16-byte aligned. */
+int hdc_similarity(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qnorm2, const int16_t* d_rows,
+                   const int64_t* d_row_norm2, const int64_t* d_ref_rows, const uint8_t* d_ref_whole,
+                   const int32_t* d_pair_q, const int32_t* d_pair_ref, int64_t n_pairs, int score_mode,
+                   float* d_score, int32_t* d_window, void* stream);
+
+/* Hierarchical identification with the reference's own scoring
+ * (targets/identify.cpp:89-202): as hdc_beam_search, but a taxonomy node is
+ * scored as max(-1, similarity of the read against every sequence of the
+ * node), i.e. the best over all similarity rows of the node's sequences,
+ * listed in CSR d_node_rows [n_nodes+1] over d_rows [n_rows][dim] (int16,
+ * squared norms d_row_norm2; a node without sequences scores -1).  Reads
+ * d_q [nq][dim] are whole-read int16 hypervectors.  Outputs as
+ * hdc_beam_search, plus d_stop_level [nq] (may be NULL): the level at which
+ * the read stopped because its best score fell below the threshold, or -1
+ * when it ran all levels.  levels <= 8; beam <= 8; dim % 8 == 0;
+ * dim * 2 bytes <= 200 KiB. */
+int hdc_identify(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qnorm2, int64_t nq, const int16_t* d_rows,
+                 const int64_t* d_row_norm2, const int64_t* d_node_rows, const int64_t* d_child_ptr,
+                 const int32_t* d_child_idx, const int32_t* d_roots, int n_roots, int levels, int beam,
+                 double threshold, int score_mode, int32_t* d_path, float* d_path_score, int32_t* d_depth,
+                 int32_t* d_stop_level, void* stream);
+
 /* ---------------------------------------------------------------- batching form */
 
 /* A reusable encode -> tensor-core search -> top-k pipeline for batches of up

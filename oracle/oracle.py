@@ -193,20 +193,56 @@ def scores_from(dot, nl, nr, mode=SCORE_NORM):
     return out
 
 
-def beam_search(q, proto, child_ptr, child_idx, roots, levels=6, beam=5, threshold=0.0, mode=SCORE_NORM):
-    """Beam descent of targets/identify.cpp:89-202 with one prototype per node:
-    level 0 scores `roots`; each later level expands every beam entry to its
-    children (a node without children to itself, :28-33); candidates are
-    ranked by score with ties to the lower node index; a read stops with its
-    best path when the best score is below threshold (:257-269), else keeps
-    the entries with score >= threshold, at most `beam` (:271-279).
-    Returns per read (path list, score list)."""
+def similarity_rows(seqs, window, step):
+    """Similarity rows of every reference sequence, HVCache::similarity
+    (src/encoder.cpp:198-215): a sequence with len <= window is one
+    whole-sequence row (:200-203); otherwise the windows x = 0, step, ...
+    while x + window < len (strict, :205).  Returns (row strings, CSR
+    ref_rows [n+1], whole flags [n])."""
+    rows, ptr, whole = [], [0], []
+    for s in seqs:
+        if len(s) <= window:
+            rows.append(s)
+            whole.append(1)
+        else:
+            rows.extend(s[x: x + window] for x in range(0, len(s) - window, step))
+            whole.append(0)
+        ptr.append(len(rows))
+    return rows, np.array(ptr, np.int64), np.array(whole, np.uint8)
+
+
+def similarity(q, rows, ref_rows, whole, pair_q, pair_ref, mode=SCORE_NORM):
+    """HVCache::similarity (src/encoder.cpp:198-215) over int16 hypervectors:
+    for a whole-sequence reference the unclamped score of its one row, else
+    the best score over its rows starting from -1, with the first row that
+    beats the running best (strict >, :208-212).  Returns (scores, window
+    index within the reference, -1 when no row beat -1)."""
     q = np.asarray(q, np.int64)
-    proto = np.asarray(proto, np.int64)
-    pn = (proto * proto).sum(1)
+    rows = np.asarray(rows, np.int64)
+    qn = (q * q).sum(1)
+    rn = (rows * rows).sum(1)
+    out_s = np.zeros(len(pair_q), np.float32)
+    out_w = np.zeros(len(pair_q), np.int32)
+    for p, (qi, ri) in enumerate(zip(pair_q, pair_ref)):
+        r0, r1 = int(ref_rows[ri]), int(ref_rows[ri + 1])
+        sc = scores_from(rows[r0:r1] @ q[qi], qn[qi], rn[r0:r1], mode)
+        if whole[ri]:
+            out_s[p], out_w[p] = sc[0], 0
+            continue
+        best, win = np.float32(-1.0), -1
+        for j, v in enumerate(sc):
+            if v > best:
+                best, win = v, j
+        out_s[p], out_w[p] = best, win
+    return out_s, out_w
+
+
+def _descent(node_score, nq, child_ptr, child_idx, roots, levels, beam, threshold):
+    """The level loop of targets/identify.cpp:89-202.  node_score(r, nodes)
+    gives read r's float scores of the candidate nodes.  Returns per read
+    (path list, score list, stop level or -1)."""
     out = []
-    for r in range(q.shape[0]):
-        qn = int((q[r] * q[r]).sum())
+    for r in range(nq):
         beams = [([], [])]
         result = None
         for L in range(levels):
@@ -220,16 +256,54 @@ def beam_search(q, proto, child_ptr, child_idx, roots, levels=6, beam=5, thresho
                 for c in kids:
                     cands.append((path, sc, int(c)))
             nodes = np.array([c[2] for c in cands], np.int64)
-            dots = proto[nodes] @ q[r]
-            s = scores_from(dots, qn, pn[nodes], mode)
+            s = node_score(r, nodes) if len(nodes) else np.zeros(0, np.float32)
             order = sorted(range(len(cands)), key=lambda i: (-float(s[i]), int(nodes[i])))
             ranked = [(cands[i][0] + [cands[i][2]], cands[i][1] + [float(s[i])]) for i in order]
             if not ranked or ranked[0][1][-1] < threshold:
-                result = ranked[0] if ranked else beams[0]
+                result = (ranked[0] if ranked else beams[0]) + (L,)
                 break
-            keep = [e for e in ranked[:beam] if e[1][-1] >= threshold]
-            beams = keep
+            beams = [e for e in ranked[:beam] if e[1][-1] >= threshold]
             if L == levels - 1:
-                result = beams[0]
+                result = beams[0] + (-1,)
         out.append(result)
     return out
+
+
+def beam_search(q, proto, child_ptr, child_idx, roots, levels=6, beam=5, threshold=0.0, mode=SCORE_NORM):
+    """Beam descent of targets/identify.cpp:89-202 with one prototype per node:
+    level 0 scores `roots`; each later level expands every beam entry to its
+    children (a node without children to itself, :28-33); candidates are
+    ranked by score with ties to the lower node index; a read stops with its
+    best path when the best score is below threshold (:174-189), else keeps
+    the entries with score >= threshold, at most `beam` (:191-199).
+    Returns per read (path list, score list)."""
+    q = np.asarray(q, np.int64)
+    proto = np.asarray(proto, np.int64)
+    pn = (proto * proto).sum(1)
+    qn = (q * q).sum(1)
+
+    def score(r, nodes):
+        return scores_from(proto[nodes] @ q[r], qn[r], pn[nodes], mode)
+
+    return [(p, s) for p, s, _ in _descent(score, q.shape[0], child_ptr, child_idx, roots, levels, beam, threshold)]
+
+
+def identify(q, rows, node_rows, child_ptr, child_idx, roots, levels=6, beam=5, threshold=0.0, mode=SCORE_NORM):
+    """targets/identify.cpp:89-202 with its own node score: max(-1, best
+    score of the read against every similarity row of every sequence of the
+    node) (:127, :138-159), rows of node n at rows[node_rows[n]:node_rows[n+1]].
+    Returns per read (path list, score list, stop level or -1)."""
+    q = np.asarray(q, np.int64)
+    rows = np.asarray(rows, np.int64)
+    qn = (q * q).sum(1)
+    rn = (rows * rows).sum(1)
+
+    def score(r, nodes):
+        out = np.full(len(nodes), -1.0, np.float32)
+        for i, n in enumerate(nodes):
+            r0, r1 = int(node_rows[n]), int(node_rows[n + 1])
+            if r1 > r0:
+                out[i] = max(np.float32(-1.0), scores_from(rows[r0:r1] @ q[r], qn[r], rn[r0:r1], mode).max())
+        return out
+
+    return _descent(score, q.shape[0], child_ptr, child_idx, roots, levels, beam, threshold)

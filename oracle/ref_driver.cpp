@@ -24,6 +24,10 @@
  *                                         (score desc, index asc); prints
  *                                         "q rank idx score(%.9g)" lines
  *   cosine  <a.bin> <b.bin> <n> <out.txt> cosine of n int16 HV pairs
+ *   similarity <queries.txt> <refs.txt> <out.txt>
+ *                                         cache.similarity(q, r) for every pair,
+ *                                         without precompute (compute-semantics
+ *                                         windows); prints "q r score(%.9g) pos"
  *   time    <queries.txt> <refs.txt> <k>  encode + brute-force top-k; prints reads/s
  */
 #include <chrono>
@@ -172,6 +176,19 @@ int main(int argc, char** argv) {
             std::snprintf(buf, sizeof buf, "%.9g\n", (double)cosine(a, b));
             out << buf;
         }
+        return 0;
+    }
+    if (cmd == "similarity") {
+        auto qs = read_lines(argv[2]);
+        auto rs = read_lines(argv[3]);
+        std::ofstream out(argv[4]);
+        char buf[128];
+        for (size_t qi = 0; qi < qs.size(); ++qi)
+            for (size_t ri = 0; ri < rs.size(); ++ri) {
+                SIM sim = cache.similarity(qs[qi], rs[ri]);
+                std::snprintf(buf, sizeof buf, "%zu %zu %.9g %zu\n", qi, ri, (double)sim.score, sim.pos);
+                out << buf;
+            }
         return 0;
     }
     if (cmd == "time") {

@@ -61,3 +61,42 @@ def input_digest(path):
         with open(os.path.join(seq_dir, name), "rb") as f:
             h.update(f.read())
     return h.hexdigest()
+
+
+def _mutate(rng, s, rate):
+    s = list(s)
+    for p in range(len(s)):
+        if rng.random() < rate:
+            s[p] = rng.choice([b for b in "ACGT" if b != s[p]])
+    return "".join(s)
+
+
+def make_reads(path, n_reads, window, seed):
+    """reads.fasta beside the taxonomy: n_reads distinct reads cut from
+    species sequences (lengths window, window/2 and 3*window/2, 1% substitution),
+    plus an unrelated random read and one with an N.  Returns its path."""
+    import random
+    rng = random.Random(seed)
+    seq_dir = os.path.join(path, "sequences_by_category")
+    species = sorted(f for f in os.listdir(seq_dir) if f.startswith("s__"))
+    reads, seen = [], set()
+    while len(reads) < n_reads:
+        sp = rng.choice(species)
+        with open(os.path.join(seq_dir, sp)) as f:
+            seqs = [l.strip() for l in f if l.strip() and not l.startswith(">")]
+        s = rng.choice(seqs)
+        n = rng.choice([window, window, window // 2, window + window // 2])
+        start = rng.randrange(0, len(s) - n + 1)
+        r = _mutate(rng, s[start:start + n], 0.01)
+        if r not in seen:
+            seen.add(r)
+            reads.append(("read%d %s" % (len(reads), sp[:-6]), r))
+    reads.append(("random", "".join(rng.choice("ACGT") for _ in range(window))))
+    r = list(reads[0][1])
+    r[len(r) // 3] = "N"
+    reads.append(("with_n", "".join(r)))
+    out = os.path.join(path, "reads.fasta")
+    with open(out, "w") as f:
+        for name, r in reads:
+            f.write(">%s\n%s\n" % (name, r))
+    return out

@@ -108,3 +108,21 @@ def test_fast_bundle_encoder_matches_oracle(orc):
     ref, _ = orc.encode(seqs[:40], 1024, 8, "int32")
     got = orc.encode_bundles(buf, off[:40], ln[:40], 1024, 8, group=8)
     assert np.array_equal(got, ref.reshape(5, 8, -1).sum(1))
+
+
+SIM_GOLDEN = json.load(open(os.path.join(GOLD, "similarity.json")))
+
+
+@pytest.mark.parametrize("g", SIM_GOLDEN, ids=lambda g: "D%d_k%d" % (g["dim"], g["kmer"]))
+def test_similarity_matches_reference(orc, g):
+    """HVCache::similarity over the oracle's window rows equals the
+    reference's own similarity() (score bit-exact as float, position)."""
+    rows, ref_rows, whole = orc.similarity_rows(g["refs"], g["window"], g["step"])
+    q, _ = orc.encode(g["queries"], g["dim"], g["kmer"])
+    r, _ = orc.encode(rows, g["dim"], g["kmer"])
+    res = np.array(g["results"], dtype=np.float64)
+    pq, pr = res[:, 0].astype(np.int64), res[:, 1].astype(np.int64)
+    s, w = orc.similarity(q, r, ref_rows, whole, pq, pr)
+    assert np.array_equal(s, res[:, 2].astype(np.float32))
+    pos = np.where(w < 0, 0, w * g["step"])
+    assert np.array_equal(pos, res[:, 3].astype(np.int64))
