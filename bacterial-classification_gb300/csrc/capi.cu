@@ -120,7 +120,7 @@ int hdc_encode_segments(hdc_context* ctx, const char* d_bytes, const int64_t* d_
     if (n_segs < 0) return fail(HDC_ERR_INVALID, "encode: negative segment count");
     if (n_segs == 0) return HDC_OK;
     if (!d_bytes || !d_seg_off || !d_seg_len || !d_out) return fail(HDC_ERR_INVALID, "encode: null pointer");
-    if (out_kind < HDC_OUT_I16 || out_kind > HDC_OUT_BIPOLAR_F16) return fail(HDC_ERR_INVALID, "encode: bad out_kind");
+    if (out_kind < HDC_OUT_I16 || out_kind > HDC_OUT_BIPOLAR_I8) return fail(HDC_ERR_INVALID, "encode: bad out_kind");
     if (out_stride < ctx->dim) return fail(HDC_ERR_INVALID, "encode: out_stride < dim");
     if (max_len < 0) return fail(HDC_ERR_INVALID, "encode: negative max_len");
     return hdc::launch_encode(ctx, d_bytes, d_seg_off, d_seg_len, nullptr, nullptr, 0, n_segs, out_kind, d_out,
@@ -145,7 +145,8 @@ int hdc_encode_windows(hdc_context* ctx, const char* d_bytes, const int64_t* d_s
 int hdc_norms(hdc_context* ctx, const void* d_hv, int elem_bytes, int64_t n, int64_t* d_norm2, int32_t* d_maxabs,
               void* stream) {
     if (!ctx) return fail(HDC_ERR_INVALID, "norms: null context");
-    if (elem_bytes != 2 && elem_bytes != 4) return fail(HDC_ERR_INVALID, "norms: elem_bytes must be 2 or 4");
+    if (elem_bytes != 1 && elem_bytes != 2 && elem_bytes != 4)
+        return fail(HDC_ERR_INVALID, "norms: elem_bytes must be 1, 2 or 4");
     if (n < 0) return fail(HDC_ERR_INVALID, "norms: negative count");
     if (n > 0 && (!d_hv || !d_norm2)) return fail(HDC_ERR_INVALID, "norms: null pointer");
     return hdc::launch_norms(ctx, d_hv, elem_bytes, n, d_norm2, d_maxabs, static_cast<cudaStream_t>(stream));

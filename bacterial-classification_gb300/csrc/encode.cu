@@ -283,6 +283,24 @@ __global__ void __launch_bounds__(kThreads) encode_kernel(const EncodeArgs a) {
                 for (int b = 0; b < 32; ++b)
                     if (b < nd) o[b] = 2 * (int)val[b] - nvalid;
             }
+        } else if (a.out_kind == HDC_OUT_BIPOLAR_I8) {
+            int8_t* o = reinterpret_cast<int8_t*>(rowp) + seg * a.out_stride + dbase;
+            uint32_t pk[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                pk[q] = 0;
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                    pk[q] |= (2 * (int)val[4 * q + t] - nvalid >= 0 ? 0x01u : 0xffu) << (8 * t);
+            }
+            if (nd == 32 && ((reinterpret_cast<uintptr_t>(o) & 15) == 0)) {
+                reinterpret_cast<uint4*>(o)[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                reinterpret_cast<uint4*>(o)[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+            } else {
+#pragma unroll
+                for (int b = 0; b < 32; ++b)
+                    if (b < nd) o[b] = (int8_t)(pk[b >> 2] >> (8 * (b & 3)));
+            }
         } else {
             uint16_t* o = reinterpret_cast<uint16_t*>(rowp) + seg * a.out_stride + dbase;
             uint32_t pk[16];

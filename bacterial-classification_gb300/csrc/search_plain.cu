@@ -356,7 +356,10 @@ int launch_norms(hdc_context* ctx, const void* d_hv, int elem_bytes, int64_t n, 
     const int rows_per_block = 8;
     const int64_t grid = (n + rows_per_block - 1) / rows_per_block;
     if (grid > 0x7fffffff) return fail(HDC_ERR_INVALID, "norms: too many rows");
-    if (elem_bytes == 2)
+    if (elem_bytes == 1)
+        norms_kernel<int8_t><<<(unsigned)grid, 256, 0, stream>>>(static_cast<const int8_t*>(d_hv), n, ctx->dim,
+                                                                  d_norm2, d_maxabs);
+    else if (elem_bytes == 2)
         norms_kernel<int16_t><<<(unsigned)grid, 256, 0, stream>>>(static_cast<const int16_t*>(d_hv), n, ctx->dim,
                                                                    d_norm2, d_maxabs);
     else

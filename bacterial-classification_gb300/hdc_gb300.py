@@ -15,7 +15,7 @@ HDC_OK = 0
 ERR = {1: "HDC_ERR_INVALID", 2: "HDC_ERR_RANGE", 3: "HDC_ERR_CUDA", 4: "HDC_ERR_NOMEM",
        5: "HDC_ERR_UNSUPPORTED", 6: "HDC_ERR_TIMEOUT"}
 SCORE_NORM, SCORE_COS, SCORE_DOT = 0, 1, 2
-OUT_I16, OUT_I32, OUT_BIPOLAR_BF16, OUT_BIPOLAR_I16, OUT_BIPOLAR_F16 = 0, 1, 2, 3, 4
+OUT_I16, OUT_I32, OUT_BIPOLAR_BF16, OUT_BIPOLAR_I16, OUT_BIPOLAR_F16, OUT_BIPOLAR_I8 = 0, 1, 2, 3, 4, 5
 
 # (name, restype, argtypes) of every exported entry point
 P, I32, I64, SZ = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_size_t
@@ -378,6 +378,29 @@ def synth_tree(seed, n_leaves, root_len=1500, subst=(0.04, 0.03, 0.02, 0.015, 0.
     s = Seqs(buf, off, ln)
     s.nodes_per_rank = ranks
     return s
+
+
+def synth_tree_csr(n_leaves):
+    """Node numbering of the taxonomy hdc_synth_tree generates: branching
+    b = ceil(n_leaves^(1/6)), ranks 1..6 numbered rank by rank, node j of a
+    rank the child of node j // b of the rank above.  Returns (b, base
+    [7] first node of each rank, counts [6], child_ptr [n_nodes+1] int64,
+    child_idx int32)."""
+    import numpy as np
+    b = 1
+    while b ** 6 < n_leaves:
+        b += 1
+    counts = [(n_leaves + b ** (6 - r) - 1) // b ** (6 - r) for r in range(1, 7)]
+    base = np.cumsum([0] + counts)
+    n_child = np.zeros(int(base[-1]), np.int64)
+    idx = []
+    for r in range(1, 6):
+        kids = np.arange(counts[r], dtype=np.int64)
+        n_child[base[r - 1]:base[r]] = np.bincount(kids // b, minlength=counts[r - 1])
+        idx.append(base[r] + kids)
+    ptr = np.zeros(int(base[-1]) + 1, np.int64)
+    ptr[1:] = np.cumsum(n_child)
+    return b, base, counts, ptr, np.concatenate(idx).astype(np.int32)
 
 
 def synth_copies(seed, src, n_copies, subst, threads=0):

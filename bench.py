@@ -47,6 +47,12 @@ CONFIGS = {
     "c4": dict(n_leaves=200000, dim=10240, kmer=10, read_len=250, subst=0.01, topk=10, copies=8, bipolar=True,
                tree_seed=3, read_seed=104, copy_seed=203, sigma=0.5, min_read=100, max_read=1600,
                mixed_frac=0.2, mixed_rate=0.06),
+    # hierarchical descent: 500,000 leaves + internal prototypes (exact int32 sums of their
+    # children, bottom-up over the 6 ranks), D=16,384, k=12; config-4 read distribution;
+    # beam 5 per rank, root to leaf (no early stop), in one launch per batch
+    "c5": dict(n_leaves=500000, dim=16384, kmer=12, read_len=250, subst=0.01, topk=5, copies=0, bipolar=True,
+               tree_seed=5, read_seed=105, sigma=0.5, min_read=100, max_read=1600, mixed_frac=0.2,
+               mixed_rate=0.06, beam=5, levels=6, threshold=float("-inf")),
 }
 
 
@@ -376,6 +382,200 @@ def run_ours(args, cfg, rank, world):
     return res
 
 
+def build_prototypes(H, ctx, cfg, dev):
+    """Taxonomy prototypes resident in HBM: leaf encodings (int32) and every
+    internal node the exact int32 sum of its children (hdc_bundle, rank by
+    rank from the leaves up).  Also the bundle kernel's timing per rank."""
+    import torch
+    t0 = time.time()
+    tree = H.synth_tree(cfg["tree_seed"], cfg["n_leaves"])
+    b, base, counts, ptr, idx = H.synth_tree_csr(cfg["n_leaves"])
+    n_nodes, dim = int(base[-1]), cfg["dim"]
+    proto = torch.empty((n_nodes, dim), dtype=torch.int32, device=dev)
+    d_tree = torch.from_numpy(tree.buf).to(dev)
+    leaf0 = int(base[5])
+    chunk = 16384
+    for a in range(0, cfg["n_leaves"], chunk):
+        e = min(cfg["n_leaves"], a + chunk)
+        off = torch.from_numpy(np.ascontiguousarray(tree.off[a:e])).to(dev)
+        ln = torch.from_numpy(np.ascontiguousarray(tree.len[a:e])).to(dev)
+        ctx.encode_segments(d_tree, off, ln, proto[leaf0 + a:leaf0 + e], H.OUT_I32, int(tree.len[a:e].max()))
+    d_idx = torch.from_numpy(idx).to(dev)
+    bundle = []
+    for r in range(4, -1, -1):
+        lo, hi = int(base[r]), int(base[r + 1])
+        cp = torch.from_numpy(ptr[lo:hi + 1].copy()).to(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        ctx.bundle(proto, cp, d_idx, out=proto[lo:hi])
+        e1.record()
+        torch.cuda.synchronize()
+        n_child = int(ptr[hi] - ptr[lo])
+        bundle.append(dict(rank=r + 1, parents=hi - lo, children=n_child, ms=e0.elapsed_time(e1),
+                           bytes=(n_child + hi - lo) * dim * 4))
+    pn = ctx.norms(proto)
+    torch.cuda.synchronize()
+    log("prototypes: %d nodes x %d dims (%.1f GB) built in %.1f s" % (n_nodes, dim, n_nodes * dim * 4 / 1e9,
+                                                                   time.time() - t0))
+    return tree, proto, pn, (b, base, counts, ptr, idx), bundle
+
+
+def run_descent(args, cfg, rank, world):
+    """Hierarchical descent: per step, encode a batch of reads to +1/-1 int8
+    and run the beam descent over the resident prototypes (one launch)."""
+    import torch
+    import hdc_gb300 as H
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    dim, B, L, W = cfg["dim"], args.batch, cfg["levels"], cfg["beam"]
+    ctx = H.Context(dim, cfg["kmer"], cfg["read_len"], 10)
+    tree, proto, pn, (b, base, counts, ptr, idx), bundle = build_prototypes(H, ctx, cfg, dev)
+    d_ptr, d_idx = torch.from_numpy(ptr).to(dev), torch.from_numpy(idx).to(dev)
+    roots = torch.arange(0, counts[0], dtype=torch.int32, device=dev)
+    n_pool = 2
+    pool = [make_reads(H, tree, cfg, B, cfg["read_seed"] + 1000 * rank + p) for p in range(n_pool)]
+    max_len = max(r.max_len() for r in pool)
+    q8 = torch.empty((B, dim), dtype=torch.int8, device=dev)
+    qn = torch.full((B,), dim, dtype=torch.int64, device=dev)  # every element of a +1/-1 read is nonzero
+    dev_pool = [(torch.from_numpy(r.buf).to(dev), torch.from_numpy(r.off).to(dev), torch.from_numpy(r.len).to(dev))
+                for r in pool]
+    out = {}
+
+    def step(d_buf, d_off, d_len, ev=None):
+        ctx.encode_segments(d_buf, d_off, d_len, q8, H.OUT_BIPOLAR_I8, max_len)
+        if ev:
+            ev[0].record()
+        out["r"] = ctx.beam_search(q8, qn, proto, pn, d_ptr, d_idx, roots, L, W, cfg["threshold"])
+        if ev:
+            ev[1].record()
+        return out["r"]
+
+    for i in range(args.warmup):
+        step(*dev_pool[i % n_pool])
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    stream = torch.cuda.current_stream()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clk = ClockSampler(dev.index)
+    with clk:
+        torch.cuda.synchronize()
+        t0.record(stream)
+        for i in range(args.steps):
+            step(*dev_pool[i % n_pool])
+        t1.record(stream)
+        torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / args.steps
+    ev = [torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)]
+    beam_ms = []
+    for i in range(3):
+        step(*dev_pool[i % n_pool], ev=ev)
+        torch.cuda.synchronize()
+        beam_ms.append(ev[0].elapsed_time(ev[1]))
+    path, score, depth = out["r"]
+    depth_mean = float(depth.float().mean())
+    # end to end: pinned host reads copied in, paths and scores copied back, every step
+    h_pool = [(torch.from_numpy(r.buf).pin_memory(), torch.from_numpy(r.off).pin_memory(),
+               torch.from_numpy(r.len).pin_memory()) for r in pool]
+    cap = max(h[0].numel() for h in h_pool)
+    e_buf = torch.empty(cap, dtype=torch.uint8, device=dev)
+    e_off = torch.empty(B, dtype=torch.int64, device=dev)
+    e_len = torch.empty(B, dtype=torch.int32, device=dev)
+    h_path = torch.empty((B, L), dtype=torch.int32).pin_memory()
+    h_score = torch.empty((B, L), dtype=torch.float32).pin_memory()
+    io = {}
+
+    def e2e_step(i):
+        hb, ho, hl = h_pool[i % n_pool]
+        e_buf[:hb.numel()].copy_(hb, non_blocking=True)
+        e_off.copy_(ho, non_blocking=True)
+        e_len.copy_(hl, non_blocking=True)
+        p, s_, _ = step(e_buf, e_off, e_len)
+        h_path.copy_(p, non_blocking=True)
+        h_score.copy_(s_, non_blocking=True)
+        io["h2d"] = hb.numel() + ho.numel() * 8 + hl.numel() * 4
+        io["d2h"] = h_path.numel() * 4 + h_score.numel() * 4
+
+    for i in range(args.warmup):
+        e2e_step(i)
+    torch.cuda.synchronize()
+    t0.record(stream)
+    for i in range(args.steps):
+        e2e_step(i)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = t0.elapsed_time(t1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms, e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms, e2e_ms = float(t[0]), float(t[1])
+    # rows gathered per read: the level-0 candidates, then up to beam x children per level; the
+    # ranks whose prototypes together fit in half of L2 stay resident across reads
+    cand = [counts[0]] + [min(W, counts[l - 1]) * b for l in range(1, L)]
+    l2_levels = 0
+    while l2_levels < L and sum(counts[:l2_levels + 1]) * dim * 4 <= 64 << 20:
+        l2_levels += 1
+    res = dict(ms=ms, e2e_ms=e2e_ms, search_ms=float(np.median(beam_ms)), clocks=clk.summary(),
+               launches=2 * args.steps, refs=int(base[-1]), h2d=io["h2d"], d2h=io["d2h"], tree=tree,
+               bundle=bundle, depth_mean=depth_mean, rows_per_read=int(sum(cand)),
+               hbm_rows_per_read=int(sum(cand[l2_levels:])), l2_levels=l2_levels,
+               mean_len=float(np.mean(pool[0].len)))
+    if rank == 0 and not args.no_cpu_baseline:
+        # q8 and out["r"] hold the last step's batch and result
+        res["cpu"] = cpu_baseline_descent(cfg, pool[0], q8[:256].cpu().numpy(), proto, pn, ptr, idx,
+                                          list(range(counts[0])))
+        p_, s_, d_ = (x.cpu().numpy() for x in out["r"])
+        res["sample_identical"] = all(
+            d_[i] == len(wp) and list(p_[i, :len(wp)]) == wp and np.array_equal(s_[i, :len(wp)],
+                                                                                np.array(ws, np.float32))
+            for i, (wp, ws) in enumerate(res["cpu"].pop("paths")))
+    return res
+
+
+def cpu_baseline_descent(cfg, reads, q8, proto, pn, ptr, idx, roots, seconds=12.0):
+    """The descent restated on the CPU (oracle beam_search, exact int64 dots,
+    one core) for a bounded sample of the same reads, over a host copy of the
+    same prototypes; also checks those reads' paths against the GPU's."""
+    from oracle import oracle as O
+    pn_h = proto_rows = None
+    need = proto.numel() * 4
+    if host_available_bytes() > 3 * need:
+        proto_rows, how = proto.cpu().numpy(), "host copy"
+    else:  # not enough host memory for a copy: the rows each step gathers are copied from the device
+        proto_rows, how = _DeviceRows(proto), "rows gathered from device memory per step"
+    pn_h = pn.cpu().numpy()
+    done, t_total, paths = 0, 0.0, []
+    while t_total < seconds and done < q8.shape[0]:
+        t0 = time.time()
+        paths += O.beam_search(q8[done:done + 8], proto_rows, ptr, idx, roots, cfg["levels"], cfg["beam"],
+                               cfg["threshold"], O.SCORE_NORM, pn=pn_h)
+        t_total += time.time() - t0
+        done += min(8, q8.shape[0] - done)
+    return dict(value=done / t_total, cores=1, done=done, rows=how, paths=paths)
+
+
+def host_available_bytes():
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return 0
+
+
+class _DeviceRows:
+    """proto[nodes] for the CPU descent, copied from device memory on demand."""
+
+    def __init__(self, t):
+        self.t = t
+
+    def __getitem__(self, nodes):
+        import torch
+        return self.t[torch.as_tensor(np.asarray(nodes), device=self.t.device)].cpu().numpy()
+
+
 def oracle_database(cfg, threads):
     """Reference hypervectors for the reference arm, built on the CPU (no GPU):
     leaf encodings (config 2), or, for the bundled configurations, 8 x the leaf
@@ -426,14 +626,114 @@ def run_reference(args, cfg):
     return v, threads, done
 
 
+def descent_line(args, cfg, r, metric, workload, world):
+    """The JSON line of the hierarchical-descent form."""
+    pk, src = peaks()
+    B, dim = args.batch, cfg["dim"]
+    # the beam kernel gathers rows_per_read int32 prototype rows per read; those of the lower ranks
+    # (hbm_rows_per_read) come from HBM, the upper ranks' from L2; plus the int8 read once
+    per_read = r["hbm_rows_per_read"] * dim * 4 + dim
+    achieved = B * per_read / (r["search_ms"] / 1e3) / 1e9
+    bundle_bytes = sum(x["bytes"] for x in r["bundle"])
+    bundle_ms = sum(x["ms"] for x in r["bundle"])
+    line = {
+        "metric": metric, "value": B * world / (r["ms"] / 1e3), "unit": "reads/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "int8 +1/-1 reads x int32 prototypes, exact int64 dots, FP64 scores",
+        "data": "synthetic (seeded 6-rank tree, see bench.py)",
+        "config": {"workload": workload, "form": "descent", "batch_reads": B, "nodes": r["refs"],
+                   "mean_read_len": r["mean_len"], "mean_depth": r["depth_mean"],
+                   "l2": "inputs larger than L2: %.1f GB of prototypes, the lower ranks gathered from HBM "
+                         "every step" % (r["refs"] * dim * 4 / 1e9)},
+        "e2e": {"value": B * world / (r["e2e_ms"] / 1e3), "unit": "reads/s", "h2d_bytes_per_step": r["h2d"],
+                "d2h_bytes_per_step": r["d2h"]},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / pk["hbm_gbs"], "traffic": None,
+                     "peak_source": "%s HBM copy bandwidth (MEASURED_PEAKS.json)" % src,
+                     "kernel": "beam_kernel; algorithmic bytes per read: the %d int32 rows gathered below "
+                               "the top %d ranks + the int8 read (the other %d rows a read gathers belong to "
+                               "the top ranks, whose prototypes stay L2-resident)" % (
+                                   r["hbm_rows_per_read"], r["l2_levels"],
+                                   r["rows_per_read"] - r["hbm_rows_per_read"])},
+        "propagate_bundle": {"kernel": "bundle_kernel (internal prototypes = int32 sums of children)",
+                             "ms": bundle_ms, "gb_per_s": bundle_bytes / (bundle_ms / 1e3) / 1e9,
+                             "frac_of_hbm": bundle_bytes / (bundle_ms / 1e3) / 1e9 / pk["hbm_gbs"],
+                             "per_rank": r["bundle"]},
+        "clocks": r["clocks"], "gpu_launches": r["launches"],
+    }
+    if "sample_identical" in r:
+        line["paths_identical_to_oracle"] = {"reads": r["cpu"]["done"], "identical": r["sample_identical"]}
+    if "cpu" in r:
+        line["cpu_baseline"] = {"value": r["cpu"]["value"], "unit": "reads/s", "cores": r["cpu"]["cores"],
+                                "kind": "port", "sample": "%d reads of the same batch: the descent restated "
+                                                          "(oracle, exact int64 dots) over the same prototypes "
+                                                          "(%s); encode excluded" % (r["cpu"]["done"],
+                                                                                     r["cpu"]["rows"])}
+    return line
+
+
+_DESCENT = {}
+
+
+def run_reference_descent(args, cfg):
+    """Reference arm of the descent: prototypes built on the CPU (the oracle's
+    encoder + int32 sums of children), then per step a bounded sample of reads
+    encoded and descended by the oracle on every host core (forked workers
+    sharing the prototypes; no GPU in this process)."""
+    import multiprocessing as mp
+    import hdc_gb300 as H
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    t0 = time.time()
+    tree = H.synth_tree(cfg["tree_seed"], cfg["n_leaves"])
+    b, base, counts, ptr, idx = H.synth_tree_csr(cfg["n_leaves"])
+    dim = cfg["dim"]
+    proto = np.empty((int(base[-1]), dim), np.int32)
+    leaf0 = int(base[5])
+    for a in range(0, cfg["n_leaves"], 65536):
+        e = min(cfg["n_leaves"], a + 65536)
+        proto[leaf0 + a:leaf0 + e] = O.encode_bundles(tree.buf, tree.off[a:e], tree.len[a:e], dim, cfg["kmer"], 1,
+                                                      threads)
+    for r_ in range(4, -1, -1):  # children of a parent are consecutive rows of the rank below
+        lo, hi = int(base[r_]), int(base[r_ + 1])
+        first = idx[ptr[lo:hi]]
+        proto[lo:hi] = np.add.reduceat(proto[int(base[r_ + 1]):int(base[r_ + 2])], first - int(base[r_ + 1]), axis=0)
+    pn = np.concatenate([(proto[a:a + 4096].astype(np.int64) ** 2).sum(1) for a in range(0, len(proto), 4096)])
+    log("CPU prototypes built in %.1f s" % (time.time() - t0))
+    _DESCENT.update(proto=proto, pn=pn, ptr=ptr, idx=idx, roots=list(range(counts[0])), levels=cfg["levels"],
+                    beam=cfg["beam"], threshold=cfg["threshold"])
+    reads = make_reads(H, tree, cfg, 16 * threads * 8, cfg["read_seed"] + 999)
+    vals, done = [], 0
+    with mp.get_context("fork").Pool(threads) as pool:
+        for i in range(args.warmup + args.steps):
+            n = 2 * threads if i < args.warmup else 8 * threads
+            seqs = [reads.get(j % len(reads)) for j in range(i * n, (i + 1) * n)]
+            t1 = time.time()
+            q, _ = O.encode(seqs, dim, cfg["kmer"], "bipolar", threads)
+            done_n = sum(pool.map(_descent_worker_q, [q[j:j + 2] for j in range(0, n, 2)]))
+            dt = time.time() - t1
+            if i >= args.warmup:
+                vals.append(done_n / dt)
+                done = done_n
+    return float(np.median(vals)), threads, done
+
+
+def _descent_worker_q(q):
+    from oracle import oracle as O
+    d = _DESCENT
+    return len(O.beam_search(q, d["proto"], d["ptr"], d["idx"], d["roots"], d["levels"], d["beam"], d["threshold"],
+                             O.SCORE_NORM, pn=d["pn"]))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--config", default="c3", choices=sorted(CONFIGS))
-    ap.add_argument("--form", default="", choices=["", "plain", "tc", "pipe"],
-                    help="default: tc for c3, pipe for c4, plain for c2")
+    ap.add_argument("--form", default="", choices=["", "plain", "tc", "pipe", "descent"],
+                    help="default: tc for c3, pipe for c4, plain for c2, descent for c5")
     ap.add_argument("--batch", type=int, default=0,
                     help="reads per step; 0 = 2 x SMs x 128, whole waves of 128-query tensor-core tiles")
     ap.add_argument("--plain-batch", type=int, default=4096)
@@ -447,7 +747,7 @@ def main():
         args.warmup = 3
     cfg = dict(CONFIGS[args.config])
     if not args.form:
-        args.form = {"c2": "plain", "c3": "tc", "c4": "pipe"}[args.config]
+        args.form = {"c2": "plain", "c3": "tc", "c4": "pipe", "c5": "descent"}[args.config]
     if args.refs:
         cfg["n_leaves"] = args.refs
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -462,6 +762,25 @@ def main():
         workload = "%s: %d refs D=%d k=%d, %d bp reads, top-%d" % (args.config, cfg["n_leaves"], cfg["dim"], cfg["kmer"],
                                                                    cfg["read_len"], cfg["topk"])
     metric = "reads/s encode+top-%d search" % cfg["topk"]
+    if args.form == "descent":
+        metric = "reads/s encode+hierarchical descent (top-%d per rank, %d ranks, root to leaf)" % (cfg["beam"],
+                                                                                                  cfg["levels"])
+        workload = "%s: %d leaves + internal prototypes D=%d k=%d, %s" % (
+            args.config, cfg["n_leaves"], cfg["dim"], cfg["kmer"], reads_desc)
+    if args.impl == "reference" and args.form == "descent":
+        if rank != 0:
+            return
+        v, threads, done = run_reference_descent(args, cfg)
+        line = {"impl": "reference", "metric": metric, "value": v, "unit": "reads/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "int64",
+                "data": "synthetic", "config": {"workload": workload},
+                "cpu_baseline": {"value": v, "unit": "reads/s", "cores": threads, "kind": "port",
+                                 "sample": "%d reads per step (HVCache::compute restated to +1/-1, then the "
+                                           "beam descent restated with exact int64 dots); prototypes built on "
+                                           "the CPU" % done},
+                "e2e": {"value": v, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     if args.impl == "reference":
         if rank != 0:
             return
@@ -483,6 +802,13 @@ def main():
     if args.batch <= 0:
         sms = torch.cuda.get_device_properties(int(os.environ.get("LOCAL_RANK", 0))).multi_processor_count
         args.batch = 2 * sms * 128
+    if args.form == "descent":
+        r = run_descent(args, cfg, rank, world)
+        if rank == 0:
+            print(json.dumps(descent_line(args, cfg, r, metric, workload, world)), flush=True)
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
     r = run_ours(args, cfg, rank, world)
     if rank != 0:
         torch.distributed.destroy_process_group()

@@ -54,6 +54,7 @@ extern "C" {
 #define HDC_OUT_BIPOLAR_BF16 2 /* bf16 +1/-1 sign of the bundle, 0 -> +1 */
 #define HDC_OUT_BIPOLAR_I16 3  /* int16 +1/-1 sign of the bundle, 0 -> +1 */
 #define HDC_OUT_BIPOLAR_F16 4  /* fp16 +1/-1 sign of the bundle, 0 -> +1 (tensor-core queries) */
+#define HDC_OUT_BIPOLAR_I8 5   /* int8 +1/-1 sign of the bundle, 0 -> +1 (hierarchical descent reads) */
 
 typedef struct hdc_context hdc_context;
 typedef struct hdc_refdb hdc_refdb;
@@ -109,8 +110,8 @@ int hdc_encode_windows(hdc_context* ctx, const char* d_bytes, const int64_t* d_s
 /* ---------------------------------------------------------------- (b) search */
 
 /* Squared L2 norms (int64) and optional max |v| (int32 atomic max into
- * *d_maxabs, which the caller zeroes) of n rows of int16 (elem_bytes 2) or
- * int32 (elem_bytes 4) hypervectors, row stride dim. */
+ * *d_maxabs, which the caller zeroes) of n rows of int8 (elem_bytes 1),
+ * int16 (elem_bytes 2) or int32 (elem_bytes 4) hypervectors, row stride dim. */
 int hdc_norms(hdc_context* ctx, const void* d_hv, int elem_bytes, int64_t n, int64_t* d_norm2,
               int32_t* d_maxabs, void* stream);
 

@@ -269,21 +269,22 @@ def _descent(node_score, nq, child_ptr, child_idx, roots, levels, beam, threshol
     return out
 
 
-def beam_search(q, proto, child_ptr, child_idx, roots, levels=6, beam=5, threshold=0.0, mode=SCORE_NORM):
+def beam_search(q, proto, child_ptr, child_idx, roots, levels=6, beam=5, threshold=0.0, mode=SCORE_NORM, pn=None):
     """Beam descent of targets/identify.cpp:89-202 with one prototype per node:
     level 0 scores `roots`; each later level expands every beam entry to its
     children (a node without children to itself, :28-33); candidates are
     ranked by score with ties to the lower node index; a read stops with its
     best path when the best score is below threshold (:174-189), else keeps
     the entries with score >= threshold, at most `beam` (:191-199).
-    Returns per read (path list, score list)."""
+    `pn` (squared prototype norms) may be given; prototype rows are widened
+    to int64 only when gathered.  Returns per read (path list, score list)."""
     q = np.asarray(q, np.int64)
-    proto = np.asarray(proto, np.int64)
-    pn = (proto * proto).sum(1)
+    if pn is None:
+        pn = np.array([int((np.asarray(row, np.int64) ** 2).sum()) for row in proto], np.int64)
     qn = (q * q).sum(1)
 
     def score(r, nodes):
-        return scores_from(proto[nodes] @ q[r], qn[r], pn[nodes], mode)
+        return scores_from(np.asarray(proto[nodes], np.int64) @ q[r], qn[r], pn[nodes], mode)
 
     return [(p, s) for p, s, _ in _descent(score, q.shape[0], child_ptr, child_idx, roots, levels, beam, threshold)]
 

@@ -9,20 +9,10 @@ pytestmark = pytest.mark.gpu
 
 
 def _tree_csr(n_leaves, b):
-    """Nodes of all ranks (rank 1..6) numbered level by level; the layout of
-    hdc_synth_tree (node j of rank r has parent j // b)."""
-    counts = []
-    for r in range(1, 7):
-        span = b ** (6 - r)
-        counts.append((n_leaves + span - 1) // span)
-    base = np.cumsum([0] + counts)
-    children = [[] for _ in range(base[-1])]
-    for r in range(1, 6):
-        for j in range(counts[r]):
-            children[base[r - 1] + j // b].append(base[r] + j)
-    ptr = np.zeros(base[-1] + 1, np.int64)
-    ptr[1:] = np.cumsum([len(c) for c in children])
-    idx = np.array([x for c in children for x in c], np.int32)
+    """(base, counts, child_ptr, child_idx) of the hdc_synth_tree layout."""
+    import hdc_gb300
+    bb, base, counts, ptr, idx = hdc_gb300.synth_tree_csr(n_leaves)
+    assert bb == b
     return base, counts, ptr, idx
 
 
@@ -48,11 +38,10 @@ def test_beam_descent_matches_oracle(hdc, orc, cuda, dim, kmer, n_leaves, beam, 
         lo, hi = int(base[r]), int(base[r + 1])
         cp = torch.from_numpy(ptr[lo:hi + 1].copy()).to(cuda)
         proto[lo:hi] = ctx.bundle(proto, cp, torch.from_numpy(idx).to(cuda))
-    q16 = torch.empty((len(reads), dim), dtype=torch.int16, device=cuda)
+    q8 = torch.empty((len(reads), dim), dtype=torch.int8, device=cuda)
     ctx.encode_segments(torch.from_numpy(reads.buf).to(cuda), torch.from_numpy(reads.off).to(cuda),
-                        torch.from_numpy(reads.len).to(cuda), q16, H.OUT_BIPOLAR_I16, reads.max_len())
-    q8 = q16.to(torch.int8)
-    qn = ctx.norms(q16)
+                        torch.from_numpy(reads.len).to(cuda), q8, H.OUT_BIPOLAR_I8, reads.max_len())
+    qn = ctx.norms(q8)
     pn = ctx.norms(proto)
     roots = torch.arange(0, counts[0], dtype=torch.int32, device=cuda)
     path, score, depth = ctx.beam_search(q8, qn, proto, pn, torch.from_numpy(ptr).to(cuda),

@@ -32,7 +32,7 @@ def upload(seqs, dev):
 def gpu_encode(ctx, seqs, dev, kind=0, max_len=None):
     import torch
     b, o, l, mx = upload(seqs, dev)
-    dt = {0: torch.int16, 1: torch.int32, 2: torch.bfloat16, 3: torch.int16}[kind]
+    dt = {0: torch.int16, 1: torch.int32, 2: torch.bfloat16, 3: torch.int16, 4: torch.float16, 5: torch.int8}[kind]
     out = torch.full((len(seqs), ctx.dim), 7, dtype=dt, device=dev)
     nk = torch.zeros(len(seqs), dtype=torch.int32, device=dev)
     ctx.encode_segments(b, o, l, out, kind, mx if max_len is None else max_len, nk)
@@ -101,6 +101,10 @@ def test_encode_random_all_kinds(hdc, orc, cuda, dim, k):
     assert np.array_equal(outb.numpy(), bip)
     outbf, _ = gpu_encode(ctx, sub, cuda, 2)
     assert np.array_equal(outbf.float().numpy(), bip.astype(np.float32))
+    outh, _ = gpu_encode(ctx, sub, cuda, 4)
+    assert np.array_equal(outh.float().numpy(), bip.astype(np.float32))
+    out8, _ = gpu_encode(ctx, sub, cuda, 5)
+    assert np.array_equal(out8.numpy(), bip)
 
 
 def test_search_rejects_inexact_range(hdc, cuda):
