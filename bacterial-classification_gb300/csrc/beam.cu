@@ -16,8 +16,10 @@
 //   of them, go on (:191-199).  After `levels` levels the best entry's path is returned.
 //
 // One warp per read: the read's +1/-1 hypervector stays in L1 while the warp
-// streams each candidate prototype with coalesced 16-byte loads; dots are
-// exact int64 (the prototypes of internal nodes exceed int16).
+// streams each candidate prototype with coalesced 16-byte loads, several in
+// flight per lane; dots are exact int64 (the prototypes of internal nodes
+// exceed int16).  The beam bookkeeping lives in shared memory, written by
+// lane 0, so the registers go to loads in flight.
 #include "hdc_internal.cuh"
 #include "topk.cuh"
 
@@ -26,7 +28,8 @@ namespace {
 
 constexpr int kMaxBeam = 8;
 constexpr int kMaxLevels = 8;
-constexpr int kBeamWarps = 4;
+constexpr int kBeamWarps = 8;
+constexpr int kDotUnroll = 4;  // 16-byte prototype loads in flight per lane
 
 struct BeamArgs {
     const int8_t* q;        // [nq][dim] +1/-1
@@ -45,11 +48,29 @@ struct BeamArgs {
     int32_t* depth;         // [nq] levels on the returned path
 };
 
+// exact dot of a +1/-1 int8 read with an int32 prototype row, one warp:
+// lane l covers dims 4l..4l+3 of every 128-dim block; kDotUnroll blocks are
+// loaded before any is used, so each lane keeps that many 16-byte loads in
+// flight (the kernel is bound by gathering rows, not by arithmetic)
 __device__ __forceinline__ int64_t warp_dot_i8_i32(const int8_t* __restrict__ q, const int32_t* __restrict__ v, int dim) {
     const int lane = threadIdx.x & 31;
     int64_t acc = 0;
-    // 4 dims per lane per step: char4 of the query, int4 of the prototype
-    for (int d = 4 * lane; d + 3 < dim; d += 128) {
+    const int full = dim / (128 * kDotUnroll);
+    for (int blk = 0; blk < full; ++blk) {
+        const int d0 = blk * 128 * kDotUnroll + 4 * lane;
+        int4 x[kDotUnroll];
+        char4 s[kDotUnroll];
+#pragma unroll
+        for (int u = 0; u < kDotUnroll; ++u) {
+            x[u] = __ldg(reinterpret_cast<const int4*>(v + d0 + 128 * u));
+            s[u] = *reinterpret_cast<const char4*>(q + d0 + 128 * u);
+        }
+#pragma unroll
+        for (int u = 0; u < kDotUnroll; ++u)
+            acc += (int64_t)s[u].x * x[u].x + (int64_t)s[u].y * x[u].y + (int64_t)s[u].z * x[u].z +
+                   (int64_t)s[u].w * x[u].w;
+    }
+    for (int d = full * 128 * kDotUnroll + 4 * lane; d + 3 < dim; d += 128) {
         const char4 s = *reinterpret_cast<const char4*>(q + d);
         const int4 x = __ldg(reinterpret_cast<const int4*>(v + d));
         acc += (int64_t)s.x * x.x + (int64_t)s.y * x.y + (int64_t)s.z * x.z + (int64_t)s.w * x.w;
@@ -59,28 +80,35 @@ __device__ __forceinline__ int64_t warp_dot_i8_i32(const int8_t* __restrict__ q,
     return acc;
 }
 
-struct Entry {
-    uint64_t key;  // make_key(score, node): larger ranks first
-    int32_t node;
-    int32_t parent_slot;
+// one warp's descent state, in shared memory (lane 0 writes, the warp reads)
+struct WarpBeam {
+    int32_t paths[kMaxBeam][kMaxLevels];
+    float scores[kMaxBeam][kMaxLevels];
+    int32_t np[kMaxBeam][kMaxLevels];
+    float ns[kMaxBeam][kMaxLevels];
+    uint64_t key[kMaxBeam];   // make_key(score, node): larger ranks first
+    int32_t node[kMaxBeam];
+    int32_t slot[kMaxBeam];   // beam row the candidate expanded
+    int n_beam, n_top, done, out_depth;
 };
 
 __global__ void __launch_bounds__(32 * kBeamWarps) beam_kernel(const BeamArgs a) {
+    __shared__ WarpBeam st_all[kBeamWarps];
+    const int lane = threadIdx.x & 31;
+    WarpBeam& st = st_all[threadIdx.x >> 5];
     const int64_t r = (int64_t)blockIdx.x * kBeamWarps + (threadIdx.x >> 5);
-    if (r >= a.nq) return;
+    if (r >= a.nq) return;  // whole warps leave; no block-wide barrier below
     const int8_t* q = a.q + r * a.dim;
     const int64_t qn = a.qn[r];
-    // beam paths, one row per slot
-    int32_t paths[kMaxBeam][kMaxLevels];
-    float scores[kMaxBeam][kMaxLevels];
-    int n_beam = 0;
-    int out_depth = 0;
-    int32_t out_path[kMaxLevels];
-    float out_score[kMaxLevels];
-    for (int L = 0; L < a.levels; ++L) {
-        Entry top[kMaxBeam];
-        int n_top = 0;
-        const int n_src = L == 0 ? 1 : n_beam;
+    if (lane == 0) {
+        st.n_beam = 0;
+        st.done = 0;
+        st.out_depth = 0;
+    }
+    __syncwarp();
+    for (int L = 0; L < a.levels && !st.done; ++L) {
+        if (lane == 0) st.n_top = 0;
+        const int n_src = L == 0 ? 1 : st.n_beam;
         for (int b = 0; b < n_src; ++b) {
             int64_t c0, c1;
             const int32_t* list;
@@ -90,7 +118,7 @@ __global__ void __launch_bounds__(32 * kBeamWarps) beam_kernel(const BeamArgs a)
                 c0 = 0;
                 c1 = a.n_roots;
             } else {
-                const int32_t node = paths[b][L - 1];
+                const int32_t node = st.paths[b][L - 1];
                 c0 = a.child_ptr[node];
                 c1 = a.child_ptr[node + 1];
                 list = a.child_idx;
@@ -100,62 +128,65 @@ __global__ void __launch_bounds__(32 * kBeamWarps) beam_kernel(const BeamArgs a)
             for (int64_t c = 0; c < cnt; ++c) {
                 const int32_t node = self >= 0 ? self : list[c0 + c];
                 const int64_t dot = warp_dot_i8_i32(q, a.proto + (int64_t)node * a.dim, a.dim);
-                const float s = exact_score(dot, qn, a.pn[node], a.mode);
-                const uint64_t key = make_key(s, (uint32_t)node);
-                // keep the best `beam` candidates (uniform across the warp)
-                if (n_top < a.beam || key > top[n_top - 1].key) {
-                    int pos = n_top < a.beam ? n_top++ : a.beam - 1;
-                    while (pos > 0 && top[pos - 1].key < key) {
-                        top[pos] = top[pos - 1];
-                        --pos;
+                if (lane == 0) {  // keep the best `beam` candidates
+                    const uint64_t key = make_key(exact_score(dot, qn, a.pn[node], a.mode), (uint32_t)node);
+                    int n = st.n_top;
+                    if (n < a.beam || key > st.key[n - 1]) {
+                        int pos = n < a.beam ? n++ : a.beam - 1;
+                        while (pos > 0 && st.key[pos - 1] < key) {
+                            st.key[pos] = st.key[pos - 1];
+                            st.node[pos] = st.node[pos - 1];
+                            st.slot[pos] = st.slot[pos - 1];
+                            --pos;
+                        }
+                        st.key[pos] = key;
+                        st.node[pos] = node;
+                        st.slot[pos] = b;
+                        st.n_top = n;
                     }
-                    top[pos] = Entry{key, node, b};
                 }
             }
         }
-        // new beam rows from their parents' rows
-        int32_t np[kMaxBeam][kMaxLevels];
-        float ns[kMaxBeam][kMaxLevels];
-        for (int t = 0; t < n_top; ++t) {
-            for (int l = 0; l < L; ++l) {
-                np[t][l] = paths[top[t].parent_slot][l];
-                ns[t][l] = scores[top[t].parent_slot][l];
+        if (lane == 0) {
+            const int n_top = st.n_top;
+            for (int t = 0; t < n_top; ++t) {  // new beam rows from their parents' rows
+                for (int l = 0; l < L; ++l) {
+                    st.np[t][l] = st.paths[st.slot[t]][l];
+                    st.ns[t][l] = st.scores[st.slot[t]][l];
+                }
+                st.np[t][L] = st.node[t];
+                st.ns[t][L] = key_score(st.key[t]);
             }
-            np[t][L] = top[t].node;
-            ns[t][L] = key_score(top[t].key);
-        }
-        const bool stop = n_top == 0 || (double)key_score(top[0].key) < a.threshold;
-        int keep = 0;
-        while (keep < n_top && keep < a.beam && (double)key_score(top[keep].key) >= a.threshold) ++keep;
-        if (stop) {
-            out_depth = n_top ? L + 1 : L;
-            for (int l = 0; l < out_depth; ++l) {
-                out_path[l] = n_top ? np[0][l] : paths[0][l];
-                out_score[l] = n_top ? ns[0][l] : scores[0][l];
-            }
-            break;
-        }
-        n_beam = keep;
-        for (int t = 0; t < keep; ++t)
-            for (int l = 0; l <= L; ++l) {
-                paths[t][l] = np[t][l];
-                scores[t][l] = ns[t][l];
-            }
-        if (L == a.levels - 1) {
-            out_depth = a.levels;
-            for (int l = 0; l < a.levels; ++l) {
-                out_path[l] = paths[0][l];
-                out_score[l] = scores[0][l];
+            const bool stop = n_top == 0 || (double)key_score(st.key[0]) < a.threshold;
+            if (stop) {
+                st.out_depth = n_top ? L + 1 : L;
+                if (n_top)
+                    for (int l = 0; l <= L; ++l) {
+                        st.paths[0][l] = st.np[0][l];
+                        st.scores[0][l] = st.ns[0][l];
+                    }
+                st.done = 1;
+            } else {
+                int keep = 0;
+                while (keep < n_top && keep < a.beam && (double)key_score(st.key[keep]) >= a.threshold) ++keep;
+                st.n_beam = keep;
+                for (int t = 0; t < keep; ++t)
+                    for (int l = 0; l <= L; ++l) {
+                        st.paths[t][l] = st.np[t][l];
+                        st.scores[t][l] = st.ns[t][l];
+                    }
+                if (L == a.levels - 1) st.out_depth = a.levels;
             }
         }
+        __syncwarp();
     }
-    if ((threadIdx.x & 31) == 0) {
-        a.depth[r] = out_depth;
-        for (int l = 0; l < a.levels; ++l) {
-            a.path[r * a.levels + l] = l < out_depth ? out_path[l] : -1;
-            a.path_score[r * a.levels + l] = l < out_depth ? out_score[l] : 0.0f;
-        }
+    // the returned path is beam row 0
+    for (int l = lane; l < a.levels; l += 32) {
+        const bool in = l < st.out_depth;
+        a.path[r * a.levels + l] = in ? st.paths[0][l] : -1;
+        a.path_score[r * a.levels + l] = in ? st.scores[0][l] : 0.0f;
     }
+    if (lane == 0) a.depth[r] = st.out_depth;
 }
 
 }  // namespace
