@@ -100,3 +100,21 @@ def make_reads(path, n_reads, window, seed):
         for name, r in reads:
             f.write(">%s\n%s\n" % (name, r))
     return out
+
+
+if __name__ == "__main__":
+    # python tests/golden/taxonomy_fixture.py <dir> <n_leaves> <per_species> <seed> [<n_reads> <window> <read_seed>]
+    # writes the taxonomy (and reads.fasta) into <dir>, for timing the applications by hand
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(os.path.dirname(here))
+    sys.path.insert(0, os.path.join(root, "bacterial-classification_gb300"))
+    import build as pkg_build
+    pkg_build.build()
+    import hdc_gb300
+    a = sys.argv[1:]
+    os.makedirs(a[0], exist_ok=True)
+    make_taxonomy_dir(a[0], hdc_gb300, int(a[1]), int(a[2]), int(a[3]))
+    if len(a) > 4:
+        make_reads(a[0], int(a[4]), int(a[5]), int(a[6]))
+    print(input_digest(a[0]) if len(a) <= 4 else a[0])
