@@ -224,6 +224,22 @@ int hdc_search_tc_tuning(hdc_context* ctx, int group_tiles, int l2_policy, int t
     return HDC_OK;
 }
 
+int hdc_search_tc_option(hdc_context* ctx, int option, int value) {
+    if (!ctx) return fail(HDC_ERR_INVALID, "tc option: null context");
+    switch (option) {
+        case HDC_TC_PREFETCH:
+            if (value < -1 || value > 64) return fail(HDC_ERR_INVALID, "tc option: prefetch must be in -1..64");
+            ctx->tc_prefetch = value;
+            return HDC_OK;
+        case HDC_TC_CLUSTER:
+            if (value < 0 || value > 2) return fail(HDC_ERR_INVALID, "tc option: cluster must be 0, 1 or 2");
+            ctx->tc_cluster = value;
+            return HDC_OK;
+        default:
+            return fail(HDC_ERR_INVALID, "tc option: unknown option");
+    }
+}
+
 int hdc_bundle(hdc_context* ctx, const void* d_rows, int elem_bytes, const int64_t* d_child_ptr,
                const int32_t* d_child_idx, int64_t n_parents, int32_t* d_out, void* stream) {
     if (!ctx) return fail(HDC_ERR_INVALID, "bundle: null context");

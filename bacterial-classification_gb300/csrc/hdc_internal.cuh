@@ -26,6 +26,8 @@ struct hdc_context {
     int tc_policy = -1;             // tensor-core search: L2 policy (-1: automatic, see hdc_search_tc_tuning)
     int tc_tile_n = 0;              // tensor-core search: references per tile, 128 or 256 (0: automatic)
     int tc_m_blocks = 0;            // tensor-core search: 128-query M-blocks per CTA, 1 or 2 (0: automatic)
+    int tc_prefetch = -1;           // tensor-core search: K blocks prefetched into L2 ahead (-1: automatic)
+    int tc_cluster = 0;             // tensor-core search: CTAs sharing reference blocks, 1 or 2 (0: automatic)
 };
 
 // A tensor-core reference database (hdc_refdb_create).
@@ -76,6 +78,8 @@ void refdb_destroy(hdc_refdb* db);
 size_t tc_workspace_bytes(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int k);
 int tc_default_group();
 int tc_default_policy();
+int tc_default_prefetch();
+int tc_default_cluster();
 int tc_default_tile_n();
 int tc_default_m_blocks();
 int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, const int64_t* d_qn, int64_t nq,

@@ -86,6 +86,7 @@ struct TcArgs {
     int n_qtiles, n_rtiles;
     int G, S, n_groups;   // query tiles per group, reference lanes, groups
     int policy;           // 0: no L2 hint, 1: queries evict-last, 2: + references evict-first
+    int prefetch;         // K blocks of the same tile pair prefetched into L2 ahead of the ring (0: none)
     const int64_t* qn;    // [nq] squared norms of the queries
     const int64_t* rn;    // [nr] squared norms of the references
     const float* rr;      // [nr] fp32 1/sqrt(norm)
@@ -100,7 +101,7 @@ __device__ __forceinline__ float approx_tc(float af, float rq, float rr, int mod
     return mode == HDC_SCORE_NORM ? fmaf(2.0f, c, -1.0f) : c;
 }
 
-template <int L, int kBN, int MB>
+template <int L, int kBN, int MB, int CL>
 __global__ void __launch_bounds__(kThreadsTC, 1)
     tc_search_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcArgs a) {
     using T = Tile<kBN>;
@@ -127,7 +128,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         err_s = 0;
         for (int s = 0; s < STAGES; ++s) {
             tc::mbar_init(&full_bar[s], 1);
-            tc::mbar_init(&empty_bar[s], 1);
+            tc::mbar_init(&empty_bar[s], CL);  // one commit from each CTA that reads the stage's multicast
         }
         for (int b = 0; b < ACC; ++b) {
             tc::mbar_init(&accf_bar[b], 1);
@@ -144,7 +145,13 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
+    if constexpr (CL > 1) tc::cluster_sync();  // the peer's barriers exist before anything targets them
     const uint32_t tmem = tmem_base_s;
+    // A pair of CTAs (CL = 2) runs the same reference tiles for two query tiles: the pair
+    // takes part in a group when its first CTA has a query tile; a CTA without one loads
+    // the last tile again, shares its half of every reference block, and writes nothing.
+    const int gslot = (int)(blockIdx.x % a.G);
+    const int lead_slot = gslot & ~(CL - 1);
 
     if (warp == 0) {
         // ------------------------------------------------ TMA producer
@@ -155,9 +162,10 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             bool ok = true;
             const uint64_t pol_q = tc::make_policy_evict_last(), pol_r = tc::make_policy_evict_first();
             const bool hint_q = a.policy >= 1, hint_r = a.policy >= 2;
+            const int rank = CL > 1 ? (int)tc::cluster_ctarank() : 0;
             for (int grp = 0; ok && grp < a.n_groups; ++grp) {
-                const int qt = grp * a.G + (int)(blockIdx.x % a.G);
-                if (qt >= a.n_qtiles) continue;
+                if (grp * a.G + lead_slot >= a.n_qtiles) continue;
+                const int qt = min(grp * a.G + gslot, a.n_qtiles - 1);
                 for (int t = (int)(blockIdx.x / a.G); ok && t < a.n_rtiles; t += a.S) {
                     for (int kb = 0; kb < a.n_kblocks; ++kb) {
                         if (!tc::mbar_wait(&empty_bar[stage], phase ^ 1, &err_s, 1)) {
@@ -176,12 +184,30 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         }
 #pragma unroll
                         for (int l = 0; l < L; ++l) {
+                            if constexpr (CL > 1) {
+                                // this CTA's 1/CL of the block's rows, into every CTA of the pair
+                                void* dst = st + (size_t)T::A_BYTES * MB + (size_t)T::B_BYTES * l +
+                                            (size_t)rank * (T::B_BYTES / CL);
+                                const int y = (int)(l * a.r_pad + (int64_t)t * kBN) + rank * (kBN / CL);
+                                tc::tma_load_2d_mc(dst, &tmB, &full_bar[stage], kb * kBK, y, (uint16_t)((1u << CL) - 1));
+                                continue;
+                            }
                             void* dst = st + (size_t)T::A_BYTES * MB + (size_t)T::B_BYTES * l;
                             const int y = (int)(l * a.r_pad + (int64_t)t * kBN);
                             if (hint_r)
                                 tc::tma_load_2d_hint(dst, &tmB, &full_bar[stage], kb * kBK, y, pol_r);
                             else
                                 tc::tma_load_2d(dst, &tmB, &full_bar[stage], kb * kBK, y);
+                        }
+                        if (CL == 1 && a.prefetch > 0 && kb + a.prefetch < a.n_kblocks) {
+                            // the ring holds STAGES blocks in flight; start the one `prefetch` blocks
+                            // ahead toward L2 now, so its load later finds it there
+                            const int xk = (kb + a.prefetch) * kBK;
+#pragma unroll
+                            for (int m = 0; m < MB; ++m) tc::tma_prefetch_2d(&tmA, xk, qt * QT + m * kBM);
+#pragma unroll
+                            for (int l = 0; l < L; ++l)
+                                tc::tma_prefetch_2d(&tmB, xk, (int)(l * a.r_pad + (int64_t)t * kBN));
                         }
                         ++issued;
                         if (++stage == STAGES) {
@@ -210,9 +236,9 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             int stage = 0, acc = 0;
             uint32_t phase = 0, acc_phase = 0;
             bool ok = true;
+            int64_t consumed = 0;
             for (int grp = 0; ok && grp < a.n_groups; ++grp) {
-                const int qt = grp * a.G + (int)(blockIdx.x % a.G);
-                if (qt >= a.n_qtiles) continue;
+                if (grp * a.G + lead_slot >= a.n_qtiles) continue;
                 for (int t = (int)(blockIdx.x / a.G); ok && t < a.n_rtiles; t += a.S) {
                     if (!tc::mbar_wait(&acce_bar[acc], acc_phase ^ 1, &err_s, 2)) {
                         ok = false;
@@ -240,7 +266,12 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                                                 IDESC, (kb | kk) != 0 ? 1u : 0u);
                             }
                         }
-                        tc::mma_commit(&empty_bar[stage]);  // frees the stage when these MMAs finish
+                        // frees the stage (in every CTA of the pair) when these MMAs finish
+                        if constexpr (CL > 1)
+                            tc::mma_commit_mc(&empty_bar[stage], (uint16_t)((1u << CL) - 1));
+                        else
+                            tc::mma_commit(&empty_bar[stage]);
+                        ++consumed;
                         if (++stage == STAGES) {
                             stage = 0;
                             phase ^= 1;
@@ -251,6 +282,21 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     if (++acc == ACC) {
                         acc = 0;
                         acc_phase ^= 1;
+                    }
+                }
+            }
+            if constexpr (CL > 1) {
+                // the peer's commits for the last stages arrive on this CTA's barriers: let them
+                // land before the CTA can leave (bounded)
+                int s_ = stage;
+                uint32_t ph = phase;
+                for (int64_t i = 0; i < (consumed < STAGES ? consumed : (int64_t)STAGES); ++i) {
+                    if (--s_ < 0) {
+                        s_ = STAGES - 1;
+                        ph ^= 1;
+                    }
+                    const long long c0 = clock64();
+                    while (!tc::mbar_try_wait(tc::smem_u32(&empty_bar[s_]), ph) && clock64() - c0 < tc::kWaitCycles) {
                     }
                 }
             }
@@ -268,8 +314,8 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         int64_t dots[MB][kMaxKTC];
         const int lane_j = (int)(blockIdx.x / a.G);
         for (int grp = 0; ok && grp < a.n_groups; ++grp) {
-            const int qt = grp * a.G + (int)(blockIdx.x % a.G);
-            if (qt >= a.n_qtiles) continue;
+            if (grp * a.G + lead_slot >= a.n_qtiles) continue;
+            const int qt = grp * a.G + gslot;  // past the last tile for a CTA without one: no live rows
             // this thread owns query row `row` of each M-block
             int64_t gq[MB], my_qn[MB];
             float my_rq[MB], thr[MB];
@@ -358,6 +404,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         tc::tmem_dealloc(tmem, TCOLS);
     }
     if (threadIdx.x == 0 && err_s) atomicCAS(a.status, 0, 100 + err_s);
+    if constexpr (CL > 1) tc::cluster_sync();  // no CTA leaves while its peer may still write into it
 }
 
 // ---------------------------------------------------------------- database build
@@ -505,6 +552,8 @@ void refdb_destroy(hdc_refdb* db) {
 
 int tc_default_group() { return 1 << 30; }  // every SM on its own query tile, references shared
 int tc_default_policy() { return 0; }
+int tc_default_prefetch() { return 0; }
+int tc_default_cluster() { return 2; }
 int tc_default_tile_n() { return 128; }
 int tc_default_m_blocks() { return 1; }
 
@@ -521,36 +570,65 @@ static int tc_m_blocks(const hdc_context* ctx, const hdc_refdb* db) {
     return (mb == 2 && db->L <= 2 && tc_tile_n(ctx, db) == 128) ? 2 : 1;
 }
 
+// CTA pairs sharing reference blocks by multicast: N = 128, one M-block, and an
+// even number of query tiles per group (a pair must not straddle two lanes).
+static int tc_cluster(const hdc_context* ctx, const hdc_refdb* db) {
+    const int c = ctx->tc_cluster > 0 ? ctx->tc_cluster : tc_default_cluster();
+    return (c == 2 && tc_tile_n(ctx, db) == 128 && tc_m_blocks(ctx, db) == 1) ? 2 : 1;
+}
+
 static void tc_plan(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int& n_qtiles, int& n_rtiles, int& G,
-                    int& S, int& n_groups) {
+                    int& S, int& n_groups, int& CL) {
     const int qt_rows = kBM * tc_m_blocks(ctx, db);
     n_qtiles = (int)((nq + qt_rows - 1) / qt_rows);
     n_rtiles = (int)(db->r_pad / tc_tile_n(ctx, db));
     const int want = ctx->tc_group > 0 ? ctx->tc_group : tc_default_group();
     G = std::max(1, std::min(std::min(want, ctx->num_sms), n_qtiles));
+    CL = tc_cluster(ctx, db);
+    if (CL == 2 && G >= 2 && (G & 1)) --G;
+    if (G < 2) CL = 1;
     S = std::max(1, ctx->num_sms / G);
     S = std::min(S, n_rtiles);
     n_groups = (n_qtiles + G - 1) / G;
 }
 
 size_t tc_workspace_bytes(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int k) {
-    int qt, rt, G, S, ng;
-    tc_plan(ctx, nq, db, qt, rt, G, S, ng);
+    int qt, rt, G, S, ng, CL;
+    tc_plan(ctx, nq, db, qt, rt, G, S, ng, CL);
     k = (int)std::min<int64_t>(k, db->nr);
     return (size_t)S * nq * std::max(k, 1) * (sizeof(uint64_t) + sizeof(int64_t));
 }
 
-template <int L, int N, int MB>
+template <int L, int N, int MB, int CL>
 static int launch_tc_t(const __half* d_q, const hdc_refdb* db, const TcArgs& a, int grid, cudaStream_t stream) {
     CUtensorMap tmA, tmB;
+    // with CL CTAs sharing a reference block, each loads (and multicasts) N / CL of its rows
     if (!make_tmap(&tmA, d_q, a.nq, a.dim, Tile<N>::BK, kBM) ||
-        !make_tmap(&tmB, db->d_limbs, (int64_t)db->L * db->r_pad, a.dim, Tile<N>::BK, N))
+        !make_tmap(&tmB, db->d_limbs, (int64_t)db->L * db->r_pad, a.dim, Tile<N>::BK, N / CL))
         return fail(HDC_ERR_CUDA, "tc search: cuTensorMapEncodeTiled failed");
     const size_t smem = (size_t)tc_stages<N>(L, MB) * tc_stage_bytes<N>(L, MB) + 1024;
-    auto kern = tc_search_kernel<L, N, MB>;
+    auto kern = tc_search_kernel<L, N, MB, CL>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_fail(e, "tc search: cudaFuncSetAttribute");
-    kern<<<grid, kThreadsTC, smem, stream>>>(tmA, tmB, a);
+    if constexpr (CL == 1) {
+        kern<<<grid, kThreadsTC, smem, stream>>>(tmA, tmB, a);
+    } else {
+        if (grid % CL) return fail(HDC_ERR_INVALID, "tc search: grid is not a whole number of clusters");
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)grid, 1, 1);
+        cfg.blockDim = dim3(kThreadsTC, 1, 1);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = stream;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = CL;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        e = cudaLaunchKernelEx(&cfg, kern, tmA, tmB, a);
+        if (e != cudaSuccess) return cuda_fail(e, "tc search: cluster launch");
+    }
     e = cudaGetLastError();
     return e == cudaSuccess ? HDC_OK : cuda_fail(e, "tc search: launch");
 }
@@ -578,7 +656,8 @@ int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, c
     a.mode = mode;
     a.n_kblocks = (ctx->dim + (N == 256 ? Tile<256>::BK : Tile<128>::BK) - 1) / (N == 256 ? Tile<256>::BK : Tile<128>::BK);
     a.r_pad = db->r_pad;
-    tc_plan(ctx, nq, db, a.n_qtiles, a.n_rtiles, a.G, a.S, a.n_groups);
+    int CL = 1;
+    tc_plan(ctx, nq, db, a.n_qtiles, a.n_rtiles, a.G, a.S, a.n_groups, CL);
     a.qn = d_qn;
     a.rn = db->d_norm2;
     a.rr = db->d_rsq;
@@ -588,25 +667,33 @@ int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, c
     a.ws_dot = reinterpret_cast<int64_t*>(a.ws_key + (size_t)a.S * nq * k);
     a.status = d_status;
     a.policy = ctx->tc_policy >= 0 ? ctx->tc_policy : tc_default_policy();
+    a.prefetch = ctx->tc_prefetch >= 0 ? ctx->tc_prefetch : tc_default_prefetch();
     const int grid = a.G * a.S;
     int st;
     const int MB = tc_m_blocks(ctx, db);
     if (N == 256) {
         switch (db->L) {
-            case 1: st = launch_tc_t<1, 256, 1>(d_q, db, a, grid, stream); break;
-            default: st = launch_tc_t<2, 256, 1>(d_q, db, a, grid, stream); break;
+            case 1: st = launch_tc_t<1, 256, 1, 1>(d_q, db, a, grid, stream); break;
+            default: st = launch_tc_t<2, 256, 1, 1>(d_q, db, a, grid, stream); break;
         }
     } else if (MB == 2) {
         switch (db->L) {
-            case 1: st = launch_tc_t<1, 128, 2>(d_q, db, a, grid, stream); break;
-            default: st = launch_tc_t<2, 128, 2>(d_q, db, a, grid, stream); break;
+            case 1: st = launch_tc_t<1, 128, 2, 1>(d_q, db, a, grid, stream); break;
+            default: st = launch_tc_t<2, 128, 2, 1>(d_q, db, a, grid, stream); break;
+        }
+    } else if (CL == 2) {
+        switch (db->L) {
+            case 1: st = launch_tc_t<1, 128, 1, 2>(d_q, db, a, grid, stream); break;
+            case 2: st = launch_tc_t<2, 128, 1, 2>(d_q, db, a, grid, stream); break;
+            case 3: st = launch_tc_t<3, 128, 1, 2>(d_q, db, a, grid, stream); break;
+            default: st = launch_tc_t<4, 128, 1, 2>(d_q, db, a, grid, stream); break;
         }
     } else {
         switch (db->L) {
-            case 1: st = launch_tc_t<1, 128, 1>(d_q, db, a, grid, stream); break;
-            case 2: st = launch_tc_t<2, 128, 1>(d_q, db, a, grid, stream); break;
-            case 3: st = launch_tc_t<3, 128, 1>(d_q, db, a, grid, stream); break;
-            default: st = launch_tc_t<4, 128, 1>(d_q, db, a, grid, stream); break;
+            case 1: st = launch_tc_t<1, 128, 1, 1>(d_q, db, a, grid, stream); break;
+            case 2: st = launch_tc_t<2, 128, 1, 1>(d_q, db, a, grid, stream); break;
+            case 3: st = launch_tc_t<3, 128, 1, 1>(d_q, db, a, grid, stream); break;
+            default: st = launch_tc_t<4, 128, 1, 1>(d_q, db, a, grid, stream); break;
         }
     }
     if (st != HDC_OK) return st;

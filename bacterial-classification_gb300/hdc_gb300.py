@@ -15,6 +15,7 @@ HDC_OK = 0
 ERR = {1: "HDC_ERR_INVALID", 2: "HDC_ERR_RANGE", 3: "HDC_ERR_CUDA", 4: "HDC_ERR_NOMEM",
        5: "HDC_ERR_UNSUPPORTED", 6: "HDC_ERR_TIMEOUT"}
 SCORE_NORM, SCORE_COS, SCORE_DOT = 0, 1, 2
+TC_PREFETCH, TC_CLUSTER = 1, 2
 OUT_I16, OUT_I32, OUT_BIPOLAR_BF16, OUT_BIPOLAR_I16, OUT_BIPOLAR_F16, OUT_BIPOLAR_I8 = 0, 1, 2, 3, 4, 5
 
 # (name, restype, argtypes) of every exported entry point
@@ -49,6 +50,7 @@ SIGNATURES = [
     ("hdc_refdb_limbs", I32, [P]),
     ("hdc_search_tc_workspace_bytes", SZ, [P, P, I64, I32]),
     ("hdc_search_tc_tuning", I32, [P, I32, I32, I32, I32]),
+    ("hdc_search_tc_option", I32, [P, I32, I32]),
     ("hdc_pipeline_create", I32, [P, P, I64, I64, ctypes.c_int32, I32, I32, ctypes.POINTER(P)]),
     ("hdc_pipeline_destroy", None, [P]),
     ("hdc_pipeline_run", I32, [P, P, P, P, I64, P, P]),
@@ -176,6 +178,9 @@ class Context:
         st = ctypes.c_int(0)
         check(lib().hdc_context_status(self.h, ctypes.byref(st)))
         return st.value
+
+    def tc_option(self, option, value):
+        check(lib().hdc_search_tc_option(self.h, option, value))
 
     def tc_tuning(self, group_tiles=0, l2_policy=-1, tile_n=0, m_blocks=0):
         check(lib().hdc_search_tc_tuning(self.h, group_tiles, l2_policy, tile_n, m_blocks))

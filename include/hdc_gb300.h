@@ -210,6 +210,16 @@ int hdc_search_plain_noalloc(hdc_context* ctx, const int16_t* d_q, const int64_t
  * on these settings, only the speed does. */
 int hdc_search_tc_tuning(hdc_context* ctx, int group_tiles, int l2_policy, int tile_n, int m_blocks);
 
+/* Further tensor-core search settings; results do not depend on them.
+ *   HDC_TC_PREFETCH: K blocks of each query/reference tile pair prefetched
+ *     into L2 ahead of the shared-memory ring (0: none, -1: automatic, <= 64);
+ *   HDC_TC_CLUSTER: CTAs that share each reference block through a TMA
+ *     multicast, 1 or 2 (0: automatic; 2 applies with tile_n 128 and one
+ *     M-block, and pairs CTAs of neighbouring query tiles). */
+#define HDC_TC_PREFETCH 1
+#define HDC_TC_CLUSTER 2
+int hdc_search_tc_option(hdc_context* ctx, int option, int value);
+
 /* Hierarchical descent (config 5; targets/identify.cpp:89-202 with one
  * prototype hypervector per taxonomy node): beam search of +1/-1 int8 read
  * hypervectors [nq][dim] down a tree whose nodes carry int32 prototypes
