@@ -235,6 +235,10 @@ int hdc_search_tc_option(hdc_context* ctx, int option, int value) {
             if (value < 0 || value > 2) return fail(HDC_ERR_INVALID, "tc option: cluster must be 0, 1 or 2");
             ctx->tc_cluster = value;
             return HDC_OK;
+        case HDC_TC_SHARE:
+            if (value < -1 || value > 1) return fail(HDC_ERR_INVALID, "tc option: share must be -1, 0 or 1");
+            ctx->tc_share = value;
+            return HDC_OK;
         default:
             return fail(HDC_ERR_INVALID, "tc option: unknown option");
     }

@@ -27,7 +27,8 @@ struct hdc_context {
     int tc_tile_n = 0;              // tensor-core search: references per tile, 128 or 256 (0: automatic)
     int tc_m_blocks = 0;            // tensor-core search: 128-query M-blocks per CTA, 1 or 2 (0: automatic)
     int tc_prefetch = -1;           // tensor-core search: K blocks prefetched into L2 ahead (-1: automatic)
-    int tc_cluster = 0;             // tensor-core search: CTAs sharing reference blocks, 1 or 2 (0: automatic)
+    int tc_cluster = 0;             // tensor-core search: CTAs sharing an operand's blocks, 1 or 2 (0: automatic)
+    int tc_share = -1;              // tensor-core search: 0 pairs share references, 1 queries (-1: automatic)
 };
 
 // A tensor-core reference database (hdc_refdb_create).
@@ -80,6 +81,7 @@ int tc_default_group();
 int tc_default_policy();
 int tc_default_prefetch();
 int tc_default_cluster();
+int tc_default_share();
 int tc_default_tile_n();
 int tc_default_m_blocks();
 int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, const int64_t* d_qn, int64_t nq,

@@ -101,7 +101,7 @@ __device__ __forceinline__ float approx_tc(float af, float rq, float rr, int mod
     return mode == HDC_SCORE_NORM ? fmaf(2.0f, c, -1.0f) : c;
 }
 
-template <int L, int kBN, int MB, int CL>
+template <int L, int kBN, int MB, int CL, bool SHARE_A>
 __global__ void __launch_bounds__(kThreadsTC, 1)
     tc_search_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcArgs a) {
     using T = Tile<kBN>;
@@ -113,6 +113,8 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     constexpr uint32_t kStageBytes = (uint32_t)tc_stage_bytes<kBN>(L, MB);
     constexpr uint32_t kAccCols = (uint32_t)(MB * L * kBN);
     constexpr uint32_t IDESC = tc::idesc_f16_f32(kBM, kBN);
+    constexpr bool kPairLimbs = kBN == 128 && L >= 2;  // limb pairs as one N = 256 MMA
+    constexpr uint32_t IDESC2 = kPairLimbs ? tc::idesc_f16_f32(kBM, 2 * kBN) : IDESC;
     static_assert(MB * L * kBN <= 512, "accumulators exceed TMEM");
 
     extern __shared__ uint8_t smem_raw[];
@@ -147,11 +149,18 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     tc::fence_after();
     if constexpr (CL > 1) tc::cluster_sync();  // the peer's barriers exist before anything targets them
     const uint32_t tmem = tmem_base_s;
-    // A pair of CTAs (CL = 2) runs the same reference tiles for two query tiles: the pair
-    // takes part in a group when its first CTA has a query tile; a CTA without one loads
-    // the last tile again, shares its half of every reference block, and writes nothing.
-    const int gslot = (int)(blockIdx.x % a.G);
-    const int lead_slot = gslot & ~(CL - 1);
+    // CTA pairs (CL = 2) share one operand by multicast.  Sharing references: the pair
+    // runs the same reference tiles for two neighbouring query tiles, and takes part in a
+    // group when its first CTA has a query tile (a CTA without one loads the last tile
+    // again and writes nothing).  Sharing queries (SHARE_A): the pair runs one query
+    // tile on two neighbouring reference lanes, tile by tile in step (the tile count is
+    // even, so both CTAs of a pair have a tile in every step; the clamp below only guards).
+    const int gslot = SHARE_A ? (int)((blockIdx.x / CL) % a.G) : (int)(blockIdx.x % a.G);
+    const int lane_j = SHARE_A ? CL * (int)((blockIdx.x / CL) / a.G) + (int)(blockIdx.x % CL) : (int)(blockIdx.x / a.G);
+    const int lead_slot = SHARE_A ? gslot : gslot & ~(CL - 1);
+    const int pair_rank = CL > 1 ? (int)(blockIdx.x % CL) : 0;
+    const int t_first = SHARE_A ? lane_j - pair_rank : lane_j;  // both CTAs of a pair step through the same t0
+    const int t_off = SHARE_A ? pair_rank : 0;
 
     if (warp == 0) {
         // ------------------------------------------------ TMA producer
@@ -166,7 +175,8 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             for (int grp = 0; ok && grp < a.n_groups; ++grp) {
                 if (grp * a.G + lead_slot >= a.n_qtiles) continue;
                 const int qt = min(grp * a.G + gslot, a.n_qtiles - 1);
-                for (int t = (int)(blockIdx.x / a.G); ok && t < a.n_rtiles; t += a.S) {
+                for (int t0 = t_first; ok && t0 < a.n_rtiles; t0 += a.S) {
+                    const int t = min(t0 + t_off, a.n_rtiles - 1);
                     for (int kb = 0; kb < a.n_kblocks; ++kb) {
                         if (!tc::mbar_wait(&empty_bar[stage], phase ^ 1, &err_s, 1)) {
                             ok = false;
@@ -176,6 +186,13 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         tc::mbar_arrive_expect_tx(&full_bar[stage], kStageBytes);
 #pragma unroll
                         for (int m = 0; m < MB; ++m) {
+                            if constexpr (SHARE_A) {
+                                // this CTA's 1/CL of the query block's rows, into every CTA of the pair
+                                void* dst = st + (size_t)T::A_BYTES * m + (size_t)rank * (T::A_BYTES / CL);
+                                tc::tma_load_2d_mc(dst, &tmA, &full_bar[stage], kb * kBK,
+                                                   qt * QT + m * kBM + rank * (kBM / CL), (uint16_t)((1u << CL) - 1));
+                                continue;
+                            }
                             void* dst = st + (size_t)T::A_BYTES * m;
                             if (hint_q)
                                 tc::tma_load_2d_hint(dst, &tmA, &full_bar[stage], kb * kBK, qt * QT + m * kBM, pol_q);
@@ -184,7 +201,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         }
 #pragma unroll
                         for (int l = 0; l < L; ++l) {
-                            if constexpr (CL > 1) {
+                            if constexpr (CL > 1 && !SHARE_A) {
                                 // this CTA's 1/CL of the block's rows, into every CTA of the pair
                                 void* dst = st + (size_t)T::A_BYTES * MB + (size_t)T::B_BYTES * l +
                                             (size_t)rank * (T::B_BYTES / CL);
@@ -239,7 +256,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             int64_t consumed = 0;
             for (int grp = 0; ok && grp < a.n_groups; ++grp) {
                 if (grp * a.G + lead_slot >= a.n_qtiles) continue;
-                for (int t = (int)(blockIdx.x / a.G); ok && t < a.n_rtiles; t += a.S) {
+                for (int t0 = t_first; ok && t0 < a.n_rtiles; t0 += a.S) {
                     if (!tc::mbar_wait(&acce_bar[acc], acc_phase ^ 1, &err_s, 2)) {
                         ok = false;
                         break;
@@ -255,6 +272,11 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         const uint32_t sa = tc::smem_u32(ring + (size_t)stage * kStageBytes);
 #pragma unroll
                         for (int l = 0; l < L; ++l) {
+                            // With 128-row tiles two neighbouring limbs' blocks are 256 consecutive
+                            // rows, and their accumulators 256 consecutive columns: one N = 256 MMA
+                            // covers both, reading each query slice from shared memory once.
+                            if (kPairLimbs && (l & 1)) continue;
+                            const bool wide = kPairLimbs && l + 1 < L;
                             const uint64_t bdesc = tc::kmajor_desc(
                                 sa + (uint32_t)T::A_BYTES * MB + (uint32_t)T::B_BYTES * l, T::SBO, T::LAYOUT);
 #pragma unroll
@@ -263,7 +285,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
 #pragma unroll
                                 for (int kk = 0; kk < kBK / 16; ++kk)  // K = 16 fp16 per MMA = 32 bytes
                                     tc::mma_f16(d0 + (uint32_t)((m * L + l) * kBN), adesc + 2 * kk, bdesc + 2 * kk,
-                                                IDESC, (kb | kk) != 0 ? 1u : 0u);
+                                                wide ? IDESC2 : IDESC, (kb | kk) != 0 ? 1u : 0u);
                             }
                         }
                         // frees the stage (in every CTA of the pair) when these MMAs finish
@@ -312,7 +334,6 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         bool ok = true;
         uint64_t keys[MB][kMaxKTC];
         int64_t dots[MB][kMaxKTC];
-        const int lane_j = (int)(blockIdx.x / a.G);
         for (int grp = 0; ok && grp < a.n_groups; ++grp) {
             if (grp * a.G + lead_slot >= a.n_qtiles) continue;
             const int qt = grp * a.G + gslot;  // past the last tile for a CTA without one: no live rows
@@ -332,7 +353,8 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     dots[m][i] = 0;
                 }
             }
-            for (int t = lane_j; t < a.n_rtiles; t += a.S) {
+            for (int t0 = t_first; t0 < a.n_rtiles; t0 += a.S) {
+                const int t = t0 + t_off;
                 if (!tc::mbar_wait(&accf_bar[acc], acc_phase, &err_s, 4)) {
                     ok = false;
                     break;
@@ -554,6 +576,7 @@ int tc_default_group() { return 1 << 30; }  // every SM on its own query tile, r
 int tc_default_policy() { return 0; }
 int tc_default_prefetch() { return 0; }
 int tc_default_cluster() { return 2; }
+int tc_default_share() { return 0; }
 int tc_default_tile_n() { return 128; }
 int tc_default_m_blocks() { return 1; }
 
@@ -577,37 +600,50 @@ static int tc_cluster(const hdc_context* ctx, const hdc_refdb* db) {
     return (c == 2 && tc_tile_n(ctx, db) == 128 && tc_m_blocks(ctx, db) == 1) ? 2 : 1;
 }
 
+// share = 0: a pair shares reference blocks (neighbouring query tiles, G even);
+// share = 1: a pair shares query blocks (neighbouring reference lanes, S even).
 static void tc_plan(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int& n_qtiles, int& n_rtiles, int& G,
-                    int& S, int& n_groups, int& CL) {
+                    int& S, int& n_groups, int& CL, int& share) {
     const int qt_rows = kBM * tc_m_blocks(ctx, db);
     n_qtiles = (int)((nq + qt_rows - 1) / qt_rows);
     n_rtiles = (int)(db->r_pad / tc_tile_n(ctx, db));
-    const int want = ctx->tc_group > 0 ? ctx->tc_group : tc_default_group();
-    G = std::max(1, std::min(std::min(want, ctx->num_sms), n_qtiles));
     CL = tc_cluster(ctx, db);
-    if (CL == 2 && G >= 2 && (G & 1)) --G;
-    if (G < 2) CL = 1;
+    share = CL == 2 ? (ctx->tc_share >= 0 ? ctx->tc_share : tc_default_share()) : 0;
+    const int want = ctx->tc_group > 0 ? ctx->tc_group : (share ? ctx->num_sms / 2 : tc_default_group());
+    G = std::max(1, std::min(std::min(want, ctx->num_sms), n_qtiles));
+    if (CL == 2 && !share) {
+        if (G >= 2 && (G & 1)) --G;
+        if (G < 2) CL = 1;
+    }
     S = std::max(1, ctx->num_sms / G);
     S = std::min(S, n_rtiles);
+    if (CL == 2 && share) {
+        S &= ~1;
+        if (S < 2) {
+            CL = 1;
+            share = 0;
+            S = std::max(1, std::min(ctx->num_sms / G, n_rtiles));
+        }
+    }
     n_groups = (n_qtiles + G - 1) / G;
 }
 
 size_t tc_workspace_bytes(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int k) {
-    int qt, rt, G, S, ng, CL;
-    tc_plan(ctx, nq, db, qt, rt, G, S, ng, CL);
+    int qt, rt, G, S, ng, CL, share;
+    tc_plan(ctx, nq, db, qt, rt, G, S, ng, CL, share);
     k = (int)std::min<int64_t>(k, db->nr);
     return (size_t)S * nq * std::max(k, 1) * (sizeof(uint64_t) + sizeof(int64_t));
 }
 
-template <int L, int N, int MB, int CL>
+template <int L, int N, int MB, int CL, bool SHARE_A = false>
 static int launch_tc_t(const __half* d_q, const hdc_refdb* db, const TcArgs& a, int grid, cudaStream_t stream) {
     CUtensorMap tmA, tmB;
-    // with CL CTAs sharing a reference block, each loads (and multicasts) N / CL of its rows
-    if (!make_tmap(&tmA, d_q, a.nq, a.dim, Tile<N>::BK, kBM) ||
-        !make_tmap(&tmB, db->d_limbs, (int64_t)db->L * db->r_pad, a.dim, Tile<N>::BK, N / CL))
+    // with CL CTAs sharing a block, each loads (and multicasts) 1 / CL of its rows
+    if (!make_tmap(&tmA, d_q, a.nq, a.dim, Tile<N>::BK, SHARE_A ? kBM / CL : kBM) ||
+        !make_tmap(&tmB, db->d_limbs, (int64_t)db->L * db->r_pad, a.dim, Tile<N>::BK, SHARE_A ? N : N / CL))
         return fail(HDC_ERR_CUDA, "tc search: cuTensorMapEncodeTiled failed");
     const size_t smem = (size_t)tc_stages<N>(L, MB) * tc_stage_bytes<N>(L, MB) + 1024;
-    auto kern = tc_search_kernel<L, N, MB, CL>;
+    auto kern = tc_search_kernel<L, N, MB, CL, SHARE_A>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_fail(e, "tc search: cudaFuncSetAttribute");
     if constexpr (CL == 1) {
@@ -656,8 +692,8 @@ int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, c
     a.mode = mode;
     a.n_kblocks = (ctx->dim + (N == 256 ? Tile<256>::BK : Tile<128>::BK) - 1) / (N == 256 ? Tile<256>::BK : Tile<128>::BK);
     a.r_pad = db->r_pad;
-    int CL = 1;
-    tc_plan(ctx, nq, db, a.n_qtiles, a.n_rtiles, a.G, a.S, a.n_groups, CL);
+    int CL = 1, share = 0;
+    tc_plan(ctx, nq, db, a.n_qtiles, a.n_rtiles, a.G, a.S, a.n_groups, CL, share);
     a.qn = d_qn;
     a.rn = db->d_norm2;
     a.rr = db->d_rsq;
@@ -680,6 +716,13 @@ int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, c
         switch (db->L) {
             case 1: st = launch_tc_t<1, 128, 2, 1>(d_q, db, a, grid, stream); break;
             default: st = launch_tc_t<2, 128, 2, 1>(d_q, db, a, grid, stream); break;
+        }
+    } else if (CL == 2 && share) {
+        switch (db->L) {
+            case 1: st = launch_tc_t<1, 128, 1, 2, true>(d_q, db, a, grid, stream); break;
+            case 2: st = launch_tc_t<2, 128, 1, 2, true>(d_q, db, a, grid, stream); break;
+            case 3: st = launch_tc_t<3, 128, 1, 2, true>(d_q, db, a, grid, stream); break;
+            default: st = launch_tc_t<4, 128, 1, 2, true>(d_q, db, a, grid, stream); break;
         }
     } else if (CL == 2) {
         switch (db->L) {

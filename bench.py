@@ -299,6 +299,9 @@ def run_ours(args, cfg, rank, world):
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
     torch.cuda.set_device(dev)
     ctx = H.Context(cfg["dim"], cfg["kmer"], cfg["read_len"], 10)
+    if args.tc_group or args.tc_cluster:
+        ctx.tc_tuning(args.tc_group, -1, 0, 0)
+        ctx.tc_option(H.TC_CLUSTER, args.tc_cluster)
     tree, refs, rn, maxr = build_database(H, ctx, cfg, dev)
     if args.form == "pipe":
         return run_pipeline(args, cfg, rank, world, H, ctx, tree, refs, rn, maxr, dev)
@@ -741,6 +744,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--refs", type=int, default=0, help="override the number of references (small profiling cases)")
+    ap.add_argument("--tc-group", type=int, default=0, help="tensor-core search: query tiles per group (0: library default)")
+    ap.add_argument("--tc-cluster", type=int, default=0, help="tensor-core search: CTAs sharing reference blocks (0: default)")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3")

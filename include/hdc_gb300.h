@@ -213,11 +213,16 @@ int hdc_search_tc_tuning(hdc_context* ctx, int group_tiles, int l2_policy, int t
 /* Further tensor-core search settings; results do not depend on them.
  *   HDC_TC_PREFETCH: K blocks of each query/reference tile pair prefetched
  *     into L2 ahead of the shared-memory ring (0: none, -1: automatic, <= 64);
- *   HDC_TC_CLUSTER: CTAs that share each reference block through a TMA
+ *   HDC_TC_CLUSTER: CTAs that share an operand's blocks through a TMA
  *     multicast, 1 or 2 (0: automatic; 2 applies with tile_n 128 and one
- *     M-block, and pairs CTAs of neighbouring query tiles). */
+ *     M-block);
+ *   HDC_TC_SHARE: what a pair shares: 0 reference blocks (the pair runs two
+ *     neighbouring query tiles), 1 query blocks (the pair runs one query tile
+ *     on two neighbouring reference lanes; groups default to half the SMs),
+ *     -1 automatic. */
 #define HDC_TC_PREFETCH 1
 #define HDC_TC_CLUSTER 2
+#define HDC_TC_SHARE 3
 int hdc_search_tc_option(hdc_context* ctx, int option, int value);
 
 /* Hierarchical descent (config 5; targets/identify.cpp:89-202 with one

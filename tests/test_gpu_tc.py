@@ -20,22 +20,25 @@ def _setup(hdc, dev, refs, q_bipolar, dim):
     return ctx, db, tr, q16, qi, qn
 
 
-def _run_tc(ctx, db, q16, qn, maxq, k, mode, tile_n=0, group=0, m_blocks=0, cluster=0):
+def _run_tc(ctx, db, q16, qn, maxq, k, mode, tile_n=0, group=0, m_blocks=0, cluster=0, share=-1):
     import torch
     import hdc_gb300
     ctx.tc_tuning(group, -1, tile_n, m_blocks)
     ctx.tc_option(hdc_gb300.TC_CLUSTER, cluster)
+    ctx.tc_option(hdc_gb300.TC_SHARE, share)
     s, i, c, d = ctx.search_tc(db, q16, qn, maxq, k, mode)
     torch.cuda.synchronize()
     assert ctx.status() == 0
     return s.cpu().numpy(), i.cpu().numpy(), c.cpu().numpy(), d.cpu().numpy()
 
 
-# cluster 2: CTA pairs sharing reference blocks by multicast; groups of 3 query tiles
-# round down to 2, and odd tile counts leave a CTA of the last pair without a tile
-@pytest.mark.parametrize("tile_n,group,m_blocks,cluster", [(128, 0, 1, 1), (128, 0, 2, 1), (256, 0, 1, 1),
-                                                           (128, 3, 2, 1), (128, 0, 1, 2), (128, 3, 1, 2),
-                                                           (128, 4, 1, 2)])
+# cluster 2, share 0: CTA pairs sharing reference blocks by multicast; groups of 3
+# query tiles round down to 2, and odd tile counts leave a CTA of the last pair
+# without a tile.  share 1: pairs sharing query blocks over two reference lanes
+# (groups of 3 and 50 query tiles: 50 and 2 lanes).
+@pytest.mark.parametrize("tile_n,group,m_blocks,cluster,share", [
+    (128, 0, 1, 1, 0), (128, 0, 2, 1, 0), (256, 0, 1, 1, 0), (128, 3, 2, 1, 0), (128, 0, 1, 2, 0),
+    (128, 3, 1, 2, 0), (128, 4, 1, 2, 0), (128, 0, 1, 2, 1), (128, 3, 1, 2, 1), (128, 50, 1, 2, 1)])
 @pytest.mark.parametrize("dim,nq,nr,k,mode,vmax,dtype", [
     (1024, 200, 1000, 5, 0, 2000, np.int16),     # one fp16 limb (|v| <= 2048)
     (2048, 130, 3000, 10, 0, 12000, np.int16),   # two limbs (bundle of 8 copies)
@@ -46,7 +49,7 @@ def _run_tc(ctx, db, q16, qn, maxq, k, mode, tile_n=0, group=0, m_blocks=0, clus
     (640, 50, 400, 5, 0, 100000000, np.int32),   # three limbs, top limb ~ 24
     (10240, 129, 300, 5, 0, 12728, np.int16),    # precision-form dimension
 ])
-def test_tc_vs_oracle(hdc, orc, cuda, dim, nq, nr, k, mode, vmax, dtype, tile_n, group, m_blocks, cluster):
+def test_tc_vs_oracle(hdc, orc, cuda, dim, nq, nr, k, mode, vmax, dtype, tile_n, group, m_blocks, cluster, share):
     g = np.random.default_rng(dim + nq + nr)
     refs = g.integers(-vmax, vmax + 1, (nr, dim)).astype(dtype)
     refs[3] = refs[1]                       # tie: lower index first
@@ -56,7 +59,7 @@ def test_tc_vs_oracle(hdc, orc, cuda, dim, nq, nr, k, mode, vmax, dtype, tile_n,
     q = np.where(g.random((nq, dim)) < 0.5, -1, 1).astype(np.int8)
     q[0] = np.where(refs[1] >= 0, 1, -1)    # a query aligned with reference 1
     ctx, db, tr, q16, qi, qn = _setup(hdc, cuda, refs, q, dim)
-    s, i, c, d = _run_tc(ctx, db, q16, qn, 1, k, mode, tile_n, group, m_blocks, cluster)
+    s, i, c, d = _run_tc(ctx, db, q16, qn, 1, k, mode, tile_n, group, m_blocks, cluster, share)
     os_, oi, oc, od = orc.topk(q.astype(np.int32), refs.astype(np.int32), min(k, nr), mode)
     assert np.array_equal(i, oi)
     assert np.array_equal(d, od)
@@ -143,16 +146,17 @@ def test_tc_encoded_bipolar_reads(hdc, orc, cuda):
     assert np.array_equal(s.cpu().numpy(), os_)
 
 
-@pytest.mark.parametrize("group", [0, 38, 76])
-def test_tc_cluster_many_pairs(hdc, cuda, group):
-    """Every SM busy: 41 query tiles (odd) in groups spread over all SMs, the
-    paired multicast form against the unpaired one, bit for bit."""
+@pytest.mark.parametrize("group,share", [(0, 0), (38, 0), (76, 0), (0, 1), (38, 1), (19, 1)])
+def test_tc_cluster_many_pairs(hdc, cuda, group, share):
+    """Every SM busy: 41 query tiles (odd) and 22 reference tiles in groups
+    spread over all SMs, the paired multicast forms against the unpaired one,
+    bit for bit."""
     g = np.random.default_rng(77 + group)
     dim, nq, nr = 2048, 41 * 128 - 5, 2600
     refs = g.integers(-12000, 12001, (nr, dim)).astype(np.int16)
     q = np.where(g.random((nq, dim)) < 0.5, -1, 1).astype(np.int8)
     ctx, db, tr, q16, qi, qn = _setup(hdc, cuda, refs, q, dim)
-    one = _run_tc(ctx, db, q16, qn, 1, 7, 0, 128, group, 1, 1)
-    two = _run_tc(ctx, db, q16, qn, 1, 7, 0, 128, group, 1, 2)
+    one = _run_tc(ctx, db, q16, qn, 1, 7, 0, 128, group, 1, 1, 0)
+    two = _run_tc(ctx, db, q16, qn, 1, 7, 0, 128, group, 1, 2, share)
     for a, b in zip(one, two):
         assert np.array_equal(a, b)
