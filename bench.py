@@ -56,6 +56,16 @@ CONFIGS = {
 }
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the
+# dominant kernel, from single-pass ncu captures of the full-size workloads
+# (profiles/tc_search_kernel_c3.md, profiles/beam_kernel_descent.md), per unit
+# of work, so a run's `traffic` is that per-unit figure times its own units:
+#   tc_search_kernel, c3 (38,912 reads x 200,000 refs = 304 x 1,564 tile pairs): 1.48026e12 B
+#   beam_kernel, c5 (38,912 reads):                                               4.67027e11 B
+TRAFFIC_PER_TILE_PAIR_TC = (1.479787e12 + 0.475024e9) / (304 * 1564)
+TRAFFIC_PER_READ_DESCENT = (467.016836e9 + 10.247168e6) / 38912
+
+
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
@@ -652,7 +662,9 @@ def descent_line(args, cfg, r, metric, workload, world):
         "e2e": {"value": B * world / (r["e2e_ms"] / 1e3), "unit": "reads/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / pk["hbm_gbs"], "traffic": None,
+                     "frac": achieved / pk["hbm_gbs"], "traffic": TRAFFIC_PER_READ_DESCENT * B,
+                     "traffic_source": "ncu DRAM bytes of the full-size c5 launch per read, times this "
+                                       "launch's reads",
                      "peak_source": "%s HBM copy bandwidth (MEASURED_PEAKS.json)" % src,
                      "kernel": "beam_kernel; algorithmic bytes per read: the %d int32 rows gathered below "
                                "the top %d ranks + the int8 read (the other %d rows a read gathers belong to "
@@ -826,8 +838,11 @@ def main():
         # tensor work per read: one fp16 MMA pass per limb, 2*D*R*limbs flops
         flops = 2.0 * dim * nr * r["limbs"] * B
         achieved = flops / (r["search_ms"] / 1e3) / 1e12
+        tile_pairs = ((B + 127) // 128) * (((nr + 255) // 256) * 2)
         roof = {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
-                "frac": achieved / pk["bf16_tflops"], "traffic": None,
+                "frac": achieved / pk["bf16_tflops"], "traffic": TRAFFIC_PER_TILE_PAIR_TC * tile_pairs,
+                "traffic_source": "ncu DRAM bytes of the full-size c3 launch, per 128x128 tile pair, times "
+                                  "this launch's %d pairs (query tiles re-read for every reference tile)" % tile_pairs,
                 "peak_source": "%s dense bf16/fp16 burst (MEASURED_PEAKS.json)" % src,
                 "kernel": "tc_search_kernel + merge, %d fp16 limbs; algorithmic 2*D*R*limbs per read" % r["limbs"]}
         dtype = "fp16 integer limbs, fp32 accumulators (exact int64 dots), FP64 scores"
