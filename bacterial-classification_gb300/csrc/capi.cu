@@ -224,8 +224,8 @@ int hdc_search_tc_tuning(hdc_context* ctx, int group_tiles, int l2_policy, int t
     return HDC_OK;
 }
 
-int hdc_search_tc_option(hdc_context* ctx, int option, int value) {
-    if (!ctx) return fail(HDC_ERR_INVALID, "tc option: null context");
+int hdc_context_option(hdc_context* ctx, int option, int value) {
+    if (!ctx) return fail(HDC_ERR_INVALID, "option: null context");
     switch (option) {
         case HDC_TC_PREFETCH:
             if (value < -1 || value > 64) return fail(HDC_ERR_INVALID, "tc option: prefetch must be in -1..64");
@@ -239,8 +239,12 @@ int hdc_search_tc_option(hdc_context* ctx, int option, int value) {
             if (value < -1 || value > 1) return fail(HDC_ERR_INVALID, "tc option: share must be -1, 0 or 1");
             ctx->tc_share = value;
             return HDC_OK;
+        case HDC_BEAM_GROUPED:
+            if (value < -1 || value > 1) return fail(HDC_ERR_INVALID, "option: beam grouping must be -1, 0 or 1");
+            ctx->beam_grouped = value;
+            return HDC_OK;
         default:
-            return fail(HDC_ERR_INVALID, "tc option: unknown option");
+            return fail(HDC_ERR_INVALID, "option: unknown option");
     }
 }
 
@@ -271,17 +275,18 @@ int hdc_propagate_greedy(hdc_context* ctx, const int16_t* d_hv, const int64_t* d
 }
 
 int hdc_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qnorm2, int64_t nq, const int32_t* d_proto,
-                    const int64_t* d_proto_norm2, const int64_t* d_child_ptr, const int32_t* d_child_idx,
+                    const int64_t* d_proto_norm2, int64_t n_nodes, const int64_t* d_child_ptr, const int32_t* d_child_idx,
                     const int32_t* d_roots, int n_roots, int levels, int beam, double threshold, int score_mode,
                     int32_t* d_path, float* d_path_score, int32_t* d_depth, void* stream) {
     if (!ctx) return fail(HDC_ERR_INVALID, "beam: null context");
-    if (nq < 0) return fail(HDC_ERR_INVALID, "beam: negative count");
+    if (nq < 0 || n_nodes < 0) return fail(HDC_ERR_INVALID, "beam: negative count");
     if (nq == 0) return HDC_OK;
+    if (n_nodes < 1 || n_nodes > 0x7fffffffLL) return fail(HDC_ERR_INVALID, "beam: node count out of range");
     if (!hdc::valid_score_mode(score_mode)) return fail(HDC_ERR_INVALID, "beam: bad score mode");
     if (!d_q || !d_qnorm2 || !d_proto || !d_proto_norm2 || !d_child_ptr || !d_child_idx || !d_roots || !d_path ||
         !d_path_score || !d_depth)
         return fail(HDC_ERR_INVALID, "beam: null pointer");
-    return hdc::launch_beam_search(ctx, d_q, d_qnorm2, nq, d_proto, d_proto_norm2, d_child_ptr, d_child_idx, d_roots,
+    return hdc::launch_beam_search(ctx, d_q, d_qnorm2, nq, d_proto, d_proto_norm2, n_nodes, d_child_ptr, d_child_idx, d_roots,
                                    n_roots, levels, beam, threshold, score_mode, d_path, d_path_score, d_depth,
                                    static_cast<cudaStream_t>(stream));
 }

@@ -29,6 +29,7 @@ struct hdc_context {
     int tc_prefetch = -1;           // tensor-core search: K blocks prefetched into L2 ahead (-1: automatic)
     int tc_cluster = 0;             // tensor-core search: CTAs sharing an operand's blocks, 1 or 2 (0: automatic)
     int tc_share = -1;              // tensor-core search: 0 pairs share references, 1 queries (-1: automatic)
+    int beam_grouped = -1;          // descent: 1 reads grouped by candidate node, 0 warp per read (-1: automatic)
 };
 
 // A tensor-core reference database (hdc_refdb_create).
@@ -94,7 +95,7 @@ int launch_propagate_greedy(hdc_context* ctx, const int16_t* d_hv, const int64_t
                             uint8_t* d_selected, float* d_best, int32_t* d_scratch, cudaStream_t stream);
 
 int launch_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn, int64_t nq, const int32_t* d_proto,
-                       const int64_t* d_pn, const int64_t* d_child_ptr, const int32_t* d_child_idx,
+                       const int64_t* d_pn, int64_t n_nodes, const int64_t* d_child_ptr, const int32_t* d_child_idx,
                        const int32_t* d_roots, int n_roots, int levels, int beam, double threshold, int mode,
                        int32_t* d_path, float* d_path_score, int32_t* d_depth, cudaStream_t stream);
 
@@ -108,6 +109,12 @@ int launch_similarity(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qn,
                       const int64_t* d_rn, const int64_t* d_ref_rows, const uint8_t* d_ref_whole,
                       const int32_t* d_pair_q, const int32_t* d_pair_ref, int64_t n_pairs, int mode, float* d_score,
                       int32_t* d_window, cudaStream_t stream);
+
+// the descent with reads grouped by candidate node (beam_grouped.cu); dim % 1024 == 0, dim <= 16384
+int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn, int64_t nq, const int32_t* d_proto,
+                        const int64_t* d_pn, int64_t n_nodes, const int64_t* d_child_ptr, const int32_t* d_child_idx,
+                        const int32_t* d_roots, int n_roots, int levels, int beam, double threshold, int mode,
+                        int32_t* d_path, float* d_path_score, int32_t* d_depth, cudaStream_t stream);
 
 int launch_bundle(hdc_context* ctx, const void* d_rows, int elem_bytes, const int64_t* d_child_ptr,
                   const int32_t* d_child_idx, int64_t n_parents, int32_t* d_out, cudaStream_t stream);

@@ -15,7 +15,7 @@ HDC_OK = 0
 ERR = {1: "HDC_ERR_INVALID", 2: "HDC_ERR_RANGE", 3: "HDC_ERR_CUDA", 4: "HDC_ERR_NOMEM",
        5: "HDC_ERR_UNSUPPORTED", 6: "HDC_ERR_TIMEOUT"}
 SCORE_NORM, SCORE_COS, SCORE_DOT = 0, 1, 2
-TC_PREFETCH, TC_CLUSTER, TC_SHARE = 1, 2, 3
+TC_PREFETCH, TC_CLUSTER, TC_SHARE, BEAM_GROUPED = 1, 2, 3, 4
 OUT_I16, OUT_I32, OUT_BIPOLAR_BF16, OUT_BIPOLAR_I16, OUT_BIPOLAR_F16, OUT_BIPOLAR_I8 = 0, 1, 2, 3, 4, 5
 
 # (name, restype, argtypes) of every exported entry point
@@ -38,7 +38,7 @@ SIGNATURES = [
     ("hdc_search_plain", I32, [P, P, P, I64, ctypes.c_int32, P, P, I64, ctypes.c_int32, I32, I32, P, P, P, P, P,
                                SZ, P]),
     ("hdc_bundle", I32, [P, P, I32, P, P, I64, P, P]),
-    ("hdc_beam_search", I32, [P, P, P, I64, P, P, P, P, P, I32, I32, I32, ctypes.c_double, I32, P, P, P, P]),
+    ("hdc_beam_search", I32, [P, P, P, I64, P, P, I64, P, P, P, I32, I32, I32, ctypes.c_double, I32, P, P, P, P]),
     ("hdc_similarity", I32, [P, P, P, P, P, P, P, P, P, I64, I32, P, P, P]),
     ("hdc_identify", I32, [P, P, P, I64, P, P, P, P, P, P, I32, I32, I32, ctypes.c_double, I32, P, P, P, P, P]),
     ("hdc_propagate_greedy", I32, [P, P, P, P, P, P, P, I64, ctypes.c_double, I32, P, P, P, P]),
@@ -50,7 +50,7 @@ SIGNATURES = [
     ("hdc_refdb_limbs", I32, [P]),
     ("hdc_search_tc_workspace_bytes", SZ, [P, P, I64, I32]),
     ("hdc_search_tc_tuning", I32, [P, I32, I32, I32, I32]),
-    ("hdc_search_tc_option", I32, [P, I32, I32]),
+    ("hdc_context_option", I32, [P, I32, I32]),
     ("hdc_pipeline_create", I32, [P, P, I64, I64, ctypes.c_int32, I32, I32, ctypes.POINTER(P)]),
     ("hdc_pipeline_destroy", None, [P]),
     ("hdc_pipeline_run", I32, [P, P, P, P, I64, P, P]),
@@ -179,8 +179,10 @@ class Context:
         check(lib().hdc_context_status(self.h, ctypes.byref(st)))
         return st.value
 
-    def tc_option(self, option, value):
-        check(lib().hdc_search_tc_option(self.h, option, value))
+    def option(self, option, value):
+        check(lib().hdc_context_option(self.h, option, value))
+
+    tc_option = option
 
     def tc_tuning(self, group_tiles=0, l2_policy=-1, tile_n=0, m_blocks=0):
         check(lib().hdc_search_tc_tuning(self.h, group_tiles, l2_policy, tile_n, m_blocks))
@@ -226,7 +228,8 @@ class Context:
         path = torch.empty((nq, levels), dtype=torch.int32, device=q.device)
         score = torch.empty((nq, levels), dtype=torch.float32, device=q.device)
         depth = torch.empty(nq, dtype=torch.int32, device=q.device)
-        check(lib().hdc_beam_search(self.h, ptr(q), ptr(qn), nq, ptr(proto), ptr(pn), ptr(child_ptr), ptr(child_idx),
+        check(lib().hdc_beam_search(self.h, ptr(q), ptr(qn), nq, ptr(proto), ptr(pn), proto.shape[0], ptr(child_ptr),
+                                    ptr(child_idx),
                                     ptr(roots), roots.numel(), levels, beam, threshold, mode, ptr(path), ptr(score),
                                     ptr(depth), stream_ptr(stream)))
         return path, score, depth

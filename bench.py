@@ -61,9 +61,9 @@ CONFIGS = {
 # (profiles/tc_search_kernel_c3.md, profiles/beam_kernel_descent.md), per unit
 # of work, so a run's `traffic` is that per-unit figure times its own units:
 #   tc_search_kernel, c3 (38,912 reads x 200,000 refs = 304 x 1,564 tile pairs): 1.48026e12 B
-#   beam_kernel, c5 (38,912 reads):                                               4.67027e11 B
+#   grouped descent, c5 (the 6 score_kernel launches of one call, 38,912 reads):  3.76890e10 B
 TRAFFIC_PER_TILE_PAIR_TC = (1.479787e12 + 0.475024e9) / (304 * 1564)
-TRAFFIC_PER_READ_DESCENT = (467.016836e9 + 10.247168e6) / 38912
+TRAFFIC_DESCENT = {38912: 37.593492e9 + 95.516928e6}  # reads per call -> bytes (mostly the database, once)
 
 
 def log(*a):
@@ -442,6 +442,7 @@ def run_descent(args, cfg, rank, world):
     torch.cuda.set_device(dev)
     dim, B, L, W = cfg["dim"], args.batch, cfg["levels"], cfg["beam"]
     ctx = H.Context(dim, cfg["kmer"], cfg["read_len"], 10)
+    ctx.option(H.BEAM_GROUPED, args.beam_grouped)
     tree, proto, pn, (b, base, counts, ptr, idx), bundle = build_prototypes(H, ctx, cfg, dev)
     d_ptr, d_idx = torch.from_numpy(ptr).to(dev), torch.from_numpy(idx).to(dev)
     roots = torch.arange(0, counts[0], dtype=torch.int32, device=dev)
@@ -522,16 +523,11 @@ def run_descent(args, cfg, rank, world):
         t = torch.tensor([ms, e2e_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms, e2e_ms = float(t[0]), float(t[1])
-    # rows gathered per read: the level-0 candidates, then up to beam x children per level; the
-    # ranks whose prototypes together fit in half of L2 stay resident across reads
+    # candidate rows per read: the level-0 candidates, then up to beam x children per level
     cand = [counts[0]] + [min(W, counts[l - 1]) * b for l in range(1, L)]
-    l2_levels = 0
-    while l2_levels < L and sum(counts[:l2_levels + 1]) * dim * 4 <= 64 << 20:
-        l2_levels += 1
     res = dict(ms=ms, e2e_ms=e2e_ms, search_ms=float(np.median(beam_ms)), clocks=clk.summary(),
                launches=2 * args.steps, refs=int(base[-1]), h2d=io["h2d"], d2h=io["d2h"], tree=tree,
                bundle=bundle, depth_mean=depth_mean, rows_per_read=int(sum(cand)),
-               hbm_rows_per_read=int(sum(cand[l2_levels:])), l2_levels=l2_levels,
                mean_len=float(np.mean(pool[0].len)))
     if rank == 0 and not args.no_cpu_baseline:
         # q8 and out["r"] hold the last step's batch and result
@@ -643,10 +639,10 @@ def descent_line(args, cfg, r, metric, workload, world):
     """The JSON line of the hierarchical-descent form."""
     pk, src = peaks()
     B, dim = args.batch, cfg["dim"]
-    # the beam kernel gathers rows_per_read int32 prototype rows per read; those of the lower ranks
-    # (hbm_rows_per_read) come from HBM, the upper ranks' from L2; plus the int8 read once
-    per_read = r["hbm_rows_per_read"] * dim * 4 + dim
-    achieved = B * per_read / (r["search_ms"] / 1e3) / 1e9
+    # grouped descent: every prototype row is a candidate at its own rank's level only, so a
+    # call reads each at most once, plus each level's packed +1/-1 reads
+    algo_bytes = r["refs"] * dim * 4 + cfg["levels"] * B * dim / 8
+    achieved = algo_bytes / (r["search_ms"] / 1e3) / 1e9
     bundle_bytes = sum(x["bytes"] for x in r["bundle"])
     bundle_ms = sum(x["ms"] for x in r["bundle"])
     line = {
@@ -662,15 +658,15 @@ def descent_line(args, cfg, r, metric, workload, world):
         "e2e": {"value": B * world / (r["e2e_ms"] / 1e3), "unit": "reads/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / pk["hbm_gbs"], "traffic": TRAFFIC_PER_READ_DESCENT * B,
-                     "traffic_source": "ncu DRAM bytes of the full-size c5 launch per read, times this "
-                                       "launch's reads",
+                     "frac": achieved / pk["hbm_gbs"], "traffic": TRAFFIC_DESCENT.get(B),
+                     "traffic_source": "ncu DRAM bytes of the score launches of one full-size call "
+                                       "(measured at 38,912 reads; null at other batch sizes)",
                      "peak_source": "%s HBM copy bandwidth (MEASURED_PEAKS.json)" % src,
-                     "kernel": "beam_kernel; algorithmic bytes per read: the %d int32 rows gathered below "
-                               "the top %d ranks + the int8 read (the other %d rows a read gathers belong to "
-                               "the top ranks, whose prototypes stay L2-resident)" % (
-                                   r["hbm_rows_per_read"], r["l2_levels"],
-                                   r["rows_per_read"] - r["hbm_rows_per_read"])},
+                     "kernel": "grouped descent (hdc_beam_search: count/expand/scan/scatter, score_kernel, "
+                               "select per level), timed as one call; algorithmic bytes = the %.1f GB of "
+                               "prototypes once + %d levels of packed reads; it is issue-bound on the "
+                               "+p/-p integer sums (%d candidate rows per read), not HBM-bound" % (
+                                   r["refs"] * dim * 4 / 1e9, cfg["levels"], r["rows_per_read"])},
         "propagate_bundle": {"kernel": "bundle_kernel (internal prototypes = int32 sums of children)",
                              "ms": bundle_ms, "gb_per_s": bundle_bytes / (bundle_ms / 1e3) / 1e9,
                              "frac_of_hbm": bundle_bytes / (bundle_ms / 1e3) / 1e9 / pk["hbm_gbs"],
@@ -758,6 +754,8 @@ def main():
     ap.add_argument("--refs", type=int, default=0, help="override the number of references (small profiling cases)")
     ap.add_argument("--tc-group", type=int, default=0, help="tensor-core search: query tiles per group (0: library default)")
     ap.add_argument("--tc-cluster", type=int, default=0, help="tensor-core search: CTAs sharing reference blocks (0: default)")
+    ap.add_argument("--beam-grouped", type=int, default=-1,
+                    help="descent: 1 reads grouped by candidate node, 0 one warp per read (-1: default)")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3")

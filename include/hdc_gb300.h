@@ -210,7 +210,7 @@ int hdc_search_plain_noalloc(hdc_context* ctx, const int16_t* d_q, const int64_t
  * on these settings, only the speed does. */
 int hdc_search_tc_tuning(hdc_context* ctx, int group_tiles, int l2_policy, int tile_n, int m_blocks);
 
-/* Further tensor-core search settings; results do not depend on them.
+/* Further settings of a context; results do not depend on them.
  *   HDC_TC_PREFETCH: K blocks of each query/reference tile pair prefetched
  *     into L2 ahead of the shared-memory ring (0: none, -1: automatic, <= 64);
  *   HDC_TC_CLUSTER: CTAs that share an operand's blocks through a TMA
@@ -223,7 +223,10 @@ int hdc_search_tc_tuning(hdc_context* ctx, int group_tiles, int l2_policy, int t
 #define HDC_TC_PREFETCH 1
 #define HDC_TC_CLUSTER 2
 #define HDC_TC_SHARE 3
-int hdc_search_tc_option(hdc_context* ctx, int option, int value);
+#define HDC_BEAM_GROUPED 4 /* hdc_beam_search: 1 reads grouped by candidate node, 0 one warp
+                              per read, -1 automatic (grouped when dim % 1024 == 0 and
+                              dim <= 16384) */
+int hdc_context_option(hdc_context* ctx, int option, int value);
 
 /* Hierarchical descent (config 5; targets/identify.cpp:89-202 with one
  * prototype hypervector per taxonomy node): beam search of +1/-1 int8 read
@@ -235,9 +238,13 @@ int hdc_search_tc_option(hdc_context* ctx, int option, int value);
  * when the best score is below threshold (the reference uses 0 on the NORM
  * scale) and keeps the entries scoring >= threshold, at most `beam` (<= 8).
  * Outputs per read: the best path d_path [nq][levels] (-1 past its depth),
- * its per-level scores, and its depth.  levels <= 8; dim % 4 == 0. */
+ * its per-level scores, and its depth.  levels <= 8; dim % 4 == 0.
+ * Reads are scored either grouped by candidate node (each prototype row read
+ * once per level for the whole batch; needs dim % 1024 == 0, dim <= 16384,
+ * and device workspace from the stream-ordered allocator) or one warp per
+ * read; see HDC_BEAM_GROUPED.  Both give identical results. */
 int hdc_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qnorm2, int64_t nq,
-                    const int32_t* d_proto, const int64_t* d_proto_norm2, const int64_t* d_child_ptr,
+                    const int32_t* d_proto, const int64_t* d_proto_norm2, int64_t n_nodes, const int64_t* d_child_ptr,
                     const int32_t* d_child_idx, const int32_t* d_roots, int n_roots, int levels, int beam,
                     double threshold, int score_mode, int32_t* d_path, float* d_path_score, int32_t* d_depth,
                     void* stream);
