@@ -257,8 +257,9 @@ __global__ void __launch_bounds__(kScoreThreads) score_kernel(const GArgs a) {
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const uint32_t nib = w[u] >> sh;
-                acc += (int64_t)((nib & 1u) ? x[u].x : -x[u].x) + (int64_t)((nib & 2u) ? x[u].y : -x[u].y) +
-                       (int64_t)((nib & 4u) ? x[u].z : -x[u].z) + (int64_t)((nib & 8u) ? x[u].w : -x[u].w);
+                const int64_t vx = x[u].x, vy = x[u].y, vz = x[u].z, vw = x[u].w;  // widen, then negate
+                acc += ((nib & 1u) ? vx : -vx) + ((nib & 2u) ? vy : -vy) + ((nib & 4u) ? vz : -vz) +
+                       ((nib & 8u) ? vw : -vw);
             }
         }
         for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
