@@ -233,6 +233,10 @@ __global__ void scatter_kernel(const GArgs a) {
 // scored by neighbouring warps at about the same time, so its prototype row comes from
 // DRAM once and from L1/L2 for the others.  Lane l covers dims 128 j + 4 l .. + 3; four
 // 16-byte prototype loads are in flight per lane, and the read is its packed bits.
+// -x in 32 bits, with wrap-around defined (exact for every prototype element but INT32_MIN,
+// which hdc_beam_search excludes; widening before negating costs ~40 % of the kernel)
+__device__ __forceinline__ int32_t neg32(int32_t x) { return (int32_t)(0u - (uint32_t)x); }
+
 __global__ void __launch_bounds__(kScoreThreads) score_kernel(const GArgs a) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -257,9 +261,8 @@ __global__ void __launch_bounds__(kScoreThreads) score_kernel(const GArgs a) {
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 const uint32_t nib = w[u] >> sh;
-                const int64_t vx = x[u].x, vy = x[u].y, vz = x[u].z, vw = x[u].w;  // widen, then negate
-                acc += ((nib & 1u) ? vx : -vx) + ((nib & 2u) ? vy : -vy) + ((nib & 4u) ? vz : -vz) +
-                       ((nib & 8u) ? vw : -vw);
+                acc += (int64_t)((nib & 1u) ? x[u].x : neg32(x[u].x)) + (int64_t)((nib & 2u) ? x[u].y : neg32(x[u].y)) +
+                       (int64_t)((nib & 4u) ? x[u].z : neg32(x[u].z)) + (int64_t)((nib & 8u) ? x[u].w : neg32(x[u].w));
             }
         }
         for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);

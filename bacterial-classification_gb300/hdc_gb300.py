@@ -49,6 +49,9 @@ SIGNATURES = [
     ("hdc_refdb_destroy", None, [P]),
     ("hdc_refdb_limbs", I32, [P]),
     ("hdc_search_tc_workspace_bytes", SZ, [P, P, I64, I32]),
+    ("hdc_refdb_save", I32, [P, P, ctypes.c_char_p, P]),
+    ("hdc_refdb_file_info", I32, [ctypes.c_char_p, P, P, P, P, P]),
+    ("hdc_refdb_load", I32, [P, ctypes.c_char_p, P, P]),
     ("hdc_search_tc_tuning", I32, [P, I32, I32, I32, I32]),
     ("hdc_context_option", I32, [P, I32, I32]),
     ("hdc_pipeline_create", I32, [P, P, I64, I64, ctypes.c_int32, I32, I32, ctypes.POINTER(P)]),
@@ -272,14 +275,45 @@ class Context:
 
 
 class RefDB:
-    """Tensor-core reference database (fp16 limbs + exact norms) built from int16/int32 rows."""
+    """Tensor-core reference database (fp16 limbs + exact norms) built from int16/int32 rows,
+    or loaded from a file written by save()."""
 
-    def __init__(self, ctx, refs, max_abs, stream=None):
+    def __init__(self, ctx, refs, max_abs, stream=None, _handle=None, _nr=0):
         h = ctypes.c_void_p()
-        check(lib().hdc_refdb_create(ctx.h, ptr(refs), refs.element_size(), refs.shape[0], int(max_abs),
-                                     ctypes.byref(h), stream_ptr(stream)))
-        self.h, self.nr = h, refs.shape[0]
+        if _handle is None:
+            check(lib().hdc_refdb_create(ctx.h, ptr(refs), refs.element_size(), refs.shape[0], int(max_abs),
+                                         ctypes.byref(h), stream_ptr(stream)))
+            _nr = refs.shape[0]
+        else:
+            h = _handle
+        self.h, self.nr, self.ctx = h, _nr, ctx
         self.limbs = lib().hdc_refdb_limbs(h)
+
+    def save(self, path, tax_ids=None):
+        """Write the database (and optional int32 taxonomy ids, one per reference) to `path`."""
+        import numpy as np
+        ids = None if tax_ids is None else np.ascontiguousarray(tax_ids, np.int32)
+        check(lib().hdc_refdb_save(self.ctx.h, self.h, str(path).encode(),
+                                   None if ids is None else ids.ctypes.data_as(ctypes.c_void_p)))
+
+    @staticmethod
+    def file_info(path):
+        d, k, lim, ids = I32(), I32(), I32(), I32()
+        nr = ctypes.c_int64()
+        check(lib().hdc_refdb_file_info(str(path).encode(), ctypes.byref(d), ctypes.byref(k), ctypes.byref(nr),
+                                        ctypes.byref(lim), ctypes.byref(ids)))
+        return dict(dim=d.value, kmer=k.value, nr=nr.value, limbs=lim.value, has_tax_ids=bool(ids.value))
+
+    @classmethod
+    def load(cls, ctx, path):
+        """(database, taxonomy ids or None) from a file written by save()."""
+        import numpy as np
+        info = cls.file_info(path)
+        ids = np.zeros(info["nr"], np.int32) if info["has_tax_ids"] else None
+        h = ctypes.c_void_p()
+        check(lib().hdc_refdb_load(ctx.h, str(path).encode(), ctypes.byref(h),
+                                   None if ids is None else ids.ctypes.data_as(ctypes.c_void_p)))
+        return cls(ctx, None, 0, _handle=h, _nr=info["nr"]), ids
 
     def close(self):
         if self.h:

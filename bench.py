@@ -265,7 +265,8 @@ def run_pipeline(args, cfg, rank, world, H, ctx, tree, refs, rn, maxr, dev):
     max_bytes = max(int(r.len.astype(np.int64).sum()) for r in pool) + 4096
     db = ctx.refdb(refs, maxr)
     pipe = H.Pipeline(ctx, db, B, max_bytes, cfg.get("max_read", cfg["read_len"]), K)
-    pipe.run(pool[0])
+    _, first_idx = pipe.run(pool[0])
+    acc = float((first_idx[:, 0] == pool[0].label).mean())
     tuned = pipe.autotune()
     # device-resident: replay encode + search on the staged batch, timed on the pipeline's stream
     st = torch.cuda.ExternalStream(pipe.stream())
@@ -299,7 +300,7 @@ def run_pipeline(args, cfg, rank, world, H, ctx, tree, refs, rn, maxr, dev):
         ms, e2e_ms = float(t[0]), float(t[1])
     return dict(ms=ms, e2e_ms=e2e_ms, search_ms=search_ms, clocks=clk.summary(), launches=4 * args.steps,
                 refs=refs.shape[0], limbs=db.limbs, h2d=max_bytes + B * 16, d2h=B * K * 8, tree=tree,
-                tuned=tuned, mean_len=float(np.mean(pool[0].len)),
+                tuned=tuned, mean_len=float(np.mean(pool[0].len)), top1_accuracy=acc,
                 refs_host=refs.cpu().numpy() if (rank == 0 and not args.no_cpu_baseline) else None)
 
 
@@ -329,6 +330,10 @@ def run_ours(args, cfg, rank, world):
     ms, search_ms = time_form(form, batches, d_buf, args.steps, args.warmup, world, clk)
     res = dict(ms=ms, search_ms=search_ms, clocks=clk.summary(), launches=form.launches * args.steps,
                refs=refs.shape[0], limbs=form.db.limbs if form.db is not None else 0)
+    # the source leaf of every read is known: how often is it the top hit
+    form.run(d_buf, *batches[0])
+    torch.cuda.synchronize()
+    res["top1_accuracy"] = float((form.out[1][:B, 0].cpu().numpy() == reads.label[:B]).mean())
 
     # the plain drop-in on the same workload, for the tensor-core speed-up
     if args.form == "tc" and not args.no_plain:
@@ -488,6 +493,8 @@ def run_descent(args, cfg, rank, world):
         beam_ms.append(ev[0].elapsed_time(ev[1]))
     path, score, depth = out["r"]
     depth_mean = float(depth.float().mean())
+    last = 2 % n_pool  # out["r"] is from the last event-timed call, on dev_pool[2 % n_pool]
+    leaf_acc = float((path[:, L - 1].cpu().numpy() == int(base[5]) + pool[last].label[:B]).mean())
     # end to end: pinned host reads copied in, paths and scores copied back, every step
     h_pool = [(torch.from_numpy(r.buf).pin_memory(), torch.from_numpy(r.off).pin_memory(),
                torch.from_numpy(r.len).pin_memory()) for r in pool]
@@ -527,7 +534,7 @@ def run_descent(args, cfg, rank, world):
     cand = [counts[0]] + [min(W, counts[l - 1]) * b for l in range(1, L)]
     res = dict(ms=ms, e2e_ms=e2e_ms, search_ms=float(np.median(beam_ms)), clocks=clk.summary(),
                launches=2 * args.steps, refs=int(base[-1]), h2d=io["h2d"], d2h=io["d2h"], tree=tree,
-               bundle=bundle, depth_mean=depth_mean, rows_per_read=int(sum(cand)),
+               bundle=bundle, depth_mean=depth_mean, rows_per_read=int(sum(cand)), leaf_accuracy=leaf_acc,
                mean_len=float(np.mean(pool[0].len)))
     if rank == 0 and not args.no_cpu_baseline:
         # q8 and out["r"] hold the last step's batch and result
@@ -653,6 +660,7 @@ def descent_line(args, cfg, r, metric, workload, world):
         "data": "synthetic (seeded 6-rank tree, see bench.py)",
         "config": {"workload": workload, "form": "descent", "batch_reads": B, "nodes": r["refs"],
                    "mean_read_len": r["mean_len"], "mean_depth": r["depth_mean"],
+                   "leaf_accuracy": r["leaf_accuracy"],
                    "l2": "inputs larger than L2: %.1f GB of prototypes, the lower ranks gathered from HBM "
                          "every step" % (r["refs"] * dim * 4 / 1e9)},
         "e2e": {"value": B * world / (r["e2e_ms"] / 1e3), "unit": "reads/s", "h2d_bytes_per_step": r["h2d"],
@@ -865,6 +873,8 @@ def main():
                 "d2h_bytes_per_step": r["d2h"]},
         "roofline": roof, "clocks": r["clocks"], "gpu_launches": r["launches"],
     }
+    if "top1_accuracy" in r:
+        line["config"]["top1_accuracy"] = r["top1_accuracy"]  # top hit = the read's source leaf
     if "tuned" in r:
         line["config"]["autotuned_schedule"] = r["tuned"]
         line["config"]["mean_read_len"] = r["mean_len"]

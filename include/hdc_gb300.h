@@ -151,6 +151,19 @@ int hdc_refdb_create(hdc_context* ctx, const void* d_ref, int elem_bytes, int64_
                      hdc_refdb** out, void* stream);
 void hdc_refdb_destroy(hdc_refdb* db);
 int hdc_refdb_limbs(const hdc_refdb* db);
+
+/* Persisted database (no reference counterpart: the reference re-encodes its
+ * FASTA files on every run).  hdc_refdb_save writes the limbs, exact norms
+ * and reciprocal roots of `db`, the context's dim / k-mer / window / step,
+ * and optionally one taxonomy id per reference (h_tax_ids: nr host int32s,
+ * or NULL), with a checksum; hdc_refdb_file_info reads the header;
+ * hdc_refdb_load rebuilds the database on the current device (the file's dim
+ * and k-mer size must equal the context's; a checksum mismatch, truncation or
+ * foreign file is HDC_ERR_INVALID) and fills h_tax_ids (nr entries) when the
+ * file has ids and the pointer is not NULL.  Synchronous. */
+int hdc_refdb_save(hdc_context* ctx, const hdc_refdb* db, const char* path, const int32_t* h_tax_ids);
+int hdc_refdb_file_info(const char* path, int* dim, int* kmer, int64_t* nr, int* limbs, int* has_tax_ids);
+int hdc_refdb_load(hdc_context* ctx, const char* path, hdc_refdb** out, int32_t* h_tax_ids);
 size_t hdc_search_tc_workspace_bytes(const hdc_context* ctx, const hdc_refdb* db, int64_t nq, int k);
 
 /* Precision form: exact cosine top-k of fp16 integer queries (normally the
@@ -239,6 +252,7 @@ int hdc_context_option(hdc_context* ctx, int option, int value);
  * scale) and keeps the entries scoring >= threshold, at most `beam` (<= 8).
  * Outputs per read: the best path d_path [nq][levels] (-1 past its depth),
  * its per-level scores, and its depth.  levels <= 8; dim % 4 == 0.
+ * Prototype elements must be greater than INT32_MIN.
  * Reads are scored either grouped by candidate node (each prototype row read
  * once per level for the whole batch; needs dim % 1024 == 0, dim <= 16384,
  * and device workspace from the stream-ordered allocator) or one warp per
