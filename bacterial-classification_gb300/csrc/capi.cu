@@ -324,6 +324,18 @@ int hdc_identify(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qnorm2, 
                                 d_stop_level, static_cast<cudaStream_t>(stream));
 }
 
+int hdc_fasta_parse(hdc_context* ctx, const char* d_in, int64_t n, char* d_out, int64_t* d_seq_off,
+                    int32_t* d_seq_len, int64_t* d_name_off, int32_t* d_name_len, int64_t max_records,
+                    int64_t* d_count, void* stream) {
+    if (!ctx) return fail(HDC_ERR_INVALID, "fasta: null context");
+    if (n < 0 || max_records < 0) return fail(HDC_ERR_INVALID, "fasta: negative size");
+    if (!d_count || (n > 0 && (!d_in || !d_out)) ||
+        (max_records > 0 && (!d_seq_off || !d_seq_len || !d_name_off || !d_name_len)))
+        return fail(HDC_ERR_INVALID, "fasta: null pointer");
+    return hdc::launch_fasta_parse(ctx, d_in, n, d_out, d_seq_off, d_seq_len, d_name_off, d_name_len, max_records,
+                                   d_count, static_cast<cudaStream_t>(stream));
+}
+
 int hdc_device_alloc(size_t bytes, void** out) {
     if (!out) return fail(HDC_ERR_INVALID, "alloc: null output pointer");
     *out = nullptr;

@@ -116,6 +116,10 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn
                         const int32_t* d_roots, int n_roots, int levels, int beam, double threshold, int mode,
                         int32_t* d_path, float* d_path_score, int32_t* d_depth, cudaStream_t stream);
 
+int launch_fasta_parse(hdc_context* ctx, const char* d_in, int64_t n, char* d_out, int64_t* d_seq_off,
+                       int32_t* d_seq_len, int64_t* d_name_off, int32_t* d_name_len, int64_t max_records,
+                       int64_t* d_count, cudaStream_t stream);
+
 int launch_bundle(hdc_context* ctx, const void* d_rows, int elem_bytes, const int64_t* d_child_ptr,
                   const int32_t* d_child_idx, int64_t n_parents, int32_t* d_out, cudaStream_t stream);
 

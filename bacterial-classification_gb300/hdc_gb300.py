@@ -52,6 +52,7 @@ SIGNATURES = [
     ("hdc_refdb_save", I32, [P, P, ctypes.c_char_p, P]),
     ("hdc_refdb_file_info", I32, [ctypes.c_char_p, P, P, P, P, P]),
     ("hdc_refdb_load", I32, [P, ctypes.c_char_p, P, P]),
+    ("hdc_fasta_parse", I32, [P, P, I64, P, P, P, P, P, I64, P, P]),
     ("hdc_search_tc_tuning", I32, [P, I32, I32, I32, I32]),
     ("hdc_context_option", I32, [P, I32, I32]),
     ("hdc_pipeline_create", I32, [P, P, I64, I64, ctypes.c_int32, I32, I32, ctypes.POINTER(P)]),
@@ -263,6 +264,25 @@ class Context:
                                  ptr(child_idx), ptr(roots), roots.numel(), levels, beam, threshold, mode, ptr(path),
                                  ptr(score), ptr(depth), ptr(stop), stream_ptr(stream)))
         return path, score, depth, stop
+
+    def fasta_parse(self, d_bytes, max_records=None, stream=None):
+        """Device FASTA ingest of raw file bytes (uint8 tensor): returns (sequence bytes, seq_off,
+        seq_len, name_off, name_len, number of records) with the reference's reading."""
+        import torch
+        n = d_bytes.numel()
+        cap = (n + 1) if max_records is None else max_records
+        dev = d_bytes.device
+        out = torch.empty(max(n, 1), dtype=torch.uint8, device=dev)
+        so = torch.empty(max(cap, 1), dtype=torch.int64, device=dev)
+        sl = torch.empty(max(cap, 1), dtype=torch.int32, device=dev)
+        no = torch.empty(max(cap, 1), dtype=torch.int64, device=dev)
+        nl = torch.empty(max(cap, 1), dtype=torch.int32, device=dev)
+        cnt = torch.zeros(1, dtype=torch.int64, device=dev)
+        check(lib().hdc_fasta_parse(self.h, ptr(d_bytes), n, ptr(out), ptr(so), ptr(sl), ptr(no), ptr(nl), cap,
+                                    ptr(cnt), stream_ptr(stream)))
+        c = int(cnt.item())
+        m = min(c, cap)
+        return out, so[:m], sl[:m], no[:m], nl[:m], c
 
     def bundle(self, rows, child_ptr, child_idx, out=None, stream=None):
         import torch

@@ -296,6 +296,21 @@ int hdc_identify(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qnorm2, 
                  double threshold, int score_mode, int32_t* d_path, float* d_path_score, int32_t* d_depth,
                  int32_t* d_stop_level, void* stream);
 
+/* FASTA ingest on the device, with the reading of targets/identify.cpp:46-71:
+ * lines end at '\n' only (a '\r' stays part of the line); a line starting with
+ * '>' closes the current record (kept only when its sequence is not empty) and
+ * names the next (the rest of the line); other lines are appended to the
+ * sequence; bytes before the first header form a record with an empty name.
+ * In: d_in [n] raw file bytes.  Out: d_out (n bytes) the concatenated
+ * sequences; per kept record j < max_records, d_seq_off[j] / d_seq_len[j]
+ * into d_out and d_name_off[j] / d_name_len[j] into d_in; *d_count (device
+ * int64) = the number of kept records (may exceed max_records: then only the
+ * first max_records are written).  Each record's sequence must be shorter than
+ * 2^31 bytes.  Uses about 60 bytes of stream-ordered workspace per input byte. */
+int hdc_fasta_parse(hdc_context* ctx, const char* d_in, int64_t n, char* d_out, int64_t* d_seq_off,
+                    int32_t* d_seq_len, int64_t* d_name_off, int32_t* d_name_len, int64_t max_records,
+                    int64_t* d_count, void* stream);
+
 /* ---------------------------------------------------------------- batching form */
 
 /* A reusable encode -> tensor-core search -> top-k pipeline for batches of up

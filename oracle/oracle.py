@@ -308,3 +308,29 @@ def identify(q, rows, node_rows, child_ptr, child_idx, roots, levels=6, beam=5, 
         return out
 
     return _descent(score, q.shape[0], child_ptr, child_idx, roots, levels, beam, threshold)
+
+
+def fasta_records(data):
+    """The FASTA reading of targets/identify.cpp:46-71 over raw bytes: lines
+    split on b'\\n' only (a '\\r' stays part of the line); a line starting with
+    '>' closes the current record (kept only when its sequence is non-empty)
+    and names the next one (the rest of the line); any other line is appended
+    to the sequence; the sequence before the first header has an empty name.
+    Returns [(name bytes, sequence bytes)] in file order."""
+    out = []
+    seq, name = [], b""
+    lines = data.split(b"\n")
+    if data.endswith(b"\n"):
+        lines = lines[:-1]  # getline reads no empty line after a final newline
+    for line in lines:
+        if line.startswith(b">"):
+            if seq:
+                out.append((name, b"".join(seq)))
+                seq = []
+            name = line[1:]
+        else:
+            if line:
+                seq.append(line)
+    if seq:
+        out.append((name, b"".join(seq)))
+    return out
