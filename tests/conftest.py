@@ -23,7 +23,7 @@ def orc():
 
 @pytest.fixture(scope="session")
 def hdc():
-    """The built C-ABI library (built on first use, like the driver's build())."""
+    """The built C-ABI library (built on first use, as __graft_entry__.build() does)."""
     import build as pkg_build
     pkg_build.build()
     import hdc_gb300
