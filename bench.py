@@ -532,8 +532,13 @@ def run_descent(args, cfg, rank, world):
         ms, e2e_ms = float(t[0]), float(t[1])
     # candidate rows per read: the level-0 candidates, then up to beam x children per level
     cand = [counts[0]] + [min(W, counts[l - 1]) * b for l in range(1, L)]
+    # kernels per step: the read encode + the descent (grouped: max-children, bit packing,
+    # per level count / 3 scan kernels / expand / 3 scan kernels / scatter / score / select,
+    # output; one warp per read: one kernel)
+    grouped = args.beam_grouped != 0 and dim % 1024 == 0 and dim <= 16384
+    per_step = 1 + ((2 + 11 * L + 1) if grouped else 1)
     res = dict(ms=ms, e2e_ms=e2e_ms, search_ms=float(np.median(beam_ms)), clocks=clk.summary(),
-               launches=2 * args.steps, refs=int(base[-1]), h2d=io["h2d"], d2h=io["d2h"], tree=tree,
+               launches=per_step * args.steps, refs=int(base[-1]), h2d=io["h2d"], d2h=io["d2h"], tree=tree,
                bundle=bundle, depth_mean=depth_mean, rows_per_read=int(sum(cand)), leaf_accuracy=leaf_acc,
                mean_len=float(np.mean(pool[0].len)))
     if rank == 0 and not args.no_cpu_baseline:
