@@ -573,6 +573,7 @@ typedef struct {
     const int64_t* rn;
     int64_t nr;
     int k, mode, bipolar;
+    int32_t max_abs_r; /* max |reference element| (int16 rows) */
     float* out_s;
     int32_t* out_i;
     int tid, nthreads;
@@ -585,20 +586,35 @@ static void* cls_worker(void* arg) {
     uint64_t* tmp = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)j->t->W);
     float* bs = (float*)malloc(sizeof(float) * (size_t)k);
     int32_t* bi = (int32_t*)malloc(sizeof(int32_t) * (size_t)k);
+    int16_t* q16 = (int16_t*)malloc(sizeof(int16_t) * (size_t)dim);
     for (int64_t s = j->tid; s < j->n; s += j->nthreads) {
         encode_one(j->t, j->buf + j->off[s], j->len[s], acc, tmp);
         int64_t qn = 0;
+        int32_t max_q = 1;
         for (int d = 0; d < dim; ++d) {
             int32_t v = j->bipolar ? (acc[d] >= 0 ? 1 : -1) : (int32_t)(int16_t)(uint16_t)(uint32_t)acc[d];
             acc[d] = v;
+            q16[d] = (int16_t)v;
             qn += (int64_t)v * v;
+            if (v > max_q) max_q = v;
+            if (-v > max_q) max_q = -v;
         }
+        /* int16 x int16 products summed in int32 over chunks short enough that no sum can
+           overflow (chunk * max|q| * max|r| < 2^31), then in int64: exact, and vectorisable */
+        const int64_t bound = (int64_t)max_q * (j->max_abs_r > 0 ? j->max_abs_r : 1);
+        int chunk = (int)(2147483647LL / bound);
+        if (chunk < 1) chunk = 1;
         int filled = 0;
         for (int64_t ri = 0; ri < j->nr; ++ri) {
             int64_t dot = 0;
             if (j->ref_bytes == 2) {
                 const int16_t* r = (const int16_t*)j->refs + (size_t)ri * dim;
-                for (int d = 0; d < dim; ++d) dot += (int64_t)acc[d] * r[d];
+                for (int d0 = 0; d0 < dim; d0 += chunk) {
+                    const int d1 = dim - d0 < chunk ? dim : d0 + chunk;
+                    int32_t part = 0;
+                    for (int d = d0; d < d1; ++d) part += (int32_t)q16[d] * (int32_t)r[d];
+                    dot += part;
+                }
             } else {
                 const int32_t* r = (const int32_t*)j->refs + (size_t)ri * dim;
                 for (int d = 0; d < dim; ++d) dot += (int64_t)acc[d] * r[d];
@@ -620,6 +636,7 @@ static void* cls_worker(void* arg) {
             j->out_i[s * k + t] = t < filled ? bi[t] : -1;
         }
     }
+    free(q16);
     free(bi);
     free(bs);
     free(tmp);
@@ -635,19 +652,22 @@ int orc_classify(int dim, int kmer, const char* buf, const int64_t* off, const i
     orc_tables t;
     tables_init(&t, dim, kmer);
     int64_t* rn = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nr > 0 ? nr : 1));
+    int32_t max_abs_r = 0;
     for (int64_t i = 0; i < nr; ++i) {
         int64_t s = 0;
         for (int d = 0; d < dim; ++d) {
             int64_t v = ref_bytes == 2 ? ((const int16_t*)refs)[(size_t)i * dim + d]
                                        : ((const int32_t*)refs)[(size_t)i * dim + d];
             s += v * v;
+            const int64_t a = v < 0 ? -v : v;
+            if (ref_bytes == 2 && a > max_abs_r) max_abs_r = (int32_t)a;
         }
         rn[i] = s;
     }
     pthread_t th[256];
     cls_job jobs[256];
     for (int i = 0; i < nthreads; ++i) {
-        jobs[i] = (cls_job){&t, buf, off, len, n, refs, ref_bytes, rn, nr, k, mode, bipolar, out_s, out_i, i,
+        jobs[i] = (cls_job){&t, buf, off, len, n, refs, ref_bytes, rn, nr, k, mode, bipolar, max_abs_r, out_s, out_i, i,
                             nthreads};
         pthread_create(&th[i], NULL, cls_worker, &jobs[i]);
     }
