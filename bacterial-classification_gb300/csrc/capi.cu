@@ -239,6 +239,10 @@ int hdc_context_option(hdc_context* ctx, int option, int value) {
             if (value < -1 || value > 1) return fail(HDC_ERR_INVALID, "tc option: share must be -1, 0 or 1");
             ctx->tc_share = value;
             return HDC_OK;
+        case HDC_TC_SCATTER:
+            if (value < -1 || value > 1) return fail(HDC_ERR_INVALID, "option: tile order must be -1, 0 or 1");
+            ctx->tc_scatter = value;
+            return HDC_OK;
         case HDC_BEAM_GROUPED:
             if (value < -1 || value > 1) return fail(HDC_ERR_INVALID, "option: beam grouping must be -1, 0 or 1");
             ctx->beam_grouped = value;

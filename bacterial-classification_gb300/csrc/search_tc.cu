@@ -36,6 +36,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <numeric>
 #include <vector>
 
 #include "hdc_internal.cuh"
@@ -87,6 +88,7 @@ struct TcArgs {
     int G, S, n_groups;   // query tiles per group, reference lanes, groups
     int policy;           // 0: no L2 hint, 1: queries evict-last, 2: + references evict-first
     int prefetch;         // K blocks of the same tile pair prefetched into L2 ahead of the ring (0: none)
+    int t_stride;         // reference tiles are visited in the order (t * t_stride) mod n_rtiles
     const int64_t* qn;    // [nq] squared norms of the queries
     const int64_t* rn;    // [nr] squared norms of the references
     const float* rr;      // [nr] fp32 1/sqrt(norm)
@@ -176,7 +178,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 if (grp * a.G + lead_slot >= a.n_qtiles) continue;
                 const int qt = min(grp * a.G + gslot, a.n_qtiles - 1);
                 for (int t0 = t_first; ok && t0 < a.n_rtiles; t0 += a.S) {
-                    const int t = min(t0 + t_off, a.n_rtiles - 1);
+                    const int t = (int)((int64_t)min(t0 + t_off, a.n_rtiles - 1) * a.t_stride % a.n_rtiles);
                     for (int kb = 0; kb < a.n_kblocks; ++kb) {
                         if (!tc::mbar_wait(&empty_bar[stage], phase ^ 1, &err_s, 1)) {
                             ok = false;
@@ -354,7 +356,9 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 }
             }
             for (int t0 = t_first; t0 < a.n_rtiles; t0 += a.S) {
-                const int t = t0 + t_off;
+                // the tile the producer loaded (a step past the last tile keeps its columns past nr)
+                const int t = t0 + t_off < a.n_rtiles ? (int)((int64_t)(t0 + t_off) * a.t_stride % a.n_rtiles)
+                                                      : t0 + t_off;
                 if (!tc::mbar_wait(&accf_bar[acc], acc_phase, &err_s, 4)) {
                     ok = false;
                     break;
@@ -577,6 +581,18 @@ int tc_default_policy() { return 0; }
 int tc_default_prefetch() { return 0; }
 int tc_default_cluster() { return 2; }
 int tc_default_share() { return 0; }
+int tc_default_scatter() { return 1; }
+
+// A stride coprime to n near n / golden ratio: consecutive steps visit reference tiles
+// far apart, so a query's scores do not rise tile after tile as the scan approaches its
+// own part of a tree-ordered database (every new best costs an exact score and an insert).
+static int tile_stride(int n) {
+    if (n <= 2) return 1;
+    int s = (int)(0.6180339887 * n);
+    if (s < 1) s = 1;
+    while (std::gcd(s, n) != 1) ++s;
+    return s % n ? s : 1;
+}
 int tc_default_tile_n() { return 128; }
 int tc_default_m_blocks() { return 1; }
 
@@ -704,6 +720,7 @@ int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, c
     a.status = d_status;
     a.policy = ctx->tc_policy >= 0 ? ctx->tc_policy : tc_default_policy();
     a.prefetch = ctx->tc_prefetch >= 0 ? ctx->tc_prefetch : tc_default_prefetch();
+    a.t_stride = (ctx->tc_scatter >= 0 ? ctx->tc_scatter : tc_default_scatter()) ? tile_stride(a.n_rtiles) : 1;
     const int grid = a.G * a.S;
     int st;
     const int MB = tc_m_blocks(ctx, db);

@@ -236,6 +236,9 @@ int hdc_search_tc_tuning(hdc_context* ctx, int group_tiles, int l2_policy, int t
 #define HDC_TC_PREFETCH 1
 #define HDC_TC_CLUSTER 2
 #define HDC_TC_SHARE 3
+#define HDC_TC_SCATTER 5   /* tensor-core search: 1 visits reference tiles in a scattered fixed
+                              order (fewer top-k insertions on tree-ordered databases), 0 in
+                              index order, -1 automatic */
 #define HDC_BEAM_GROUPED 4 /* hdc_beam_search: 1 reads grouped by candidate node, 0 one warp
                               per read, -1 automatic (grouped when dim % 1024 == 0 and
                               dim <= 16384) */

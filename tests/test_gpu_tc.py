@@ -160,3 +160,22 @@ def test_tc_cluster_many_pairs(hdc, cuda, group, share):
     two = _run_tc(ctx, db, q16, qn, 1, 7, 0, 128, group, 1, 2, share)
     for a, b in zip(one, two):
         assert np.array_equal(a, b)
+
+
+def test_tc_tile_order_does_not_change_results(hdc, cuda):
+    """Reference tiles visited in index order or in the scattered order:
+    identical scores, indices, cosines and dots (k = 1, 5, 32)."""
+    import torch
+    import hdc_gb300
+    g = np.random.default_rng(31)
+    dim, nq, nr = 2048, 700, 9000
+    refs = g.integers(-12000, 12001, (nr, dim)).astype(np.int16)
+    q = np.where(g.random((nq, dim)) < 0.5, -1, 1).astype(np.int8)
+    ctx, db, tr, q16, qi, qn = _setup(hdc, cuda, refs, q, dim)
+    for k in (1, 5, 32):
+        res = []
+        for scatter in (0, 1):
+            ctx.option(hdc_gb300.TC_SCATTER, scatter)
+            res.append(_run_tc(ctx, db, q16, qn, 1, k, 0))
+        for a, b in zip(*res):
+            assert np.array_equal(a, b)
