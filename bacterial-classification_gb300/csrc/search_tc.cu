@@ -373,7 +373,11 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         for (int l = 0; l < L; ++l) tc::tmem_ld32(d0 + (uint32_t)((m * L + l) * kBN + c0), v[l]);
                         tc::tmem_ld_wait();
                         const int64_t rbase = (int64_t)t * kBN + c0;
-                        const float rr_lane = (rbase + lane < a.nr) ? __ldg(a.rr + rbase + lane) : 0.0f;
+                        // the chunk's 32 reference norms, one per lane (coalesced), for the rare
+                        // candidates that pass the fp32 filter
+                        const bool in_lane = rbase + lane < a.nr;
+                        const float rr_lane = in_lane ? __ldg(a.rr + rbase + lane) : 0.0f;
+                        const int64_t rn_lane = in_lane ? __ldg(a.rn + rbase + lane) : 0;
 #pragma unroll
                         for (int c = 0; c < 32; ++c) {
                             const float rrc = __shfl_sync(0xffffffffu, rr_lane, c);
@@ -385,13 +389,16 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                                 af = fmaf(__uint_as_float(v[l][c]), scale, af);
                             }
                             const float ap = approx_tc(af, my_rq[m], rrc, a.mode);
-                            if (!(ap >= thr[m]) || !live[m] || rbase + c >= a.nr) continue;
+                            const bool pass = ap >= thr[m] && live[m] && rbase + c < a.nr;
+                            if (!__any_sync(0xffffffffu, pass)) continue;  // the common case: no lane
+                            const int64_t rnc = __shfl_sync(0xffffffffu, rn_lane, c);
+                            if (!pass) continue;
                             int64_t dot = 0;
 #pragma unroll
                             for (int l = 0; l < L; ++l)
                                 dot += (int64_t)__float2ll_rn(__uint_as_float(v[l][c])) * ((int64_t)1 << (11 * l));
                             const int64_t gr = rbase + c;
-                            const float s = exact_score(dot, my_qn[m], __ldg(a.rn + gr), a.mode);
+                            const float s = exact_score(dot, my_qn[m], rnc, a.mode);
                             const uint64_t key = make_key(s, (uint32_t)gr);
                             if (key <= keys[m][k - 1]) continue;
                             list_insert(keys[m], dots[m], k, key, dot);
