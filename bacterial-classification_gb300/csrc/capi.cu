@@ -243,6 +243,13 @@ int hdc_context_option(hdc_context* ctx, int option, int value) {
             if (value < -1 || value > 1) return fail(HDC_ERR_INVALID, "option: tile order must be -1, 0 or 1");
             ctx->tc_scatter = value;
             return HDC_OK;
+        case HDC_TC_PAIR_MMA:
+            ctx->tc_pair_mma = value < 0 ? -1 : (value != 0);
+            return HDC_OK;
+        case HDC_TC_KBLOCK:
+            if (value != 0 && value != 32 && value != 64) return fail(HDC_ERR_INVALID, "option: K block must be 0, 32 or 64");
+            ctx->tc_kblock = value;
+            return HDC_OK;
         case HDC_BEAM_GROUPED:
             if (value < -1 || value > 1) return fail(HDC_ERR_INVALID, "option: beam grouping must be -1, 0 or 1");
             ctx->beam_grouped = value;

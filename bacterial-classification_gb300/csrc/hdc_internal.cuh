@@ -29,6 +29,8 @@ struct hdc_context {
     int tc_prefetch = -1;           // tensor-core search: K blocks prefetched into L2 ahead (-1: automatic)
     int tc_cluster = 0;             // tensor-core search: CTAs sharing an operand's blocks, 1 or 2 (0: automatic)
     int tc_share = -1;              // tensor-core search: 0 pairs share references, 1 queries (-1: automatic)
+    int tc_pair_mma = -1;           // tensor-core search: CTA pairs as one M = 256 MMA (-1: automatic)
+    int tc_kblock = 0;              // tensor-core search: dims per K block, 32 or 64 (0: automatic)
     int tc_scatter = -1;            // tensor-core search: 1 scattered reference-tile order, 0 index order (-1: auto)
     int beam_grouped = -1;          // descent: 1 reads grouped by candidate node, 0 warp per read (-1: automatic)
 };
@@ -85,6 +87,8 @@ int tc_default_prefetch();
 int tc_default_cluster();
 int tc_default_share();
 int tc_default_scatter();
+int tc_default_kblock();
+int tc_default_pair_mma();
 int tc_default_tile_n();
 int tc_default_m_blocks();
 int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, const int64_t* d_qn, int64_t nq,

@@ -52,27 +52,31 @@ constexpr int kThreadsTC = 192;  // warp 0 TMA, warp 1 MMA, warps 2-5 epilogue
 constexpr int kMaxLimbs = 4;
 constexpr int kMaxKTC = 32;
 
-// Tile shapes: N references per tile.  N = 128 streams K blocks of 64 dims
-// (128-byte rows, 128-byte swizzle); N = 256 uses K blocks of 32 dims
-// (64-byte rows, 64-byte swizzle) so that a stage stays small enough for a
-// deep ring.  Swizzle atoms are 8 rows, so the descriptor stride between
-// 8-row groups is 8 * row bytes.
-template <int N>
+// Tile shapes: N references per tile and K blocks of BK dims: BK = 64 gives
+// 128-byte rows (128-byte swizzle), BK = 32 64-byte rows (64-byte swizzle),
+// half the bytes per stage for a deeper ring (N = 256 always uses 32).
+// Swizzle atoms are 8 rows, so the descriptor stride between 8-row groups is
+// 8 * row bytes.
+template <int N, int BKX = (N == 256 ? 32 : 64)>
 struct Tile {
-    static constexpr int BK = N == 256 ? 32 : 64;
+    static constexpr int BK = BKX;
     static constexpr int ROWB = BK * 2;
     static constexpr int A_BYTES = kBM * ROWB;
     static constexpr int B_BYTES = N * ROWB;  // per limb
     static constexpr uint32_t SBO = 8 * ROWB;
-    static constexpr uint32_t LAYOUT = N == 256 ? 4u : 2u;  // descriptor swizzle code: 64B : 128B
+    static constexpr uint32_t LAYOUT = BK == 32 ? 4u : 2u;  // descriptor swizzle code: 64B : 128B
 };
 
-// A stage holds MB query tiles (M-blocks of 128 rows) and L reference-limb tiles.
-template <int N>
-__host__ __device__ constexpr int tc_stage_bytes(int L, int MB) { return MB * Tile<N>::A_BYTES + L * Tile<N>::B_BYTES; }
-template <int N>
+// A stage holds MB query tiles (M-blocks of 128 rows) and L reference-limb tiles; the ring
+// gets as many stages as fit in 216 KB (at most 12).
+constexpr int kRingBytes = 216 * 1024;
+template <int N, int BK = Tile<N>::BK>
+__host__ __device__ constexpr int tc_stage_bytes(int L, int MB) {
+    return MB * Tile<N, BK>::A_BYTES + L * Tile<N, BK>::B_BYTES;
+}
+template <int N, int BK = Tile<N>::BK>
 __host__ __device__ constexpr int tc_stages(int L, int MB) {
-    return 204800 / tc_stage_bytes<N>(L, MB) < 8 ? 204800 / tc_stage_bytes<N>(L, MB) : 8;
+    return kRingBytes / tc_stage_bytes<N, BK>(L, MB) < 12 ? kRingBytes / tc_stage_bytes<N, BK>(L, MB) : 12;
 }
 // accumulator sets (TMEM columns MB * L * N each): two when they fit in 256 columns
 __host__ __device__ constexpr int tc_acc_bufs(int L, int N, int MB) { return MB * L * N <= 256 ? 2 : 1; }
@@ -103,20 +107,28 @@ __device__ __forceinline__ float approx_tc(float af, float rq, float rr, int mod
     return mode == HDC_SCORE_NORM ? fmaf(2.0f, c, -1.0f) : c;
 }
 
-template <int L, int kBN, int MB, int CL, bool SHARE_A>
+// PAIR_MMA: the CTA pair is one M = 256 MMA (cta_group::2) over its two query
+// tiles; with two limbs the even CTA stages limb 0 of the reference tile and the
+// odd CTA limb 1, and one 256 x 256 x 16 MMA covers both (each CTA's TMEM gets
+// its own 128 queries x both limbs, the layout of the single-CTA form), so each
+// SM holds half the reference bytes per stage.
+template <int L, int kBN, int MB, int CL, bool SHARE_A, int BKT, bool PAIR_MMA>
 __global__ void __launch_bounds__(kThreadsTC, 1)
     tc_search_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcArgs a) {
-    using T = Tile<kBN>;
+    using T = Tile<kBN, BKT>;
     constexpr int kBK = T::BK;
-    constexpr int STAGES = tc_stages<kBN>(L, MB);
+    static_assert(!PAIR_MMA || (L == 2 && kBN == 128 && MB == 1 && CL == 2 && !SHARE_A), "pair MMA shape");
+    constexpr int LS = PAIR_MMA ? 1 : L;  // limb blocks this CTA stages
+    constexpr int STAGES = tc_stages<kBN, BKT>(LS, MB);
     constexpr int ACC = tc_acc_bufs(L, kBN, MB);
     constexpr int TCOLS = tc_tmem_cols(L, kBN, MB);
     constexpr int QT = MB * kBM;  // queries per query tile
-    constexpr uint32_t kStageBytes = (uint32_t)tc_stage_bytes<kBN>(L, MB);
+    constexpr uint32_t kStageBytes = (uint32_t)tc_stage_bytes<kBN, BKT>(LS, MB);
     constexpr uint32_t kAccCols = (uint32_t)(MB * L * kBN);
     constexpr uint32_t IDESC = tc::idesc_f16_f32(kBM, kBN);
-    constexpr bool kPairLimbs = kBN == 128 && L >= 2;  // limb pairs as one N = 256 MMA
+    constexpr bool kPairLimbs = kBN == 128 && L >= 2 && !PAIR_MMA;  // limb pairs as one N = 256 MMA
     constexpr uint32_t IDESC2 = kPairLimbs ? tc::idesc_f16_f32(kBM, 2 * kBN) : IDESC;
+    constexpr uint32_t IDESC_PAIR = tc::idesc_f16_f32(2 * kBM, 2 * kBN);
     static_assert(MB * L * kBN <= 512, "accumulators exceed TMEM");
 
     extern __shared__ uint8_t smem_raw[];
@@ -132,19 +144,25 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         err_s = 0;
         for (int s = 0; s < STAGES; ++s) {
             tc::mbar_init(&full_bar[s], 1);
-            tc::mbar_init(&empty_bar[s], CL);  // one commit from each CTA that reads the stage's multicast
+            // one commit from each CTA that reads the stage's multicast (the even CTA's, with pair MMAs)
+            tc::mbar_init(&empty_bar[s], PAIR_MMA ? 1 : CL);
         }
         for (int b = 0; b < ACC; ++b) {
             tc::mbar_init(&accf_bar[b], 1);
-            tc::mbar_init(&acce_bar[b], 128);
+            tc::mbar_init(&acce_bar[b], PAIR_MMA ? 8 : 128);  // pair MMAs: each epilogue warp of both CTAs
         }
         tc::fence_mbar_init();
         tc::prefetch_tmap(&tmA);
         tc::prefetch_tmap(&tmB);
     }
     if (warp == 1) {
-        tc::tmem_alloc(&tmem_base_s, TCOLS);
-        tc::tmem_relinquish();
+        if constexpr (PAIR_MMA) {
+            tc::tmem_alloc_pair(&tmem_base_s, TCOLS);
+            tc::tmem_relinquish_pair();
+        } else {
+            tc::tmem_alloc(&tmem_base_s, TCOLS);
+            tc::tmem_relinquish();
+        }
     }
     tc::fence_before();
     __syncthreads();
@@ -163,6 +181,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     const int pair_rank = CL > 1 ? (int)(blockIdx.x % CL) : 0;
     const int t_first = SHARE_A ? lane_j - pair_rank : lane_j;  // both CTAs of a pair step through the same t0
     const int t_off = SHARE_A ? pair_rank : 0;
+    const int crank = CL > 1 ? (int)tc::cluster_ctarank() : 0;
 
     if (warp == 0) {
         // ------------------------------------------------ TMA producer
@@ -173,7 +192,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             bool ok = true;
             const uint64_t pol_q = tc::make_policy_evict_last(), pol_r = tc::make_policy_evict_first();
             const bool hint_q = a.policy >= 1, hint_r = a.policy >= 2;
-            const int rank = CL > 1 ? (int)tc::cluster_ctarank() : 0;
+            const int rank = crank;
             for (int grp = 0; ok && grp < a.n_groups; ++grp) {
                 if (grp * a.G + lead_slot >= a.n_qtiles) continue;
                 const int qt = min(grp * a.G + gslot, a.n_qtiles - 1);
@@ -185,6 +204,21 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                             break;
                         }
                         uint8_t* st = ring + (size_t)stage * kStageBytes;
+                        if constexpr (PAIR_MMA) {
+                            // this CTA's query block and its limb's reference block; the bytes of
+                            // both CTAs complete on the even CTA's full barrier, where its MMA waits
+                            if (rank == 0) tc::mbar_arrive_expect_tx(&full_bar[stage], 2 * kStageBytes);
+                            const uint32_t fb = tc::cluster_addr(&full_bar[stage], 0);
+                            tc::tma_load_2d_pair(st, &tmA, fb, kb * kBK, qt * QT);
+                            tc::tma_load_2d_pair(st + T::A_BYTES, &tmB, fb, kb * kBK,
+                                                 (int)(rank * a.r_pad + (int64_t)t * kBN));
+                            ++issued;
+                            if (++stage == STAGES) {
+                                stage = 0;
+                                phase ^= 1;
+                            }
+                            continue;
+                        }
                         tc::mbar_arrive_expect_tx(&full_bar[stage], kStageBytes);
 #pragma unroll
                         for (int m = 0; m < MB; ++m) {
@@ -236,7 +270,8 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     }
                 }
             }
-            // before leaving, let the last loads land (bounded)
+            // before leaving, let the last loads land (bounded); with pair MMAs they land on the
+            // even CTA's barriers, so wait until the commits that free them reach this CTA
             int s = stage;
             uint32_t ph = phase;
             for (int64_t i = 0; i < (issued < STAGES ? issued : (int64_t)STAGES); ++i) {
@@ -244,22 +279,24 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     s = STAGES - 1;
                     ph ^= 1;
                 }
+                uint64_t* bar = PAIR_MMA ? &empty_bar[s] : &full_bar[s];
                 const long long c0 = clock64();
-                while (!tc::mbar_try_wait(tc::smem_u32(&full_bar[s]), ph) && clock64() - c0 < tc::kWaitCycles) {
+                while (!tc::mbar_try_wait(tc::smem_u32(bar), ph) && clock64() - c0 < tc::kWaitCycles) {
                 }
             }
         }
     } else if (warp == 1) {
-        // ------------------------------------------------ MMA issuer
-        if (lane == 0) {
+        // ------------------------------------------------ MMA issuer (the even CTA's, with pair MMAs)
+        if (lane == 0 && (!PAIR_MMA || crank == 0)) {
             int stage = 0, acc = 0;
             uint32_t phase = 0, acc_phase = 0;
             bool ok = true;
-            int64_t consumed = 0;
+            int64_t consumed = 0, tiles = 0;
             for (int grp = 0; ok && grp < a.n_groups; ++grp) {
                 if (grp * a.G + lead_slot >= a.n_qtiles) continue;
                 for (int t0 = t_first; ok && t0 < a.n_rtiles; t0 += a.S) {
-                    if (!tc::mbar_wait(&acce_bar[acc], acc_phase ^ 1, &err_s, 2)) {
+                    if (!(PAIR_MMA ? tc::mbar_wait_cluster(&acce_bar[acc], acc_phase ^ 1, &err_s, 2)
+                                   : tc::mbar_wait(&acce_bar[acc], acc_phase ^ 1, &err_s, 2))) {
                         ok = false;
                         break;
                     }
@@ -272,29 +309,38 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         }
                         tc::fence_after();
                         const uint32_t sa = tc::smem_u32(ring + (size_t)stage * kStageBytes);
+                        if constexpr (PAIR_MMA) {
+                            const uint64_t adesc = tc::kmajor_desc(sa, T::SBO, T::LAYOUT);
+                            const uint64_t bdesc = tc::kmajor_desc(sa + (uint32_t)T::A_BYTES, T::SBO, T::LAYOUT);
 #pragma unroll
-                        for (int l = 0; l < L; ++l) {
-                            // With 128-row tiles two neighbouring limbs' blocks are 256 consecutive
-                            // rows, and their accumulators 256 consecutive columns: one N = 256 MMA
-                            // covers both, reading each query slice from shared memory once.
-                            if (kPairLimbs && (l & 1)) continue;
-                            const bool wide = kPairLimbs && l + 1 < L;
-                            const uint64_t bdesc = tc::kmajor_desc(
-                                sa + (uint32_t)T::A_BYTES * MB + (uint32_t)T::B_BYTES * l, T::SBO, T::LAYOUT);
+                            for (int kk = 0; kk < kBK / 16; ++kk)
+                                tc::mma_f16_pair(d0, adesc + 2 * kk, bdesc + 2 * kk, IDESC_PAIR, (kb | kk) != 0 ? 1u : 0u);
+                            tc::mma_commit_pair_mc(&empty_bar[stage], 3);
+                        } else {
 #pragma unroll
-                            for (int m = 0; m < MB; ++m) {
-                                const uint64_t adesc = tc::kmajor_desc(sa + (uint32_t)T::A_BYTES * m, T::SBO, T::LAYOUT);
+                            for (int l = 0; l < L; ++l) {
+                                // With 128-row tiles two neighbouring limbs' blocks are 256 consecutive
+                                // rows, and their accumulators 256 consecutive columns: one N = 256 MMA
+                                // covers both, reading each query slice from shared memory once.
+                                if (kPairLimbs && (l & 1)) continue;
+                                const bool wide = kPairLimbs && l + 1 < L;
+                                const uint64_t bdesc = tc::kmajor_desc(
+                                    sa + (uint32_t)T::A_BYTES * MB + (uint32_t)T::B_BYTES * l, T::SBO, T::LAYOUT);
 #pragma unroll
-                                for (int kk = 0; kk < kBK / 16; ++kk)  // K = 16 fp16 per MMA = 32 bytes
-                                    tc::mma_f16(d0 + (uint32_t)((m * L + l) * kBN), adesc + 2 * kk, bdesc + 2 * kk,
-                                                wide ? IDESC2 : IDESC, (kb | kk) != 0 ? 1u : 0u);
+                                for (int m = 0; m < MB; ++m) {
+                                    const uint64_t adesc = tc::kmajor_desc(sa + (uint32_t)T::A_BYTES * m, T::SBO, T::LAYOUT);
+#pragma unroll
+                                    for (int kk = 0; kk < kBK / 16; ++kk)  // K = 16 fp16 per MMA = 32 bytes
+                                        tc::mma_f16(d0 + (uint32_t)((m * L + l) * kBN), adesc + 2 * kk, bdesc + 2 * kk,
+                                                    wide ? IDESC2 : IDESC, (kb | kk) != 0 ? 1u : 0u);
+                                }
                             }
+                            // frees the stage (in every CTA of the pair) when these MMAs finish
+                            if constexpr (CL > 1)
+                                tc::mma_commit_mc(&empty_bar[stage], (uint16_t)((1u << CL) - 1));
+                            else
+                                tc::mma_commit(&empty_bar[stage]);
                         }
-                        // frees the stage (in every CTA of the pair) when these MMAs finish
-                        if constexpr (CL > 1)
-                            tc::mma_commit_mc(&empty_bar[stage], (uint16_t)((1u << CL) - 1));
-                        else
-                            tc::mma_commit(&empty_bar[stage]);
                         ++consumed;
                         if (++stage == STAGES) {
                             stage = 0;
@@ -302,14 +348,32 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         }
                     }
                     if (!ok) break;
-                    tc::mma_commit(&accf_bar[acc]);  // accumulators of this tile are complete
+                    // accumulators of this tile are complete
+                    if constexpr (PAIR_MMA)
+                        tc::mma_commit_pair_mc(&accf_bar[acc], 3);
+                    else
+                        tc::mma_commit(&accf_bar[acc]);
+                    ++tiles;
                     if (++acc == ACC) {
                         acc = 0;
                         acc_phase ^= 1;
                     }
                 }
             }
-            if constexpr (CL > 1) {
+            if constexpr (PAIR_MMA) {
+                // the odd CTA's epilogue warps arrive on this CTA's barriers: let the arrivals
+                // for the last tiles land before the CTA can leave (bounded)
+                for (int64_t i = 0; i < (tiles < ACC ? tiles : (int64_t)ACC); ++i) {
+                    const long long c0 = clock64();
+                    while (!tc::mbar_try_wait_cluster(tc::smem_u32(&acce_bar[acc]), acc_phase ^ 1) &&
+                           clock64() - c0 < tc::kWaitCycles) {
+                    }
+                    if (++acc == ACC) {
+                        acc = 0;
+                        acc_phase ^= 1;
+                    }
+                }
+            } else if constexpr (CL > 1) {
                 // the peer's commits for the last stages arrive on this CTA's barriers: let them
                 // land before the CTA can leave (bounded)
                 int s_ = stage;
@@ -410,7 +474,18 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     }
                 }
                 tc::fence_before();
-                tc::mbar_arrive(&acce_bar[acc]);
+                if constexpr (PAIR_MMA) {
+                    // one arrival per warp, on the even CTA's barrier (its MMAs write both TMEMs)
+                    __syncwarp();
+                    if (lane == 0) {
+                        if (crank == 0)
+                            tc::mbar_arrive(&acce_bar[acc]);
+                        else
+                            tc::mbar_arrive_cluster(tc::cluster_addr(&acce_bar[acc], 0));
+                    }
+                } else {
+                    tc::mbar_arrive(&acce_bar[acc]);
+                }
                 if (++acc == ACC) {
                     acc = 0;
                     acc_phase ^= 1;
@@ -432,9 +507,15 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
 
     tc::fence_before();
     __syncthreads();
+    // pair MMAs: the even CTA's MMAs into this CTA's TMEM are complete (its epilogue waited for
+    // every tile) and both CTAs free the columns together
+    if constexpr (PAIR_MMA) tc::cluster_sync();
     if (warp == 1) {
         tc::fence_after();
-        tc::tmem_dealloc(tmem, TCOLS);
+        if constexpr (PAIR_MMA)
+            tc::tmem_dealloc_pair(tmem, TCOLS);
+        else
+            tc::tmem_dealloc(tmem, TCOLS);
     }
     if (threadIdx.x == 0 && err_s) atomicCAS(a.status, 0, 100 + err_s);
     if constexpr (CL > 1) tc::cluster_sync();  // no CTA leaves while its peer may still write into it
@@ -589,6 +670,8 @@ int tc_default_prefetch() { return 0; }
 int tc_default_cluster() { return 2; }
 int tc_default_share() { return 0; }
 int tc_default_scatter() { return 1; }
+int tc_default_kblock() { return 64; }
+int tc_default_pair_mma() { return 1; }
 
 // A stride coprime to n near n / golden ratio: consecutive steps visit reference tiles
 // far apart, so a query's scores do not rise tile after tile as the scan approaches its
@@ -658,15 +741,17 @@ size_t tc_workspace_bytes(const hdc_context* ctx, int64_t nq, const hdc_refdb* d
     return (size_t)S * nq * std::max(k, 1) * (sizeof(uint64_t) + sizeof(int64_t));
 }
 
-template <int L, int N, int MB, int CL, bool SHARE_A = false>
+template <int L, int N, int MB, int CL, bool SHARE_A = false, int BKT = Tile<N>::BK, bool PAIR_MMA = false>
 static int launch_tc_t(const __half* d_q, const hdc_refdb* db, const TcArgs& a, int grid, cudaStream_t stream) {
     CUtensorMap tmA, tmB;
-    // with CL CTAs sharing a block, each loads (and multicasts) 1 / CL of its rows
-    if (!make_tmap(&tmA, d_q, a.nq, a.dim, Tile<N>::BK, SHARE_A ? kBM / CL : kBM) ||
-        !make_tmap(&tmB, db->d_limbs, (int64_t)db->L * db->r_pad, a.dim, Tile<N>::BK, SHARE_A ? N : N / CL))
+    // with CL CTAs sharing a block by multicast, each loads 1 / CL of its rows; with pair
+    // MMAs each CTA loads whole blocks of its own
+    if (!make_tmap(&tmA, d_q, a.nq, a.dim, BKT, SHARE_A ? kBM / CL : kBM) ||
+        !make_tmap(&tmB, db->d_limbs, (int64_t)db->L * db->r_pad, a.dim, BKT, (SHARE_A || PAIR_MMA) ? N : N / CL))
         return fail(HDC_ERR_CUDA, "tc search: cuTensorMapEncodeTiled failed");
-    const size_t smem = (size_t)tc_stages<N>(L, MB) * tc_stage_bytes<N>(L, MB) + 1024;
-    auto kern = tc_search_kernel<L, N, MB, CL, SHARE_A>;
+    constexpr int LS = PAIR_MMA ? 1 : L;
+    const size_t smem = (size_t)tc_stages<N, BKT>(LS, MB) * tc_stage_bytes<N, BKT>(LS, MB) + 1024;
+    auto kern = tc_search_kernel<L, N, MB, CL, SHARE_A, BKT, PAIR_MMA>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_fail(e, "tc search: cudaFuncSetAttribute");
     if constexpr (CL == 1) {
@@ -713,7 +798,12 @@ int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, c
     a.dim = ctx->dim;
     a.k = k;
     a.mode = mode;
-    a.n_kblocks = (ctx->dim + (N == 256 ? Tile<256>::BK : Tile<128>::BK) - 1) / (N == 256 ? Tile<256>::BK : Tile<128>::BK);
+    // 32-dim K blocks (deeper ring) on the paired reference-sharing path when chosen
+    const bool kb32 = N == 128 && tc_m_blocks(ctx, db) == 1 && tc_cluster(ctx, db) == 2 &&
+                      (ctx->tc_share >= 0 ? ctx->tc_share : tc_default_share()) == 0 &&
+                      (ctx->tc_kblock > 0 ? ctx->tc_kblock : tc_default_kblock()) == 32;
+    const int bk = (N == 256 || kb32) ? 32 : 64;
+    a.n_kblocks = (ctx->dim + bk - 1) / bk;
     a.r_pad = db->r_pad;
     int CL = 1, share = 0;
     tc_plan(ctx, nq, db, a.n_qtiles, a.n_rtiles, a.G, a.S, a.n_groups, CL, share);
@@ -731,6 +821,9 @@ int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, c
     const int grid = a.G * a.S;
     int st;
     const int MB = tc_m_blocks(ctx, db);
+    // the pair as one M = 256 MMA: two limbs, 64-dim K blocks, no L2 hints
+    const bool pair_mma = N == 128 && MB == 1 && CL == 2 && !share && bk == 64 && db->L == 2 && a.policy == 0 &&
+                          (ctx->tc_pair_mma >= 0 ? ctx->tc_pair_mma : tc_default_pair_mma()) != 0;
     if (N == 256) {
         switch (db->L) {
             case 1: st = launch_tc_t<1, 256, 1, 1>(d_q, db, a, grid, stream); break;
@@ -747,6 +840,15 @@ int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, c
             case 2: st = launch_tc_t<2, 128, 1, 2, true>(d_q, db, a, grid, stream); break;
             case 3: st = launch_tc_t<3, 128, 1, 2, true>(d_q, db, a, grid, stream); break;
             default: st = launch_tc_t<4, 128, 1, 2, true>(d_q, db, a, grid, stream); break;
+        }
+    } else if (CL == 2 && pair_mma) {
+        st = launch_tc_t<2, 128, 1, 2, false, 64, true>(d_q, db, a, grid, stream);
+    } else if (CL == 2 && kb32) {
+        switch (db->L) {
+            case 1: st = launch_tc_t<1, 128, 1, 2, false, 32>(d_q, db, a, grid, stream); break;
+            case 2: st = launch_tc_t<2, 128, 1, 2, false, 32>(d_q, db, a, grid, stream); break;
+            case 3: st = launch_tc_t<3, 128, 1, 2, false, 32>(d_q, db, a, grid, stream); break;
+            default: st = launch_tc_t<4, 128, 1, 2, false, 32>(d_q, db, a, grid, stream); break;
         }
     } else if (CL == 2) {
         switch (db->L) {

@@ -20,12 +20,13 @@ def _setup(hdc, dev, refs, q_bipolar, dim):
     return ctx, db, tr, q16, qi, qn
 
 
-def _run_tc(ctx, db, q16, qn, maxq, k, mode, tile_n=0, group=0, m_blocks=0, cluster=0, share=-1):
+def _run_tc(ctx, db, q16, qn, maxq, k, mode, tile_n=0, group=0, m_blocks=0, cluster=0, share=-1, pair=-1):
     import torch
     import hdc_gb300
     ctx.tc_tuning(group, -1, tile_n, m_blocks)
     ctx.tc_option(hdc_gb300.TC_CLUSTER, cluster)
     ctx.tc_option(hdc_gb300.TC_SHARE, share)
+    ctx.tc_option(hdc_gb300.TC_PAIR_MMA, pair)
     s, i, c, d = ctx.search_tc(db, q16, qn, maxq, k, mode)
     torch.cuda.synchronize()
     assert ctx.status() == 0
@@ -179,3 +180,71 @@ def test_tc_tile_order_does_not_change_results(hdc, cuda):
             res.append(_run_tc(ctx, db, q16, qn, 1, k, 0))
         for a, b in zip(*res):
             assert np.array_equal(a, b)
+
+def test_tc_kblock32_equals_kblock64(hdc, cuda):
+    """The paired search with 32-dim K blocks (64-byte swizzle, deeper ring)
+    and with 64-dim K blocks: identical scores, indices, cosines and dots,
+    including a dim that is not a multiple of 64 (k = 1, 5, 32)."""
+    import hdc_gb300
+    g = np.random.default_rng(37)
+    for dim, nr, lim in ((2048, 9000, 12000), (1056, 5000, 20000000)):
+        nq = 700
+        refs = g.integers(-lim, lim + 1, (nr, dim)).astype(np.int32 if lim > 32767 else np.int16)
+        q = np.where(g.random((nq, dim)) < 0.5, -1, 1).astype(np.int8)
+        ctx, db, tr, q16, qi, qn = _setup(hdc, cuda, refs, q, dim)
+        for k in (1, 5, 32):
+            res = []
+            for kb in (64, 32):
+                ctx.option(hdc_gb300.TC_KBLOCK, kb)
+                res.append(_run_tc(ctx, db, q16, qn, 1, k, 0))
+            for a, b in zip(*res):
+                assert np.array_equal(a, b)
+
+
+# CTA pairs as one M = 256 MMA (two limbs only; other limb counts take the
+# multicast form whatever the option says).  Groups of 3 query tiles round down
+# to 2; 129 / 300 queries leave the odd CTA of the last pair without a tile.
+@pytest.mark.parametrize("group", [0, 3, 4])
+@pytest.mark.parametrize("dim,nq,nr,k,mode,vmax,dtype", [
+    (2048, 130, 3000, 10, 0, 12000, np.int16),   # two limbs
+    (1024, 300, 777, 1, 1, 12000, np.int16),     # argmax, COS scale, ragged sizes
+    (512, 64, 500, 32, 2, 3000, np.int16),       # DOT scale, largest k
+    (1024, 100, 600, 5, 0, 3000000, np.int32),   # two limbs, the top one above 1024
+    (1056, 200, 900, 5, 0, 12000, np.int16),     # dim not a multiple of the 64-dim K block
+    (10240, 129, 300, 5, 0, 12728, np.int16),    # precision-form dimension
+    (1024, 100, 600, 5, 0, 20000000, np.int32),  # three limbs: multicast form
+    (1024, 200, 1000, 5, 0, 2000, np.int16),     # one limb: multicast form
+])
+def test_tc_pair_mma_vs_oracle(hdc, orc, cuda, dim, nq, nr, k, mode, vmax, dtype, group):
+    g = np.random.default_rng(dim + nq + nr + 7)
+    refs = g.integers(-vmax, vmax + 1, (nr, dim)).astype(dtype)
+    refs[3] = refs[1]
+    refs[4] = 0
+    refs[5, :] = vmax
+    refs[6, ::2] = -vmax
+    q = np.where(g.random((nq, dim)) < 0.5, -1, 1).astype(np.int8)
+    q[0] = np.where(refs[1] >= 0, 1, -1)
+    ctx, db, tr, q16, qi, qn = _setup(hdc, cuda, refs, q, dim)
+    s, i, c, d = _run_tc(ctx, db, q16, qn, 1, k, mode, 128, group, 1, 2, 0, 1)
+    os_, oi, oc, od = orc.topk(q.astype(np.int32), refs.astype(np.int32), min(k, nr), mode)
+    assert np.array_equal(i, oi)
+    assert np.array_equal(d, od)
+    assert np.array_equal(s, os_)
+    assert np.array_equal(c, oc)
+
+
+def test_tc_pair_mma_equals_multicast(hdc, cuda):
+    """Pairs as one M = 256 MMA and pairs sharing reference blocks by
+    multicast: identical scores, indices, cosines and dots (k = 1, 5, 32) on a
+    grid with many pairs and reference lanes."""
+    g = np.random.default_rng(41)
+    dim, nq, nr = 2048, 5000, 20000
+    refs = g.integers(-12000, 12001, (nr, dim)).astype(np.int16)
+    q = np.where(g.random((nq, dim)) < 0.5, -1, 1).astype(np.int8)
+    ctx, db, tr, q16, qi, qn = _setup(hdc, cuda, refs, q, dim)
+    for k in (1, 5, 32):
+        a = _run_tc(ctx, db, q16, qn, 1, k, 0, pair=0)
+        b = _run_tc(ctx, db, q16, qn, 1, k, 0, pair=1)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
+
