@@ -243,6 +243,10 @@ int hdc_context_option(hdc_context* ctx, int option, int value) {
             if (value < -1 || value > 1) return fail(HDC_ERR_INVALID, "option: tile order must be -1, 0 or 1");
             ctx->tc_scatter = value;
             return HDC_OK;
+        case HDC_TC_LANES:
+            if (value < 0) return fail(HDC_ERR_INVALID, "option: lanes must be >= 0");
+            ctx->tc_lanes = value;
+            return HDC_OK;
         case HDC_TC_PAIR_MMA:
             ctx->tc_pair_mma = value < 0 ? -1 : (value != 0);
             return HDC_OK;

@@ -29,6 +29,7 @@ struct hdc_context {
     int tc_prefetch = -1;           // tensor-core search: K blocks prefetched into L2 ahead (-1: automatic)
     int tc_cluster = 0;             // tensor-core search: CTAs sharing an operand's blocks, 1 or 2 (0: automatic)
     int tc_share = -1;              // tensor-core search: 0 pairs share references, 1 queries (-1: automatic)
+    int tc_lanes = 0;               // tensor-core search: at most this many reference lanes (0: SMs / G)
     int tc_pair_mma = -1;           // tensor-core search: CTA pairs as one M = 256 MMA (-1: automatic)
     int tc_kblock = 0;              // tensor-core search: dims per K block, 32 or 64 (0: automatic)
     int tc_scatter = -1;            // tensor-core search: 1 scattered reference-tile order, 0 index order (-1: auto)
@@ -42,6 +43,7 @@ struct hdc_refdb {
     __half* d_limbs = nullptr;  // [L][r_pad][dim]
     int64_t* d_norm2 = nullptr; // [nr]
     float* d_rsq = nullptr;     // [nr]
+    double* d_sqrt = nullptr;   // [nr] sqrt(norm2) rounded to double (the exact score's factor)
     int32_t limb_max[4] = {0, 0, 0, 0};
     int32_t max_abs = 0;
 };
@@ -89,6 +91,8 @@ int tc_default_share();
 int tc_default_scatter();
 int tc_default_kblock();
 int tc_default_pair_mma();
+// Fill db->d_sqrt (allocated here) from db->d_norm2.
+int refdb_sqrt_table(hdc_refdb* db, cudaStream_t stream);
 int tc_default_tile_n();
 int tc_default_m_blocks();
 int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, const int64_t* d_qn, int64_t nq,

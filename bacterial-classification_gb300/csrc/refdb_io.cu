@@ -211,6 +211,11 @@ int hdc_refdb_load(hdc_context* ctx, const char* path, hdc_refdb** out, int32_t*
     }
     if (st == HDC_OK && fnv.done() != h.payload_fnv)
         st = hdc::fail(HDC_ERR_INVALID, "refdb load: checksum mismatch (corrupted file)");
+    if (st == HDC_OK) st = hdc::refdb_sqrt_table(db, 0);
+    if (st == HDC_OK) {
+        const cudaError_t e2 = cudaStreamSynchronize(0);
+        if (e2 != cudaSuccess) st = hdc::cuda_fail(e2, "refdb load: norms");
+    }
     if (st != HDC_OK) {
         hdc::refdb_destroy(db);
         return st;

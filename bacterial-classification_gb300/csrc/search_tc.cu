@@ -99,7 +99,18 @@ struct TcArgs {
     uint64_t* ws_key;     // [S][nq][k]
     int64_t* ws_dot;
     int* status;          // device status word (0 = ok)
+    const double* rs;     // [nr] sqrt(norm2) of the references
+    // [S][nq] the orderable k-th best score of each reference lane's list (0: not full),
+    // zeroed before the launch; null when the lanes do not exchange them
+    uint32_t* lane_kth;
 };
+
+// Filter threshold below a k-th best score sk: the fp32 estimate of any score
+// that can still beat sk is at least this (DOT estimates are within a
+// relative 4e-6 plus one unit).
+__device__ __forceinline__ float filter_below(float sk, int mode) {
+    return mode == HDC_SCORE_DOT ? sk - (fabsf(sk) * 4e-6f + 1.0f) : sk - kFilterMargin;
+}
 
 __device__ __forceinline__ float approx_tc(float af, float rq, float rr, int mode) {
     if (mode == HDC_SCORE_DOT) return af;
@@ -209,9 +220,15 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                             // both CTAs complete on the even CTA's full barrier, where its MMA waits
                             if (rank == 0) tc::mbar_arrive_expect_tx(&full_bar[stage], 2 * kStageBytes);
                             const uint32_t fb = tc::cluster_addr(&full_bar[stage], 0);
-                            tc::tma_load_2d_pair(st, &tmA, fb, kb * kBK, qt * QT);
-                            tc::tma_load_2d_pair(st + T::A_BYTES, &tmB, fb, kb * kBK,
-                                                 (int)(rank * a.r_pad + (int64_t)t * kBN));
+                            const int yb = (int)(rank * a.r_pad + (int64_t)t * kBN);
+                            if (hint_q)
+                                tc::tma_load_2d_pair_hint(st, &tmA, fb, kb * kBK, qt * QT, pol_q);
+                            else
+                                tc::tma_load_2d_pair(st, &tmA, fb, kb * kBK, qt * QT);
+                            if (hint_r)
+                                tc::tma_load_2d_pair_hint(st + T::A_BYTES, &tmB, fb, kb * kBK, yb, pol_r);
+                            else
+                                tc::tma_load_2d_pair(st + T::A_BYTES, &tmB, fb, kb * kBK, yb);
                             ++issued;
                             if (++stage == STAGES) {
                                 stage = 0;
@@ -404,16 +421,21 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             if (grp * a.G + lead_slot >= a.n_qtiles) continue;
             const int qt = grp * a.G + gslot;  // past the last tile for a CTA without one: no live rows
             // this thread owns query row `row` of each M-block
-            int64_t gq[MB], my_qn[MB];
+            int64_t gq[MB];
+            double my_sq[MB];
             float my_rq[MB], thr[MB];
+            uint32_t other_kth[MB], told[MB];  // best k-th of the other lanes; the value this lane last told
             bool live[MB];
 #pragma unroll
             for (int m = 0; m < MB; ++m) {
                 gq[m] = (int64_t)qt * QT + m * kBM + row;
                 live[m] = gq[m] < a.nq;
-                my_qn[m] = live[m] ? a.qn[gq[m]] : 0;
-                my_rq[m] = rsqrt_norm(my_qn[m]);
+                const int64_t qn = live[m] ? a.qn[gq[m]] : 0;
+                my_rq[m] = rsqrt_norm(qn);
+                my_sq[m] = __dsqrt_rn((double)qn);
                 thr[m] = -INFINITY;
+                other_kth[m] = 0;
+                told[m] = 0;
                 for (int i = 0; i < k; ++i) {
                     keys[m][i] = 0;
                     dots[m][i] = 0;
@@ -441,7 +463,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         // candidates that pass the fp32 filter
                         const bool in_lane = rbase + lane < a.nr;
                         const float rr_lane = in_lane ? __ldg(a.rr + rbase + lane) : 0.0f;
-                        const int64_t rn_lane = in_lane ? __ldg(a.rn + rbase + lane) : 0;
+                        const double rs_lane = in_lane ? __ldg(a.rs + rbase + lane) : 0.0;
 #pragma unroll
                         for (int c = 0; c < 32; ++c) {
                             const float rrc = __shfl_sync(0xffffffffu, rr_lane, c);
@@ -455,21 +477,39 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                             const float ap = approx_tc(af, my_rq[m], rrc, a.mode);
                             const bool pass = ap >= thr[m] && live[m] && rbase + c < a.nr;
                             if (!__any_sync(0xffffffffu, pass)) continue;  // the common case: no lane
-                            const int64_t rnc = __shfl_sync(0xffffffffu, rn_lane, c);
+                            const double rsc = __shfl_sync(0xffffffffu, rs_lane, c);
                             if (!pass) continue;
                             int64_t dot = 0;
 #pragma unroll
                             for (int l = 0; l < L; ++l)
                                 dot += (int64_t)__float2ll_rn(__uint_as_float(v[l][c])) * ((int64_t)1 << (11 * l));
                             const int64_t gr = rbase + c;
-                            const float s = exact_score(dot, my_qn[m], rnc, a.mode);
+                            const float s = exact_score_sqrt(dot, my_sq[m], rsc, a.mode);
                             const uint64_t key = make_key(s, (uint32_t)gr);
-                            if (key <= keys[m][k - 1]) continue;
+                            // below another lane's k-th best: k better references already exist
+                            if (key <= keys[m][k - 1] || (uint32_t)(key >> 32) < other_kth[m]) continue;
                             list_insert(keys[m], dots[m], k, key, dot);
-                            if (keys[m][k - 1] != 0) {
-                                const float sk = key_score(keys[m][k - 1]);
-                                thr[m] = a.mode == HDC_SCORE_DOT ? sk - (fabsf(sk) * 4e-6f + 1.0f) : sk - kFilterMargin;
-                            }
+                            if (keys[m][k - 1] != 0) thr[m] = fmaxf(thr[m], filter_below(key_score(keys[m][k - 1]), a.mode));
+                        }
+                    }
+                }
+                if (a.lane_kth) {
+                    // tell the other reference lanes this lane's k-th best of each query, and
+                    // filter by theirs (stale values are lower, so only less selective)
+#pragma unroll
+                    for (int m = 0; m < MB; ++m) {
+                        if (!live[m]) continue;
+                        const uint32_t mine = keys[m][k - 1] != 0 ? (uint32_t)(keys[m][k - 1] >> 32) : 0u;
+                        if (mine != told[m]) {
+                            tc::st_relaxed_u32(a.lane_kth + (int64_t)lane_j * a.nq + gq[m], mine);
+                            told[m] = mine;
+                        }
+                        uint32_t best = other_kth[m];
+                        for (int j = 0; j < a.S; ++j)
+                            if (j != lane_j) best = max(best, tc::ld_relaxed_u32(a.lane_kth + (int64_t)j * a.nq + gq[m]));
+                        if (best > other_kth[m]) {
+                            other_kth[m] = best;
+                            thr[m] = fmaxf(thr[m], filter_below(unord_float(best), a.mode));
                         }
                     }
                 }
@@ -556,6 +596,11 @@ __global__ void rsqrt_kernel(const int64_t* __restrict__ n2, int64_t n, float* _
     if (i < n) out[i] = rsqrt_norm(n2[i]);
 }
 
+__global__ void sqrt_kernel(const int64_t* __restrict__ n2, int64_t n, double* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = __dsqrt_rn((double)n2[i]);
+}
+
 // cuTensorMapEncodeTiled resolved through the runtime, so the library does not
 // link libcuda (it must load on hosts without a driver).
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -639,6 +684,7 @@ int refdb_create(hdc_context* ctx, const void* d_ref, int elem_bytes, int64_t nr
     if (st == HDC_OK) {
         rsqrt_kernel<<<(unsigned)((nr + 255) / 256), 256, 0, stream>>>(db->d_norm2, nr, db->d_rsq);
         e = cudaGetLastError();
+        if (e == cudaSuccess && refdb_sqrt_table(db, stream) != HDC_OK) e = cudaErrorMemoryAllocation;
         if (e == cudaSuccess) e = cudaMemcpyAsync(db->limb_max, d_lmax, sizeof(int32_t) * kMaxLimbs,
                                                   cudaMemcpyDeviceToHost, stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
@@ -646,10 +692,7 @@ int refdb_create(hdc_context* ctx, const void* d_ref, int elem_bytes, int64_t nr
     }
     cudaFree(d_lmax);
     if (st != HDC_OK) {
-        cudaFree(db->d_limbs);
-        cudaFree(db->d_norm2);
-        cudaFree(db->d_rsq);
-        delete db;
+        refdb_destroy(db);
         return st;
     }
     *out = db;
@@ -661,7 +704,16 @@ void refdb_destroy(hdc_refdb* db) {
     cudaFree(db->d_limbs);
     cudaFree(db->d_norm2);
     cudaFree(db->d_rsq);
+    cudaFree(db->d_sqrt);
     delete db;
+}
+
+int refdb_sqrt_table(hdc_refdb* db, cudaStream_t stream) {
+    cudaError_t e = cudaMalloc(&db->d_sqrt, (size_t)db->nr * sizeof(double));
+    if (e != cudaSuccess) return cuda_fail(e, "refdb: allocation");
+    sqrt_kernel<<<(unsigned)((db->nr + 255) / 256), 256, 0, stream>>>(db->d_norm2, db->nr, db->d_sqrt);
+    e = cudaGetLastError();
+    return e == cudaSuccess ? HDC_OK : cuda_fail(e, "refdb: norms");
 }
 
 int tc_default_group() { return 1 << 30; }  // every SM on its own query tile, references shared
@@ -706,8 +758,30 @@ static int tc_cluster(const hdc_context* ctx, const hdc_refdb* db) {
     return (c == 2 && tc_tile_n(ctx, db) == 128 && tc_m_blocks(ctx, db) == 1) ? 2 : 1;
 }
 
+// 32-dim K blocks (deeper ring) on the paired reference-sharing path, when chosen.
+static bool tc_kb32(const hdc_context* ctx, const hdc_refdb* db) {
+    return tc_tile_n(ctx, db) == 128 && tc_m_blocks(ctx, db) == 1 && tc_cluster(ctx, db) == 2 &&
+           (ctx->tc_share >= 0 ? ctx->tc_share : tc_default_share()) == 0 &&
+           (ctx->tc_kblock > 0 ? ctx->tc_kblock : tc_default_kblock()) == 32;
+}
+
+// The reference-sharing pair as one M = 256 MMA: two limbs, 64-dim K blocks.
+static bool tc_pair_mma(const hdc_context* ctx, const hdc_refdb* db) {
+    return db->L == 2 && tc_tile_n(ctx, db) == 128 && tc_m_blocks(ctx, db) == 1 && tc_cluster(ctx, db) == 2 &&
+           (ctx->tc_share >= 0 ? ctx->tc_share : tc_default_share()) == 0 && !tc_kb32(ctx, db) &&
+           (ctx->tc_pair_mma >= 0 ? ctx->tc_pair_mma : tc_default_pair_mma()) != 0;
+}
+
+// Reference lanes of one query tile exchange their k-th best scores when there
+// are 2 to 4 of them (each reads the others' after every tile).
+static size_t tc_lane_kth_bytes(int S, int64_t nq) {
+    return (S >= 2 && S <= 4) ? ((size_t)S * nq * sizeof(uint32_t) + 15) / 16 * 16 : 0;
+}
+
 // share = 0: a pair shares reference blocks (neighbouring query tiles, G even);
 // share = 1: a pair shares query blocks (neighbouring reference lanes, S even).
+// Pair MMAs default to two reference lanes (G = SMs / 2): the two CTAs on a query
+// tile read its blocks at about the same time, so half of the query re-reads hit L2.
 static void tc_plan(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int& n_qtiles, int& n_rtiles, int& G,
                     int& S, int& n_groups, int& CL, int& share) {
     const int qt_rows = kBM * tc_m_blocks(ctx, db);
@@ -715,13 +789,16 @@ static void tc_plan(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int
     n_rtiles = (int)(db->r_pad / tc_tile_n(ctx, db));
     CL = tc_cluster(ctx, db);
     share = CL == 2 ? (ctx->tc_share >= 0 ? ctx->tc_share : tc_default_share()) : 0;
-    const int want = ctx->tc_group > 0 ? ctx->tc_group : (share ? ctx->num_sms / 2 : tc_default_group());
+    const int want = ctx->tc_group > 0                                ? ctx->tc_group
+                     : (share || (CL == 2 && tc_pair_mma(ctx, db))) ? ctx->num_sms / 2
+                                                                      : tc_default_group();
     G = std::max(1, std::min(std::min(want, ctx->num_sms), n_qtiles));
     if (CL == 2 && !share) {
         if (G >= 2 && (G & 1)) --G;
         if (G < 2) CL = 1;
     }
     S = std::max(1, ctx->num_sms / G);
+    if (ctx->tc_lanes > 0) S = std::min(S, ctx->tc_lanes);
     S = std::min(S, n_rtiles);
     if (CL == 2 && share) {
         S &= ~1;
@@ -738,7 +815,7 @@ size_t tc_workspace_bytes(const hdc_context* ctx, int64_t nq, const hdc_refdb* d
     int qt, rt, G, S, ng, CL, share;
     tc_plan(ctx, nq, db, qt, rt, G, S, ng, CL, share);
     k = (int)std::min<int64_t>(k, db->nr);
-    return (size_t)S * nq * std::max(k, 1) * (sizeof(uint64_t) + sizeof(int64_t));
+    return (size_t)S * nq * std::max(k, 1) * (sizeof(uint64_t) + sizeof(int64_t)) + tc_lane_kth_bytes(S, nq);
 }
 
 template <int L, int N, int MB, int CL, bool SHARE_A = false, int BKT = Tile<N>::BK, bool PAIR_MMA = false>
@@ -798,10 +875,7 @@ int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, c
     a.dim = ctx->dim;
     a.k = k;
     a.mode = mode;
-    // 32-dim K blocks (deeper ring) on the paired reference-sharing path when chosen
-    const bool kb32 = N == 128 && tc_m_blocks(ctx, db) == 1 && tc_cluster(ctx, db) == 2 &&
-                      (ctx->tc_share >= 0 ? ctx->tc_share : tc_default_share()) == 0 &&
-                      (ctx->tc_kblock > 0 ? ctx->tc_kblock : tc_default_kblock()) == 32;
+    const bool kb32 = tc_kb32(ctx, db);
     const int bk = (N == 256 || kb32) ? 32 : 64;
     a.n_kblocks = (ctx->dim + bk - 1) / bk;
     a.r_pad = db->r_pad;
@@ -810,10 +884,17 @@ int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, c
     a.qn = d_qn;
     a.rn = db->d_norm2;
     a.rr = db->d_rsq;
-    const size_t need = (size_t)a.S * nq * k * (sizeof(uint64_t) + sizeof(int64_t));
-    if (!d_work || work_bytes < need) return fail(HDC_ERR_INVALID, "tc search: workspace too small");
+    const size_t lists = (size_t)a.S * nq * k * (sizeof(uint64_t) + sizeof(int64_t));
+    const size_t kth_bytes = tc_lane_kth_bytes(a.S, nq);
+    if (!d_work || work_bytes < lists + kth_bytes) return fail(HDC_ERR_INVALID, "tc search: workspace too small");
     a.ws_key = static_cast<uint64_t*>(d_work);
     a.ws_dot = reinterpret_cast<int64_t*>(a.ws_key + (size_t)a.S * nq * k);
+    a.lane_kth = kth_bytes ? reinterpret_cast<uint32_t*>(static_cast<uint8_t*>(d_work) + lists) : nullptr;
+    if (a.lane_kth) {
+        cudaError_t e = cudaMemsetAsync(a.lane_kth, 0, kth_bytes, stream);
+        if (e != cudaSuccess) return cuda_fail(e, "tc search: clear lane thresholds");
+    }
+    a.rs = db->d_sqrt;
     a.status = d_status;
     a.policy = ctx->tc_policy >= 0 ? ctx->tc_policy : tc_default_policy();
     a.prefetch = ctx->tc_prefetch >= 0 ? ctx->tc_prefetch : tc_default_prefetch();
@@ -821,9 +902,7 @@ int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, c
     const int grid = a.G * a.S;
     int st;
     const int MB = tc_m_blocks(ctx, db);
-    // the pair as one M = 256 MMA: two limbs, 64-dim K blocks, no L2 hints
-    const bool pair_mma = N == 128 && MB == 1 && CL == 2 && !share && bk == 64 && db->L == 2 && a.policy == 0 &&
-                          (ctx->tc_pair_mma >= 0 ? ctx->tc_pair_mma : tc_default_pair_mma()) != 0;
+    const bool pair_mma = CL == 2 && !share && tc_pair_mma(ctx, db);
     if (N == 256) {
         switch (db->L) {
             case 1: st = launch_tc_t<1, 256, 1, 1>(d_q, db, a, grid, stream); break;

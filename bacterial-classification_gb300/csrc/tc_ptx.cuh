@@ -96,6 +96,16 @@ __device__ __forceinline__ void tma_load_2d_mc(void* dst, const CUtensorMap* map
         : "memory");
 }
 
+// Relaxed, device-scope 32-bit global accesses (a value other CTAs poll).
+__device__ __forceinline__ void st_relaxed_u32(uint32_t* p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
 __device__ __forceinline__ uint32_t cluster_ctarank() {
     uint32_t r;
     asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
@@ -218,6 +228,16 @@ __device__ __forceinline__ void tma_load_2d_pair(void* dst, const CUtensorMap* m
         "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes "
         "[%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
         "l"(map), "r"(cluster_bar), "r"(x), "r"(y)
+        : "memory");
+}
+
+// Same, with an L2 eviction-priority policy (from make_policy_*).
+__device__ __forceinline__ void tma_load_2d_pair_hint(void* dst, const CUtensorMap* map, uint32_t cluster_bar, int x,
+                                                      int y, uint64_t policy) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint "
+        "[%0], [%1, {%3, %4}], [%2], %5;" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(cluster_bar), "r"(x), "r"(y), "l"(policy)
         : "memory");
 }
 

@@ -64,6 +64,17 @@ __device__ __forceinline__ float exact_score(int64_t dot, int64_t nq, int64_t nr
 // error, still < 1e-6).  DOT scores are exact and need no margin.
 constexpr float kFilterMargin = 4e-6f;
 
+// The same score from sq = sqrt(nq) and sr = sqrt(nr), each already rounded to
+// double (0 for a zero norm): the identical sequence of IEEE operations, with
+// the two square roots computed once per query and per reference.
+__device__ __forceinline__ float exact_score_sqrt(int64_t dot, double sq, double sr, int mode) {
+    if (mode == HDC_SCORE_DOT) return __ll2float_rn(dot);
+    if (sq == 0.0 || sr == 0.0) return -1.0f;
+    const double c = __ddiv_rn((double)dot, __dmul_rn(sq, sr));
+    if (mode == HDC_SCORE_NORM) return __double2float_rn(__dmul_rn(2.0, __dadd_rn(c, -0.5)));
+    return __double2float_rn(c);
+}
+
 __device__ __forceinline__ float approx_score(float dotf, float rq, float rr, int mode) {
     if (mode == HDC_SCORE_DOT) return dotf;
     const float c = dotf * rq * rr;  // rq/rr are 0 for zero norms

@@ -15,7 +15,7 @@ HDC_OK = 0
 ERR = {1: "HDC_ERR_INVALID", 2: "HDC_ERR_RANGE", 3: "HDC_ERR_CUDA", 4: "HDC_ERR_NOMEM",
        5: "HDC_ERR_UNSUPPORTED", 6: "HDC_ERR_TIMEOUT"}
 SCORE_NORM, SCORE_COS, SCORE_DOT = 0, 1, 2
-TC_PREFETCH, TC_CLUSTER, TC_SHARE, BEAM_GROUPED, TC_SCATTER, TC_KBLOCK, TC_PAIR_MMA = 1, 2, 3, 4, 5, 6, 7
+TC_PREFETCH, TC_CLUSTER, TC_SHARE, BEAM_GROUPED, TC_SCATTER, TC_KBLOCK, TC_PAIR_MMA, TC_LANES = 1, 2, 3, 4, 5, 6, 7, 8
 OUT_I16, OUT_I32, OUT_BIPOLAR_BF16, OUT_BIPOLAR_I16, OUT_BIPOLAR_F16, OUT_BIPOLAR_I8 = 0, 1, 2, 3, 4, 5
 
 # (name, restype, argtypes) of every exported entry point

@@ -243,6 +243,8 @@ int hdc_search_tc_tuning(hdc_context* ctx, int group_tiles, int l2_policy, int t
                               32 (half the bytes per stage, a deeper ring) or 64; 0 automatic */
 #define HDC_TC_PAIR_MMA 7  /* tensor-core search, two limbs: each CTA pair as one M = 256 MMA
                               (cta_group::2), 1 on, 0 off, -1 automatic */
+#define HDC_TC_LANES 8     /* tensor-core search: at most this many reference lanes per query tile
+                              (CTAs that split the references of one query tile); 0 automatic */
 #define HDC_BEAM_GROUPED 4 /* hdc_beam_search: 1 reads grouped by candidate node, 0 one warp
                               per read, -1 automatic (grouped when dim % 1024 == 0 and
                               dim <= 16384) */

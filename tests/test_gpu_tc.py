@@ -242,9 +242,52 @@ def test_tc_pair_mma_equals_multicast(hdc, cuda):
     refs = g.integers(-12000, 12001, (nr, dim)).astype(np.int16)
     q = np.where(g.random((nq, dim)) < 0.5, -1, 1).astype(np.int8)
     ctx, db, tr, q16, qi, qn = _setup(hdc, cuda, refs, q, dim)
+    import torch
     for k in (1, 5, 32):
         a = _run_tc(ctx, db, q16, qn, 1, k, 0, pair=0)
         b = _run_tc(ctx, db, q16, qn, 1, k, 0, pair=1)
         for x, y in zip(a, b):
             assert np.array_equal(x, y)
+    # with L2 eviction hints on the pair loads (queries evict-last, + references evict-first)
+    for policy in (1, 2):
+        ctx.tc_tuning(8, policy, 0, 0)
+        c = ctx.search_tc(db, q16, qn, 1, 32, 0)
+        torch.cuda.synchronize()
+        assert ctx.status() == 0
+        for x, y in zip(a, c):
+            assert np.array_equal(x, y.cpu().numpy())
 
+
+
+_LANE_ORACLE = {}
+
+
+# Reference lanes of one query tile exchange their k-th best scores (2 to 4
+# lanes) and filter by them.  A clustered database (rows near a few centres,
+# so many references score close to a query's best) with duplicated rows
+# placed in other lanes' tiles (equal scores across lanes: ties go to the
+# lower index) checks that no reference of the final top-k is dropped.
+@pytest.mark.parametrize("lanes", [2, 3, 4])
+@pytest.mark.parametrize("pair", [0, 1])
+@pytest.mark.parametrize("k,mode", [(1, 0), (5, 0), (32, 0), (5, 2), (10, 1)])
+def test_tc_lane_exchange_vs_oracle(hdc, orc, cuda, lanes, pair, k, mode):
+    import hdc_gb300
+    g = np.random.default_rng(100 + k)
+    dim, nq, nr = 512, 520, 12000
+    centres = g.integers(-9000, 9001, (6, dim))
+    refs = (centres[g.integers(0, 6, nr)] + g.integers(-400, 401, (nr, dim))).astype(np.int16)
+    src = g.choice(nr // 2, 300, replace=False)
+    dst = nr // 2 + g.choice(nr // 2, 300, replace=False)
+    refs[dst] = refs[src]                  # equal scores in other reference tiles
+    q = np.where(g.random((nq, dim)) < 0.5, -1, 1).astype(np.int8)
+    q[:64] = np.where(centres[g.integers(0, 6, 64)] >= 0, 1, -1)  # queries near a centre
+    ctx, db, tr, q16, qi, qn = _setup(hdc, cuda, refs, q, dim)
+    ctx.option(hdc_gb300.TC_LANES, lanes)
+    s, i, c, d = _run_tc(ctx, db, q16, qn, 1, k, mode, 128, 0, 1, 2, 0, pair)
+    if (k, mode) not in _LANE_ORACLE:  # the same inputs for every lane count and form
+        _LANE_ORACLE[(k, mode)] = orc.topk(q.astype(np.int32), refs.astype(np.int32), min(k, nr), mode)
+    os_, oi, oc, od = _LANE_ORACLE[(k, mode)]
+    assert np.array_equal(i, oi)
+    assert np.array_equal(d, od)
+    assert np.array_equal(s, os_)
+    assert np.array_equal(c, oc)
