@@ -212,6 +212,12 @@ int hdc_search_tc(hdc_context* ctx, const hdc_refdb* db, const void* d_q, const 
                                  static_cast<cudaStream_t>(stream));
 }
 
+int hdc_search_tc_last_shape(const hdc_context* ctx, int32_t shape[5]) {
+    if (!ctx || !shape) return hdc::fail(HDC_ERR_INVALID, "tc shape: null argument");
+    for (int i = 0; i < 5; ++i) shape[i] = ctx->tc_last_shape[i];
+    return HDC_OK;
+}
+
 int hdc_search_tc_tuning(hdc_context* ctx, int group_tiles, int l2_policy, int tile_n, int m_blocks) {
     if (!ctx) return fail(HDC_ERR_INVALID, "tc tuning: null context");
     if (group_tiles < 0 || l2_policy < -1 || l2_policy > 2 || (tile_n != 0 && tile_n != 128 && tile_n != 256) ||
@@ -232,7 +238,8 @@ int hdc_context_option(hdc_context* ctx, int option, int value) {
             ctx->tc_prefetch = value;
             return HDC_OK;
         case HDC_TC_CLUSTER:
-            if (value < 0 || value > 2) return fail(HDC_ERR_INVALID, "tc option: cluster must be 0, 1 or 2");
+            if (value < 0 || value > 4 || value == 3)
+                return fail(HDC_ERR_INVALID, "tc option: cluster must be 0, 1, 2 or 4");
             ctx->tc_cluster = value;
             return HDC_OK;
         case HDC_TC_SHARE:

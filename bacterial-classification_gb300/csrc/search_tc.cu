@@ -122,13 +122,19 @@ __device__ __forceinline__ float approx_tc(float af, float rq, float rr, int mod
 // tiles; with two limbs the even CTA stages limb 0 of the reference tile and the
 // odd CTA limb 1, and one 256 x 256 x 16 MMA covers both (each CTA's TMEM gets
 // its own 128 queries x both limbs, the layout of the single-CTA form), so each
-// SM holds half the reference bytes per stage.
+// SM holds half the reference bytes per stage.  With CL = 4 two such pairs run
+// the same two query tiles on two neighbouring reference lanes: each query block
+// is loaded once, half by each pair, and multicast into both, which also keeps
+// the two lanes in step (a lane with fewer tiles runs empty ones at the end).
 template <int L, int kBN, int MB, int CL, bool SHARE_A, int BKT, bool PAIR_MMA>
 __global__ void __launch_bounds__(kThreadsTC, 1)
     tc_search_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcArgs a) {
     using T = Tile<kBN, BKT>;
     constexpr int kBK = T::BK;
-    static_assert(!PAIR_MMA || (L == 2 && kBN == 128 && MB == 1 && CL == 2 && !SHARE_A), "pair MMA shape");
+    static_assert(!PAIR_MMA || (L == 2 && kBN == 128 && MB == 1 && (CL == 2 || CL == 4) && !SHARE_A),
+                  "pair MMA shape");
+    static_assert(CL <= 2 || PAIR_MMA, "clusters of 4 pair the MMA");
+    constexpr bool QUAD = PAIR_MMA && CL == 4;
     constexpr int LS = PAIR_MMA ? 1 : L;  // limb blocks this CTA stages
     constexpr int STAGES = tc_stages<kBN, BKT>(LS, MB);
     constexpr int ACC = tc_acc_bufs(L, kBN, MB);
@@ -155,8 +161,9 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         err_s = 0;
         for (int s = 0; s < STAGES; ++s) {
             tc::mbar_init(&full_bar[s], 1);
-            // one commit from each CTA that reads the stage's multicast (the even CTA's, with pair MMAs)
-            tc::mbar_init(&empty_bar[s], PAIR_MMA ? 1 : CL);
+            // one commit from each CTA that reads the stage's multicast (with pair MMAs: from the
+            // even CTA of each pair that reads it)
+            tc::mbar_init(&empty_bar[s], PAIR_MMA ? CL / 2 : CL);
         }
         for (int b = 0; b < ACC; ++b) {
             tc::mbar_init(&accf_bar[b], 1);
@@ -186,9 +193,17 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     // again and writes nothing).  Sharing queries (SHARE_A): the pair runs one query
     // tile on two neighbouring reference lanes, tile by tile in step (the tile count is
     // even, so both CTAs of a pair have a tile in every step; the clamp below only guards).
-    const int gslot = SHARE_A ? (int)((blockIdx.x / CL) % a.G) : (int)(blockIdx.x % a.G);
-    const int lane_j = SHARE_A ? CL * (int)((blockIdx.x / CL) / a.G) + (int)(blockIdx.x % CL) : (int)(blockIdx.x / a.G);
-    const int lead_slot = SHARE_A ? gslot : gslot & ~(CL - 1);
+    // clusters of 4: CTA 2p + r runs query tile r of the cluster's two on reference lane p of its two
+    const int quad = (int)(blockIdx.x / 4), qr = (int)(blockIdx.x % 4);
+    const int gslot = QUAD      ? 2 * (quad % (a.G / 2)) + (qr & 1)
+                      : SHARE_A ? (int)((blockIdx.x / CL) % a.G)
+                                : (int)(blockIdx.x % a.G);
+    const int lane_j = QUAD      ? 2 * (quad / (a.G / 2)) + (qr >> 1)
+                       : SHARE_A ? CL * (int)((blockIdx.x / CL) / a.G) + (int)(blockIdx.x % CL)
+                                 : (int)(blockIdx.x / a.G);
+    const int lead_slot = SHARE_A ? gslot : gslot & ~(QUAD ? 1 : CL - 1);
+    // every lane of a cluster of 4 steps through the same number of tiles
+    const int t_end = QUAD ? (a.n_rtiles + a.S - 1) / a.S * a.S : a.n_rtiles;
     const int pair_rank = CL > 1 ? (int)(blockIdx.x % CL) : 0;
     const int t_first = SHARE_A ? lane_j - pair_rank : lane_j;  // both CTAs of a pair step through the same t0
     const int t_off = SHARE_A ? pair_rank : 0;
@@ -207,7 +222,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             for (int grp = 0; ok && grp < a.n_groups; ++grp) {
                 if (grp * a.G + lead_slot >= a.n_qtiles) continue;
                 const int qt = min(grp * a.G + gslot, a.n_qtiles - 1);
-                for (int t0 = t_first; ok && t0 < a.n_rtiles; t0 += a.S) {
+                for (int t0 = t_first; ok && t0 < t_end; t0 += a.S) {
                     const int t = (int)((int64_t)min(t0 + t_off, a.n_rtiles - 1) * a.t_stride % a.n_rtiles);
                     for (int kb = 0; kb < a.n_kblocks; ++kb) {
                         if (!tc::mbar_wait(&empty_bar[stage], phase ^ 1, &err_s, 1)) {
@@ -218,13 +233,21 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         if constexpr (PAIR_MMA) {
                             // this CTA's query block and its limb's reference block; the bytes of
                             // both CTAs complete on the even CTA's full barrier, where its MMA waits
-                            if (rank == 0) tc::mbar_arrive_expect_tx(&full_bar[stage], 2 * kStageBytes);
-                            const uint32_t fb = tc::cluster_addr(&full_bar[stage], 0);
-                            const int yb = (int)(rank * a.r_pad + (int64_t)t * kBN);
-                            if (hint_q)
+                            const int pr = rank & 1;  // rank in the pair: limb and query tile
+                            if (pr == 0) tc::mbar_arrive_expect_tx(&full_bar[stage], 2 * kStageBytes);
+                            const uint32_t fb = tc::cluster_addr(&full_bar[stage], (uint32_t)(rank & ~1));
+                            const int yb = (int)(pr * a.r_pad + (int64_t)t * kBN);
+                            if constexpr (QUAD) {
+                                // half of the query block (pair p loads rows 64p..64p+63), into this
+                                // CTA and the CTA of the other pair that runs the same query tile
+                                const int pp = rank >> 1;
+                                tc::tma_load_2d_pair_mc(st + pp * (T::A_BYTES / 2), &tmA, fb, kb * kBK,
+                                                        qt * QT + pp * (kBM / 2), (uint16_t)((1u << pr) | (4u << pr)));
+                            } else if (hint_q) {
                                 tc::tma_load_2d_pair_hint(st, &tmA, fb, kb * kBK, qt * QT, pol_q);
-                            else
+                            } else {
                                 tc::tma_load_2d_pair(st, &tmA, fb, kb * kBK, qt * QT);
+                            }
                             if (hint_r)
                                 tc::tma_load_2d_pair_hint(st + T::A_BYTES, &tmB, fb, kb * kBK, yb, pol_r);
                             else
@@ -304,14 +327,14 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         }
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issuer (the even CTA's, with pair MMAs)
-        if (lane == 0 && (!PAIR_MMA || crank == 0)) {
+        if (lane == 0 && (!PAIR_MMA || (crank & 1) == 0)) {
             int stage = 0, acc = 0;
             uint32_t phase = 0, acc_phase = 0;
             bool ok = true;
             int64_t consumed = 0, tiles = 0;
             for (int grp = 0; ok && grp < a.n_groups; ++grp) {
                 if (grp * a.G + lead_slot >= a.n_qtiles) continue;
-                for (int t0 = t_first; ok && t0 < a.n_rtiles; t0 += a.S) {
+                for (int t0 = t_first; ok && t0 < t_end; t0 += a.S) {
                     if (!(PAIR_MMA ? tc::mbar_wait_cluster(&acce_bar[acc], acc_phase ^ 1, &err_s, 2)
                                    : tc::mbar_wait(&acce_bar[acc], acc_phase ^ 1, &err_s, 2))) {
                         ok = false;
@@ -332,7 +355,9 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
 #pragma unroll
                             for (int kk = 0; kk < kBK / 16; ++kk)
                                 tc::mma_f16_pair(d0, adesc + 2 * kk, bdesc + 2 * kk, IDESC_PAIR, (kb | kk) != 0 ? 1u : 0u);
-                            tc::mma_commit_pair_mc(&empty_bar[stage], 3);
+                            // frees the stage in the pair (and, in a cluster of 4, in the other pair,
+                            // whose query-block half landed there too)
+                            tc::mma_commit_pair_mc(&empty_bar[stage], QUAD ? 0xF : 3);
                         } else {
 #pragma unroll
                             for (int l = 0; l < L; ++l) {
@@ -367,7 +392,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     if (!ok) break;
                     // accumulators of this tile are complete
                     if constexpr (PAIR_MMA)
-                        tc::mma_commit_pair_mc(&accf_bar[acc], 3);
+                        tc::mma_commit_pair_mc(&accf_bar[acc], (uint16_t)(3u << (crank & 2)));
                     else
                         tc::mma_commit(&accf_bar[acc]);
                     ++tiles;
@@ -441,7 +466,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     dots[m][i] = 0;
                 }
             }
-            for (int t0 = t_first; t0 < a.n_rtiles; t0 += a.S) {
+            for (int t0 = t_first; t0 < t_end; t0 += a.S) {
                 // the tile the producer loaded (a step past the last tile keeps its columns past nr)
                 const int t = t0 + t_off < a.n_rtiles ? (int)((int64_t)(t0 + t_off) * a.t_stride % a.n_rtiles)
                                                       : t0 + t_off;
@@ -518,10 +543,10 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                     // one arrival per warp, on the even CTA's barrier (its MMAs write both TMEMs)
                     __syncwarp();
                     if (lane == 0) {
-                        if (crank == 0)
+                        if ((crank & 1) == 0)
                             tc::mbar_arrive(&acce_bar[acc]);
                         else
-                            tc::mbar_arrive_cluster(tc::cluster_addr(&acce_bar[acc], 0));
+                            tc::mbar_arrive_cluster(tc::cluster_addr(&acce_bar[acc], (uint32_t)(crank & ~1)));
                     }
                 } else {
                     tc::mbar_arrive(&acce_bar[acc]);
@@ -719,7 +744,7 @@ int refdb_sqrt_table(hdc_refdb* db, cudaStream_t stream) {
 int tc_default_group() { return 1 << 30; }  // every SM on its own query tile, references shared
 int tc_default_policy() { return 0; }
 int tc_default_prefetch() { return 0; }
-int tc_default_cluster() { return 2; }
+int tc_default_cluster() { return 4; }
 int tc_default_share() { return 0; }
 int tc_default_scatter() { return 1; }
 int tc_default_kblock() { return 64; }
@@ -755,7 +780,7 @@ static int tc_m_blocks(const hdc_context* ctx, const hdc_refdb* db) {
 // even number of query tiles per group (a pair must not straddle two lanes).
 static int tc_cluster(const hdc_context* ctx, const hdc_refdb* db) {
     const int c = ctx->tc_cluster > 0 ? ctx->tc_cluster : tc_default_cluster();
-    return (c == 2 && tc_tile_n(ctx, db) == 128 && tc_m_blocks(ctx, db) == 1) ? 2 : 1;
+    return (c >= 2 && tc_tile_n(ctx, db) == 128 && tc_m_blocks(ctx, db) == 1) ? 2 : 1;
 }
 
 // 32-dim K blocks (deeper ring) on the paired reference-sharing path, when chosen.
@@ -773,57 +798,103 @@ static bool tc_pair_mma(const hdc_context* ctx, const hdc_refdb* db) {
 }
 
 // Reference lanes of one query tile exchange their k-th best scores when there
-// are 2 to 4 of them (each reads the others' after every tile).
+// are 2 to 16 of them (each reads the others' after every tile).
 static size_t tc_lane_kth_bytes(int S, int64_t nq) {
-    return (S >= 2 && S <= 4) ? ((size_t)S * nq * sizeof(uint32_t) + 15) / 16 * 16 : 0;
+    return (S >= 2 && S <= 16) ? ((size_t)S * nq * sizeof(uint32_t) + 15) / 16 * 16 : 0;
 }
 
 // share = 0: a pair shares reference blocks (neighbouring query tiles, G even);
 // share = 1: a pair shares query blocks (neighbouring reference lanes, S even).
 // Pair MMAs default to two reference lanes (G = SMs / 2): the two CTAs on a query
 // tile read its blocks at about the same time, so half of the query re-reads hit L2.
-static void tc_plan(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int& n_qtiles, int& n_rtiles, int& G,
-                    int& S, int& n_groups, int& CL, int& share) {
+struct TcShape {
+    int n_qtiles = 0, n_rtiles = 0, G = 1, S = 1, n_groups = 0, CL = 1, share = 0;
+};
+
+// group / lanes > 0 override the group size and cap the lanes; no_quad keeps pairs.
+static TcShape tc_plan(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int group = 0, int lanes = 0,
+                       bool no_quad = false) {
+    TcShape p;
     const int qt_rows = kBM * tc_m_blocks(ctx, db);
-    n_qtiles = (int)((nq + qt_rows - 1) / qt_rows);
-    n_rtiles = (int)(db->r_pad / tc_tile_n(ctx, db));
-    CL = tc_cluster(ctx, db);
-    share = CL == 2 ? (ctx->tc_share >= 0 ? ctx->tc_share : tc_default_share()) : 0;
-    const int want = ctx->tc_group > 0                                ? ctx->tc_group
-                     : (share || (CL == 2 && tc_pair_mma(ctx, db))) ? ctx->num_sms / 2
-                                                                      : tc_default_group();
-    G = std::max(1, std::min(std::min(want, ctx->num_sms), n_qtiles));
-    if (CL == 2 && !share) {
-        if (G >= 2 && (G & 1)) --G;
-        if (G < 2) CL = 1;
+    p.n_qtiles = (int)((nq + qt_rows - 1) / qt_rows);
+    p.n_rtiles = (int)(db->r_pad / tc_tile_n(ctx, db));
+    p.CL = tc_cluster(ctx, db);
+    p.share = p.CL == 2 ? (ctx->tc_share >= 0 ? ctx->tc_share : tc_default_share()) : 0;
+    const int want = group > 0            ? group
+                     : ctx->tc_group > 0 ? ctx->tc_group
+                     : (p.share || (p.CL == 2 && tc_pair_mma(ctx, db))) ? ctx->num_sms / 2
+                                                                          : tc_default_group();
+    p.G = std::max(1, std::min(std::min(want, ctx->num_sms), p.n_qtiles));
+    if (p.CL == 2 && !p.share) {
+        if (p.G >= 2 && (p.G & 1)) --p.G;
+        if (p.G < 2) p.CL = 1;
     }
-    S = std::max(1, ctx->num_sms / G);
-    if (ctx->tc_lanes > 0) S = std::min(S, ctx->tc_lanes);
-    S = std::min(S, n_rtiles);
-    if (CL == 2 && share) {
-        S &= ~1;
-        if (S < 2) {
-            CL = 1;
-            share = 0;
-            S = std::max(1, std::min(ctx->num_sms / G, n_rtiles));
+    p.S = std::max(1, ctx->num_sms / p.G);
+    if (ctx->tc_lanes > 0) p.S = std::min(p.S, ctx->tc_lanes);
+    if (lanes > 0) p.S = std::min(p.S, lanes);
+    p.S = std::min(p.S, p.n_rtiles);
+    // clusters of 4 (pair MMAs on two reference lanes): G and S even
+    if (!no_quad && p.CL == 2 && !p.share && p.G >= 2 && p.S >= 2 && tc_pair_mma(ctx, db) &&
+        (ctx->tc_cluster > 0 ? ctx->tc_cluster : tc_default_cluster()) == 4) {
+        p.CL = 4;
+        p.S &= ~1;
+    }
+    if (p.CL == 2 && p.share) {
+        p.S &= ~1;
+        if (p.S < 2) {
+            p.CL = 1;
+            p.share = 0;
+            p.S = std::max(1, std::min(ctx->num_sms / p.G, p.n_rtiles));
         }
     }
-    n_groups = (n_qtiles + G - 1) / G;
+    p.n_groups = (p.n_qtiles + p.G - 1) / p.G;
+    return p;
+}
+
+// Workspace of one launch: S partial lists per query, then the lanes' k-th scores.
+static size_t tc_part_bytes(const TcShape& p, int64_t nq, int k) {
+    return (size_t)p.S * nq * k * (sizeof(uint64_t) + sizeof(int64_t)) + tc_lane_kth_bytes(p.S, nq);
+}
+
+static int quad_clusters_fit(const hdc_context* ctx);
+
+// Clusters of 4 may fit on fewer SMs than the grid of the plan (on GB300, 36
+// clusters of 4 = 144 of the 152 SMs).  Then the leading whole groups of the
+// largest even size that fits run as clusters of 4 and the remaining queries as
+// pairs on every SM.  Returns the number of leading queries for clusters of 4
+// (nq: all of them, 0: none) and their group size and lanes.
+static int64_t tc_quad_queries(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int& G4, int& S4) {
+    const TcShape p = tc_plan(ctx, nq, db);
+    G4 = p.G;
+    S4 = p.S;
+    if (p.CL != 4) return 0;
+    const int fit = quad_clusters_fit(ctx);
+    if (fit * 4 >= p.G * p.S) return nq;
+    G4 = 2 * (fit / (p.S / 2));
+    if (G4 < 2) return 0;
+    const int64_t rows = (int64_t)G4 * kBM;
+    return nq / rows * rows;
 }
 
 size_t tc_workspace_bytes(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int k) {
-    int qt, rt, G, S, ng, CL, share;
-    tc_plan(ctx, nq, db, qt, rt, G, S, ng, CL, share);
-    k = (int)std::min<int64_t>(k, db->nr);
-    return (size_t)S * nq * std::max(k, 1) * (sizeof(uint64_t) + sizeof(int64_t)) + tc_lane_kth_bytes(S, nq);
+    k = std::max(1, (int)std::min<int64_t>(k, db->nr));
+    int G4, S4;
+    const int64_t n4 = tc_quad_queries(ctx, nq, db, G4, S4);
+    if (n4 == nq) return tc_part_bytes(tc_plan(ctx, nq, db), nq, k);
+    if (n4 == 0) return tc_part_bytes(tc_plan(ctx, nq, db, 0, 0, true), nq, k);
+    return tc_part_bytes(tc_plan(ctx, n4, db, G4, S4), n4, k) +
+           tc_part_bytes(tc_plan(ctx, nq - n4, db, 0, 0, true), nq - n4, k);
 }
+
+constexpr int kNoClusterFit = -1;  // launch_tc_t: the clusters cannot all be resident
 
 template <int L, int N, int MB, int CL, bool SHARE_A = false, int BKT = Tile<N>::BK, bool PAIR_MMA = false>
 static int launch_tc_t(const __half* d_q, const hdc_refdb* db, const TcArgs& a, int grid, cudaStream_t stream) {
     CUtensorMap tmA, tmB;
     // with CL CTAs sharing a block by multicast, each loads 1 / CL of its rows; with pair
     // MMAs each CTA loads whole blocks of its own
-    if (!make_tmap(&tmA, d_q, a.nq, a.dim, BKT, SHARE_A ? kBM / CL : kBM) ||
+    constexpr bool QUAD = PAIR_MMA && CL == 4;  // query blocks loaded in halves, one by each pair
+    if (!make_tmap(&tmA, d_q, a.nq, a.dim, BKT, SHARE_A ? kBM / CL : QUAD ? kBM / 2 : kBM) ||
         !make_tmap(&tmB, db->d_limbs, (int64_t)db->L * db->r_pad, a.dim, BKT, (SHARE_A || PAIR_MMA) ? N : N / CL))
         return fail(HDC_ERR_CUDA, "tc search: cuTensorMapEncodeTiled failed");
     constexpr int LS = PAIR_MMA ? 1 : L;
@@ -847,6 +918,15 @@ static int launch_tc_t(const __half* d_q, const hdc_refdb* db, const TcArgs& a, 
         at[0].val.clusterDim.z = 1;
         cfg.attrs = at;
         cfg.numAttrs = 1;
+        if constexpr (CL > 2) {
+            // the persistent grid needs every cluster resident at once: otherwise run pairs
+            int fit = 0;
+            e = cudaOccupancyMaxActiveClusters(&fit, kern, &cfg);
+            if (e != cudaSuccess || fit * CL < grid) {
+                cudaGetLastError();
+                return kNoClusterFit;
+            }
+        }
         e = cudaLaunchKernelEx(&cfg, kern, tmA, tmB, a);
         if (e != cudaSuccess) return cuda_fail(e, "tc search: cluster launch");
     }
@@ -854,20 +934,10 @@ static int launch_tc_t(const __half* d_q, const hdc_refdb* db, const TcArgs& a, 
     return e == cudaSuccess ? HDC_OK : cuda_fail(e, "tc search: launch");
 }
 
-int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, const int64_t* d_qn, int64_t nq,
-                     int32_t maxq, int k, int mode, float* d_score, int32_t* d_idx, double* d_cos, int64_t* d_dot,
-                     void* d_work, size_t work_bytes, int* d_status, cudaStream_t stream) {
-    if (nq == 0) return HDC_OK;
-    if (db->dim != ctx->dim) return fail(HDC_ERR_INVALID, "tc search: database and context dims differ");
-    if (k > db->nr) k = (int)db->nr;
-    if (k < 1 || k > kMaxKTC) return fail(HDC_ERR_INVALID, "tc search: k must be in 1..32");
-    if (maxq < 0 || maxq > 2048) return fail(HDC_ERR_RANGE, "tc search: queries must be integers with |q| <= 2048");
-    for (int l = 0; l < db->L; ++l) {
-        const double bound = (double)ctx->dim * std::max(maxq, 1) * std::max(db->limb_max[l], 1);
-        if (bound > 16777216.0)
-            return fail(HDC_ERR_RANGE, "tc search: dim * max|q| * max|limb| exceeds 2^24 (fp32 accumulators inexact)");
-    }
-    if ((reinterpret_cast<uintptr_t>(d_q) & 15) != 0) return fail(HDC_ERR_INVALID, "tc search: queries not 16B aligned");
+// One launch of the search over queries [0, nq) of d_q with the schedule p.
+static int search_part(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, const int64_t* d_qn, int64_t nq, int k,
+                       int mode, float* d_score, int32_t* d_idx, double* d_cos, int64_t* d_dot, void* d_work,
+                       size_t work_bytes, int* d_status, cudaStream_t stream, const TcShape& p, bool record) {
     const int N = tc_tile_n(ctx, db);
     TcArgs a{};
     a.nq = nq;
@@ -879,8 +949,13 @@ int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, c
     const int bk = (N == 256 || kb32) ? 32 : 64;
     a.n_kblocks = (ctx->dim + bk - 1) / bk;
     a.r_pad = db->r_pad;
-    int CL = 1, share = 0;
-    tc_plan(ctx, nq, db, a.n_qtiles, a.n_rtiles, a.G, a.S, a.n_groups, CL, share);
+    int CL = p.CL;
+    const int share = p.share;
+    a.n_qtiles = p.n_qtiles;
+    a.n_rtiles = p.n_rtiles;
+    a.G = p.G;
+    a.S = p.S;
+    a.n_groups = p.n_groups;
     a.qn = d_qn;
     a.rn = db->d_norm2;
     a.rr = db->d_rsq;
@@ -920,6 +995,12 @@ int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, c
             case 3: st = launch_tc_t<3, 128, 1, 2, true>(d_q, db, a, grid, stream); break;
             default: st = launch_tc_t<4, 128, 1, 2, true>(d_q, db, a, grid, stream); break;
         }
+    } else if (CL == 4) {
+        st = launch_tc_t<2, 128, 1, 4, false, 64, true>(d_q, db, a, grid, stream);
+        if (st == kNoClusterFit) {
+            CL = 2;
+            st = launch_tc_t<2, 128, 1, 2, false, 64, true>(d_q, db, a, grid, stream);
+        }
     } else if (CL == 2 && pair_mma) {
         st = launch_tc_t<2, 128, 1, 2, false, 64, true>(d_q, db, a, grid, stream);
     } else if (CL == 2 && kb32) {
@@ -945,7 +1026,78 @@ int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, c
         }
     }
     if (st != HDC_OK) return st;
+    if (record) {
+        ctx->tc_last_shape[0] = CL;
+        ctx->tc_last_shape[1] = a.G;
+        ctx->tc_last_shape[2] = a.S;
+        ctx->tc_last_shape[3] = (CL == 4 || pair_mma || (CL == 2 && tc_pair_mma(ctx, db) && !share)) ? 1 : 0;
+        ctx->tc_last_shape[4] = 0;
+    }
+    ctx->tc_last_shape[4] += 2;  // the search kernel and its merge
     return launch_merge(a.ws_key, a.ws_dot, a.S, nq, k, d_qn, db->d_norm2, d_score, d_idx, d_cos, d_dot, stream);
+}
+
+
+static int quad_clusters_fit(const hdc_context* ctx) {
+    if (ctx->tc_quad_fit >= 0) return ctx->tc_quad_fit;
+    auto kern = tc_search_kernel<2, 128, 1, 4, false, 64, true>;
+    const size_t smem = (size_t)tc_stages<128, 64>(1, 1) * tc_stage_bytes<128, 64>(1, 1) + 1024;
+    int fit = 0;
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(4 * (unsigned)ctx->num_sms, 1, 1);
+        cfg.blockDim = dim3(kThreadsTC, 1, 1);
+        cfg.dynamicSmemBytes = smem;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = 4;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        if (cudaOccupancyMaxActiveClusters(&fit, kern, &cfg) != cudaSuccess) fit = 0;
+    }
+    cudaGetLastError();
+    const_cast<hdc_context*>(ctx)->tc_quad_fit = fit;
+    return fit;
+}
+
+int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, const int64_t* d_qn, int64_t nq,
+                     int32_t maxq, int k, int mode, float* d_score, int32_t* d_idx, double* d_cos, int64_t* d_dot,
+                     void* d_work, size_t work_bytes, int* d_status, cudaStream_t stream) {
+    if (nq == 0) return HDC_OK;
+    if (db->dim != ctx->dim) return fail(HDC_ERR_INVALID, "tc search: database and context dims differ");
+    if (k > db->nr) k = (int)db->nr;
+    if (k < 1 || k > kMaxKTC) return fail(HDC_ERR_INVALID, "tc search: k must be in 1..32");
+    if (maxq < 0 || maxq > 2048) return fail(HDC_ERR_RANGE, "tc search: queries must be integers with |q| <= 2048");
+    for (int l = 0; l < db->L; ++l) {
+        const double bound = (double)ctx->dim * std::max(maxq, 1) * std::max(db->limb_max[l], 1);
+        if (bound > 16777216.0)
+            return fail(HDC_ERR_RANGE, "tc search: dim * max|q| * max|limb| exceeds 2^24 (fp32 accumulators inexact)");
+    }
+    if ((reinterpret_cast<uintptr_t>(d_q) & 15) != 0) return fail(HDC_ERR_INVALID, "tc search: queries not 16B aligned");
+    int G4, S4;
+    const int64_t n4 = tc_quad_queries(ctx, nq, db, G4, S4);
+    if (n4 == nq)
+        return search_part(ctx, db, d_q, d_qn, nq, k, mode, d_score, d_idx, d_cos, d_dot, d_work, work_bytes, d_status,
+                           stream, tc_plan(ctx, nq, db), true);
+    const TcShape rest = tc_plan(ctx, nq - n4, db, 0, 0, true);
+    if (n4 == 0)
+        return search_part(ctx, db, d_q, d_qn, nq, k, mode, d_score, d_idx, d_cos, d_dot, d_work, work_bytes, d_status,
+                           stream, rest, true);
+    // leading whole groups as clusters of 4, the remaining queries as pairs
+    const TcShape lead = tc_plan(ctx, n4, db, G4, S4);
+    const size_t w4 = tc_part_bytes(lead, n4, k);
+    if (!d_work || work_bytes < w4 + tc_part_bytes(rest, nq - n4, k))
+        return fail(HDC_ERR_INVALID, "tc search: workspace too small");
+    int st = search_part(ctx, db, d_q, d_qn, n4, k, mode, d_score, d_idx, d_cos, d_dot, d_work, w4, d_status, stream,
+                         lead, true);
+    if (st != HDC_OK) return st;
+    const int64_t o = n4;  // outputs the caller does not want stay null
+    return search_part(ctx, db, d_q + o * ctx->dim, d_qn + o, nq - n4, k, mode, d_score ? d_score + o * k : nullptr,
+                       d_idx ? d_idx + o * k : nullptr, d_cos ? d_cos + o * k : nullptr,
+                       d_dot ? d_dot + o * k : nullptr, static_cast<uint8_t*>(d_work) + w4, work_bytes - w4, d_status,
+                       stream, rest, false);
 }
 
 }  // namespace hdc

@@ -241,6 +241,18 @@ __device__ __forceinline__ void tma_load_2d_pair_hint(void* dst, const CUtensorM
         : "memory");
 }
 
+// tma_load_2d_pair written to the same offset of every CTA in cta_mask; each
+// destination's bytes complete on the mbarrier at `cluster_bar`'s offset in
+// the even CTA of that destination's pair.
+__device__ __forceinline__ void tma_load_2d_pair_mc(void* dst, const CUtensorMap* map, uint32_t cluster_bar, int x,
+                                                    int y, uint16_t cta_mask) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster "
+        "[%0], [%1, {%3, %4}], [%2], %5;" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(cluster_bar), "r"(x), "r"(y), "h"(cta_mask)
+        : "memory");
+}
+
 __device__ __forceinline__ void tmem_alloc_pair(uint32_t* dst, uint32_t ncols) {  // one warp of each CTA
     asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)),
                  "r"(ncols)

@@ -54,6 +54,7 @@ SIGNATURES = [
     ("hdc_refdb_load", I32, [P, ctypes.c_char_p, P, P]),
     ("hdc_fasta_parse", I32, [P, P, I64, P, P, P, P, P, I64, P, P]),
     ("hdc_search_tc_tuning", I32, [P, I32, I32, I32, I32]),
+    ("hdc_search_tc_last_shape", I32, [P, P]),
     ("hdc_context_option", I32, [P, I32, I32]),
     ("hdc_pipeline_create", I32, [P, P, I64, I64, ctypes.c_int32, I32, I32, ctypes.POINTER(P)]),
     ("hdc_pipeline_destroy", None, [P]),
@@ -190,6 +191,13 @@ class Context:
 
     def tc_tuning(self, group_tiles=0, l2_policy=-1, tile_n=0, m_blocks=0):
         check(lib().hdc_search_tc_tuning(self.h, group_tiles, l2_policy, tile_n, m_blocks))
+
+    def tc_last_shape(self):
+        """(CTAs per cluster, query tiles per group, reference lanes, pair MMA, kernels launched)
+        of the last search_tc."""
+        out = (ctypes.c_int32 * 5)()
+        check(lib().hdc_search_tc_last_shape(self.h, ctypes.addressof(out)))
+        return tuple(out)
 
     def refdb(self, refs, max_abs, stream=None):
         return RefDB(self, refs, max_abs, stream)

@@ -60,9 +60,10 @@ CONFIGS = {
 # dominant kernel, from single-pass ncu captures of the full-size workloads
 # (profiles/tc_search_kernel_c3.md, profiles/beam_kernel_descent.md), per unit
 # of work, so a run's `traffic` is that per-unit figure times its own units:
-#   tc_search_kernel, c3 (38,912 reads x 200,000 refs = 304 x 1,564 tile pairs): 1.48026e12 B
+#   tc_search_kernel, c3 (38,912 reads x 200,000 refs = 304 x 1,564 tile pairs; the
+#     288 leading query tiles in clusters of 4 + the other 16 in pairs): 1.01427e12 B
 #   grouped descent, c5 (the 6 score_kernel launches of one call, 38,912 reads):  3.76890e10 B
-TRAFFIC_PER_TILE_PAIR_TC = (1.479787e12 + 0.475024e9) / (304 * 1564)
+TRAFFIC_PER_TILE_PAIR_TC = (975.445256e9 + 0.170780e9 + 38.640838e9 + 0.012020e9) / (304 * 1564)
 TRAFFIC_DESCENT = {38912: 37.593492e9 + 95.516928e6}  # reads per call -> bytes (mostly the database, once)
 
 
@@ -212,6 +213,8 @@ class Form:
             ev[0].record(stream)
         if self.name == "tc":
             ctx.search_tc(self.db, self.q, qn, 1, self.K, H.SCORE_NORM, work=self.work, out=self.out)
+            # encode, [norms], then the search kernels and merges the library reports (one or two parts)
+            self.launches = (1 if self.cfg["bipolar"] else 2) + ctx.tc_last_shape()[4]
         else:
             ctx.search_plain(self.q, qn, self.maxq, self.refs, self.rn, self.maxr, self.K, H.SCORE_NORM,
                              work=self.work, out=self.out)
@@ -289,6 +292,9 @@ def run_pipeline(args, cfg, rank, world, H, ctx, tree, refs, rn, maxr, dev):
     for i in range(args.steps):
         pipe.run(pool[i % 2])
     e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    # each graph replay runs encode_kernel, then the search and merge kernels of each part of the
+    # search (memset nodes aside): the search the graph captured after the autotune
+    per_step = 1 + ctx.tc_last_shape()[4]
     # the search kernel alone on the same batch, for the roofline
     form = Form(H, ctx, cfg, "tc", refs, rn, maxr, B, dev)
     d_buf = torch.from_numpy(pool[0].buf).to(dev)
@@ -298,8 +304,7 @@ def run_pipeline(args, cfg, rank, world, H, ctx, tree, refs, rn, maxr, dev):
         t = torch.tensor([ms, e2e_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms, e2e_ms = float(t[0]), float(t[1])
-    # each graph replay runs encode_kernel, tc_search_kernel and merge_kernel (plus a memset node)
-    return dict(ms=ms, e2e_ms=e2e_ms, search_ms=search_ms, clocks=clk.summary(), launches=3 * args.steps,
+    return dict(ms=ms, e2e_ms=e2e_ms, search_ms=search_ms, clocks=clk.summary(), launches=per_step * args.steps,
                 refs=refs.shape[0], limbs=db.limbs, h2d=max_bytes + B * 16, d2h=B * K * 8, tree=tree,
                 tuned=tuned, mean_len=float(np.mean(pool[0].len)), top1_accuracy=acc,
                 refs_host=refs.cpu().numpy() if (rank == 0 and not args.no_cpu_baseline) else None)
@@ -853,10 +858,12 @@ def main():
         tile_pairs = ((B + 127) // 128) * (((nr + 255) // 256) * 2)
         roof = {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
                 "frac": achieved / pk["bf16_tflops"], "traffic": TRAFFIC_PER_TILE_PAIR_TC * tile_pairs,
-                "traffic_source": "ncu DRAM bytes of the full-size c3 launch, per 128x128 tile pair, times "
-                                  "this launch's %d pairs (query tiles re-read for every reference tile)" % tile_pairs,
+                "traffic_source": "ncu DRAM bytes of the two search launches of a full-size c3 call, per "
+                                  "128x128 tile pair, times this call's %d pairs (query tiles re-read for every "
+                                  "reference tile, half of them through L2)" % tile_pairs,
                 "peak_source": "%s dense bf16/fp16 burst (MEASURED_PEAKS.json)" % src,
-                "kernel": "tc_search_kernel + merge, %d fp16 limbs; algorithmic 2*D*R*limbs per read" % r["limbs"]}
+                "kernel": "tc_search_kernel (clusters of 4 + pair remainder) + merge, %d fp16 limbs; "
+                          "algorithmic 2*D*R*limbs per read" % r["limbs"]}
         dtype = "fp16 integer limbs, fp32 accumulators (exact int64 dots), FP64 scores"
     else:
         flops = 2.0 * dim * nr * B

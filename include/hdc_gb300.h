@@ -223,12 +223,21 @@ int hdc_search_plain_noalloc(hdc_context* ctx, const int16_t* d_q, const int64_t
  * on these settings, only the speed does. */
 int hdc_search_tc_tuning(hdc_context* ctx, int group_tiles, int l2_policy, int tile_n, int m_blocks);
 
+/* Shape of the last hdc_search_tc on this context (diagnostic): shape[0] =
+ * CTAs per cluster, [1] = query tiles per group, [2] = reference lanes (of
+ * the leading part, when the batch ran in two), [3] = 1 when each CTA pair
+ * ran as one M = 256 MMA, [4] = kernels launched (a search and a merge per
+ * part).  All 0 before the first search. */
+int hdc_search_tc_last_shape(const hdc_context* ctx, int32_t shape[5]);
+
 /* Further settings of a context; results do not depend on them.
  *   HDC_TC_PREFETCH: K blocks of each query/reference tile pair prefetched
  *     into L2 ahead of the shared-memory ring (0: none, -1: automatic, <= 64);
  *   HDC_TC_CLUSTER: CTAs that share an operand's blocks through a TMA
- *     multicast, 1 or 2 (0: automatic; 2 applies with tile_n 128 and one
- *     M-block);
+ *     multicast, 1, 2 or 4 (0: automatic; 2 applies with tile_n 128 and one
+ *     M-block; 4, two limbs with pair MMAs: two pairs on two reference lanes
+ *     share their query blocks, falling back to 2 where the clusters cannot
+ *     all be resident);
  *   HDC_TC_SHARE: what a pair shares: 0 reference blocks (the pair runs two
  *     neighbouring query tiles), 1 query blocks (the pair runs one query tile
  *     on two neighbouring reference lanes; groups default to half the SMs),

@@ -248,7 +248,15 @@ def test_tc_pair_mma_equals_multicast(hdc, cuda):
         b = _run_tc(ctx, db, q16, qn, 1, k, 0, pair=1)
         for x, y in zip(a, b):
             assert np.array_equal(x, y)
+    # clusters of 4: two pair MMAs on two reference lanes sharing query blocks
+    for k in (1, 32):
+        ref = _run_tc(ctx, db, q16, qn, 1, k, 0, pair=0)
+        c4 = _run_tc(ctx, db, q16, qn, 1, k, 0, cluster=4, pair=1)
+        for x, y in zip(ref, c4):
+            assert np.array_equal(x, y)
     # with L2 eviction hints on the pair loads (queries evict-last, + references evict-first)
+    import hdc_gb300
+    ctx.tc_option(hdc_gb300.TC_CLUSTER, 0)
     for policy in (1, 2):
         ctx.tc_tuning(8, policy, 0, 0)
         c = ctx.search_tc(db, q16, qn, 1, 32, 0)
@@ -267,10 +275,13 @@ _LANE_ORACLE = {}
 # so many references score close to a query's best) with duplicated rows
 # placed in other lanes' tiles (equal scores across lanes: ties go to the
 # lower index) checks that no reference of the final top-k is dropped.
-@pytest.mark.parametrize("lanes", [2, 3, 4])
-@pytest.mark.parametrize("pair", [0, 1])
+# Forms: multicast pairs, pair MMAs, and clusters of 4 (two pair MMAs on two
+# lanes sharing query blocks; 3 lanes round down to 2, and 94 reference tiles
+# over 4 lanes leave two lanes an empty last tile).
+@pytest.mark.parametrize("lanes", [2, 3, 4, 8])
+@pytest.mark.parametrize("pair,cluster", [(0, 2), (1, 2), (1, 4)])
 @pytest.mark.parametrize("k,mode", [(1, 0), (5, 0), (32, 0), (5, 2), (10, 1)])
-def test_tc_lane_exchange_vs_oracle(hdc, orc, cuda, lanes, pair, k, mode):
+def test_tc_lane_exchange_vs_oracle(hdc, orc, cuda, lanes, pair, cluster, k, mode):
     import hdc_gb300
     g = np.random.default_rng(100 + k)
     dim, nq, nr = 512, 520, 12000
@@ -283,7 +294,8 @@ def test_tc_lane_exchange_vs_oracle(hdc, orc, cuda, lanes, pair, k, mode):
     q[:64] = np.where(centres[g.integers(0, 6, 64)] >= 0, 1, -1)  # queries near a centre
     ctx, db, tr, q16, qi, qn = _setup(hdc, cuda, refs, q, dim)
     ctx.option(hdc_gb300.TC_LANES, lanes)
-    s, i, c, d = _run_tc(ctx, db, q16, qn, 1, k, mode, 128, 0, 1, 2, 0, pair)
+    s, i, c, d = _run_tc(ctx, db, q16, qn, 1, k, mode, 128, 0, 1, cluster, 0, pair)
+    assert ctx.status() == 0
     if (k, mode) not in _LANE_ORACLE:  # the same inputs for every lane count and form
         _LANE_ORACLE[(k, mode)] = orc.topk(q.astype(np.int32), refs.astype(np.int32), min(k, nr), mode)
     os_, oi, oc, od = _LANE_ORACLE[(k, mode)]
@@ -291,3 +303,31 @@ def test_tc_lane_exchange_vs_oracle(hdc, orc, cuda, lanes, pair, k, mode):
     assert np.array_equal(d, od)
     assert np.array_equal(s, os_)
     assert np.array_equal(c, oc)
+
+
+def test_tc_quad_split_vs_pairs_and_oracle(hdc, orc, cuda):
+    """A batch whose clusters of 4 do not all fit (75 query tiles: 74 x 2
+    lanes = 148 CTAs, of which 144 can run as clusters of 4): the leading 72
+    tiles run as clusters of 4, the other 293 queries as pairs.  Identical to
+    pairs for the whole batch, and to the oracle on sampled rows, including
+    rows on both sides of the split."""
+    import hdc_gb300
+    g = np.random.default_rng(53)
+    dim, nr, nq = 1024, 4000, 75 * 128 - 91
+    refs = g.integers(-12000, 12001, (nr, dim)).astype(np.int16)
+    q = np.where(g.random((nq, dim)) < 0.5, -1, 1).astype(np.int8)
+    ctx, db, tr, q16, qi, qn = _setup(hdc, cuda, refs, q, dim)
+    for k, mode in ((5, 0), (32, 2)):
+        pairs = _run_tc(ctx, db, q16, qn, 1, k, mode, cluster=2, pair=1)
+        quads = _run_tc(ctx, db, q16, qn, 1, k, mode, cluster=4, pair=1)
+        shape = ctx.tc_last_shape()
+        assert shape[3] == 1 and shape[0] in (2, 4)
+        for x, y in zip(pairs, quads):
+            assert np.array_equal(x, y)
+        rows = np.concatenate([np.arange(9200, 9240), g.choice(nq, 120, replace=False)])
+        os_, oi, oc, od = orc.topk(q[rows].astype(np.int32), refs.astype(np.int32), k, mode)
+        s, i, c, d = quads
+        assert np.array_equal(i[rows], oi)
+        assert np.array_equal(d[rows], od)
+        assert np.array_equal(s[rows], os_)
+        assert np.array_equal(c[rows], oc)
