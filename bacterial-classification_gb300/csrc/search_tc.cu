@@ -94,7 +94,6 @@ struct TcArgs {
     int prefetch;         // K blocks of the same tile pair prefetched into L2 ahead of the ring (0: none)
     int t_stride;         // reference tiles are visited in the order (t * t_stride) mod n_rtiles
     const int64_t* qn;    // [nq] squared norms of the queries
-    const int64_t* rn;    // [nr] squared norms of the references
     const float* rr;      // [nr] fp32 1/sqrt(norm)
     uint64_t* ws_key;     // [S][nq][k]
     int64_t* ws_dot;
@@ -863,11 +862,16 @@ static int quad_clusters_fit(const hdc_context* ctx);
 // largest even size that fits run as clusters of 4 and the remaining queries as
 // pairs on every SM.  Returns the number of leading queries for clusters of 4
 // (nq: all of them, 0: none) and their group size and lanes.
-static int64_t tc_quad_queries(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int& G4, int& S4) {
+// With the cluster size left automatic, clusters of 4 are used up to k = 16: past that the
+// epilogue's exact scores bound the kernel, and clusters of 4, which hold two pairs' MMAs in
+// step, pass each pair's epilogue stalls on to the other (k = 32: 4 % slower than pairs).
+constexpr int kQuadMaxK = 16;
+
+static int64_t tc_quad_queries(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int k, int& G4, int& S4) {
     const TcShape p = tc_plan(ctx, nq, db);
     G4 = p.G;
     S4 = p.S;
-    if (p.CL != 4) return 0;
+    if (p.CL != 4 || (ctx->tc_cluster <= 0 && k > kQuadMaxK)) return 0;
     const int fit = quad_clusters_fit(ctx);
     if (fit * 4 >= p.G * p.S) return nq;
     G4 = 2 * (fit / (p.S / 2));
@@ -879,7 +883,7 @@ static int64_t tc_quad_queries(const hdc_context* ctx, int64_t nq, const hdc_ref
 size_t tc_workspace_bytes(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int k) {
     k = std::max(1, (int)std::min<int64_t>(k, db->nr));
     int G4, S4;
-    const int64_t n4 = tc_quad_queries(ctx, nq, db, G4, S4);
+    const int64_t n4 = tc_quad_queries(ctx, nq, db, k, G4, S4);
     if (n4 == nq) return tc_part_bytes(tc_plan(ctx, nq, db), nq, k);
     if (n4 == 0) return tc_part_bytes(tc_plan(ctx, nq, db, 0, 0, true), nq, k);
     return tc_part_bytes(tc_plan(ctx, n4, db, G4, S4), n4, k) +
@@ -957,7 +961,6 @@ static int search_part(hdc_context* ctx, const hdc_refdb* db, const __half* d_q,
     a.S = p.S;
     a.n_groups = p.n_groups;
     a.qn = d_qn;
-    a.rn = db->d_norm2;
     a.rr = db->d_rsq;
     const size_t lists = (size_t)a.S * nq * k * (sizeof(uint64_t) + sizeof(int64_t));
     const size_t kth_bytes = tc_lane_kth_bytes(a.S, nq);
@@ -1077,7 +1080,7 @@ int launch_search_tc(hdc_context* ctx, const hdc_refdb* db, const __half* d_q, c
     }
     if ((reinterpret_cast<uintptr_t>(d_q) & 15) != 0) return fail(HDC_ERR_INVALID, "tc search: queries not 16B aligned");
     int G4, S4;
-    const int64_t n4 = tc_quad_queries(ctx, nq, db, G4, S4);
+    const int64_t n4 = tc_quad_queries(ctx, nq, db, k, G4, S4);
     if (n4 == nq)
         return search_part(ctx, db, d_q, d_qn, nq, k, mode, d_score, d_idx, d_cos, d_dot, d_work, work_bytes, d_status,
                            stream, tc_plan(ctx, nq, db), true);

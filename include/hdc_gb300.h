@@ -234,10 +234,11 @@ int hdc_search_tc_last_shape(const hdc_context* ctx, int32_t shape[5]);
  *   HDC_TC_PREFETCH: K blocks of each query/reference tile pair prefetched
  *     into L2 ahead of the shared-memory ring (0: none, -1: automatic, <= 64);
  *   HDC_TC_CLUSTER: CTAs that share an operand's blocks through a TMA
- *     multicast, 1, 2 or 4 (0: automatic; 2 applies with tile_n 128 and one
- *     M-block; 4, two limbs with pair MMAs: two pairs on two reference lanes
- *     share their query blocks, falling back to 2 where the clusters cannot
- *     all be resident);
+ *     multicast, 1, 2 or 4 (2 applies with tile_n 128 and one M-block; 4,
+ *     two limbs with pair MMAs: two pairs on two reference lanes share their
+ *     query blocks; where not every cluster of 4 can be resident, the leading
+ *     whole groups that fit run as clusters of 4 and the other queries as
+ *     pairs; 0 automatic: 4 up to k = 16, else 2);
  *   HDC_TC_SHARE: what a pair shares: 0 reference blocks (the pair runs two
  *     neighbouring query tiles), 1 query blocks (the pair runs one query tile
  *     on two neighbouring reference lanes; groups default to half the SMs),
