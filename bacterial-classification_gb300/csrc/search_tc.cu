@@ -102,7 +102,21 @@ struct TcArgs {
     // [S][nq] the orderable k-th best score of each reference lane's list (0: not full),
     // zeroed before the launch; null when the lanes do not exchange them
     uint32_t* lane_kth;
+    int slist;  // 1: the top-k lists live in shared memory after the tile ring, else in local memory
 };
+
+// Insert (key, dot) into a descending list of length k whose entry i is at keys[i * st].
+__device__ __forceinline__ void list_insert_strided(uint64_t* keys, int64_t* dots, int st, int k, uint64_t key,
+                                                    int64_t dot) {
+    int pos = k - 1;
+    while (pos > 0 && keys[(pos - 1) * st] < key) {
+        keys[pos * st] = keys[(pos - 1) * st];
+        dots[pos * st] = dots[(pos - 1) * st];
+        --pos;
+    }
+    keys[pos * st] = key;
+    dots[pos * st] = dot;
+}
 
 // Filter threshold below a k-th best score sk: the fp32 estimate of any score
 // that can still beat sk is at least this (DOT estimates are within a
@@ -439,8 +453,25 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
         int acc = 0;
         uint32_t acc_phase = 0;
         bool ok = true;
-        uint64_t keys[MB][kMaxKTC];
-        int64_t dots[MB][kMaxKTC];
+        // this thread's top-k list of each M-block: entry i at lk[m][i * ls] / ld[m][i * ls], in
+        // shared memory after the ring (one column per TMEM lane) when it fits, else local memory
+        uint64_t keys_local[MB][kMaxKTC];
+        int64_t dots_local[MB][kMaxKTC];
+        uint64_t* lk[MB];
+        int64_t* ld[MB];
+        const int ls = a.slist ? kBM : 1;
+#pragma unroll
+        for (int m = 0; m < MB; ++m) {
+            if (a.slist) {
+                uint64_t* sk = reinterpret_cast<uint64_t*>(ring + (size_t)STAGES * kStageBytes);
+                lk[m] = sk + (size_t)m * k * kBM + row;
+                ld[m] = reinterpret_cast<int64_t*>(sk + (size_t)MB * k * kBM) + (size_t)m * k * kBM + row;
+            } else {
+                lk[m] = keys_local[m];
+                ld[m] = dots_local[m];
+            }
+        }
+        uint64_t kth[MB];  // each list's k-th key (0 while it has fewer than k entries)
         for (int grp = 0; ok && grp < a.n_groups; ++grp) {
             if (grp * a.G + lead_slot >= a.n_qtiles) continue;
             const int qt = grp * a.G + gslot;  // past the last tile for a CTA without one: no live rows
@@ -461,9 +492,10 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 other_kth[m] = 0;
                 told[m] = 0;
                 for (int i = 0; i < k; ++i) {
-                    keys[m][i] = 0;
-                    dots[m][i] = 0;
+                    lk[m][i * ls] = 0;
+                    ld[m][i * ls] = 0;
                 }
+                kth[m] = 0;
             }
             for (int t0 = t_first; t0 < t_end; t0 += a.S) {
                 // the tile the producer loaded (a step past the last tile keeps its columns past nr)
@@ -511,9 +543,10 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                             const float s = exact_score_sqrt(dot, my_sq[m], rsc, a.mode);
                             const uint64_t key = make_key(s, (uint32_t)gr);
                             // below another lane's k-th best: k better references already exist
-                            if (key <= keys[m][k - 1] || (uint32_t)(key >> 32) < other_kth[m]) continue;
-                            list_insert(keys[m], dots[m], k, key, dot);
-                            if (keys[m][k - 1] != 0) thr[m] = fmaxf(thr[m], filter_below(key_score(keys[m][k - 1]), a.mode));
+                            if (key <= kth[m] || (uint32_t)(key >> 32) < other_kth[m]) continue;
+                            list_insert_strided(lk[m], ld[m], ls, k, key, dot);
+                            kth[m] = lk[m][(k - 1) * ls];
+                            if (kth[m] != 0) thr[m] = fmaxf(thr[m], filter_below(key_score(kth[m]), a.mode));
                         }
                     }
                 }
@@ -523,7 +556,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
 #pragma unroll
                     for (int m = 0; m < MB; ++m) {
                         if (!live[m]) continue;
-                        const uint32_t mine = keys[m][k - 1] != 0 ? (uint32_t)(keys[m][k - 1] >> 32) : 0u;
+                        const uint32_t mine = (uint32_t)(kth[m] >> 32);  // 0 while the list is not full
                         if (mine != told[m]) {
                             tc::st_relaxed_u32(a.lane_kth + (int64_t)lane_j * a.nq + gq[m], mine);
                             told[m] = mine;
@@ -562,8 +595,8 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 uint64_t* ok_ = a.ws_key + ((int64_t)lane_j * a.nq + gq[m]) * k;
                 int64_t* od = a.ws_dot + ((int64_t)lane_j * a.nq + gq[m]) * k;
                 for (int i = 0; i < k; ++i) {
-                    ok_[i] = keys[m][i];
-                    od[i] = dots[m][i];
+                    ok_[i] = lk[m][i * ls];
+                    od[i] = ld[m][i * ls];
                 }
             }
         }
@@ -891,6 +924,9 @@ size_t tc_workspace_bytes(const hdc_context* ctx, int64_t nq, const hdc_refdb* d
 }
 
 constexpr int kNoClusterFit = -1;  // launch_tc_t: the clusters cannot all be resident
+// dynamic shared memory a CTA may opt into (227 KB), less 1 KB for the kernel's static
+// shared memory (its mbarriers and flags)
+constexpr size_t kMaxDynSmem = 226 * 1024;
 
 template <int L, int N, int MB, int CL, bool SHARE_A = false, int BKT = Tile<N>::BK, bool PAIR_MMA = false>
 static int launch_tc_t(const __half* d_q, const hdc_refdb* db, const TcArgs& a, int grid, cudaStream_t stream) {
@@ -902,12 +938,17 @@ static int launch_tc_t(const __half* d_q, const hdc_refdb* db, const TcArgs& a, 
         !make_tmap(&tmB, db->d_limbs, (int64_t)db->L * db->r_pad, a.dim, BKT, (SHARE_A || PAIR_MMA) ? N : N / CL))
         return fail(HDC_ERR_CUDA, "tc search: cuTensorMapEncodeTiled failed");
     constexpr int LS = PAIR_MMA ? 1 : L;
-    const size_t smem = (size_t)tc_stages<N, BKT>(LS, MB) * tc_stage_bytes<N, BKT>(LS, MB) + 1024;
+    const size_t ring = (size_t)tc_stages<N, BKT>(LS, MB) * tc_stage_bytes<N, BKT>(LS, MB) + 1024;
+    // the top-k lists (k keys + k dots per query row) go into shared memory when they fit
+    const size_t lists = (size_t)MB * a.k * kBM * (sizeof(uint64_t) + sizeof(int64_t));
+    TcArgs args = a;
+    args.slist = ring + lists <= kMaxDynSmem ? 1 : 0;
+    const size_t smem = ring + (args.slist ? lists : 0);
     auto kern = tc_search_kernel<L, N, MB, CL, SHARE_A, BKT, PAIR_MMA>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_fail(e, "tc search: cudaFuncSetAttribute");
     if constexpr (CL == 1) {
-        kern<<<grid, kThreadsTC, smem, stream>>>(tmA, tmB, a);
+        kern<<<grid, kThreadsTC, smem, stream>>>(tmA, tmB, args);
     } else {
         if (grid % CL) return fail(HDC_ERR_INVALID, "tc search: grid is not a whole number of clusters");
         cudaLaunchConfig_t cfg = {};
@@ -931,7 +972,7 @@ static int launch_tc_t(const __half* d_q, const hdc_refdb* db, const TcArgs& a, 
                 return kNoClusterFit;
             }
         }
-        e = cudaLaunchKernelEx(&cfg, kern, tmA, tmB, a);
+        e = cudaLaunchKernelEx(&cfg, kern, tmA, tmB, args);
         if (e != cudaSuccess) return cuda_fail(e, "tc search: cluster launch");
     }
     e = cudaGetLastError();
