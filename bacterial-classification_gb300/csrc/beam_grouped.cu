@@ -18,6 +18,7 @@
 // instead of once per read that needs it, and a read costs 2 KB of bits
 // (D = 16,384) instead of a 64 KB row per candidate.
 #include "hdc_internal.cuh"
+#include "tc_ptx.cuh"
 #include "topk.cuh"
 
 namespace hdc {
@@ -336,6 +337,391 @@ __global__ void output_kernel(const GArgs a, int32_t* __restrict__ path, float* 
     depth[r] = d;
 }
 
+// ---------------------------------------------------------------- tensor-core scoring
+// Levels above the leaves score on the tensor cores, grouped by parent: the entries (read,
+// beam slot) whose beam row is node P are scored against P's children (a childless P
+// against itself) as one dense [entries] x [children] product.  A work item is up to 128
+// entries x 32 children of one parent.  Eight producer warps write the entries' +1/-1 signs
+// (from the packed bits) and the children's int32 prototype rows, split into three
+// balanced base-2048 fp16 limbs, into 128-byte-swizzled shared memory (two groups of four
+// warps on alternate K blocks); one thread issues M128 x N96 x K16 tcgen05 MMAs, the three
+// limb tiles side by side, into one fp32 TMEM accumulator of 32 columns per limb; four epilogue
+// warps recombine the exact int64 dots and write the pair keys the select kernel reads.
+// Exact: a limb is at most 1024 in magnitude (the top one 512), so every partial sum is an
+// integer of magnitude <= dim * 1024 <= 2^24.  Level 0 is one parent (-1) whose children
+// are the roots and whose entries are all reads.
+constexpr int kTcE = 128;                                         // entries per item (TMEM lanes)
+constexpr int kTcC = 32;                                          // children per item (MMA N)
+constexpr int kTcLimbs = 3;
+constexpr int kTcStages = 4;  // even: each stage is always filled by the same producer group
+static_assert(kTcStages % 2 == 0, "producer groups alternate K blocks");
+// Each producer thread streams its own slice of a K block (16 prototype values, 64 bits of
+// its entry's read) with cp.async this many of its blocks ahead, into a private staging
+// area of shared memory ([slot][16-byte part][thread]: conflict-free), and converts it when
+// its copy group has landed.
+constexpr int kTcDepth = 4;
+constexpr int kTcProducers = 256;
+constexpr size_t kTcStageArea = (size_t)kTcDepth * 5 * kTcProducers * 16;  // 4 x 16 B values + 16 B bits
+constexpr int kTcAccCols = kTcLimbs * kTcC;                       // one accumulator set
+constexpr int kTcTmemCols = 256;                                  // two sets
+constexpr int kTcThreads = 416;                                   // warps 0-7 produce, 8-11 epilogue, 12 MMA
+constexpr int kTcABytes = kTcE * 128;                             // 64 dims of fp16 per row
+constexpr int kTcBBytes = kTcC * 128;                             // per limb
+constexpr int kTcStageBytes = kTcABytes + kTcLimbs * kTcBBytes;   // 28 KB
+constexpr size_t kTcSmem = (size_t)kTcStages * kTcStageBytes + kTcStageArea + 1024;
+
+struct TcItems {
+    int32_t* ent_read;    // [entries] grouped by parent
+    int32_t* ent_p0;      // first pair index of the entry's candidates
+    int32_t* par_cnt;     // [n_nodes] entries per parent
+    int32_t* par_off;     // [n_nodes + 1]
+    int32_t* par_cursor;  // [n_nodes]
+    int32_t* item_cnt;    // [n_nodes]
+    int32_t* item_off;    // [n_nodes + 1]; item_off[n_nodes] = number of items of the level
+    int32_t* item_par;    // [items] parent (-1: level 0)
+    int32_t* item_e0;     // first entry of the item among its parent's
+    int32_t* item_j0;     // first child
+    int* status;          // context status word: 100 + code of a wait that gave up
+};
+
+__device__ __forceinline__ int32_t n_children(const GArgs& a, int32_t P) {
+    if (P < 0) return a.n_roots;
+    const int32_t c = (int32_t)(a.child_ptr[P + 1] - a.child_ptr[P]);
+    return c ? c : 1;
+}
+
+__device__ __forceinline__ int32_t child_at(const GArgs& a, int32_t P, int32_t j) {
+    if (P < 0) return a.roots[j];
+    const int64_t c0 = a.child_ptr[P];
+    return c0 == a.child_ptr[P + 1] ? P : a.child_idx[c0 + j];
+}
+
+// entries (read, beam slot) per parent, then their slots in parent order
+__global__ void par_count_kernel(const GArgs a, TcItems t, int L) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= a.nq || a.done[r]) return;
+    for (int b = 0; b < a.nbeam[r]; ++b) atomicAdd(t.par_cnt + a.paths[state_at(r, b, L - 1)], 1);
+}
+
+__global__ void par_scatter_kernel(const GArgs a, TcItems t, int L) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= a.nq || a.done[r]) return;
+    int32_t p = a.off[r];  // the candidates of beam slot b follow those of slots < b (expand_kernel)
+    for (int b = 0; b < a.nbeam[r]; ++b) {
+        const int32_t P = a.paths[state_at(r, b, L - 1)];
+        const int32_t pos = atomicAdd(t.par_cursor + P, 1);
+        t.ent_read[pos] = (int32_t)r;
+        t.ent_p0[pos] = p;
+        p += n_children(a, P);
+    }
+}
+
+__global__ void item_count_kernel(const GArgs a, TcItems t) {
+    const int64_t P = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (P >= a.n_nodes) return;
+    const int32_t m = t.par_cnt[P];
+    t.item_cnt[P] = m ? ((m + kTcE - 1) / kTcE) * ((n_children(a, (int32_t)P) + kTcC - 1) / kTcC) : 0;
+}
+
+__global__ void item_write_kernel(const GArgs a, TcItems t) {
+    const int64_t P = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (P >= a.n_nodes) return;
+    const int32_t n = t.item_cnt[P];
+    const int32_t nj = (n_children(a, (int32_t)P) + kTcC - 1) / kTcC;
+    for (int32_t i = 0; i < n; ++i) {
+        const int32_t x = t.item_off[P] + i;
+        t.item_par[x] = (int32_t)P;
+        t.item_e0[x] = (i / nj) * kTcE;
+        t.item_j0[x] = (i % nj) * kTcC;
+    }
+}
+
+// level 0: every read against the roots
+__global__ void items_level0_kernel(const GArgs a, TcItems t) {
+    const int32_t ne = (int32_t)((a.nq + kTcE - 1) / kTcE), nj = (a.n_roots + kTcC - 1) / kTcC;
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) t.item_off[a.n_nodes] = ne * nj;
+    if (i >= ne * nj) return;
+    t.item_par[i] = -1;
+    t.item_e0[i] = (i / nj) * kTcE;
+    t.item_j0[i] = (i % nj) * kTcC;
+}
+
+// v = l0 + 2048 l1 + 2048^2 l2 with l0, l1 in [-1024, 1023] and |l2| <= 512, for every int32 v
+__device__ __forceinline__ void limbs3(int32_t v, int32_t& l0, int32_t& l1, int32_t& l2) {
+    const int32_t q1 = (v >> 11) + (((v & 2047) + 1024) >> 11);  // floor((v + 1024) / 2048)
+    l0 = (int32_t)((uint32_t)v - ((uint32_t)q1 << 11));
+    const int32_t q2 = (q1 >> 11) + (((q1 & 2047) + 1024) >> 11);
+    l1 = q1 - q2 * 2048;
+    l2 = q2;
+}
+
+// Two small integers (|x| <= 2048) as an fp16 pair: each becomes an fp32 by the magic
+// number 1.5 * 2^23 (exact for |x| < 2^22: one integer and one float add, no conversion
+// unit), and the pair is packed with one cvt.rn.f16x2.f32 (exact: both fit 11 bits).
+__device__ __forceinline__ uint32_t half2_bits(int32_t x, int32_t y) {
+    const float fx = __int_as_float(0x4B400000 + x) - 12582912.0f;
+    const float fy = __int_as_float(0x4B400000 + y) - 12582912.0f;
+    const __half2 h = __floats2half2_rn(fx, fy);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// 4 sign bits (bit i set: +1) -> 4 fp16 values, +1 = 0x3C00, -1 = 0xBC00: the table
+// entries are 8 bytes, so the 16 of them cover the 32 banks and lookups never conflict
+__device__ __forceinline__ uint2 signs4_entry(uint32_t n) {
+    uint32_t v[2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+        v[i] = 0xBC00BC00u ^ (((n >> (2 * i)) & 1u) << 15) ^ (((n >> (2 * i + 1)) & 1u) << 31);
+    return make_uint2(v[0], v[1]);
+}
+
+// cp.async of 16 / 8 bytes global -> shared; with src_bytes 0 nothing is read and zeros land
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, uint32_t src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(tc::smem_u32(dst)), "l"(src), "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src, uint32_t src_bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(tc::smem_u32(dst)), "l"(src), "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// 16-byte chunk c of row r of a 128-byte-row tile in the 128-byte swizzle layout
+__device__ __forceinline__ uint8_t* swz(uint8_t* tile, int r, int c) { return tile + r * 128 + ((c ^ (r & 7)) << 4); }
+
+__global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a, const TcItems t) {
+    extern __shared__ uint8_t smem_raw[];
+    const uint32_t raw_addr = tc::smem_u32(smem_raw);
+    uint8_t* ring = smem_raw + ((1024 - (raw_addr & 1023)) & 1023);
+    uint4* staging = reinterpret_cast<uint4*>(ring + (size_t)kTcStages * kTcStageBytes);
+    __shared__ uint64_t full_bar[kTcStages], empty_bar[kTcStages], accf_bar[2], acce_bar[2];
+    __shared__ uint32_t tmem_base_s;
+    __shared__ volatile int err_s;
+    __shared__ uint2 signs_lut[16];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x < 16) signs_lut[threadIdx.x] = signs4_entry(threadIdx.x);
+    if (threadIdx.x == 0) {
+        err_s = 0;
+        for (int s = 0; s < kTcStages; ++s) {
+            tc::mbar_init(&full_bar[s], 4);  // one arrival per warp of the producer group
+            tc::mbar_init(&empty_bar[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&accf_bar[b], 1);
+            tc::mbar_init(&acce_bar[b], 4);  // one arrival per epilogue warp
+        }
+        tc::fence_mbar_init();
+    }
+    if (warp == 12) {
+        tc::tmem_alloc(&tmem_base_s, kTcTmemCols);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = tmem_base_s;
+    const int32_t n_items = t.item_off[a.n_nodes];
+    const int kblocks = a.dim / 64;
+
+    if (warp < 8) {
+        // ------------------------------------------------ producers: group g takes K blocks g, g + 2, ...
+        const int g = warp >> 2;
+        const int tid = threadIdx.x & 127, js = tid >> 2, q = tid & 3;  // A row tid; B child js, dims 16q..+15
+        int64_t nbase = 0;  // K blocks of the items before this one (the ring position)
+        bool ok = true;
+        for (int32_t it = blockIdx.x; ok && it < n_items; it += gridDim.x, nbase += kblocks) {
+            const int32_t P = t.item_par[it], e0 = t.item_e0[it], j0 = t.item_j0[it];
+            int64_t rrow = -1;
+            if (P < 0) {
+                if (e0 + tid < a.nq) rrow = e0 + tid;
+            } else if (e0 + tid < t.par_cnt[P]) {
+                rrow = t.ent_read[t.par_off[P] + e0 + tid];
+            }
+            const int32_t child = j0 + js < n_children(a, P) ? child_at(a, P, j0 + js) : -1;
+            // an unused row or child copies nothing (zeros) from a valid address
+            const uint2* bits_row = reinterpret_cast<const uint2*>(a.bits + (rrow >= 0 ? rrow : 0) * a.words);
+            const int4* prow = reinterpret_cast<const int4*>(a.proto + (int64_t)(child >= 0 ? child : 0) * a.dim + 16 * q);
+            const uint32_t wbytes = rrow >= 0 ? 8u : 0u, pbytes = child >= 0 ? 16u : 0u;
+            const int ptid = threadIdx.x;  // 0..255: this thread's staging column
+            auto issue = [&](int kb, int slot) {  // this thread's slice of K block kb, into staging slot `slot`
+                if (kb < kblocks) {
+                    uint4* sb = staging + (size_t)slot * 5 * kTcProducers;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) cp_async16(sb + u * kTcProducers + ptid, prow + kb * 16 + u, pbytes);
+                    cp_async8(sb + 4 * kTcProducers + ptid, bits_row + kb, wbytes);
+                }
+                cp_async_commit();  // one group per call (possibly empty), so the wait below counts blocks
+            };
+#pragma unroll
+            for (int i = 0; i < kTcDepth; ++i) issue(g + 2 * i, i);
+            for (int kb = g, i = 0; kb < kblocks; kb += 2, ++i) {
+                cp_async_wait<kTcDepth - 1>();  // this thread's copies of block kb have landed
+                const int slot = i % kTcDepth;
+                const uint4* sb = staging + (size_t)slot * 5 * kTcProducers;
+                int4 pv[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const uint4 x = sb[u * kTcProducers + ptid];
+                    pv[u] = make_int4((int)x.x, (int)x.y, (int)x.z, (int)x.w);
+                }
+                const uint2 w = *reinterpret_cast<const uint2*>(sb + 4 * kTcProducers + ptid);
+                issue(kb + 2 * kTcDepth, slot);  // the slot is free again: refill it kTcDepth blocks ahead
+                const int64_t n = nbase + kb;
+                const int stage = (int)(n % kTcStages);
+                const uint32_t phase = (uint32_t)((n / kTcStages) & 1);
+                const bool got = tc::mbar_wait(&empty_bar[stage], phase ^ 1, &err_s, 11);
+                if (__any_sync(0xffffffffu, !got)) {
+                    ok = false;
+                    break;
+                }
+                uint8_t* st = ring + (size_t)stage * kTcStageBytes;
+                // A: this entry's 64 signs; an unused row is zero
+                if (rrow >= 0) {
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) {
+                        const uint32_t byte = ((c < 4 ? w.x : w.y) >> (8 * (c & 3))) & 0xffu;
+                        const uint2 lo = signs_lut[byte & 15u], hi = signs_lut[byte >> 4];
+                        *reinterpret_cast<uint4*>(swz(st, tid, c)) = make_uint4(lo.x, lo.y, hi.x, hi.y);
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) *reinterpret_cast<uint4*>(swz(st, tid, c)) = make_uint4(0, 0, 0, 0);
+                }
+                // B: 16 prototype values in three limbs, 8 (one 16-byte chunk per limb) at a time;
+                // an unused child is zero
+                if (child >= 0) {
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        int32_t lv[3][8];
+#pragma unroll
+                        for (int u = 0; u < 2; ++u) {
+                            const int4 p4 = pv[2 * h + u];
+                            const int32_t x[4] = {p4.x, p4.y, p4.z, p4.w};
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) limbs3(x[e], lv[0][4 * u + e], lv[1][4 * u + e], lv[2][4 * u + e]);
+                        }
+#pragma unroll
+                        for (int l = 0; l < kTcLimbs; ++l)
+                            *reinterpret_cast<uint4*>(swz(st + kTcABytes + l * kTcBBytes, js, 2 * q + h)) =
+                                make_uint4(half2_bits(lv[l][0], lv[l][1]), half2_bits(lv[l][2], lv[l][3]),
+                                           half2_bits(lv[l][4], lv[l][5]), half2_bits(lv[l][6], lv[l][7]));
+                    }
+                } else {
+#pragma unroll
+                    for (int l = 0; l < kTcLimbs; ++l)
+#pragma unroll
+                        for (int h = 0; h < 2; ++h)
+                            *reinterpret_cast<uint4*>(swz(st + kTcABytes + l * kTcBBytes, js, 2 * q + h)) =
+                                make_uint4(0, 0, 0, 0);
+                }
+                tc::fence_proxy_async();  // the writes above are read by the tensor cores
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&full_bar[stage]);
+            }
+        }
+        cp_async_wait<0>();  // no copy may still be landing when the CTA leaves
+    } else if (warp < 12) {
+        // ------------------------------------------------ epilogue
+        const int quarter = warp & 3, row = quarter * 32 + lane;
+        int acc = 0;
+        uint32_t acc_phase = 0;
+        for (int32_t it = blockIdx.x; it < n_items; it += gridDim.x) {
+            const int32_t P = t.item_par[it], e0 = t.item_e0[it], j0 = t.item_j0[it];
+            int64_t r = -1;
+            int32_t p0 = 0;
+            if (P < 0) {
+                if (e0 + row < a.nq) {
+                    r = e0 + row;
+                    p0 = a.off[r];
+                }
+            } else if (e0 + row < t.par_cnt[P]) {
+                r = t.ent_read[t.par_off[P] + e0 + row];
+                p0 = t.ent_p0[t.par_off[P] + e0 + row];
+            }
+            const int32_t nc = min(kTcC, n_children(a, P) - j0);
+            if (!tc::mbar_wait(&accf_bar[acc], acc_phase, &err_s, 12)) break;
+            tc::fence_after();
+            const uint32_t d = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * kTcAccCols);
+            const int64_t qn = r >= 0 ? a.qn[r] : 0;
+            // the exact dots of 16 children at a time (limb l of child j is column 32 l + j)
+            for (int h = 0; h < kTcC; h += 16) {
+                if (h >= nc) break;  // nc is the same for the whole warp
+                uint32_t v0[16], v1[16], v2[16];
+                tc::tmem_ld16(d + h, v0);
+                tc::tmem_ld16(d + kTcC + h, v1);
+                tc::tmem_ld16(d + 2 * kTcC + h, v2);
+                tc::tmem_ld_wait();
+                if (r < 0) continue;
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    if (h + j >= nc) break;
+                    const int32_t c = child_at(a, P, j0 + h + j);
+                    const int64_t dot = (int64_t)__float2ll_rn(__uint_as_float(v0[j])) +
+                                        (int64_t)__float2ll_rn(__uint_as_float(v1[j])) * 2048 +
+                                        (int64_t)__float2ll_rn(__uint_as_float(v2[j])) * (2048 * 2048);
+                    a.pair_key[p0 + j0 + h + j] = make_key(exact_score(dot, qn, a.pn[c], a.mode), (uint32_t)c);
+                }
+            }
+            tc::fence_before();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&acce_bar[acc]);  // the accumulators may be reused
+            if (++acc == 2) {
+                acc = 0;
+                acc_phase ^= 1;
+            }
+        }
+    } else if (lane == 0) {
+        // ------------------------------------------------ MMA issuer
+        // the three limb tiles of B are 96 consecutive rows of shared memory and their
+        // accumulators 96 consecutive columns: one N = 96 MMA covers all three
+        constexpr uint32_t IDESC = tc::idesc_f16_f32(kTcE, kTcLimbs * kTcC);
+        int stage = 0, acc = 0;
+        uint32_t phase = 0, acc_phase = 0;
+        bool ok = true;
+        for (int32_t it = blockIdx.x; ok && it < n_items; it += gridDim.x) {
+            if (!tc::mbar_wait(&acce_bar[acc], acc_phase ^ 1, &err_s, 13)) break;
+            tc::fence_after();
+            const uint32_t d = tmem + (uint32_t)(acc * kTcAccCols);
+            for (int kb = 0; kb < kblocks; ++kb) {
+                if (!tc::mbar_wait(&full_bar[stage], phase, &err_s, 14)) {
+                    ok = false;
+                    break;
+                }
+                tc::fence_after();
+                const uint32_t sa = tc::smem_u32(ring + (size_t)stage * kTcStageBytes);
+                const uint64_t adesc = tc::kmajor_desc(sa, 1024, 2);
+                const uint64_t bdesc = tc::kmajor_desc(sa + kTcABytes, 1024, 2);
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk)
+                    tc::mma_f16(d, adesc + 2 * kk, bdesc + 2 * kk, IDESC, (kb | kk) != 0 ? 1u : 0u);
+                tc::mma_commit(&empty_bar[stage]);
+                if (++stage == kTcStages) {
+                    stage = 0;
+                    phase ^= 1;
+                }
+            }
+            if (!ok) break;
+            tc::mma_commit(&accf_bar[acc]);
+            if (++acc == 2) {
+                acc = 0;
+                acc_phase ^= 1;
+            }
+        }
+    }
+    tc::fence_before();
+    __syncthreads();
+    if (warp == 12) {
+        tc::fence_after();
+        tc::tmem_dealloc(tmem, kTcTmemCols);
+    }
+    if (threadIdx.x == 0 && err_s) atomicCAS(t.status, 0, 100 + err_s);
+}
+
 template <typename T>
 T* carve(uint8_t*& cur, int64_t n) {
     T* p = reinterpret_cast<T*>(cur);
@@ -386,6 +772,12 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn
     const int64_t sums = std::max(scan_blocks_needed(nq), scan_blocks_needed(n_nodes));
     int32_t* d_sums = nullptr;
     uint32_t* bits = nullptr;
+    // every level but the last on the tensor cores (HDC_BEAM_GROUPED 2 or automatic)
+    const bool use_tc = (ctx->beam_grouped == 2 || ctx->beam_grouped < 0) && a.dim % 64 == 0 && a.dim <= 16384;
+    TcItems t{};
+    t.status = ctx->d_status;
+    const int64_t cchunks = (std::max<int64_t>(std::max(maxc, n_roots), 1) + kTcC - 1) / kTcC;
+    const int64_t max_items = (nq * beam + 2) * cchunks + ((nq + kTcE - 1) / kTcE) * ((n_roots + kTcC - 1) / kTcC);
     // carve the workspace: once from address 0 to measure it, then from the allocation
     auto carve_all = [&](uint8_t* base) {
         uint8_t* cur = base;
@@ -406,6 +798,18 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn
         a.sorted = carve<int32_t>(cur, P);
         a.pair_key = carve<uint64_t>(cur, P);
         d_sums = carve<int32_t>(cur, sums);
+        if (use_tc) {
+            t.ent_read = carve<int32_t>(cur, nq * beam);
+            t.ent_p0 = carve<int32_t>(cur, nq * beam);
+            t.par_cnt = carve<int32_t>(cur, n_nodes);
+            t.par_off = carve<int32_t>(cur, n_nodes + 1);
+            t.par_cursor = carve<int32_t>(cur, n_nodes);
+            t.item_cnt = carve<int32_t>(cur, n_nodes);
+            t.item_off = carve<int32_t>(cur, n_nodes + 1);
+            t.item_par = carve<int32_t>(cur, max_items);
+            t.item_e0 = carve<int32_t>(cur, max_items);
+            t.item_j0 = carve<int32_t>(cur, max_items);
+        }
         return (size_t)(cur - base);
     };
     const size_t bytes = carve_all(nullptr);
@@ -421,15 +825,39 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn
     cudaMemsetAsync(a.out_depth, 0, nq * 4, stream);
     pack_bits_kernel<<<(unsigned)((nq * a.words + 255) / 256), 256, 0, stream>>>(d_q, nq, a.dim, bits);
     const int work_grid = ctx->num_sms * 8;
+    const unsigned nb = (unsigned)((n_nodes + 255) / 256);
+    if (use_tc && (e = cudaFuncSetAttribute(descent_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)kTcSmem)) != cudaSuccess) {
+        cudaFreeAsync(ws, stream);
+        return cuda_fail(e, "beam: tensor-core scoring setup");
+    }
     for (int L = 0; L < levels; ++L) {
         count_kernel<<<rb, 256, 0, stream>>>(a, L);
         exclusive_scan(a.cnt, a.off, nq, d_sums, stream);
         cudaMemsetAsync(a.node_cnt, 0, (size_t)n_nodes * 4, stream);
         expand_kernel<<<rb, 256, 0, stream>>>(a, L);
-        exclusive_scan(a.node_cnt, a.node_off, n_nodes, d_sums, stream);
-        cudaMemcpyAsync(a.cursor, a.node_off, (size_t)n_nodes * 4, cudaMemcpyDeviceToDevice, stream);
-        scatter_kernel<<<work_grid, 256, 0, stream>>>(a);
-        score_kernel<<<work_grid, kScoreThreads, 0, stream>>>(a);
+        if (use_tc && L < levels - 1) {
+            // entries grouped by parent, then items of up to 128 entries x 32 children
+            if (L == 0) {
+                const int64_t n0 = ((nq + kTcE - 1) / kTcE) * ((n_roots + kTcC - 1) / kTcC);
+                items_level0_kernel<<<(unsigned)((n0 + 255) / 256), 256, 0, stream>>>(a, t);
+            } else {
+                cudaMemsetAsync(t.par_cnt, 0, (size_t)n_nodes * 4, stream);
+                par_count_kernel<<<rb, 256, 0, stream>>>(a, t, L);
+                exclusive_scan(t.par_cnt, t.par_off, n_nodes, d_sums, stream);
+                cudaMemcpyAsync(t.par_cursor, t.par_off, (size_t)n_nodes * 4, cudaMemcpyDeviceToDevice, stream);
+                par_scatter_kernel<<<rb, 256, 0, stream>>>(a, t, L);
+                item_count_kernel<<<nb, 256, 0, stream>>>(a, t);
+                exclusive_scan(t.item_cnt, t.item_off, n_nodes, d_sums, stream);
+                item_write_kernel<<<nb, 256, 0, stream>>>(a, t);
+            }
+            descent_tc_kernel<<<ctx->num_sms, kTcThreads, kTcSmem, stream>>>(a, t);
+        } else {
+            exclusive_scan(a.node_cnt, a.node_off, n_nodes, d_sums, stream);
+            cudaMemcpyAsync(a.cursor, a.node_off, (size_t)n_nodes * 4, cudaMemcpyDeviceToDevice, stream);
+            scatter_kernel<<<work_grid, 256, 0, stream>>>(a);
+            score_kernel<<<work_grid, kScoreThreads, 0, stream>>>(a);
+        }
         select_kernel<<<rb, 256, 0, stream>>>(a, L);
     }
     output_kernel<<<rb, 256, 0, stream>>>(a, d_path, d_path_score, d_depth);

@@ -262,7 +262,7 @@ int hdc_context_option(hdc_context* ctx, int option, int value) {
             ctx->tc_kblock = value;
             return HDC_OK;
         case HDC_BEAM_GROUPED:
-            if (value < -1 || value > 1) return fail(HDC_ERR_INVALID, "option: beam grouping must be -1, 0 or 1");
+            if (value < -1 || value > 2) return fail(HDC_ERR_INVALID, "option: beam grouping must be -1, 0, 1 or 2");
             ctx->beam_grouped = value;
             return HDC_OK;
         default:

@@ -35,7 +35,7 @@ struct hdc_context {
     int tc_pair_mma = -1;           // tensor-core search: CTA pairs as one M = 256 MMA (-1: automatic)
     int tc_kblock = 0;              // tensor-core search: dims per K block, 32 or 64 (0: automatic)
     int tc_scatter = -1;            // tensor-core search: 1 scattered reference-tile order, 0 index order (-1: auto)
-    int beam_grouped = -1;          // descent: 1 reads grouped by candidate node, 0 warp per read (-1: automatic)
+    int beam_grouped = -1;          // descent: 1 grouped by candidate node, 2 + tensor-core levels, 0 warp per read
 };
 
 // A tensor-core reference database (hdc_refdb_create).

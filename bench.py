@@ -538,11 +538,20 @@ def run_descent(args, cfg, rank, world):
         ms, e2e_ms = float(t[0]), float(t[1])
     # candidate rows per read: the level-0 candidates, then up to beam x children per level
     cand = [counts[0]] + [min(W, counts[l - 1]) * b for l in range(1, L)]
-    # kernels per step: the read encode + the descent (grouped: max-children, bit packing,
-    # per level count / 3 scan kernels / expand / 3 scan kernels / scatter / score / select,
-    # output; one warp per read: one kernel)
+    # kernels per step: the read encode + the descent.  Grouped: max-children, bit packing
+    # and output, and per level count / 3 scan kernels / expand / select plus the scoring:
+    # on CUDA cores 3 scan kernels / scatter / score; on the tensor cores (every level but
+    # the last; the default) level 0 its item list and descent_tc_kernel, a later level the
+    # parents' entry count / 3 scans / scatter, item count / 3 scans / write and
+    # descent_tc_kernel.  One warp per read: one kernel.
     grouped = args.beam_grouped != 0 and dim % 1024 == 0 and dim <= 16384
-    per_step = 1 + ((2 + 11 * L + 1) if grouped else 1)
+    tc_levels = grouped and args.beam_grouped in (-1, 2)
+    if not grouped:
+        per_step = 2
+    elif tc_levels and L > 1:
+        per_step = 1 + 3 + 6 * L + 2 + 11 * (L - 2) + 5
+    else:
+        per_step = 1 + 3 + 11 * L
     res = dict(ms=ms, e2e_ms=e2e_ms, search_ms=float(np.median(beam_ms)), clocks=clk.summary(),
                launches=per_step * args.steps, refs=int(base[-1]), h2d=io["h2d"], d2h=io["d2h"], tree=tree,
                bundle=bundle, depth_mean=depth_mean, rows_per_read=int(sum(cand)), leaf_accuracy=leaf_acc,

@@ -255,9 +255,10 @@ int hdc_search_tc_last_shape(const hdc_context* ctx, int32_t shape[5]);
                               (cta_group::2), 1 on, 0 off, -1 automatic */
 #define HDC_TC_LANES 8     /* tensor-core search: at most this many reference lanes per query tile
                               (CTAs that split the references of one query tile); 0 automatic */
-#define HDC_BEAM_GROUPED 4 /* hdc_beam_search: 1 reads grouped by candidate node, 0 one warp
-                              per read, -1 automatic (grouped when dim % 1024 == 0 and
-                              dim <= 16384) */
+#define HDC_BEAM_GROUPED 4 /* hdc_beam_search: 1 reads grouped by candidate node, 2 the same
+                              with every level but the last scored on the tensor cores
+                              (entries grouped by parent), 0 one warp per read, -1
+                              automatic (2 when dim % 1024 == 0 and dim <= 16384, else 0) */
 int hdc_context_option(hdc_context* ctx, int option, int value);
 
 /* Hierarchical descent (config 5; targets/identify.cpp:89-202 with one

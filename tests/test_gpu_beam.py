@@ -27,8 +27,9 @@ def _drop_children(ptr, idx, nodes):
     return out_ptr, np.array([x for k in kids for x in k], np.int32)
 
 
-# grouped: 1 reads grouped by candidate node, 0 one warp per read (identical results)
-@pytest.mark.parametrize("grouped", [0, 1])
+# grouped: 1 reads grouped by candidate node, 2 the same with the levels above the last on
+# the tensor cores, 0 one warp per read (identical results)
+@pytest.mark.parametrize("grouped", [0, 1, 2])
 @pytest.mark.parametrize("dim,kmer,n_leaves,beam,threshold,childless", [
     (1024, 10, 200, 5, 0.0, False), (2048, 12, 300, 3, 0.0, False), (1024, 8, 150, 5, 0.6, False),
     (2048, 10, 300, 5, -2.0, True), (1024, 10, 200, 8, float("-inf"), True)])
@@ -97,13 +98,68 @@ def test_beam_grouped_equals_per_read(hdc, cuda):
     qn, pn = ctx.norms(q8), ctx.norms(proto)
     roots = torch.arange(0, counts[0], dtype=torch.int32, device=cuda)
     out = []
-    for grouped in (0, 1):
+    for grouped in (0, 1, 2):
         ctx.option(H.BEAM_GROUPED, grouped)
         for threshold in (0.0, float("-inf")):
             res = ctx.beam_search(q8, qn, proto, pn, torch.from_numpy(ptr).to(cuda), d_idx, roots, 6, 5, threshold)
             out.append([x.cpu().numpy() for x in res])
     torch.cuda.synchronize()
-    for a, b_ in zip(out[:2], out[2:]):
+    for a, b_ in zip(out[:2], out[2:4]):
+        for x, y in zip(a, b_):
+            assert np.array_equal(x, y)
+    for a, b_ in zip(out[:2], out[4:]):
         for x, y in zip(a, b_):
             assert np.array_equal(x, y)
     assert (out[3][2] == 6).all()  # no early stop: every read reaches a leaf
+
+
+def test_beam_tensor_core_levels_wide_nodes_and_limbs(hdc, cuda):
+    """The tensor-core levels against the CUDA-core grouped descent on a tree
+    that stresses them: 3 roots with 40 children each (items of 32 children
+    and a remainder of 8), 2 leaves per level-1 node, 300 reads (more than 128
+    entries per parent), prototype values up to 2^26 in magnitude (three
+    non-zero limbs) with rows at the limb edges, D = 1,024."""
+    import torch
+    H = hdc
+    g = np.random.default_rng(61)
+    dim, nq = 1024, 300
+    n0, n1 = 3, 3 * 40
+    n2 = 2 * n1
+    ptr = np.zeros(n0 + n1 + n2 + 1, np.int64)
+    idx = []
+    for r in range(n0):
+        idx += list(range(n0 + 40 * r, n0 + 40 * (r + 1)))
+        ptr[r + 1] = len(idx)
+    for v in range(n1):
+        idx += [n0 + n1 + 2 * v, n0 + n1 + 2 * v + 1]
+        ptr[n0 + v + 1] = len(idx)
+    ptr[n0 + n1 + 1:] = len(idx)
+    idx = np.array(idx, np.int32)
+    lim = 1 << 26
+    proto_h = g.integers(-lim, lim + 1, (n0 + n1 + n2, dim)).astype(np.int32)
+    proto_h[5, :] = lim
+    proto_h[6, :] = -lim
+    proto_h[7, ::2] = 1023
+    proto_h[7, 1::2] = -1024
+    proto_h[8, :] = 2048 * 2048 - 1
+    proto_h[9, :] = -(2048 * 2048) + 1
+    q = np.where(g.random((nq, dim)) < 0.5, -1, 1).astype(np.int8)
+    q[:40] = np.where(proto_h[n0 + 7] >= 0, 1, -1)  # many reads follow one level-1 node
+    proto = torch.from_numpy(proto_h).to(cuda)
+    q8 = torch.from_numpy(q).to(cuda)
+    ctx = H.Context(dim, 10, 250, 10)
+    qn, pn = ctx.norms(q8), ctx.norms(proto)
+    roots = torch.arange(0, n0, dtype=torch.int32, device=cuda)
+    d_ptr, d_idx = torch.from_numpy(ptr).to(cuda), torch.from_numpy(idx).to(cuda)
+    out = []
+    for grouped in (1, 2):
+        ctx.option(H.BEAM_GROUPED, grouped)
+        for beam, threshold in ((5, float("-inf")), (8, 0.0), (3, -0.5)):
+            res = ctx.beam_search(q8, qn, proto, pn, d_ptr, d_idx, roots, 3, beam, threshold)
+            out.append([x.cpu().numpy() for x in res])
+    torch.cuda.synchronize()
+    assert ctx.status() == 0
+    for a, b_ in zip(out[:3], out[3:]):
+        for x, y in zip(a, b_):
+            assert np.array_equal(x, y)
+
