@@ -62,9 +62,10 @@ CONFIGS = {
 # of work, so a run's `traffic` is that per-unit figure times its own units:
 #   tc_search_kernel, c3 (38,912 reads x 200,000 refs = 304 x 1,564 tile pairs; the
 #     288 leading query tiles in clusters of 4 + the other 16 in pairs): 1.01427e12 B
-#   grouped descent, c5 (the 6 score_kernel launches of one call, 38,912 reads):  3.76890e10 B
+#   grouped descent, c5 (one call's 5 descent_tc_kernel launches + the leaf-level score_kernel,
+#     38,912 reads): 3.64798e10 B
 TRAFFIC_PER_TILE_PAIR_TC = (975.445256e9 + 0.170780e9 + 38.640838e9 + 0.012020e9) / (304 * 1564)
-TRAFFIC_DESCENT = {38912: 37.593492e9 + 95.516928e6}  # reads per call -> bytes (mostly the database, once)
+TRAFFIC_DESCENT = {38912: 36.409726e9 + 70.093e6}  # reads per call -> bytes (mostly the database, once)
 
 
 def log(*a):
@@ -687,13 +688,16 @@ def descent_line(args, cfg, r, metric, workload, world):
                 "d2h_bytes_per_step": r["d2h"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / pk["hbm_gbs"], "traffic": TRAFFIC_DESCENT.get(B),
-                     "traffic_source": "ncu DRAM bytes of the score launches of one full-size call "
-                                       "(measured at 38,912 reads; null at other batch sizes)",
+                     "traffic_source": "ncu DRAM bytes of the scoring launches of one full-size call "
+                                       "(descent_tc_kernel x 5 + score_kernel; measured at 38,912 reads; "
+                                       "null at other batch sizes)",
                      "peak_source": "%s HBM copy bandwidth (MEASURED_PEAKS.json)" % src,
-                     "kernel": "grouped descent (hdc_beam_search: count/expand/scan/scatter, score_kernel, "
-                               "select per level), timed as one call; algorithmic bytes = the %.1f GB of "
-                               "prototypes once + %d levels of packed reads; it is issue-bound on the "
-                               "+p/-p integer sums (%d candidate rows per read), not HBM-bound" % (
+                     "kernel": "grouped descent (hdc_beam_search: per level count/expand/select; levels "
+                               "above the leaves scored by descent_tc_kernel on the tensor cores, the "
+                               "leaves by score_kernel), timed as one call; algorithmic bytes = the %.1f GB "
+                               "of prototypes once + %d levels of packed reads; the tensor-core levels are "
+                               "bound by their producers' conversions, the leaf level by HBM "
+                               "(%d candidate rows per read)" % (
                                    r["refs"] * dim * 4 / 1e9, cfg["levels"], r["rows_per_read"])},
         "propagate_bundle": {"kernel": "bundle_kernel (internal prototypes = int32 sums of children)",
                              "ms": bundle_ms, "gb_per_s": bundle_bytes / (bundle_ms / 1e3) / 1e9,
