@@ -120,7 +120,7 @@ int hdc_encode_segments(hdc_context* ctx, const char* d_bytes, const int64_t* d_
     if (n_segs < 0) return fail(HDC_ERR_INVALID, "encode: negative segment count");
     if (n_segs == 0) return HDC_OK;
     if (!d_bytes || !d_seg_off || !d_seg_len || !d_out) return fail(HDC_ERR_INVALID, "encode: null pointer");
-    if (out_kind < HDC_OUT_I16 || out_kind > HDC_OUT_BIPOLAR_I8) return fail(HDC_ERR_INVALID, "encode: bad out_kind");
+    if (out_kind < HDC_OUT_I16 || out_kind > HDC_OUT_F16) return fail(HDC_ERR_INVALID, "encode: bad out_kind");
     if (out_stride < ctx->dim) return fail(HDC_ERR_INVALID, "encode: out_stride < dim");
     if (max_len < 0) return fail(HDC_ERR_INVALID, "encode: negative max_len");
     return hdc::launch_encode(ctx, d_bytes, d_seg_off, d_seg_len, nullptr, nullptr, 0, n_segs, out_kind, d_out,
@@ -140,6 +140,12 @@ int hdc_encode_windows(hdc_context* ctx, const char* d_bytes, const int64_t* d_s
     if (!d_bytes || !d_seq_off || !d_win_off || !d_out) return fail(HDC_ERR_INVALID, "encode_windows: null pointer");
     return hdc::launch_encode(ctx, d_bytes, nullptr, nullptr, d_seq_off, d_win_off, n_seqs, n_windows, HDC_OUT_I16,
                               d_out, ctx->dim, nullptr, ctx->window, static_cast<cudaStream_t>(stream));
+}
+
+int hdc_norms_f16(hdc_context* ctx, const void* d_hv, int64_t n, int64_t* d_norm2, int32_t* d_maxabs, void* stream) {
+    if (!ctx || (!d_hv && n) || (!d_norm2 && n)) return fail(HDC_ERR_INVALID, "norms: null pointer");
+    if (n < 0) return fail(HDC_ERR_INVALID, "norms: negative count");
+    return hdc::launch_norms(ctx, d_hv, hdc::kNormsF16, n, d_norm2, d_maxabs, static_cast<cudaStream_t>(stream));
 }
 
 int hdc_norms(hdc_context* ctx, const void* d_hv, int elem_bytes, int64_t n, int64_t* d_norm2, int32_t* d_maxabs,
@@ -187,8 +193,23 @@ int hdc_refdb_create(hdc_context* ctx, const void* d_ref, int elem_bytes, int64_
     if (elem_bytes != 2 && elem_bytes != 4) return fail(HDC_ERR_INVALID, "refdb: elem_bytes must be 2 or 4");
     if (nr < 1 || !d_ref) return fail(HDC_ERR_INVALID, "refdb: empty reference set");
     if (max_abs < 0) return fail(HDC_ERR_INVALID, "refdb: negative max_abs");
-    return hdc::refdb_create(ctx, d_ref, elem_bytes, nr, max_abs, out, static_cast<cudaStream_t>(stream));
+    return hdc::refdb_create(ctx, d_ref, elem_bytes, nr, max_abs, 0, out, static_cast<cudaStream_t>(stream));
 }
+
+int hdc_refdb_create_ex(hdc_context* ctx, const void* d_ref, int elem_bytes, int64_t nr, int32_t max_abs,
+                        int32_t max_query_abs, hdc_refdb** out, void* stream) {
+    if (!ctx || !out) return fail(HDC_ERR_INVALID, "refdb: null argument");
+    *out = nullptr;
+    if (elem_bytes != 2 && elem_bytes != 4) return fail(HDC_ERR_INVALID, "refdb: elem_bytes must be 2 or 4");
+    if (nr < 1 || !d_ref) return fail(HDC_ERR_INVALID, "refdb: empty reference set");
+    if (max_abs < 0) return fail(HDC_ERR_INVALID, "refdb: negative max_abs");
+    if (max_query_abs < 1 || max_query_abs > 2048)
+        return fail(HDC_ERR_RANGE, "refdb: max_query_abs must be in 1..2048 (exact fp16 queries)");
+    return hdc::refdb_create(ctx, d_ref, elem_bytes, nr, max_abs, max_query_abs, out,
+                             static_cast<cudaStream_t>(stream));
+}
+
+int hdc_refdb_limb_bits(const hdc_refdb* db) { return db ? db->limb_bits : 0; }
 
 void hdc_refdb_destroy(hdc_refdb* db) { hdc::refdb_destroy(db); }
 

@@ -316,6 +316,8 @@ __global__ void __launch_bounds__(kThreads) encode_kernel(const EncodeArgs a) {
                         h2[t] = v >= 0 ? 0x0001u : 0xffffu;
                     else if (a.out_kind == HDC_OUT_BIPOLAR_F16)
                         h2[t] = v >= 0 ? 0x3c00u : 0xbc00u;  // fp16 +1 / -1
+                    else if (a.out_kind == HDC_OUT_F16)
+                        h2[t] = __half_as_ushort(__int2half_rn(v));  // exact: |v| <= 2048
                     else
                         h2[t] = v >= 0 ? 0x3f80u : 0xbf80u;  // bf16 +1 / -1
                 }
@@ -406,6 +408,8 @@ int launch_encode(hdc_context* ctx, const char* d_bytes, const int64_t* d_seg_of
         nh = 12;  // counts modulo 2^16
     if (out_kind != HDC_OUT_I16 && max_nk > 65535)
         return fail(HDC_ERR_RANGE, "encode: segments longer than 65535 k-mers need HDC_OUT_I16 (counts wrap)");
+    if (out_kind == HDC_OUT_F16 && max_nk > 2048)
+        return fail(HDC_ERR_RANGE, "encode: fp16 counts are exact for segments of at most 2048 k-mers");
 
     const int n_slabs = (a.W32 + 31) / 32;
     const size_t smem = (size_t)a.table_rows * 32 * 4 + (size_t)kWarps * kChunk * 8;

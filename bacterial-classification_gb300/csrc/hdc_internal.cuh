@@ -47,6 +47,7 @@ struct hdc_refdb {
     float* d_rsq = nullptr;     // [nr]
     double* d_sqrt = nullptr;   // [nr] sqrt(norm2) rounded to double (the exact score's factor)
     int32_t limb_max[4] = {0, 0, 0, 0};
+    int limb_bits = 11;         // limbs are balanced base-2^limb_bits digits (the top one within the cap)
     int32_t max_abs = 0;
 };
 
@@ -81,7 +82,11 @@ int launch_merge(const uint64_t* ws_key, const int64_t* ws_dot, int n_lists, int
                  const int64_t* d_rn, float* d_score, int32_t* d_idx, double* d_cos, int64_t* d_dot,
                  cudaStream_t stream);
 
-int refdb_create(hdc_context* ctx, const void* d_ref, int elem_bytes, int64_t nr, int32_t max_abs, hdc_refdb** out,
+// launch_norms element code of integer-valued fp16 rows (1, 2, 4: int8 / int16 / int32)
+constexpr int kNormsF16 = -2;
+
+int refdb_create(hdc_context* ctx, const void* d_ref, int elem_bytes, int64_t nr, int32_t max_abs,
+                 int32_t max_query_abs, hdc_refdb** out,
                  cudaStream_t stream);
 void refdb_destroy(hdc_refdb* db);
 size_t tc_workspace_bytes(const hdc_context* ctx, int64_t nq, const hdc_refdb* db, int k);

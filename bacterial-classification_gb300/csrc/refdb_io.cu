@@ -24,7 +24,7 @@ struct FileHeader {
     int32_t dim, kmer, window, step, limbs, max_abs;
     int32_t limb_max[4];
     int64_t nr, r_pad;
-    uint32_t has_ids, reserved;
+    uint32_t has_ids, limb_bits;  // limb_bits 0: 11 (files written before the field)
     uint64_t payload_bytes, payload_fnv;
     uint8_t pad[128 - 8 - 8 - 24 - 16 - 16 - 8 - 16];
 };
@@ -99,6 +99,7 @@ int read_header(FILE* f, FileHeader& h) {
     if (h.version != kVersion || h.header_bytes != sizeof h)
         return hdc::fail(HDC_ERR_INVALID, "refdb file: unsupported version");
     if (h.dim < 8 || h.dim % 8 || h.limbs < 1 || h.limbs > 4 || h.nr < 1 || h.r_pad < h.nr || h.r_pad % 256 ||
+        h.limb_bits > 11 ||
         h.payload_bytes != payload_bytes(h))
         return hdc::fail(HDC_ERR_INVALID, "refdb file: inconsistent header");
     return HDC_OK;
@@ -126,6 +127,7 @@ int hdc_refdb_save(hdc_context* ctx, const hdc_refdb* db, const char* path, cons
     h.nr = db->nr;
     h.r_pad = db->r_pad;
     h.has_ids = h_tax_ids ? 1 : 0;
+    h.limb_bits = db->limb_bits == 11 ? 0u : (uint32_t)db->limb_bits;
     h.payload_bytes = payload_bytes(h);
     // the checksum goes into the header: write the payload after a placeholder header, then rewrite it
     File out;
@@ -186,6 +188,7 @@ int hdc_refdb_load(hdc_context* ctx, const char* path, hdc_refdb** out, int32_t*
     db->r_pad = h.r_pad;
     db->dim = h.dim;
     db->L = h.limbs;
+    db->limb_bits = h.limb_bits ? (int)h.limb_bits : 11;
     db->max_abs = h.max_abs;
     for (int l = 0; l < 4; ++l) db->limb_max[l] = h.limb_max[l];
     cudaError_t e = cudaMalloc(&db->d_limbs, limb_bytes(h));

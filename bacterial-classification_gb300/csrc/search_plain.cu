@@ -38,6 +38,11 @@ constexpr int kBR = 128;        // references per CTA tile
 constexpr int kMaxK = 32;       // largest top-k
 
 // ---------------------------------------------------------------- norms
+__device__ __forceinline__ int64_t as_i64(int8_t x) { return x; }
+__device__ __forceinline__ int64_t as_i64(int16_t x) { return x; }
+__device__ __forceinline__ int64_t as_i64(int32_t x) { return x; }
+__device__ __forceinline__ int64_t as_i64(__half x) { return (int64_t)__half2int_rn(x); }  // integer-valued fp16
+
 template <typename T>
 __global__ void norms_kernel(const T* __restrict__ v, int64_t n, int dim, int64_t* __restrict__ norm2,
                              int32_t* __restrict__ maxabs) {
@@ -48,7 +53,7 @@ __global__ void norms_kernel(const T* __restrict__ v, int64_t n, int dim, int64_
     int64_t s = 0;
     int32_t m = 0;
     for (int d = lane; d < dim; d += 32) {
-        const int64_t x = p[d];
+        const int64_t x = as_i64(p[d]);
         s += x * x;
         m = max(m, (int32_t)(x < 0 ? -x : x));
     }
@@ -362,6 +367,9 @@ int launch_norms(hdc_context* ctx, const void* d_hv, int elem_bytes, int64_t n, 
     else if (elem_bytes == 2)
         norms_kernel<int16_t><<<(unsigned)grid, 256, 0, stream>>>(static_cast<const int16_t*>(d_hv), n, ctx->dim,
                                                                    d_norm2, d_maxabs);
+    else if (elem_bytes == kNormsF16)
+        norms_kernel<__half><<<(unsigned)grid, 256, 0, stream>>>(static_cast<const __half*>(d_hv), n, ctx->dim,
+                                                                  d_norm2, d_maxabs);
     else
         norms_kernel<int32_t><<<(unsigned)grid, 256, 0, stream>>>(static_cast<const int32_t*>(d_hv), n, ctx->dim,
                                                                    d_norm2, d_maxabs);

@@ -103,6 +103,8 @@ struct TcArgs {
     // zeroed before the launch; null when the lanes do not exchange them
     uint32_t* lane_kth;
     int slist;  // 1: the top-k lists live in shared memory after the tile ring, else in local memory
+    int limb_bits;     // the database's limbs are base-2^limb_bits digits
+    float limb_base;   // 2^limb_bits
 };
 
 // Insert (key, dot) into a descending list of length k whose entry i is at keys[i * st].
@@ -527,7 +529,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                             float scale = 1.0f;
 #pragma unroll
                             for (int l = 1; l < L; ++l) {
-                                scale *= 2048.0f;
+                                scale *= a.limb_base;
                                 af = fmaf(__uint_as_float(v[l][c]), scale, af);
                             }
                             const float ap = approx_tc(af, my_rq[m], rrc, a.mode);
@@ -538,7 +540,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                             int64_t dot = 0;
 #pragma unroll
                             for (int l = 0; l < L; ++l)
-                                dot += (int64_t)__float2ll_rn(__uint_as_float(v[l][c])) * ((int64_t)1 << (11 * l));
+                                dot += (int64_t)__float2ll_rn(__uint_as_float(v[l][c])) * ((int64_t)1 << (a.limb_bits * l));
                             const int64_t gr = rbase + c;
                             const float s = exact_score_sqrt(dot, my_sq[m], rsc, a.mode);
                             const uint64_t key = make_key(s, (uint32_t)gr);
@@ -621,8 +623,9 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
 // ---------------------------------------------------------------- database build
 // limbs[l][r][d] (fp16) of ref[r][d]; rows r >= nr of each limb are zero.
 template <typename T>
-__global__ void limbs_kernel(const T* __restrict__ ref, int64_t nr, int dim, int L, int64_t r_pad,
+__global__ void limbs_kernel(const T* __restrict__ ref, int64_t nr, int dim, int L, int bits, int64_t r_pad,
                              __half* __restrict__ limbs, int32_t* __restrict__ limb_max) {
+    const int64_t base = (int64_t)1 << bits, half = base >> 1;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t total = r_pad * dim;
     int32_t mx[kMaxLimbs] = {0, 0, 0, 0};
@@ -634,8 +637,8 @@ __global__ void limbs_kernel(const T* __restrict__ ref, int64_t nr, int dim, int
             if (l == L - 1) {
                 digit = v;
             } else {
-                digit = ((v + 1024) & 2047) - 1024;
-                v = (v - digit) / 2048;
+                digit = ((v + half) & (base - 1)) - half;
+                v = (v - digit) / base;
             }
             limbs[(int64_t)l * total + i] = __int2half_rn((int)digit);
             mx[l] = (int32_t)(digit < 0 ? -digit : digit);
@@ -695,23 +698,36 @@ bool make_tmap(CUtensorMap* map, const void* base, int64_t rows, int dim, int bk
 }  // namespace
 
 int refdb_create(hdc_context* ctx, const void* d_ref, int elem_bytes, int64_t nr, int32_t max_abs,
-                 hdc_refdb** out, cudaStream_t stream) {
+                 int32_t max_query_abs, hdc_refdb** out, cudaStream_t stream) {
     *out = nullptr;
     const int dim = ctx->dim;
     if (dim % 8 != 0) return fail(HDC_ERR_INVALID, "refdb: dim must be a multiple of 8 (TMA row stride)");
     if (nr < 1) return fail(HDC_ERR_INVALID, "refdb: empty reference set");
-    // limbs needed for |v| <= max_abs: L-1 balanced digits of 11 bits, then a top digit within 2048
+    // Limb magnitude cap T: every limb is an exact fp16 (<= 2048), and with queries up to
+    // max_query_abs every fp32 partial sum stays an exact integer (dim * max|q| * T <= 2^24).
+    // The base is the largest power of two whose balanced digits stay within T.
+    int bits = 11;
+    int64_t cap = 2048;
+    if (max_query_abs > 0) {
+        cap = std::min<int64_t>(2048, ((int64_t)1 << 24) / ((int64_t)dim * max_query_abs));
+        if (cap < 1) return fail(HDC_ERR_RANGE, "refdb: dim * max query magnitude exceeds 2^24 (fp32 inexact)");
+        bits = 1;
+        while (bits < 11 && ((int64_t)1 << bits) <= cap) ++bits;  // 2^(bits-1) <= cap
+    }
+    // limbs needed for |v| <= max_abs: L-1 balanced base-2^bits digits, then a top digit
+    // within the cap (cover_L = cover_{L-1} * base + base/2 - 1 bounds every digit by the cap)
     int L = 1;
-    int64_t cover = 2048;
+    int64_t cover = cap;
     while ((int64_t)max_abs > cover) {
         ++L;
-        cover = cover * 2048 + 1023;
+        cover = cover * ((int64_t)1 << bits) + ((int64_t)1 << (bits - 1)) - 1;
         if (L > kMaxLimbs) return fail(HDC_ERR_RANGE, "refdb: values need more than 4 limbs");
     }
     auto* db = new hdc_refdb();
     db->nr = nr;
     db->dim = dim;
     db->L = L;
+    db->limb_bits = bits;
     db->max_abs = max_abs;
     db->r_pad = (nr + kRowPad - 1) / kRowPad * kRowPad;
     const size_t nl = (size_t)L * db->r_pad * dim;
@@ -732,10 +748,10 @@ int refdb_create(hdc_context* ctx, const void* d_ref, int elem_bytes, int64_t nr
     const int64_t total = db->r_pad * dim;
     const unsigned grid = (unsigned)((total + 255) / 256);
     if (elem_bytes == 2)
-        limbs_kernel<int16_t><<<grid, 256, 0, stream>>>(static_cast<const int16_t*>(d_ref), nr, dim, L, db->r_pad,
+        limbs_kernel<int16_t><<<grid, 256, 0, stream>>>(static_cast<const int16_t*>(d_ref), nr, dim, L, bits, db->r_pad,
                                                         db->d_limbs, d_lmax);
     else
-        limbs_kernel<int32_t><<<grid, 256, 0, stream>>>(static_cast<const int32_t*>(d_ref), nr, dim, L, db->r_pad,
+        limbs_kernel<int32_t><<<grid, 256, 0, stream>>>(static_cast<const int32_t*>(d_ref), nr, dim, L, bits, db->r_pad,
                                                         db->d_limbs, d_lmax);
     int st = launch_norms(ctx, d_ref, elem_bytes, nr, db->d_norm2, nullptr, stream);
     if (st == HDC_OK) {
@@ -1014,6 +1030,8 @@ static int search_part(hdc_context* ctx, const hdc_refdb* db, const __half* d_q,
         if (e != cudaSuccess) return cuda_fail(e, "tc search: clear lane thresholds");
     }
     a.rs = db->d_sqrt;
+    a.limb_bits = db->limb_bits;
+    a.limb_base = (float)(1 << db->limb_bits);
     a.status = d_status;
     a.policy = ctx->tc_policy >= 0 ? ctx->tc_policy : tc_default_policy();
     a.prefetch = ctx->tc_prefetch >= 0 ? ctx->tc_prefetch : tc_default_prefetch();

@@ -16,7 +16,7 @@ ERR = {1: "HDC_ERR_INVALID", 2: "HDC_ERR_RANGE", 3: "HDC_ERR_CUDA", 4: "HDC_ERR_
        5: "HDC_ERR_UNSUPPORTED", 6: "HDC_ERR_TIMEOUT"}
 SCORE_NORM, SCORE_COS, SCORE_DOT = 0, 1, 2
 TC_PREFETCH, TC_CLUSTER, TC_SHARE, BEAM_GROUPED, TC_SCATTER, TC_KBLOCK, TC_PAIR_MMA, TC_LANES = 1, 2, 3, 4, 5, 6, 7, 8
-OUT_I16, OUT_I32, OUT_BIPOLAR_BF16, OUT_BIPOLAR_I16, OUT_BIPOLAR_F16, OUT_BIPOLAR_I8 = 0, 1, 2, 3, 4, 5
+OUT_I16, OUT_I32, OUT_BIPOLAR_BF16, OUT_BIPOLAR_I16, OUT_BIPOLAR_F16, OUT_BIPOLAR_I8, OUT_F16 = 0, 1, 2, 3, 4, 5, 6
 
 # (name, restype, argtypes) of every exported entry point
 P, I32, I64, SZ = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_size_t
@@ -48,6 +48,9 @@ SIGNATURES = [
     ("hdc_refdb_create", I32, [P, P, I32, I64, ctypes.c_int32, ctypes.POINTER(P), P]),
     ("hdc_refdb_destroy", None, [P]),
     ("hdc_refdb_limbs", I32, [P]),
+    ("hdc_norms_f16", I32, [P, P, I64, P, P, P]),
+    ("hdc_refdb_create_ex", I32, [P, P, I32, I64, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(P), P]),
+    ("hdc_refdb_limb_bits", I32, [P]),
     ("hdc_search_tc_workspace_bytes", SZ, [P, P, I64, I32]),
     ("hdc_refdb_save", I32, [P, P, ctypes.c_char_p, P]),
     ("hdc_refdb_file_info", I32, [ctypes.c_char_p, P, P, P, P, P]),
@@ -154,8 +157,11 @@ class Context:
     def norms(self, hv, maxabs=None, stream=None):
         import torch
         n2 = torch.empty(hv.shape[0], dtype=torch.int64, device=hv.device)
-        check(lib().hdc_norms(self.h, ptr(hv), hv.element_size(), hv.shape[0], ptr(n2), ptr(maxabs),
-                              stream_ptr(stream)))
+        if hv.dtype == torch.float16:  # integer-valued fp16 rows
+            check(lib().hdc_norms_f16(self.h, ptr(hv), hv.shape[0], ptr(n2), ptr(maxabs), stream_ptr(stream)))
+        else:
+            check(lib().hdc_norms(self.h, ptr(hv), hv.element_size(), hv.shape[0], ptr(n2), ptr(maxabs),
+                                  stream_ptr(stream)))
         return n2
 
     def workspace_bytes(self, nq, nr, k):
@@ -199,8 +205,8 @@ class Context:
         check(lib().hdc_search_tc_last_shape(self.h, ctypes.addressof(out)))
         return tuple(out)
 
-    def refdb(self, refs, max_abs, stream=None):
-        return RefDB(self, refs, max_abs, stream)
+    def refdb(self, refs, max_abs, stream=None, max_query_abs=0):
+        return RefDB(self, refs, max_abs, stream, max_query_abs=max_query_abs)
 
     def search_tc(self, db, q, qn, maxq, k, mode=SCORE_NORM, work=None, out=None, stream=None):
         import torch
@@ -306,16 +312,21 @@ class RefDB:
     """Tensor-core reference database (fp16 limbs + exact norms) built from int16/int32 rows,
     or loaded from a file written by save()."""
 
-    def __init__(self, ctx, refs, max_abs, stream=None, _handle=None, _nr=0):
+    def __init__(self, ctx, refs, max_abs, stream=None, _handle=None, _nr=0, max_query_abs=0):
         h = ctypes.c_void_p()
         if _handle is None:
-            check(lib().hdc_refdb_create(ctx.h, ptr(refs), refs.element_size(), refs.shape[0], int(max_abs),
-                                         ctypes.byref(h), stream_ptr(stream)))
+            if max_query_abs:  # limbs sized for count-valued queries up to max_query_abs
+                check(lib().hdc_refdb_create_ex(ctx.h, ptr(refs), refs.element_size(), refs.shape[0], int(max_abs),
+                                                int(max_query_abs), ctypes.byref(h), stream_ptr(stream)))
+            else:
+                check(lib().hdc_refdb_create(ctx.h, ptr(refs), refs.element_size(), refs.shape[0], int(max_abs),
+                                             ctypes.byref(h), stream_ptr(stream)))
             _nr = refs.shape[0]
         else:
             h = _handle
         self.h, self.nr, self.ctx = h, _nr, ctx
         self.limbs = lib().hdc_refdb_limbs(h)
+        self.limb_bits = lib().hdc_refdb_limb_bits(h)
 
     def save(self, path, tax_ids=None):
         """Write the database (and optional int32 taxonomy ids, one per reference) to `path`."""

@@ -55,6 +55,8 @@ extern "C" {
 #define HDC_OUT_BIPOLAR_I16 3  /* int16 +1/-1 sign of the bundle, 0 -> +1 */
 #define HDC_OUT_BIPOLAR_F16 4  /* fp16 +1/-1 sign of the bundle, 0 -> +1 (tensor-core queries) */
 #define HDC_OUT_BIPOLAR_I8 5   /* int8 +1/-1 sign of the bundle, 0 -> +1 (hierarchical descent reads) */
+#define HDC_OUT_F16 6          /* fp16 bundle, exact (segments of <= 2048 k-mers): count-valued
+                                  tensor-core queries */
 
 typedef struct hdc_context hdc_context;
 typedef struct hdc_refdb hdc_refdb;
@@ -114,6 +116,8 @@ int hdc_encode_windows(hdc_context* ctx, const char* d_bytes, const int64_t* d_s
  * int16 (elem_bytes 2) or int32 (elem_bytes 4) hypervectors, row stride dim. */
 int hdc_norms(hdc_context* ctx, const void* d_hv, int elem_bytes, int64_t n, int64_t* d_norm2,
               int32_t* d_maxabs, void* stream);
+/* The same for integer-valued fp16 rows (HDC_OUT_F16 / HDC_OUT_BIPOLAR_F16 queries). */
+int hdc_norms_f16(hdc_context* ctx, const void* d_hv, int64_t n, int64_t* d_norm2, int32_t* d_maxabs, void* stream);
 
 /* Workspace the plain search needs for nq queries and top-k. */
 size_t hdc_search_workspace_bytes(const hdc_context* ctx, int64_t nq, int64_t nr, int k);
@@ -149,8 +153,17 @@ int hdc_context_status(hdc_context* ctx, int* status);
  * 512-533). */
 int hdc_refdb_create(hdc_context* ctx, const void* d_ref, int elem_bytes, int64_t nr, int32_t max_abs,
                      hdc_refdb** out, void* stream);
+/* The same for queries of magnitude up to max_query_abs (1..2048; count-valued
+ * queries, e.g. HDC_OUT_F16 reads): the limbs become balanced base-2^b digits
+ * with every limb within T = min(2048, 2^24 / (dim * max_query_abs)) (b the
+ * largest with 2^(b-1) <= T, at most 11), so that every fp32 partial sum of a
+ * search with such queries is an exact integer.  max_query_abs = 1 (+1/-1
+ * queries) gives the base-2048 limbs of hdc_refdb_create up to dim 16384. */
+int hdc_refdb_create_ex(hdc_context* ctx, const void* d_ref, int elem_bytes, int64_t nr, int32_t max_abs,
+                        int32_t max_query_abs, hdc_refdb** out, void* stream);
 void hdc_refdb_destroy(hdc_refdb* db);
 int hdc_refdb_limbs(const hdc_refdb* db);
+int hdc_refdb_limb_bits(const hdc_refdb* db);
 
 /* Persisted database (no reference counterpart: the reference re-encodes its
  * FASTA files on every run).  hdc_refdb_save writes the limbs, exact norms

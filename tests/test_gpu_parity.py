@@ -32,7 +32,8 @@ def upload(seqs, dev):
 def gpu_encode(ctx, seqs, dev, kind=0, max_len=None):
     import torch
     b, o, l, mx = upload(seqs, dev)
-    dt = {0: torch.int16, 1: torch.int32, 2: torch.bfloat16, 3: torch.int16, 4: torch.float16, 5: torch.int8}[kind]
+    dt = {0: torch.int16, 1: torch.int32, 2: torch.bfloat16, 3: torch.int16, 4: torch.float16, 5: torch.int8,
+          6: torch.float16}[kind]
     out = torch.full((len(seqs), ctx.dim), 7, dtype=dt, device=dev)
     nk = torch.zeros(len(seqs), dtype=torch.int32, device=dev)
     ctx.encode_segments(b, o, l, out, kind, mx if max_len is None else max_len, nk)
@@ -105,6 +106,12 @@ def test_encode_random_all_kinds(hdc, orc, cuda, dim, k):
     assert np.array_equal(outh.float().numpy(), bip.astype(np.float32))
     out8, _ = gpu_encode(ctx, sub, cuda, 5)
     assert np.array_equal(out8.numpy(), bip)
+    # fp16 counts (exact): segments up to 2048 k-mers; longer ones are refused
+    f16 = [i for i, s in enumerate(seqs) if len(s) - k + 1 <= 2048]
+    outf, _ = gpu_encode(ctx, [seqs[i] for i in f16], cuda, 6)
+    assert np.array_equal(outf.float().numpy(), ref32[f16].astype(np.float32))
+    with pytest.raises(hdc.HDCError):
+        gpu_encode(ctx, [seqs[i] for i in range(len(seqs)) if len(seqs[i]) - k + 1 > 2048][:1], cuda, 6)
 
 
 def test_search_rejects_inexact_range(hdc, cuda):

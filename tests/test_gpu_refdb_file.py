@@ -64,3 +64,27 @@ def test_load_rejects_bad_files(hdc, cuda, tmp_path):
     other = hdc.Context(1024, 12, 250, 10)
     with pytest.raises(RuntimeError, match="k-mer"):
         hdc.RefDB.load(other, path)
+
+
+def test_save_load_keeps_limb_base(hdc, cuda, tmp_path):
+    """A database sized for count-valued queries (base-64 limbs) survives the
+    file round trip: same limbs, same limb base, identical search results."""
+    import torch
+    g = np.random.default_rng(9)
+    dim, nr, nq = 1024, 500, 60
+    refs = g.integers(-30000, 30001, (nr, dim)).astype(np.int16)
+    q = g.integers(-300, 301, (nq, dim)).astype(np.int16)
+    ctx = hdc.Context(dim, 10, 250, 10)
+    db = ctx.refdb(torch.from_numpy(refs).to(cuda), 30000, max_query_abs=300)
+    q16 = torch.from_numpy(q.astype(np.float16)).to(cuda)
+    qn = ctx.norms(torch.from_numpy(q).to(cuda))
+    path = tmp_path / "counts.hdcdb"
+    db.save(path)
+    db2, _ = hdc.RefDB.load(ctx, path)
+    assert (db2.limbs, db2.limb_bits) == (db.limbs, db.limb_bits) and db.limb_bits < 11
+    a = ctx.search_tc(db, q16, qn, 300, 5)
+    b = ctx.search_tc(db2, q16, qn, 300, 5)
+    torch.cuda.synchronize()
+    for x, y in zip(a, b):
+        assert torch.equal(x, y)
+

@@ -331,3 +331,37 @@ def test_tc_quad_split_vs_pairs_and_oracle(hdc, orc, cuda):
         assert np.array_equal(d[rows], od)
         assert np.array_equal(s[rows], os_)
         assert np.array_equal(c[rows], oc)
+
+
+# Count-valued queries (e.g. fp16 k-mer counts of reads): the database's limbs are sized for
+# the largest query magnitude (hdc_refdb_create_ex), every fp32 partial sum stays exact.
+@pytest.mark.parametrize("dim,nq,nr,k,mode,qmax,vmax,dtype,bits,limbs", [
+    (2048, 140, 3000, 5, 0, 200, 30000, np.int16, 6, 3),     # base 64
+    (1024, 100, 900, 10, 1, 2048, 1600, np.int16, 4, 3),     # base 16: |q| up to 2048
+    (1056, 200, 700, 1, 2, 143, 1000000, np.int32, 7, 3),    # base 128, int32 references
+])
+def test_tc_count_queries_vs_oracle(hdc, orc, cuda, dim, nq, nr, k, mode, qmax, vmax, dtype, bits, limbs):
+    import torch
+    g = np.random.default_rng(dim + qmax)
+    refs = g.integers(-vmax, vmax + 1, (nr, dim)).astype(dtype)
+    refs[3] = refs[1]
+    refs[5, :] = vmax
+    refs[6, ::2] = -vmax
+    q = g.integers(-qmax, qmax + 1, (nq, dim)).astype(np.int16)
+    q[0, :] = qmax
+    q[1] = np.where(refs[1] >= 0, qmax, -qmax)
+    ctx = hdc.Context(dim, 10, 250, 10)
+    tr = torch.from_numpy(refs).to(cuda)
+    db = ctx.refdb(tr, int(np.abs(refs).max()), max_query_abs=qmax)
+    assert (db.limb_bits, db.limbs) == (bits, limbs)
+    q16 = torch.from_numpy(q.astype(np.float16)).to(cuda)
+    qn = ctx.norms(q16)  # integer-valued fp16 rows (hdc_norms_f16)
+    assert torch.equal(qn, ctx.norms(torch.from_numpy(q).to(cuda)))
+    for cluster, pair in ((0, -1), (2, 0)):
+        s, i, c, d = _run_tc(ctx, db, q16, qn, qmax, k, mode, cluster=cluster, pair=pair)
+        os_, oi, oc, od = orc.topk(q.astype(np.int32), refs.astype(np.int32), min(k, nr), mode)
+        assert np.array_equal(i, oi)
+        assert np.array_equal(d, od)
+        assert np.array_equal(s, os_)
+        assert np.array_equal(c, oc)
+
