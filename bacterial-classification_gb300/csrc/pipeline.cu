@@ -263,8 +263,10 @@ int hdc_pipeline_autotune(hdc_pipeline* p, int* best_group, int* best_policy, in
     struct Cand {
         int g, pol, n, mb;
     };
-    std::vector<Cand> cands = {{sms, 0, 128, 1}, {sms, 1, 128, 1}, {sms / 2, 0, 128, 1}, {sms / 4, 0, 128, 1},
-                               {sms, 0, 128, 2}, {sms, 0, 256, 1}, {16, 1, 128, 1}, {8, 1, 128, 1}};
+    // the library's automatic schedule first (group, L2 policy, tile and M-blocks left to the search)
+    std::vector<Cand> cands = {{0, -1, 0, 0},       {sms, 0, 128, 1}, {sms, 1, 128, 1}, {sms / 2, 0, 128, 1},
+                               {sms / 4, 0, 128, 1}, {sms, 0, 128, 2}, {sms, 0, 256, 1}, {16, 1, 128, 1},
+                               {8, 1, 128, 1}};
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
