@@ -376,11 +376,15 @@ struct TcItems {
     int32_t* par_cnt;     // [n_nodes] entries per parent
     int32_t* par_off;     // [n_nodes + 1]
     int32_t* par_cursor;  // [n_nodes]
-    int32_t* item_cnt;    // [n_nodes]
-    int32_t* item_off;    // [n_nodes + 1]; item_off[n_nodes] = number of items of the level
-    int32_t* item_par;    // [items] parent (-1: level 0)
-    int32_t* item_e0;     // first entry of the item among its parent's
-    int32_t* item_j0;     // first child
+    int32_t* item_cnt;    // [n_nodes] items of a parent of its own
+    int32_t* item_off;    // [n_nodes + 1]; item_off[n_nodes] = number of such items of the level
+    int32_t* small;       // [n_nodes] 1: the parent shares an item (<= 64 entries, <= 16 children)
+    int32_t* small_off;   // [n_nodes + 1]; small_off[n_nodes] = number of such parents
+    // item i: parent, first entry, first child (-1 parent: level 0); an item shared by two
+    // parents (after the others) has item_e0 = -1, parent item_par and second parent item_j0 (or -1)
+    int32_t* item_par;
+    int32_t* item_e0;
+    int32_t* item_j0;
     int* status;          // context status word: 100 + code of a wait that gave up
 };
 
@@ -416,16 +420,34 @@ __global__ void par_scatter_kernel(const GArgs a, TcItems t, int L) {
     }
 }
 
+// A parent with at most 64 entries and 16 children shares an item with another such parent
+// (entries in rows 0-63 / 64-127, children in slots 0-15 / 16-31): the K loop of an item costs
+// the same whatever its fill, and most parents of the lower levels are that small.
+constexpr int kTcHalfE = kTcE / 2, kTcHalfC = kTcC / 2;
+
 __global__ void item_count_kernel(const GArgs a, TcItems t) {
     const int64_t P = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (P >= a.n_nodes) return;
-    const int32_t m = t.par_cnt[P];
-    t.item_cnt[P] = m ? ((m + kTcE - 1) / kTcE) * ((n_children(a, (int32_t)P) + kTcC - 1) / kTcC) : 0;
+    const int32_t m = t.par_cnt[P], nch = n_children(a, (int32_t)P);
+    const bool small = m > 0 && m <= kTcHalfE && nch <= kTcHalfC;
+    t.small[P] = small ? 1 : 0;
+    t.item_cnt[P] = m && !small ? ((m + kTcE - 1) / kTcE) * ((nch + kTcC - 1) / kTcC) : 0;
 }
 
 __global__ void item_write_kernel(const GArgs a, TcItems t) {
     const int64_t P = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (P >= a.n_nodes) return;
+    if (t.small[P]) {
+        const int32_t slot = t.small_off[P], x = t.item_off[a.n_nodes] + slot / 2;
+        if (slot & 1) {
+            t.item_j0[x] = (int32_t)P;
+        } else {
+            t.item_par[x] = (int32_t)P;
+            t.item_e0[x] = -1;
+            if (slot + 1 == t.small_off[a.n_nodes]) t.item_j0[x] = -1;  // an odd one out
+        }
+        return;
+    }
     const int32_t n = t.item_cnt[P];
     const int32_t nj = (n_children(a, (int32_t)P) + kTcC - 1) / kTcC;
     for (int32_t i = 0; i < n; ++i) {
@@ -436,11 +458,63 @@ __global__ void item_write_kernel(const GArgs a, TcItems t) {
     }
 }
 
+// What row `row` (an entry) and child slot `js` of item `it` are.
+struct ItemRow {
+    int64_t r = -1;       // the entry's read (-1: an unused row)
+    int32_t p0 = 0;       // its first pair index
+    int32_t P = -1;       // the parent its columns belong to (-1 with level 0's roots too)
+    int32_t cbase = 0;    // first column of that parent in the item
+    int32_t cfirst = 0;   // the child index of column cbase
+    int32_t ncols = 0;    // columns of that parent in the item
+};
+
+__device__ __forceinline__ ItemRow item_row(const GArgs& a, const TcItems& t, int32_t it, int row) {
+    ItemRow x;
+    const int32_t p = t.item_par[it], e0 = t.item_e0[it], j0 = t.item_j0[it];
+    int32_t e;
+    if (e0 < 0) {  // shared: rows 0-63 the first parent, 64-127 the second
+        const int seg = row / kTcHalfE;
+        x.P = seg ? j0 : p;
+        if (x.P < 0) return x;
+        e = row % kTcHalfE;
+        x.cbase = seg * kTcHalfC;
+        x.ncols = n_children(a, x.P);
+    } else {
+        x.P = p;
+        e = e0 + row;
+        x.cfirst = j0;
+        x.ncols = min(kTcC, n_children(a, p) - j0);
+    }
+    if (x.P < 0 && e0 >= 0) {  // level 0: entry e is read e
+        if (e < a.nq) {
+            x.r = e;
+            x.p0 = a.off[e];
+        }
+    } else if (e < t.par_cnt[x.P]) {
+        x.r = t.ent_read[t.par_off[x.P] + e];
+        x.p0 = t.ent_p0[t.par_off[x.P] + e];
+    }
+    return x;
+}
+
+__device__ __forceinline__ int32_t item_child(const GArgs& a, const TcItems& t, int32_t it, int js) {
+    const int32_t p = t.item_par[it], e0 = t.item_e0[it], j0 = t.item_j0[it];
+    if (e0 < 0) {
+        const int seg = js / kTcHalfC, c = js % kTcHalfC;
+        const int32_t P = seg ? j0 : p;
+        return P >= 0 && c < n_children(a, P) ? child_at(a, P, c) : -1;
+    }
+    return j0 + js < n_children(a, p) ? child_at(a, p, j0 + js) : -1;
+}
+
 // level 0: every read against the roots
 __global__ void items_level0_kernel(const GArgs a, TcItems t) {
     const int32_t ne = (int32_t)((a.nq + kTcE - 1) / kTcE), nj = (a.n_roots + kTcC - 1) / kTcC;
     const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) t.item_off[a.n_nodes] = ne * nj;
+    if (i == 0) {
+        t.item_off[a.n_nodes] = ne * nj;
+        t.small_off[a.n_nodes] = 0;
+    }
     if (i >= ne * nj) return;
     t.item_par[i] = -1;
     t.item_e0[i] = (i / nj) * kTcE;
@@ -525,7 +599,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a
     __syncthreads();
     tc::fence_after();
     const uint32_t tmem = tmem_base_s;
-    const int32_t n_items = t.item_off[a.n_nodes];
+    const int32_t n_items = t.item_off[a.n_nodes] + (t.small_off[a.n_nodes] + 1) / 2;
     const int kblocks = a.dim / 64;
 
     if (warp < 8) {
@@ -535,14 +609,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a
         int64_t nbase = 0;  // K blocks of the items before this one (the ring position)
         bool ok = true;
         for (int32_t it = blockIdx.x; ok && it < n_items; it += gridDim.x, nbase += kblocks) {
-            const int32_t P = t.item_par[it], e0 = t.item_e0[it], j0 = t.item_j0[it];
-            int64_t rrow = -1;
-            if (P < 0) {
-                if (e0 + tid < a.nq) rrow = e0 + tid;
-            } else if (e0 + tid < t.par_cnt[P]) {
-                rrow = t.ent_read[t.par_off[P] + e0 + tid];
-            }
-            const int32_t child = j0 + js < n_children(a, P) ? child_at(a, P, j0 + js) : -1;
+            const int64_t rrow = item_row(a, t, it, tid).r;
+            const int32_t child = item_child(a, t, it, js);
             // an unused row or child copies nothing (zeros) from a valid address
             const uint2* bits_row = reinterpret_cast<const uint2*>(a.bits + (rrow >= 0 ? rrow : 0) * a.words);
             const int4* prow = reinterpret_cast<const int4*>(a.proto + (int64_t)(child >= 0 ? child : 0) * a.dim + 16 * q);
@@ -631,40 +699,30 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a
         int acc = 0;
         uint32_t acc_phase = 0;
         for (int32_t it = blockIdx.x; it < n_items; it += gridDim.x) {
-            const int32_t P = t.item_par[it], e0 = t.item_e0[it], j0 = t.item_j0[it];
-            int64_t r = -1;
-            int32_t p0 = 0;
-            if (P < 0) {
-                if (e0 + row < a.nq) {
-                    r = e0 + row;
-                    p0 = a.off[r];
-                }
-            } else if (e0 + row < t.par_cnt[P]) {
-                r = t.ent_read[t.par_off[P] + e0 + row];
-                p0 = t.ent_p0[t.par_off[P] + e0 + row];
-            }
-            const int32_t nc = min(kTcC, n_children(a, P) - j0);
+            // this row's entry and its parent's columns (the same for the warp's 32 rows: a shared
+            // item's halves are 64 rows)
+            const ItemRow x = item_row(a, t, it, row);
             if (!tc::mbar_wait(&accf_bar[acc], acc_phase, &err_s, 12)) break;
             tc::fence_after();
             const uint32_t d = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * kTcAccCols);
-            const int64_t qn = r >= 0 ? a.qn[r] : 0;
-            // the exact dots of 16 children at a time (limb l of child j is column 32 l + j)
-            for (int h = 0; h < kTcC; h += 16) {
-                if (h >= nc) break;  // nc is the same for the whole warp
+            const int64_t qn = x.r >= 0 ? a.qn[x.r] : 0;
+            // the exact dots of 16 columns at a time (limb l of column j is TMEM column 32 l + j)
+            for (int h = x.cbase; h < x.cbase + x.ncols; h += 16) {
                 uint32_t v0[16], v1[16], v2[16];
                 tc::tmem_ld16(d + h, v0);
                 tc::tmem_ld16(d + kTcC + h, v1);
                 tc::tmem_ld16(d + 2 * kTcC + h, v2);
                 tc::tmem_ld_wait();
-                if (r < 0) continue;
+                if (x.r < 0) continue;
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
-                    if (h + j >= nc) break;
-                    const int32_t c = child_at(a, P, j0 + h + j);
+                    if (h + j >= x.cbase + x.ncols) break;
+                    const int32_t ci = x.cfirst + h + j - x.cbase;  // child index within the parent
+                    const int32_t c = child_at(a, x.P, ci);
                     const int64_t dot = (int64_t)__float2ll_rn(__uint_as_float(v0[j])) +
                                         (int64_t)__float2ll_rn(__uint_as_float(v1[j])) * 2048 +
                                         (int64_t)__float2ll_rn(__uint_as_float(v2[j])) * (2048 * 2048);
-                    a.pair_key[p0 + j0 + h + j] = make_key(exact_score(dot, qn, a.pn[c], a.mode), (uint32_t)c);
+                    a.pair_key[x.p0 + ci] = make_key(exact_score(dot, qn, a.pn[c], a.mode), (uint32_t)c);
                 }
             }
             tc::fence_before();
@@ -806,6 +864,8 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn
             t.par_cursor = carve<int32_t>(cur, n_nodes);
             t.item_cnt = carve<int32_t>(cur, n_nodes);
             t.item_off = carve<int32_t>(cur, n_nodes + 1);
+            t.small = carve<int32_t>(cur, n_nodes);
+            t.small_off = carve<int32_t>(cur, n_nodes + 1);
             t.item_par = carve<int32_t>(cur, max_items);
             t.item_e0 = carve<int32_t>(cur, max_items);
             t.item_j0 = carve<int32_t>(cur, max_items);
@@ -849,6 +909,7 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn
                 par_scatter_kernel<<<rb, 256, 0, stream>>>(a, t, L);
                 item_count_kernel<<<nb, 256, 0, stream>>>(a, t);
                 exclusive_scan(t.item_cnt, t.item_off, n_nodes, d_sums, stream);
+                exclusive_scan(t.small, t.small_off, n_nodes, d_sums, stream);
                 item_write_kernel<<<nb, 256, 0, stream>>>(a, t);
             }
             descent_tc_kernel<<<ctx->num_sms, kTcThreads, kTcSmem, stream>>>(a, t);

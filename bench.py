@@ -562,14 +562,14 @@ def run_descent(args, cfg, rank, world):
     # and output, and per level count / 3 scan kernels / expand / select plus the scoring:
     # on CUDA cores 3 scan kernels / scatter / score; on the tensor cores (every level but
     # the last; the default) level 0 its item list and descent_tc_kernel, a later level the
-    # parents' entry count / 3 scans / scatter, item count / 3 scans / write and
+    # parents' entry count / 3 scans / scatter, item count / 2 x 3 scans / write and
     # descent_tc_kernel.  One warp per read: one kernel.
     grouped = args.beam_grouped != 0 and dim % 1024 == 0 and dim <= 16384
     tc_levels = grouped and args.beam_grouped in (-1, 2)
     if not grouped:
         per_step = 2
     elif tc_levels and L > 1:
-        per_step = 1 + 3 + 6 * L + 2 + 11 * (L - 2) + 5
+        per_step = 1 + 3 + 6 * L + 2 + 14 * (L - 2) + 5
     else:
         per_step = 1 + 3 + 11 * L
     res = dict(ms=ms, e2e_ms=e2e_ms, search_ms=float(np.median(beam_ms)), clocks=clk.summary(),
