@@ -251,19 +251,42 @@ __global__ void __launch_bounds__(kScoreThreads) score_kernel(const GArgs a) {
         const int32_t* row = a.proto + (int64_t)node * a.dim + 4 * lane;
         const uint32_t* qb = a.bits + r * a.words + (lane >> 3);
         int64_t acc = 0;
-        for (int j = 0; j < nsteps; j += 4) {
-            int4 x[4];
-            uint32_t w[4];
+        if (a.pn[node] < ((int64_t)1 << 44)) {
+            // every |p| < 2^22, so a lane's (at most 512) terms sum below 2^31: int32 throughout
+            int32_t acc32 = 0;
+            for (int j = 0; j < nsteps; j += 4) {
+                int4 x[4];
+                uint32_t w[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                x[u] = __ldg(reinterpret_cast<const int4*>(row + 128 * (j + u)));
-                w[u] = __ldg(qb + 4 * (j + u));
+                for (int u = 0; u < 4; ++u) {
+                    x[u] = __ldg(reinterpret_cast<const int4*>(row + 128 * (j + u)));
+                    w[u] = __ldg(qb + 4 * (j + u));
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const uint32_t nib = w[u] >> sh;
+                    acc32 += ((nib & 1u) ? x[u].x : -x[u].x) + ((nib & 2u) ? x[u].y : -x[u].y) +
+                             ((nib & 4u) ? x[u].z : -x[u].z) + ((nib & 8u) ? x[u].w : -x[u].w);
+                }
             }
+            acc = acc32;
+        } else {
+            for (int j = 0; j < nsteps; j += 4) {
+                int4 x[4];
+                uint32_t w[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const uint32_t nib = w[u] >> sh;
-                acc += (int64_t)((nib & 1u) ? x[u].x : neg32(x[u].x)) + (int64_t)((nib & 2u) ? x[u].y : neg32(x[u].y)) +
-                       (int64_t)((nib & 4u) ? x[u].z : neg32(x[u].z)) + (int64_t)((nib & 8u) ? x[u].w : neg32(x[u].w));
+                for (int u = 0; u < 4; ++u) {
+                    x[u] = __ldg(reinterpret_cast<const int4*>(row + 128 * (j + u)));
+                    w[u] = __ldg(qb + 4 * (j + u));
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const uint32_t nib = w[u] >> sh;
+                    acc += (int64_t)((nib & 1u) ? x[u].x : neg32(x[u].x)) +
+                           (int64_t)((nib & 2u) ? x[u].y : neg32(x[u].y)) +
+                           (int64_t)((nib & 4u) ? x[u].z : neg32(x[u].z)) +
+                           (int64_t)((nib & 8u) ? x[u].w : neg32(x[u].w));
+                }
             }
         }
         for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
