@@ -1,3 +1,3 @@
 """CPU oracle for the hypervector encode / cosine top-k / propagate path.
 
-Test infrastructure only (the checker): the product never imports this."""
+Test infrastructure only: the product never imports this."""

@@ -1,7 +1,7 @@
 """ctypes front end of the CPU oracle (oracle/hdc_oracle.c).
 
-TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as
-the checker and by bench.py's CPU-baseline leg; never by the product path.
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() to
+check its result, and by bench.py's CPU-baseline leg; never by the product path.
 Every function restates the reference CPU algorithm (see hdc_oracle.c for
 the file:line citations into benlaflen/bacterial-classification).
 """
