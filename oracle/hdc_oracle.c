@@ -2,7 +2,7 @@
  * hdc_oracle.c -- CPU oracle for the k-mer hypervector encode / cosine top-k /
  * propagate-children path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker: only the test suite,
+ * TEST INFRASTRUCTURE ONLY.  Only the test suite,
  * the smoke check and the CPU-baseline leg of the benchmark load it.  The
  * product library never links or calls it.
  *
