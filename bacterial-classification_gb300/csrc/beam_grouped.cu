@@ -627,24 +627,50 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a
 
     if (warp < 8) {
         // ------------------------------------------------ producers: group g takes K blocks g, g + 2, ...
+        // Row tid of A is this thread's entry.  The valid children's values of a K block are
+        // groups of 4 (group 16 v + u: the item's v-th valid child, dims 4u..4u+3); group x
+        // goes to thread x mod 128, so the limb split is spread over the whole group.  Nothing
+        // is written for an unused row or child slot: an accumulator row or column depends only
+        // on its own A row or B row, and the epilogue never reads those of unused ones.
         const int g = warp >> 2;
-        const int tid = threadIdx.x & 127, js = tid >> 2, q = tid & 3;  // A row tid; B child js, dims 16q..+15
-        int64_t nbase = 0;  // K blocks of the items before this one (the ring position)
+        const int tid = threadIdx.x & 127;
+        const int ptid = threadIdx.x;  // 0..255: this thread's staging column
+        int64_t nbase = 0;             // K blocks of the items before this one (the ring position)
         bool ok = true;
         for (int32_t it = blockIdx.x; ok && it < n_items; it += gridDim.x, nbase += kblocks) {
             const int64_t rrow = item_row(a, t, it, tid).r;
-            const int32_t child = item_child(a, t, it, js);
-            // an unused row or child copies nothing (zeros) from a valid address
             const uint2* bits_row = reinterpret_cast<const uint2*>(a.bits + (rrow >= 0 ? rrow : 0) * a.words);
-            const int4* prow = reinterpret_cast<const int4*>(a.proto + (int64_t)(child >= 0 ? child : 0) * a.dim + 16 * q);
-            const uint32_t wbytes = rrow >= 0 ? 8u : 0u, pbytes = child >= 0 ? 16u : 0u;
-            const int ptid = threadIdx.x;  // 0..255: this thread's staging column
-            auto issue = [&](int kb, int slot) {  // this thread's slice of K block kb, into staging slot `slot`
+            // the valid child slots: 0..n0-1 and, in a shared item, 16..16+n1-1
+            const int32_t ip = t.item_par[it], ie0 = t.item_e0[it], ij0 = t.item_j0[it];
+            int n0, n1 = 0;
+            if (ie0 < 0) {
+                n0 = n_children(a, ip);
+                n1 = ij0 >= 0 ? n_children(a, ij0) : 0;
+            } else {
+                n0 = min(kTcC, n_children(a, ip) - ij0);
+            }
+            const int ngroups = (n0 + n1) * 16;
+            const int4* gsrc[4];
+            int gdst[4];  // child slot * 16 + u
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int x = tid + kTcE * i;
+                gsrc[i] = reinterpret_cast<const int4*>(a.proto);
+                gdst[i] = 0;
+                if (x < ngroups) {
+                    const int v = x >> 4, u = x & 15;
+                    const int js = v < n0 ? v : kTcHalfC + (v - n0);
+                    gsrc[i] = reinterpret_cast<const int4*>(a.proto + (int64_t)item_child(a, t, it, js) * a.dim) + u;
+                    gdst[i] = js * 16 + u;
+                }
+            }
+            auto issue = [&](int kb, int slot) {  // this thread's slices of K block kb, into staging slot `slot`
                 if (kb < kblocks) {
                     uint4* sb = staging + (size_t)slot * 5 * kTcProducers;
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) cp_async16(sb + u * kTcProducers + ptid, prow + kb * 16 + u, pbytes);
-                    cp_async8(sb + 4 * kTcProducers + ptid, bits_row + kb, wbytes);
+                    for (int i = 0; i < 4; ++i)
+                        if (tid + kTcE * i < ngroups) cp_async16(sb + i * kTcProducers + ptid, gsrc[i] + kb * 16, 16);
+                    if (rrow >= 0) cp_async8(sb + 4 * kTcProducers + ptid, bits_row + kb, 8);
                 }
                 cp_async_commit();  // one group per call (possibly empty), so the wait below counts blocks
             };
@@ -654,13 +680,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a
                 cp_async_wait<kTcDepth - 1>();  // this thread's copies of block kb have landed
                 const int slot = i % kTcDepth;
                 const uint4* sb = staging + (size_t)slot * 5 * kTcProducers;
-                int4 pv[4];
+                uint4 pv[4];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const uint4 x = sb[u * kTcProducers + ptid];
-                    pv[u] = make_int4((int)x.x, (int)x.y, (int)x.z, (int)x.w);
-                }
-                const uint2 w = *reinterpret_cast<const uint2*>(sb + 4 * kTcProducers + ptid);
+                for (int j = 0; j < 4; ++j) pv[j] = tid + kTcE * j < ngroups ? sb[j * kTcProducers + ptid] : make_uint4(0, 0, 0, 0);
+                const uint2 w = rrow >= 0 ? *reinterpret_cast<const uint2*>(sb + 4 * kTcProducers + ptid) : make_uint2(0, 0);
                 issue(kb + 2 * kTcDepth, slot);  // the slot is free again: refill it kTcDepth blocks ahead
                 const int64_t n = nbase + kb;
                 const int stage = (int)(n % kTcStages);
@@ -671,7 +694,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a
                     break;
                 }
                 uint8_t* st = ring + (size_t)stage * kTcStageBytes;
-                // A: this entry's 64 signs; an unused row is zero
+                // A: this entry's 64 signs
                 if (rrow >= 0) {
 #pragma unroll
                     for (int c = 0; c < 8; ++c) {
@@ -679,36 +702,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a
                         const uint2 lo = signs_lut[byte & 15u], hi = signs_lut[byte >> 4];
                         *reinterpret_cast<uint4*>(swz(st, tid, c)) = make_uint4(lo.x, lo.y, hi.x, hi.y);
                     }
-                } else {
-#pragma unroll
-                    for (int c = 0; c < 8; ++c) *reinterpret_cast<uint4*>(swz(st, tid, c)) = make_uint4(0, 0, 0, 0);
                 }
-                // B: 16 prototype values in three limbs, 8 (one 16-byte chunk per limb) at a time;
-                // an unused child is zero
-                if (child >= 0) {
+                // B: this thread's groups of 4 prototype values, each in three limbs (8 bytes per limb)
 #pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        int32_t lv[3][8];
+                for (int j = 0; j < 4; ++j) {
+                    if (tid + kTcE * j >= ngroups) break;
+                    int32_t l0[4], l1[4], l2[4];
+                    const int32_t x[4] = {(int32_t)pv[j].x, (int32_t)pv[j].y, (int32_t)pv[j].z, (int32_t)pv[j].w};
 #pragma unroll
-                        for (int u = 0; u < 2; ++u) {
-                            const int4 p4 = pv[2 * h + u];
-                            const int32_t x[4] = {p4.x, p4.y, p4.z, p4.w};
-#pragma unroll
-                            for (int e = 0; e < 4; ++e) limbs3(x[e], lv[0][4 * u + e], lv[1][4 * u + e], lv[2][4 * u + e]);
-                        }
-#pragma unroll
-                        for (int l = 0; l < kTcLimbs; ++l)
-                            *reinterpret_cast<uint4*>(swz(st + kTcABytes + l * kTcBBytes, js, 2 * q + h)) =
-                                make_uint4(half2_bits(lv[l][0], lv[l][1]), half2_bits(lv[l][2], lv[l][3]),
-                                           half2_bits(lv[l][4], lv[l][5]), half2_bits(lv[l][6], lv[l][7]));
-                    }
-                } else {
-#pragma unroll
-                    for (int l = 0; l < kTcLimbs; ++l)
-#pragma unroll
-                        for (int h = 0; h < 2; ++h)
-                            *reinterpret_cast<uint4*>(swz(st + kTcABytes + l * kTcBBytes, js, 2 * q + h)) =
-                                make_uint4(0, 0, 0, 0);
+                    for (int e = 0; e < 4; ++e) limbs3(x[e], l0[e], l1[e], l2[e]);
+                    const int js = gdst[j] >> 4, u = gdst[j] & 15;
+                    const int off = (u & 1) * 8;
+                    *reinterpret_cast<uint2*>(swz(st + kTcABytes, js, u >> 1) + off) =
+                        make_uint2(half2_bits(l0[0], l0[1]), half2_bits(l0[2], l0[3]));
+                    *reinterpret_cast<uint2*>(swz(st + kTcABytes + kTcBBytes, js, u >> 1) + off) =
+                        make_uint2(half2_bits(l1[0], l1[1]), half2_bits(l1[2], l1[3]));
+                    *reinterpret_cast<uint2*>(swz(st + kTcABytes + 2 * kTcBBytes, js, u >> 1) + off) =
+                        make_uint2(half2_bits(l2[0], l2[1]), half2_bits(l2[2], l2[3]));
                 }
                 tc::fence_proxy_async();  // the writes above are read by the tensor cores
                 __syncwarp();
