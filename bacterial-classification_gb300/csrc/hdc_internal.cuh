@@ -29,7 +29,7 @@ struct hdc_context {
     int tc_prefetch = -1;           // tensor-core search: K blocks prefetched into L2 ahead (-1: automatic)
     int tc_cluster = 0;             // tensor-core search: CTAs sharing an operand's blocks, 1 or 2 (0: automatic)
     int tc_share = -1;              // tensor-core search: 0 pairs share references, 1 queries (-1: automatic)
-    int tc_quad_fit = -1;           // clusters of 4 of the pair-MMA search resident at once (-1: not asked)
+    mutable int tc_quad_fit = -1;   // clusters of 4 of the pair-MMA search resident at once (-1: not asked yet)
     int32_t tc_last_shape[5] = {0, 0, 0, 0, 0};  // cluster, G, S, pair MMA, kernels of the last tc search
     int tc_lanes = 0;               // tensor-core search: at most this many reference lanes (0: SMs / G)
     int tc_pair_mma = -1;           // tensor-core search: CTA pairs as one M = 256 MMA (-1: automatic)

@@ -1120,7 +1120,7 @@ static int quad_clusters_fit(const hdc_context* ctx) {
         if (cudaOccupancyMaxActiveClusters(&fit, kern, &cfg) != cudaSuccess) fit = 0;
     }
     cudaGetLastError();
-    const_cast<hdc_context*>(ctx)->tc_quad_fit = fit;
+    ctx->tc_quad_fit = fit;  // a cache of a device property
     return fit;
 }
 
