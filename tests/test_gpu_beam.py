@@ -152,14 +152,17 @@ def test_beam_tensor_core_levels_wide_nodes_and_limbs(hdc, cuda):
     roots = torch.arange(0, n0, dtype=torch.int32, device=cuda)
     d_ptr, d_idx = torch.from_numpy(ptr).to(cuda), torch.from_numpy(idx).to(cuda)
     out = []
+    cases = [(levels, beam, threshold) for levels in (1, 2, 3)  # 1: no tensor-core level; 2: level 0 only
+             for beam, threshold in ((5, float("-inf")), (8, 0.0), (3, -0.5))]
     for grouped in (1, 2):
         ctx.option(H.BEAM_GROUPED, grouped)
-        for beam, threshold in ((5, float("-inf")), (8, 0.0), (3, -0.5)):
-            res = ctx.beam_search(q8, qn, proto, pn, d_ptr, d_idx, roots, 3, beam, threshold)
+        for levels, beam, threshold in cases:
+            res = ctx.beam_search(q8, qn, proto, pn, d_ptr, d_idx, roots, levels, beam, threshold)
             out.append([x.cpu().numpy() for x in res])
     torch.cuda.synchronize()
     assert ctx.status() == 0
-    for a, b_ in zip(out[:3], out[3:]):
+    n = len(cases)
+    for a, b_ in zip(out[:n], out[n:]):
         for x, y in zip(a, b_):
             assert np.array_equal(x, y)
 
