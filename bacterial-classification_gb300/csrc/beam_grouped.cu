@@ -27,6 +27,8 @@ namespace {
 constexpr int kMaxBeamG = 8;
 constexpr int kMaxLevelsG = 8;
 constexpr int kScoreThreads = 256;          // 8 warps, one pair each at a time
+constexpr int kScoreBlocks = 8;             // resident per SM; the grid is one wave
+constexpr int kScoreBlocks16 = 6;           // the same with int16 rows (40 registers a thread)
 constexpr int kScanItems = 16;              // elements per thread of the scan
 constexpr int kScanBlock = 256 * kScanItems;
 
@@ -152,7 +154,9 @@ struct GArgs {
     double threshold;
     const uint32_t* bits;     // [nq][words]
     const int64_t* qn;        // [nq]
-    const int32_t* proto;     // [n_nodes][dim]
+    const int32_t* proto;     // [n32][dim] int32 rows of nodes < n32
+    const int16_t* proto16;   // [n_nodes - n32][dim] int16 rows of nodes >= n32 (row node - n32)
+    int64_t n32;
     const int64_t* pn;        // [n_nodes]
     const int64_t* child_ptr;
     const int32_t* child_idx;
@@ -232,66 +236,130 @@ __global__ void scatter_kernel(const GArgs a) {
 
 // One warp per pair, the warps walking the pairs in node order: the pairs of a node are
 // scored by neighbouring warps at about the same time, so its prototype row comes from
-// DRAM once and from L1/L2 for the others.  Lane l covers dims 128 j + 4 l .. + 3; four
-// 16-byte prototype loads are in flight per lane, and the read is its packed bits.
+// DRAM once and from L1/L2 for the others.  Four 16-byte prototype loads are in flight per
+// lane, and the read is its packed bits.  With int16 rows (about twice the pairs per second)
+// the FP64 scores are computed 32 pairs at a time, one per lane: the warp keeps pair i's dot
+// in lane i mod 32.
 // -x in 32 bits, with wrap-around defined (exact for every prototype element but INT32_MIN,
 // which hdc_beam_search excludes; widening before negating costs ~40 % of the kernel)
 __device__ __forceinline__ int32_t neg32(int32_t x) { return (int32_t)(0u - (uint32_t)x); }
 
-__global__ void __launch_bounds__(kScoreThreads) score_kernel(const GArgs a) {
+// Lane l's share of the dot of an int32 row: dims 128 j + 4 l .. + 3.
+__device__ __forceinline__ int64_t lane_dot32(const GArgs& a, int lane, int32_t node, int64_t r) {
+    const int nsteps = a.dim / 128;  // a multiple of 8 (dim % 1024 == 0)
+    const int sh = (lane & 7) * 4;
+    const int32_t* row = a.proto + (int64_t)node * a.dim + 4 * lane;
+    const uint32_t* qb = a.bits + r * a.words + (lane >> 3);
+    if (a.pn[node] < ((int64_t)1 << 44)) {
+        // every |p| < 2^22, so a lane's (at most 512) terms sum below 2^31: int32 throughout
+        int32_t acc32 = 0;
+        for (int j = 0; j < nsteps; j += 4) {
+            int4 x[4];
+            uint32_t w[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                x[u] = __ldg(reinterpret_cast<const int4*>(row + 128 * (j + u)));
+                w[u] = __ldg(qb + 4 * (j + u));
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t nib = w[u] >> sh;
+                acc32 += ((nib & 1u) ? x[u].x : -x[u].x) + ((nib & 2u) ? x[u].y : -x[u].y) +
+                         ((nib & 4u) ? x[u].z : -x[u].z) + ((nib & 8u) ? x[u].w : -x[u].w);
+            }
+        }
+        return acc32;
+    }
+    int64_t acc = 0;
+    for (int j = 0; j < nsteps; j += 4) {
+        int4 x[4];
+        uint32_t w[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            x[u] = __ldg(reinterpret_cast<const int4*>(row + 128 * (j + u)));
+            w[u] = __ldg(qb + 4 * (j + u));
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t nib = w[u] >> sh;
+            acc += (int64_t)((nib & 1u) ? x[u].x : neg32(x[u].x)) + (int64_t)((nib & 2u) ? x[u].y : neg32(x[u].y)) +
+                   (int64_t)((nib & 4u) ? x[u].z : neg32(x[u].z)) + (int64_t)((nib & 8u) ? x[u].w : neg32(x[u].w));
+        }
+    }
+    return acc;
+}
+
+// Four sign bits (bit i set: +1) as four signed bytes +1 / -1: the bits spread to the low bit
+// of each byte (the four shifted copies of the nibble do not overlap), then 1 -> 0x01 and
+// 0 -> 0xFF by ~(b * 0xFE) per byte.
+__device__ __forceinline__ int signs4_bytes(uint32_t nib) {
+    return (int)~(((nib * 0x00204081u) & 0x01010101u) * 0xFEu);
+}
+
+// Lane l's share of the dot of an int16 row: dims 256 j + 8 l .. + 7 (one 16-byte load, one
+// byte of the read's bits).  Each word holds two int16 values (the lower dim in the low half);
+// dp2a multiplies them by two of the signed sign bytes and accumulates, exactly.  |p| <= 2^15
+// and at most 512 terms a lane: int32 throughout.
+__device__ __forceinline__ int64_t lane_dot16(const GArgs& a, int lane, int32_t node, int64_t r) {
+    const int nsteps = a.dim / 256;  // a multiple of 4 (dim % 1024 == 0)
+    const int sh = (lane & 3) * 8;
+    const int4* row = reinterpret_cast<const int4*>(a.proto16 + (node - a.n32) * a.dim) + lane;
+    const uint32_t* qb = a.bits + r * a.words + (lane >> 2);
+    int acc = 0;
+    for (int j = 0; j < nsteps; j += 4) {
+        int4 x[4];
+        uint32_t w[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            x[u] = __ldg(row + 32 * (j + u));
+            w[u] = __ldg(qb + 8 * (j + u));
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t byte = w[u] >> sh;
+            const int s0 = signs4_bytes(byte & 15u), s1 = signs4_bytes((byte >> 4) & 15u);
+            acc = __dp2a_lo(x[u].x, s0, acc);  // dims 0, 1
+            acc = __dp2a_hi(x[u].y, s0, acc);  // dims 2, 3
+            acc = __dp2a_lo(x[u].z, s1, acc);  // dims 4, 5
+            acc = __dp2a_hi(x[u].w, s1, acc);  // dims 6, 7
+        }
+    }
+    return acc;
+}
+
+// ROWS16: some nodes have int16 rows (hdc_beam_search_split); without, the kernel is the
+// int32 one alone (fewer registers, every warp slot of the SM resident)
+template <bool ROWS16>
+__global__ void __launch_bounds__(kScoreThreads, ROWS16 ? kScoreBlocks16 : kScoreBlocks) score_kernel(const GArgs a) {
     const int lane = threadIdx.x & 31;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int32_t total = a.off[a.nq];
-    const int nsteps = a.dim / 128;  // a multiple of 8 (dim % 1024 == 0)
-    const int sh = (lane & 7) * 4;
-    for (int64_t s = (((int64_t)blockIdx.x * blockDim.x) >> 5) + (threadIdx.x >> 5); s < total; s += nw) {
+    int32_t my_pi = -1, my_node = 0;
+    int64_t my_r = 0, my_dot = 0;
+    int i = 0;
+    for (int64_t s = (((int64_t)blockIdx.x * blockDim.x) >> 5) + (threadIdx.x >> 5); s < total; s += nw, ++i) {
         const int32_t pi = a.sorted[s];
         const int32_t node = a.pair_node[pi];
         const int64_t r = a.pair_read[pi];
-        const int32_t* row = a.proto + (int64_t)node * a.dim + 4 * lane;
-        const uint32_t* qb = a.bits + r * a.words + (lane >> 3);
-        int64_t acc = 0;
-        if (a.pn[node] < ((int64_t)1 << 44)) {
-            // every |p| < 2^22, so a lane's (at most 512) terms sum below 2^31: int32 throughout
-            int32_t acc32 = 0;
-            for (int j = 0; j < nsteps; j += 4) {
-                int4 x[4];
-                uint32_t w[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    x[u] = __ldg(reinterpret_cast<const int4*>(row + 128 * (j + u)));
-                    w[u] = __ldg(qb + 4 * (j + u));
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const uint32_t nib = w[u] >> sh;
-                    acc32 += ((nib & 1u) ? x[u].x : -x[u].x) + ((nib & 2u) ? x[u].y : -x[u].y) +
-                             ((nib & 4u) ? x[u].z : -x[u].z) + ((nib & 8u) ? x[u].w : -x[u].w);
-                }
-            }
-            acc = acc32;
-        } else {
-            for (int j = 0; j < nsteps; j += 4) {
-                int4 x[4];
-                uint32_t w[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    x[u] = __ldg(reinterpret_cast<const int4*>(row + 128 * (j + u)));
-                    w[u] = __ldg(qb + 4 * (j + u));
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const uint32_t nib = w[u] >> sh;
-                    acc += (int64_t)((nib & 1u) ? x[u].x : neg32(x[u].x)) +
-                           (int64_t)((nib & 2u) ? x[u].y : neg32(x[u].y)) +
-                           (int64_t)((nib & 4u) ? x[u].z : neg32(x[u].z)) +
-                           (int64_t)((nib & 8u) ? x[u].w : neg32(x[u].w));
-                }
-            }
-        }
+        int64_t acc = ROWS16 && node >= a.n32 ? lane_dot16(a, lane, node, r) : lane_dot32(a, lane, node, r);
         for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) a.pair_key[pi] = make_key(exact_score(acc, a.qn[r], a.pn[node], a.mode), (uint32_t)node);
+        if (!ROWS16) {  // the int32 kernel scores on lane 0 (holding 32 pairs would spill at 32 registers)
+            if (lane == 0) a.pair_key[pi] = make_key(exact_score(acc, a.qn[r], a.pn[node], a.mode), (uint32_t)node);
+            continue;
+        }
+        if (lane == (i & 31)) {
+            my_pi = pi;
+            my_node = node;
+            my_r = r;
+            my_dot = acc;
+        }
+        if ((i & 31) == 31 && my_pi >= 0) {
+            a.pair_key[my_pi] = make_key(exact_score(my_dot, a.qn[my_r], a.pn[my_node], a.mode), (uint32_t)my_node);
+            my_pi = -1;
+        }
     }
+    if (my_pi >= 0)
+        a.pair_key[my_pi] = make_key(exact_score(my_dot, a.qn[my_r], a.pn[my_node], a.mode), (uint32_t)my_node);
 }
 
 // Per read: the best `beam` candidates, then the rule of the per-read kernel (stop below
@@ -650,80 +718,107 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a
                 n0 = min(kTcC, n_children(a, ip) - ij0);
             }
             const int ngroups = (n0 + n1) * 16;
-            const int4* gsrc[4];
-            int gdst[4];  // child slot * 16 + u
+            const char* gsrc[4];  // this group's 4 values in K block 0: 16 bytes of an int32 row or 8 of an int16 row
+            int gdst[4];          // child slot * 16 + u
+            bool g16[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 const int x = tid + kTcE * i;
-                gsrc[i] = reinterpret_cast<const int4*>(a.proto);
+                gsrc[i] = reinterpret_cast<const char*>(a.proto);
                 gdst[i] = 0;
+                g16[i] = false;
                 if (x < ngroups) {
                     const int v = x >> 4, u = x & 15;
                     const int js = v < n0 ? v : kTcHalfC + (v - n0);
-                    gsrc[i] = reinterpret_cast<const int4*>(a.proto + (int64_t)item_child(a, t, it, js) * a.dim) + u;
+                    const int64_t c = item_child(a, t, it, js);
+                    g16[i] = c >= a.n32;
+                    gsrc[i] = g16[i] ? reinterpret_cast<const char*>(a.proto16 + (c - a.n32) * a.dim + 4 * u)
+                                     : reinterpret_cast<const char*>(a.proto + c * a.dim + 4 * u);
                     gdst[i] = js * 16 + u;
                 }
             }
-            auto issue = [&](int kb, int slot) {  // this thread's slices of K block kb, into staging slot `slot`
-                if (kb < kblocks) {
-                    uint4* sb = staging + (size_t)slot * 5 * kTcProducers;
+            // a warp whose groups are all int32 rows runs the int32-only body
+            bool my16 = false;
 #pragma unroll
-                    for (int i = 0; i < 4; ++i)
-                        if (tid + kTcE * i < ngroups) cp_async16(sb + i * kTcProducers + ptid, gsrc[i] + kb * 16, 16);
-                    if (rrow >= 0) cp_async8(sb + 4 * kTcProducers + ptid, bits_row + kb, 8);
-                }
-                cp_async_commit();  // one group per call (possibly empty), so the wait below counts blocks
-            };
+            for (int i = 0; i < 4; ++i) my16 |= g16[i];
+            auto body = [&](auto rows16) {
+                constexpr bool R16 = decltype(rows16)::value;
+                auto issue = [&](int kb, int slot) {  // this thread's slices of K block kb, into staging slot `slot`
+                    if (kb < kblocks) {
+                        uint4* sb = staging + (size_t)slot * 5 * kTcProducers;
 #pragma unroll
-            for (int i = 0; i < kTcDepth; ++i) issue(g + 2 * i, i);
-            for (int kb = g, i = 0; kb < kblocks; kb += 2, ++i) {
-                cp_async_wait<kTcDepth - 1>();  // this thread's copies of block kb have landed
-                const int slot = i % kTcDepth;
-                const uint4* sb = staging + (size_t)slot * 5 * kTcProducers;
-                uint4 pv[4];
-#pragma unroll
-                for (int j = 0; j < 4; ++j) pv[j] = tid + kTcE * j < ngroups ? sb[j * kTcProducers + ptid] : make_uint4(0, 0, 0, 0);
-                const uint2 w = rrow >= 0 ? *reinterpret_cast<const uint2*>(sb + 4 * kTcProducers + ptid) : make_uint2(0, 0);
-                issue(kb + 2 * kTcDepth, slot);  // the slot is free again: refill it kTcDepth blocks ahead
-                const int64_t n = nbase + kb;
-                const int stage = (int)(n % kTcStages);
-                const uint32_t phase = (uint32_t)((n / kTcStages) & 1);
-                const bool got = tc::mbar_wait(&empty_bar[stage], phase ^ 1, &err_s, 11);
-                if (__any_sync(0xffffffffu, !got)) {
-                    ok = false;
-                    break;
-                }
-                uint8_t* st = ring + (size_t)stage * kTcStageBytes;
-                // A: this entry's 64 signs
-                if (rrow >= 0) {
-#pragma unroll
-                    for (int c = 0; c < 8; ++c) {
-                        const uint32_t byte = ((c < 4 ? w.x : w.y) >> (8 * (c & 3))) & 0xffu;
-                        const uint2 lo = signs_lut[byte & 15u], hi = signs_lut[byte >> 4];
-                        *reinterpret_cast<uint4*>(swz(st, tid, c)) = make_uint4(lo.x, lo.y, hi.x, hi.y);
+                        for (int i = 0; i < 4; ++i)
+                            if (tid + kTcE * i < ngroups) {
+                                if (R16 && g16[i])
+                                    cp_async8(sb + i * kTcProducers + ptid, gsrc[i] + kb * 128, 8);
+                                else
+                                    cp_async16(sb + i * kTcProducers + ptid, gsrc[i] + kb * 256, 16);
+                            }
+                        if (rrow >= 0) cp_async8(sb + 4 * kTcProducers + ptid, bits_row + kb, 8);
                     }
-                }
-                // B: this thread's groups of 4 prototype values, each in three limbs (8 bytes per limb)
+                    cp_async_commit();  // one group per call (possibly empty), so the wait below counts blocks
+                };
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    if (tid + kTcE * j >= ngroups) break;
-                    int32_t l0[4], l1[4], l2[4];
-                    const int32_t x[4] = {(int32_t)pv[j].x, (int32_t)pv[j].y, (int32_t)pv[j].z, (int32_t)pv[j].w};
+                for (int i = 0; i < kTcDepth; ++i) issue(g + 2 * i, i);
+                for (int kb = g, i = 0; kb < kblocks; kb += 2, ++i) {
+                    cp_async_wait<kTcDepth - 1>();  // this thread's copies of block kb have landed
+                    const int slot = i % kTcDepth;
+                    const uint4* sb = staging + (size_t)slot * 5 * kTcProducers;
+                    uint4 pv[4];
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) limbs3(x[e], l0[e], l1[e], l2[e]);
-                    const int js = gdst[j] >> 4, u = gdst[j] & 15;
-                    const int off = (u & 1) * 8;
-                    *reinterpret_cast<uint2*>(swz(st + kTcABytes, js, u >> 1) + off) =
-                        make_uint2(half2_bits(l0[0], l0[1]), half2_bits(l0[2], l0[3]));
-                    *reinterpret_cast<uint2*>(swz(st + kTcABytes + kTcBBytes, js, u >> 1) + off) =
-                        make_uint2(half2_bits(l1[0], l1[1]), half2_bits(l1[2], l1[3]));
-                    *reinterpret_cast<uint2*>(swz(st + kTcABytes + 2 * kTcBBytes, js, u >> 1) + off) =
-                        make_uint2(half2_bits(l2[0], l2[1]), half2_bits(l2[2], l2[3]));
+                    for (int j = 0; j < 4; ++j) pv[j] = tid + kTcE * j < ngroups ? sb[j * kTcProducers + ptid] : make_uint4(0, 0, 0, 0);
+                    const uint2 w = rrow >= 0 ? *reinterpret_cast<const uint2*>(sb + 4 * kTcProducers + ptid) : make_uint2(0, 0);
+                    issue(kb + 2 * kTcDepth, slot);  // the slot is free again: refill it kTcDepth blocks ahead
+                    const int64_t n = nbase + kb;
+                    const int stage = (int)(n % kTcStages);
+                    const uint32_t phase = (uint32_t)((n / kTcStages) & 1);
+                    const bool got = tc::mbar_wait(&empty_bar[stage], phase ^ 1, &err_s, 11);
+                    if (__any_sync(0xffffffffu, !got)) {
+                        ok = false;
+                        break;
+                    }
+                    uint8_t* st = ring + (size_t)stage * kTcStageBytes;
+                    // A: this entry's 64 signs
+                    if (rrow >= 0) {
+#pragma unroll
+                        for (int c = 0; c < 8; ++c) {
+                            const uint32_t byte = ((c < 4 ? w.x : w.y) >> (8 * (c & 3))) & 0xffu;
+                            const uint2 lo = signs_lut[byte & 15u], hi = signs_lut[byte >> 4];
+                            *reinterpret_cast<uint4*>(swz(st, tid, c)) = make_uint4(lo.x, lo.y, hi.x, hi.y);
+                        }
+                    }
+                    // B: this thread's groups of 4 prototype values, each in three limbs (8 bytes per limb)
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        if (tid + kTcE * j >= ngroups) break;
+                        int32_t l0[4], l1[4], l2[4];
+                        int32_t x[4] = {(int32_t)pv[j].x, (int32_t)pv[j].y, (int32_t)pv[j].z, (int32_t)pv[j].w};
+                        if (R16 && g16[j]) {  // four int16 values in the first 8 bytes
+                            x[0] = (int32_t)(pv[j].x << 16) >> 16;
+                            x[1] = (int32_t)pv[j].x >> 16;
+                            x[2] = (int32_t)(pv[j].y << 16) >> 16;
+                            x[3] = (int32_t)pv[j].y >> 16;
+                        }
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) limbs3(x[e], l0[e], l1[e], l2[e]);
+                        const int js = gdst[j] >> 4, u = gdst[j] & 15;
+                        const int off = (u & 1) * 8;
+                        *reinterpret_cast<uint2*>(swz(st + kTcABytes, js, u >> 1) + off) =
+                            make_uint2(half2_bits(l0[0], l0[1]), half2_bits(l0[2], l0[3]));
+                        *reinterpret_cast<uint2*>(swz(st + kTcABytes + kTcBBytes, js, u >> 1) + off) =
+                            make_uint2(half2_bits(l1[0], l1[1]), half2_bits(l1[2], l1[3]));
+                        *reinterpret_cast<uint2*>(swz(st + kTcABytes + 2 * kTcBBytes, js, u >> 1) + off) =
+                            make_uint2(half2_bits(l2[0], l2[1]), half2_bits(l2[2], l2[3]));
+                    }
+                    tc::fence_proxy_async();  // the writes above are read by the tensor cores
+                    __syncwarp();
+                    if (lane == 0) tc::mbar_arrive(&full_bar[stage]);
                 }
-                tc::fence_proxy_async();  // the writes above are read by the tensor cores
-                __syncwarp();
-                if (lane == 0) tc::mbar_arrive(&full_bar[stage]);
-            }
+            };
+            if (__any_sync(0xffffffffu, my16))
+                body(std::true_type{});
+            else
+                body(std::false_type{});
         }
         cp_async_wait<0>();  // no copy may still be landing when the CTA leaves
     } else if (warp < 12) {
@@ -823,7 +918,7 @@ T* carve(uint8_t*& cur, int64_t n) {
 }  // namespace
 
 int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn, int64_t nq, const int32_t* d_proto,
-                        const int64_t* d_pn, int64_t n_nodes, const int64_t* d_child_ptr, const int32_t* d_child_idx,
+                        int64_t n32, const int16_t* d_proto16, const int64_t* d_pn, int64_t n_nodes, const int64_t* d_child_ptr, const int32_t* d_child_idx,
                         const int32_t* d_roots, int n_roots, int levels, int beam, double threshold, int mode,
                         int32_t* d_path, float* d_path_score, int32_t* d_depth, cudaStream_t stream) {
     if ((int64_t)n_nodes > (int64_t)kScanBlock * kScanBlock || nq > (int64_t)kScanBlock * kScanBlock)
@@ -856,6 +951,8 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn
     a.threshold = threshold;
     a.qn = d_qn;
     a.proto = d_proto;
+    a.proto16 = d_proto16;
+    a.n32 = n32;
     a.pn = d_pn;
     a.child_ptr = d_child_ptr;
     a.child_idx = d_child_idx;
@@ -950,7 +1047,10 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn
             exclusive_scan(a.node_cnt, a.node_off, n_nodes, d_sums, stream);
             cudaMemcpyAsync(a.cursor, a.node_off, (size_t)n_nodes * 4, cudaMemcpyDeviceToDevice, stream);
             scatter_kernel<<<work_grid, 256, 0, stream>>>(a);
-            score_kernel<<<work_grid, kScoreThreads, 0, stream>>>(a);
+            if (n32 < n_nodes)
+                score_kernel<true><<<ctx->num_sms * kScoreBlocks16, kScoreThreads, 0, stream>>>(a);
+            else
+                score_kernel<false><<<ctx->num_sms * kScoreBlocks, kScoreThreads, 0, stream>>>(a);
         }
         select_kernel<<<rb, 256, 0, stream>>>(a, L);
     }

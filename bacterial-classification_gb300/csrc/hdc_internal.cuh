@@ -112,9 +112,10 @@ int launch_propagate_greedy(hdc_context* ctx, const int16_t* d_hv, const int64_t
                             uint8_t* d_selected, float* d_best, int32_t* d_scratch, cudaStream_t stream);
 
 int launch_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn, int64_t nq, const int32_t* d_proto,
-                       const int64_t* d_pn, int64_t n_nodes, const int64_t* d_child_ptr, const int32_t* d_child_idx,
-                       const int32_t* d_roots, int n_roots, int levels, int beam, double threshold, int mode,
-                       int32_t* d_path, float* d_path_score, int32_t* d_depth, cudaStream_t stream);
+                       int64_t n32, const int16_t* d_proto16, const int64_t* d_pn, int64_t n_nodes,
+                       const int64_t* d_child_ptr, const int32_t* d_child_idx, const int32_t* d_roots, int n_roots,
+                       int levels, int beam, double threshold, int mode, int32_t* d_path, float* d_path_score,
+                       int32_t* d_depth, cudaStream_t stream);
 
 int launch_identify(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qn, int64_t nq, const int16_t* d_rows,
                     const int64_t* d_rn, const int64_t* d_node_rows, const int64_t* d_child_ptr,
@@ -127,9 +128,10 @@ int launch_similarity(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qn,
                       const int32_t* d_pair_q, const int32_t* d_pair_ref, int64_t n_pairs, int mode, float* d_score,
                       int32_t* d_window, cudaStream_t stream);
 
-// the descent with reads grouped by candidate node (beam_grouped.cu); dim % 1024 == 0, dim <= 16384
+// the descent with reads grouped by candidate node (beam_grouped.cu); dim % 1024 == 0, dim <= 16384;
+// nodes < n32 have int32 rows in d_proto, the others int16 rows in d_proto16 (row node - n32)
 int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn, int64_t nq, const int32_t* d_proto,
-                        const int64_t* d_pn, int64_t n_nodes, const int64_t* d_child_ptr, const int32_t* d_child_idx,
+                        int64_t n32, const int16_t* d_proto16, const int64_t* d_pn, int64_t n_nodes, const int64_t* d_child_ptr, const int32_t* d_child_idx,
                         const int32_t* d_roots, int n_roots, int levels, int beam, double threshold, int mode,
                         int32_t* d_path, float* d_path_score, int32_t* d_depth, cudaStream_t stream);
 

@@ -39,6 +39,8 @@ SIGNATURES = [
                                SZ, P]),
     ("hdc_bundle", I32, [P, P, I32, P, P, I64, P, P]),
     ("hdc_beam_search", I32, [P, P, P, I64, P, P, I64, P, P, P, I32, I32, I32, ctypes.c_double, I32, P, P, P, P]),
+    ("hdc_beam_search_split", I32, [P, P, P, I64, P, I64, P, P, I64, P, P, P, I32, I32, I32, ctypes.c_double, I32, P,
+                                    P, P, P]),
     ("hdc_similarity", I32, [P, P, P, P, P, P, P, P, P, I64, I32, P, P, P]),
     ("hdc_identify", I32, [P, P, P, I64, P, P, P, P, P, P, I32, I32, I32, ctypes.c_double, I32, P, P, P, P, P]),
     ("hdc_propagate_greedy", I32, [P, P, P, P, P, P, P, I64, ctypes.c_double, I32, P, P, P, P]),
@@ -250,6 +252,23 @@ class Context:
                                     ptr(child_idx),
                                     ptr(roots), roots.numel(), levels, beam, threshold, mode, ptr(path), ptr(score),
                                     ptr(depth), stream_ptr(stream)))
+        return path, score, depth
+
+    def beam_search_split(self, q, qn, proto32, proto16, pn, child_ptr, child_idx, roots, levels=6, beam=5,
+                          threshold=0.0, mode=SCORE_NORM, stream=None):
+        """hdc_beam_search_split: nodes < proto32.shape[0] have int32 rows, the
+        others int16 rows in proto16 (node n is row n - proto32.shape[0])."""
+        import torch
+        nq = q.shape[0]
+        n_wide = proto32.shape[0] if proto32 is not None else 0
+        n_nodes = n_wide + (proto16.shape[0] if proto16 is not None else 0)
+        path = torch.empty((nq, levels), dtype=torch.int32, device=q.device)
+        score = torch.empty((nq, levels), dtype=torch.float32, device=q.device)
+        depth = torch.empty(nq, dtype=torch.int32, device=q.device)
+        check(lib().hdc_beam_search_split(self.h, ptr(q), ptr(qn), nq, ptr(proto32), n_wide, ptr(proto16), ptr(pn),
+                                          n_nodes, ptr(child_ptr), ptr(child_idx), ptr(roots), roots.numel(), levels,
+                                          beam, threshold, mode, ptr(path), ptr(score), ptr(depth),
+                                          stream_ptr(stream)))
         return path, score, depth
 
     def similarity(self, q, qn, rows, rn, ref_rows, ref_whole, pair_q, pair_ref, mode=SCORE_NORM, stream=None):

@@ -63,9 +63,10 @@ CONFIGS = {
 #   tc_search_kernel, c3 (38,912 reads x 200,000 refs = 304 x 1,564 tile pairs; the
 #     288 leading query tiles in clusters of 4 + the other 16 in pairs): 1.01427e12 B
 #   grouped descent, c5 (one call's 5 descent_tc_kernel launches + the leaf-level score_kernel,
-#     38,912 reads): 3.64798e10 B
+#     38,912 reads): 3.64798e10 B with every row int32, 2.03736e10 B with int16 leaf rows
 TRAFFIC_PER_TILE_PAIR_TC = (975.445256e9 + 0.170780e9 + 38.640838e9 + 0.012020e9) / (304 * 1564)
-TRAFFIC_DESCENT = {38912: 36.409726e9 + 70.093e6}  # reads per call -> bytes (mostly the database, once)
+# (reads per call, int16 rows) -> bytes (mostly the database, once)
+TRAFFIC_DESCENT = {(38912, False): 36.409726e9 + 70.093e6, (38912, True): 2.037361e10}
 
 
 def log(*a):
@@ -477,6 +478,17 @@ def run_descent(args, cfg, rank, world):
     tree, proto, pn, (b, base, counts, ptr, idx), bundle = build_prototypes(H, ctx, cfg, dev)
     d_ptr, d_idx = torch.from_numpy(ptr).to(dev), torch.from_numpy(idx).to(dev)
     roots = torch.arange(0, counts[0], dtype=torch.int32, device=dev)
+    n_nodes = proto.shape[0]
+    # the leaves are scored from an int16 copy of their rows (hdc_beam_search_split) when they
+    # fit 16 bits (whole-sequence counts): their level streams its rows from HBM, so it reads
+    # half the bytes.  The ranks above stay int32: the tensor-core levels are bound by their
+    # producers' conversions, not by bytes, and an int32 row converts in fewer instructions.
+    split = not args.proto_int32 and args.beam_grouped != 0 and dim % 1024 == 0 and dim <= 16384
+    n_wide = max(first_int16_row(proto), int(base[5])) if split else n_nodes
+    proto32 = proto[:n_wide]
+    proto16 = torch.empty((n_nodes - n_wide, dim), dtype=torch.int16, device=dev)
+    for i in range(0, n_nodes - n_wide, 8192):
+        proto16[i:i + 8192].copy_(proto[n_wide + i:n_wide + i + 8192])
     n_pool = 2
     pool = [make_reads(H, tree, cfg, B, cfg["read_seed"] + 1000 * rank + p) for p in range(n_pool)]
     max_len = max(r.max_len() for r in pool)
@@ -490,7 +502,11 @@ def run_descent(args, cfg, rank, world):
         ctx.encode_segments(d_buf, d_off, d_len, q8, H.OUT_BIPOLAR_I8, max_len)
         if ev:
             ev[0].record()
-        out["r"] = ctx.beam_search(q8, qn, proto, pn, d_ptr, d_idx, roots, L, W, cfg["threshold"])
+        if split:
+            out["r"] = ctx.beam_search_split(q8, qn, proto32, proto16, pn, d_ptr, d_idx, roots, L, W,
+                                             cfg["threshold"])
+        else:
+            out["r"] = ctx.beam_search(q8, qn, proto, pn, d_ptr, d_idx, roots, L, W, cfg["threshold"])
         if ev:
             ev[1].record()
         return out["r"]
@@ -575,7 +591,8 @@ def run_descent(args, cfg, rank, world):
     res = dict(ms=ms, e2e_ms=e2e_ms, search_ms=float(np.median(beam_ms)), clocks=clk.summary(),
                launches=per_step * args.steps, refs=int(base[-1]), h2d=io["h2d"], d2h=io["d2h"], tree=tree,
                bundle=bundle, depth_mean=depth_mean, rows_per_read=int(sum(cand)), leaf_accuracy=leaf_acc,
-               mean_len=float(np.mean(pool[0].len)))
+               mean_len=float(np.mean(pool[0].len)), n_wide=n_wide,
+               proto_bytes=n_wide * dim * 4 + (n_nodes - n_wide) * dim * 2)
     if rank == 0 and not args.no_cpu_baseline:
         # q8 and out["r"] hold the last step's batch and result
         res["cpu"] = cpu_baseline_descent(cfg, pool[0], q8[:256].cpu().numpy(), proto, pn, ptr, idx,
@@ -586,6 +603,16 @@ def run_descent(args, cfg, rank, world):
                                                                                 np.array(ws, np.float32))
             for i, (wp, ws) in enumerate(res["cpu"].pop("paths")))
     return res
+
+
+def first_int16_row(proto, chunk=8192):
+    """The smallest n such that every row of proto from n on fits int16."""
+    import torch
+    fits = torch.empty(proto.shape[0], dtype=torch.bool, device=proto.device)
+    for i in range(0, proto.shape[0], chunk):
+        fits[i:i + chunk] = proto[i:i + chunk].abs().amax(dim=1) <= 32767
+    bad = torch.nonzero(~fits).flatten()
+    return int(bad[-1]) + 1 if bad.numel() else 0
 
 
 def cpu_baseline_descent(cfg, reads, q8, proto, pn, ptr, idx, roots, seconds=12.0):
@@ -688,7 +715,8 @@ def descent_line(args, cfg, r, metric, workload, world):
     B, dim = args.batch, cfg["dim"]
     # grouped descent: every prototype row is a candidate at its own rank's level only, so a
     # call reads each at most once, plus each level's packed +1/-1 reads
-    algo_bytes = r["refs"] * dim * 4 + cfg["levels"] * B * dim / 8
+    algo_bytes = r["proto_bytes"] + cfg["levels"] * B * dim / 8
+    split = r["n_wide"] < r["refs"]
     achieved = algo_bytes / (r["search_ms"] / 1e3) / 1e9
     bundle_bytes = sum(x["bytes"] for x in r["bundle"])
     bundle_ms = sum(x["ms"] for x in r["bundle"])
@@ -696,28 +724,31 @@ def descent_line(args, cfg, r, metric, workload, world):
         "metric": metric, "value": B * world / (r["ms"] / 1e3), "unit": "reads/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "int8 +1/-1 reads x int32 prototypes, exact int64 dots, FP64 scores",
+        "dtype": "int8 +1/-1 reads x %s prototypes, exact int64 dots, FP64 scores" % (
+            "int32 (ranks above) / int16 (nodes %d on)" % r["n_wide"] if split else "int32"),
         "data": "synthetic (seeded 6-rank tree, see bench.py)",
         "config": {"workload": workload, "form": "descent", "batch_reads": B, "nodes": r["refs"],
                    "mean_read_len": r["mean_len"], "mean_depth": r["depth_mean"],
                    "leaf_accuracy": r["leaf_accuracy"],
+                   "int16_rows_from_node": r["n_wide"],
                    "l2": "inputs larger than L2: %.1f GB of prototypes, the lower ranks gathered from HBM "
-                         "every step" % (r["refs"] * dim * 4 / 1e9)},
+                         "every step" % (r["proto_bytes"] / 1e9)},
         "e2e": {"value": B * world / (r["e2e_ms"] / 1e3), "unit": "reads/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                     "frac": achieved / pk["hbm_gbs"], "traffic": TRAFFIC_DESCENT.get(B),
+                     "frac": achieved / pk["hbm_gbs"], "traffic": TRAFFIC_DESCENT.get((B, split)),
                      "traffic_source": "ncu DRAM bytes of the scoring launches of one full-size call "
                                        "(descent_tc_kernel x 5 + score_kernel; measured at 38,912 reads; "
                                        "null at other batch sizes)",
                      "peak_source": "%s HBM copy bandwidth (MEASURED_PEAKS.json)" % src,
-                     "kernel": "grouped descent (hdc_beam_search: per level count/expand/select; levels "
+                     "kernel": "grouped descent (hdc_beam_search%s: per level count/expand/select; levels "
                                "above the leaves scored by descent_tc_kernel on the tensor cores, the "
                                "leaves by score_kernel), timed as one call; algorithmic bytes = the %.1f GB "
                                "of prototypes once + %d levels of packed reads; the tensor-core levels are "
                                "bound by their producers' conversions, the leaf level by HBM "
                                "(%d candidate rows per read)" % (
-                                   r["refs"] * dim * 4 / 1e9, cfg["levels"], r["rows_per_read"])},
+                                   "_split" if split else "", r["proto_bytes"] / 1e9, cfg["levels"],
+                                   r["rows_per_read"])},
         "propagate_bundle": {"kernel": "bundle_kernel (internal prototypes = int32 sums of children)",
                              "ms": bundle_ms, "gb_per_s": bundle_bytes / (bundle_ms / 1e3) / 1e9,
                              "frac_of_hbm": bundle_bytes / (bundle_ms / 1e3) / 1e9 / pk["hbm_gbs"],
@@ -807,6 +838,8 @@ def main():
     ap.add_argument("--tc-cluster", type=int, default=0, help="tensor-core search: CTAs sharing reference blocks (0: default)")
     ap.add_argument("--beam-grouped", type=int, default=-1,
                     help="descent: 1 reads grouped by candidate node, 0 one warp per read (-1: default)")
+    ap.add_argument("--proto-int32", action="store_true",
+                    help="descent: every prototype row int32 (default: int16 rows from the first node whose rows fit)")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3")

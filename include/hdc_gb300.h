@@ -296,6 +296,24 @@ int hdc_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qnorm2
                     double threshold, int score_mode, int32_t* d_path, float* d_path_score, int32_t* d_depth,
                     void* stream);
 
+/* The same descent (targets/identify.cpp:89-202, as hdc_beam_search) over
+ * prototypes stored in two widths.  Leaf prototypes are whole-sequence k-mer
+ * counts (|v| <= sequence length) and the lowest internal ranks sums of a
+ * few of them, so most of a taxonomy fits 16 bits and the descent, which
+ * streams those rows from HBM, reads half the bytes.  Nodes [0, n_wide)
+ * have int32 rows d_proto32 [n_wide][dim]; nodes [n_wide, n_nodes) int16
+ * rows d_proto16 [n_nodes - n_wide][dim] (node n is row n - n_wide).  The
+ * results are identical to hdc_beam_search on the same values.  Needs the
+ * grouped descent: dim % 1024 == 0, dim <= 16384, 16-byte aligned rows and
+ * reads, HDC_BEAM_GROUPED != 0 (HDC_ERR_INVALID otherwise, unless every row
+ * is int32, n_wide == n_nodes). */
+int hdc_beam_search_split(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qnorm2, int64_t nq,
+                          const int32_t* d_proto32, int64_t n_wide, const int16_t* d_proto16,
+                          const int64_t* d_proto_norm2, int64_t n_nodes, const int64_t* d_child_ptr,
+                          const int32_t* d_child_idx, const int32_t* d_roots, int n_roots, int levels, int beam,
+                          double threshold, int score_mode, int32_t* d_path, float* d_path_score, int32_t* d_depth,
+                          void* stream);
+
 /* Windowed similarity, HVCache::similarity (src/encoder.cpp:198-215), for a
  * list of (query, reference sequence) pairs.  A reference's "similarity rows"
  * are the int16 hypervectors of its windows x = 0, step, ... while

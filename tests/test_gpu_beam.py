@@ -27,6 +27,16 @@ def _drop_children(ptr, idx, nodes):
     return out_ptr, np.array([x for k in kids for x in k], np.int32)
 
 
+def _first_int16_node(proto):
+    """The smallest n such that every row >= n fits int16."""
+    import torch
+    fits = (proto.abs().amax(dim=1) <= 32767).cpu().numpy()
+    n = len(fits)
+    while n > 0 and fits[n - 1]:
+        n -= 1
+    return n
+
+
 # grouped: 1 reads grouped by candidate node, 2 the same with the levels above the last on
 # the tensor cores, 0 one warp per read (identical results)
 @pytest.mark.parametrize("grouped", [0, 1, 2])
@@ -64,6 +74,13 @@ def test_beam_descent_matches_oracle(hdc, orc, cuda, dim, kmer, n_leaves, beam, 
         ptr, idx = _drop_children(ptr, idx, list(range(int(base[2]), int(base[3]), 3)) + [int(base[1])])
     path, score, depth = ctx.beam_search(q8, qn, proto, pn, torch.from_numpy(ptr).to(cuda),
                                          torch.from_numpy(idx).to(cuda), roots, 6, beam, threshold)
+    if grouped:  # the same descent over int16 rows from the first node whose rows all fit 16 bits
+        n_wide = _first_int16_node(proto)
+        split = ctx.beam_search_split(q8, qn, proto[:n_wide].contiguous(), proto[n_wide:].to(torch.int16), pn,
+                                      torch.from_numpy(ptr).to(cuda), torch.from_numpy(idx).to(cuda), roots, 6, beam,
+                                      threshold)
+        for x, y in zip((path, score, depth), split):
+            assert torch.equal(x, y)
     torch.cuda.synchronize()
     want = orc.beam_search(q8.cpu().numpy(), proto.cpu().numpy(), ptr, idx, list(range(counts[0])), 6, beam,
                            threshold)
@@ -166,3 +183,99 @@ def test_beam_tensor_core_levels_wide_nodes_and_limbs(hdc, cuda):
         for x, y in zip(a, b_):
             assert np.array_equal(x, y)
 
+
+
+def test_beam_split_rows_equal_int32(hdc, cuda):
+    """hdc_beam_search_split (nodes from n_wide on as int16 rows) returns the
+    paths, scores and depths of hdc_beam_search on the same values, in both
+    grouped forms, with the cut at the leaves, at the first node whose rows
+    fit 16 bits, at 0 (every row int16) where they all fit, and at n_nodes
+    (every row int32); the one-warp-per-read form refuses int16 rows."""
+    import torch
+    H = hdc
+    dim, n_leaves, nq = 2048, 20000, 3000
+    b, base, counts, ptr, idx = H.synth_tree_csr(n_leaves)
+    tree = H.synth_tree(17, n_leaves)
+    reads = H.synth_reads(18, tree, nq, 250, subst=0.01, sigma=0.5, min_read=100, max_read=800,
+                          mixed_frac=0.2, mixed_rate=0.06)
+    ctx = H.Context(dim, 12, 250, 10)
+    proto = torch.zeros((int(base[-1]), dim), dtype=torch.int32, device=cuda)
+    ctx.encode_segments(torch.from_numpy(tree.buf).to(cuda), torch.from_numpy(tree.off).to(cuda),
+                        torch.from_numpy(tree.len).to(cuda), proto[int(base[5]):], H.OUT_I32, tree.max_len())
+    d_idx = torch.from_numpy(idx).to(cuda)
+    for r in range(4, -1, -1):
+        lo, hi = int(base[r]), int(base[r + 1])
+        ctx.bundle(proto, torch.from_numpy(ptr[lo:hi + 1].copy()).to(cuda), d_idx, out=proto[lo:hi])
+    q8 = torch.empty((nq, dim), dtype=torch.int8, device=cuda)
+    ctx.encode_segments(torch.from_numpy(reads.buf).to(cuda), torch.from_numpy(reads.off).to(cuda),
+                        torch.from_numpy(reads.len).to(cuda), q8, H.OUT_BIPOLAR_I8, reads.max_len())
+    qn, pn = ctx.norms(q8), ctx.norms(proto)
+    roots = torch.arange(0, counts[0], dtype=torch.int32, device=cuda)
+    d_ptr = torch.from_numpy(ptr).to(cuda)
+    first16 = _first_int16_node(proto)
+    assert first16 < int(base[5])  # the lowest internal rank fits 16 bits too
+    n_nodes = proto.shape[0]
+    for grouped in (1, 2):
+        ctx.option(H.BEAM_GROUPED, grouped)
+        for threshold in (0.0, float("-inf")):
+            want = ctx.beam_search(q8, qn, proto, pn, d_ptr, d_idx, roots, 6, 5, threshold)
+            for n_wide in (int(base[5]), first16, n_nodes):
+                got = ctx.beam_search_split(q8, qn, proto[:n_wide].contiguous(), proto[n_wide:].to(torch.int16),
+                                            pn, d_ptr, d_idx, roots, 6, 5, threshold)
+                for x, y in zip(want, got):
+                    assert torch.equal(x, y), (grouped, threshold, n_wide)
+    ctx.option(H.BEAM_GROUPED, 0)
+    with pytest.raises(H.HDCError):
+        ctx.beam_search_split(q8, qn, proto[:first16].contiguous(), proto[first16:].to(torch.int16), pn, d_ptr,
+                              d_idx, roots, 6, 5, 0.0)
+    torch.cuda.synchronize()
+    assert ctx.status() == 0
+
+
+def test_beam_split_tensor_core_levels_int16_children(hdc, cuda):
+    """The tensor-core levels with int16 children: the wide tree (3 roots of 40
+    children, items of 32 + 8) with values in the int16 range, rows at its
+    edges (32767, -32768, alternating), every row int16 (n_wide = 0), all but
+    the roots, or a cut between the 21st and 22nd child of the first root (one
+    item, and one producer warp, with both widths), against the int32 descent."""
+    import torch
+    H = hdc
+    g = np.random.default_rng(62)
+    dim, nq = 1024, 300
+    n0, n1 = 3, 3 * 40
+    n2 = 2 * n1
+    ptr = np.zeros(n0 + n1 + n2 + 1, np.int64)
+    idx = []
+    for r in range(n0):
+        idx += list(range(n0 + 40 * r, n0 + 40 * (r + 1)))
+        ptr[r + 1] = len(idx)
+    for v in range(n1):
+        idx += [n0 + n1 + 2 * v, n0 + n1 + 2 * v + 1]
+        ptr[n0 + v + 1] = len(idx)
+    ptr[n0 + n1 + 1:] = len(idx)
+    idx = np.array(idx, np.int32)
+    proto_h = g.integers(-32768, 32768, (n0 + n1 + n2, dim)).astype(np.int32)
+    proto_h[5, :] = 32767
+    proto_h[6, :] = -32768
+    proto_h[7, ::2] = 32767
+    proto_h[7, 1::2] = -32768
+    proto_h[n0 + n1 + 3, :] = -32768
+    q = np.where(g.random((nq, dim)) < 0.5, -1, 1).astype(np.int8)
+    q[:40] = np.where(proto_h[n0 + 7] >= 0, 1, -1)
+    proto = torch.from_numpy(proto_h).to(cuda)
+    q8 = torch.from_numpy(q).to(cuda)
+    ctx = H.Context(dim, 10, 250, 10)
+    qn, pn = ctx.norms(q8), ctx.norms(proto)
+    roots = torch.arange(0, n0, dtype=torch.int32, device=cuda)
+    d_ptr, d_idx = torch.from_numpy(ptr).to(cuda), torch.from_numpy(idx).to(cuda)
+    for grouped in (1, 2):
+        ctx.option(H.BEAM_GROUPED, grouped)
+        for levels, beam, threshold in ((1, 5, float("-inf")), (2, 8, 0.0), (3, 5, float("-inf")), (3, 3, -0.5)):
+            want = ctx.beam_search(q8, qn, proto, pn, d_ptr, d_idx, roots, levels, beam, threshold)
+            for n_wide in (0, n0, n0 + 21):
+                got = ctx.beam_search_split(q8, qn, proto[:n_wide].contiguous(), proto[n_wide:].to(torch.int16),
+                                            pn, d_ptr, d_idx, roots, levels, beam, threshold)
+                for x, y in zip(want, got):
+                    assert torch.equal(x, y), (grouped, levels, beam, threshold, n_wide)
+    torch.cuda.synchronize()
+    assert ctx.status() == 0
