@@ -194,8 +194,8 @@ __global__ void __launch_bounds__(32 * kBeamWarps) beam_kernel(const BeamArgs a)
 int launch_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn, int64_t nq, const int32_t* d_proto,
                        int64_t n32, const int16_t* d_proto16, const int64_t* d_pn, int64_t n_nodes,
                        const int64_t* d_child_ptr, const int32_t* d_child_idx, const int32_t* d_roots, int n_roots,
-                       int levels, int beam, double threshold, int mode, int32_t* d_path, float* d_path_score,
-                       int32_t* d_depth, cudaStream_t stream) {
+                       int max_children, int levels, int beam, double threshold, int mode, int32_t* d_path,
+                       float* d_path_score, int32_t* d_depth, cudaStream_t stream) {
     if (nq == 0) return HDC_OK;
     if (levels < 1 || levels > kMaxLevels) return fail(HDC_ERR_INVALID, "beam: levels must be in 1..8");
     if (beam < 1 || beam > kMaxBeam) return fail(HDC_ERR_INVALID, "beam: beam width must be in 1..8");
@@ -204,8 +204,8 @@ int launch_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn,
                             (reinterpret_cast<uintptr_t>(d_proto16) & 15) == 0 && (reinterpret_cast<uintptr_t>(d_q) & 15) == 0;
     if (ctx->beam_grouped != 0 && grouped_ok)
         return launch_beam_grouped(ctx, d_q, d_qn, nq, d_proto, n32, d_proto16, d_pn, n_nodes, d_child_ptr,
-                                   d_child_idx, d_roots, n_roots, levels, beam, threshold, mode, d_path, d_path_score,
-                                   d_depth, stream);
+                                   d_child_idx, d_roots, n_roots, max_children, levels, beam, threshold, mode, d_path,
+                                   d_path_score, d_depth, stream);
     if (n32 < n_nodes)
         return fail(HDC_ERR_INVALID, "beam: int16 rows need the grouped descent (dim % 1024 == 0, dim <= 16384, "
                                      "16-byte aligned rows and reads, HDC_BEAM_GROUPED != 0)");

@@ -28,7 +28,7 @@ constexpr int kMaxBeamG = 8;
 constexpr int kMaxLevelsG = 8;
 constexpr int kScoreThreads = 256;          // 8 warps, one pair each at a time
 constexpr int kScoreBlocks = 8;             // resident per SM; the grid is one wave
-constexpr int kScoreBlocks16 = 6;           // the same with int16 rows (40 registers a thread)
+constexpr int kScoreBlocks16 = 5;           // the same with int16 rows (48 registers a thread)
 constexpr int kScanItems = 16;              // elements per thread of the scan
 constexpr int kScanBlock = 256 * kScanItems;
 
@@ -178,6 +178,17 @@ struct GArgs {
     int32_t* sorted;          // [P] pair indices ordered by node
 };
 
+// A caller-given largest child count below the tree's sizes the pair arrays too small: every
+// read is marked done before level 0 (no candidates, depth 0) and the context status records
+// kStatusChildCount.
+constexpr int kStatusChildCount = 200;
+__global__ void check_children_kernel(const GArgs a, const int32_t* __restrict__ maxc, int32_t given, int* status) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (*maxc <= given || r >= a.nq) return;
+    a.done[r] = 1;
+    if (r == 0) atomicCAS(status, 0, kStatusChildCount);
+}
+
 __device__ __forceinline__ int64_t state_at(int64_t r, int b, int l) {
     return (r * kMaxBeamG + b) * kMaxLevelsG + l;
 }
@@ -200,28 +211,31 @@ __global__ void count_kernel(const GArgs a, int L) {
     a.cnt[r] = c;
 }
 
-__device__ __forceinline__ void put_pair(const GArgs& a, int32_t p, int64_t r, int32_t node, int slot) {
+// count_nodes: the level is scored from node-sorted pairs (score_kernel), which need the
+// pairs per node; a tensor-core level groups the entries by parent instead
+__device__ __forceinline__ void put_pair(const GArgs& a, int32_t p, int64_t r, int32_t node, int slot,
+                                         bool count_nodes) {
     a.pair_read[p] = (int32_t)r;
     a.pair_node[p] = node;
     a.pair_slot[p] = slot;
-    atomicAdd(a.node_cnt + node, 1);
+    if (count_nodes) atomicAdd(a.node_cnt + node, 1);
 }
 
-__global__ void expand_kernel(const GArgs a, int L) {
+__global__ void expand_kernel(const GArgs a, int L, bool count_nodes) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= a.nq || a.done[r]) return;
     int32_t p = a.off[r];
     if (L == 0) {
-        for (int i = 0; i < a.n_roots; ++i) put_pair(a, p++, r, a.roots[i], 0);
+        for (int i = 0; i < a.n_roots; ++i) put_pair(a, p++, r, a.roots[i], 0, count_nodes);
         return;
     }
     for (int b = 0; b < a.nbeam[r]; ++b) {
         const int32_t node = a.paths[state_at(r, b, L - 1)];
         const int64_t c0 = a.child_ptr[node], c1 = a.child_ptr[node + 1];
         if (c0 == c1) {
-            put_pair(a, p++, r, node, b);
+            put_pair(a, p++, r, node, b, count_nodes);
         } else {
-            for (int64_t c = c0; c < c1; ++c) put_pair(a, p++, r, a.child_idx[c], b);
+            for (int64_t c = c0; c < c1; ++c) put_pair(a, p++, r, a.child_idx[c], b, count_nodes);
         }
     }
 }
@@ -297,25 +311,26 @@ __device__ __forceinline__ int signs4_bytes(uint32_t nib) {
 }
 
 // Lane l's share of the dot of an int16 row: dims 256 j + 8 l .. + 7 (one 16-byte load, one
-// byte of the read's bits).  Each word holds two int16 values (the lower dim in the low half);
-// dp2a multiplies them by two of the signed sign bytes and accumulates, exactly.  |p| <= 2^15
-// and at most 512 terms a lane: int32 throughout.
-__device__ __forceinline__ int64_t lane_dot16(const GArgs& a, int lane, int32_t node, int64_t r) {
-    const int nsteps = a.dim / 256;  // a multiple of 4 (dim % 1024 == 0)
+// byte of the read's bits), U loads in flight.  Each word holds two int16 values (the lower
+// dim in the low half); dp2a multiplies them by two of the signed sign bytes and accumulates,
+// exactly.  |p| <= 2^15 and at most 512 terms a lane: int32 throughout.
+template <int U>
+__device__ __forceinline__ int64_t lane_dot16_u(const GArgs& a, int lane, int32_t node, int64_t r) {
+    const int nsteps = a.dim / 256;  // a multiple of U
     const int sh = (lane & 3) * 8;
     const int4* row = reinterpret_cast<const int4*>(a.proto16 + (node - a.n32) * a.dim) + lane;
     const uint32_t* qb = a.bits + r * a.words + (lane >> 2);
     int acc = 0;
-    for (int j = 0; j < nsteps; j += 4) {
-        int4 x[4];
-        uint32_t w[4];
+    for (int j = 0; j < nsteps; j += U) {
+        int4 x[U];
+        uint32_t w[U];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < U; ++u) {
             x[u] = __ldg(row + 32 * (j + u));
             w[u] = __ldg(qb + 8 * (j + u));
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < U; ++u) {
             const uint32_t byte = w[u] >> sh;
             const int s0 = signs4_bytes(byte & 15u), s1 = signs4_bytes((byte >> 4) & 15u);
             acc = __dp2a_lo(x[u].x, s0, acc);  // dims 0, 1
@@ -325,6 +340,12 @@ __device__ __forceinline__ int64_t lane_dot16(const GArgs& a, int lane, int32_t 
         }
     }
     return acc;
+}
+
+// eight loads in flight where the row has a multiple of 8 steps (dim % 2048 == 0), else four
+// (dim % 1024 == 0 gives a multiple of 4)
+__device__ __forceinline__ int64_t lane_dot16(const GArgs& a, int lane, int32_t node, int64_t r) {
+    return (a.dim / 256) % 8 == 0 ? lane_dot16_u<8>(a, lane, node, r) : lane_dot16_u<4>(a, lane, node, r);
 }
 
 // ROWS16: some nodes have int16 rows (hdc_beam_search_split); without, the kernel is the
@@ -919,21 +940,26 @@ T* carve(uint8_t*& cur, int64_t n) {
 
 int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn, int64_t nq, const int32_t* d_proto,
                         int64_t n32, const int16_t* d_proto16, const int64_t* d_pn, int64_t n_nodes, const int64_t* d_child_ptr, const int32_t* d_child_idx,
-                        const int32_t* d_roots, int n_roots, int levels, int beam, double threshold, int mode,
-                        int32_t* d_path, float* d_path_score, int32_t* d_depth, cudaStream_t stream) {
+                        const int32_t* d_roots, int n_roots, int max_children, int levels, int beam,
+                        double threshold, int mode, int32_t* d_path, float* d_path_score, int32_t* d_depth,
+                        cudaStream_t stream) {
     if ((int64_t)n_nodes > (int64_t)kScanBlock * kScanBlock || nq > (int64_t)kScanBlock * kScanBlock)
         return fail(HDC_ERR_INVALID, "beam: too many reads or nodes for one grouped launch");
     cudaError_t e;
-    // the largest child count bounds a read's candidates, hence the pair arrays
-    int32_t* d_maxc = nullptr;
-    if ((e = cudaMallocAsync(&d_maxc, sizeof(int32_t), stream)) != cudaSuccess) return cuda_fail(e, "beam: workspace");
-    cudaMemsetAsync(d_maxc, 0, sizeof(int32_t), stream);
-    max_children_kernel<<<std::max(1, std::min(ctx->num_sms * 4, (int)((n_nodes + 255) / 256))), 256, 0, stream>>>(
-        d_child_ptr, n_nodes, d_maxc);
-    int32_t maxc = 0;
-    cudaMemcpyAsync(&maxc, d_maxc, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
-    cudaFreeAsync(d_maxc, stream);
-    if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return cuda_fail(e, "beam: child count");
+    // the largest child count bounds a read's candidates, hence the pair arrays: the caller's
+    // value (checked on the device below), or read back from the device
+    const unsigned mc_grid = (unsigned)std::max(1, std::min(ctx->num_sms * 4, (int)((n_nodes + 255) / 256)));
+    int32_t maxc = max_children;
+    if (maxc <= 0) {
+        int32_t* d_maxc = nullptr;
+        if ((e = cudaMallocAsync(&d_maxc, sizeof(int32_t), stream)) != cudaSuccess)
+            return cuda_fail(e, "beam: workspace");
+        cudaMemsetAsync(d_maxc, 0, sizeof(int32_t), stream);
+        max_children_kernel<<<mc_grid, 256, 0, stream>>>(d_child_ptr, n_nodes, d_maxc);
+        cudaMemcpyAsync(&maxc, d_maxc, sizeof(int32_t), cudaMemcpyDeviceToHost, stream);
+        cudaFreeAsync(d_maxc, stream);
+        if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return cuda_fail(e, "beam: child count");
+    }
     const int64_t per_read = std::max<int64_t>(n_roots, (int64_t)beam * std::max(maxc, 1));
     const int64_t P = nq * per_read;
     if (P > 0x7fffffffLL) return fail(HDC_ERR_INVALID, "beam: too many candidate pairs for one grouped launch");
@@ -959,6 +985,7 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn
     a.roots = d_roots;
     const int64_t sums = std::max(scan_blocks_needed(nq), scan_blocks_needed(n_nodes));
     int32_t* d_sums = nullptr;
+    int32_t* d_maxc_dev = nullptr;
     uint32_t* bits = nullptr;
     // every level but the last on the tensor cores (HDC_BEAM_GROUPED 2 or automatic)
     const bool use_tc = (ctx->beam_grouped == 2 || ctx->beam_grouped < 0) && a.dim % 64 == 0 && a.dim <= 16384;
@@ -986,6 +1013,7 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn
         a.sorted = carve<int32_t>(cur, P);
         a.pair_key = carve<uint64_t>(cur, P);
         d_sums = carve<int32_t>(cur, sums);
+        d_maxc_dev = carve<int32_t>(cur, 1);
         if (use_tc) {
             t.ent_read = carve<int32_t>(cur, nq * beam);
             t.ent_p0 = carve<int32_t>(cur, nq * beam);
@@ -1013,6 +1041,11 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn
     cudaMemsetAsync(a.nbeam, 0, nq * 4, stream);
     cudaMemsetAsync(a.done, 0, nq * 4, stream);
     cudaMemsetAsync(a.out_depth, 0, nq * 4, stream);
+    if (max_children > 0) {  // a count below the tree's: every read stops at depth 0 (no pair is written)
+        cudaMemsetAsync(d_maxc_dev, 0, sizeof(int32_t), stream);
+        max_children_kernel<<<mc_grid, 256, 0, stream>>>(d_child_ptr, n_nodes, d_maxc_dev);
+        check_children_kernel<<<rb, 256, 0, stream>>>(a, d_maxc_dev, max_children, ctx->d_status);
+    }
     pack_bits_kernel<<<(unsigned)((nq * a.words + 255) / 256), 256, 0, stream>>>(d_q, nq, a.dim, bits);
     const int work_grid = ctx->num_sms * 8;
     const unsigned nb = (unsigned)((n_nodes + 255) / 256);
@@ -1022,11 +1055,12 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn
         return cuda_fail(e, "beam: tensor-core scoring setup");
     }
     for (int L = 0; L < levels; ++L) {
+        const bool tc_level = use_tc && L < levels - 1;
         count_kernel<<<rb, 256, 0, stream>>>(a, L);
         exclusive_scan(a.cnt, a.off, nq, d_sums, stream);
-        cudaMemsetAsync(a.node_cnt, 0, (size_t)n_nodes * 4, stream);
-        expand_kernel<<<rb, 256, 0, stream>>>(a, L);
-        if (use_tc && L < levels - 1) {
+        if (!tc_level) cudaMemsetAsync(a.node_cnt, 0, (size_t)n_nodes * 4, stream);
+        expand_kernel<<<rb, 256, 0, stream>>>(a, L, !tc_level);
+        if (tc_level) {
             // entries grouped by parent, then items of up to 128 entries x 32 children
             if (L == 0) {
                 const int64_t n0 = ((nq + kTcE - 1) / kTcE) * ((n_roots + kTcC - 1) / kTcC);

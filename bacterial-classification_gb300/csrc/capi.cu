@@ -330,27 +330,29 @@ int hdc_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qnorm2
         !d_path_score || !d_depth)
         return fail(HDC_ERR_INVALID, "beam: null pointer");
     return hdc::launch_beam_search(ctx, d_q, d_qnorm2, nq, d_proto, n_nodes, nullptr, d_proto_norm2, n_nodes,
-                                   d_child_ptr, d_child_idx, d_roots, n_roots, levels, beam, threshold, score_mode,
+                                   d_child_ptr, d_child_idx, d_roots, n_roots, 0, levels, beam, threshold, score_mode,
                                    d_path, d_path_score, d_depth, static_cast<cudaStream_t>(stream));
 }
 
 int hdc_beam_search_split(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qnorm2, int64_t nq,
                           const int32_t* d_proto32, int64_t n_wide, const int16_t* d_proto16,
                           const int64_t* d_proto_norm2, int64_t n_nodes, const int64_t* d_child_ptr,
-                          const int32_t* d_child_idx, const int32_t* d_roots, int n_roots, int levels, int beam,
-                          double threshold, int score_mode, int32_t* d_path, float* d_path_score, int32_t* d_depth,
-                          void* stream) {
+                          const int32_t* d_child_idx, const int32_t* d_roots, int n_roots, int max_children,
+                          int levels, int beam, double threshold, int score_mode, int32_t* d_path,
+                          float* d_path_score, int32_t* d_depth, void* stream) {
     if (!ctx) return fail(HDC_ERR_INVALID, "beam split: null context");
     if (nq < 0 || n_nodes < 0) return fail(HDC_ERR_INVALID, "beam split: negative count");
     if (nq == 0) return HDC_OK;
     if (n_nodes < 1 || n_nodes > 0x7fffffffLL) return fail(HDC_ERR_INVALID, "beam split: node count out of range");
     if (n_wide < 0 || n_wide > n_nodes) return fail(HDC_ERR_INVALID, "beam split: n_wide must be in 0..n_nodes");
     if (!hdc::valid_score_mode(score_mode)) return fail(HDC_ERR_INVALID, "beam split: bad score mode");
+    if (max_children < 0) return fail(HDC_ERR_INVALID, "beam split: negative max_children");
     if (!d_q || !d_qnorm2 || (n_wide > 0 && !d_proto32) || (n_wide < n_nodes && !d_proto16) || !d_proto_norm2 ||
         !d_child_ptr || !d_child_idx || !d_roots || !d_path || !d_path_score || !d_depth)
         return fail(HDC_ERR_INVALID, "beam split: null pointer");
     return hdc::launch_beam_search(ctx, d_q, d_qnorm2, nq, d_proto32, n_wide, d_proto16, d_proto_norm2, n_nodes,
-                                   d_child_ptr, d_child_idx, d_roots, n_roots, levels, beam, threshold, score_mode,
+                                   d_child_ptr, d_child_idx, d_roots, n_roots, max_children, levels, beam, threshold,
+                                   score_mode,
                                    d_path, d_path_score, d_depth, static_cast<cudaStream_t>(stream));
 }
 

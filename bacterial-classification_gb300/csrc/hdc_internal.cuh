@@ -113,7 +113,7 @@ int launch_propagate_greedy(hdc_context* ctx, const int16_t* d_hv, const int64_t
 
 int launch_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn, int64_t nq, const int32_t* d_proto,
                        int64_t n32, const int16_t* d_proto16, const int64_t* d_pn, int64_t n_nodes,
-                       const int64_t* d_child_ptr, const int32_t* d_child_idx, const int32_t* d_roots, int n_roots,
+                       const int64_t* d_child_ptr, const int32_t* d_child_idx, const int32_t* d_roots, int n_roots, int max_children,
                        int levels, int beam, double threshold, int mode, int32_t* d_path, float* d_path_score,
                        int32_t* d_depth, cudaStream_t stream);
 
@@ -132,7 +132,7 @@ int launch_similarity(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qn,
 // nodes < n32 have int32 rows in d_proto, the others int16 rows in d_proto16 (row node - n32)
 int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn, int64_t nq, const int32_t* d_proto,
                         int64_t n32, const int16_t* d_proto16, const int64_t* d_pn, int64_t n_nodes, const int64_t* d_child_ptr, const int32_t* d_child_idx,
-                        const int32_t* d_roots, int n_roots, int levels, int beam, double threshold, int mode,
+                        const int32_t* d_roots, int n_roots, int max_children, int levels, int beam, double threshold, int mode,
                         int32_t* d_path, float* d_path_score, int32_t* d_depth, cudaStream_t stream);
 
 int launch_fasta_parse(hdc_context* ctx, const char* d_in, int64_t n, char* d_out, int64_t* d_seq_off,

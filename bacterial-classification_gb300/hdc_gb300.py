@@ -39,8 +39,8 @@ SIGNATURES = [
                                SZ, P]),
     ("hdc_bundle", I32, [P, P, I32, P, P, I64, P, P]),
     ("hdc_beam_search", I32, [P, P, P, I64, P, P, I64, P, P, P, I32, I32, I32, ctypes.c_double, I32, P, P, P, P]),
-    ("hdc_beam_search_split", I32, [P, P, P, I64, P, I64, P, P, I64, P, P, P, I32, I32, I32, ctypes.c_double, I32, P,
-                                    P, P, P]),
+    ("hdc_beam_search_split", I32, [P, P, P, I64, P, I64, P, P, I64, P, P, P, I32, I32, I32, I32, ctypes.c_double,
+                                    I32, P, P, P, P]),
     ("hdc_similarity", I32, [P, P, P, P, P, P, P, P, P, I64, I32, P, P, P]),
     ("hdc_identify", I32, [P, P, P, I64, P, P, P, P, P, P, I32, I32, I32, ctypes.c_double, I32, P, P, P, P, P]),
     ("hdc_propagate_greedy", I32, [P, P, P, P, P, P, P, I64, ctypes.c_double, I32, P, P, P, P]),
@@ -255,9 +255,10 @@ class Context:
         return path, score, depth
 
     def beam_search_split(self, q, qn, proto32, proto16, pn, child_ptr, child_idx, roots, levels=6, beam=5,
-                          threshold=0.0, mode=SCORE_NORM, stream=None):
+                          threshold=0.0, mode=SCORE_NORM, stream=None, max_children=0):
         """hdc_beam_search_split: nodes < proto32.shape[0] have int32 rows, the
-        others int16 rows in proto16 (node n is row n - proto32.shape[0])."""
+        others int16 rows in proto16 (node n is row n - proto32.shape[0]);
+        max_children > 0 spares the call its host synchronisation."""
         import torch
         nq = q.shape[0]
         n_wide = proto32.shape[0] if proto32 is not None else 0
@@ -266,8 +267,8 @@ class Context:
         score = torch.empty((nq, levels), dtype=torch.float32, device=q.device)
         depth = torch.empty(nq, dtype=torch.int32, device=q.device)
         check(lib().hdc_beam_search_split(self.h, ptr(q), ptr(qn), nq, ptr(proto32), n_wide, ptr(proto16), ptr(pn),
-                                          n_nodes, ptr(child_ptr), ptr(child_idx), ptr(roots), roots.numel(), levels,
-                                          beam, threshold, mode, ptr(path), ptr(score), ptr(depth),
+                                          n_nodes, ptr(child_ptr), ptr(child_idx), ptr(roots), roots.numel(),
+                                          max_children, levels, beam, threshold, mode, ptr(path), ptr(score), ptr(depth),
                                           stream_ptr(stream)))
         return path, score, depth
 

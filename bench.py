@@ -63,10 +63,10 @@ CONFIGS = {
 #   tc_search_kernel, c3 (38,912 reads x 200,000 refs = 304 x 1,564 tile pairs; the
 #     288 leading query tiles in clusters of 4 + the other 16 in pairs): 1.01427e12 B
 #   grouped descent, c5 (one call's 5 descent_tc_kernel launches + the leaf-level score_kernel,
-#     38,912 reads): 3.64798e10 B with every row int32, 2.03736e10 B with int16 leaf rows
+#     38,912 reads): 3.64798e10 B with every row int32, 2.03567e10 B with int16 leaf rows
 TRAFFIC_PER_TILE_PAIR_TC = (975.445256e9 + 0.170780e9 + 38.640838e9 + 0.012020e9) / (304 * 1564)
 # (reads per call, int16 rows) -> bytes (mostly the database, once)
-TRAFFIC_DESCENT = {(38912, False): 36.409726e9 + 70.093e6, (38912, True): 2.037361e10}
+TRAFFIC_DESCENT = {(38912, False): 36.409726e9 + 70.093e6, (38912, True): 2.035667e10}
 
 
 def log(*a):
@@ -479,6 +479,7 @@ def run_descent(args, cfg, rank, world):
     d_ptr, d_idx = torch.from_numpy(ptr).to(dev), torch.from_numpy(idx).to(dev)
     roots = torch.arange(0, counts[0], dtype=torch.int32, device=dev)
     n_nodes = proto.shape[0]
+    max_children = int(np.diff(ptr).max())
     # the leaves are scored from an int16 copy of their rows (hdc_beam_search_split) when they
     # fit 16 bits (whole-sequence counts): their level streams its rows from HBM, so it reads
     # half the bytes.  The ranks above stay int32: the tensor-core levels are bound by their
@@ -502,9 +503,9 @@ def run_descent(args, cfg, rank, world):
         ctx.encode_segments(d_buf, d_off, d_len, q8, H.OUT_BIPOLAR_I8, max_len)
         if ev:
             ev[0].record()
-        if split:
+        if split:  # the tree's largest child count is known here: no host synchronisation in the call
             out["r"] = ctx.beam_search_split(q8, qn, proto32, proto16, pn, d_ptr, d_idx, roots, L, W,
-                                             cfg["threshold"])
+                                             cfg["threshold"], max_children=max_children)
         else:
             out["r"] = ctx.beam_search(q8, qn, proto, pn, d_ptr, d_idx, roots, L, W, cfg["threshold"])
         if ev:

@@ -139,8 +139,9 @@ int hdc_search_plain(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qnor
                      double* d_cos, int64_t* d_dot, void* d_work, size_t work_bytes, void* stream);
 
 /* Read and clear the device status word of the context (synchronizes the
- * device): 0, or 100 + the code of a bounded device-side wait that gave up
- * in a tensor-core search (the search then returned partial results). */
+ * device): 0, 100 + the code of a bounded device-side wait that gave up in
+ * a tensor-core search or descent (which then returned partial results), or
+ * 200 when hdc_beam_search_split was given a max_children below the tree's. */
 int hdc_context_status(hdc_context* ctx, int* status);
 
 /* Precision form, reference side: build a tensor-core database from int16
@@ -306,13 +307,18 @@ int hdc_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qnorm2
  * results are identical to hdc_beam_search on the same values.  Needs the
  * grouped descent: dim % 1024 == 0, dim <= 16384, 16-byte aligned rows and
  * reads, HDC_BEAM_GROUPED != 0 (HDC_ERR_INVALID otherwise, unless every row
- * is int32, n_wide == n_nodes). */
+ * is int32, n_wide == n_nodes).
+ * max_children: the largest child count of any node, known to the caller who
+ * built the tree, which sizes the call's workspace without a host
+ * synchronisation; 0 has the call read it back from the device (as
+ * hdc_beam_search does).  A value below the tree's is caught on the device:
+ * every read stops at depth 0 and hdc_context_status reports 200. */
 int hdc_beam_search_split(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qnorm2, int64_t nq,
                           const int32_t* d_proto32, int64_t n_wide, const int16_t* d_proto16,
                           const int64_t* d_proto_norm2, int64_t n_nodes, const int64_t* d_child_ptr,
-                          const int32_t* d_child_idx, const int32_t* d_roots, int n_roots, int levels, int beam,
-                          double threshold, int score_mode, int32_t* d_path, float* d_path_score, int32_t* d_depth,
-                          void* stream);
+                          const int32_t* d_child_idx, const int32_t* d_roots, int n_roots, int max_children,
+                          int levels, int beam, double threshold, int score_mode, int32_t* d_path,
+                          float* d_path_score, int32_t* d_depth, void* stream);
 
 /* Windowed similarity, HVCache::similarity (src/encoder.cpp:198-215), for a
  * list of (query, reference sequence) pairs.  A reference's "similarity rows"

@@ -224,6 +224,21 @@ def test_beam_split_rows_equal_int32(hdc, cuda):
                                             pn, d_ptr, d_idx, roots, 6, 5, threshold)
                 for x, y in zip(want, got):
                     assert torch.equal(x, y), (grouped, threshold, n_wide)
+        # the largest child count given by the caller (no host synchronisation): the same results;
+        # one below the tree's stops every read at depth 0 and sets status 200
+        maxc = int(np.diff(ptr).max())
+        for given in (maxc, maxc + 3):
+            got = ctx.beam_search_split(q8, qn, proto[:first16].contiguous(), proto[first16:].to(torch.int16), pn,
+                                        d_ptr, d_idx, roots, 6, 5, 0.0, max_children=given)
+            want = ctx.beam_search(q8, qn, proto, pn, d_ptr, d_idx, roots, 6, 5, 0.0)
+            for x, y in zip(want, got):
+                assert torch.equal(x, y), (grouped, given)
+        assert ctx.status() == 0
+        _, _, depth = ctx.beam_search_split(q8, qn, proto[:first16].contiguous(), proto[first16:].to(torch.int16),
+                                            pn, d_ptr, d_idx, roots, 6, 5, 0.0, max_children=maxc - 1)
+        assert (depth == 0).all()
+        assert ctx.status() == 200
+        assert ctx.status() == 0  # read and cleared
     ctx.option(H.BEAM_GROUPED, 0)
     with pytest.raises(H.HDCError):
         ctx.beam_search_split(q8, qn, proto[:first16].contiguous(), proto[first16:].to(torch.int16), pn, d_ptr,
