@@ -53,3 +53,12 @@ def test_null_context_is_an_error(hdc):
     assert lib.hdc_norms(None, None, 2, 0, None, None, None) == 1
     assert lib.hdc_search_workspace_bytes(None, 1, 1, 1) == 0
     assert lib.hdc_num_windows(None, 500) == 0
+
+
+def test_beam_search_split_argument_checks_without_gpu(hdc):
+    """hdc_beam_search_split rejects a null context before any device work."""
+    lib = hdc.lib()
+    args = [None, None, None, 4, None, 0, None, None, 10, None, None, None, 1, 0, 6, 5, 0.0, 0, None, None, None,
+            None]
+    assert lib.hdc_beam_search_split(*args) == 1
+    assert b"null context" in lib.hdc_last_error()
