@@ -191,7 +191,8 @@ __global__ void __launch_bounds__(32 * kBeamWarps) beam_kernel(const BeamArgs a)
 
 }  // namespace
 
-int launch_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn, int64_t nq, const int32_t* d_proto,
+int launch_beam_search(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_qbits, const int64_t* d_qn, int64_t nq,
+                       const int32_t* d_proto,
                        int64_t n32, const int16_t* d_proto16, const int64_t* d_pn, int64_t n_nodes,
                        const int64_t* d_child_ptr, const int32_t* d_child_idx, const int32_t* d_roots, int n_roots,
                        int max_children, int levels, int beam, double threshold, int mode, int32_t* d_path,
@@ -201,14 +202,15 @@ int launch_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn,
     if (beam < 1 || beam > kMaxBeam) return fail(HDC_ERR_INVALID, "beam: beam width must be in 1..8");
     if (n_roots < 1) return fail(HDC_ERR_INVALID, "beam: no level-0 candidates");
     const bool grouped_ok = ctx->dim % 1024 == 0 && ctx->dim <= 16384 && (reinterpret_cast<uintptr_t>(d_proto) & 15) == 0 &&
-                            (reinterpret_cast<uintptr_t>(d_proto16) & 15) == 0 && (reinterpret_cast<uintptr_t>(d_q) & 15) == 0;
+                            (reinterpret_cast<uintptr_t>(d_proto16) & 15) == 0 && (reinterpret_cast<uintptr_t>(d_q) & 15) == 0 &&
+                            (reinterpret_cast<uintptr_t>(d_qbits) & 15) == 0;
     if (ctx->beam_grouped != 0 && grouped_ok)
-        return launch_beam_grouped(ctx, d_q, d_qn, nq, d_proto, n32, d_proto16, d_pn, n_nodes, d_child_ptr,
+        return launch_beam_grouped(ctx, d_q, d_qbits, d_qn, nq, d_proto, n32, d_proto16, d_pn, n_nodes, d_child_ptr,
                                    d_child_idx, d_roots, n_roots, max_children, levels, beam, threshold, mode, d_path,
                                    d_path_score, d_depth, stream);
-    if (n32 < n_nodes)
-        return fail(HDC_ERR_INVALID, "beam: int16 rows need the grouped descent (dim % 1024 == 0, dim <= 16384, "
-                                     "16-byte aligned rows and reads, HDC_BEAM_GROUPED != 0)");
+    if (n32 < n_nodes || d_qbits)
+        return fail(HDC_ERR_INVALID, "beam: int16 rows and bit reads need the grouped descent (dim % 1024 == 0, "
+                                     "dim <= 16384, 16-byte aligned rows and reads, HDC_BEAM_GROUPED != 0)");
     if (ctx->dim % 4 != 0 || (reinterpret_cast<uintptr_t>(d_proto) & 15) || (reinterpret_cast<uintptr_t>(d_q) & 3))
         return fail(HDC_ERR_INVALID, "beam: dim must be a multiple of 4 and rows aligned");
     BeamArgs a{d_q, d_qn, nq, d_proto, d_pn, d_child_ptr, d_child_idx, d_roots, n_roots, ctx->dim, levels, beam,

@@ -938,7 +938,8 @@ T* carve(uint8_t*& cur, int64_t n) {
 
 }  // namespace
 
-int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn, int64_t nq, const int32_t* d_proto,
+int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_qbits, const int64_t* d_qn, int64_t nq,
+                        const int32_t* d_proto,
                         int64_t n32, const int16_t* d_proto16, const int64_t* d_pn, int64_t n_nodes, const int64_t* d_child_ptr, const int32_t* d_child_idx,
                         const int32_t* d_roots, int n_roots, int max_children, int levels, int beam,
                         double threshold, int mode, int32_t* d_path, float* d_path_score, int32_t* d_depth,
@@ -996,7 +997,7 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn
     // carve the workspace: once from address 0 to measure it, then from the allocation
     auto carve_all = [&](uint8_t* base) {
         uint8_t* cur = base;
-        bits = carve<uint32_t>(cur, nq * a.words);
+        if (!d_qbits) bits = carve<uint32_t>(cur, nq * a.words);
         a.paths = carve<int32_t>(cur, nq * kMaxBeamG * kMaxLevelsG);
         a.scores = carve<float>(cur, nq * kMaxBeamG * kMaxLevelsG);
         a.nbeam = carve<int32_t>(cur, nq);
@@ -1035,7 +1036,7 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn
     if ((e = cudaMallocAsync(reinterpret_cast<void**>(&ws), bytes, stream)) != cudaSuccess)
         return cuda_fail(e, "beam: workspace");
     carve_all(ws);
-    a.bits = bits;
+    a.bits = d_qbits ? d_qbits : bits;
 
     const unsigned rb = (unsigned)((nq + 255) / 256);
     cudaMemsetAsync(a.nbeam, 0, nq * 4, stream);
@@ -1046,7 +1047,7 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn
         max_children_kernel<<<mc_grid, 256, 0, stream>>>(d_child_ptr, n_nodes, d_maxc_dev);
         check_children_kernel<<<rb, 256, 0, stream>>>(a, d_maxc_dev, max_children, ctx->d_status);
     }
-    pack_bits_kernel<<<(unsigned)((nq * a.words + 255) / 256), 256, 0, stream>>>(d_q, nq, a.dim, bits);
+    if (!d_qbits) pack_bits_kernel<<<(unsigned)((nq * a.words + 255) / 256), 256, 0, stream>>>(d_q, nq, a.dim, bits);
     const int work_grid = ctx->num_sms * 8;
     const unsigned nb = (unsigned)((n_nodes + 255) / 256);
     if (use_tc && (e = cudaFuncSetAttribute(descent_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -120,8 +120,9 @@ int hdc_encode_segments(hdc_context* ctx, const char* d_bytes, const int64_t* d_
     if (n_segs < 0) return fail(HDC_ERR_INVALID, "encode: negative segment count");
     if (n_segs == 0) return HDC_OK;
     if (!d_bytes || !d_seg_off || !d_seg_len || !d_out) return fail(HDC_ERR_INVALID, "encode: null pointer");
-    if (out_kind < HDC_OUT_I16 || out_kind > HDC_OUT_F16) return fail(HDC_ERR_INVALID, "encode: bad out_kind");
-    if (out_stride < ctx->dim) return fail(HDC_ERR_INVALID, "encode: out_stride < dim");
+    if (out_kind < HDC_OUT_I16 || out_kind > HDC_OUT_SIGN_BITS) return fail(HDC_ERR_INVALID, "encode: bad out_kind");
+    if (out_stride < (out_kind == HDC_OUT_SIGN_BITS ? (ctx->dim + 31) / 32 : ctx->dim))
+        return fail(HDC_ERR_INVALID, "encode: out_stride below the row length");
     if (max_len < 0) return fail(HDC_ERR_INVALID, "encode: negative max_len");
     return hdc::launch_encode(ctx, d_bytes, d_seg_off, d_seg_len, nullptr, nullptr, 0, n_segs, out_kind, d_out,
                               out_stride, d_nkmers, max_len, static_cast<cudaStream_t>(stream));
@@ -329,12 +330,12 @@ int hdc_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qnorm2
     if (!d_q || !d_qnorm2 || !d_proto || !d_proto_norm2 || !d_child_ptr || !d_child_idx || !d_roots || !d_path ||
         !d_path_score || !d_depth)
         return fail(HDC_ERR_INVALID, "beam: null pointer");
-    return hdc::launch_beam_search(ctx, d_q, d_qnorm2, nq, d_proto, n_nodes, nullptr, d_proto_norm2, n_nodes,
+    return hdc::launch_beam_search(ctx, d_q, nullptr, d_qnorm2, nq, d_proto, n_nodes, nullptr, d_proto_norm2, n_nodes,
                                    d_child_ptr, d_child_idx, d_roots, n_roots, 0, levels, beam, threshold, score_mode,
                                    d_path, d_path_score, d_depth, static_cast<cudaStream_t>(stream));
 }
 
-int hdc_beam_search_split(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qnorm2, int64_t nq,
+static int beam_split(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_qbits, const int64_t* d_qnorm2, int64_t nq,
                           const int32_t* d_proto32, int64_t n_wide, const int16_t* d_proto16,
                           const int64_t* d_proto_norm2, int64_t n_nodes, const int64_t* d_child_ptr,
                           const int32_t* d_child_idx, const int32_t* d_roots, int n_roots, int max_children,
@@ -347,13 +348,36 @@ int hdc_beam_search_split(hdc_context* ctx, const int8_t* d_q, const int64_t* d_
     if (n_wide < 0 || n_wide > n_nodes) return fail(HDC_ERR_INVALID, "beam split: n_wide must be in 0..n_nodes");
     if (!hdc::valid_score_mode(score_mode)) return fail(HDC_ERR_INVALID, "beam split: bad score mode");
     if (max_children < 0) return fail(HDC_ERR_INVALID, "beam split: negative max_children");
-    if (!d_q || !d_qnorm2 || (n_wide > 0 && !d_proto32) || (n_wide < n_nodes && !d_proto16) || !d_proto_norm2 ||
+    if ((!d_q && !d_qbits) || !d_qnorm2 || (n_wide > 0 && !d_proto32) || (n_wide < n_nodes && !d_proto16) || !d_proto_norm2 ||
         !d_child_ptr || !d_child_idx || !d_roots || !d_path || !d_path_score || !d_depth)
         return fail(HDC_ERR_INVALID, "beam split: null pointer");
-    return hdc::launch_beam_search(ctx, d_q, d_qnorm2, nq, d_proto32, n_wide, d_proto16, d_proto_norm2, n_nodes,
+    return hdc::launch_beam_search(ctx, d_q, d_qbits, d_qnorm2, nq, d_proto32, n_wide, d_proto16, d_proto_norm2, n_nodes,
                                    d_child_ptr, d_child_idx, d_roots, n_roots, max_children, levels, beam, threshold,
                                    score_mode,
                                    d_path, d_path_score, d_depth, static_cast<cudaStream_t>(stream));
+}
+
+int hdc_beam_search_split(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qnorm2, int64_t nq,
+                          const int32_t* d_proto32, int64_t n_wide, const int16_t* d_proto16,
+                          const int64_t* d_proto_norm2, int64_t n_nodes, const int64_t* d_child_ptr,
+                          const int32_t* d_child_idx, const int32_t* d_roots, int n_roots, int max_children,
+                          int levels, int beam, double threshold, int score_mode, int32_t* d_path,
+                          float* d_path_score, int32_t* d_depth, void* stream) {
+    return beam_split(ctx, d_q, nullptr, d_qnorm2, nq, d_proto32, n_wide, d_proto16, d_proto_norm2, n_nodes,
+                      d_child_ptr, d_child_idx, d_roots, n_roots, max_children, levels, beam, threshold, score_mode,
+                      d_path, d_path_score, d_depth, stream);
+}
+
+int hdc_beam_search_split_bits(hdc_context* ctx, const uint32_t* d_qbits, const int64_t* d_qnorm2, int64_t nq,
+                               const int32_t* d_proto32, int64_t n_wide, const int16_t* d_proto16,
+                               const int64_t* d_proto_norm2, int64_t n_nodes, const int64_t* d_child_ptr,
+                               const int32_t* d_child_idx, const int32_t* d_roots, int n_roots, int max_children,
+                               int levels, int beam, double threshold, int score_mode, int32_t* d_path,
+                               float* d_path_score, int32_t* d_depth, void* stream) {
+    if (!d_qbits && nq > 0) return fail(HDC_ERR_INVALID, "beam split: null pointer");
+    return beam_split(ctx, nullptr, d_qbits, d_qnorm2, nq, d_proto32, n_wide, d_proto16, d_proto_norm2, n_nodes,
+                      d_child_ptr, d_child_idx, d_roots, n_roots, max_children, levels, beam, threshold, score_mode,
+                      d_path, d_path_score, d_depth, stream);
 }
 
 int hdc_similarity(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qnorm2, const int16_t* d_rows,

@@ -251,6 +251,32 @@ __global__ void __launch_bounds__(kThreads) encode_kernel(const EncodeArgs a) {
         }
         if (w32 >= a.W32) continue;
 
+        if (a.out_kind == HDC_OUT_SIGN_BITS) {
+            // 2 count - nvalid >= 0, i.e. count >= ceil(nvalid / 2), compared plane by plane
+            // from the most significant: gt = lanes already above, eq = equal so far
+            const uint32_t thr = (uint32_t)(nvalid + 1) >> 1;
+            uint32_t gt = 0, eq = 0xffffffffu;
+            auto cmp = [&](uint32_t plane, int bit) {
+                if ((thr >> bit) & 1u) {
+                    eq &= plane;
+                } else {
+                    gt |= eq & plane;
+                    eq &= ~plane;
+                }
+            };
+#pragma unroll
+            for (int h = NH - 1; h >= 0; --h) cmp(hi[h], 4 + h);
+            cmp(eights, 3);
+            cmp(fours, 2);
+            cmp(twos, 1);
+            cmp(ones, 0);
+            uint32_t bits = gt | eq;
+            const int nd = min(32, a.dim - w32 * 32);
+            if (nd < 32) bits &= (1u << nd) - 1u;
+            reinterpret_cast<uint32_t*>(a.out)[seg * a.out_stride + w32] = bits;
+            continue;
+        }
+
         // ---- counts -> output values, dims b and b+16 in 16-bit fields ----
         uint32_t val[32];
 #pragma unroll

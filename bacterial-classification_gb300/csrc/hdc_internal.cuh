@@ -111,7 +111,7 @@ int launch_propagate_greedy(hdc_context* ctx, const int16_t* d_hv, const int64_t
                             const int32_t* d_rep_idx, int64_t n_parents, double threshold, int mode,
                             uint8_t* d_selected, float* d_best, int32_t* d_scratch, cudaStream_t stream);
 
-int launch_beam_search(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn, int64_t nq, const int32_t* d_proto,
+int launch_beam_search(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_qbits, const int64_t* d_qn, int64_t nq, const int32_t* d_proto,
                        int64_t n32, const int16_t* d_proto16, const int64_t* d_pn, int64_t n_nodes,
                        const int64_t* d_child_ptr, const int32_t* d_child_idx, const int32_t* d_roots, int n_roots, int max_children,
                        int levels, int beam, double threshold, int mode, int32_t* d_path, float* d_path_score,
@@ -129,8 +129,9 @@ int launch_similarity(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qn,
                       int32_t* d_window, cudaStream_t stream);
 
 // the descent with reads grouped by candidate node (beam_grouped.cu); dim % 1024 == 0, dim <= 16384;
-// nodes < n32 have int32 rows in d_proto, the others int16 rows in d_proto16 (row node - n32)
-int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const int64_t* d_qn, int64_t nq, const int32_t* d_proto,
+// nodes < n32 have int32 rows in d_proto, the others int16 rows in d_proto16 (row node - n32);
+// reads as int8 +1/-1 rows d_q, or as sign bits d_qbits [nq][dim / 32] (then d_q is unused)
+int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_qbits, const int64_t* d_qn, int64_t nq, const int32_t* d_proto,
                         int64_t n32, const int16_t* d_proto16, const int64_t* d_pn, int64_t n_nodes, const int64_t* d_child_ptr, const int32_t* d_child_idx,
                         const int32_t* d_roots, int n_roots, int max_children, int levels, int beam, double threshold, int mode,
                         int32_t* d_path, float* d_path_score, int32_t* d_depth, cudaStream_t stream);

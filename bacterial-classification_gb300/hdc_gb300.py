@@ -17,6 +17,7 @@ ERR = {1: "HDC_ERR_INVALID", 2: "HDC_ERR_RANGE", 3: "HDC_ERR_CUDA", 4: "HDC_ERR_
 SCORE_NORM, SCORE_COS, SCORE_DOT = 0, 1, 2
 TC_PREFETCH, TC_CLUSTER, TC_SHARE, BEAM_GROUPED, TC_SCATTER, TC_KBLOCK, TC_PAIR_MMA, TC_LANES = 1, 2, 3, 4, 5, 6, 7, 8
 OUT_I16, OUT_I32, OUT_BIPOLAR_BF16, OUT_BIPOLAR_I16, OUT_BIPOLAR_F16, OUT_BIPOLAR_I8, OUT_F16 = 0, 1, 2, 3, 4, 5, 6
+OUT_SIGN_BITS = 7  # sign bits, int32 [n][dim / 32] (bit b of word w: element 32 w + b >= 0)
 
 # (name, restype, argtypes) of every exported entry point
 P, I32, I64, SZ = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_size_t
@@ -41,6 +42,8 @@ SIGNATURES = [
     ("hdc_beam_search", I32, [P, P, P, I64, P, P, I64, P, P, P, I32, I32, I32, ctypes.c_double, I32, P, P, P, P]),
     ("hdc_beam_search_split", I32, [P, P, P, I64, P, I64, P, P, I64, P, P, P, I32, I32, I32, I32, ctypes.c_double,
                                     I32, P, P, P, P]),
+    ("hdc_beam_search_split_bits", I32, [P, P, P, I64, P, I64, P, P, I64, P, P, P, I32, I32, I32, I32,
+                                         ctypes.c_double, I32, P, P, P, P]),
     ("hdc_similarity", I32, [P, P, P, P, P, P, P, P, P, I64, I32, P, P, P]),
     ("hdc_identify", I32, [P, P, P, I64, P, P, P, P, P, P, I32, I32, I32, ctypes.c_double, I32, P, P, P, P, P]),
     ("hdc_propagate_greedy", I32, [P, P, P, P, P, P, P, I64, ctypes.c_double, I32, P, P, P, P]),
@@ -258,7 +261,9 @@ class Context:
                           threshold=0.0, mode=SCORE_NORM, stream=None, max_children=0):
         """hdc_beam_search_split: nodes < proto32.shape[0] have int32 rows, the
         others int16 rows in proto16 (node n is row n - proto32.shape[0]);
-        max_children > 0 spares the call its host synchronisation."""
+        max_children > 0 spares the call its host synchronisation.  q: int8
+        +1/-1 rows, or int32 [nq][dim / 32] sign bits (HDC_OUT_SIGN_BITS rows,
+        hdc_beam_search_split_bits)."""
         import torch
         nq = q.shape[0]
         n_wide = proto32.shape[0] if proto32 is not None else 0
@@ -266,10 +271,10 @@ class Context:
         path = torch.empty((nq, levels), dtype=torch.int32, device=q.device)
         score = torch.empty((nq, levels), dtype=torch.float32, device=q.device)
         depth = torch.empty(nq, dtype=torch.int32, device=q.device)
-        check(lib().hdc_beam_search_split(self.h, ptr(q), ptr(qn), nq, ptr(proto32), n_wide, ptr(proto16), ptr(pn),
-                                          n_nodes, ptr(child_ptr), ptr(child_idx), ptr(roots), roots.numel(),
-                                          max_children, levels, beam, threshold, mode, ptr(path), ptr(score), ptr(depth),
-                                          stream_ptr(stream)))
+        fn = lib().hdc_beam_search_split_bits if q.dtype == torch.int32 else lib().hdc_beam_search_split
+        check(fn(self.h, ptr(q), ptr(qn), nq, ptr(proto32), n_wide, ptr(proto16), ptr(pn), n_nodes, ptr(child_ptr),
+                 ptr(child_idx), ptr(roots), roots.numel(), max_children, levels, beam, threshold, mode, ptr(path),
+                 ptr(score), ptr(depth), stream_ptr(stream)))
         return path, score, depth
 
     def similarity(self, q, qn, rows, rn, ref_rows, ref_whole, pair_q, pair_ref, mode=SCORE_NORM, stream=None):

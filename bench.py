@@ -499,12 +499,18 @@ def run_descent(args, cfg, rank, world):
                 for r in pool]
     out = {}
 
+    # split form: the reads go straight to sign bits (HDC_OUT_SIGN_BITS, hdc_beam_search_split_bits)
+    qbits = torch.empty((B, dim // 32), dtype=torch.int32, device=dev) if split else None
+
     def step(d_buf, d_off, d_len, ev=None):
-        ctx.encode_segments(d_buf, d_off, d_len, q8, H.OUT_BIPOLAR_I8, max_len)
+        if split:
+            ctx.encode_segments(d_buf, d_off, d_len, qbits, H.OUT_SIGN_BITS, max_len)
+        else:
+            ctx.encode_segments(d_buf, d_off, d_len, q8, H.OUT_BIPOLAR_I8, max_len)
         if ev:
             ev[0].record()
         if split:  # the tree's largest child count is known here: no host synchronisation in the call
-            out["r"] = ctx.beam_search_split(q8, qn, proto32, proto16, pn, d_ptr, d_idx, roots, L, W,
+            out["r"] = ctx.beam_search_split(qbits, qn, proto32, proto16, pn, d_ptr, d_idx, roots, L, W,
                                              cfg["threshold"], max_children=max_children)
         else:
             out["r"] = ctx.beam_search(q8, qn, proto, pn, d_ptr, d_idx, roots, L, W, cfg["threshold"])
@@ -569,6 +575,8 @@ def run_descent(args, cfg, rank, world):
     t1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = t0.elapsed_time(t1) / args.steps
+    if split:  # the last step's reads as int8 rows too (untimed), for the oracle's sample
+        ctx.encode_segments(e_buf, e_off, e_len, q8, H.OUT_BIPOLAR_I8, max_len)
     if world > 1:
         t = torch.tensor([ms, e2e_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -576,7 +584,8 @@ def run_descent(args, cfg, rank, world):
     # candidate rows per read: the level-0 candidates, then up to beam x children per level
     cand = [counts[0]] + [min(W, counts[l - 1]) * b for l in range(1, L)]
     # kernels per step: the read encode + the descent.  Grouped: max-children, bit packing
-    # and output, and per level count / 3 scan kernels / expand / select plus the scoring:
+    # (with sign-bit reads and the caller's child count: the count's check instead) and
+    # output, and per level count / 3 scan kernels / expand / select plus the scoring:
     # on CUDA cores 3 scan kernels / scatter / score; on the tensor cores (every level but
     # the last; the default) level 0 its item list and descent_tc_kernel, a later level the
     # parents' entry count / 3 scans / scatter, item count / 2 x 3 scans / write and
@@ -725,7 +734,8 @@ def descent_line(args, cfg, r, metric, workload, world):
         "metric": metric, "value": B * world / (r["ms"] / 1e3), "unit": "reads/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "int8 +1/-1 reads x %s prototypes, exact int64 dots, FP64 scores" % (
+        "dtype": "%s x %s prototypes, exact int64 dots, FP64 scores" % (
+            "+1/-1 reads as sign bits" if split else "int8 +1/-1 reads",
             "int32 (ranks above) / int16 (nodes %d on)" % r["n_wide"] if split else "int32"),
         "data": "synthetic (seeded 6-rank tree, see bench.py)",
         "config": {"workload": workload, "form": "descent", "batch_reads": B, "nodes": r["refs"],

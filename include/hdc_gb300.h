@@ -57,6 +57,10 @@ extern "C" {
 #define HDC_OUT_BIPOLAR_I8 5   /* int8 +1/-1 sign of the bundle, 0 -> +1 (hierarchical descent reads) */
 #define HDC_OUT_F16 6          /* fp16 bundle, exact (segments of <= 2048 k-mers): count-valued
                                   tensor-core queries */
+#define HDC_OUT_SIGN_BITS 7    /* the +1/-1 signs as bits (0 -> +1): bit b of uint32 word w of a
+                                  row is set when element 32 w + b is >= 0, bits past dim are 0;
+                                  out_stride in words (>= ceil(dim / 32)); the reads of
+                                  hdc_beam_search_split_bits */
 
 typedef struct hdc_context hdc_context;
 typedef struct hdc_refdb hdc_refdb;
@@ -319,6 +323,15 @@ int hdc_beam_search_split(hdc_context* ctx, const int8_t* d_q, const int64_t* d_
                           const int32_t* d_child_idx, const int32_t* d_roots, int n_roots, int max_children,
                           int levels, int beam, double threshold, int score_mode, int32_t* d_path,
                           float* d_path_score, int32_t* d_depth, void* stream);
+/* The same with the reads as sign bits d_qbits [nq][dim / 32] (HDC_OUT_SIGN_BITS
+ * rows, 16-byte aligned): no int8 rows and no packing pass.  As
+ * hdc_beam_search_split for everything else; needs the grouped descent. */
+int hdc_beam_search_split_bits(hdc_context* ctx, const uint32_t* d_qbits, const int64_t* d_qnorm2, int64_t nq,
+                               const int32_t* d_proto32, int64_t n_wide, const int16_t* d_proto16,
+                               const int64_t* d_proto_norm2, int64_t n_nodes, const int64_t* d_child_ptr,
+                               const int32_t* d_child_idx, const int32_t* d_roots, int n_roots, int max_children,
+                               int levels, int beam, double threshold, int score_mode, int32_t* d_path,
+                               float* d_path_score, int32_t* d_depth, void* stream);
 
 /* Windowed similarity, HVCache::similarity (src/encoder.cpp:198-215), for a
  * list of (query, reference sequence) pairs.  A reference's "similarity rows"

@@ -294,3 +294,80 @@ def test_beam_split_tensor_core_levels_int16_children(hdc, cuda):
                     assert torch.equal(x, y), (grouped, levels, beam, threshold, n_wide)
     torch.cuda.synchronize()
     assert ctx.status() == 0
+
+
+def _pack_signs(q8, dim):
+    """int64 [n][ceil(dim / 32)] words of the +1 signs of int8 rows (bit b of word w: element 32 w + b > 0)."""
+    import torch
+    n = q8.shape[0]
+    words = (dim + 31) // 32
+    pos = torch.zeros((n, words * 32), dtype=torch.int64, device=q8.device)
+    pos[:, :dim] = (q8[:, :dim] > 0).to(torch.int64)
+    weights = (torch.ones(32, dtype=torch.int64, device=q8.device) << torch.arange(32, device=q8.device))
+    return (pos.view(n, words, 32) * weights).sum(dim=2)
+
+
+@pytest.mark.parametrize("dim,kmer", [(1000, 8), (1024, 12), (2048, 10)])
+def test_sign_bits_output_equals_packed_bipolar(hdc, cuda, dim, kmer):
+    """HDC_OUT_SIGN_BITS rows are the packed signs of HDC_OUT_BIPOLAR_I8 rows
+    (0 -> +1, bits past dim 0), for segments of 0 to 1,600 bytes (counters of
+    4, 8 and 12 high planes) with N and lowercase bytes."""
+    import torch
+    H = hdc
+    rng = np.random.default_rng(dim + kmer)
+    lens = [0, 1, kmer - 1, kmer, kmer + 1, 255 + kmer, 300, 1600] + list(rng.integers(100, 1600, 40))
+    seqs = ["".join(rng.choice(list("ACGTACGTACGTNa"), n)) for n in lens]
+    ctx = H.Context(dim, kmer, 250, 10)
+    short = [x for x in seqs if len(x) <= 200]
+    # max_len picks the counter width: <= 255 k-mers 4 high planes, <= 4095 8, else 12
+    for batch, max_len in ((short, 200), (seqs, 1600), (seqs, 5000)):
+        buf, off, ln = H.pack_sequences(batch)
+        d_buf, d_off, d_len = (torch.from_numpy(x.copy()).to(cuda) for x in (buf, off, ln))
+        q8 = torch.empty((len(batch), dim), dtype=torch.int8, device=cuda)
+        ctx.encode_segments(d_buf, d_off, d_len, q8, H.OUT_BIPOLAR_I8, max_len)
+        bits = torch.empty((len(batch), (dim + 31) // 32), dtype=torch.int32, device=cuda)
+        ctx.encode_segments(d_buf, d_off, d_len, bits, H.OUT_SIGN_BITS, max_len)
+        want = _pack_signs(q8, dim)
+        assert torch.equal(bits.to(torch.int64) & 0xFFFFFFFF, want), max_len
+
+
+def test_beam_split_bit_reads_equal_int8_reads(hdc, cuda):
+    """hdc_beam_search_split_bits over HDC_OUT_SIGN_BITS reads returns what
+    hdc_beam_search_split returns over the same reads as int8 rows, in both
+    grouped forms."""
+    import torch
+    H = hdc
+    dim, n_leaves, nq = 2048, 20000, 3000
+    b, base, counts, ptr, idx = H.synth_tree_csr(n_leaves)
+    tree = H.synth_tree(27, n_leaves)
+    reads = H.synth_reads(28, tree, nq, 250, subst=0.01, sigma=0.5, min_read=100, max_read=800,
+                          mixed_frac=0.2, mixed_rate=0.06)
+    ctx = H.Context(dim, 12, 250, 10)
+    proto = torch.zeros((int(base[-1]), dim), dtype=torch.int32, device=cuda)
+    ctx.encode_segments(torch.from_numpy(tree.buf).to(cuda), torch.from_numpy(tree.off).to(cuda),
+                        torch.from_numpy(tree.len).to(cuda), proto[int(base[5]):], H.OUT_I32, tree.max_len())
+    d_idx = torch.from_numpy(idx).to(cuda)
+    for r in range(4, -1, -1):
+        lo, hi = int(base[r]), int(base[r + 1])
+        ctx.bundle(proto, torch.from_numpy(ptr[lo:hi + 1].copy()).to(cuda), d_idx, out=proto[lo:hi])
+    rb, ro, rl = (torch.from_numpy(x).to(cuda) for x in (reads.buf, reads.off, reads.len))
+    q8 = torch.empty((nq, dim), dtype=torch.int8, device=cuda)
+    ctx.encode_segments(rb, ro, rl, q8, H.OUT_BIPOLAR_I8, reads.max_len())
+    qbits = torch.empty((nq, dim // 32), dtype=torch.int32, device=cuda)
+    ctx.encode_segments(rb, ro, rl, qbits, H.OUT_SIGN_BITS, reads.max_len())
+    qn, pn = ctx.norms(q8), ctx.norms(proto)
+    roots = torch.arange(0, counts[0], dtype=torch.int32, device=cuda)
+    d_ptr = torch.from_numpy(ptr).to(cuda)
+    n_wide = int(base[5])
+    p32, p16 = proto[:n_wide].contiguous(), proto[n_wide:].to(torch.int16)
+    maxc = int(np.diff(ptr).max())
+    for grouped in (1, 2):
+        ctx.option(H.BEAM_GROUPED, grouped)
+        for threshold in (0.0, float("-inf")):
+            want = ctx.beam_search_split(q8, qn, p32, p16, pn, d_ptr, d_idx, roots, 6, 5, threshold)
+            got = ctx.beam_search_split(qbits, qn, p32, p16, pn, d_ptr, d_idx, roots, 6, 5, threshold,
+                                        max_children=maxc)
+            for x, y in zip(want, got):
+                assert torch.equal(x, y), (grouped, threshold)
+    torch.cuda.synchronize()
+    assert ctx.status() == 0
