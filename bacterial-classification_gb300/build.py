@@ -59,6 +59,25 @@ def build(force=False, verbose=False):
     return LIB
 
 
+SYNTH_SRC = os.path.join(HERE, "synth", "synth.cpp")
+SYNTH_LIB = os.path.join(OUT, "libhdc_synth.so")
+
+
+def build_synth(force=False):
+    """libhdc_synth.so: the seeded synthetic-workload generator (include/hdc_synth.h),
+    host C++ only and kept out of libhdc_gb300.so, so that a CPU-only user of the
+    workloads (the benchmark's reference arm) maps no GPU library."""
+    os.makedirs(OUT, exist_ok=True)
+    hdr = os.path.join(ROOT, "include", "hdc_synth.h")
+    newest = max(os.path.getmtime(SYNTH_SRC), os.path.getmtime(hdr))
+    if not force and os.path.exists(SYNTH_LIB) and os.path.getmtime(SYNTH_LIB) >= newest:
+        return SYNTH_LIB
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", "-I" + os.path.join(ROOT, "include"),
+                           SYNTH_SRC, "-o", SYNTH_LIB + ".tmp"])
+    os.replace(SYNTH_LIB + ".tmp", SYNTH_LIB)
+    return SYNTH_LIB
+
+
 DROPIN = os.path.join(HERE, "dropin")
 
 
@@ -96,3 +115,4 @@ def build_dropin(dim=1024, kmer=8, window=150, step=10, force=False):
 
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build_synth(force="--force" in sys.argv))

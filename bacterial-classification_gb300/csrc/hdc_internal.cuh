@@ -36,6 +36,7 @@ struct hdc_context {
     int tc_kblock = 0;              // tensor-core search: dims per K block, 32 or 64 (0: automatic)
     int tc_scatter = -1;            // tensor-core search: 1 scattered reference-tile order, 0 index order (-1: auto)
     int beam_grouped = -1;          // descent: 1 grouped by candidate node, 2 + tensor-core levels, 0 warp per read
+    void* noalloc_scratch = nullptr;  // device address of hdc_search_plain_noalloc's fixed scratch (first call)
 };
 
 // A tensor-core reference database (hdc_refdb_create).

@@ -493,29 +493,28 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[HDC_NOALLOC_SCR
 
 namespace hdc {
 namespace {
-constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mutex;
-void* g_noalloc_addr[kMaxDevices] = {};
 }  // namespace
 
-// Device address of the fixed scratch on the current device.  In host code
-// the array's name only stands in for the symbol, so the address is asked of
-// the runtime once per device (with that device current) and then reused.
-static int noalloc_scratch(const hdc_context* ctx, void** out) {
+// Device address of the fixed scratch on the context's device (which must be
+// current).  In host code the array's name only stands in for the symbol, so
+// the address is asked of the runtime on the first call with a context and
+// kept in the context.  A context does not outlive its device's state, so
+// after cudaDeviceReset the new contexts look the address up again.
+static int noalloc_scratch(hdc_context* ctx, void** out) {
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_fail(e, "search_plain_noalloc: cudaGetDevice");
     if (dev != ctx->device)
         return fail(HDC_ERR_INVALID, "search_plain_noalloc: the context's device must be the current device");
-    if (dev < 0 || dev >= kMaxDevices) return fail(HDC_ERR_INVALID, "search_plain_noalloc: device ordinal >= 64");
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_addr[dev]) {
+    if (!ctx->noalloc_scratch) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return cuda_fail(e, "search_plain_noalloc: cudaGetSymbolAddress");
-        g_noalloc_addr[dev] = p;
+        ctx->noalloc_scratch = p;
     }
-    *out = g_noalloc_addr[dev];
+    *out = ctx->noalloc_scratch;
     return HDC_OK;
 }
 
@@ -533,6 +532,8 @@ extern "C" int hdc_search_plain_noalloc(hdc_context* ctx, const int16_t* d_q, co
     if (!d_q || !d_qnorm2 || !d_r || !d_rnorm2 || !d_score || !d_idx)
         return fail(HDC_ERR_INVALID, "search_plain_noalloc: null pointer");
     if (nr <= 0) return fail(HDC_ERR_INVALID, "search_plain_noalloc: empty reference set");
+    const int64_t kk = std::min<int64_t>(k, nr);  // as hdc_search_plain: k is clamped to nr, then checked
+    if (kk < 1 || kk > kMaxK) return fail(HDC_ERR_INVALID, "search_plain_noalloc: k must be in 1..32");
     const size_t need = plain_workspace_bytes(ctx, nq, nr, k);
     if (need > (size_t)HDC_NOALLOC_SCRATCH_BYTES)
         return fail(HDC_ERR_RANGE, "search_plain_noalloc: this batch needs " + std::to_string(need) +

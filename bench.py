@@ -18,8 +18,11 @@ which is available here):
 --impl reference times the reference CPU algorithm (the C restatement in
 oracle/, the reference's own sources being unavailable on the GPU host) on
 the host cores, on a bounded sample of the same workload.
-With torchrun (N > 1) every rank runs an independent replica on its own GPU
-(reads shard with no exchange); the step time is the max over ranks.
+
+The library is single-GPU: its tensor-core search multicasts operand tiles
+between the CTAs of a cluster, within the calling GPU's own memory only.
+Launched with WORLD_SIZE > 1 the benchmark does no work: rank 0 prints an
+"unavailable" line and every rank exits 0.
 """
 import argparse
 import json
@@ -57,9 +60,8 @@ CONFIGS = {
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the
-# dominant kernel, from single-pass ncu captures of the full-size workloads
-# (profiles/tc_search_kernel_c3.md, profiles/beam_kernel_descent.md), per unit
-# of work, so a run's `traffic` is that per-unit figure times its own units:
+# dominant kernel, from single-pass ncu captures of the full-size workloads, per
+# unit of work, so a run's `traffic` is that per-unit figure times its own units:
 #   tc_search_kernel, c3 (38,912 reads x 200,000 refs = 304 x 1,564 tile pairs; the
 #     288 leading query tiles in clusters of 4 + the other 16 in pairs): 1.01427e12 B
 #   grouped descent, c5 (one call's 5 descent_tc_kernel launches + the leaf-level score_kernel,
@@ -67,6 +69,12 @@ CONFIGS = {
 TRAFFIC_PER_TILE_PAIR_TC = (975.445256e9 + 0.170780e9 + 38.640838e9 + 0.012020e9) / (304 * 1564)
 # (reads per call, int16 rows) -> bytes (mostly the database, once)
 TRAFFIC_DESCENT = {(38912, False): 36.409726e9 + 70.093e6, (38912, True): 2.035667e10}
+
+
+# the CPU port against the reference's own compiled code, both on one x86 thread at the c3 shape
+# (D = 10,240, k = 10, 250 bp reads, 2,000 references): 48.8 vs 64.8 reads/s
+PORT_NOTE = ("the oracle port of the reference's CPU path (its sources are not on this host); on x86 the "
+             "port ran at 0.75x the compiled reference (48.8 vs 64.8 reads/s, one thread, c3 shape)")
 
 
 def log(*a):
@@ -181,7 +189,7 @@ class Form:
              search on tcgen05 tensor cores (hdc_search_tc against an fp16-limb
              database whose limbs are sized for the largest query magnitude)"""
 
-    def __init__(self, H, ctx, cfg, name, refs, rn, maxr, B, dev):
+    def __init__(self, H, ctx, cfg, name, refs, rn, maxr, B, dev, db=None):
         import torch
         self.H, self.ctx, self.cfg, self.name, self.B = H, ctx, cfg, name, B
         self.refs, self.rn, self.maxr = refs, rn, maxr
@@ -189,7 +197,7 @@ class Form:
         self.K = K
         if name == "tc":
             if cfg["bipolar"]:
-                self.db = ctx.refdb(refs, maxr)
+                self.db = db if db is not None else ctx.refdb(refs, maxr)
                 self.kind, self.maxq = H.OUT_BIPOLAR_F16, 1
             else:  # count-valued reads: fp16 counts, limbs sized for them
                 self.maxq = cfg["read_len"] - cfg["kmer"] + 1
@@ -231,7 +239,7 @@ class Form:
         return self.out
 
 
-def time_form(form, batches, d_buf, steps, warmup, world, sampler=None):
+def time_form(form, batches, d_buf, steps, warmup, sampler=None):
     """Device-timed steps of one form on resident batches; also the median
     duration of its search kernel (+ merge) alone, on the same stream."""
     import torch
@@ -239,8 +247,6 @@ def time_form(form, batches, d_buf, steps, warmup, world, sampler=None):
     for i in range(warmup):
         form.run(d_buf, *batches[i % len(batches)])
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ctxm = sampler if sampler is not None else _Null()
     with ctxm:
@@ -268,16 +274,17 @@ class _Null:
         return False
 
 
-def run_pipeline(args, cfg, rank, world, H, ctx, tree, refs, rn, maxr, dev):
-    """Batching form: the CUDA-graph pipeline over host batches of uneven reads."""
+def run_pipeline(args, cfg, H, ctx, tree, refs, rn, maxr, dev, db=None):
+    """Batching form: the CUDA-graph pipeline over host batches of uneven reads
+    (against `db` when the tensor-core database is already built)."""
     import torch
     B, K = args.batch, cfg["topk"]
-    pool = [make_reads(H, tree, cfg, B, cfg["read_seed"] + 1000 * rank + p) for p in range(2)]
+    pool = [make_reads(H, tree, cfg, B, cfg["read_seed"] + p) for p in range(2)]
     max_bytes = max(int(r.len.astype(np.int64).sum()) for r in pool) + 4096
-    db = ctx.refdb(refs, maxr)
+    if db is None:
+        db = ctx.refdb(refs, maxr)
     pipe = H.Pipeline(ctx, db, B, max_bytes, cfg.get("max_read", cfg["read_len"]), K)
-    _, first_idx = pipe.run(pool[0])
-    acc = float((first_idx[:, 0] == pool[0].label).mean())
+    pipe.run(pool[0])
     tuned = pipe.autotune()
     # device-resident: replay encode + search on the staged batch, timed on the pipeline's stream
     st = torch.cuda.ExternalStream(pipe.stream())
@@ -300,28 +307,28 @@ def run_pipeline(args, cfg, rank, world, H, ctx, tree, refs, rn, maxr, dev):
     for i in range(args.steps):
         pipe.run(pool[i % 2])
     e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    # the timed schedule's results on the first batch: accuracy, and the oracle's parity sample
+    first_s, first_idx = pipe.run(pool[0])
+    acc = float((first_idx[:, 0] == pool[0].label).mean())
     # each graph replay runs encode_kernel, then the search and merge kernels of each part of the
     # search (memset nodes aside): the search the graph captured after the autotune
     per_step = 1 + ctx.tc_last_shape()[4]
     # the search kernel alone on the same batch, for the roofline
-    form = Form(H, ctx, cfg, "tc", refs, rn, maxr, B, dev)
+    form = Form(H, ctx, cfg, "tc", refs, rn, maxr, B, dev, db=db)
     d_buf = torch.from_numpy(pool[0].buf).to(dev)
     bat = [(torch.from_numpy(pool[0].off).to(dev), torch.from_numpy(pool[0].len).to(dev))]
-    _, search_ms = time_form(form, bat, d_buf, 2, 3, 1)
-    if world > 1:
-        t = torch.tensor([ms, e2e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms, e2e_ms = float(t[0]), float(t[1])
+    _, search_ms = time_form(form, bat, d_buf, 2, 3)
     return dict(ms=ms, e2e_ms=e2e_ms, search_ms=search_ms, clocks=clk.summary(), launches=per_step * args.steps,
                 refs=refs.shape[0], limbs=db.limbs, h2d=max_bytes + B * 16, d2h=B * K * 8, tree=tree,
                 tuned=tuned, mean_len=float(np.mean(pool[0].len)), top1_accuracy=acc,
-                refs_host=refs.cpu().numpy() if (rank == 0 and not args.no_cpu_baseline) else None)
+                refs_host=refs.cpu().numpy() if not args.no_cpu_baseline else None, reads=pool[0],
+                gpu_first=(first_s[:1024], first_idx[:1024], None, None))
 
 
-def run_ours(args, cfg, rank, world):
+def run_ours(args, cfg):
     import torch
     import hdc_gb300 as H
-    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     ctx = H.Context(cfg["dim"], cfg["kmer"], cfg["read_len"], 10)
     if args.tc_group or args.tc_cluster:
@@ -329,10 +336,10 @@ def run_ours(args, cfg, rank, world):
         ctx.tc_option(H.TC_CLUSTER, args.tc_cluster)
     tree, refs, rn, maxr = build_database(H, ctx, cfg, dev)
     if args.form == "pipe":
-        return run_pipeline(args, cfg, rank, world, H, ctx, tree, refs, rn, maxr, dev)
+        return run_pipeline(args, cfg, H, ctx, tree, refs, rn, maxr, dev)
     B = args.batch
     n_pool = 2
-    reads = make_reads(H, tree, cfg, B * n_pool, cfg["read_seed"] + 1000 * rank)
+    reads = make_reads(H, tree, cfg, B * n_pool, cfg["read_seed"])
     d_buf = torch.from_numpy(reads.buf).to(dev)
     batches = []
     for p in range(n_pool):
@@ -341,20 +348,22 @@ def run_ours(args, cfg, rank, world):
         batches.append((off, ln))
     form = Form(H, ctx, cfg, args.form, refs, rn, maxr, B, dev)
     clk = ClockSampler(dev.index)
-    ms, search_ms = time_form(form, batches, d_buf, args.steps, args.warmup, world, clk)
+    ms, search_ms = time_form(form, batches, d_buf, args.steps, args.warmup, clk)
     res = dict(ms=ms, search_ms=search_ms, clocks=clk.summary(), launches=form.launches * args.steps,
                refs=refs.shape[0], limbs=form.db.limbs if form.db is not None else 0)
     # the source leaf of every read is known: how often is it the top hit
     form.run(d_buf, *batches[0])
     torch.cuda.synchronize()
     res["top1_accuracy"] = float((form.out[1][:B, 0].cpu().numpy() == reads.label[:B]).mean())
+    res["gpu_first"] = tuple(x[:1024].cpu().numpy() for x in form.out)  # for the oracle's parity sample
+    res["reads"] = reads
 
     # the plain drop-in on the same workload, for the tensor-core speed-up
     if args.form == "tc" and not args.no_plain:
         pb = min(B, args.plain_batch)
         pbat = [(o[:pb], l[:pb]) for o, l in batches]
         plain = Form(H, ctx, cfg, "plain", refs, rn, maxr, pb, dev)
-        pms, psearch = time_form(plain, pbat, d_buf, max(2, args.steps // 2), 3, world)
+        pms, psearch = time_form(plain, pbat, d_buf, max(2, args.steps // 2), 3)
         res["plain"] = dict(value=pb / (pms / 1e3), ms=pms, batch=pb, search_ms=psearch)
         del plain
         # identical labels: the first plain batch against the tensor-core result
@@ -369,7 +378,7 @@ def run_ours(args, cfg, rank, world):
     # the precision form on the plain drop-in's workload (count-valued reads), for the speed-up
     if args.form == "plain" and not cfg["bipolar"] and not args.no_plain:
         tcf = Form(H, ctx, cfg, "tc", refs, rn, maxr, B, dev)
-        tms, tsearch = time_form(tcf, batches, d_buf, max(2, args.steps // 2), 3, world)
+        tms, tsearch = time_form(tcf, batches, d_buf, max(2, args.steps // 2), 3)
         tcf.run(d_buf, *batches[0])
         form.run(d_buf, *batches[0])
         torch.cuda.synchronize()
@@ -418,12 +427,15 @@ def run_ours(args, cfg, rank, world):
     t1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = t0.elapsed_time(t1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms, e2e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        res["ms"], e2e_ms = float(t[0]), float(t[1])
     res.update(e2e_ms=e2e_ms, h2d=io["h2d"], d2h=io["d2h"], tree=tree)
-    res["refs_host"] = refs.cpu().numpy() if (rank == 0 and not args.no_cpu_baseline) else None
+    res["refs_host"] = refs.cpu().numpy() if not args.no_cpu_baseline else None
+
+    # the batching form on the same database: the c4 reads (log-normal lengths, 20 % with mixed
+    # errors, top-10) through the CUDA-graph pipeline, after its autotune
+    if args.form == "tc" and cfg["copies"] and not args.no_batching:
+        c4 = dict(CONFIGS["c4"], n_leaves=cfg["n_leaves"])
+        res["batching"] = run_pipeline(args, c4, H, ctx, tree, refs, rn, maxr, dev, db=form.db)
+        res["batching"]["cfg"] = c4
     return res
 
 
@@ -465,12 +477,12 @@ def build_prototypes(H, ctx, cfg, dev):
     return tree, proto, pn, (b, base, counts, ptr, idx), bundle
 
 
-def run_descent(args, cfg, rank, world):
+def run_descent(args, cfg):
     """Hierarchical descent: per step, encode a batch of reads to +1/-1 int8
     and run the beam descent over the resident prototypes (one launch)."""
     import torch
     import hdc_gb300 as H
-    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     dim, B, L, W = cfg["dim"], args.batch, cfg["levels"], cfg["beam"]
     ctx = H.Context(dim, cfg["kmer"], cfg["read_len"], 10)
@@ -491,7 +503,7 @@ def run_descent(args, cfg, rank, world):
     for i in range(0, n_nodes - n_wide, 8192):
         proto16[i:i + 8192].copy_(proto[n_wide + i:n_wide + i + 8192])
     n_pool = 2
-    pool = [make_reads(H, tree, cfg, B, cfg["read_seed"] + 1000 * rank + p) for p in range(n_pool)]
+    pool = [make_reads(H, tree, cfg, B, cfg["read_seed"] + p) for p in range(n_pool)]
     max_len = max(r.max_len() for r in pool)
     q8 = torch.empty((B, dim), dtype=torch.int8, device=dev)
     qn = torch.full((B,), dim, dtype=torch.int64, device=dev)  # every element of a +1/-1 read is nonzero
@@ -521,8 +533,6 @@ def run_descent(args, cfg, rank, world):
     for i in range(args.warmup):
         step(*dev_pool[i % n_pool])
     torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
     stream = torch.cuda.current_stream()
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     clk = ClockSampler(dev.index)
@@ -577,10 +587,6 @@ def run_descent(args, cfg, rank, world):
     e2e_ms = t0.elapsed_time(t1) / args.steps
     if split:  # the last step's reads as int8 rows too (untimed), for the oracle's sample
         ctx.encode_segments(e_buf, e_off, e_len, q8, H.OUT_BIPOLAR_I8, max_len)
-    if world > 1:
-        t = torch.tensor([ms, e2e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms, e2e_ms = float(t[0]), float(t[1])
     # candidate rows per read: the level-0 candidates, then up to beam x children per level
     cand = [counts[0]] + [min(W, counts[l - 1]) * b for l in range(1, L)]
     # kernels per step: the read encode + the descent.  Grouped: max-children, bit packing
@@ -603,7 +609,7 @@ def run_descent(args, cfg, rank, world):
                bundle=bundle, depth_mean=depth_mean, rows_per_read=int(sum(cand)), leaf_accuracy=leaf_acc,
                mean_len=float(np.mean(pool[0].len)), n_wide=n_wide,
                proto_bytes=n_wide * dim * 4 + (n_nodes - n_wide) * dim * 2)
-    if rank == 0 and not args.no_cpu_baseline:
+    if not args.no_cpu_baseline:
         # q8 and out["r"] hold the last step's batch and result
         res["cpu"] = cpu_baseline_descent(cfg, pool[0], q8[:256].cpu().numpy(), proto, pn, ptr, idx,
                                           list(range(counts[0])))
@@ -670,56 +676,125 @@ class _DeviceRows:
 
 
 def oracle_database(cfg, threads):
-    """Reference hypervectors for the reference arm, built on the CPU (no GPU):
-    leaf encodings (config 2), or, for the bundled configurations, 8 x the leaf
-    encoding in place of the sum of 8 noisy copies -- the per-read work timed
-    against them (encode + one int64 dot per reference) is the same, and the
-    exact copies would cost minutes of CPU setup."""
-    import hdc_gb300 as H
+    """Reference hypervectors for the reference arm, built on the CPU by the
+    oracle from the same seeded workload as the GPU arm (no GPU library is
+    loaded): leaf encodings (c2), or, for the bundled configurations, the exact
+    sum of the same 8 noisy copies of each leaf (encode_copy_bundles: the
+    leaf's encoding plus the k-mers each copy changes).  Rows are
+    bit-identical to the GPU arm's database."""
+    import hdc_synth as S
     from oracle import oracle as O
-    tree = H.synth_tree(cfg["tree_seed"], cfg["n_leaves"])
-    refs = O.encode_bundles(tree.buf, tree.off, tree.len, cfg["dim"], cfg["kmer"], 1, threads)
-    if cfg["copies"]:
-        refs *= cfg["copies"]
-    return tree, refs.astype(np.int16)
+    tree = S.synth_tree(cfg["tree_seed"], cfg["n_leaves"])
+    nr, dim = cfg["n_leaves"], cfg["dim"]
+    if not cfg["copies"]:
+        refs = O.encode_bundles(tree.buf, tree.off, tree.len, dim, cfg["kmer"], 1, threads).astype(np.int16)
+        return tree, refs
+    refs = np.empty((nr, dim), np.int16)
+    chunk = 8192  # the GPU arm's chunks: copy seeds are per chunk
+    for a in range(0, nr, chunk):
+        b = min(nr, a + chunk)
+        sub = S.Seqs(tree.buf, tree.off[a:b], tree.len[a:b])
+        cp = S.synth_copies(cfg["copy_seed"] + a, sub, cfg["copies"], 0.01)
+        refs[a:b] = O.encode_copy_bundles(sub, cp, cfg["copies"], dim, cfg["kmer"], threads)
+    return tree, refs
 
 
-def cpu_baseline(cfg, tree, refs, seconds=12.0, threads=None):
-    """The reference CPU algorithm (oracle restatement: HVCache::compute per read
-    then brute-force cosine over every reference) on a bounded sample of reads."""
-    import hdc_gb300 as H
+def cpu_calls(cfg, refs, reads, first, n, threads, exact=False):
+    """The reference CPU algorithm (oracle restatement: HVCache::compute per read,
+    then brute-force cosine over every reference, top-k) on reads first ..
+    first + n - 1 of `reads`, in calls of 2 x threads reads (two per thread).
+    Returns (seconds, [scores, idx, cos, dot] or None)."""
     from oracle import oracle as O
-    threads = threads or (os.cpu_count() or 1)
-    reads = make_reads(H, tree, cfg, 4096, cfg["read_seed"] + 999)
-    n = max(threads, 1)
-    done = 0
-    t_total = 0.0
-    while t_total < seconds and done < len(reads):
-        batch = [reads.get(i) for i in range(done, min(len(reads), done + n))]
+    per_call = 2 * threads
+    outs, t_total = [], 0.0
+    for a in range(first, first + n, per_call):
+        batch = [reads.get(j % len(reads)) for j in range(a, min(first + n, a + per_call))]
         t0 = time.time()
-        O.classify(batch, refs, cfg["dim"], cfg["kmer"], cfg["topk"], O.SCORE_NORM, cfg["bipolar"], threads)
+        r = O.classify(batch, refs, cfg["dim"], cfg["kmer"], cfg["topk"], O.SCORE_NORM, cfg["bipolar"], threads,
+                       exact=exact)
         t_total += time.time() - t0
-        done += len(batch)
-        n = min(4 * n, 1024)
-    return done / t_total, threads, done
+        outs.append(r)
+    if not exact:
+        return t_total, None
+    return t_total, [np.concatenate([o[x] for o in outs]) for x in range(4)]
+
+
+def cpu_baseline(cfg, refs, reads, gpu_out, min_reads=256, seconds=12.0, threads=None):
+    """cpu_baseline leg of our arm: the oracle on the first reads of the GPU
+    arm's own timed batch, against the same database (rows copied from the
+    device), until both min_reads reads and `seconds` are done; the same reads'
+    GPU results are compared with it (the parity sample)."""
+    threads = threads or (os.cpu_count() or 1)
+    per_call = 2 * threads
+    done, t_total, res = 0, 0.0, []
+    limit = gpu_out[0].shape[0]
+    while (done < min_reads or t_total < seconds) and done + per_call <= limit:
+        dt, r = cpu_calls(cfg, refs, reads, done, per_call, threads, exact=True)
+        t_total += dt
+        done += per_call
+        res.append(r)
+    cs, ci, cc, cd = (np.concatenate([r[x] for r in res]) for x in range(4))
+    gs, gi, gc, gd = (None if g is None else g[:done] for g in gpu_out)
+    parity = {"reads": done, "from": "the first %d reads of the timed batch" % done,
+              "topk_indices_identical": bool(np.array_equal(gi, ci)),
+              "float_scores_identical": bool(np.array_equal(gs, cs)),
+              "oracle": "oracle/hdc_oracle.c classify (HVCache::compute, int64 dots, FP64 cosine, "
+                        "ties to the lower index)"}
+    ok = parity["topk_indices_identical"] and parity["float_scores_identical"]
+    if gd is not None:  # the search entry points also return each hit's exact dot and FP64 cosine
+        with np.errstate(divide="ignore", invalid="ignore"):
+            rel = np.abs(gc - cc) / np.maximum(np.abs(cc), np.finfo(np.float64).tiny)
+        parity["dots_identical"] = bool(np.array_equal(gd, cd))
+        parity["cosine_fp64_max_rel_err"] = float(rel.max()) if rel.size else 0.0
+        parity["cosine_fp64_bound"] = 1e-12
+        ok = ok and parity["dots_identical"] and parity["cosine_fp64_max_rel_err"] <= 1e-12
+    parity["identical"] = ok
+    return done / t_total, threads, done, parity
 
 
 def run_reference(args, cfg):
-    """Reference arm: the reference CPU path on the host cores, per step a bounded sample."""
+    """Reference arm: the reference CPU path on the host cores, per step a
+    bounded sample (2 reads per core) of the GPU arm's own reads."""
+    import hdc_synth as S
     threads = os.cpu_count() or 1
     t0 = time.time()
     tree, refs = oracle_database(cfg, threads)
     log("oracle database built in %.1f s" % (time.time() - t0))
-    vals = []
+    reads = make_reads(S, tree, cfg, 4096, cfg["read_seed"])  # the GPU arm's first reads
+    vals, per_call = [], 2 * threads
     for i in range(args.warmup + args.steps):
-        v, threads, done = cpu_baseline(cfg, tree, refs, seconds=2.0 if i < args.warmup else 6.0, threads=threads)
+        dt, _ = cpu_calls(cfg, refs, reads, (i * per_call) % len(reads), per_call, threads)
         if i >= args.warmup:
-            vals.append(v)
-    v = float(np.median(vals))
-    return v, threads, done
+            vals.append(per_call / dt)
+    return float(np.median(vals)), threads, per_call
 
 
-def descent_line(args, cfg, r, metric, workload, world):
+def batching_line(args, b, refs_host, pk):
+    """The batching form measured inside the c3 run (same database): reads/s
+    resident and end to end, its search's roofline, the autotuned schedule and
+    the oracle's parity sample on the first reads of its batch."""
+    cfg = b["cfg"]
+    B = args.batch
+    flops = 2.0 * cfg["dim"] * b["refs"] * b["limbs"] * B
+    achieved = flops / (b["search_ms"] / 1e3) / 1e12
+    out = {"workload": "c4 reads on this database: log-normal lengths (median %d bp, sigma %.1f, %d-%d bp), %d%% "
+                       "with %d%% sub:ins:del 3:1:1, top-%d, CUDA-graph encode -> search -> top-k" % (
+                           cfg["read_len"], cfg["sigma"], cfg["min_read"], cfg["max_read"], 100 * cfg["mixed_frac"],
+                           100 * cfg["mixed_rate"], cfg["topk"]),
+           "value": B / (b["ms"] / 1e3), "unit": "reads/s", "batch_reads": B, "ms_per_step": b["ms"],
+           "e2e": {"value": B / (b["e2e_ms"] / 1e3), "unit": "reads/s", "h2d_bytes_per_step": b["h2d"],
+                   "d2h_bytes_per_step": b["d2h"]},
+           "search_roofline": {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_tflops"],
+                               "unit": "TFLOP/s", "frac": achieved / pk["bf16_tflops"]},
+           "autotuned_schedule": b["tuned"], "mean_read_len": b["mean_len"], "top1_accuracy": b["top1_accuracy"],
+           "gpu_launches": b["launches"], "clocks": b["clocks"]}
+    if refs_host is not None:
+        _, _, _, parity = cpu_baseline(cfg, refs_host, b["reads"], b["gpu_first"], min_reads=128, seconds=0.0)
+        out["parity_sample"] = parity
+    return out
+
+
+def descent_line(args, cfg, r, metric, workload):
     """The JSON line of the hierarchical-descent form."""
     pk, src = peaks()
     B, dim = args.batch, cfg["dim"]
@@ -731,7 +806,7 @@ def descent_line(args, cfg, r, metric, workload, world):
     bundle_bytes = sum(x["bytes"] for x in r["bundle"])
     bundle_ms = sum(x["ms"] for x in r["bundle"])
     line = {
-        "metric": metric, "value": B * world / (r["ms"] / 1e3), "unit": "reads/s", "n_gpus": world,
+        "metric": metric, "value": B / (r["ms"] / 1e3), "unit": "reads/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "%s x %s prototypes, exact int64 dots, FP64 scores" % (
@@ -744,7 +819,7 @@ def descent_line(args, cfg, r, metric, workload, world):
                    "int16_rows_from_node": r["n_wide"],
                    "l2": "inputs larger than L2: %.1f GB of prototypes, the lower ranks gathered from HBM "
                          "every step" % (r["proto_bytes"] / 1e9)},
-        "e2e": {"value": B * world / (r["e2e_ms"] / 1e3), "unit": "reads/s", "h2d_bytes_per_step": r["h2d"],
+        "e2e": {"value": B / (r["e2e_ms"] / 1e3), "unit": "reads/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / pk["hbm_gbs"], "traffic": TRAFFIC_DESCENT.get((B, split)),
@@ -786,12 +861,12 @@ def run_reference_descent(args, cfg):
     encoded and descended by the oracle on every host core (forked workers
     sharing the prototypes; no GPU in this process)."""
     import multiprocessing as mp
-    import hdc_gb300 as H
+    import hdc_synth as S
     from oracle import oracle as O
     threads = os.cpu_count() or 1
     t0 = time.time()
-    tree = H.synth_tree(cfg["tree_seed"], cfg["n_leaves"])
-    b, base, counts, ptr, idx = H.synth_tree_csr(cfg["n_leaves"])
+    tree = S.synth_tree(cfg["tree_seed"], cfg["n_leaves"])
+    b, base, counts, ptr, idx = S.synth_tree_csr(cfg["n_leaves"])
     dim = cfg["dim"]
     proto = np.empty((int(base[-1]), dim), np.int32)
     leaf0 = int(base[5])
@@ -807,7 +882,7 @@ def run_reference_descent(args, cfg):
     log("CPU prototypes built in %.1f s" % (time.time() - t0))
     _DESCENT.update(proto=proto, pn=pn, ptr=ptr, idx=idx, roots=list(range(counts[0])), levels=cfg["levels"],
                     beam=cfg["beam"], threshold=cfg["threshold"])
-    reads = make_reads(H, tree, cfg, 16 * threads * 8, cfg["read_seed"] + 999)
+    reads = make_reads(S, tree, cfg, 16 * threads * 8, cfg["read_seed"])  # the GPU arm's first reads
     vals, done = [], 0
     with mp.get_context("fork").Pool(threads) as pool:
         for i in range(args.warmup + args.steps):
@@ -842,6 +917,8 @@ def main():
                     help="reads per step; 0 = 2 x SMs x 128, whole waves of 128-query tensor-core tiles")
     ap.add_argument("--plain-batch", type=int, default=4096)
     ap.add_argument("--no-plain", action="store_true", help="skip timing the plain form beside the tc form")
+    ap.add_argument("--no-batching", action="store_true",
+                    help="c3: skip the batching form (c4 reads through the pipeline) on the same database")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--refs", type=int, default=0, help="override the number of references (small profiling cases)")
@@ -860,8 +937,6 @@ def main():
         args.form = {"c2": "plain", "c3": "tc", "c4": "pipe", "c5": "descent"}[args.config]
     if args.refs:
         cfg["n_leaves"] = args.refs
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
     if cfg.get("sigma"):
         reads_desc = "log-normal reads (median %d bp, sigma %.1f, %d-%d bp, %d%% with %d%% sub:ins:del 3:1:1)" % (
             cfg["read_len"], cfg["sigma"], cfg["min_read"], cfg["max_read"], 100 * cfg["mixed_frac"],
@@ -877,9 +952,15 @@ def main():
                                                                                                   cfg["levels"])
         workload = "%s: %d leaves + internal prototypes D=%d k=%d, %s" % (
             args.config, cfg["n_leaves"], cfg["dim"], cfg["kmer"], reads_desc)
+    if int(os.environ.get("WORLD_SIZE", "1")) > 1 or args.gpus > 1:
+        # single-GPU library: the tensor-core search's multicast loads stay within one GPU's memory
+        if int(os.environ.get("RANK", "0")) == 0:
+            print(json.dumps({"impl": args.impl, "metric": metric, "unit": "reads/s", "n_gpus": args.gpus,
+                              "unavailable": "single-GPU library: every form runs on one GPU (reads are "
+                                             "independent; run one process per GPU as separate replicas)"}),
+                  flush=True)
+        return
     if args.impl == "reference" and args.form == "descent":
-        if rank != 0:
-            return
         v, threads, done = run_reference_descent(args, cfg)
         line = {"impl": "reference", "metric": metric, "value": v, "unit": "reads/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "int64",
@@ -892,40 +973,32 @@ def main():
         print(json.dumps(line), flush=True)
         return
     if args.impl == "reference":
-        if rank != 0:
-            return
         v, threads, done = run_reference(args, cfg)
         line = {"impl": "reference", "metric": metric, "value": v, "unit": "reads/s", "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "int64",
                 "data": "synthetic", "config": {"workload": workload},
                 "cpu_baseline": {"value": v, "unit": "reads/s", "cores": threads, "kind": "port",
-                                 "sample": "%d reads per step (HVCache::compute restated + brute-force int64 "
-                                           "cosine over all %d references); database rows built on the CPU%s" %
-                                           (done, cfg["n_leaves"], " as 8 x leaf encodings" if cfg["copies"] else "")},
+                                 "sample": "%d reads per step, 2 per core, from the GPU arm's own reads "
+                                           "(HVCache::compute restated + brute-force int64 cosine over all %d "
+                                           "references); database rows built on the CPU from the same workload%s; "
+                                           "%s" % (done, cfg["n_leaves"], " (sums of the same 8 noisy copies)"
+                                                   if cfg["copies"] else "", PORT_NOTE)},
                 "e2e": {"value": v, "unit": "reads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
 
     import torch
-    if world > 1:
-        torch.distributed.init_process_group("nccl")
     if args.batch <= 0:
-        sms = torch.cuda.get_device_properties(int(os.environ.get("LOCAL_RANK", 0))).multi_processor_count
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
         args.batch = 2 * sms * 128
     if args.form == "descent":
-        r = run_descent(args, cfg, rank, world)
-        if rank == 0:
-            print(json.dumps(descent_line(args, cfg, r, metric, workload, world)), flush=True)
-        if world > 1:
-            torch.distributed.destroy_process_group()
+        r = run_descent(args, cfg)
+        print(json.dumps(descent_line(args, cfg, r, metric, workload)), flush=True)
         return
-    r = run_ours(args, cfg, rank, world)
-    if rank != 0:
-        torch.distributed.destroy_process_group()
-        return
+    r = run_ours(args, cfg)
     pk, src = peaks()
     B = args.batch
-    value = B * world / (r["ms"] / 1e3)
+    value = B / (r["ms"] / 1e3)
     dim, nr = cfg["dim"], r["refs"]
     if args.form in ("tc", "pipe"):
         # tensor work per read: one fp16 MMA pass per limb, 2*D*R*limbs flops
@@ -952,13 +1025,13 @@ def main():
                 "kernel": "plain_kernel + merge on CUDA cores; algorithmic 2*D*R per read"}
         dtype = "int16 (exact integer dots on the fp32 pipe), FP64 scores"
     line = {
-        "metric": metric, "value": value, "unit": "reads/s", "n_gpus": world, "steps": args.steps,
+        "metric": metric, "value": value, "unit": "reads/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded 6-rank tree, see bench.py)",
         "config": {"workload": workload, "form": args.form, "batch_reads": B,
                    "l2": "inputs larger than L2: %.0f MB reference database streamed every step" %
                          (nr * dim * 2 * max(1, r["limbs"]) / 1e6)},
-        "e2e": {"value": B * world / (r["e2e_ms"] / 1e3), "unit": "reads/s", "h2d_bytes_per_step": r["h2d"],
+        "e2e": {"value": B / (r["e2e_ms"] / 1e3), "unit": "reads/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"]},
         "roofline": roof, "clocks": r["clocks"], "gpu_launches": r["launches"],
     }
@@ -980,14 +1053,15 @@ def main():
                            "note": "the same count-valued reads as fp16 queries on the tensor cores, the "
                                    "database's limbs sized for the largest count (exact)"}
     if not args.no_cpu_baseline:
-        v, threads, done = cpu_baseline(cfg, r["tree"], r["refs_host"])
+        v, threads, done, parity = cpu_baseline(cfg, r["refs_host"], r["reads"], r["gpu_first"])
         line["cpu_baseline"] = {"value": v, "unit": "reads/s", "cores": threads, "kind": "port",
-                                "sample": "%d reads of the same workload (encode + brute-force top-%d against "
-                                          "all %d references; database hypervectors from the GPU encoder, "
-                                          "bit-identical to the oracle's)" % (done, cfg["topk"], nr)}
+                                "sample": "the first %d reads of the timed batch, %d per call (encode + "
+                                          "brute-force top-%d against all %d references, the database rows copied "
+                                          "from the device); %s" % (done, 2 * threads, cfg["topk"], nr, PORT_NOTE)}
+        line["parity_sample"] = parity
+    if "batching" in r:
+        line["batching_form"] = batching_line(args, r["batching"], r.get("refs_host"), pk)
     print(json.dumps(line), flush=True)
-    if world > 1:
-        torch.distributed.destroy_process_group()
 
 
 if __name__ == "__main__":

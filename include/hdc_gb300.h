@@ -60,7 +60,8 @@ extern "C" {
 #define HDC_OUT_SIGN_BITS 7    /* the +1/-1 signs as bits (0 -> +1): bit b of uint32 word w of a
                                   row is set when element 32 w + b is >= 0, bits past dim are 0;
                                   out_stride in words (>= ceil(dim / 32)); the reads of
-                                  hdc_beam_search_split_bits */
+                                  hdc_beam_search_split_bits, which reads rows of exactly
+                                  dim / 32 words: encode them with out_stride == dim / 32 */
 
 typedef struct hdc_context hdc_context;
 typedef struct hdc_refdb hdc_refdb;
@@ -215,9 +216,12 @@ int hdc_search_tc(hdc_context* ctx, const hdc_refdb* db, const void* d_q, const 
  *   - a batch whose workspace (hdc_search_workspace_bytes) exceeds
  *     HDC_NOALLOC_SCRATCH_BYTES is rejected with HDC_ERR_RANGE and a message
  *     naming both sizes; pass fewer queries per call;
- *   - the context's device must be the current device; the first call on a
- *     device looks up the scratch's device address there (once per device),
- *     so make that first call before any stream capture;
+ *   - k is checked first (1..32 after clamping to nr, else HDC_ERR_INVALID,
+ *     as hdc_search_plain), then the scratch size;
+ *   - the context's device must be the current device; the first call with
+ *     a context looks up the scratch's device address on its device (once
+ *     per context), so make that first call before any stream capture;
+ *     after cudaDeviceReset create new contexts, which look it up again;
  *   - every call on a device uses the same scratch, which keeps the previous
  *     call's contents (the search overwrites every entry it reads, so
  *     nothing needs clearing); calls that overlap on the GPU (other streams,
@@ -324,7 +328,9 @@ int hdc_beam_search_split(hdc_context* ctx, const int8_t* d_q, const int64_t* d_
                           int levels, int beam, double threshold, int score_mode, int32_t* d_path,
                           float* d_path_score, int32_t* d_depth, void* stream);
 /* The same with the reads as sign bits d_qbits [nq][dim / 32] (HDC_OUT_SIGN_BITS
- * rows, 16-byte aligned): no int8 rows and no packing pass.  As
+ * rows, 16-byte aligned): no int8 rows and no packing pass.  Row q starts at
+ * word q * (dim / 32): the rows must be dense, so encode them with
+ * out_stride == dim / 32 (a wider stride would be misread).  As
  * hdc_beam_search_split for everything else; needs the grouped descent. */
 int hdc_beam_search_split_bits(hdc_context* ctx, const uint32_t* d_qbits, const int64_t* d_qnorm2, int64_t nq,
                                const int32_t* d_proto32, int64_t n_wide, const int16_t* d_proto16,

@@ -1,7 +1,8 @@
 /*
- * hdc_synth.h -- seeded synthetic 16S-like workloads (host code in
- * libhdc_gb300).  They stand in for the reference's real-data front ends,
- * which need data absent here: the SILVA / Greengenes inductors
+ * hdc_synth.h -- seeded synthetic 16S-like workloads (host C++ in its own
+ * library, libhdc_synth.so, kept apart from the GPU library libhdc_gb300.so).
+ * They stand in for the reference's real-data front ends, which need data
+ * absent here: the SILVA / Greengenes inductors
  * (db_inductors/induct_silva.py:95-181 writes taxonomy_index.tsv and one FASTA
  * per leaf) and the ART-based read simulator (tests/Make_Mixed_Sample.py:
  * 96-97,137-143,185-197,210).  Every item is derived from its own

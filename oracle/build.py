@@ -6,7 +6,8 @@ import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
-REF_ROOT = os.environ.get("REF_ROOT", "/root/reference")
+# the reference checkout: $REF_ROOT, else a directory "reference" beside this repository
+REF_ROOT = os.environ.get("REF_ROOT", os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 
 
 def build_oracle(force=False):

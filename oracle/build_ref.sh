@@ -9,8 +9,9 @@
 # Flags follow the reference's Release build (src/CMakeLists.txt:28 and
 # install.sh:3): -O3 -march=native -ffast-math, NORM_COSINE on.
 set -e
-REF=${REF_ROOT:-/root/reference}
+# the reference checkout: $REF_ROOT, else a directory "reference" beside this repository
 HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${REF_ROOT:-$(cd "$HERE/../.." && pwd)/reference}
 D=$1; K=$2; L=$3; S=$4
 [ -n "$S" ] || { echo "usage: $0 DIM KMER WINDOW STEP" >&2; exit 1; }
 [ -f "$REF/src/HV.cpp" ] || { echo "reference sources not found under $REF" >&2; exit 3; }

@@ -7,8 +7,9 @@
 # Output in oracle/_ref/.  Test infrastructure only; needs the reference.
 #   sh oracle/build_ref_identify.sh <HV_DIM> <KMER_SIZE> <SEQUENCE_LENGTH> <SIM_STEP>
 set -e
-REF=${REF_ROOT:-/root/reference}
+# the reference checkout: $REF_ROOT, else a directory "reference" beside this repository
 HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${REF_ROOT:-$(cd "$HERE/../.." && pwd)/reference}
 D=$1; K=$2; L=$3; S=$4
 [ -n "$S" ] || { echo "usage: $0 DIM KMER WINDOW STEP" >&2; exit 1; }
 mkdir -p "$HERE/_ref"

@@ -6,8 +6,9 @@
 # Test infrastructure only (golden vectors); needs the reference checkout.
 #   sh oracle/build_ref_propagate.sh <HV_DIM> <KMER_SIZE> <SEQUENCE_LENGTH> <SIM_STEP>
 set -e
-REF=${REF_ROOT:-/root/reference}
+# the reference checkout: $REF_ROOT, else a directory "reference" beside this repository
 HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${REF_ROOT:-$(cd "$HERE/../.." && pwd)/reference}
 D=$1; K=$2; L=$3; S=$4
 [ -n "$S" ] || { echo "usage: $0 DIM KMER WINDOW STEP" >&2; exit 1; }
 mkdir -p "$HERE/_ref"

@@ -341,6 +341,40 @@ static void fast_free(fast_tables* f) {
     for (int p = 0; p < f->np; ++p) free(f->tab[p]);
 }
 
+/* ripple-carry add of one binder's bits into a bit-sliced counter */
+static void planes_add(uint64_t* planes, int nplanes, int W, const uint64_t* word) {
+    for (int w = 0; w < W; ++w) {
+        uint64_t c = word[w];
+        for (int b = 0; b < nplanes && c; ++b) {
+            uint64_t t = planes[(size_t)b * W + w] & c;
+            planes[(size_t)b * W + w] ^= c;
+            c = t;
+        }
+    }
+}
+
+/* the binder of canonical k-mer code `canon` from the fragment tables */
+static void fast_binder(const fast_tables* f, int64_t canon, uint64_t* word) {
+    const int W = f->W, k = f->k;
+    const uint64_t* rows[4];
+    for (int q = 0; q < f->np; ++q) {
+        int shift = 2 * (k - f->first[q] - f->len[q]);
+        rows[q] = f->tab[q] + (size_t)((canon >> shift) & ((1 << (2 * f->len[q])) - 1)) * W;
+    }
+    for (int w = 0; w < W; ++w) {
+        uint64_t x = rows[0][w];
+        for (int q = 1; q < f->np; ++q) x ^= rows[q][w];
+        word[w] = x;
+    }
+}
+
+/* value of element d of a bit-sliced counter */
+static int32_t planes_get(const uint64_t* planes, int nplanes, int W, int d) {
+    int32_t c = 0;
+    for (int b = 0; b < nplanes; ++b) c |= (int32_t)((planes[(size_t)b * W + (d >> 6)] >> (d & 63)) & 1) << b;
+    return c;
+}
+
 /* counts[d] for d < dim into acc (int32), returns the number of k-mers */
 static int64_t fast_encode_one(const fast_tables* f, const char* seq, int64_t len, int32_t* acc, uint64_t* planes,
                                int nplanes, uint64_t* word) {
@@ -350,31 +384,11 @@ static int64_t fast_encode_one(const fast_tables* f, const char* seq, int64_t le
     for (int64_t p = 0; p + k <= len; ++p) {
         int64_t canon = orc_canonical(seq + p, k);
         if (canon < 0) continue;
-        const uint64_t* rows[4];
-        for (int q = 0; q < f->np; ++q) {
-            int shift = 2 * (k - f->first[q] - f->len[q]);
-            rows[q] = f->tab[q] + (size_t)((canon >> shift) & ((1 << (2 * f->len[q])) - 1)) * W;
-        }
-        for (int w = 0; w < W; ++w) {
-            uint64_t x = rows[0][w];
-            for (int q = 1; q < f->np; ++q) x ^= rows[q][w];
-            word[w] = x;
-        }
-        for (int w = 0; w < W; ++w) { /* ripple-carry add into the bit-sliced counter */
-            uint64_t c = word[w];
-            for (int b = 0; b < nplanes && c; ++b) {
-                uint64_t t = planes[(size_t)b * W + w] & c;
-                planes[(size_t)b * W + w] ^= c;
-                c = t;
-            }
-        }
+        fast_binder(f, canon, word);
+        planes_add(planes, nplanes, W, word);
         ++n;
     }
-    for (int d = 0; d < f->dim; ++d) {
-        int32_t c = 0;
-        for (int b = 0; b < nplanes; ++b) c |= (int32_t)((planes[(size_t)b * W + (d >> 6)] >> (d & 63)) & 1) << b;
-        acc[d] = 2 * c - (int32_t)n;
-    }
+    for (int d = 0; d < f->dim; ++d) acc[d] = 2 * planes_get(planes, nplanes, W, d) - (int32_t)n;
     return n;
 }
 
@@ -427,6 +441,138 @@ int orc_encode_bundles(int dim, int k, const char* buf, const int64_t* off, cons
     for (int i = 0; i < nthreads; ++i) {
         jobs[i] = (fast_job){&f, buf, off, len, n, group, out, i, nthreads};
         pthread_create(&th[i], NULL, fast_worker, &jobs[i]);
+    }
+    for (int i = 0; i < nthreads; ++i) pthread_join(th[i], NULL);
+    fast_free(&f);
+    tables_free(&t);
+    return 0;
+}
+
+/* Bundles of noisy copies, computed from differences (test infrastructure:
+ * builds the same rows as orc_encode_bundles on the copies, faster).
+ * out[i] = sum over c < group of encode(copy[i * group + c]).  A copy of the
+ * same length as its source leaf differs from it only in the k-mers that
+ * overlap a changed base, so
+ *   count_bits(bundle) = group * bits(leaf) + bits(new k-mers) - bits(old k-mers)
+ *   n_kmers(bundle)    = group * n(leaf)    + n(new)           - n(old)
+ * and element d is 2 * count_bits[d] - n_kmers (the HVCache::compute sum,
+ * src/encoder.cpp:106-132, over every copy).  A copy whose length differs is
+ * encoded whole.  Three bit-sliced counters (leaf, added, removed). */
+typedef struct {
+    const fast_tables* f;
+    const char *leaf_buf, *copy_buf;
+    const int64_t *leaf_off, *leaf_len, *copy_off, *copy_len;
+    int64_t n_leaves;
+    int group;
+    int32_t* out;
+    int tid, nthreads;
+} delta_job;
+
+static void* delta_worker(void* arg) {
+    delta_job* j = (delta_job*)arg;
+    const fast_tables* f = j->f;
+    const int dim = f->dim, W = f->W, k = f->k, np = 17;
+    uint64_t* pl = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)np * W);
+    uint64_t* pa = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)np * W);
+    uint64_t* ps = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)np * W);
+    uint64_t* word = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)W);
+    int32_t* acc = (int32_t*)malloc(sizeof(int32_t) * (size_t)dim);
+    int64_t cap = 0;
+    uint8_t* mark = NULL;
+    for (int64_t i = j->tid; i < j->n_leaves; i += j->nthreads) {
+        const char* leaf = j->leaf_buf + j->leaf_off[i];
+        const int64_t L = j->leaf_len[i];
+        if (L + 1 > cap) {
+            cap = L + 1;
+            mark = (uint8_t*)realloc(mark, (size_t)cap);
+        }
+        memset(pl, 0, sizeof(uint64_t) * (size_t)np * W);
+        memset(pa, 0, sizeof(uint64_t) * (size_t)np * W);
+        memset(ps, 0, sizeof(uint64_t) * (size_t)np * W);
+        int64_t n_leaf = 0, n_add = 0, n_sub = 0;
+        for (int64_t p = 0; p + k <= L; ++p) {
+            int64_t c = orc_canonical(leaf + p, k);
+            if (c < 0) continue;
+            fast_binder(f, c, word);
+            planes_add(pl, np, W, word);
+            ++n_leaf;
+        }
+        for (int g = 0; g < j->group; ++g) {
+            const int64_t s = i * j->group + g;
+            const char* cp = j->copy_buf + j->copy_off[s];
+            const int64_t CL = j->copy_len[s];
+            if (CL != L) { /* not a substitution-only copy: encode it whole */
+                for (int64_t p = 0; p + k <= CL; ++p) {
+                    int64_t c = orc_canonical(cp + p, k);
+                    if (c < 0) continue;
+                    fast_binder(f, c, word);
+                    planes_add(pa, np, W, word);
+                    ++n_add;
+                }
+                /* the leaf term counted this copy as the leaf: take one leaf back out */
+                for (int64_t p = 0; p + k <= L; ++p) {
+                    int64_t c = orc_canonical(leaf + p, k);
+                    if (c < 0) continue;
+                    fast_binder(f, c, word);
+                    planes_add(ps, np, W, word);
+                }
+                n_sub += n_leaf;
+                continue;
+            }
+            memset(mark, 0, (size_t)cap);
+            for (int64_t b = 0; b < L; ++b) {
+                if (cp[b] == leaf[b]) continue;
+                const int64_t lo = b - k + 1 > 0 ? b - k + 1 : 0;
+                for (int64_t p = lo; p <= b && p + k <= L; ++p) mark[p] = 1;
+            }
+            for (int64_t p = 0; p + k <= L; ++p) {
+                if (!mark[p]) continue;
+                int64_t co = orc_canonical(leaf + p, k), cn = orc_canonical(cp + p, k);
+                if (co >= 0) {
+                    fast_binder(f, co, word);
+                    planes_add(ps, np, W, word);
+                    ++n_sub;
+                }
+                if (cn >= 0) {
+                    fast_binder(f, cn, word);
+                    planes_add(pa, np, W, word);
+                    ++n_add;
+                }
+            }
+        }
+        const int64_t n_tot = (int64_t)j->group * n_leaf + n_add - n_sub;
+        int32_t* dst = j->out + (size_t)i * dim;
+        for (int d = 0; d < dim; ++d) {
+            const int64_t bits = (int64_t)j->group * planes_get(pl, np, W, d) + planes_get(pa, np, W, d) -
+                                 planes_get(ps, np, W, d);
+            dst[d] = (int32_t)(2 * bits - n_tot);
+        }
+    }
+    free(mark);
+    free(acc);
+    free(word);
+    free(ps);
+    free(pa);
+    free(pl);
+    return NULL;
+}
+
+int orc_encode_copy_bundles(int dim, int k, const char* leaf_buf, const int64_t* leaf_off, const int64_t* leaf_len,
+                            int64_t n_leaves, const char* copy_buf, const int64_t* copy_off, const int64_t* copy_len,
+                            int group, int32_t* out, int nthreads) {
+    if (group < 1) return -1;
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    orc_tables t;
+    tables_init(&t, dim, k);
+    fast_tables f;
+    fast_init(&f, &t);
+    pthread_t th[256];
+    delta_job jobs[256];
+    for (int i = 0; i < nthreads; ++i) {
+        jobs[i] = (delta_job){&f, leaf_buf, copy_buf, leaf_off, leaf_len, copy_off, copy_len, n_leaves, group, out, i,
+                              nthreads};
+        pthread_create(&th[i], NULL, delta_worker, &jobs[i]);
     }
     for (int i = 0; i < nthreads; ++i) pthread_join(th[i], NULL);
     fast_free(&f);
@@ -576,6 +722,8 @@ typedef struct {
     int32_t max_abs_r; /* max |reference element| (int16 rows) */
     float* out_s;
     int32_t* out_i;
+    double* out_c;    /* optional: FP64 cosine of each hit */
+    int64_t* out_dot; /* optional: exact dot of each hit */
     int tid, nthreads;
 } cls_job;
 
@@ -586,6 +734,7 @@ static void* cls_worker(void* arg) {
     uint64_t* tmp = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)j->t->W);
     float* bs = (float*)malloc(sizeof(float) * (size_t)k);
     int32_t* bi = (int32_t*)malloc(sizeof(int32_t) * (size_t)k);
+    int64_t* bd = (int64_t*)malloc(sizeof(int64_t) * (size_t)k);
     int16_t* q16 = (int16_t*)malloc(sizeof(int16_t) * (size_t)dim);
     for (int64_t s = j->tid; s < j->n; s += j->nthreads) {
         encode_one(j->t, j->buf + j->off[s], j->len[s], acc, tmp);
@@ -625,18 +774,23 @@ static void* cls_worker(void* arg) {
             while (pos > 0 && better(sc, (int32_t)ri, bs[pos - 1], bi[pos - 1])) {
                 bs[pos] = bs[pos - 1];
                 bi[pos] = bi[pos - 1];
+                bd[pos] = bd[pos - 1];
                 --pos;
             }
             bs[pos] = sc;
             bi[pos] = (int32_t)ri;
+            bd[pos] = dot;
             if (filled < k) ++filled;
         }
         for (int t = 0; t < k; ++t) {
             j->out_s[s * k + t] = t < filled ? bs[t] : -INFINITY;
             j->out_i[s * k + t] = t < filled ? bi[t] : -1;
+            if (j->out_c) j->out_c[s * k + t] = t < filled ? cos_from(bd[t], qn, j->rn[bi[t]]) : 0.0;
+            if (j->out_dot) j->out_dot[s * k + t] = t < filled ? bd[t] : 0;
         }
     }
     free(q16);
+    free(bd);
     free(bi);
     free(bs);
     free(tmp);
@@ -644,9 +798,11 @@ static void* cls_worker(void* arg) {
     return NULL;
 }
 
-int orc_classify(int dim, int kmer, const char* buf, const int64_t* off, const int64_t* len, int64_t n,
-                 const void* refs, int ref_bytes, int64_t nr, int k, int mode, int bipolar, float* out_s,
-                 int32_t* out_i, int nthreads) {
+/* Encode every read then rank it against every reference: scores and indices,
+ * and, when out_c / out_dot are given, each hit's FP64 cosine and exact dot. */
+int orc_classify_ex(int dim, int kmer, const char* buf, const int64_t* off, const int64_t* len, int64_t n,
+                    const void* refs, int ref_bytes, int64_t nr, int k, int mode, int bipolar, float* out_s,
+                    int32_t* out_i, double* out_c, int64_t* out_dot, int nthreads) {
     if (nthreads < 1) nthreads = 1;
     if (nthreads > 256) nthreads = 256;
     orc_tables t;
@@ -667,14 +823,21 @@ int orc_classify(int dim, int kmer, const char* buf, const int64_t* off, const i
     pthread_t th[256];
     cls_job jobs[256];
     for (int i = 0; i < nthreads; ++i) {
-        jobs[i] = (cls_job){&t, buf, off, len, n, refs, ref_bytes, rn, nr, k, mode, bipolar, max_abs_r, out_s, out_i, i,
-                            nthreads};
+        jobs[i] = (cls_job){&t,    buf,      off,   len,   n,     refs,  ref_bytes, rn, nr, k, mode, bipolar, max_abs_r,
+                            out_s, out_i, out_c, out_dot, i, nthreads};
         pthread_create(&th[i], NULL, cls_worker, &jobs[i]);
     }
     for (int i = 0; i < nthreads; ++i) pthread_join(th[i], NULL);
     free(rn);
     tables_free(&t);
     return 0;
+}
+
+int orc_classify(int dim, int kmer, const char* buf, const int64_t* off, const int64_t* len, int64_t n,
+                 const void* refs, int ref_bytes, int64_t nr, int k, int mode, int bipolar, float* out_s,
+                 int32_t* out_i, int nthreads) {
+    return orc_classify_ex(dim, kmer, buf, off, len, n, refs, ref_bytes, nr, k, mode, bipolar, out_s, out_i, NULL,
+                           NULL, nthreads);
 }
 
 /* ------------------------------------------------------------------ */

@@ -37,6 +37,9 @@ def lib():
         L.orc_cosine_i32.restype = ctypes.c_float
         L.orc_topk_i32.argtypes = [P, i64, P, i64, i32, i32, i32, P, P, P, P, i32]
         L.orc_classify.argtypes = [i32, i32, P, P, P, i64, P, i32, i64, i32, i32, i32, P, P, i32]
+        L.orc_classify_ex.argtypes = [i32, i32, P, P, P, i64, P, i32, i64, i32, i32, i32, P, P, P, P, i32]
+        L.orc_encode_copy_bundles.argtypes = [i32, i32, P, P, P, i64, P, P, P, i32, P, i32]
+        L.orc_encode_copy_bundles.restype = i32
         L.orc_bundle.argtypes = [P, i32, P, P, i64, P]
         L.orc_encode_bundles.argtypes = [i32, i32, P, P, P, i64, i32, P, i32]
         L.orc_scores_from.argtypes = [P, P, P, i64, i32, P]
@@ -115,6 +118,25 @@ def encode_bundles(buf, off, lens, dim, k, group=1, nthreads=None):
     return out
 
 
+def encode_copy_bundles(leaves, copies, group, dim, k, nthreads=None):
+    """Rows of the sums of `group` consecutive noisy copies of each leaf (exact
+    int32): the same rows as encode_bundles(copies, group), computed from each
+    leaf's encoding plus the k-mers its copies change.  leaves / copies:
+    objects with buf, off, len (copies[i * group + c] is a copy of leaf i)."""
+    lb, lo, ll = (np.ascontiguousarray(leaves.buf, np.uint8), np.ascontiguousarray(leaves.off, np.int64),
+                  np.ascontiguousarray(leaves.len, np.int64))
+    cb, co, cl = (np.ascontiguousarray(copies.buf, np.uint8), np.ascontiguousarray(copies.off, np.int64),
+                  np.ascontiguousarray(copies.len, np.int64))
+    n = len(lo)
+    if len(co) != n * group:
+        raise ValueError("encode_copy_bundles: %d copies for %d leaves x %d" % (len(co), n, group))
+    out = np.zeros((n, dim), np.int32)
+    if lib().orc_encode_copy_bundles(dim, k, _p(lb), _p(lo), _p(ll), n, _p(cb), _p(co), _p(cl), group, _p(out),
+                                     nthreads or nthreads_default()) != 0:
+        raise ValueError("encode_copy_bundles: bad group")
+    return out
+
+
 def window_segments(seqs, window, step):
     """Windows of every sequence: (len-window)//step+1 of them (none when
     len < window), window w covering [w*step, w*step+window)."""
@@ -148,8 +170,9 @@ def topk(q, r, k, mode=SCORE_NORM, nthreads=None):
     return s, i, c, d
 
 
-def classify(reads, refs, dim, kmer, k, mode=SCORE_NORM, bipolar=False, nthreads=None):
-    """Encode every read and rank it against refs [nr, dim] (int16 or int32): the CPU path."""
+def classify(reads, refs, dim, kmer, k, mode=SCORE_NORM, bipolar=False, nthreads=None, exact=False):
+    """Encode every read and rank it against refs [nr, dim] (int16 or int32): the CPU path.
+    Returns (scores f32, idx i32), or with exact=True also (FP64 cosines, int64 dots) of the hits."""
     buf, offs, lens = pack_segments(reads)
     if refs.dtype != np.int16:
         refs = np.ascontiguousarray(refs, np.int32)
@@ -157,9 +180,12 @@ def classify(reads, refs, dim, kmer, k, mode=SCORE_NORM, bipolar=False, nthreads
     n = len(lens)
     s = np.zeros((n, k), np.float32)
     i = np.zeros((n, k), np.int32)
-    lib().orc_classify(dim, kmer, _p(buf), _p(offs), _p(lens), n, _p(refs), refs.dtype.itemsize, refs.shape[0], k,
-                       mode, int(bipolar), _p(s), _p(i), nthreads or nthreads_default())
-    return s, i
+    c = np.zeros((n, k), np.float64) if exact else None
+    d = np.zeros((n, k), np.int64) if exact else None
+    lib().orc_classify_ex(dim, kmer, _p(buf), _p(offs), _p(lens), n, _p(refs), refs.dtype.itemsize, refs.shape[0],
+                          k, mode, int(bipolar), _p(s), _p(i), None if c is None else _p(c),
+                          None if d is None else _p(d), nthreads or nthreads_default())
+    return (s, i, c, d) if exact else (s, i)
 
 
 def bundle(rows, child_ptr, child_idx):

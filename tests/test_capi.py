@@ -1,16 +1,15 @@
-"""CPU checks of the C-ABI library: it builds, loads, and exports every
-symbol include/hdc_gb300.h declares (no compute call needs a GPU here)."""
+"""CPU checks of the C-ABI libraries: they build, load, and export every
+symbol their headers declare -- include/hdc_gb300.h by libhdc_gb300.so,
+include/hdc_synth.h by libhdc_synth.so (no compute call needs a GPU here)."""
 import os
 import re
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared_functions():
+def declared_functions(headers=("hdc_gb300.h",)):
     names = []
-    for h in os.listdir(os.path.join(ROOT, "include")):
-        if not h.endswith(".h"):
-            continue
+    for h in headers:
         src = open(os.path.join(ROOT, "include", h)).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
         names += re.findall(r"^[A-Za-z_][\w \*]*?\b(hdc_\w+)\s*\(", src, flags=re.M)
@@ -31,6 +30,25 @@ def test_library_exports_every_declared_symbol(hdc):
 def test_binding_covers_header(hdc):
     bound = {name for name, _, _ in hdc.SIGNATURES}
     assert set(declared_functions()) <= bound
+
+
+def test_every_header_is_checked():
+    assert sorted(h for h in os.listdir(os.path.join(ROOT, "include")) if h.endswith(".h")) == \
+        ["hdc_gb300.h", "hdc_synth.h"]
+
+
+def test_synth_library_exports_its_header():
+    import build as pkg_build
+    pkg_build.build_synth()
+    import hdc_synth
+    names = declared_functions(("hdc_synth.h",))
+    assert names == ["hdc_synth_copies", "hdc_synth_reads", "hdc_synth_tree"]
+    assert all(hasattr(hdc_synth.lib(), n) for n in names)
+    assert {n for n, _, _ in hdc_synth.SIGNATURES} == set(names)
+
+
+def test_product_library_holds_no_workload_generator(hdc):
+    assert not any(hasattr(hdc.lib(), n) for n in declared_functions(("hdc_synth.h",)))
 
 
 def test_status_strings(hdc):

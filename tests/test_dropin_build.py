@@ -9,7 +9,8 @@ import tempfile
 
 import pytest
 
-REF = os.environ.get("REF_ROOT", "/root/reference")
+from oracle.build import REF_ROOT as REF
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PKG = os.path.join(ROOT, "bacterial-classification_gb300")
 

@@ -71,3 +71,31 @@ def test_noalloc_rejects_batches_beyond_the_fixed_scratch(hdc, cuda):
         _noalloc(hdc, torch, ctx, q, qn, 1, r, rn, 1, k, hdc.SCORE_NORM)
     assert e.value.status == 2
     assert "scratch" in str(e.value)
+
+
+def test_noalloc_checks_k_before_the_scratch_size(hdc, cuda):
+    """k = 33 is an invalid argument (as for hdc_search_plain) even on a batch
+    whose lists would not fit the fixed scratch; k above nr is clamped to nr."""
+    import torch
+    dim = 64
+    ctx = hdc.Context(dim, 8, 150, 10)
+    nq = 65536
+    q = torch.ones((nq, dim), dtype=torch.int16, device=cuda)
+    r = torch.ones((64, dim), dtype=torch.int16, device=cuda)
+    qn, rn = ctx.norms(q), ctx.norms(r)
+    p = hdc.ptr
+    out = [torch.empty((nq, 32), dtype=t, device=cuda) for t in (torch.float32, torch.int32, torch.float64,
+                                                                 torch.int64)]
+    for fn in ("hdc_search_plain_noalloc", "hdc_search_plain"):
+        extra = [] if fn.endswith("noalloc") else [None, 0]
+        st = getattr(hdc.lib(), fn)(ctx.h, p(q), p(qn), nq, 1, p(r), p(rn), 64, 1, 33, hdc.SCORE_NORM,
+                                    *[p(o) for o in out], *extra, hdc.stream_ptr())
+        assert st == 1 and b"k must be in 1..32" in hdc.lib().hdc_last_error(), fn
+    # 40 > nr = 4 is clamped to 4 (a small batch: fits the scratch)
+    q4, r4 = q[:8], r[:4]
+    got = _noalloc(hdc, torch, ctx, q4, qn[:8], 1, r4, rn[:4], 1, 4, hdc.SCORE_NORM)
+    st = hdc.lib().hdc_search_plain_noalloc(ctx.h, p(q4), p(qn), 8, 1, p(r4), p(rn), 4, 1, 40, hdc.SCORE_NORM,
+                                            p(got[0]), p(got[1]), p(got[2]), p(got[3]), hdc.stream_ptr())
+    assert st == 0
+    torch.cuda.synchronize()
+    assert torch.equal(got[1][:, :4].cpu(), torch.arange(4, dtype=torch.int32).expand(8, 4))
