@@ -287,6 +287,15 @@ int hdc_context_option(hdc_context* ctx, int option, int value) {
             if (value < -1 || value > 2) return fail(HDC_ERR_INVALID, "option: beam grouping must be -1, 0, 1 or 2");
             ctx->beam_grouped = value;
             return HDC_OK;
+        case HDC_WAIT_LIMIT:
+            if (value < 0 || value > 4000000)
+                return fail(HDC_ERR_INVALID, "option: wait limit must be 0 .. 4,000,000 thousand cycles");
+            ctx->wait_cycles = (long long)value * 1000;
+            return HDC_OK;
+        case HDC_TEST_WITHHOLD_LOADS:
+            if (value < 0 || value > 1) return fail(HDC_ERR_INVALID, "option: withhold must be 0 or 1");
+            ctx->test_withhold_loads = value;
+            return HDC_OK;
         default:
             return fail(HDC_ERR_INVALID, "option: unknown option");
     }

@@ -37,6 +37,8 @@ struct hdc_context {
     int tc_scatter = -1;            // tensor-core search: 1 scattered reference-tile order, 0 index order (-1: auto)
     int beam_grouped = -1;          // descent: 1 grouped by candidate node, 2 + tensor-core levels, 0 warp per read
     void* noalloc_scratch = nullptr;  // device address of hdc_search_plain_noalloc's fixed scratch (first call)
+    long long wait_cycles = 0;        // tensor-core search: limit of its bounded waits in SM cycles (0: default)
+    int test_withhold_loads = 0;      // tensor-core search: test hook, the producer issues no loads
 };
 
 // A tensor-core reference database (hdc_refdb_create).
@@ -78,9 +80,9 @@ int launch_search_plain(hdc_context* ctx, const int16_t* d_q, const int64_t* d_q
                         size_t work_bytes, cudaStream_t stream);
 
 // Merge n_lists partial top-k lists per query ([n_lists][nq][k] keys and dots)
-// into the final outputs.
+// into the final outputs; keys whose index is not below nr count as empty.
 int launch_merge(const uint64_t* ws_key, const int64_t* ws_dot, int n_lists, int64_t nq, int k, const int64_t* d_qn,
-                 const int64_t* d_rn, float* d_score, int32_t* d_idx, double* d_cos, int64_t* d_dot,
+                 const int64_t* d_rn, int64_t nr, float* d_score, int32_t* d_idx, double* d_cos, int64_t* d_dot,
                  cudaStream_t stream);
 
 // launch_norms element code of integer-valued fp16 rows (1, 2, 4: int8 / int16 / int32)

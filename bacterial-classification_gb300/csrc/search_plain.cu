@@ -304,8 +304,8 @@ __global__ void __launch_bounds__(kThreadsP, 1) plain_kernel(const PlainArgs a) 
 // Final merge of the per-range lists: one thread per query.
 __global__ void merge_kernel(const uint64_t* __restrict__ ws_key, const int64_t* __restrict__ ws_dot, int n_splits,
                              int64_t nq, int k, const int64_t* __restrict__ qn, const int64_t* __restrict__ rn,
-                             float* __restrict__ out_s, int32_t* __restrict__ out_i, double* __restrict__ out_c,
-                             int64_t* __restrict__ out_d) {
+                             int64_t nr, float* __restrict__ out_s, int32_t* __restrict__ out_i,
+                             double* __restrict__ out_c, int64_t* __restrict__ out_d) {
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nq) return;
     uint64_t keys[kMaxK];
@@ -326,7 +326,9 @@ __global__ void merge_kernel(const uint64_t* __restrict__ ws_key, const int64_t*
     const int64_t nqv = qn[q];
     for (int i = 0; i < k; ++i) {
         const uint32_t idx = key_idx(keys[i]);
-        const bool ok = keys[i] != 0;
+        // a list a search left unwritten (a bounded wait that gave up) holds stale keys: never
+        // follow an index past the references
+        const bool ok = keys[i] != 0 && (int64_t)idx < nr;
         out_s[q * k + i] = ok ? key_score(keys[i]) : -INFINITY;
         out_i[q * k + i] = ok ? (int32_t)idx : -1;
         if (out_c) out_c[q * k + i] = ok ? exact_cos(dots[i], nqv, rn[idx]) : 0.0;
@@ -445,14 +447,14 @@ int launch_search_plain(hdc_context* ctx, const int16_t* d_q, const int64_t* d_q
     else
         st = vec ? launch_plain_t<8, false, true>(a, nq, stream) : launch_plain_t<8, false, false>(a, nq, stream);
     if (st != HDC_OK) return st;
-    return launch_merge(a.ws_key, a.ws_dot, a.n_splits, nq, k, d_qn, d_rn, d_score, d_idx, d_cos, d_dot, stream);
+    return launch_merge(a.ws_key, a.ws_dot, a.n_splits, nq, k, d_qn, d_rn, nr, d_score, d_idx, d_cos, d_dot, stream);
 }
 
 int launch_merge(const uint64_t* ws_key, const int64_t* ws_dot, int n_lists, int64_t nq, int k, const int64_t* d_qn,
-                 const int64_t* d_rn, float* d_score, int32_t* d_idx, double* d_cos, int64_t* d_dot,
+                 const int64_t* d_rn, int64_t nr, float* d_score, int32_t* d_idx, double* d_cos, int64_t* d_dot,
                  cudaStream_t stream) {
     const int mt = 128;
-    merge_kernel<<<(unsigned)((nq + mt - 1) / mt), mt, 0, stream>>>(ws_key, ws_dot, n_lists, nq, k, d_qn, d_rn,
+    merge_kernel<<<(unsigned)((nq + mt - 1) / mt), mt, 0, stream>>>(ws_key, ws_dot, n_lists, nq, k, d_qn, d_rn, nr,
                                                                   d_score, d_idx, d_cos, d_dot);
     cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? HDC_OK : cuda_fail(e, "search: merge launch");

@@ -105,6 +105,8 @@ struct TcArgs {
     int slist;  // 1: the top-k lists live in shared memory after the tile ring, else in local memory
     int limb_bits;     // the database's limbs are base-2^limb_bits digits
     float limb_base;   // 2^limb_bits
+    long long wait_cycles;  // limit of the pipeline's bounded waits (SM cycles)
+    int withhold;           // test hook: the producer issues no loads, so the waits run out
 };
 
 // Insert (key, dot) into a descending list of length k whose entry i is at keys[i * st].
@@ -234,13 +236,15 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             const uint64_t pol_q = tc::make_policy_evict_last(), pol_r = tc::make_policy_evict_first();
             const bool hint_q = a.policy >= 1, hint_r = a.policy >= 2;
             const int rank = crank;
-            for (int grp = 0; ok && grp < a.n_groups; ++grp) {
+            // a.withhold (tests of the bounded waits): no load is issued, so the MMA issuer's and the
+            // epilogue's waits run out with nothing in flight
+            for (int grp = 0; ok && !a.withhold && grp < a.n_groups; ++grp) {
                 if (grp * a.G + lead_slot >= a.n_qtiles) continue;
                 const int qt = min(grp * a.G + gslot, a.n_qtiles - 1);
                 for (int t0 = t_first; ok && t0 < t_end; t0 += a.S) {
                     const int t = (int)((int64_t)min(t0 + t_off, a.n_rtiles - 1) * a.t_stride % a.n_rtiles);
                     for (int kb = 0; kb < a.n_kblocks; ++kb) {
-                        if (!tc::mbar_wait(&empty_bar[stage], phase ^ 1, &err_s, 1)) {
+                        if (!tc::mbar_wait(&empty_bar[stage], phase ^ 1, &err_s, 1, a.wait_cycles)) {
                             ok = false;
                             break;
                         }
@@ -350,15 +354,15 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             for (int grp = 0; ok && grp < a.n_groups; ++grp) {
                 if (grp * a.G + lead_slot >= a.n_qtiles) continue;
                 for (int t0 = t_first; ok && t0 < t_end; t0 += a.S) {
-                    if (!(PAIR_MMA ? tc::mbar_wait_cluster(&acce_bar[acc], acc_phase ^ 1, &err_s, 2)
-                                   : tc::mbar_wait(&acce_bar[acc], acc_phase ^ 1, &err_s, 2))) {
+                    if (!(PAIR_MMA ? tc::mbar_wait_cluster(&acce_bar[acc], acc_phase ^ 1, &err_s, 2, a.wait_cycles)
+                                   : tc::mbar_wait(&acce_bar[acc], acc_phase ^ 1, &err_s, 2, a.wait_cycles))) {
                         ok = false;
                         break;
                     }
                     tc::fence_after();
                     const uint32_t d0 = tmem + (uint32_t)acc * kAccCols;
                     for (int kb = 0; kb < a.n_kblocks; ++kb) {
-                        if (!tc::mbar_wait(&full_bar[stage], phase, &err_s, 3)) {
+                        if (!tc::mbar_wait(&full_bar[stage], phase, &err_s, 3, a.wait_cycles)) {
                             ok = false;
                             break;
                         }
@@ -503,7 +507,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 // the tile the producer loaded (a step past the last tile keeps its columns past nr)
                 const int t = t0 + t_off < a.n_rtiles ? (int)((int64_t)(t0 + t_off) * a.t_stride % a.n_rtiles)
                                                       : t0 + t_off;
-                if (!tc::mbar_wait(&accf_bar[acc], acc_phase, &err_s, 4)) {
+                if (!tc::mbar_wait(&accf_bar[acc], acc_phase, &err_s, 4, a.wait_cycles)) {
                     ok = false;
                     break;
                 }
@@ -1033,6 +1037,8 @@ static int search_part(hdc_context* ctx, const hdc_refdb* db, const __half* d_q,
     a.limb_bits = db->limb_bits;
     a.limb_base = (float)(1 << db->limb_bits);
     a.status = d_status;
+    a.wait_cycles = ctx->wait_cycles > 0 ? ctx->wait_cycles : tc::kWaitCycles;
+    a.withhold = ctx->test_withhold_loads;
     a.policy = ctx->tc_policy >= 0 ? ctx->tc_policy : tc_default_policy();
     a.prefetch = ctx->tc_prefetch >= 0 ? ctx->tc_prefetch : tc_default_prefetch();
     a.t_stride = (ctx->tc_scatter >= 0 ? ctx->tc_scatter : tc_default_scatter()) ? tile_stride(a.n_rtiles) : 1;
@@ -1096,7 +1102,8 @@ static int search_part(hdc_context* ctx, const hdc_refdb* db, const __half* d_q,
         ctx->tc_last_shape[4] = 0;
     }
     ctx->tc_last_shape[4] += 2;  // the search kernel and its merge
-    return launch_merge(a.ws_key, a.ws_dot, a.S, nq, k, d_qn, db->d_norm2, d_score, d_idx, d_cos, d_dot, stream);
+    return launch_merge(a.ws_key, a.ws_dot, a.S, nq, k, d_qn, db->d_norm2, db->nr, d_score, d_idx, d_cos, d_dot,
+                        stream);
 }
 
 

@@ -8,8 +8,10 @@
 namespace hdc {
 namespace tc {
 
-// A bounded wait gives up after this many SM cycles (about 2 s at 2 GHz); a
-// normal wait in these kernels lasts at most one reference tile (~1e5 cycles).
+// A bounded wait gives up after this many SM cycles (about 2 s at 2 GHz) unless
+// the caller passes another limit; a normal wait in these kernels lasts at
+// most one reference tile (~1e5 cycles).  The drains before a CTA exits
+// (waits for copies and commits already issued) always use this limit.
 constexpr long long kWaitCycles = 4000000000LL;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -45,14 +47,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t addr, uint32_t parity) {
 // false when the CTA's error flag is raised (by this wait running out of
 // time, or by another warp that gave up), so that every role can leave its
 // loop and reach the common teardown.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* err, int code) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* err, int code,
+                                          long long limit = kWaitCycles) {
     const uint32_t addr = smem_u32(bar);
     if (mbar_try_wait(addr, parity)) return true;
     const long long t0 = clock64();
     while (true) {
         if (mbar_try_wait(addr, parity)) return true;
         if (*err) return false;
-        if (clock64() - t0 > kWaitCycles) {
+        if (clock64() - t0 > limit) {
             atomicCAS(const_cast<int*>(err), 0, code);
             return false;
         }
@@ -210,14 +213,15 @@ __device__ __forceinline__ bool mbar_try_wait_cluster(uint32_t addr, uint32_t pa
 }
 
 // mbar_wait for a barrier that other CTAs of the cluster arrive on (acquire, cluster scope).
-__device__ __forceinline__ bool mbar_wait_cluster(uint64_t* bar, uint32_t parity, volatile int* err, int code) {
+__device__ __forceinline__ bool mbar_wait_cluster(uint64_t* bar, uint32_t parity, volatile int* err, int code,
+                                                  long long limit = kWaitCycles) {
     const uint32_t addr = smem_u32(bar);
     if (mbar_try_wait_cluster(addr, parity)) return true;
     const long long t0 = clock64();
     while (true) {
         if (mbar_try_wait_cluster(addr, parity)) return true;
         if (*err) return false;
-        if (clock64() - t0 > kWaitCycles) {
+        if (clock64() - t0 > limit) {
             atomicCAS(const_cast<int*>(err), 0, code);
             return false;
         }

@@ -724,7 +724,9 @@ def cpu_baseline(cfg, refs, reads, gpu_out, min_reads=256, seconds=12.0, threads
     arm's own timed batch, against the same database (rows copied from the
     device), until both min_reads reads and `seconds` are done; the same reads'
     GPU results are compared with it (the parity sample)."""
+    from oracle import oracle as O
     threads = threads or (os.cpu_count() or 1)
+    O.ref_norms(refs, threads)  # once per database, outside the timed calls
     per_call = 2 * threads
     done, t_total, res = 0, 0.0, []
     limit = gpu_out[0].shape[0]
@@ -760,7 +762,9 @@ def run_reference(args, cfg):
     t0 = time.time()
     tree, refs = oracle_database(cfg, threads)
     log("oracle database built in %.1f s" % (time.time() - t0))
+    from oracle import oracle as O
     reads = make_reads(S, tree, cfg, 4096, cfg["read_seed"])  # the GPU arm's first reads
+    O.ref_norms(refs, threads)  # once per database, outside the timed calls
     vals, per_call = [], 2 * threads
     for i in range(args.warmup + args.steps):
         dt, _ = cpu_calls(cfg, refs, reads, (i * per_call) % len(reads), per_call, threads)

@@ -281,6 +281,15 @@ int hdc_search_tc_last_shape(const hdc_context* ctx, int32_t shape[5]);
                               with every level but the last scored on the tensor cores
                               (entries grouped by parent), 0 one warp per read, -1
                               automatic (2 when dim % 1024 == 0 and dim <= 16384, else 0) */
+#define HDC_WAIT_LIMIT 9   /* tensor-core search: its bounded device-side waits give up after
+                              value x 1,000 SM cycles, 1 .. 4,000,000 (0: the default,
+                              4,000,000, about 2 s at 2 GHz); a wait that gives up makes the
+                              search return partial results and hdc_context_status report
+                              100 + its code */
+#define HDC_TEST_WITHHOLD_LOADS 10 /* tensor-core search, for tests of the bounded waits only: 1
+                              makes the producer issue no operand loads, so the MMA issuer's
+                              and the epilogue's waits run out (after HDC_WAIT_LIMIT) with
+                              nothing in flight and the search reports a timeout; 0 off */
 int hdc_context_option(hdc_context* ctx, int option, int value);
 
 /* Hierarchical descent (config 5; targets/identify.cpp:89-202 with one

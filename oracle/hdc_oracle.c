@@ -798,28 +798,73 @@ static void* cls_worker(void* arg) {
     return NULL;
 }
 
+typedef struct {
+    const void* refs;
+    int ref_bytes, dim;
+    int64_t nr;
+    int64_t* rn;
+    int32_t max_abs; /* this thread's max |element| */
+    int tid, nthreads;
+} norms_job;
+
+static void* norms_worker(void* arg) {
+    norms_job* j = (norms_job*)arg;
+    int32_t mx = 0;
+    for (int64_t i = j->tid; i < j->nr; i += j->nthreads) {
+        int64_t s = 0;
+        for (int d = 0; d < j->dim; ++d) {
+            const int64_t v = j->ref_bytes == 2 ? ((const int16_t*)j->refs)[(size_t)i * j->dim + d]
+                                                : ((const int32_t*)j->refs)[(size_t)i * j->dim + d];
+            s += v * v;
+            const int64_t a = v < 0 ? -v : v;
+            if (a > mx) mx = a > 0x7fffffff ? 0x7fffffff : (int32_t)a;
+        }
+        j->rn[i] = s;
+    }
+    j->max_abs = mx;
+    return NULL;
+}
+
+/* Squared norms of the references (int16 or int32 rows) into rn, and the
+ * largest |element|; rows split over threads. */
+int32_t orc_ref_norms(const void* refs, int ref_bytes, int64_t nr, int dim, int64_t* rn, int nthreads) {
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    pthread_t th[256];
+    norms_job jobs[256];
+    for (int i = 0; i < nthreads; ++i) {
+        jobs[i] = (norms_job){refs, ref_bytes, dim, nr, rn, 0, i, nthreads};
+        pthread_create(&th[i], NULL, norms_worker, &jobs[i]);
+    }
+    int32_t mx = 0;
+    for (int i = 0; i < nthreads; ++i) {
+        pthread_join(th[i], NULL);
+        if (jobs[i].max_abs > mx) mx = jobs[i].max_abs;
+    }
+    return mx;
+}
+
 /* Encode every read then rank it against every reference: scores and indices,
- * and, when out_c / out_dot are given, each hit's FP64 cosine and exact dot. */
+ * and, when out_c / out_dot are given, each hit's FP64 cosine and exact dot.
+ * rn_in (optional): the references' squared norms from orc_ref_norms, with
+ * max_abs_in their largest |element|; computed here when null. */
 int orc_classify_ex(int dim, int kmer, const char* buf, const int64_t* off, const int64_t* len, int64_t n,
-                    const void* refs, int ref_bytes, int64_t nr, int k, int mode, int bipolar, float* out_s,
-                    int32_t* out_i, double* out_c, int64_t* out_dot, int nthreads) {
+                    const void* refs, int ref_bytes, int64_t nr, const int64_t* rn_in, int32_t max_abs_in, int k,
+                    int mode, int bipolar, float* out_s, int32_t* out_i, double* out_c, int64_t* out_dot,
+                    int nthreads) {
     if (nthreads < 1) nthreads = 1;
     if (nthreads > 256) nthreads = 256;
     orc_tables t;
     tables_init(&t, dim, kmer);
-    int64_t* rn = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nr > 0 ? nr : 1));
-    int32_t max_abs_r = 0;
-    for (int64_t i = 0; i < nr; ++i) {
-        int64_t s = 0;
-        for (int d = 0; d < dim; ++d) {
-            int64_t v = ref_bytes == 2 ? ((const int16_t*)refs)[(size_t)i * dim + d]
-                                       : ((const int32_t*)refs)[(size_t)i * dim + d];
-            s += v * v;
-            const int64_t a = v < 0 ? -v : v;
-            if (ref_bytes == 2 && a > max_abs_r) max_abs_r = (int32_t)a;
-        }
-        rn[i] = s;
+    int64_t* rn_own = NULL;
+    const int64_t* rn = rn_in;
+    int32_t max_abs_r = max_abs_in;
+    if (!rn) {
+        rn_own = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nr > 0 ? nr : 1));
+        max_abs_r = orc_ref_norms(refs, ref_bytes, nr, dim, rn_own, nthreads);
+        rn = rn_own;
     }
+    if (ref_bytes != 2) max_abs_r = 0; /* int32 rows are summed in int64 directly */
     pthread_t th[256];
     cls_job jobs[256];
     for (int i = 0; i < nthreads; ++i) {
@@ -828,7 +873,7 @@ int orc_classify_ex(int dim, int kmer, const char* buf, const int64_t* off, cons
         pthread_create(&th[i], NULL, cls_worker, &jobs[i]);
     }
     for (int i = 0; i < nthreads; ++i) pthread_join(th[i], NULL);
-    free(rn);
+    free(rn_own);
     tables_free(&t);
     return 0;
 }
@@ -836,8 +881,8 @@ int orc_classify_ex(int dim, int kmer, const char* buf, const int64_t* off, cons
 int orc_classify(int dim, int kmer, const char* buf, const int64_t* off, const int64_t* len, int64_t n,
                  const void* refs, int ref_bytes, int64_t nr, int k, int mode, int bipolar, float* out_s,
                  int32_t* out_i, int nthreads) {
-    return orc_classify_ex(dim, kmer, buf, off, len, n, refs, ref_bytes, nr, k, mode, bipolar, out_s, out_i, NULL,
-                           NULL, nthreads);
+    return orc_classify_ex(dim, kmer, buf, off, len, n, refs, ref_bytes, nr, NULL, 0, k, mode, bipolar, out_s, out_i,
+                           NULL, NULL, nthreads);
 }
 
 /* ------------------------------------------------------------------ */

@@ -37,7 +37,9 @@ def lib():
         L.orc_cosine_i32.restype = ctypes.c_float
         L.orc_topk_i32.argtypes = [P, i64, P, i64, i32, i32, i32, P, P, P, P, i32]
         L.orc_classify.argtypes = [i32, i32, P, P, P, i64, P, i32, i64, i32, i32, i32, P, P, i32]
-        L.orc_classify_ex.argtypes = [i32, i32, P, P, P, i64, P, i32, i64, i32, i32, i32, P, P, P, P, i32]
+        L.orc_classify_ex.argtypes = [i32, i32, P, P, P, i64, P, i32, i64, P, i32, i32, i32, i32, P, P, P, P, i32]
+        L.orc_ref_norms.argtypes = [P, i32, i64, i32, P, i32]
+        L.orc_ref_norms.restype = i32
         L.orc_encode_copy_bundles.argtypes = [i32, i32, P, P, P, i64, P, P, P, i32, P, i32]
         L.orc_encode_copy_bundles.restype = i32
         L.orc_bundle.argtypes = [P, i32, P, P, i64, P]
@@ -170,20 +172,40 @@ def topk(q, r, k, mode=SCORE_NORM, nthreads=None):
     return s, i, c, d
 
 
+_NORMS = {}  # id of a reference array -> (array, squared norms, max |element|)
+
+
+def ref_norms(refs, nthreads=None):
+    """(squared norms int64 [nr], max |element|) of reference rows, computed
+    once per array object (the array must not change in place afterwards)."""
+    hit = _NORMS.get(id(refs))
+    if hit is not None and hit[0] is refs:
+        return hit[1], hit[2]
+    r = np.ascontiguousarray(refs)
+    rn = np.zeros(r.shape[0], np.int64)
+    mx = lib().orc_ref_norms(_p(r), r.dtype.itemsize, r.shape[0], r.shape[1], _p(rn), nthreads or nthreads_default())
+    _NORMS.clear()
+    _NORMS[id(refs)] = (refs, rn, mx)
+    return rn, mx
+
+
 def classify(reads, refs, dim, kmer, k, mode=SCORE_NORM, bipolar=False, nthreads=None, exact=False):
     """Encode every read and rank it against refs [nr, dim] (int16 or int32): the CPU path.
-    Returns (scores f32, idx i32), or with exact=True also (FP64 cosines, int64 dots) of the hits."""
+    Returns (scores f32, idx i32), or with exact=True also (FP64 cosines, int64 dots) of the hits.
+    The references' norms are computed on the first call with an array and reused."""
     buf, offs, lens = pack_segments(reads)
-    if refs.dtype != np.int16:
+    if refs.dtype not in (np.int16, np.int32):
         refs = np.ascontiguousarray(refs, np.int32)
-    refs = np.ascontiguousarray(refs)
+    if not refs.flags.c_contiguous:
+        refs = np.ascontiguousarray(refs)
+    rn, mx = ref_norms(refs, nthreads)
     n = len(lens)
     s = np.zeros((n, k), np.float32)
     i = np.zeros((n, k), np.int32)
     c = np.zeros((n, k), np.float64) if exact else None
     d = np.zeros((n, k), np.int64) if exact else None
     lib().orc_classify_ex(dim, kmer, _p(buf), _p(offs), _p(lens), n, _p(refs), refs.dtype.itemsize, refs.shape[0],
-                          k, mode, int(bipolar), _p(s), _p(i), None if c is None else _p(c),
+                          _p(rn), mx, k, mode, int(bipolar), _p(s), _p(i), None if c is None else _p(c),
                           None if d is None else _p(d), nthreads or nthreads_default())
     return (s, i, c, d) if exact else (s, i)
 

@@ -365,3 +365,50 @@ def test_tc_count_queries_vs_oracle(hdc, orc, cuda, dim, nq, nr, k, mode, qmax, 
         assert np.array_equal(s, os_)
         assert np.array_equal(c, oc)
 
+
+
+# schedules: one CTA per tile; multicast pairs sharing references; pairs sharing queries;
+# pair MMA (cta_group::2); pair MMAs in clusters of 4
+@pytest.mark.parametrize("cluster,share,pair", [(1, 0, 0), (2, 0, 0), (2, 1, 0), (2, 0, 1), (4, 0, 1)])
+def test_tc_bounded_wait_runs_out_and_context_recovers(hdc, orc, cuda, cluster, share, pair):
+    """A bounded device-side wait that runs out, without faulting anything:
+    with HDC_TEST_WITHHOLD_LOADS the producer issues no operand load, so the
+    MMA issuer's wait for the first stage (and the epilogue's for the first
+    accumulators) runs out after HDC_WAIT_LIMIT with no copy and no MMA in
+    flight; every role leaves its loop, TMEM is freed and the context status
+    reports 100 + the wait's code.  The next search on the same context (hook
+    off, default limit) returns the oracle's results."""
+    import torch
+    H = hdc
+    g = np.random.default_rng(77)
+    dim, nq, nr, k = 1024, 512, 1500, 5
+    refs = g.integers(-12000, 12001, (nr, dim)).astype(np.int16)  # two limbs
+    q = np.where(g.random((nq, dim)) < 0.5, -1, 1).astype(np.int8)
+    ctx, db, tr, q16, qi, qn = _setup(hdc, cuda, refs, q, dim)
+    ctx.tc_option(H.TC_CLUSTER, cluster)
+    ctx.tc_option(H.TC_SHARE, share)
+    ctx.tc_option(H.TC_PAIR_MMA, pair)
+    assert ctx.status() == 0
+    ctx.option(H.WAIT_LIMIT, 1000)  # 10^6 SM cycles, about half a millisecond
+    ctx.option(H.TEST_WITHHOLD_LOADS, 1)
+    ctx.search_tc(db, q16, qn, 1, k, H.SCORE_NORM)
+    torch.cuda.synchronize()
+    st = ctx.status()
+    assert 101 <= st <= 104, st  # a pipeline wait of the search gave up
+    assert ctx.tc_last_shape()[0] == cluster
+    ctx.option(H.TEST_WITHHOLD_LOADS, 0)
+    ctx.option(H.WAIT_LIMIT, 0)
+    s, i, c, d = ctx.search_tc(db, q16, qn, 1, k, H.SCORE_NORM)
+    torch.cuda.synchronize()
+    assert ctx.status() == 0
+    os_, oi, oc, od = orc.topk(q.astype(np.int32), refs.astype(np.int32), k, H.SCORE_NORM)
+    assert np.array_equal(i.cpu().numpy(), oi) and np.array_equal(d.cpu().numpy(), od)
+    assert np.array_equal(s.cpu().numpy(), os_) and np.array_equal(c.cpu().numpy(), oc)
+
+
+def test_wait_options_are_checked(hdc, cuda):
+    H = hdc
+    ctx = H.Context(1024, 10, 250, 10)
+    for opt, bad in ((H.WAIT_LIMIT, -1), (H.WAIT_LIMIT, 4000001), (H.TEST_WITHHOLD_LOADS, 2)):
+        with pytest.raises(H.HDCError):
+            ctx.option(opt, bad)
