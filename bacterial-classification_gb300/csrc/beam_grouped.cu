@@ -193,9 +193,8 @@ __device__ __forceinline__ int64_t state_at(int64_t r, int b, int l) {
     return (r * kMaxBeamG + b) * kMaxLevelsG + l;
 }
 
-__global__ void count_kernel(const GArgs a, int L) {
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= a.nq) return;
+// candidates of read r at level L (0 once it is done)
+__device__ __forceinline__ int32_t count_one(const GArgs& a, int L, int64_t r) {
     int32_t c = 0;
     if (!a.done[r]) {
         if (L == 0) {
@@ -208,7 +207,13 @@ __global__ void count_kernel(const GArgs a, int L) {
             }
         }
     }
-    a.cnt[r] = c;
+    return c;
+}
+
+__global__ void count_kernel(const GArgs a, int L) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= a.nq) return;
+    a.cnt[r] = count_one(a, L, r);
 }
 
 // count_nodes: the level is scored from node-sorted pairs (score_kernel), which need the
@@ -221,9 +226,9 @@ __device__ __forceinline__ void put_pair(const GArgs& a, int32_t p, int64_t r, i
     if (count_nodes) atomicAdd(a.node_cnt + node, 1);
 }
 
-__global__ void expand_kernel(const GArgs a, int L, bool count_nodes) {
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= a.nq || a.done[r]) return;
+// the candidate pairs of read r at level L, from a.off[r] on
+__device__ void expand_one(const GArgs& a, int L, int64_t r, bool count_nodes) {
+    if (a.done[r]) return;
     int32_t p = a.off[r];
     if (L == 0) {
         for (int i = 0; i < a.n_roots; ++i) put_pair(a, p++, r, a.roots[i], 0, count_nodes);
@@ -240,12 +245,23 @@ __global__ void expand_kernel(const GArgs a, int L, bool count_nodes) {
     }
 }
 
-__global__ void scatter_kernel(const GArgs a) {
+__global__ void expand_kernel(const GArgs a, int L, bool count_nodes) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= a.nq) return;
+    expand_one(a, L, r, count_nodes);
+}
+
+// pairs p = first, first + stride, ... to their node-ordered slots
+__device__ __forceinline__ void scatter_range(const GArgs& a, int64_t first, int64_t stride) {
     const int32_t total = a.off[a.nq];
-    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < total; p += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t p = first; p < total; p += stride) {
         const int32_t pos = atomicAdd(a.cursor + a.pair_node[p], 1);
         a.sorted[pos] = (int32_t)p;
     }
+}
+
+__global__ void scatter_kernel(const GArgs a) {
+    scatter_range(a, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
 }
 
 // One warp per pair, the warps walking the pairs in node order: the pairs of a node are
@@ -350,15 +366,15 @@ __device__ __forceinline__ int64_t lane_dot16(const GArgs& a, int lane, int32_t 
 
 // ROWS16: some nodes have int16 rows (hdc_beam_search_split); without, the kernel is the
 // int32 one alone (fewer registers, every warp slot of the SM resident)
+// Warp w of nw scores the node-ordered pairs w, w + nw, ...
 template <bool ROWS16>
-__global__ void __launch_bounds__(kScoreThreads, ROWS16 ? kScoreBlocks16 : kScoreBlocks) score_kernel(const GArgs a) {
+__device__ __forceinline__ void score_pairs(const GArgs& a, int64_t w, int64_t nw) {
     const int lane = threadIdx.x & 31;
-    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int32_t total = a.off[a.nq];
     int32_t my_pi = -1, my_node = 0;
     int64_t my_r = 0, my_dot = 0;
     int i = 0;
-    for (int64_t s = (((int64_t)blockIdx.x * blockDim.x) >> 5) + (threadIdx.x >> 5); s < total; s += nw, ++i) {
+    for (int64_t s = w; s < total; s += nw, ++i) {
         const int32_t pi = a.sorted[s];
         const int32_t node = a.pair_node[pi];
         const int64_t r = a.pair_read[pi];
@@ -383,11 +399,16 @@ __global__ void __launch_bounds__(kScoreThreads, ROWS16 ? kScoreBlocks16 : kScor
         a.pair_key[my_pi] = make_key(exact_score(my_dot, a.qn[my_r], a.pn[my_node], a.mode), (uint32_t)my_node);
 }
 
+template <bool ROWS16>
+__global__ void __launch_bounds__(kScoreThreads, ROWS16 ? kScoreBlocks16 : kScoreBlocks) score_kernel(const GArgs a) {
+    score_pairs<ROWS16>(a, (((int64_t)blockIdx.x * blockDim.x) >> 5) + (threadIdx.x >> 5),
+                        ((int64_t)gridDim.x * blockDim.x) >> 5);
+}
+
 // Per read: the best `beam` candidates, then the rule of the per-read kernel (stop below
 // the threshold with the best path, else keep the entries >= threshold, at most `beam`).
-__global__ void select_kernel(const GArgs a, int L) {
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= a.nq || a.done[r]) return;
+__device__ void select_one(const GArgs& a, int L, int64_t r) {
+    if (a.done[r]) return;
     uint64_t key[kMaxBeamG];
     int32_t node[kMaxBeamG], slot[kMaxBeamG];
     int n = 0;
@@ -437,16 +458,27 @@ __global__ void select_kernel(const GArgs a, int L) {
         }
 }
 
-__global__ void output_kernel(const GArgs a, int32_t* __restrict__ path, float* __restrict__ path_score,
-                              int32_t* __restrict__ depth) {
+__global__ void select_kernel(const GArgs a, int L) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= a.nq) return;
+    select_one(a, L, r);
+}
+
+__device__ __forceinline__ void output_one(const GArgs& a, int64_t r, int32_t* path, float* path_score,
+                                           int32_t* depth) {
     const int d = a.out_depth[r];
     for (int l = 0; l < a.levels; ++l) {
         path[r * a.levels + l] = l < d ? a.paths[state_at(r, 0, l)] : -1;
         path_score[r * a.levels + l] = l < d ? a.scores[state_at(r, 0, l)] : 0.0f;
     }
     depth[r] = d;
+}
+
+__global__ void output_kernel(const GArgs a, int32_t* __restrict__ path, float* __restrict__ path_score,
+                              int32_t* __restrict__ depth) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= a.nq) return;
+    output_one(a, r, path, path_score, depth);
 }
 
 // ---------------------------------------------------------------- tensor-core scoring
@@ -513,15 +545,19 @@ __device__ __forceinline__ int32_t child_at(const GArgs& a, int32_t P, int32_t j
 }
 
 // entries (read, beam slot) per parent, then their slots in parent order
-__global__ void par_count_kernel(const GArgs a, TcItems t, int L) {
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= a.nq || a.done[r]) return;
+__device__ __forceinline__ void par_count_one(const GArgs& a, const TcItems& t, int L, int64_t r) {
+    if (a.done[r]) return;
     for (int b = 0; b < a.nbeam[r]; ++b) atomicAdd(t.par_cnt + a.paths[state_at(r, b, L - 1)], 1);
 }
 
-__global__ void par_scatter_kernel(const GArgs a, TcItems t, int L) {
+__global__ void par_count_kernel(const GArgs a, TcItems t, int L) {
     const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= a.nq || a.done[r]) return;
+    if (r >= a.nq) return;
+    par_count_one(a, t, L, r);
+}
+
+__device__ __forceinline__ void par_scatter_one(const GArgs& a, const TcItems& t, int L, int64_t r) {
+    if (a.done[r]) return;
     int32_t p = a.off[r];  // the candidates of beam slot b follow those of slots < b (expand_kernel)
     for (int b = 0; b < a.nbeam[r]; ++b) {
         const int32_t P = a.paths[state_at(r, b, L - 1)];
@@ -532,23 +568,31 @@ __global__ void par_scatter_kernel(const GArgs a, TcItems t, int L) {
     }
 }
 
+__global__ void par_scatter_kernel(const GArgs a, TcItems t, int L) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= a.nq) return;
+    par_scatter_one(a, t, L, r);
+}
+
 // A parent with at most 64 entries and 16 children shares an item with another such parent
 // (entries in rows 0-63 / 64-127, children in slots 0-15 / 16-31): the K loop of an item costs
 // the same whatever its fill, and most parents of the lower levels are that small.
 constexpr int kTcHalfE = kTcE / 2, kTcHalfC = kTcC / 2;
 
-__global__ void item_count_kernel(const GArgs a, TcItems t) {
-    const int64_t P = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (P >= a.n_nodes) return;
+__device__ __forceinline__ void item_count_one(const GArgs& a, const TcItems& t, int64_t P) {
     const int32_t m = t.par_cnt[P], nch = n_children(a, (int32_t)P);
     const bool small = m > 0 && m <= kTcHalfE && nch <= kTcHalfC;
     t.small[P] = small ? 1 : 0;
     t.item_cnt[P] = m && !small ? ((m + kTcE - 1) / kTcE) * ((nch + kTcC - 1) / kTcC) : 0;
 }
 
-__global__ void item_write_kernel(const GArgs a, TcItems t) {
+__global__ void item_count_kernel(const GArgs a, TcItems t) {
     const int64_t P = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (P >= a.n_nodes) return;
+    item_count_one(a, t, P);
+}
+
+__device__ void item_write_one(const GArgs& a, const TcItems& t, int64_t P) {
     if (t.small[P]) {
         const int32_t slot = t.small_off[P], x = t.item_off[a.n_nodes] + slot / 2;
         if (slot & 1) {
@@ -568,6 +612,12 @@ __global__ void item_write_kernel(const GArgs a, TcItems t) {
         t.item_e0[x] = (i / nj) * kTcE;
         t.item_j0[x] = (i % nj) * kTcC;
     }
+}
+
+__global__ void item_write_kernel(const GArgs a, TcItems t) {
+    const int64_t P = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (P >= a.n_nodes) return;
+    item_write_one(a, t, P);
 }
 
 // What row `row` (an entry) and child slot `js` of item `it` are.
@@ -619,18 +669,22 @@ __device__ __forceinline__ int32_t item_child(const GArgs& a, const TcItems& t, 
     return j0 + js < n_children(a, p) ? child_at(a, p, j0 + js) : -1;
 }
 
-// level 0: every read against the roots
-__global__ void items_level0_kernel(const GArgs a, TcItems t) {
+// level 0: every read against the roots; items i = first, first + stride, ...
+__device__ __forceinline__ void items_level0_range(const GArgs& a, const TcItems& t, int64_t first, int64_t stride) {
     const int32_t ne = (int32_t)((a.nq + kTcE - 1) / kTcE), nj = (a.n_roots + kTcC - 1) / kTcC;
-    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) {
+    if (first == 0) {
         t.item_off[a.n_nodes] = ne * nj;
         t.small_off[a.n_nodes] = 0;
     }
-    if (i >= ne * nj) return;
-    t.item_par[i] = -1;
-    t.item_e0[i] = (i / nj) * kTcE;
-    t.item_j0[i] = (i % nj) * kTcC;
+    for (int64_t i = first; i < (int64_t)ne * nj; i += stride) {
+        t.item_par[i] = -1;
+        t.item_e0[i] = (int32_t)(i / nj) * kTcE;
+        t.item_j0[i] = (int32_t)(i % nj) * kTcC;
+    }
+}
+
+__global__ void items_level0_kernel(const GArgs a, TcItems t) {
+    items_level0_range(a, t, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
 }
 
 // v = l0 + 2048 l1 + 2048^2 l2 with l0, l1 in [-1024, 1023] and |l2| <= 512, for every int32 v
@@ -680,37 +734,54 @@ __device__ __forceinline__ void cp_async_wait() {
 // 16-byte chunk c of row r of a 128-byte-row tile in the 128-byte swizzle layout
 __device__ __forceinline__ uint8_t* swz(uint8_t* tile, int r, int c) { return tile + r * 128 + ((c ^ (r & 7)) << 4); }
 
-__global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a, const TcItems t) {
-    extern __shared__ uint8_t smem_raw[];
-    const uint32_t raw_addr = tc::smem_u32(smem_raw);
-    uint8_t* ring = smem_raw + ((1024 - (raw_addr & 1023)) & 1023);
-    uint4* staging = reinterpret_cast<uint4*>(ring + (size_t)kTcStages * kTcStageBytes);
-    __shared__ uint64_t full_bar[kTcStages], empty_bar[kTcStages], accf_bar[2], acce_bar[2];
-    __shared__ uint32_t tmem_base_s;
-    __shared__ volatile int err_s;
-    __shared__ uint2 signs_lut[16];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (threadIdx.x < 16) signs_lut[threadIdx.x] = signs4_entry(threadIdx.x);
+// Shared-memory state of the tensor-core scoring (one CTA per SM).
+struct TcShared {
+    uint64_t full_bar[kTcStages], empty_bar[kTcStages], accf_bar[2], acce_bar[2];
+    uint64_t drain_bar;  // the MMA issuer's last commit before TMEM is freed
+    uint32_t tmem_base;
+    int err;             // code of a wait that gave up (0: none)
+    uint2 signs_lut[16];
+};
+
+// Ring positions of the roles, carried from one scoring phase to the next when one
+// launch scores several levels (each role keeps its own copy in its threads).
+struct TcRun {
+    int64_t nbase = 0;          // producers: K blocks of the items this CTA has staged
+    int stage = 0, acc = 0;     // MMA issuer: next stage and accumulator set; epilogue: next set
+    uint32_t phase = 0, acc_phase = 0;
+};
+
+// Barriers, sign table and 256 TMEM columns of the CTA (every thread calls it).
+__device__ void tc_setup(TcShared& sm) {
+    const int warp = threadIdx.x >> 5;
+    if (threadIdx.x < 16) sm.signs_lut[threadIdx.x] = signs4_entry(threadIdx.x);
     if (threadIdx.x == 0) {
-        err_s = 0;
+        sm.err = 0;
         for (int s = 0; s < kTcStages; ++s) {
-            tc::mbar_init(&full_bar[s], 4);  // one arrival per warp of the producer group
-            tc::mbar_init(&empty_bar[s], 1);
+            tc::mbar_init(&sm.full_bar[s], 4);  // one arrival per warp of the producer group
+            tc::mbar_init(&sm.empty_bar[s], 1);
         }
         for (int b = 0; b < 2; ++b) {
-            tc::mbar_init(&accf_bar[b], 1);
-            tc::mbar_init(&acce_bar[b], 4);  // one arrival per epilogue warp
+            tc::mbar_init(&sm.accf_bar[b], 1);
+            tc::mbar_init(&sm.acce_bar[b], 4);  // one arrival per epilogue warp
         }
+        tc::mbar_init(&sm.drain_bar, 1);
         tc::fence_mbar_init();
     }
     if (warp == 12) {
-        tc::tmem_alloc(&tmem_base_s, kTcTmemCols);
+        tc::tmem_alloc(&sm.tmem_base, kTcTmemCols);
         tc::tmem_relinquish();
     }
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
-    const uint32_t tmem = tmem_base_s;
+}
+
+// Scores the items of one level: warps 0-7 produce, 8-11 run the epilogue, lane 0 of warp 12
+// issues the MMAs.  Every thread of the CTA calls it; the items are blockIdx.x, + gridDim.x, ...
+__device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& run, uint8_t* ring, uint4* staging) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t tmem = sm.tmem_base;
     const int32_t n_items = t.item_off[a.n_nodes] + (t.small_off[a.n_nodes] + 1) / 2;
     const int kblocks = a.dim / 64;
 
@@ -724,7 +795,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a
         const int g = warp >> 2;
         const int tid = threadIdx.x & 127;
         const int ptid = threadIdx.x;  // 0..255: this thread's staging column
-        int64_t nbase = 0;             // K blocks of the items before this one (the ring position)
+        int64_t& nbase = run.nbase;    // K blocks of the items before this one (the ring position)
         bool ok = true;
         for (int32_t it = blockIdx.x; ok && it < n_items; it += gridDim.x, nbase += kblocks) {
             const int64_t rrow = item_row(a, t, it, tid).r;
@@ -793,7 +864,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a
                     const int64_t n = nbase + kb;
                     const int stage = (int)(n % kTcStages);
                     const uint32_t phase = (uint32_t)((n / kTcStages) & 1);
-                    const bool got = tc::mbar_wait(&empty_bar[stage], phase ^ 1, &err_s, 11);
+                    const bool got = tc::mbar_wait(&sm.empty_bar[stage], phase ^ 1, &sm.err, 11);
                     if (__any_sync(0xffffffffu, !got)) {
                         ok = false;
                         break;
@@ -804,7 +875,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a
 #pragma unroll
                         for (int c = 0; c < 8; ++c) {
                             const uint32_t byte = ((c < 4 ? w.x : w.y) >> (8 * (c & 3))) & 0xffu;
-                            const uint2 lo = signs_lut[byte & 15u], hi = signs_lut[byte >> 4];
+                            const uint2 lo = sm.signs_lut[byte & 15u], hi = sm.signs_lut[byte >> 4];
                             *reinterpret_cast<uint4*>(swz(st, tid, c)) = make_uint4(lo.x, lo.y, hi.x, hi.y);
                         }
                     }
@@ -833,7 +904,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a
                     }
                     tc::fence_proxy_async();  // the writes above are read by the tensor cores
                     __syncwarp();
-                    if (lane == 0) tc::mbar_arrive(&full_bar[stage]);
+                    if (lane == 0) tc::mbar_arrive(&sm.full_bar[stage]);
                 }
             };
             if (__any_sync(0xffffffffu, my16))
@@ -845,13 +916,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a
     } else if (warp < 12) {
         // ------------------------------------------------ epilogue
         const int quarter = warp & 3, row = quarter * 32 + lane;
-        int acc = 0;
-        uint32_t acc_phase = 0;
+        int& acc = run.acc;
+        uint32_t& acc_phase = run.acc_phase;
         for (int32_t it = blockIdx.x; it < n_items; it += gridDim.x) {
             // this row's entry and its parent's columns (the same for the warp's 32 rows: a shared
             // item's halves are 64 rows)
             const ItemRow x = item_row(a, t, it, row);
-            if (!tc::mbar_wait(&accf_bar[acc], acc_phase, &err_s, 12)) break;
+            if (!tc::mbar_wait(&sm.accf_bar[acc], acc_phase, &sm.err, 12)) break;
             tc::fence_after();
             const uint32_t d = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * kTcAccCols);
             const int64_t qn = x.r >= 0 ? a.qn[x.r] : 0;
@@ -876,7 +947,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a
             }
             tc::fence_before();
             __syncwarp();
-            if (lane == 0) tc::mbar_arrive(&acce_bar[acc]);  // the accumulators may be reused
+            if (lane == 0) tc::mbar_arrive(&sm.acce_bar[acc]);  // the accumulators may be reused
             if (++acc == 2) {
                 acc = 0;
                 acc_phase ^= 1;
@@ -887,15 +958,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a
         // the three limb tiles of B are 96 consecutive rows of shared memory and their
         // accumulators 96 consecutive columns: one N = 96 MMA covers all three
         constexpr uint32_t IDESC = tc::idesc_f16_f32(kTcE, kTcLimbs * kTcC);
-        int stage = 0, acc = 0;
-        uint32_t phase = 0, acc_phase = 0;
+        int& stage = run.stage;
+        int& acc = run.acc;
+        uint32_t& phase = run.phase;
+        uint32_t& acc_phase = run.acc_phase;
         bool ok = true;
         for (int32_t it = blockIdx.x; ok && it < n_items; it += gridDim.x) {
-            if (!tc::mbar_wait(&acce_bar[acc], acc_phase ^ 1, &err_s, 13)) break;
+            if (!tc::mbar_wait(&sm.acce_bar[acc], acc_phase ^ 1, &sm.err, 13)) break;
             tc::fence_after();
             const uint32_t d = tmem + (uint32_t)(acc * kTcAccCols);
             for (int kb = 0; kb < kblocks; ++kb) {
-                if (!tc::mbar_wait(&full_bar[stage], phase, &err_s, 14)) {
+                if (!tc::mbar_wait(&sm.full_bar[stage], phase, &sm.err, 14)) {
                     ok = false;
                     break;
                 }
@@ -906,27 +979,305 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a
 #pragma unroll
                 for (int kk = 0; kk < 4; ++kk)
                     tc::mma_f16(d, adesc + 2 * kk, bdesc + 2 * kk, IDESC, (kb | kk) != 0 ? 1u : 0u);
-                tc::mma_commit(&empty_bar[stage]);
+                tc::mma_commit(&sm.empty_bar[stage]);
                 if (++stage == kTcStages) {
                     stage = 0;
                     phase ^= 1;
                 }
             }
             if (!ok) break;
-            tc::mma_commit(&accf_bar[acc]);
+            tc::mma_commit(&sm.accf_bar[acc]);
             if (++acc == 2) {
                 acc = 0;
                 acc_phase ^= 1;
             }
         }
     }
+}
+
+// After the last scoring phase: wait (bounded) until every MMA this CTA issued has
+// completed, then free the TMEM columns and record a wait that gave up.
+__device__ void tc_teardown(TcShared& sm, int* status) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == 12 && lane == 0) {
+        tc::mma_commit(&sm.drain_bar);
+        const long long c0 = clock64();
+        while (!tc::mbar_try_wait(tc::smem_u32(&sm.drain_bar), 0) && clock64() - c0 < tc::kWaitCycles) {
+        }
+    }
     tc::fence_before();
     __syncthreads();
     if (warp == 12) {
         tc::fence_after();
-        tc::tmem_dealloc(tmem, kTcTmemCols);
+        tc::tmem_dealloc(sm.tmem_base, kTcTmemCols);
     }
-    if (threadIdx.x == 0 && err_s) atomicCAS(t.status, 0, 100 + err_s);
+    if (threadIdx.x == 0 && sm.err) atomicCAS(status, 0, 100 + sm.err);
+}
+
+__device__ __forceinline__ uint8_t* tc_ring(uint8_t* smem_raw) {
+    const uint32_t raw_addr = tc::smem_u32(smem_raw);
+    return smem_raw + ((1024 - (raw_addr & 1023)) & 1023);
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a, const TcItems t) {
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ TcShared sm;
+    uint8_t* ring = tc_ring(smem_raw);
+    uint4* staging = reinterpret_cast<uint4*>(ring + (size_t)kTcStages * kTcStageBytes);
+    tc_setup(sm);
+    TcRun run;
+    tc_phase(a, t, sm, run, ring, staging);
+    tc_teardown(sm, t.status);
+}
+
+// ---------------------------------------------------------------- the whole descent in one launch
+// descent_one_kernel runs every level of the grouped descent in one cooperative launch (one
+// CTA per SM, all resident): the phases the multi-launch form runs as separate kernels are
+// separated here by a grid-wide barrier, and each CTA owns a fixed chunk of the reads (count,
+// expand, select and output of a read run in the CTA that owns it, so those phases need no
+// barrier between them) and a fixed chunk of the nodes (the per-node scans).  The tensor-core
+// scoring keeps its TMEM columns and mbarrier ring positions from one level to the next.
+
+constexpr int kCodeGridBarrier = 20;  // status 100 + this: a grid barrier gave up
+
+struct OneArgs {
+    unsigned* bar_count;  // arrivals at the current grid barrier
+    unsigned* bar_gen;    // barriers passed
+    int* abort;           // 1 once a CTA gave up: every CTA then leaves at its next barrier
+    int32_t* blk;         // [3][gridDim.x] per-CTA partial sums of the scans
+    int32_t* maxc;        // the tree's largest child count, computed in the launch (null: not checked)
+    int32_t given;        // the caller's largest child count
+    int* status;
+    int use_tc;
+    int32_t* out_path;
+    float* out_score;
+    int32_t* out_depth;
+};
+
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_volatile(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
+
+// Grid-wide barrier of a cooperative launch (every CTA is resident).  The wait is bounded: a
+// barrier that runs out of time, or a CTA whose scoring gave up, raises o.abort, and every
+// CTA then returns false here and leaves.  Writes before the barrier are visible after it.
+__device__ bool grid_barrier(const OneArgs& o, const TcShared& sm, int* ok_s) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (sm.err) atomicExch(o.abort, 1);
+        __threadfence();
+        const unsigned g = ld_acquire_gpu(o.bar_gen);
+        if (atomicAdd(o.bar_count, 1u) == gridDim.x - 1) {
+            atomicExch(o.bar_count, 0u);
+            __threadfence();
+            st_release_gpu(o.bar_gen, g + 1);
+        } else {
+            const long long t0 = clock64();
+            while (ld_acquire_gpu(o.bar_gen) == g) {
+                if (ld_volatile(o.abort)) break;
+                if (clock64() - t0 > tc::kWaitCycles) {
+                    if (atomicExch(o.abort, 1) == 0) atomicCAS(o.status, 0, 100 + kCodeGridBarrier);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        *ok_s = ld_volatile(o.abort) == 0;
+    }
+    __syncthreads();
+    return *ok_s != 0;
+}
+
+// sum over in[lo, hi) (every thread of the CTA gets it)
+__device__ int32_t cta_sum(const int32_t* in, int64_t lo, int64_t hi, int32_t* sh) {
+    int32_t v = 0;
+    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) v += in[i];
+    int32_t total;
+    block_scan_excl(v, sh, &total);
+    return total;
+}
+
+// out[i] (and out2[i]) = base + sum(in[lo .. i)) for i in [lo, hi); returns base + sum(in[lo, hi))
+__device__ int32_t cta_scan(const int32_t* in, int32_t* out, int32_t* out2, int64_t lo, int64_t hi, int32_t base,
+                            int32_t* sh) {
+    const int64_t per = (hi - lo + blockDim.x - 1) / blockDim.x;
+    const int64_t a0 = min(hi, lo + (int64_t)threadIdx.x * per), a1 = min(hi, a0 + per);
+    int32_t v = 0;
+    for (int64_t i = a0; i < a1; ++i) v += in[i];
+    int32_t total;
+    int32_t run = base + block_scan_excl(v, sh, &total);
+    for (int64_t i = a0; i < a1; ++i) {
+        const int32_t x = in[i];
+        out[i] = run;
+        if (out2) out2[i] = run;
+        run += x;
+    }
+    return base + total;
+}
+
+// sum of the first b entries of a per-CTA array (every thread of the CTA gets it)
+__device__ int32_t cta_prefix(const int32_t* blk, int b, int32_t* sh) {
+    int32_t v = 0;
+    for (int j = threadIdx.x; j < b; j += blockDim.x) v += blk[j];
+    int32_t total;
+    block_scan_excl(v, sh, &total);
+    return total;
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs a, const TcItems t, const OneArgs o) {
+    extern __shared__ uint8_t smem_raw[];
+    __shared__ TcShared sm;
+    __shared__ int32_t sh[32];
+    __shared__ int ok_s;
+    uint8_t* ring = tc_ring(smem_raw);
+    uint4* staging = reinterpret_cast<uint4*>(ring + (size_t)kTcStages * kTcStageBytes);
+    if (o.use_tc) {
+        tc_setup(sm);
+    } else {
+        if (threadIdx.x == 0) sm.err = 0;
+        __syncthreads();
+    }
+    TcRun run;
+    const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+    // this CTA's reads [r0, r1) and nodes [n0, n1)
+    const int64_t rc = (a.nq + G - 1) / G, r0 = min(a.nq, (int64_t)b * rc), r1 = min(a.nq, r0 + rc);
+    const int64_t ncn = (a.n_nodes + G - 1) / G, n0 = min(a.n_nodes, (int64_t)b * ncn), n1 = min(a.n_nodes, n0 + ncn);
+    const bool last_reads = r0 < r1 && r1 == a.nq, last_nodes = n0 < n1 && n1 == a.n_nodes;
+    const int64_t gtid = (int64_t)b * nt + tid, gstride = (int64_t)G * nt;
+    int32_t* blk0 = o.blk;
+    int32_t* blk1 = o.blk + G;
+    int32_t* blk2 = o.blk + 2 * G;
+    const bool rows16 = a.n32 < a.n_nodes;
+
+    for (int64_t r = r0 + tid; r < r1; r += nt) {
+        a.nbeam[r] = 0;
+        a.done[r] = 0;
+        a.out_depth[r] = 0;
+    }
+    if (o.maxc) {  // the caller's largest child count is checked against the tree's
+        int32_t m = 0;
+        for (int64_t i = gtid; i < a.n_nodes; i += gstride) m = max(m, (int32_t)(a.child_ptr[i + 1] - a.child_ptr[i]));
+        for (int off = 16; off; off >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, off));
+        if ((tid & 31) == 0 && m) atomicMax(o.maxc, m);
+    }
+    bool ok = grid_barrier(o, sm, &ok_s);
+    if (ok && o.maxc && ld_volatile(o.maxc) > o.given) {
+        // too small: the pair arrays could overflow, so every read stops at depth 0
+        for (int64_t r = r0 + tid; r < r1; r += nt) a.done[r] = 1;
+        if (b == 0 && tid == 0) atomicCAS(o.status, 0, kStatusChildCount);
+    }
+    __syncthreads();
+    for (int L = 0; ok && L < a.levels; ++L) {
+        const bool tcl = o.use_tc && L < a.levels - 1;
+        // A: candidate counts of this CTA's reads and their sum; zero this level's node counters
+        for (int64_t r = r0 + tid; r < r1; r += nt) a.cnt[r] = count_one(a, L, r);
+        int32_t* node_counter = tcl ? (L > 0 ? t.par_cnt : nullptr) : a.node_cnt;
+        if (node_counter)
+            for (int64_t i = gtid; i < a.n_nodes; i += gstride) node_counter[i] = 0;
+        __syncthreads();
+        int32_t sum = cta_sum(a.cnt, r0, r1, sh);
+        if (tid == 0) blk0[b] = sum;
+        if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+        // B: pair offsets of this CTA's reads, their pairs and (tensor-core levels) the entries per parent
+        int32_t base = cta_prefix(blk0, b, sh);
+        int32_t total = cta_scan(a.cnt, a.off, nullptr, r0, r1, base, sh);
+        if (last_reads && tid == 0) a.off[a.nq] = total;
+        __syncthreads();
+        for (int64_t r = r0 + tid; r < r1; r += nt) {
+            expand_one(a, L, r, !tcl);
+            if (tcl && L > 0) par_count_one(a, t, L, r);
+        }
+        if (tcl && L == 0) items_level0_range(a, t, gtid, gstride);
+        if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+        if (tcl) {
+            if (L > 0) {
+                // C: entries per parent, summed per CTA
+                sum = cta_sum(t.par_cnt, n0, n1, sh);
+                if (tid == 0) blk0[b] = sum;
+                if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+                // D: parent offsets and cursors; items per parent and the small parents, summed per CTA
+                base = cta_prefix(blk0, b, sh);
+                total = cta_scan(t.par_cnt, t.par_off, t.par_cursor, n0, n1, base, sh);
+                if (last_nodes && tid == 0) t.par_off[a.n_nodes] = total;
+                for (int64_t P = n0 + tid; P < n1; P += nt) item_count_one(a, t, P);
+                __syncthreads();
+                sum = cta_sum(t.item_cnt, n0, n1, sh);
+                const int32_t sum2 = cta_sum(t.small, n0, n1, sh);
+                if (tid == 0) {
+                    blk1[b] = sum;
+                    blk2[b] = sum2;
+                }
+                if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+                // E: entries to their parents' slots; item and small-parent offsets
+                for (int64_t r = r0 + tid; r < r1; r += nt) par_scatter_one(a, t, L, r);
+                base = cta_prefix(blk1, b, sh);
+                total = cta_scan(t.item_cnt, t.item_off, nullptr, n0, n1, base, sh);
+                if (last_nodes && tid == 0) t.item_off[a.n_nodes] = total;
+                base = cta_prefix(blk2, b, sh);
+                total = cta_scan(t.small, t.small_off, nullptr, n0, n1, base, sh);
+                if (last_nodes && tid == 0) t.small_off[a.n_nodes] = total;
+                if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+                // F: the items
+                for (int64_t P = n0 + tid; P < n1; P += nt) item_write_one(a, t, P);
+                if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+            }
+            // G: the level's pairs scored on the tensor cores
+            tc_phase(a, t, sm, run, ring, staging);
+        } else {
+            // C: pairs per node, summed per CTA
+            sum = cta_sum(a.node_cnt, n0, n1, sh);
+            if (tid == 0) blk0[b] = sum;
+            if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+            // D: node offsets and cursors
+            base = cta_prefix(blk0, b, sh);
+            total = cta_scan(a.node_cnt, a.node_off, a.cursor, n0, n1, base, sh);
+            if (last_nodes && tid == 0) a.node_off[a.n_nodes] = total;
+            if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+            // E: the pairs in node order
+            scatter_range(a, gtid, gstride);
+            if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+            // F: the pairs scored on the CUDA cores, one warp per pair
+            if (rows16)
+                score_pairs<true>(a, gtid >> 5, gstride >> 5);
+            else
+                score_pairs<false>(a, gtid >> 5, gstride >> 5);
+        }
+        if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+        // H: the beams of this CTA's reads
+        for (int64_t r = r0 + tid; r < r1; r += nt) select_one(a, L, r);
+        __syncthreads();
+    }
+    if (ok)
+        for (int64_t r = r0 + tid; r < r1; r += nt) output_one(a, r, o.out_path, o.out_score, o.out_depth);
+    if (o.use_tc) {
+        tc_teardown(sm, o.status);
+    } else if (tid == 0 && sm.err) {
+        atomicCAS(o.status, 0, 100 + sm.err);
+    }
+}
+
+// The one-launch descent needs every CTA (one per SM) resident at once; checked once per
+// context, with the kernel's shared memory set.
+bool one_launch_fits(hdc_context* ctx) {
+    if (ctx->beam_one == 0) return false;
+    if (ctx->beam_one_fit < 0) {
+        int per_sm = 0;
+        cudaError_t e = cudaFuncSetAttribute(descent_one_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kTcSmem);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, descent_one_kernel, kTcThreads, kTcSmem);
+        int coop = 0;
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device);
+        cudaGetLastError();
+        ctx->beam_one_fit = e == cudaSuccess && per_sm >= 1 && coop ? 1 : 0;
+    }
+    return ctx->beam_one_fit == 1;
 }
 
 template <typename T>
@@ -988,6 +1339,8 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
     int32_t* d_sums = nullptr;
     int32_t* d_maxc_dev = nullptr;
     uint32_t* bits = nullptr;
+    uint32_t* one_state = nullptr;
+    int32_t* one_blk = nullptr;
     // every level but the last on the tensor cores (HDC_BEAM_GROUPED 2 or automatic)
     const bool use_tc = (ctx->beam_grouped == 2 || ctx->beam_grouped < 0) && a.dim % 64 == 0 && a.dim <= 16384;
     TcItems t{};
@@ -1015,6 +1368,8 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
         a.pair_key = carve<uint64_t>(cur, P);
         d_sums = carve<int32_t>(cur, sums);
         d_maxc_dev = carve<int32_t>(cur, 1);
+        one_state = carve<uint32_t>(cur, 4);  // barrier count, barrier generation, abort, child count
+        one_blk = carve<int32_t>(cur, 3 * (int64_t)ctx->num_sms);
         if (use_tc) {
             t.ent_read = carve<int32_t>(cur, nq * beam);
             t.ent_p0 = carve<int32_t>(cur, nq * beam);
@@ -1039,6 +1394,29 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
     a.bits = d_qbits ? d_qbits : bits;
 
     const unsigned rb = (unsigned)((nq + 255) / 256);
+    if (!d_qbits) pack_bits_kernel<<<(unsigned)((nq * a.words + 255) / 256), 256, 0, stream>>>(d_q, nq, a.dim, bits);
+    if (one_launch_fits(ctx)) {
+        // every level in one cooperative launch (descent_one_kernel)
+        OneArgs o{};
+        o.bar_count = one_state;
+        o.bar_gen = one_state + 1;
+        o.abort = reinterpret_cast<int*>(one_state + 2);
+        o.maxc = max_children > 0 ? reinterpret_cast<int32_t*>(one_state + 3) : nullptr;
+        o.given = max_children;
+        o.blk = one_blk;
+        o.status = ctx->d_status;
+        o.use_tc = use_tc ? 1 : 0;
+        o.out_path = d_path;
+        o.out_score = d_path_score;
+        o.out_depth = d_depth;
+        e = cudaMemsetAsync(one_state, 0, 4 * sizeof(uint32_t), stream);
+        void* args[] = {(void*)&a, (void*)&t, (void*)&o};
+        if (e == cudaSuccess)
+            e = cudaLaunchCooperativeKernel((const void*)descent_one_kernel, dim3((unsigned)ctx->num_sms),
+                                            dim3(kTcThreads), args, kTcSmem, stream);
+        cudaFreeAsync(ws, stream);
+        return e == cudaSuccess ? HDC_OK : cuda_fail(e, "beam: one-launch descent");
+    }
     cudaMemsetAsync(a.nbeam, 0, nq * 4, stream);
     cudaMemsetAsync(a.done, 0, nq * 4, stream);
     cudaMemsetAsync(a.out_depth, 0, nq * 4, stream);
@@ -1047,7 +1425,6 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
         max_children_kernel<<<mc_grid, 256, 0, stream>>>(d_child_ptr, n_nodes, d_maxc_dev);
         check_children_kernel<<<rb, 256, 0, stream>>>(a, d_maxc_dev, max_children, ctx->d_status);
     }
-    if (!d_qbits) pack_bits_kernel<<<(unsigned)((nq * a.words + 255) / 256), 256, 0, stream>>>(d_q, nq, a.dim, bits);
     const int work_grid = ctx->num_sms * 8;
     const unsigned nb = (unsigned)((n_nodes + 255) / 256);
     if (use_tc && (e = cudaFuncSetAttribute(descent_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -37,6 +37,9 @@ struct hdc_context {
     int tc_scatter = -1;            // tensor-core search: 1 scattered reference-tile order, 0 index order (-1: auto)
     int beam_grouped = -1;          // descent: 1 grouped by candidate node, 2 + tensor-core levels, 0 warp per read
     void* noalloc_scratch = nullptr;  // device address of hdc_search_plain_noalloc's fixed scratch (first call)
+    int beam_one = -1;                // grouped descent: 1 every level in one cooperative launch, 0 a launch
+                                      // sequence per level, -1 automatic (one launch where it fits)
+    mutable int beam_one_fit = -1;    // the one-launch descent's CTAs all fit at once (-1: not asked yet)
     long long wait_cycles = 0;        // tensor-core search: limit of its bounded waits in SM cycles (0: default)
     int test_withhold_loads = 0;      // tensor-core search: test hook, the producer issues no loads
 };

@@ -487,6 +487,7 @@ def run_descent(args, cfg):
     dim, B, L, W = cfg["dim"], args.batch, cfg["levels"], cfg["beam"]
     ctx = H.Context(dim, cfg["kmer"], cfg["read_len"], 10)
     ctx.option(H.BEAM_GROUPED, args.beam_grouped)
+    ctx.option(H.BEAM_ONE_LAUNCH, args.beam_one)
     tree, proto, pn, (b, base, counts, ptr, idx), bundle = build_prototypes(H, ctx, cfg, dev)
     d_ptr, d_idx = torch.from_numpy(ptr).to(dev), torch.from_numpy(idx).to(dev)
     roots = torch.arange(0, counts[0], dtype=torch.int32, device=dev)
@@ -598,7 +599,7 @@ def run_descent(args, cfg):
     # descent_tc_kernel.  One warp per read: one kernel.
     grouped = args.beam_grouped != 0 and dim % 1024 == 0 and dim <= 16384
     tc_levels = grouped and args.beam_grouped in (-1, 2)
-    if not grouped:
+    if not grouped or args.beam_one != 0:  # one warp per read, or every level in one cooperative launch
         per_step = 2
     elif tc_levels and L > 1:
         per_step = 1 + 3 + 6 * L + 2 + 14 * (L - 2) + 5
@@ -831,13 +832,15 @@ def descent_line(args, cfg, r, metric, workload):
                                        "(descent_tc_kernel x 5 + score_kernel; measured at 38,912 reads; "
                                        "null at other batch sizes)",
                      "peak_source": "%s HBM copy bandwidth (MEASURED_PEAKS.json)" % src,
-                     "kernel": "grouped descent (hdc_beam_search%s: per level count/expand/select; levels "
-                               "above the leaves scored by descent_tc_kernel on the tensor cores, the "
-                               "leaves by score_kernel), timed as one call; algorithmic bytes = the %.1f GB "
+                     "kernel": "grouped descent (hdc_beam_search%s, %s: per level count/expand/select; "
+                               "levels above the leaves scored on the tensor cores, the leaves on the CUDA "
+                               "cores), timed as one call; algorithmic bytes = the %.1f GB "
                                "of prototypes once + %d levels of packed reads; the tensor-core levels are "
                                "bound by their producers' conversions, the leaf level by HBM "
                                "(%d candidate rows per read)" % (
-                                   "_split" if split else "", r["proto_bytes"] / 1e9, cfg["levels"],
+                                   "_split" if split else "",
+                                   "descent_one_kernel, every level in one cooperative launch" if args.beam_one != 0
+                                   else "kernels per level", r["proto_bytes"] / 1e9, cfg["levels"],
                                    r["rows_per_read"])},
         "propagate_bundle": {"kernel": "bundle_kernel (internal prototypes = int32 sums of children)",
                              "ms": bundle_ms, "gb_per_s": bundle_bytes / (bundle_ms / 1e3) / 1e9,
@@ -930,6 +933,8 @@ def main():
     ap.add_argument("--tc-cluster", type=int, default=0, help="tensor-core search: CTAs sharing reference blocks (0: default)")
     ap.add_argument("--beam-grouped", type=int, default=-1,
                     help="descent: 1 reads grouped by candidate node, 0 one warp per read (-1: default)")
+    ap.add_argument("--beam-one", type=int, default=-1,
+                    help="descent: 1 every level in one launch, 0 kernels per level (-1: default, one launch)")
     ap.add_argument("--proto-int32", action="store_true",
                     help="descent: every prototype row int32 (default: int16 rows from the first node whose rows fit)")
     args = ap.parse_args()

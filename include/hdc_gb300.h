@@ -281,6 +281,11 @@ int hdc_search_tc_last_shape(const hdc_context* ctx, int32_t shape[5]);
                               with every level but the last scored on the tensor cores
                               (entries grouped by parent), 0 one warp per read, -1
                               automatic (2 when dim % 1024 == 0 and dim <= 16384, else 0) */
+#define HDC_BEAM_ONE_LAUNCH 11 /* grouped descent (HDC_BEAM_GROUPED 1 or 2): 1 runs every level
+                              in one cooperative launch (one CTA per SM, the phases of a level
+                              separated by bounded grid-wide barriers), 0 a sequence of kernels
+                              per level, -1 automatic (one launch where all its CTAs fit);
+                              results are identical */
 #define HDC_WAIT_LIMIT 9   /* tensor-core search: its bounded device-side waits give up after
                               value x 1,000 SM cycles, 1 .. 4,000,000 (0: the default,
                               4,000,000, about 2 s at 2 GHz); a wait that gives up makes the

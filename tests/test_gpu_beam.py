@@ -39,11 +39,11 @@ def _first_int16_node(proto):
 
 # grouped: 1 reads grouped by candidate node, 2 the same with the levels above the last on
 # the tensor cores, 0 one warp per read (identical results)
-@pytest.mark.parametrize("grouped", [0, 1, 2])
+@pytest.mark.parametrize("grouped,one", [(0, 0), (1, 0), (1, 1), (2, 0), (2, 1)])
 @pytest.mark.parametrize("dim,kmer,n_leaves,beam,threshold,childless", [
     (1024, 10, 200, 5, 0.0, False), (2048, 12, 300, 3, 0.0, False), (1024, 8, 150, 5, 0.6, False),
     (2048, 10, 300, 5, -2.0, True), (1024, 10, 200, 8, float("-inf"), True)])
-def test_beam_descent_matches_oracle(hdc, orc, cuda, dim, kmer, n_leaves, beam, threshold, childless, grouped):
+def test_beam_descent_matches_oracle(hdc, orc, cuda, dim, kmer, n_leaves, beam, threshold, childless, grouped, one):
     import torch
     H = hdc
     b = 1
@@ -54,6 +54,7 @@ def test_beam_descent_matches_oracle(hdc, orc, cuda, dim, kmer, n_leaves, beam, 
                           mixed_frac=0.2, mixed_rate=0.06)
     ctx = H.Context(dim, kmer, 250, 10)
     ctx.option(H.BEAM_GROUPED, grouped)
+    ctx.option(H.BEAM_ONE_LAUNCH, one)  # grouped: every level in one launch, or kernels per level
     base, counts, ptr, idx = _tree_csr(n_leaves, b)
     n_nodes = int(base[-1])
     proto = torch.zeros((n_nodes, dim), dtype=torch.int32, device=cuda)
@@ -370,4 +371,72 @@ def test_beam_split_bit_reads_equal_int8_reads(hdc, cuda):
             for x, y in zip(want, got):
                 assert torch.equal(x, y), (grouped, threshold)
     torch.cuda.synchronize()
+    assert ctx.status() == 0
+
+
+def test_beam_one_launch_equals_level_kernels(hdc, cuda):
+    """The one-launch descent (descent_one_kernel: every level in one cooperative
+    launch) against the same grouped descent run as kernels per level, on a
+    20,000-leaf tree with 3,000 reads: identical paths, scores and depths for
+    int32 rows and for split int16 rows with sign-bit reads, both grouped forms,
+    thresholds 0 and -inf, 6 and 3 levels, a caller-given child count (equal,
+    over, and under the tree's: every read stops at depth 0, status 200), and a
+    tree with childless internal nodes."""
+    import torch
+    H = hdc
+    dim, n_leaves, nq = 2048, 20000, 3000
+    b, base, counts, ptr, idx = H.synth_tree_csr(n_leaves)
+    tree = H.synth_tree(23, n_leaves)
+    reads = H.synth_reads(24, tree, nq, 250, subst=0.01, sigma=0.5, min_read=100, max_read=800,
+                          mixed_frac=0.2, mixed_rate=0.06)
+    ctx = H.Context(dim, 12, 250, 10)
+    proto = torch.zeros((int(base[-1]), dim), dtype=torch.int32, device=cuda)
+    ctx.encode_segments(torch.from_numpy(tree.buf).to(cuda), torch.from_numpy(tree.off).to(cuda),
+                        torch.from_numpy(tree.len).to(cuda), proto[int(base[5]):], H.OUT_I32, tree.max_len())
+    d_idx = torch.from_numpy(idx).to(cuda)
+    for r in range(4, -1, -1):
+        lo, hi = int(base[r]), int(base[r + 1])
+        ctx.bundle(proto, torch.from_numpy(ptr[lo:hi + 1].copy()).to(cuda), d_idx, out=proto[lo:hi])
+    rb, ro, rl = (torch.from_numpy(x).to(cuda) for x in (reads.buf, reads.off, reads.len))
+    q8 = torch.empty((nq, dim), dtype=torch.int8, device=cuda)
+    qbits = torch.empty((nq, dim // 32), dtype=torch.int32, device=cuda)
+    ctx.encode_segments(rb, ro, rl, q8, H.OUT_BIPOLAR_I8, reads.max_len())
+    ctx.encode_segments(rb, ro, rl, qbits, H.OUT_SIGN_BITS, reads.max_len())
+    qn, pn = ctx.norms(q8), ctx.norms(proto)
+    roots = torch.arange(0, counts[0], dtype=torch.int32, device=cuda)
+    d_ptr = torch.from_numpy(ptr).to(cuda)
+    n_wide = int(base[5])
+    p32, p16 = proto[:n_wide].contiguous(), proto[n_wide:].to(torch.int16)
+    maxc = int(np.diff(ptr).max())
+    cptr, cidx = _drop_children(ptr, idx, list(range(int(base[2]), int(base[3]), 5)) + [int(base[1])])
+    c_ptr, c_idx = torch.from_numpy(cptr).to(cuda), torch.from_numpy(cidx).to(cuda)
+
+    def runs():
+        out = []
+        for grouped in (1, 2):
+            ctx.option(H.BEAM_GROUPED, grouped)
+            for levels, threshold in ((6, 0.0), (6, float("-inf")), (3, 0.0)):
+                out.append(ctx.beam_search(q8, qn, proto, pn, d_ptr, d_idx, roots, levels, 5, threshold))
+                out.append(ctx.beam_search_split(qbits, qn, p32, p16, pn, d_ptr, d_idx, roots, levels, 5, threshold,
+                                                 max_children=maxc))
+            out.append(ctx.beam_search_split(qbits, qn, p32, p16, pn, d_ptr, d_idx, roots, 6, 5, 0.0,
+                                             max_children=maxc + 2))
+            out.append(ctx.beam_search(q8, qn, proto, pn, c_ptr, c_idx, roots, 6, 4, -2.0))
+        torch.cuda.synchronize()
+        assert ctx.status() == 0
+        return [[x.cpu().numpy() for x in res] for res in out]
+
+    ctx.option(H.BEAM_ONE_LAUNCH, 0)
+    want = runs()
+    ctx.option(H.BEAM_ONE_LAUNCH, 1)
+    got = runs()
+    for w, g in zip(want, got):
+        for x, y in zip(w, g):
+            assert np.array_equal(x, y)
+    # a child count below the tree's: every read stops at depth 0 and the status reports it
+    _, _, depth = ctx.beam_search_split(qbits, qn, p32, p16, pn, d_ptr, d_idx, roots, 6, 5, 0.0,
+                                        max_children=maxc - 1)
+    torch.cuda.synchronize()
+    assert (depth == 0).all()
+    assert ctx.status() == 200
     assert ctx.status() == 0
