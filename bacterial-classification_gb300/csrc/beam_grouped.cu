@@ -1039,6 +1039,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a
 // scoring keeps its TMEM columns and mbarrier ring positions from one level to the next.
 
 constexpr int kCodeGridBarrier = 20;  // status 100 + this: a grid barrier gave up
+constexpr int kMaxPhaseTs = 64;       // phase timestamps kept of a launch (hdc_beam_phase_times)
 
 struct OneArgs {
     unsigned* bar_count;  // arrivals at the current grid barrier
@@ -1052,7 +1053,14 @@ struct OneArgs {
     int32_t* out_path;
     float* out_score;
     int32_t* out_depth;
+    unsigned long long* phase_ts;  // [kMaxPhaseTs] CTA 0's clock at the start and after every barrier
 };
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
 
 __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
     unsigned v;
@@ -1067,7 +1075,7 @@ __device__ __forceinline__ int ld_volatile(const int* p) { return *reinterpret_c
 // Grid-wide barrier of a cooperative launch (every CTA is resident).  The wait is bounded: a
 // barrier that runs out of time, or a CTA whose scoring gave up, raises o.abort, and every
 // CTA then returns false here and leaves.  Writes before the barrier are visible after it.
-__device__ bool grid_barrier(const OneArgs& o, const TcShared& sm, int* ok_s) {
+__device__ bool grid_barrier(const OneArgs& o, const TcShared& sm, int* ok_s, int* n_ts) {
     __syncthreads();
     if (threadIdx.x == 0) {
         if (sm.err) atomicExch(o.abort, 1);
@@ -1089,6 +1097,7 @@ __device__ bool grid_barrier(const OneArgs& o, const TcShared& sm, int* ok_s) {
             }
         }
         *ok_s = ld_volatile(o.abort) == 0;
+        if (blockIdx.x == 0 && *n_ts < kMaxPhaseTs) o.phase_ts[(*n_ts)++] = global_ns();
     }
     __syncthreads();
     return *ok_s != 0;
@@ -1135,7 +1144,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs 
     __shared__ TcShared sm;
     __shared__ int32_t sh[32];
     __shared__ int ok_s;
+    __shared__ int n_ts;
     uint8_t* ring = tc_ring(smem_raw);
+    if (threadIdx.x == 0) {
+        n_ts = 0;
+        if (blockIdx.x == 0) o.phase_ts[n_ts++] = global_ns();
+    }
     uint4* staging = reinterpret_cast<uint4*>(ring + (size_t)kTcStages * kTcStageBytes);
     if (o.use_tc) {
         tc_setup(sm);
@@ -1166,7 +1180,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs 
         for (int off = 16; off; off >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, off));
         if ((tid & 31) == 0 && m) atomicMax(o.maxc, m);
     }
-    bool ok = grid_barrier(o, sm, &ok_s);
+    bool ok = grid_barrier(o, sm, &ok_s, &n_ts);
     if (ok && o.maxc && ld_volatile(o.maxc) > o.given) {
         // too small: the pair arrays could overflow, so every read stops at depth 0
         for (int64_t r = r0 + tid; r < r1; r += nt) a.done[r] = 1;
@@ -1183,7 +1197,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs 
         __syncthreads();
         int32_t sum = cta_sum(a.cnt, r0, r1, sh);
         if (tid == 0) blk0[b] = sum;
-        if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+        if (!(ok = grid_barrier(o, sm, &ok_s, &n_ts))) break;
         // B: pair offsets of this CTA's reads, their pairs and (tensor-core levels) the entries per parent
         int32_t base = cta_prefix(blk0, b, sh);
         int32_t total = cta_scan(a.cnt, a.off, nullptr, r0, r1, base, sh);
@@ -1194,13 +1208,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs 
             if (tcl && L > 0) par_count_one(a, t, L, r);
         }
         if (tcl && L == 0) items_level0_range(a, t, gtid, gstride);
-        if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+        if (!(ok = grid_barrier(o, sm, &ok_s, &n_ts))) break;
         if (tcl) {
             if (L > 0) {
                 // C: entries per parent, summed per CTA
                 sum = cta_sum(t.par_cnt, n0, n1, sh);
                 if (tid == 0) blk0[b] = sum;
-                if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+                if (!(ok = grid_barrier(o, sm, &ok_s, &n_ts))) break;
                 // D: parent offsets and cursors; items per parent and the small parents, summed per CTA
                 base = cta_prefix(blk0, b, sh);
                 total = cta_scan(t.par_cnt, t.par_off, t.par_cursor, n0, n1, base, sh);
@@ -1213,7 +1227,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs 
                     blk1[b] = sum;
                     blk2[b] = sum2;
                 }
-                if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+                if (!(ok = grid_barrier(o, sm, &ok_s, &n_ts))) break;
                 // E: entries to their parents' slots; item and small-parent offsets
                 for (int64_t r = r0 + tid; r < r1; r += nt) par_scatter_one(a, t, L, r);
                 base = cta_prefix(blk1, b, sh);
@@ -1222,10 +1236,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs 
                 base = cta_prefix(blk2, b, sh);
                 total = cta_scan(t.small, t.small_off, nullptr, n0, n1, base, sh);
                 if (last_nodes && tid == 0) t.small_off[a.n_nodes] = total;
-                if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+                if (!(ok = grid_barrier(o, sm, &ok_s, &n_ts))) break;
                 // F: the items
                 for (int64_t P = n0 + tid; P < n1; P += nt) item_write_one(a, t, P);
-                if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+                if (!(ok = grid_barrier(o, sm, &ok_s, &n_ts))) break;
             }
             // G: the level's pairs scored on the tensor cores
             tc_phase(a, t, sm, run, ring, staging);
@@ -1233,28 +1247,32 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs 
             // C: pairs per node, summed per CTA
             sum = cta_sum(a.node_cnt, n0, n1, sh);
             if (tid == 0) blk0[b] = sum;
-            if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+            if (!(ok = grid_barrier(o, sm, &ok_s, &n_ts))) break;
             // D: node offsets and cursors
             base = cta_prefix(blk0, b, sh);
             total = cta_scan(a.node_cnt, a.node_off, a.cursor, n0, n1, base, sh);
             if (last_nodes && tid == 0) a.node_off[a.n_nodes] = total;
-            if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+            if (!(ok = grid_barrier(o, sm, &ok_s, &n_ts))) break;
             // E: the pairs in node order
             scatter_range(a, gtid, gstride);
-            if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+            if (!(ok = grid_barrier(o, sm, &ok_s, &n_ts))) break;
             // F: the pairs scored on the CUDA cores, one warp per pair
             if (rows16)
                 score_pairs<true>(a, gtid >> 5, gstride >> 5);
             else
                 score_pairs<false>(a, gtid >> 5, gstride >> 5);
         }
-        if (!(ok = grid_barrier(o, sm, &ok_s))) break;
+        if (!(ok = grid_barrier(o, sm, &ok_s, &n_ts))) break;
         // H: the beams of this CTA's reads
         for (int64_t r = r0 + tid; r < r1; r += nt) select_one(a, L, r);
         __syncthreads();
     }
     if (ok)
         for (int64_t r = r0 + tid; r < r1; r += nt) output_one(a, r, o.out_path, o.out_score, o.out_depth);
+    if (b == 0 && tid == 0) {
+        if (n_ts < kMaxPhaseTs) o.phase_ts[n_ts++] = global_ns();
+        for (int i = n_ts; i < kMaxPhaseTs; ++i) o.phase_ts[i] = 0;
+    }
     if (o.use_tc) {
         tc_teardown(sm, o.status);
     } else if (tid == 0 && sm.err) {
@@ -1409,6 +1427,15 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
         o.out_path = d_path;
         o.out_score = d_path_score;
         o.out_depth = d_depth;
+        if (!ctx->d_phase_ts) {
+            e = cudaMalloc(&ctx->d_phase_ts, kMaxPhaseTs * sizeof(unsigned long long));
+            if (e == cudaSuccess) e = cudaMemset(ctx->d_phase_ts, 0, kMaxPhaseTs * sizeof(unsigned long long));
+            if (e != cudaSuccess) {
+                cudaFreeAsync(ws, stream);
+                return cuda_fail(e, "beam: phase clock buffer");
+            }
+        }
+        o.phase_ts = ctx->d_phase_ts;
         e = cudaMemsetAsync(one_state, 0, 4 * sizeof(uint32_t), stream);
         void* args[] = {(void*)&a, (void*)&t, (void*)&o};
         if (e == cudaSuccess)
@@ -1470,6 +1497,18 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
     e = cudaGetLastError();
     cudaFreeAsync(ws, stream);
     return e == cudaSuccess ? HDC_OK : cuda_fail(e, "beam: grouped launch");
+}
+
+int beam_phase_times(const hdc_context* ctx, int64_t* out_ns, int max_n) {
+    std::fill(out_ns, out_ns + max_n, 0);
+    if (!ctx->d_phase_ts) return 0;
+    unsigned long long ts[kMaxPhaseTs];
+    cudaError_t e = cudaMemcpy(ts, ctx->d_phase_ts, sizeof ts, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return -1;
+    int n = 0;
+    while (n < kMaxPhaseTs && ts[n]) ++n;
+    for (int i = 1; i < n && i - 1 < max_n; ++i) out_ns[i - 1] = (int64_t)(ts[i] - ts[i - 1]);
+    return n > 0 ? n - 1 : 0;
 }
 
 }  // namespace hdc

@@ -101,6 +101,7 @@ int hdc_context_create(int dim, int kmer, int window, int step, hdc_context** ou
 
 void hdc_context_destroy(hdc_context* ctx) {
     if (!ctx) return;
+    cudaFree(ctx->d_phase_ts);
     cudaFree(ctx->d_base32);
     cudaFree(ctx->d_status);
     delete[] ctx->host_base;
@@ -126,6 +127,39 @@ int hdc_encode_segments(hdc_context* ctx, const char* d_bytes, const int64_t* d_
     if (max_len < 0) return fail(HDC_ERR_INVALID, "encode: negative max_len");
     return hdc::launch_encode(ctx, d_bytes, d_seg_off, d_seg_len, nullptr, nullptr, 0, n_segs, out_kind, d_out,
                               out_stride, d_nkmers, max_len, static_cast<cudaStream_t>(stream));
+}
+
+int hdc_beam_phase_times(const hdc_context* ctx, int64_t* out_ns, int max_n, int* n_out) {
+    if (!ctx || !out_ns || !n_out || max_n < 0) return fail(HDC_ERR_INVALID, "beam_phase_times: null argument");
+    const int n = hdc::beam_phase_times(ctx, out_ns, max_n);
+    if (n < 0) return fail(HDC_ERR_CUDA, "beam_phase_times: read back");
+    *n_out = n;
+    return HDC_OK;
+}
+
+int hdc_pack_2bit(hdc_context* ctx, const char* d_bytes, int64_t n_bytes, uint32_t* d_words, void* stream) {
+    if (!ctx) return fail(HDC_ERR_INVALID, "pack_2bit: null context");
+    if (n_bytes < 0) return fail(HDC_ERR_INVALID, "pack_2bit: negative length");
+    if (n_bytes == 0) return HDC_OK;
+    if (!d_bytes || !d_words) return fail(HDC_ERR_INVALID, "pack_2bit: null pointer");
+    return hdc::launch_pack_2bit(ctx, d_bytes, n_bytes, d_words, static_cast<cudaStream_t>(stream));
+}
+
+int hdc_encode_packed(hdc_context* ctx, const uint32_t* d_words, const int64_t* d_base_off, const int32_t* d_len,
+                      int64_t n_segs, int32_t max_len, int out_kind, void* d_out, int64_t out_stride,
+                      int32_t* d_nkmers, void* stream) {
+    if (!ctx) return fail(HDC_ERR_INVALID, "encode_packed: null context");
+    if (n_segs < 0) return fail(HDC_ERR_INVALID, "encode_packed: negative segment count");
+    if (n_segs == 0) return HDC_OK;
+    if (!d_words || !d_base_off || !d_len || !d_out) return fail(HDC_ERR_INVALID, "encode_packed: null pointer");
+    if (out_kind < HDC_OUT_I16 || out_kind > HDC_OUT_SIGN_BITS)
+        return fail(HDC_ERR_INVALID, "encode_packed: bad out_kind");
+    if (out_stride < (out_kind == HDC_OUT_SIGN_BITS ? (ctx->dim + 31) / 32 : ctx->dim))
+        return fail(HDC_ERR_INVALID, "encode_packed: out_stride below the row length");
+    if (max_len < 0) return fail(HDC_ERR_INVALID, "encode_packed: negative max_len");
+    return hdc::launch_encode(ctx, nullptr, d_base_off, d_len, nullptr, nullptr, 0, n_segs, out_kind, d_out,
+                              out_stride, d_nkmers, max_len, static_cast<cudaStream_t>(stream), nullptr, nullptr,
+                              d_words);
 }
 
 int64_t hdc_num_windows(const hdc_context* ctx, int64_t len) {

@@ -51,6 +51,9 @@ struct EncodeArgs {
     int zero_row;
     int table_rows;
     const unsigned char* bytes;
+    // 2-bit packed input (when set, instead of bytes): base i of the stream at bits 2 (i % 16)
+    // of words[i / 16], A=0 C=1 G=2 T=3; segment offsets count bases
+    const uint32_t* words;
     const int64_t* seg_off;  // explicit segments
     const int32_t* seg_len;
     const int64_t* seq_off;  // window segments: [n_seqs+1]
@@ -165,7 +168,7 @@ __global__ void __launch_bounds__(kThreads) encode_kernel(const EncodeArgs a) {
         int64_t start;
         int len;
         get_segment(a, seg, start, len);
-        const unsigned char* s = a.bytes + start;
+        const unsigned char* s = a.words ? nullptr : a.bytes + start;
         const int npos = len >= k ? len - k + 1 : 0;
         uint32_t ones = 0, twos = 0, fours = 0, eights = 0;
         uint32_t hi[NH];
@@ -178,9 +181,17 @@ __global__ void __launch_bounds__(kThreads) encode_kernel(const EncodeArgs a) {
             const int p0 = c0 + lane * 8;
             uint32_t x = 0, m = 0;
             auto push = [&](int pos) {
-                uint32_t c = pos < len ? (uint32_t)__ldg(s + pos) : 0u;
-                uint32_t inv = pos < len ? (is_base(c) ^ 1u) : 1u;
-                x = (x >> 2) | (base_code(c) << (2 * (k - 1)));
+                uint32_t code, inv;
+                if (a.words) {  // packed: every position of the segment is a base
+                    const int64_t i = start + pos;
+                    code = pos < len ? (__ldg(a.words + (i >> 4)) >> (2 * (int)(i & 15))) & 3u : 0u;
+                    inv = pos < len ? 0u : 1u;
+                } else {
+                    const uint32_t c = pos < len ? (uint32_t)__ldg(s + pos) : 0u;
+                    code = base_code(c);
+                    inv = pos < len ? (is_base(c) ^ 1u) : 1u;
+                }
+                x = (x >> 2) | (code << (2 * (k - 1)));
                 m = (m >> 1) | (inv << (k - 1));
             };
             for (int j = 0; j < k - 1; ++j) push(p0 + j);
@@ -383,10 +394,52 @@ int launch_np(const EncodeArgs& a, int nh, int grid_x, int n_slabs, size_t smem,
 
 int encode_slabs(const hdc_context* ctx) { return (ctx->words32 + 31) / 32; }
 
+namespace {
+// 2-bit code of a byte as the reference packs it (src/encode.cu:169-185): A/a=0, C/c=1,
+// G/g=2, T/t=3, anything else 0
+__device__ __forceinline__ uint32_t pack_code(uint32_t c) {
+    c &= 0xdfu;  // upper case
+    return c == 'C' ? 1u : c == 'G' ? 2u : c == 'T' ? 3u : 0u;
+}
+
+// words[j] = the codes of bytes 16 j .. 16 j + 15 (a 128-bit load per word; bytes past n count 0)
+__global__ void pack_2bit_kernel(const unsigned char* __restrict__ bytes, int64_t n, uint32_t* __restrict__ words,
+                                 int64_t n_words) {
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n_words; j += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t b[16];
+        const int64_t o = j * 16;
+        if (o + 16 <= n && (reinterpret_cast<uintptr_t>(bytes) & 15) == 0) {
+            const uint4 v = __ldg(reinterpret_cast<const uint4*>(bytes + o));
+            const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int i = 0; i < 16; ++i) b[i] = (w4[i >> 2] >> (8 * (i & 3))) & 0xffu;
+        } else {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) b[i] = o + i < n ? bytes[o + i] : 0u;
+        }
+        uint32_t w = 0;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) w |= pack_code(b[i]) << (2 * i);
+        words[j] = w;
+    }
+}
+}  // namespace
+
+int launch_pack_2bit(hdc_context* ctx, const char* d_bytes, int64_t n_bytes, uint32_t* d_words, cudaStream_t stream) {
+    const int64_t n_words = (n_bytes + 15) / 16;
+    if (n_words == 0) return HDC_OK;
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->num_sms * 16,
+                                                                          (n_words + 255) / 256));
+    pack_2bit_kernel<<<grid, 256, 0, stream>>>(reinterpret_cast<const unsigned char*>(d_bytes), n_bytes, d_words,
+                                               n_words);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? HDC_OK : cuda_fail(e, "pack_2bit: launch");
+}
+
 int launch_encode(hdc_context* ctx, const char* d_bytes, const int64_t* d_seg_off, const int32_t* d_seg_len,
                   const int64_t* d_seq_off, const int64_t* d_win_off, int64_t n_seqs, int64_t n_segs, int out_kind,
                   void* d_out, int64_t out_stride, int32_t* d_nkmers, int max_seg_len, cudaStream_t stream,
-                  const int32_t* d_order, int* d_queue) {
+                  const int32_t* d_order, int* d_queue, const uint32_t* d_words) {
     if (n_segs == 0) return HDC_OK;
     EncodeArgs a{};
     a.base32 = ctx->d_base32;
@@ -408,6 +461,7 @@ int launch_encode(hdc_context* ctx, const char* d_bytes, const int64_t* d_seg_of
     a.zero_row = row0;
     a.table_rows = row0 + 1;
     a.bytes = reinterpret_cast<const unsigned char*>(d_bytes);
+    a.words = d_words;
     a.seg_off = d_seg_off;
     a.seg_len = d_seg_len;
     a.seq_off = d_seq_off;

@@ -40,6 +40,7 @@ struct hdc_context {
     int beam_one = -1;                // grouped descent: 1 every level in one cooperative launch, 0 a launch
                                       // sequence per level, -1 automatic (one launch where it fits)
     mutable int beam_one_fit = -1;    // the one-launch descent's CTAs all fit at once (-1: not asked yet)
+    unsigned long long* d_phase_ts = nullptr;  // phase clock of the last one-launch descent (diagnostic)
     long long wait_cycles = 0;        // tensor-core search: limit of its bounded waits in SM cycles (0: default)
     int test_withhold_loads = 0;      // tensor-core search: test hook, the producer issues no loads
 };
@@ -69,8 +70,11 @@ inline bool valid_score_mode(int m) { return m == HDC_SCORE_NORM || m == HDC_SCO
 int launch_encode(hdc_context* ctx, const char* d_bytes, const int64_t* d_seg_off, const int32_t* d_seg_len,
                   const int64_t* d_seq_off, const int64_t* d_win_off, int64_t n_seqs, int64_t n_segs,
                   int out_kind, void* d_out, int64_t out_stride, int32_t* d_nkmers, int max_seg_len,
-                  cudaStream_t stream, const int32_t* d_order = nullptr, int* d_queue = nullptr);
+                  cudaStream_t stream, const int32_t* d_order = nullptr, int* d_queue = nullptr,
+                  const uint32_t* d_words = nullptr);
 int encode_slabs(const hdc_context* ctx);
+// ASCII bytes -> 2-bit words (16 bases per word, the reference's packing)
+int launch_pack_2bit(hdc_context* ctx, const char* d_bytes, int64_t n_bytes, uint32_t* d_words, cudaStream_t stream);
 
 int launch_norms(hdc_context* ctx, const void* d_hv, int elem_bytes, int64_t n, int64_t* d_norm2,
                  int32_t* d_maxabs, cudaStream_t stream);
@@ -137,6 +141,8 @@ int launch_similarity(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qn,
 // the descent with reads grouped by candidate node (beam_grouped.cu); dim % 1024 == 0, dim <= 16384;
 // nodes < n32 have int32 rows in d_proto, the others int16 rows in d_proto16 (row node - n32);
 // reads as int8 +1/-1 rows d_q, or as sign bits d_qbits [nq][dim / 32] (then d_q is unused)
+// durations of the phases of the last one-launch descent (ns), returns how many
+int beam_phase_times(const hdc_context* ctx, int64_t* out_ns, int max_n);
 int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_qbits, const int64_t* d_qn, int64_t nq, const int32_t* d_proto,
                         int64_t n32, const int16_t* d_proto16, const int64_t* d_pn, int64_t n_nodes, const int64_t* d_child_ptr, const int32_t* d_child_idx,
                         const int32_t* d_roots, int n_roots, int max_children, int levels, int beam, double threshold, int mode,

@@ -34,6 +34,9 @@ SIGNATURES = [
     ("hdc_stream_sync", I32, [P]),
     ("hdc_encode_segments", I32, [P, P, P, P, I64, ctypes.c_int32, I32, P, I64, P, P]),
     ("hdc_num_windows", I64, [P, I64]),
+    ("hdc_pack_2bit", I32, [P, P, I64, P, P]),
+    ("hdc_beam_phase_times", I32, [P, P, I32, ctypes.POINTER(I32)]),
+    ("hdc_encode_packed", I32, [P, P, P, P, I64, ctypes.c_int32, I32, P, I64, P, P]),
     ("hdc_encode_windows", I32, [P, P, P, P, I64, I64, P, P]),
     ("hdc_norms", I32, [P, P, I32, I64, P, P, P]),
     ("hdc_search_workspace_bytes", SZ, [P, I64, I64, I32]),
@@ -145,6 +148,20 @@ class Context:
         n = d_off.numel()
         check(lib().hdc_encode_segments(self.h, ptr(d_bytes), ptr(d_off), ptr(d_len), n, int(max_len), out_kind,
                                         ptr(out), out.stride(0), ptr(nkmers), stream_ptr(stream)))
+        return out
+
+    def pack_2bit(self, d_bytes, n_bytes=None, stream=None):
+        """2-bit words (int32 tensor, ceil(n / 16)) of the first n bytes of a uint8 tensor."""
+        import torch
+        n = d_bytes.numel() if n_bytes is None else n_bytes
+        words = torch.empty(max(1, (n + 15) // 16), dtype=torch.int32, device=d_bytes.device)
+        check(lib().hdc_pack_2bit(self.h, ptr(d_bytes), n, ptr(words), stream_ptr(stream)))
+        return words
+
+    def encode_packed(self, d_words, d_base_off, d_len, out, out_kind=OUT_I16, max_len=0, nkmers=None, stream=None):
+        n = d_base_off.numel()
+        check(lib().hdc_encode_packed(self.h, ptr(d_words), ptr(d_base_off), ptr(d_len), n, int(max_len), out_kind,
+                                      ptr(out), out.stride(0), ptr(nkmers), stream_ptr(stream)))
         return out
 
     def num_windows(self, length):
@@ -273,6 +290,14 @@ class Context:
                  ptr(child_idx), ptr(roots), roots.numel(), max_children, levels, beam, threshold, mode, ptr(path),
                  ptr(score), ptr(depth), stream_ptr(stream)))
         return path, score, depth
+
+    def beam_phase_times(self):
+        """Durations (ms) of the phases of the last one-launch descent, as its first CTA saw them."""
+        import numpy as np
+        out = np.zeros(64, np.int64)
+        n = I32()
+        check(lib().hdc_beam_phase_times(self.h, out.ctypes.data_as(ctypes.c_void_p), 64, ctypes.byref(n)))
+        return [float(x) / 1e6 for x in out[:n.value]]
 
     def similarity(self, q, qn, rows, rn, ref_rows, ref_whole, pair_q, pair_ref, mode=SCORE_NORM, stream=None):
         """HVCache::similarity for (query, reference) pairs; returns (scores,

@@ -552,6 +552,8 @@ def run_descent(args, cfg):
         torch.cuda.synchronize()
         beam_ms.append(ev[0].elapsed_time(ev[1]))
     path, score, depth = out["r"]
+    phases = descent_phases(ctx.beam_phase_times(), L, grouped_tc=args.beam_grouped in (-1, 2)) \
+        if split and args.beam_one != 0 else None
     depth_mean = float(depth.float().mean())
     last = 2 % n_pool  # out["r"] is from the last event-timed call, on dev_pool[2 % n_pool]
     leaf_acc = float((path[:, L - 1].cpu().numpy() == int(base[5]) + pool[last].label[:B]).mean())
@@ -608,7 +610,7 @@ def run_descent(args, cfg):
     res = dict(ms=ms, e2e_ms=e2e_ms, search_ms=float(np.median(beam_ms)), clocks=clk.summary(),
                launches=per_step * args.steps, refs=int(base[-1]), h2d=io["h2d"], d2h=io["d2h"], tree=tree,
                bundle=bundle, depth_mean=depth_mean, rows_per_read=int(sum(cand)), leaf_accuracy=leaf_acc,
-               mean_len=float(np.mean(pool[0].len)), n_wide=n_wide,
+               mean_len=float(np.mean(pool[0].len)), n_wide=n_wide, phases=phases,
                proto_bytes=n_wide * dim * 4 + (n_nodes - n_wide) * dim * 2)
     if not args.no_cpu_baseline:
         # q8 and out["r"] hold the last step's batch and result
@@ -620,6 +622,36 @@ def run_descent(args, cfg):
                                                                                 np.array(ws, np.float32))
             for i, (wp, ws) in enumerate(res["cpu"].pop("paths")))
     return res
+
+
+def descent_phases(ms, levels, grouped_tc=True):
+    """Per-level times (ms) of a one-launch descent from its phase clock: a level's
+    phases end at its scoring; the select of a level is counted with the next."""
+    names = ["setup"]
+    for L in range(levels):
+        tcl = grouped_tc and L < levels - 1
+        if tcl and L == 0:
+            names += ["count", "expand", "score_tc"]
+        elif tcl:
+            names += ["count", "expand", "parent_sums", "parent_scan", "scatter", "items", "score_tc"]
+        else:
+            names += ["count", "expand", "node_sums", "node_scan", "scatter", "score_cuda"]
+    names += ["select_output"]
+    if len(ms) != len(names):
+        return {"raw_ms": ms}
+    out = {"setup": ms[0]}
+    per_level = [dict() for _ in range(levels)]
+    i = 1
+    for L in range(levels):
+        tcl = grouped_tc and L < levels - 1
+        n = 3 if (tcl and L == 0) else 7 if tcl else 6
+        for nm in names[i:i + n]:
+            per_level[L][nm] = per_level[L].get(nm, 0.0) + ms[i]
+            i += 1
+    out["levels"] = [{k: round(v, 4) for k, v in d.items()} for d in per_level]
+    out["select_output"] = ms[-1]
+    out["total"] = sum(ms)
+    return out
 
 
 def first_int16_row(proto, chunk=8192):
@@ -848,6 +880,8 @@ def descent_line(args, cfg, r, metric, workload):
                              "per_rank": r["bundle"]},
         "clocks": r["clocks"], "gpu_launches": r["launches"],
     }
+    if r.get("phases"):
+        line["descent_phases_ms"] = r["phases"]
     if "sample_identical" in r:
         line["paths_identical_to_oracle"] = {"reads": r["cpu"]["done"], "identical": r["sample_identical"]}
     if "cpu" in r:

@@ -87,6 +87,28 @@ int hdc_stream_sync(void* stream);
 
 /* ---------------------------------------------------------------- (a) encode */
 
+/* 2-bit packing of reads on the device, the format of the reference's
+ * pack_sequence (src/encode.cu:169-185): base i of the byte stream d_bytes
+ * [n_bytes] goes to bits 2 (i % 16) of d_words[i / 16] (ceil(n_bytes / 16)
+ * words), A/a = 0, C/c = 1, G/g = 2, T/t = 3, any other byte 0 (as A).  One
+ * 128-bit load per word (a 16-byte aligned d_bytes).  Offsets into the bytes
+ * stay valid as base offsets into the words: a sequence at byte offset o is
+ * at base offset o of the packed stream. */
+int hdc_pack_2bit(hdc_context* ctx, const char* d_bytes, int64_t n_bytes, uint32_t* d_words, void* stream);
+
+/* hdc_encode_segments over 2-bit packed reads (hdc_pack_2bit's format, or the
+ * reference's packed sequences placed at base offsets that are multiples of
+ * 16): segment i is bases d_base_off[i] .. + d_len[i] - 1 of the packed
+ * stream.  Every position of a packed segment is a base, so no k-mer is
+ * skipped: on sequences of A, C, G, T the result equals hdc_encode_segments on
+ * the ASCII bytes; bytes the packing turned into A (N, IUPAC codes) count as
+ * A, as in the reference's GPU encoder (src/encode.cu:21-38), not skipped as
+ * in HVCache::compute.  Same outputs, limits and errors as
+ * hdc_encode_segments. */
+int hdc_encode_packed(hdc_context* ctx, const uint32_t* d_words, const int64_t* d_base_off, const int32_t* d_len,
+                      int64_t n_segs, int32_t max_len, int out_kind, void* d_out, int64_t out_stride,
+                      int32_t* d_nkmers, void* stream);
+
 /* Encode n_segs byte segments d_bytes[d_seg_off[i] .. d_seg_off[i]+d_seg_len[i])
  * with the whole-segment semantics of HVCache::compute (src/encoder.cpp:106-132):
  * sum over every k-mer position of the +1/-1 binder of the canonical k-mer.
@@ -341,6 +363,13 @@ int hdc_beam_search_split(hdc_context* ctx, const int8_t* d_q, const int64_t* d_
                           const int32_t* d_child_idx, const int32_t* d_roots, int n_roots, int max_children,
                           int levels, int beam, double threshold, int score_mode, int32_t* d_path,
                           float* d_path_score, int32_t* d_depth, void* stream);
+/* Diagnostic of the last one-launch descent on this context (HDC_BEAM_ONE_LAUNCH):
+ * the duration in ns of each of its phases as its first CTA saw them (from the
+ * launch's start to its first grid barrier, between consecutive barriers, and
+ * from the last barrier to the end), at most max_n of them, their number in
+ * *n_out (0 before the first such descent).  Synchronises the device. */
+int hdc_beam_phase_times(const hdc_context* ctx, int64_t* out_ns, int max_n, int* n_out);
+
 /* The same with the reads as sign bits d_qbits [nq][dim / 32] (HDC_OUT_SIGN_BITS
  * rows, 16-byte aligned): no int8 rows and no packing pass.  Row q starts at
  * word q * (dim / 32): the rows must be dense, so encode them with

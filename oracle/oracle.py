@@ -139,6 +139,26 @@ def encode_copy_bundles(leaves, copies, group, dim, k, nthreads=None):
     return out
 
 
+def pack_2bit(data):
+    """The reference's 2-bit packing (src/encode.cu:169-185, pack_sequence) of a
+    byte string as one stream: base i at bits 2 (i % 16) of word i // 16,
+    A/a = 0, C/c = 1, G/g = 2, T/t = 3, any other byte 0.  Returns uint32
+    words, ceil(len / 16) of them."""
+    b = np.frombuffer(bytes(data), np.uint8)
+    n = len(b)
+    code = np.zeros(((n + 15) // 16) * 16, np.uint32)
+    up = b & 0xDF
+    code[:n] = np.select([up == ord("C"), up == ord("G"), up == ord("T")], [1, 2, 3], 0)
+    code = code.reshape(-1, 16) << (2 * np.arange(16, dtype=np.uint32))
+    return np.bitwise_or.reduce(code, axis=1).astype(np.uint32)
+
+
+def packed_view(seq):
+    """The sequence the packed encoder sees: every byte a base by pack_2bit's
+    codes (lowercase as its base, any other byte as A)."""
+    return "".join(ch.upper() if ch.upper() in "CGT" else "A" for ch in seq)
+
+
 def window_segments(seqs, window, step):
     """Windows of every sequence: (len-window)//step+1 of them (none when
     len < window), window w covering [w*step, w*step+window)."""
