@@ -82,16 +82,19 @@ DROPIN = os.path.join(HERE, "dropin")
 
 
 def build_dropin(dim=1024, kmer=8, window=150, step=10, force=False):
-    """The GPU.cuh drop-in (dropin/gpu_dropin.cpp), its self-check driver and
-    the GPU propagate-children and identify applications for one compile-time
-    configuration, linked against libhdc_gb300.so."""
+    """The GPU.cuh drop-in (dropin/gpu_dropin.cpp, libhdc_dropin.so), the
+    self-check drivers of it and of the encoder.h drop-in (dropin/hvcache/),
+    and the GPU propagate-children and identify applications for one
+    compile-time configuration, linked against libhdc_gb300.so."""
     lib = build(force=force)
     out = os.path.join(OUT, "dropin_D%d_k%d_L%d_s%d" % (dim, kmer, window, step))
     os.makedirs(out, exist_ok=True)
     so = os.path.join(out, "libhdc_dropin.so")
     exe = os.path.join(out, "selftest")
     srcs = [os.path.join(DROPIN, f) for f in ("gpu_dropin.cpp", "selftest.cpp", "GPU.cuh", "config.h",
-                                             "hierarchy.cpp", "hierarchy.h", "propagate_gpu.cpp", "identify_gpu.cpp")]
+                                             "hierarchy.cpp", "hierarchy.h", "propagate_gpu.cpp", "identify_gpu.cpp",
+                                             "hvcache/encoder.h", "hvcache/encoder_gpu.cpp",
+                                             "hvcache/hvcache_selftest.cpp")]
     newest = max([os.path.getmtime(x) for x in srcs] + [os.path.getmtime(lib)])
     last = os.path.join(out, "identify")  # built last
     if not force and os.path.exists(last) and os.path.getmtime(last) >= newest:
@@ -101,6 +104,11 @@ def build_dropin(dim=1024, kmer=8, window=150, step=10, force=False):
     rpath = "-Wl,-rpath," + OUT + ":" + out
     subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared"] + defs + inc +
                           [os.path.join(DROPIN, "gpu_dropin.cpp"), "-L" + OUT, "-lhdc_gb300", rpath, "-o", so])
+    # the encoder.h drop-in (its own directory: a build opts in by putting it on the include path)
+    hv = os.path.join(DROPIN, "hvcache")
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-DNORM_COSINE", "-I" + hv] + defs + inc +
+                          [os.path.join(hv, "hvcache_selftest.cpp"), os.path.join(hv, "encoder_gpu.cpp"),
+                           "-L" + OUT, "-lhdc_gb300", rpath, "-o", os.path.join(out, "hvcache_selftest")])
     subprocess.check_call(["g++", "-O2", "-std=c++17"] + defs + inc +
                           [os.path.join(DROPIN, "selftest.cpp"), "-L" + out, "-lhdc_dropin", "-L" + OUT,
                            "-lhdc_gb300", rpath, "-o", exe])

@@ -137,6 +137,30 @@ int hdc_beam_phase_times(const hdc_context* ctx, int64_t* out_ns, int max_n, int
     return HDC_OK;
 }
 
+int hdc_binders(const hdc_context* ctx, const int64_t* codes, int64_t n, uint64_t* host_out) {
+    if (!ctx || (n > 0 && (!codes || !host_out))) return fail(HDC_ERR_INVALID, "binders: null argument");
+    if (n < 0) return fail(HDC_ERR_INVALID, "binders: negative count");
+    const int W = ctx->words64, k = ctx->kmer;
+    const int excess = W * 64 - ctx->dim;
+    const uint64_t tail = excess > 0 ? (~uint64_t(0)) >> excess : ~uint64_t(0);
+    const int64_t n_codes = (int64_t)1 << (2 * k);
+    for (int64_t i = 0; i < n; ++i)
+        if (codes[i] < 0 || codes[i] >= n_codes) return fail(HDC_ERR_RANGE, "binders: k-mer code out of range");
+    for (int64_t i = 0; i < n; ++i) {
+        uint64_t* out = host_out + (size_t)i * W;
+        for (int w = 0; w < W; ++w) out[w] = ~uint64_t(0);
+        for (int d = 0; d < k; ++d) {  // digit d (d = 0: the first base) rotated by d over the 64 W-bit ring
+            const uint64_t* b = ctx->host_base + (size_t)((codes[i] >> (2 * (k - 1 - d))) & 3) * W;
+            for (int w = 0; w < W; ++w) {
+                const uint64_t next = b[w + 1 == W ? 0 : w + 1];
+                out[w] ^= d == 0 ? b[w] : (b[w] >> d) | (next << (64 - d));
+            }
+        }
+        out[W - 1] &= tail;
+    }
+    return HDC_OK;
+}
+
 int hdc_pack_2bit(hdc_context* ctx, const char* d_bytes, int64_t n_bytes, uint32_t* d_words, void* stream) {
     if (!ctx) return fail(HDC_ERR_INVALID, "pack_2bit: null context");
     if (n_bytes < 0) return fail(HDC_ERR_INVALID, "pack_2bit: negative length");

@@ -35,6 +35,7 @@ SIGNATURES = [
     ("hdc_encode_segments", I32, [P, P, P, P, I64, ctypes.c_int32, I32, P, I64, P, P]),
     ("hdc_num_windows", I64, [P, I64]),
     ("hdc_pack_2bit", I32, [P, P, I64, P, P]),
+    ("hdc_binders", I32, [P, P, I64, P]),
     ("hdc_beam_phase_times", I32, [P, P, I32, ctypes.POINTER(I32)]),
     ("hdc_encode_packed", I32, [P, P, P, P, I64, ctypes.c_int32, I32, P, I64, P, P]),
     ("hdc_encode_windows", I32, [P, P, P, P, I64, I64, P, P]),
@@ -148,6 +149,15 @@ class Context:
         n = d_off.numel()
         check(lib().hdc_encode_segments(self.h, ptr(d_bytes), ptr(d_off), ptr(d_len), n, int(max_len), out_kind,
                                         ptr(out), out.stride(0), ptr(nkmers), stream_ptr(stream)))
+        return out
+
+    def binders(self, codes):
+        """Binder hypervectors [n][ceil(dim / 64)] uint64 of k-mer codes (host)."""
+        import numpy as np
+        c = np.ascontiguousarray(codes, np.int64)
+        out = np.zeros((len(c), (self.dim + 63) // 64), np.uint64)
+        check(lib().hdc_binders(self.h, c.ctypes.data_as(ctypes.c_void_p), len(c),
+                                out.ctypes.data_as(ctypes.c_void_p)))
         return out
 
     def pack_2bit(self, d_bytes, n_bytes=None, stream=None):

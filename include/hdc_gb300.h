@@ -87,6 +87,15 @@ int hdc_stream_sync(void* stream);
 
 /* ---------------------------------------------------------------- (a) encode */
 
+/* K-mer binder hypervectors, the values of HVCache::kmers (src/encoder.cpp:
+ * 47-74), computed on the host from the context's base hypervectors: for each
+ * of n k-mer codes (2 bits a base, A=0 C=1 G=2 T=3, the first base in the most
+ * significant digit, below 4^kmer) the binder ~0 ^ XOR_d rot_d(base[digit d])
+ * over the ring of 64 W bits with the tail masked, W = ceil(dim / 64) uint64
+ * words each, into host_out [n][W].  The code is used as given: pass the
+ * canonical k-mer (the smaller of the k-mer and its reverse complement). */
+int hdc_binders(const hdc_context* ctx, const int64_t* codes, int64_t n, uint64_t* host_out);
+
 /* 2-bit packing of reads on the device, the format of the reference's
  * pack_sequence (src/encode.cu:169-185): base i of the byte stream d_bytes
  * [n_bytes] goes to bits 2 (i % 16) of d_words[i / 16] (ceil(n_bytes / 16)
