@@ -263,6 +263,9 @@ __global__ void __launch_bounds__(kThreads) encode_kernel(const EncodeArgs a) {
         if (w32 >= a.W32) continue;
 
         if (a.out_kind == HDC_OUT_SIGN_BITS) {
+            // a row has ceil(dim / 32) words: a lane whose word starts at or past dim writes nothing
+            // (the ring of 64-bit words can hold one more 32-bit word than that)
+            if (w32 * 32 >= a.dim) continue;
             // 2 count - nvalid >= 0, i.e. count >= ceil(nvalid / 2), compared plane by plane
             // from the most significant: gt = lanes already above, eq = equal so far
             const uint32_t thr = (uint32_t)(nvalid + 1) >> 1;

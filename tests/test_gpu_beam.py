@@ -308,11 +308,13 @@ def _pack_signs(q8, dim):
     return (pos.view(n, words, 32) * weights).sum(dim=2)
 
 
-@pytest.mark.parametrize("dim,kmer", [(1000, 8), (1024, 12), (2048, 10)])
+@pytest.mark.parametrize("dim,kmer", [(1000, 8), (1024, 12), (2048, 10), (200, 3), (1056, 8), (96, 5)])
 def test_sign_bits_output_equals_packed_bipolar(hdc, cuda, dim, kmer):
     """HDC_OUT_SIGN_BITS rows are the packed signs of HDC_OUT_BIPOLAR_I8 rows
     (0 -> +1, bits past dim 0), for segments of 0 to 1,600 bytes (counters of
-    4, 8 and 12 high planes) with N and lowercase bytes."""
+    4, 8 and 12 high planes) with N and lowercase bytes; dense rows of
+    ceil(dim / 32) words and nothing written past them (dims 200, 1056, 96:
+    one 32-bit word fewer than the ring of 64-bit words holds)."""
     import torch
     H = hdc
     rng = np.random.default_rng(dim + kmer)
@@ -326,10 +328,13 @@ def test_sign_bits_output_equals_packed_bipolar(hdc, cuda, dim, kmer):
         d_buf, d_off, d_len = (torch.from_numpy(x.copy()).to(cuda) for x in (buf, off, ln))
         q8 = torch.empty((len(batch), dim), dtype=torch.int8, device=cuda)
         ctx.encode_segments(d_buf, d_off, d_len, q8, H.OUT_BIPOLAR_I8, max_len)
-        bits = torch.empty((len(batch), (dim + 31) // 32), dtype=torch.int32, device=cuda)
+        words = (dim + 31) // 32
+        guard = torch.full((len(batch) * words + 64,), 0x5A5A5A5A, dtype=torch.int32, device=cuda)
+        bits = guard[:len(batch) * words].view(len(batch), words)
         ctx.encode_segments(d_buf, d_off, d_len, bits, H.OUT_SIGN_BITS, max_len)
         want = _pack_signs(q8, dim)
         assert torch.equal(bits.to(torch.int64) & 0xFFFFFFFF, want), max_len
+        assert (guard[len(batch) * words:] == 0x5A5A5A5A).all()  # nothing past the last row
 
 
 def test_beam_split_bit_reads_equal_int8_reads(hdc, cuda):
