@@ -734,10 +734,14 @@ __device__ __forceinline__ void cp_async_wait() {
 // 16-byte chunk c of row r of a 128-byte-row tile in the 128-byte swizzle layout
 __device__ __forceinline__ uint8_t* swz(uint8_t* tile, int r, int c) { return tile + r * 128 + ((c ^ (r & 7)) << 4); }
 
+constexpr int kRowSlots = 8;        // at most this many rows of a streamed level in shared memory
+constexpr int kRowConsumers = 12;   // warps 1-12 score the streamed rows' pairs; warp 0 stages them
+
 // Shared-memory state of the tensor-core scoring (one CTA per SM).
 struct TcShared {
     uint64_t full_bar[kTcStages], empty_bar[kTcStages], accf_bar[2], acce_bar[2];
     uint64_t drain_bar;  // the MMA issuer's last commit before TMEM is freed
+    uint64_t row_full[kRowSlots], row_empty[kRowSlots];  // the streamed rows of a CUDA-core level
     uint32_t tmem_base;
     int err;             // code of a wait that gave up (0: none)
     uint2 signs_lut[16];
@@ -749,6 +753,7 @@ struct TcRun {
     int64_t nbase = 0;          // producers: K blocks of the items this CTA has staged
     int stage = 0, acc = 0;     // MMA issuer: next stage and accumulator set; epilogue: next set
     uint32_t phase = 0, acc_phase = 0;
+    int64_t row_ord = 0;        // streamed levels: rows this CTA has staged (producer) or scored (consumers)
 };
 
 // Barriers, sign table and 256 TMEM columns of the CTA (every thread calls it).
@@ -766,6 +771,10 @@ __device__ void tc_setup(TcShared& sm) {
             tc::mbar_init(&sm.acce_bar[b], 4);  // one arrival per epilogue warp
         }
         tc::mbar_init(&sm.drain_bar, 1);
+        for (int i = 0; i < kRowSlots; ++i) {
+            tc::mbar_init(&sm.row_full[i], 1);
+            tc::mbar_init(&sm.row_empty[i], kRowConsumers);
+        }
         tc::fence_mbar_init();
     }
     if (warp == 12) {
@@ -1139,6 +1148,140 @@ __device__ int32_t cta_prefix(const int32_t* blk, int b, int32_t* sh) {
     return total;
 }
 
+// A streamed CUDA-core level (the leaves of the one-launch descent): the pairs are in node
+// order, so each candidate node's prototype row is copied once from HBM into shared memory by
+// a 1-D bulk copy (warp 0) and its pairs are scored from there by warps 1-12, rows in a ring
+// of kRowSlots slots.  CTA b owns the nodes whose first pair falls in its share of the pair
+// list.  The FP64 scores are computed 32 pairs at a time, one per lane.
+__device__ __forceinline__ int64_t smem_dot16(const GArgs& a, const int4* rowv, int lane, int64_t r) {
+    constexpr int U = 8;
+    const int nsteps = a.dim / 256;  // a multiple of 4 (dim % 1024 == 0)
+    const int sh = (lane & 3) * 8;
+    const uint32_t* qb = a.bits + r * a.words + (lane >> 2);
+    int acc = 0;
+    for (int j = 0; j < nsteps; j += U) {
+        int4 x[U];
+        uint32_t w[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const bool in = j + u < nsteps;
+            x[u] = in ? rowv[32 * (j + u)] : make_int4(0, 0, 0, 0);
+            w[u] = in ? __ldg(qb + 8 * (j + u)) : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint32_t byte = w[u] >> sh;
+            const int s0 = signs4_bytes(byte & 15u), s1 = signs4_bytes((byte >> 4) & 15u);
+            acc = __dp2a_lo(x[u].x, s0, acc);
+            acc = __dp2a_hi(x[u].y, s0, acc);
+            acc = __dp2a_lo(x[u].z, s1, acc);
+            acc = __dp2a_hi(x[u].w, s1, acc);
+        }
+    }
+    return acc;
+}
+
+__device__ __forceinline__ int64_t smem_dot32(const GArgs& a, const int4* rowv, int lane, int64_t r) {
+    const int nsteps = a.dim / 128;
+    const int sh = (lane & 7) * 4;
+    const uint32_t* qb = a.bits + r * a.words + (lane >> 3);
+    int64_t acc = 0;
+    for (int j = 0; j < nsteps; ++j) {
+        const int4 x = rowv[32 * j];
+        const uint32_t nib = __ldg(qb + 4 * j) >> sh;
+        acc += (int64_t)((nib & 1u) ? x.x : neg32(x.x)) + (int64_t)((nib & 2u) ? x.y : neg32(x.y)) +
+               (int64_t)((nib & 4u) ? x.z : neg32(x.z)) + (int64_t)((nib & 8u) ? x.w : neg32(x.w));
+    }
+    return acc;
+}
+
+// first n in [0, n_nodes] with node_off[n] >= x
+__device__ __forceinline__ int64_t first_node_at(const GArgs& a, int64_t x) {
+    int64_t lo = 0, hi = a.n_nodes;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (a.node_off[mid] >= x)
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    return lo;
+}
+
+__device__ void stream_phase(const GArgs& a, TcShared& sm, TcRun& run, uint8_t* ring) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t total = a.off[a.nq];
+    const int64_t pc = (total + gridDim.x - 1) / gridDim.x;
+    const int64_t n_lo = first_node_at(a, (int64_t)blockIdx.x * pc);
+    const int64_t n_hi = blockIdx.x + 1 == gridDim.x ? a.n_nodes : first_node_at(a, (int64_t)(blockIdx.x + 1) * pc);
+    const uint32_t slot_bytes = (uint32_t)a.dim * (a.n32 > 0 ? 4u : 2u);
+    const int S = min(kRowSlots, (int)((size_t)(kTcStages * kTcStageBytes + kTcStageArea) / slot_bytes));
+    if (warp == 0) {
+        if (lane != 0) return;
+        tc::fence_proxy_async();  // the ring's earlier generic-proxy writes come before the bulk copies
+        int64_t issued = 0;
+        for (int64_t n = n_lo; n < n_hi; ++n) {
+            if (a.node_off[n + 1] == a.node_off[n]) continue;
+            const int64_t i = run.row_ord++;
+            const int slot = (int)(i % S);
+            if (!tc::mbar_wait(&sm.row_empty[slot], (uint32_t)((i / S) & 1) ^ 1u, &sm.err, 15)) break;
+            const bool w16 = n >= a.n32;
+            const uint32_t bytes = (uint32_t)a.dim * (w16 ? 2u : 4u);
+            const void* src = w16 ? (const void*)(a.proto16 + (n - a.n32) * a.dim) : (const void*)(a.proto + n * a.dim);
+            tc::mbar_arrive_expect_tx(&sm.row_full[slot], bytes);
+            tc::bulk_load_1d(ring + (size_t)slot * slot_bytes, src, bytes, &sm.row_full[slot]);
+            ++issued;
+        }
+        // copies still landing when the consumers gave up early: let them finish (bounded)
+        for (int64_t k = 0; k < min(issued, (int64_t)S); ++k) {
+            const int64_t i = run.row_ord - 1 - k;
+            const long long c0 = clock64();
+            while (!tc::mbar_try_wait(tc::smem_u32(&sm.row_full[i % S]), (uint32_t)((i / S) & 1)) &&
+                   clock64() - c0 < tc::kWaitCycles) {
+            }
+        }
+        return;
+    }
+    // consumers: warp c takes the pairs at positions P0 + c, P0 + c + 12, ... of the CTA's range
+    const int c = warp - 1;
+    const int64_t P0 = a.node_off[n_lo];
+    int32_t my_pi = -1, my_node = 0;
+    int64_t my_r = 0, my_dot = 0;
+    int cnt = 0;
+    auto flush = [&]() {
+        if (my_pi >= 0)
+            a.pair_key[my_pi] = make_key(exact_score(my_dot, a.qn[my_r], a.pn[my_node], a.mode), (uint32_t)my_node);
+        my_pi = -1;
+    };
+    for (int64_t n = n_lo; n < n_hi; ++n) {
+        const int64_t ps = a.node_off[n], pe = a.node_off[n + 1];
+        if (ps == pe) continue;
+        const int64_t i = run.row_ord++;
+        const int slot = (int)(i % S);
+        if (!tc::mbar_wait(&sm.row_full[slot], (uint32_t)((i / S) & 1), &sm.err, 16)) break;
+        const int4* rowv = reinterpret_cast<const int4*>(ring + (size_t)slot * slot_bytes) + lane;
+        const bool w16 = n >= a.n32;
+        for (int64_t s = ps + ((c - (ps - P0) % kRowConsumers) + kRowConsumers) % kRowConsumers; s < pe;
+             s += kRowConsumers) {
+            const int32_t pi = a.sorted[s];
+            const int64_t r = a.pair_read[pi];
+            int64_t acc = w16 ? smem_dot16(a, rowv, lane, r) : smem_dot32(a, rowv, lane, r);
+            for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == (cnt & 31)) {
+                my_pi = pi;
+                my_node = (int32_t)n;
+                my_r = r;
+                my_dot = acc;
+            }
+            if ((cnt & 31) == 31) flush();
+            ++cnt;
+        }
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&sm.row_empty[slot]);
+    }
+    flush();
+}
+
 __global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs a, const TcItems t, const OneArgs o) {
     extern __shared__ uint8_t smem_raw[];
     __shared__ TcShared sm;
@@ -1256,8 +1399,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs 
             // E: the pairs in node order
             scatter_range(a, gtid, gstride);
             if (!(ok = grid_barrier(o, sm, &ok_s, &n_ts))) break;
-            // F: the pairs scored on the CUDA cores, one warp per pair
-            if (rows16)
+            // F: the pairs scored on the CUDA cores: the leaf level's rows streamed through shared
+            // memory, other levels (every level without the tensor cores) one warp per pair
+            if (o.use_tc)
+                stream_phase(a, sm, run, ring);
+            else if (rows16)
                 score_pairs<true>(a, gtid >> 5, gstride >> 5);
             else
                 score_pairs<false>(a, gtid >> 5, gstride >> 5);

@@ -946,12 +946,126 @@ def _descent_worker_q(q):
                              O.SCORE_NORM, pn=d["pn"]))
 
 
+def _event_ms(fn, reps=5):
+    """Median CUDA-event time (ms) of fn() on the current stream, after one warm-up call."""
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = []
+    for _ in range(reps):
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        out.append(e0.elapsed_time(e1))
+    return float(np.median(out))
+
+
+def fasta_bytes(n_records, read_len, line=60, seed=0):
+    """A FASTA file of n_records random reads (names ">r" + 9 digits) in lines of `line` bases."""
+    rng = np.random.default_rng(seed)
+    bases = np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, (n_records, read_len))]
+    nl = (read_len + line - 1) // line
+    body = np.full((n_records, read_len + nl), ord("\n"), np.uint8)
+    for j in range(nl):
+        a, b = j * line, min(read_len, (j + 1) * line)
+        body[:, a + j:b + j] = bases[:, a:b]
+    ids = np.arange(n_records)
+    name = np.empty((n_records, 11), np.uint8)
+    name[:, 0] = ord(">")
+    name[:, 1] = ord("r")
+    for p in range(9):
+        name[:, 10 - p] = ord("0") + (ids // 10 ** p) % 10
+    return np.concatenate([name, np.full((n_records, 1), ord("\n"), np.uint8), body], axis=1).reshape(-1)
+
+
+def run_aux(args):
+    """Kernels beside the headline path, at sizes above L2, each timed alone with CUDA events
+    (median of 5 after a warm-up): FASTA ingest, 2-bit packing, read encode from ASCII and from
+    packed words, windowed similarity.  One JSON line with each kernel's time and achieved
+    bandwidth against the measured HBM peak."""
+    import torch
+    import hdc_gb300 as H
+    pk, src = peaks()
+    hbm = pk["hbm_gbs"]
+    dev = torch.device("cuda", 0)
+    out = {}
+    # FASTA ingest: 3,000,000 records of 250 bp in 60-column lines
+    data = fasta_bytes(3000000, 250)
+    d = torch.from_numpy(data).to(dev)
+    ctx = H.Context(10240, 10, 250, 10)
+    ms = _event_ms(lambda: ctx.fasta_parse(d, 3000001))
+    seq_bytes, so, sl, _, _, n_rec = ctx.fasta_parse(d, 3000001)
+    out["fasta_parse"] = {"input_bytes": int(d.numel()), "records": int(n_rec), "ms": ms,
+                          "input_gb_per_s": d.numel() / (ms / 1e3) / 1e9,
+                          "note": "several byte-parallel passes over ~61 bytes of workspace per input byte"}
+    # 2-bit packing of the parsed sequence bytes (read 1 byte, write 1/4 byte per base)
+    n_seq = int(so[-1] + sl[-1])
+    words = ctx.pack_2bit(seq_bytes, n_seq)
+    ms = _event_ms(lambda: ctx.pack_2bit(seq_bytes, n_seq))
+    moved = n_seq + 4 * ((n_seq + 15) // 16)
+    out["pack_2bit"] = {"bases": n_seq, "ms": ms, "gb_per_s": moved / (ms / 1e3) / 1e9,
+                        "frac_of_hbm": moved / (ms / 1e3) / 1e9 / hbm}
+    # read encode, c3 shape (38,912 reads of 250 bp, D = 10,240, k = 10, +1/-1 fp16 rows), from
+    # ASCII and from packed words
+    B = 38912
+    offs, lens = so[:B], sl[:B]
+    q = torch.empty((B, 10240), dtype=torch.float16, device=dev)
+    t_ascii = _event_ms(lambda: ctx.encode_segments(seq_bytes, offs, lens, q, H.OUT_BIPOLAR_F16, 250))
+    a = q.clone()
+    t_packed = _event_ms(lambda: ctx.encode_packed(words, offs, lens, q, H.OUT_BIPOLAR_F16, 250))
+    torch.cuda.synchronize()
+    out["encode_reads"] = {"reads": B, "ascii_ms": t_ascii, "packed_ms": t_packed,
+                           "identical": bool(torch.equal(a, q)),
+                           "reads_per_s_ascii": B / (t_ascii / 1e3), "reads_per_s_packed": B / (t_packed / 1e3),
+                           "bound": "integer/logic pipe (bundling), not bytes: 250 B of ASCII per read in"}
+    del d, seq_bytes, words, q, a
+    # windowed similarity (HVCache::similarity batched): 4,096 queries of 150 bp x 16 references of
+    # 1,500 bp each (135 windows), D = 8,192, k = 8
+    sctx = H.Context(8192, 8, 150, 10)
+    tree = H.synth_tree(21, 2000)
+    reads = H.synth_reads(22, tree, 4096, 150, subst=0.01)
+    wins_off, ref_rows, whole = [], [0], []
+    for i in range(len(tree)):
+        o, n = int(tree.off[i]), int(tree.len[i])
+        xs = list(range(0, n - 150, 10))
+        wins_off += [o + x for x in xs]
+        ref_rows.append(len(wins_off))
+        whole.append(0)
+    d_tree = torch.from_numpy(tree.buf).to(dev)
+    rows = torch.empty((len(wins_off), 8192), dtype=torch.int16, device=dev)
+    sctx.encode_segments(d_tree, torch.tensor(wins_off, dtype=torch.int64, device=dev),
+                         torch.full((len(wins_off),), 150, dtype=torch.int32, device=dev), rows, H.OUT_I16, 150)
+    qv = torch.empty((4096, 8192), dtype=torch.int16, device=dev)
+    sctx.encode_segments(torch.from_numpy(reads.buf).to(dev), torch.from_numpy(reads.off).to(dev),
+                         torch.from_numpy(reads.len).to(dev), qv, H.OUT_I16, 150)
+    qn, rn = sctx.norms(qv), sctx.norms(rows)
+    g = np.random.default_rng(5)
+    pq = np.repeat(np.arange(4096), 16).astype(np.int32)
+    pr = (np.asarray(reads.label)[pq] + g.integers(-8, 8, pq.size)).clip(0, len(tree) - 1).astype(np.int32)
+    d_rr = torch.tensor(ref_rows, dtype=torch.int64, device=dev)
+    d_pq, d_pr = torch.from_numpy(pq).to(dev), torch.from_numpy(pr).to(dev)
+    ms = _event_ms(lambda: sctx.similarity(qv, qn, rows, rn, d_rr, None, d_pq, d_pr))
+    n_pairs = pq.size
+    row_bytes = float(np.sum(np.diff(ref_rows)[pr])) * 8192 * 2
+    out["similarity"] = {"pairs": int(n_pairs), "window_rows_read": int(np.sum(np.diff(ref_rows)[pr])), "ms": ms,
+                         "row_gb_per_s": row_bytes / (ms / 1e3) / 1e9,
+                         "unique_row_bytes": int(rows.numel() * 2),
+                         "note": "row bytes of every pair (rows shared by pairs come from L2)"}
+    line = {"metric": "auxiliary kernels (ms, GB/s)", "unit": "ms", "n_gpus": 1, "higher_is_better": False,
+            "data": "synthetic", "config": {"workload": "aux: FASTA ingest, 2-bit packing, read encode, "
+                                                         "windowed similarity"},
+            "peak_hbm_gbs": hbm, "peak_source": "%s (MEASURED_PEAKS.json)" % src, "kernels": out}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--config", default="c3", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="c3", choices=sorted(CONFIGS) + ["aux"])
     ap.add_argument("--form", default="", choices=["", "plain", "tc", "pipe", "descent"],
                     help="default: tc for c3, pipe for c4, plain for c2, descent for c5")
     ap.add_argument("--batch", type=int, default=0,
@@ -963,6 +1077,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--refs", type=int, default=0, help="override the number of references (small profiling cases)")
+    ap.add_argument("--topk", type=int, default=0, help="override k of the top-k search (0: the workload's)")
     ap.add_argument("--tc-group", type=int, default=0, help="tensor-core search: query tiles per group (0: library default)")
     ap.add_argument("--tc-cluster", type=int, default=0, help="tensor-core search: CTAs sharing reference blocks (0: default)")
     ap.add_argument("--beam-grouped", type=int, default=-1,
@@ -975,11 +1090,17 @@ def main():
     if args.warmup < 3:
         log("warmup raised to 3")
         args.warmup = 3
+    if args.config == "aux":  # kernels beside the headline path, timed one by one
+        if int(os.environ.get("WORLD_SIZE", "1")) == 1 and args.impl == "ours":
+            run_aux(args)
+        return
     cfg = dict(CONFIGS[args.config])
     if not args.form:
         args.form = {"c2": "plain", "c3": "tc", "c4": "pipe", "c5": "descent"}[args.config]
     if args.refs:
         cfg["n_leaves"] = args.refs
+    if args.topk:
+        cfg["topk"] = args.topk
     if cfg.get("sigma"):
         reads_desc = "log-normal reads (median %d bp, sigma %.1f, %d-%d bp, %d%% with %d%% sub:ins:del 3:1:1)" % (
             cfg["read_len"], cfg["sigma"], cfg["min_read"], cfg["max_read"], 100 * cfg["mixed_frac"],
