@@ -176,6 +176,8 @@ struct GArgs {
     int32_t* pair_slot;       // [P] beam row the candidate expands
     uint64_t* pair_key;       // [P]
     int32_t* sorted;          // [P] pair indices ordered by node
+    int64_t* part;            // [kQuarters][pstride] partial dots of a streamed level (one-launch form)
+    int64_t pstride;
 };
 
 // A caller-given largest child count below the tree's sizes the pair arrays too small: every
@@ -485,11 +487,14 @@ __global__ void output_kernel(const GArgs a, int32_t* __restrict__ path, float* 
 // Levels above the leaves score on the tensor cores, grouped by parent: the entries (read,
 // beam slot) whose beam row is node P are scored against P's children (a childless P
 // against itself) as one dense [entries] x [children] product.  A work item is up to 128
-// entries x 32 children of one parent.  Eight producer warps write the entries' +1/-1 signs
-// (from the packed bits) and the children's int32 prototype rows, split into three
-// balanced base-2048 fp16 limbs, into 128-byte-swizzled shared memory (two groups of four
-// warps on alternate K blocks); one thread issues M128 x N96 x K16 tcgen05 MMAs, the three
-// limb tiles side by side, into one fp32 TMEM accumulator of 32 columns per limb; four epilogue
+// entries x 32 children of one parent.  Eight producer warps (two groups of four on alternate
+// K blocks) write the entries' +1/-1 signs (from the packed bits) as fp16 straight into TMEM
+// with tcgen05.st (the A operand: lane = entry, two signs a column), and the children's int32
+// prototype rows, split into three balanced base-2048 fp16 limbs, into 128-byte-swizzled
+// shared memory (the B operand); one thread issues M128 x N96 x K16 tcgen05 MMAs with A from
+// TMEM, the three limb tiles side by side, into one fp32 TMEM accumulator of 32 columns per
+// limb.  A in TMEM takes the signs' shared-memory stores and the MMAs' shared-memory reads of
+// A (32 KB of the ~60 KB of shared-memory traffic of a K block) off the shared memory.  Four epilogue
 // warps recombine the exact int64 dots and write the pair keys the select kernel reads.
 // Exact: a limb is at most 1024 in magnitude (the top one 512), so every partial sum is an
 // integer of magnitude <= dim * 1024 <= 2^24.  Level 0 is one parent (-1) whose children
@@ -507,11 +512,12 @@ constexpr int kTcDepth = 4;
 constexpr int kTcProducers = 256;
 constexpr size_t kTcStageArea = (size_t)kTcDepth * 5 * kTcProducers * 16;  // 4 x 16 B values + 16 B bits
 constexpr int kTcAccCols = kTcLimbs * kTcC;                       // one accumulator set
-constexpr int kTcTmemCols = 256;                                  // two sets
+constexpr int kTcTmemCols = 512;                                  // two sets, then the A stages
+constexpr int kTcACol = 256;                                      // A of stage s: columns kTcACol + 32 s
 constexpr int kTcThreads = 416;                                   // warps 0-7 produce, 8-11 epilogue, 12 MMA
-constexpr int kTcABytes = kTcE * 128;                             // 64 dims of fp16 per row
 constexpr int kTcBBytes = kTcC * 128;                             // per limb
-constexpr int kTcStageBytes = kTcABytes + kTcLimbs * kTcBBytes;   // 28 KB
+constexpr int kTcStageBytes = kTcLimbs * kTcBBytes;              // 12 KB of B (A is in TMEM)
+static_assert(kTcACol + 32 * kTcStages <= kTcTmemCols, "the A stages fit the TMEM allocation");
 constexpr size_t kTcSmem = (size_t)kTcStages * kTcStageBytes + kTcStageArea + 1024;
 
 struct TcItems {
@@ -706,16 +712,6 @@ __device__ __forceinline__ uint32_t half2_bits(int32_t x, int32_t y) {
     return *reinterpret_cast<const uint32_t*>(&h);
 }
 
-// 4 sign bits (bit i set: +1) -> 4 fp16 values, +1 = 0x3C00, -1 = 0xBC00: the table
-// entries are 8 bytes, so the 16 of them cover the 32 banks and lookups never conflict
-__device__ __forceinline__ uint2 signs4_entry(uint32_t n) {
-    uint32_t v[2];
-#pragma unroll
-    for (int i = 0; i < 2; ++i)
-        v[i] = 0xBC00BC00u ^ (((n >> (2 * i)) & 1u) << 15) ^ (((n >> (2 * i + 1)) & 1u) << 31);
-    return make_uint2(v[0], v[1]);
-}
-
 // cp.async of 16 / 8 bytes global -> shared; with src_bytes 0 nothing is read and zeros land
 __device__ __forceinline__ void cp_async16(void* dst, const void* src, uint32_t src_bytes) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(tc::smem_u32(dst)), "l"(src), "r"(src_bytes)
@@ -734,17 +730,21 @@ __device__ __forceinline__ void cp_async_wait() {
 // 16-byte chunk c of row r of a 128-byte-row tile in the 128-byte swizzle layout
 __device__ __forceinline__ uint8_t* swz(uint8_t* tile, int r, int c) { return tile + r * 128 + ((c ^ (r & 7)) << 4); }
 
-constexpr int kRowSlots = 8;        // at most this many rows of a streamed level in shared memory
-constexpr int kRowConsumers = 12;   // warps 1-12 score the streamed rows' pairs; warp 0 stages them
+// A streamed level's rows are staged in dim quarters, one ring of at most kRowSlots slots per
+// quarter; warps 1-12 score (three groups of four, warp 1 + 4 g + q takes quarter q of group g's
+// pairs) and warp 0 stages.
+constexpr int kRowSlots = 8;
+constexpr int kRowConsumers = 12;
+constexpr int kQuarters = 4;
+constexpr int kRowGroups = kRowConsumers / kQuarters;
 
 // Shared-memory state of the tensor-core scoring (one CTA per SM).
 struct TcShared {
     uint64_t full_bar[kTcStages], empty_bar[kTcStages], accf_bar[2], acce_bar[2];
     uint64_t drain_bar;  // the MMA issuer's last commit before TMEM is freed
-    uint64_t row_full[kRowSlots], row_empty[kRowSlots];  // the streamed rows of a CUDA-core level
+    uint64_t row_full[kQuarters * kRowSlots], row_empty[kQuarters * kRowSlots];  // quarter q's ring: [q * kRowSlots, ..)
     uint32_t tmem_base;
     int err;             // code of a wait that gave up (0: none)
-    uint2 signs_lut[16];
 };
 
 // Ring positions of the roles, carried from one scoring phase to the next when one
@@ -756,10 +756,9 @@ struct TcRun {
     int64_t row_ord = 0;        // streamed levels: rows this CTA has staged (producer) or scored (consumers)
 };
 
-// Barriers, sign table and 256 TMEM columns of the CTA (every thread calls it).
+// Barriers and the TMEM columns of the CTA (every thread calls it).
 __device__ void tc_setup(TcShared& sm) {
     const int warp = threadIdx.x >> 5;
-    if (threadIdx.x < 16) sm.signs_lut[threadIdx.x] = signs4_entry(threadIdx.x);
     if (threadIdx.x == 0) {
         sm.err = 0;
         for (int s = 0; s < kTcStages; ++s) {
@@ -771,9 +770,9 @@ __device__ void tc_setup(TcShared& sm) {
             tc::mbar_init(&sm.acce_bar[b], 4);  // one arrival per epilogue warp
         }
         tc::mbar_init(&sm.drain_bar, 1);
-        for (int i = 0; i < kRowSlots; ++i) {
+        for (int i = 0; i < kQuarters * kRowSlots; ++i) {
             tc::mbar_init(&sm.row_full[i], 1);
-            tc::mbar_init(&sm.row_empty[i], kRowConsumers);
+            tc::mbar_init(&sm.row_empty[i], kRowGroups);  // one warp per group reads a quarter
         }
         tc::fence_mbar_init();
     }
@@ -879,14 +878,16 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
                         break;
                     }
                     uint8_t* st = ring + (size_t)stage * kTcStageBytes;
-                    // A: this entry's 64 signs
-                    if (rrow >= 0) {
+                    // A: this entry's 64 signs, two fp16 to a column, into TMEM lane tid (an unused
+                    // row's garbage only reaches its own accumulator row, which is never read)
+                    {
+                        uint32_t col[32];
 #pragma unroll
-                        for (int c = 0; c < 8; ++c) {
-                            const uint32_t byte = ((c < 4 ? w.x : w.y) >> (8 * (c & 3))) & 0xffu;
-                            const uint2 lo = sm.signs_lut[byte & 15u], hi = sm.signs_lut[byte >> 4];
-                            *reinterpret_cast<uint4*>(swz(st, tid, c)) = make_uint4(lo.x, lo.y, hi.x, hi.y);
+                        for (int j = 0; j < 32; ++j) {
+                            const uint32_t t = (j < 16 ? w.x : w.y) >> (2 * (j & 15));
+                            col[j] = 0xBC00BC00u ^ ((t & 1u) << 15) ^ ((t & 2u) << 30);
                         }
+                        tc::tmem_st32(tmem + ((uint32_t)(warp & 3) << 21) + (uint32_t)(kTcACol + 32 * stage), col);
                     }
                     // B: this thread's groups of 4 prototype values, each in three limbs (8 bytes per limb)
 #pragma unroll
@@ -904,14 +905,16 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
                         for (int e = 0; e < 4; ++e) limbs3(x[e], l0[e], l1[e], l2[e]);
                         const int js = gdst[j] >> 4, u = gdst[j] & 15;
                         const int off = (u & 1) * 8;
-                        *reinterpret_cast<uint2*>(swz(st + kTcABytes, js, u >> 1) + off) =
+                        *reinterpret_cast<uint2*>(swz(st, js, u >> 1) + off) =
                             make_uint2(half2_bits(l0[0], l0[1]), half2_bits(l0[2], l0[3]));
-                        *reinterpret_cast<uint2*>(swz(st + kTcABytes + kTcBBytes, js, u >> 1) + off) =
+                        *reinterpret_cast<uint2*>(swz(st + kTcBBytes, js, u >> 1) + off) =
                             make_uint2(half2_bits(l1[0], l1[1]), half2_bits(l1[2], l1[3]));
-                        *reinterpret_cast<uint2*>(swz(st + kTcABytes + 2 * kTcBBytes, js, u >> 1) + off) =
+                        *reinterpret_cast<uint2*>(swz(st + 2 * kTcBBytes, js, u >> 1) + off) =
                             make_uint2(half2_bits(l2[0], l2[1]), half2_bits(l2[2], l2[3]));
                     }
-                    tc::fence_proxy_async();  // the writes above are read by the tensor cores
+                    tc::tmem_st_wait();       // the A columns are written
+                    tc::fence_before();       // ... before the arrive below (tcgen05 ordering)
+                    tc::fence_proxy_async();  // the B writes above are read by the tensor cores
                     __syncwarp();
                     if (lane == 0) tc::mbar_arrive(&sm.full_bar[stage]);
                 }
@@ -983,11 +986,11 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
                 }
                 tc::fence_after();
                 const uint32_t sa = tc::smem_u32(ring + (size_t)stage * kTcStageBytes);
-                const uint64_t adesc = tc::kmajor_desc(sa, 1024, 2);
-                const uint64_t bdesc = tc::kmajor_desc(sa + kTcABytes, 1024, 2);
+                const uint64_t bdesc = tc::kmajor_desc(sa, 1024, 2);
+                const uint32_t a_tm = tmem + (uint32_t)(kTcACol + 32 * stage);  // 8 columns per K = 16
 #pragma unroll
                 for (int kk = 0; kk < 4; ++kk)
-                    tc::mma_f16(d, adesc + 2 * kk, bdesc + 2 * kk, IDESC, (kb | kk) != 0 ? 1u : 0u);
+                    tc::mma_f16_ta(d, a_tm + 8 * kk, bdesc + 2 * kk, IDESC, (kb | kk) != 0 ? 1u : 0u);
                 tc::mma_commit(&sm.empty_bar[stage]);
                 if (++stage == kTcStages) {
                     stage = 0;
@@ -1048,6 +1051,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a
 // scoring keeps its TMEM columns and mbarrier ring positions from one level to the next.
 
 constexpr int kCodeGridBarrier = 20;  // status 100 + this: a grid barrier gave up
+// Dynamic shared memory of the one-launch kernel: the tensor-core levels use the first kTcSmem
+// bytes; the streamed leaf level uses all of it (row slots + the consumers' bit buffers).
+constexpr size_t kOneSmem = 225 * 1024;
+static_assert(kOneSmem >= kTcSmem, "the one-launch kernel also runs the tensor-core levels");
 constexpr int kMaxPhaseTs = 64;       // phase timestamps kept of a launch (hdc_beam_phase_times)
 
 struct OneArgs {
@@ -1150,15 +1157,25 @@ __device__ int32_t cta_prefix(const int32_t* blk, int b, int32_t* sh) {
 
 // A streamed CUDA-core level (the leaves of the one-launch descent): the pairs are in node
 // order, so each candidate node's prototype row is copied once from HBM into shared memory by
-// a 1-D bulk copy (warp 0) and its pairs are scored from there by warps 1-12, rows in a ring
-// of kRowSlots slots.  CTA b owns the nodes whose first pair falls in its share of the pair
-// list.  The FP64 scores are computed 32 pairs at a time, one per lane.
-__device__ __forceinline__ int64_t smem_dot16(const GArgs& a, const int4* rowv, int lane, int64_t r) {
+// 1-D bulk copies (warp 0, evict-first in L2: a row is read once per call) and its pairs are
+// scored from there.  A row travels as four quarters of its dims, each through its own ring;
+// warp 1 + 4 g + q sums quarter q of the pairs of group g (the pairs at positions P0 + g,
+// P0 + g + 3, ... of the CTA's share of the node-ordered list) and writes that partial dot,
+// so a pair is scored by four warps at once and a quarter row is held only while three warps
+// use it: more of the shared memory holds rows in flight.  The bits of a warp's next pair (its
+// quarter) are copied into a private buffer (cp.async) while it scores the current one.  The
+// partial dots are summed, and the FP64 scores computed, by the CTA that owns the read, after
+// the next grid barrier (keys_from_parts).  CTA b owns the nodes whose first pair falls in its
+// share of the pair list.
+constexpr int kBitsBufs = 2;  // per consumer warp: the current pair's bits and the next one's
+
+// Lane l's share of a quarter of int16 row dims: steps j of 256 dims, 8 dims a lane (one
+// 16-byte word of the row, one byte of the read's bits)
+__device__ __forceinline__ int64_t smem_dot16(const int4* rowv, const uint32_t* bits, int lane, int nsteps) {
     constexpr int U = 8;
-    const int nsteps = a.dim / 256;  // a multiple of 4 (dim % 1024 == 0)
     const int sh = (lane & 3) * 8;
-    const uint32_t* qb = a.bits + r * a.words + (lane >> 2);
-    int acc = 0;
+    const uint32_t* qb = bits + (lane >> 2);
+    int acc0 = 0, acc1 = 0, acc2 = 0, acc3 = 0;  // four independent dp2a chains
     for (int j = 0; j < nsteps; j += U) {
         int4 x[U];
         uint32_t w[U];
@@ -1166,29 +1183,29 @@ __device__ __forceinline__ int64_t smem_dot16(const GArgs& a, const int4* rowv, 
         for (int u = 0; u < U; ++u) {
             const bool in = j + u < nsteps;
             x[u] = in ? rowv[32 * (j + u)] : make_int4(0, 0, 0, 0);
-            w[u] = in ? __ldg(qb + 8 * (j + u)) : 0u;
+            w[u] = in ? qb[8 * (j + u)] : 0u;
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const uint32_t byte = w[u] >> sh;
             const int s0 = signs4_bytes(byte & 15u), s1 = signs4_bytes((byte >> 4) & 15u);
-            acc = __dp2a_lo(x[u].x, s0, acc);
-            acc = __dp2a_hi(x[u].y, s0, acc);
-            acc = __dp2a_lo(x[u].z, s1, acc);
-            acc = __dp2a_hi(x[u].w, s1, acc);
+            acc0 = __dp2a_lo(x[u].x, s0, acc0);
+            acc1 = __dp2a_hi(x[u].y, s0, acc1);
+            acc2 = __dp2a_lo(x[u].z, s1, acc2);
+            acc3 = __dp2a_hi(x[u].w, s1, acc3);
         }
     }
-    return acc;
+    return (int64_t)acc0 + acc1 + acc2 + acc3;
 }
 
-__device__ __forceinline__ int64_t smem_dot32(const GArgs& a, const int4* rowv, int lane, int64_t r) {
-    const int nsteps = a.dim / 128;
+// the same for int32 rows: steps of 128 dims, 4 dims a lane
+__device__ __forceinline__ int64_t smem_dot32(const int4* rowv, const uint32_t* bits, int lane, int nsteps) {
     const int sh = (lane & 7) * 4;
-    const uint32_t* qb = a.bits + r * a.words + (lane >> 3);
+    const uint32_t* qb = bits + (lane >> 3);
     int64_t acc = 0;
     for (int j = 0; j < nsteps; ++j) {
         const int4 x = rowv[32 * j];
-        const uint32_t nib = __ldg(qb + 4 * j) >> sh;
+        const uint32_t nib = qb[4 * j] >> sh;
         acc += (int64_t)((nib & 1u) ? x.x : neg32(x.x)) + (int64_t)((nib & 2u) ? x.y : neg32(x.y)) +
                (int64_t)((nib & 4u) ? x.z : neg32(x.z)) + (int64_t)((nib & 8u) ? x.w : neg32(x.w));
     }
@@ -1208,78 +1225,185 @@ __device__ __forceinline__ int64_t first_node_at(const GArgs& a, int64_t x) {
     return lo;
 }
 
-__device__ void stream_phase(const GArgs& a, TcShared& sm, TcRun& run, uint8_t* ring) {
+// first n in [lo, hi) with node_off[n + 1] > y (hi if none): skips the nodes without pairs
+// before position y
+__device__ __forceinline__ int64_t first_node_after(const GArgs& a, int64_t lo, int64_t hi, int64_t y) {
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (a.node_off[mid + 1] > y)
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    return lo;
+}
+
+// `area` bytes of shared memory from `ring` on: the four rings' slots, then the consumers'
+// bit buffers
+__device__ void stream_phase(const GArgs& a, TcShared& sm, TcRun& run, uint8_t* ring, size_t area) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t total = a.off[a.nq];
     const int64_t pc = (total + gridDim.x - 1) / gridDim.x;
-    const int64_t n_lo = first_node_at(a, (int64_t)blockIdx.x * pc);
     const int64_t n_hi = blockIdx.x + 1 == gridDim.x ? a.n_nodes : first_node_at(a, (int64_t)(blockIdx.x + 1) * pc);
-    const uint32_t slot_bytes = (uint32_t)a.dim * (a.n32 > 0 ? 4u : 2u);
-    const int S = min(kRowSlots, (int)((size_t)(kTcStages * kTcStageBytes + kTcStageArea) / slot_bytes));
+    int64_t n_lo = first_node_at(a, (int64_t)blockIdx.x * pc);
+    // the range starts at its first node with pairs (CTA 0's would start at node 0, and every
+    // node of the ranks above the level has none)
+    n_lo = first_node_after(a, n_lo, n_hi, a.node_off[n_lo]);
+    const int qdim = a.dim / kQuarters;  // a multiple of 256
+    const uint32_t item_bytes = (uint32_t)qdim * (n_lo < a.n32 ? 4u : 2u);  // a slot holds any quarter of the range
+    const uint32_t qbits_bytes = (uint32_t)qdim / 8u;                       // a quarter of a read's bits
+    const size_t bits_area = (size_t)kRowConsumers * kBitsBufs * qbits_bytes;
+    // >= 3 for every dim <= 16384
+    const int S = min(kRowSlots, (int)((area - bits_area) / ((size_t)kQuarters * item_bytes)));
+    uint8_t* bits_sm = ring + (size_t)kQuarters * S * item_bytes;
+    const int64_t ord0 = run.row_ord;  // this phase's first row ordinal (every role's copy agrees)
     if (warp == 0) {
-        if (lane != 0) return;
+        // the warp walks the nodes (their offsets loaded 31 at a time, lane j holding
+        // node_off[nb + j]); lane 0 waits for the slots and issues the copies
         tc::fence_proxy_async();  // the ring's earlier generic-proxy writes come before the bulk copies
-        int64_t issued = 0;
-        for (int64_t n = n_lo; n < n_hi; ++n) {
-            if (a.node_off[n + 1] == a.node_off[n]) continue;
-            const int64_t i = run.row_ord++;
-            const int slot = (int)(i % S);
-            if (!tc::mbar_wait(&sm.row_empty[slot], (uint32_t)((i / S) & 1) ^ 1u, &sm.err, 15)) break;
-            const bool w16 = n >= a.n32;
-            const uint32_t bytes = (uint32_t)a.dim * (w16 ? 2u : 4u);
-            const void* src = w16 ? (const void*)(a.proto16 + (n - a.n32) * a.dim) : (const void*)(a.proto + n * a.dim);
-            tc::mbar_arrive_expect_tx(&sm.row_full[slot], bytes);
-            tc::bulk_load_1d(ring + (size_t)slot * slot_bytes, src, bytes, &sm.row_full[slot]);
-            ++issued;
-        }
-        // copies still landing when the consumers gave up early: let them finish (bounded)
-        for (int64_t k = 0; k < min(issued, (int64_t)S); ++k) {
-            const int64_t i = run.row_ord - 1 - k;
-            const long long c0 = clock64();
-            while (!tc::mbar_try_wait(tc::smem_u32(&sm.row_full[i % S]), (uint32_t)((i / S) & 1)) &&
-                   clock64() - c0 < tc::kWaitCycles) {
+        const uint64_t once = tc::make_policy_evict_first();
+        int64_t issued[kQuarters] = {0, 0, 0, 0};  // rows whose quarter q is on its way (lane 0)
+        bool ok = true;
+        int64_t i = run.row_ord;
+        for (int64_t nb = n_lo; ok && nb < n_hi; nb += 31) {
+            const int32_t offv = nb + lane <= a.n_nodes ? a.node_off[nb + lane] : 0;
+            const int cnt = (int)min((int64_t)31, n_hi - nb);
+            for (int j = 0; ok && j < cnt; ++j) {
+                const int32_t ps = __shfl_sync(0xffffffffu, offv, j), pe = __shfl_sync(0xffffffffu, offv, j + 1);
+                if (ps == pe) continue;
+                const int64_t n = nb + j;
+                const int slot = (int)(i % S);
+                const uint32_t parity = (uint32_t)((i / S) & 1);
+                ++i;
+                if (lane == 0) {
+                    const bool w16 = n >= a.n32;
+                    const uint32_t bytes = (uint32_t)qdim * (w16 ? 2u : 4u);
+                    const char* src = w16 ? reinterpret_cast<const char*>(a.proto16 + (n - a.n32) * a.dim)
+                                          : reinterpret_cast<const char*>(a.proto + n * a.dim);
+                    for (int q = 0; q < kQuarters; ++q) {
+                        const int b = q * kRowSlots + slot;
+                        if (!tc::mbar_wait(&sm.row_empty[b], parity ^ 1u, &sm.err, 15)) {
+                            ok = false;
+                            break;
+                        }
+                        tc::mbar_arrive_expect_tx(&sm.row_full[b], bytes);
+                        tc::bulk_load_1d_hint(ring + ((size_t)q * S + slot) * item_bytes, src + (size_t)q * bytes,
+                                              bytes, &sm.row_full[b], once);
+                        ++issued[q];
+                    }
+                }
+                ok = __shfl_sync(0xffffffffu, ok, 0);
             }
         }
+        run.row_ord = i;
+        // copies still landing when the consumers gave up early: let them finish (bounded)
+        if (lane == 0)
+            for (int q = 0; q < kQuarters; ++q)
+                for (int64_t k = ord0 + issued[q] - min(issued[q], (int64_t)S); k < ord0 + issued[q]; ++k) {
+                    const long long c0 = clock64();
+                    while (!tc::mbar_try_wait(tc::smem_u32(&sm.row_full[q * kRowSlots + (int)(k % S)]),
+                                              (uint32_t)((k / S) & 1)) &&
+                           clock64() - c0 < tc::kWaitCycles) {
+                    }
+                }
+        __syncwarp();
         return;
     }
-    // consumers: warp c takes the pairs at positions P0 + c, P0 + c + 12, ... of the CTA's range
-    const int c = warp - 1;
-    const int64_t P0 = a.node_off[n_lo];
-    int32_t my_pi = -1, my_node = 0;
-    int64_t my_r = 0, my_dot = 0;
-    int cnt = 0;
-    auto flush = [&]() {
-        if (my_pi >= 0)
-            a.pair_key[my_pi] = make_key(exact_score(my_dot, a.qn[my_r], a.pn[my_node], a.mode), (uint32_t)my_node);
-        my_pi = -1;
-    };
-    for (int64_t n = n_lo; n < n_hi; ++n) {
-        const int64_t ps = a.node_off[n], pe = a.node_off[n + 1];
-        if (ps == pe) continue;
-        const int64_t i = run.row_ord++;
-        const int slot = (int)(i % S);
-        if (!tc::mbar_wait(&sm.row_full[slot], (uint32_t)((i / S) & 1), &sm.err, 16)) break;
-        const int4* rowv = reinterpret_cast<const int4*>(ring + (size_t)slot * slot_bytes) + lane;
-        const bool w16 = n >= a.n32;
-        for (int64_t s = ps + ((c - (ps - P0) % kRowConsumers) + kRowConsumers) % kRowConsumers; s < pe;
-             s += kRowConsumers) {
-            const int32_t pi = a.sorted[s];
-            const int64_t r = a.pair_read[pi];
-            int64_t acc = w16 ? smem_dot16(a, rowv, lane, r) : smem_dot32(a, rowv, lane, r);
-            for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == (cnt & 31)) {
-                my_pi = pi;
-                my_node = (int32_t)n;
-                my_r = r;
-                my_dot = acc;
-            }
-            if ((cnt & 31) == 31) flush();
-            ++cnt;
+    // consumers: warp c = 4 g + q scores quarter q of group g's k-th pair, at position
+    // s_first + 3 k of the CTA's range
+    const int c = warp - 1, q = c % kQuarters, g = c / kQuarters;
+    const int64_t P0 = a.node_off[n_lo], P1 = a.node_off[n_hi];
+    const int64_t s_first = P0 + g;
+    const int64_t nk = P1 > s_first ? (P1 - s_first + kRowGroups - 1) / kRowGroups : 0;
+    uint8_t* wbits = bits_sm + (size_t)c * kBitsBufs * qbits_bytes;
+    int64_t* part = a.part + (size_t)q * a.pstride;
+    // lane j holds the pair index and read of the group's pair 32 b + j, for the current batch
+    // b and the next one
+    int64_t batch = 0;
+    int32_t pi_cur = -1, r_cur = 0, pi_nxt = -1, r_nxt = 0;
+    auto load_batch = [&](int64_t b, int32_t& pi, int32_t& r) {
+        const int64_t k = 32 * b + lane;
+        pi = -1;
+        r = 0;
+        if (k < nk) {
+            pi = a.sorted[s_first + kRowGroups * k];
+            r = a.pair_read[pi];
         }
-        __syncwarp();
-        if (lane == 0) tc::mbar_arrive(&sm.row_empty[slot]);
+    };
+    load_batch(0, pi_cur, r_cur);
+    load_batch(1, pi_nxt, r_nxt);
+    // quarter q of the bits of pair k (in the current or the next batch) into buffer
+    // k % kBitsBufs; one cp.async group per call, possibly empty, so the waits below count pairs
+    auto prefetch = [&](int64_t k) {
+        if (k < nk) {
+            // k is the same in every lane; the next batch's indices are only read once needed
+            const int64_t r = (k >> 5) == batch ? __shfl_sync(0xffffffffu, r_cur, (int)(k & 31))
+                                                : __shfl_sync(0xffffffffu, r_nxt, (int)(k & 31));
+            const char* src = reinterpret_cast<const char*>(a.bits + r * a.words) + (size_t)q * qbits_bytes;
+            uint8_t* dst = wbits + (size_t)(k % kBitsBufs) * qbits_bytes;
+            for (uint32_t o = 16u * lane; o < qbits_bytes; o += 512u) cp_async16(dst + o, src + o, 16);
+        }
+        cp_async_commit();
+    };
+    prefetch(0);
+    int64_t k = 0;
+    int64_t s = s_first;  // the group's next pair position
+    int64_t i = run.row_ord;
+    bool ok = true;
+    // the node offsets 31 nodes at a time (lane j holds node_off[nb + j]), the next batch's
+    // loaded while this one is walked
+    int32_t offn = n_lo + lane <= a.n_nodes ? a.node_off[n_lo + lane] : 0;
+    for (int64_t nb = n_lo; ok && nb < n_hi; nb += 31) {
+        const int32_t offv = offn;
+        offn = nb + 31 + lane <= a.n_nodes ? a.node_off[nb + 31 + lane] : 0;
+        const int cnt = (int)min((int64_t)31, n_hi - nb);
+        for (int j = 0; j < cnt; ++j) {
+            const int32_t ps = __shfl_sync(0xffffffffu, offv, j), pe = __shfl_sync(0xffffffffu, offv, j + 1);
+            if (ps == pe) continue;
+            const int64_t n = nb + j;
+            const int slot = (int)(i % S);
+            const int b = q * kRowSlots + slot;
+            if (!tc::mbar_wait(&sm.row_full[b], (uint32_t)((i / S) & 1), &sm.err, 16)) {
+                ok = false;
+                break;
+            }
+            ++i;
+            const int4* rowv = reinterpret_cast<const int4*>(ring + ((size_t)q * S + slot) * item_bytes) + lane;
+            const bool w16 = n >= a.n32;
+            for (; s < pe; s += kRowGroups, ++k) {
+                if (k > 0 && (k & 31) == 0) {  // a new batch: its indices move up
+                    ++batch;
+                    pi_cur = pi_nxt;
+                    r_cur = r_nxt;
+                    load_batch(batch + 1, pi_nxt, r_nxt);
+                }
+                prefetch(k + 1);
+                cp_async_wait<1>();  // this lane's copies of pair k have landed
+                __syncwarp();        // and every lane's
+                const uint32_t* qb = reinterpret_cast<const uint32_t*>(wbits + (size_t)(k % kBitsBufs) * qbits_bytes);
+                int64_t acc = w16 ? smem_dot16(rowv, qb, lane, qdim / 256) : smem_dot32(rowv, qb, lane, qdim / 128);
+                for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                if (lane == (int)(k & 31)) part[pi_cur] = acc;
+                __syncwarp();  // buffer k % kBitsBufs is refilled by the prefetch of pair k + 2
+            }
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&sm.row_empty[b]);
+        }
     }
-    flush();
+    run.row_ord = i;
+    cp_async_wait<0>();  // no copy may still be landing when the phase ends
+}
+
+// The keys of the pairs of reads [r0, r1) from a streamed level's partial dots (every thread of
+// the CTA, the pairs spread over its threads).
+__device__ void keys_from_parts(const GArgs& a, int64_t r0, int64_t r1) {
+    for (int64_t p = a.off[r0] + threadIdx.x; p < a.off[r1]; p += blockDim.x) {
+        int64_t dot = 0;
+#pragma unroll
+        for (int q = 0; q < kQuarters; ++q) dot += a.part[(size_t)q * a.pstride + p];
+        const int32_t node = a.pair_node[p];
+        a.pair_key[p] = make_key(exact_score(dot, a.qn[a.pair_read[p]], a.pn[node], a.mode), (uint32_t)node);
+    }
 }
 
 __global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs a, const TcItems t, const OneArgs o) {
@@ -1402,14 +1526,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs 
             // F: the pairs scored on the CUDA cores: the leaf level's rows streamed through shared
             // memory, other levels (every level without the tensor cores) one warp per pair
             if (o.use_tc)
-                stream_phase(a, sm, run, ring);
+                stream_phase(a, sm, run, ring, kOneSmem - 1024);
             else if (rows16)
                 score_pairs<true>(a, gtid >> 5, gstride >> 5);
             else
                 score_pairs<false>(a, gtid >> 5, gstride >> 5);
         }
         if (!(ok = grid_barrier(o, sm, &ok_s, &n_ts))) break;
-        // H: the beams of this CTA's reads
+        // H: the beams of this CTA's reads (after a streamed level, their pairs' keys first)
+        if (o.use_tc && !tcl && r0 < r1) {
+            keys_from_parts(a, r0, r1);
+            __syncthreads();
+        }
         for (int64_t r = r0 + tid; r < r1; r += nt) select_one(a, L, r);
         __syncthreads();
     }
@@ -1433,9 +1561,9 @@ bool one_launch_fits(hdc_context* ctx) {
     if (ctx->beam_one_fit < 0) {
         int per_sm = 0;
         cudaError_t e = cudaFuncSetAttribute(descent_one_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kTcSmem);
+                                             (int)kOneSmem);
         if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, descent_one_kernel, kTcThreads, kTcSmem);
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, descent_one_kernel, kTcThreads, kOneSmem);
         int coop = 0;
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device);
         cudaGetLastError();
@@ -1511,6 +1639,7 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
     t.status = ctx->d_status;
     const int64_t cchunks = (std::max<int64_t>(std::max(maxc, n_roots), 1) + kTcC - 1) / kTcC;
     const int64_t max_items = (nq * beam + 2) * cchunks + ((nq + kTcE - 1) / kTcE) * ((n_roots + kTcC - 1) / kTcC);
+    const bool one = one_launch_fits(ctx);
     // carve the workspace: once from address 0 to measure it, then from the allocation
     auto carve_all = [&](uint8_t* base) {
         uint8_t* cur = base;
@@ -1530,6 +1659,10 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
         a.pair_slot = carve<int32_t>(cur, P);
         a.sorted = carve<int32_t>(cur, P);
         a.pair_key = carve<uint64_t>(cur, P);
+        if (one && use_tc) {
+            a.part = carve<int64_t>(cur, (int64_t)kQuarters * P);
+            a.pstride = P;
+        }
         d_sums = carve<int32_t>(cur, sums);
         d_maxc_dev = carve<int32_t>(cur, 1);
         one_state = carve<uint32_t>(cur, 4);  // barrier count, barrier generation, abort, child count
@@ -1559,7 +1692,7 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
 
     const unsigned rb = (unsigned)((nq + 255) / 256);
     if (!d_qbits) pack_bits_kernel<<<(unsigned)((nq * a.words + 255) / 256), 256, 0, stream>>>(d_q, nq, a.dim, bits);
-    if (one_launch_fits(ctx)) {
+    if (one) {
         // every level in one cooperative launch (descent_one_kernel)
         OneArgs o{};
         o.bar_count = one_state;
@@ -1586,7 +1719,7 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
         void* args[] = {(void*)&a, (void*)&t, (void*)&o};
         if (e == cudaSuccess)
             e = cudaLaunchCooperativeKernel((const void*)descent_one_kernel, dim3((unsigned)ctx->num_sms),
-                                            dim3(kTcThreads), args, kTcSmem, stream);
+                                            dim3(kTcThreads), args, kOneSmem, stream);
         cudaFreeAsync(ws, stream);
         return e == cudaSuccess ? HDC_OK : cuda_fail(e, "beam: one-launch descent");
     }

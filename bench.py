@@ -991,12 +991,14 @@ def run_aux(args):
     hbm = pk["hbm_gbs"]
     dev = torch.device("cuda", 0)
     out = {}
-    # FASTA ingest: 3,000,000 records of 250 bp in 60-column lines
-    data = fasta_bytes(3000000, 250)
+    scale = args.aux_scale
+    # FASTA ingest: 3,000,000 records of 250 bp in 60-column lines (times the scale)
+    n_fa = max(40000, int(3000000 * scale))
+    data = fasta_bytes(n_fa, 250)
     d = torch.from_numpy(data).to(dev)
     ctx = H.Context(10240, 10, 250, 10)
-    ms = _event_ms(lambda: ctx.fasta_parse(d, 3000001))
-    seq_bytes, so, sl, _, _, n_rec = ctx.fasta_parse(d, 3000001)
+    ms = _event_ms(lambda: ctx.fasta_parse(d, n_fa + 1))
+    seq_bytes, so, sl, _, _, n_rec = ctx.fasta_parse(d, n_fa + 1)
     out["fasta_parse"] = {"input_bytes": int(d.numel()), "records": int(n_rec), "ms": ms,
                           "input_gb_per_s": d.numel() / (ms / 1e3) / 1e9,
                           "note": "several byte-parallel passes over ~61 bytes of workspace per input byte"}
@@ -1009,7 +1011,7 @@ def run_aux(args):
                         "frac_of_hbm": moved / (ms / 1e3) / 1e9 / hbm}
     # read encode, c3 shape (38,912 reads of 250 bp, D = 10,240, k = 10, +1/-1 fp16 rows), from
     # ASCII and from packed words
-    B = 38912
+    B = min(38912, n_fa)
     offs, lens = so[:B], sl[:B]
     q = torch.empty((B, 10240), dtype=torch.float16, device=dev)
     t_ascii = _event_ms(lambda: ctx.encode_segments(seq_bytes, offs, lens, q, H.OUT_BIPOLAR_F16, 250))
@@ -1053,9 +1055,64 @@ def run_aux(args):
                          "row_gb_per_s": row_bytes / (ms / 1e3) / 1e9,
                          "unique_row_bytes": int(rows.numel() * 2),
                          "note": "row bytes of every pair (rows shared by pairs come from L2)"}
+    del rows, qv
+    # propagate-children's greedy representatives and identify's descent on a tree of the C1
+    # shape: 2,000 leaves of 1,400-1,600 bp (times the scale), D = 8,192, k = 8
+    n_leaves = max(200, int(2000 * scale))
+    tree = H.synth_tree(23, n_leaves)
+    d_tree = torch.from_numpy(tree.buf).to(dev)
+    hv = torch.empty((n_leaves, 8192), dtype=torch.int16, device=dev)
+    sctx.encode_segments(d_tree, torch.from_numpy(tree.off).to(dev), torch.from_numpy(tree.len).to(dev), hv,
+                         H.OUT_I16, tree.max_len())
+    hn = sctx.norms(hv)
+    b, base, counts, cptr, cidx = H.synth_tree_csr(n_leaves)
+    groups = []  # every internal node with its descendant leaves, in order
+    for r in range(1, 6):
+        span = b ** (6 - r)
+        groups += [list(range(j * span, min(n_leaves, (j + 1) * span))) for j in range(counts[r - 1])]
+    cand_ptr = np.zeros(len(groups) + 1, np.int64)
+    cand_ptr[1:] = np.cumsum([len(x) for x in groups])
+    cand_idx = np.array([x for grp in groups for x in grp], np.int32)
+    t = lambda a: torch.from_numpy(a).to(dev)
+    gp, gi, rp, ri = t(cand_ptr), t(cand_idx), t(np.zeros(len(groups) + 1, np.int64)), t(np.zeros(1, np.int32))
+    ms = _event_ms(lambda: sctx.propagate_greedy(hv, hn, gp, gi, rp, ri, 0.75))
+    sel, _ = sctx.propagate_greedy(hv, hn, gp, gi, rp, ri, 0.75)
+    out["propagate_greedy"] = {"parents": len(groups), "candidates": int(cand_idx.size),
+                               "selected": int(sel.sum().item()), "ms": ms,
+                               "bound": "latency: each parent's candidates are decided in order"}
+    # identify: a leaf's similarity rows are its windows (135 of 150 bp, step 10); an internal
+    # node's are the first 20 windows of its first descendant leaf
+    row_off, node_rows = [], [0]
+    for node in range(int(base[-1])):
+        rank = int(np.searchsorted(base, node, side="right")) - 1
+        leaf = (node - int(base[rank])) * b ** (5 - rank)
+        o, n = int(tree.off[leaf]), int(tree.len[leaf])
+        xs = list(range(0, n - 150, 10))
+        if rank < 5:
+            xs = xs[:20]
+        row_off += [o + x for x in xs]
+        node_rows.append(len(row_off))
+    rows = torch.empty((len(row_off), 8192), dtype=torch.int16, device=dev)
+    sctx.encode_segments(d_tree, torch.tensor(row_off, dtype=torch.int64, device=dev),
+                         torch.full((len(row_off),), 150, dtype=torch.int32, device=dev), rows, H.OUT_I16, 150)
+    rn = sctx.norms(rows)
+    reads = H.synth_reads(24, tree, 4096, 150, subst=0.01)
+    qv = torch.empty((4096, 8192), dtype=torch.int16, device=dev)
+    sctx.encode_segments(torch.from_numpy(reads.buf).to(dev), torch.from_numpy(reads.off).to(dev),
+                         torch.from_numpy(reads.len).to(dev), qv, H.OUT_I16, 150)
+    qn = sctx.norms(qv)
+    d_nr, d_cp, d_ci = t(np.array(node_rows, np.int64)), t(cptr), t(cidx)
+    d_roots = torch.arange(counts[0], dtype=torch.int32, device=dev)
+    ms = _event_ms(lambda: sctx.identify(qv, qn, rows, rn, d_nr, d_cp, d_ci, d_roots, 6, 5, 0.0))
+    path, _, depth, _ = sctx.identify(qv, qn, rows, rn, d_nr, d_cp, d_ci, d_roots, 6, 5, 0.0)
+    out["identify"] = {"reads": 4096, "nodes": int(base[-1]), "similarity_rows": len(row_off),
+                       "row_bytes": len(row_off) * 8192 * 2, "ms": ms, "reads_per_s": 4096 / (ms / 1e3),
+                       "mean_depth": float(depth.float().mean().item()),
+                       "bound": "gathers of each candidate node's rows (one CTA per read)"}
     line = {"metric": "auxiliary kernels (ms, GB/s)", "unit": "ms", "n_gpus": 1, "higher_is_better": False,
             "data": "synthetic", "config": {"workload": "aux: FASTA ingest, 2-bit packing, read encode, "
-                                                         "windowed similarity"},
+                                                         "windowed similarity, propagate greedy, identify",
+                                            "scale": scale},
             "peak_hbm_gbs": hbm, "peak_source": "%s (MEASURED_PEAKS.json)" % src, "kernels": out}
     print(json.dumps(line), flush=True)
 
@@ -1084,6 +1141,8 @@ def main():
                     help="descent: 1 reads grouped by candidate node, 0 one warp per read (-1: default)")
     ap.add_argument("--beam-one", type=int, default=-1,
                     help="descent: 1 every level in one launch, 0 kernels per level (-1: default, one launch)")
+    ap.add_argument("--aux-scale", type=float, default=1.0,
+                    help="aux: sizes of the FASTA and tree cases times this (small profiling cases)")
     ap.add_argument("--proto-int32", action="store_true",
                     help="descent: every prototype row int32 (default: int16 rows from the first node whose rows fit)")
     args = ap.parse_args()
