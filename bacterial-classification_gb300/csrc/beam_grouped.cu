@@ -1167,11 +1167,11 @@ __device__ int32_t cta_prefix(const int32_t* blk, int b, int32_t* sh) {
 // partial dots are summed, and the FP64 scores computed, by the CTA that owns the read, after
 // the next grid barrier (keys_from_parts).  CTA b owns the nodes whose first pair falls in its
 // share of the pair list.
-constexpr int kBitsBufs = 2;  // per consumer warp: the current pair's bits and the next one's
+constexpr int kBitsBufs = 4;  // per consumer warp: the bits of the pairs being scored and of the next ones
 
 // Lane l's share of a quarter of int16 row dims: steps j of 256 dims, 8 dims a lane (one
 // 16-byte word of the row, one byte of the read's bits)
-__device__ __forceinline__ int64_t smem_dot16(const int4* rowv, const uint32_t* bits, int lane, int nsteps) {
+__device__ __forceinline__ int smem_dot16(const int4* rowv, const uint32_t* bits, int lane, int nsteps) {
     constexpr int U = 8;
     const int sh = (lane & 3) * 8;
     const uint32_t* qb = bits + (lane >> 2);
@@ -1195,7 +1195,43 @@ __device__ __forceinline__ int64_t smem_dot16(const int4* rowv, const uint32_t* 
             acc3 = __dp2a_hi(x[u].w, s1, acc3);
         }
     }
-    return (int64_t)acc0 + acc1 + acc2 + acc3;
+    return acc0 + acc1 + acc2 + acc3;  // |sum| <= 4,096 x 32,767 a lane at D = 16,384: int32
+}
+
+// The same for two pairs of one row (one shared-memory read of the row for both).
+__device__ __forceinline__ int2 smem_dot16x2(const int4* rowv, const uint32_t* bits0, const uint32_t* bits1, int lane,
+                                             int nsteps) {
+    constexpr int U = 8;
+    const int sh = (lane & 3) * 8;
+    const uint32_t* qb0 = bits0 + (lane >> 2);
+    const uint32_t* qb1 = bits1 + (lane >> 2);
+    int a0 = 0, a1 = 0, c0 = 0, c1 = 0;
+    for (int j = 0; j < nsteps; j += U) {
+        int4 x[U];
+        uint32_t w[U], v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const bool in = j + u < nsteps;
+            x[u] = in ? rowv[32 * (j + u)] : make_int4(0, 0, 0, 0);
+            w[u] = in ? qb0[8 * (j + u)] : 0u;
+            v[u] = in ? qb1[8 * (j + u)] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint32_t bw = w[u] >> sh, bv = v[u] >> sh;
+            const int s0 = signs4_bytes(bw & 15u), s1 = signs4_bytes((bw >> 4) & 15u);
+            const int t0 = signs4_bytes(bv & 15u), t1 = signs4_bytes((bv >> 4) & 15u);
+            a0 = __dp2a_lo(x[u].x, s0, a0);
+            a1 = __dp2a_hi(x[u].y, s0, a1);
+            a0 = __dp2a_lo(x[u].z, s1, a0);
+            a1 = __dp2a_hi(x[u].w, s1, a1);
+            c0 = __dp2a_lo(x[u].x, t0, c0);
+            c1 = __dp2a_hi(x[u].y, t0, c1);
+            c0 = __dp2a_lo(x[u].z, t1, c0);
+            c1 = __dp2a_hi(x[u].w, t1, c1);
+        }
+    }
+    return make_int2(a0 + a1, c0 + c1);
 }
 
 // the same for int32 rows: steps of 128 dims, 4 dims a lane
@@ -1265,6 +1301,8 @@ __device__ void stream_phase(const GArgs& a, TcShared& sm, TcRun& run, uint8_t* 
         int64_t issued[kQuarters] = {0, 0, 0, 0};  // rows whose quarter q is on its way (lane 0)
         bool ok = true;
         int64_t i = run.row_ord;
+        int slot = (int)(i % S);  // i % S and (i / S) & 1, kept incrementally
+        uint32_t parity = (uint32_t)((i / S) & 1);
         for (int64_t nb = n_lo; ok && nb < n_hi; nb += 31) {
             const int32_t offv = nb + lane <= a.n_nodes ? a.node_off[nb + lane] : 0;
             const int cnt = (int)min((int64_t)31, n_hi - nb);
@@ -1272,9 +1310,6 @@ __device__ void stream_phase(const GArgs& a, TcShared& sm, TcRun& run, uint8_t* 
                 const int32_t ps = __shfl_sync(0xffffffffu, offv, j), pe = __shfl_sync(0xffffffffu, offv, j + 1);
                 if (ps == pe) continue;
                 const int64_t n = nb + j;
-                const int slot = (int)(i % S);
-                const uint32_t parity = (uint32_t)((i / S) & 1);
-                ++i;
                 if (lane == 0) {
                     const bool w16 = n >= a.n32;
                     const uint32_t bytes = (uint32_t)qdim * (w16 ? 2u : 4u);
@@ -1293,6 +1328,11 @@ __device__ void stream_phase(const GArgs& a, TcShared& sm, TcRun& run, uint8_t* 
                     }
                 }
                 ok = __shfl_sync(0xffffffffu, ok, 0);
+                ++i;
+                if (++slot == S) {
+                    slot = 0;
+                    parity ^= 1u;
+                }
             }
         }
         run.row_ord = i;
@@ -1309,12 +1349,16 @@ __device__ void stream_phase(const GArgs& a, TcShared& sm, TcRun& run, uint8_t* 
         __syncwarp();
         return;
     }
-    // consumers: warp c = 4 g + q scores quarter q of group g's k-th pair, at position
-    // s_first + 3 k of the CTA's range
+    // consumers: warp c = 4 g + q scores quarter q of group g's pairs.  The CTA's pair list is cut
+    // into chunks of two consecutive pairs, chunk t going to group t % 3, so group g's k-th pair
+    // is at position P0 + 2 g + 6 (k / 2) + k % 2; the two pairs of a chunk inside one node are
+    // scored together from one read of the row.
     const int c = warp - 1, q = c % kQuarters, g = c / kQuarters;
     const int64_t P0 = a.node_off[n_lo], P1 = a.node_off[n_hi];
-    const int64_t s_first = P0 + g;
-    const int64_t nk = P1 > s_first ? (P1 - s_first + kRowGroups - 1) / kRowGroups : 0;
+    const int64_t g0 = P0 + 2 * g;
+    const int64_t span = P1 - g0;
+    const int64_t nk = span > 0 ? 2 * (span / 6) + min((int64_t)2, span % 6) : 0;
+    auto pos = [&](int64_t k) { return g0 + 6 * (k >> 1) + (k & 1); };
     uint8_t* wbits = bits_sm + (size_t)c * kBitsBufs * qbits_bytes;
     int64_t* part = a.part + (size_t)q * a.pstride;
     // lane j holds the pair index and read of the group's pair 32 b + j, for the current batch
@@ -1326,29 +1370,37 @@ __device__ void stream_phase(const GArgs& a, TcShared& sm, TcRun& run, uint8_t* 
         pi = -1;
         r = 0;
         if (k < nk) {
-            pi = a.sorted[s_first + kRowGroups * k];
+            pi = a.sorted[pos(k)];
             r = a.pair_read[pi];
         }
     };
     load_batch(0, pi_cur, r_cur);
     load_batch(1, pi_nxt, r_nxt);
     // quarter q of the bits of pair k (in the current or the next batch) into buffer
-    // k % kBitsBufs; one cp.async group per call, possibly empty, so the waits below count pairs
-    auto prefetch = [&](int64_t k) {
-        if (k < nk) {
-            // k is the same in every lane; the next batch's indices are only read once needed
-            const int64_t r = (k >> 5) == batch ? __shfl_sync(0xffffffffu, r_cur, (int)(k & 31))
-                                                : __shfl_sync(0xffffffffu, r_nxt, (int)(k & 31));
-            const char* src = reinterpret_cast<const char*>(a.bits + r * a.words) + (size_t)q * qbits_bytes;
-            uint8_t* dst = wbits + (size_t)(k % kBitsBufs) * qbits_bytes;
-            for (uint32_t o = 16u * lane; o < qbits_bytes; o += 512u) cp_async16(dst + o, src + o, 16);
+    // k % kBitsBufs; one cp.async group per pair, possibly empty, so the waits below count pairs
+    int64_t issued = 0;
+    auto prefetch_to = [&](int64_t last) {
+        for (; issued <= last; ++issued) {
+            const int64_t k = issued;
+            if (k < nk) {
+                // k is the same in every lane; the next batch's indices are only read once needed
+                const int64_t r = (k >> 5) == batch ? __shfl_sync(0xffffffffu, r_cur, (int)(k & 31))
+                                                    : __shfl_sync(0xffffffffu, r_nxt, (int)(k & 31));
+                const char* src = reinterpret_cast<const char*>(a.bits + r * a.words) + (size_t)q * qbits_bytes;
+                uint8_t* dst = wbits + (size_t)(k % kBitsBufs) * qbits_bytes;
+                for (uint32_t o = 16u * lane; o < qbits_bytes; o += 512u) cp_async16(dst + o, src + o, 16);
+            }
+            cp_async_commit();
         }
-        cp_async_commit();
     };
-    prefetch(0);
+    auto qbits = [&](int64_t k) {
+        return reinterpret_cast<const uint32_t*>(wbits + (size_t)(k % kBitsBufs) * qbits_bytes);
+    };
     int64_t k = 0;
-    int64_t s = s_first;  // the group's next pair position
+    int64_t s = nk > 0 ? pos(0) : P1;  // the group's next pair position
     int64_t i = run.row_ord;
+    int slot = (int)(i % S);  // i % S and (i / S) & 1, kept incrementally
+    uint32_t parity = (uint32_t)((i / S) & 1);
     bool ok = true;
     // the node offsets 31 nodes at a time (lane j holds node_off[nb + j]), the next batch's
     // loaded while this one is walked
@@ -1361,33 +1413,55 @@ __device__ void stream_phase(const GArgs& a, TcShared& sm, TcRun& run, uint8_t* 
             const int32_t ps = __shfl_sync(0xffffffffu, offv, j), pe = __shfl_sync(0xffffffffu, offv, j + 1);
             if (ps == pe) continue;
             const int64_t n = nb + j;
-            const int slot = (int)(i % S);
             const int b = q * kRowSlots + slot;
-            if (!tc::mbar_wait(&sm.row_full[b], (uint32_t)((i / S) & 1), &sm.err, 16)) {
+            if (!tc::mbar_wait(&sm.row_full[b], parity, &sm.err, 16)) {
                 ok = false;
                 break;
             }
             ++i;
             const int4* rowv = reinterpret_cast<const int4*>(ring + ((size_t)q * S + slot) * item_bytes) + lane;
             const bool w16 = n >= a.n32;
-            for (; s < pe; s += kRowGroups, ++k) {
-                if (k > 0 && (k & 31) == 0) {  // a new batch: its indices move up
+            while (s < pe) {
+                while ((k >> 5) > batch) {  // a new batch: its indices move up
                     ++batch;
                     pi_cur = pi_nxt;
                     r_cur = r_nxt;
                     load_batch(batch + 1, pi_nxt, r_nxt);
                 }
-                prefetch(k + 1);
-                cp_async_wait<1>();  // this lane's copies of pair k have landed
-                __syncwarp();        // and every lane's
-                const uint32_t* qb = reinterpret_cast<const uint32_t*>(wbits + (size_t)(k % kBitsBufs) * qbits_bytes);
-                int64_t acc = w16 ? smem_dot16(rowv, qb, lane, qdim / 256) : smem_dot32(rowv, qb, lane, qdim / 128);
-                for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-                if (lane == (int)(k & 31)) part[pi_cur] = acc;
-                __syncwarp();  // buffer k % kBitsBufs is refilled by the prefetch of pair k + 2
+                const int u = w16 && (k & 1) == 0 && s + 1 < pe ? 2 : 1;  // both pairs of the chunk in this node
+                prefetch_to(k + u + 1);  // the bits of the next pairs are on their way while these are scored
+                cp_async_wait<2>();      // this lane's copies of pairs k .. k + u - 1 have landed
+                __syncwarp();            // and every lane's
+                if (u == 2) {  // quarters of an int16 row: |dot| <= 4,096 x 32,767 each, summed in int32
+                    int2 d = smem_dot16x2(rowv, qbits(k), qbits(k + 1), lane, qdim / 256);
+                    for (int o = 16; o; o >>= 1) {
+                        d.x += __shfl_xor_sync(0xffffffffu, d.x, o);
+                        d.y += __shfl_xor_sync(0xffffffffu, d.y, o);
+                    }
+                    if (lane == (int)(k & 31)) part[pi_cur] = d.x;
+                    if (lane == (int)((k + 1) & 31)) part[pi_cur] = d.y;
+                } else {
+                    int64_t acc;
+                    if (w16) {
+                        int a32 = smem_dot16(rowv, qbits(k), lane, qdim / 256);
+                        for (int o = 16; o; o >>= 1) a32 += __shfl_xor_sync(0xffffffffu, a32, o);
+                        acc = a32;
+                    } else {
+                        acc = smem_dot32(rowv, qbits(k), lane, qdim / 128);
+                        for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                    }
+                    if (lane == (int)(k & 31)) part[pi_cur] = acc;
+                }
+                __syncwarp();  // these buffers are refilled by the prefetches of the next pairs
+                k += u;
+                s = k < nk ? pos(k) : P1;
             }
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&sm.row_empty[b]);
+            if (++slot == S) {
+                slot = 0;
+                parity ^= 1u;
+            }
         }
     }
     run.row_ord = i;

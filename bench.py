@@ -1103,8 +1103,9 @@ def run_aux(args):
     qn = sctx.norms(qv)
     d_nr, d_cp, d_ci = t(np.array(node_rows, np.int64)), t(cptr), t(cidx)
     d_roots = torch.arange(counts[0], dtype=torch.int32, device=dev)
-    ms = _event_ms(lambda: sctx.identify(qv, qn, rows, rn, d_nr, d_cp, d_ci, d_roots, 6, 5, 0.0))
-    path, _, depth, _ = sctx.identify(qv, qn, rows, rn, d_nr, d_cp, d_ci, d_roots, 6, 5, 0.0)
+    # threshold -2 (below every NORM score): every read descends all six ranks
+    ms = _event_ms(lambda: sctx.identify(qv, qn, rows, rn, d_nr, d_cp, d_ci, d_roots, 6, 5, -2.0))
+    path, _, depth, _ = sctx.identify(qv, qn, rows, rn, d_nr, d_cp, d_ci, d_roots, 6, 5, -2.0)
     out["identify"] = {"reads": 4096, "nodes": int(base[-1]), "similarity_rows": len(row_off),
                        "row_bytes": len(row_off) * 8192 * 2, "ms": ms, "reads_per_s": 4096 / (ms / 1e3),
                        "mean_depth": float(depth.float().mean().item()),
