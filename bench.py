@@ -220,6 +220,8 @@ class Form:
                     torch.empty((B, K), dtype=torch.float64, device=dev),
                     torch.empty((B, K), dtype=torch.int64, device=dev))
         self.launches = 3 if cfg["bipolar"] else 4  # encode, [norms], search, merge
+        # the reference's NORM scale by default; --score-mode dot/cos for kernel studies
+        self.mode = {"norm": H.SCORE_NORM, "cos": H.SCORE_COS, "dot": H.SCORE_DOT}[cfg.get("score_mode", "norm")]
 
     def run(self, buf, off, ln, ev=None, stream=None):
         H, ctx = self.H, self.ctx
@@ -228,11 +230,11 @@ class Form:
         if ev is not None:
             ev[0].record(stream)
         if self.name == "tc":
-            ctx.search_tc(self.db, self.q, qn, 1, self.K, H.SCORE_NORM, work=self.work, out=self.out)
+            ctx.search_tc(self.db, self.q, qn, 1, self.K, self.mode, work=self.work, out=self.out)
             # encode, [norms], then the search kernels and merges the library reports (one or two parts)
             self.launches = (1 if self.cfg["bipolar"] else 2) + ctx.tc_last_shape()[4]
         else:
-            ctx.search_plain(self.q, qn, self.maxq, self.refs, self.rn, self.maxr, self.K, H.SCORE_NORM,
+            ctx.search_plain(self.q, qn, self.maxq, self.refs, self.rn, self.maxr, self.K, self.mode,
                              work=self.work, out=self.out)
         if ev is not None:
             ev[1].record(stream)
@@ -1142,6 +1144,8 @@ def main():
                     help="descent: 1 reads grouped by candidate node, 0 one warp per read (-1: default)")
     ap.add_argument("--beam-one", type=int, default=-1,
                     help="descent: 1 every level in one launch, 0 kernels per level (-1: default, one launch)")
+    ap.add_argument("--score-mode", default="norm", choices=["norm", "cos", "dot"],
+                    help="score of the top-k search (default the reference's NORM scale; the CPU legs need it)")
     ap.add_argument("--aux-scale", type=float, default=1.0,
                     help="aux: sizes of the FASTA and tree cases times this (small profiling cases)")
     ap.add_argument("--proto-int32", action="store_true",
@@ -1161,6 +1165,10 @@ def main():
         cfg["n_leaves"] = args.refs
     if args.topk:
         cfg["topk"] = args.topk
+    if args.score_mode != "norm":
+        if not args.no_cpu_baseline or args.impl == "reference":
+            raise SystemExit("--score-mode other than norm needs --no-cpu-baseline (the oracle legs rank by NORM)")
+        cfg["score_mode"] = args.score_mode
     if cfg.get("sigma"):
         reads_desc = "log-normal reads (median %d bp, sigma %.1f, %d-%d bp, %d%% with %d%% sub:ins:del 3:1:1)" % (
             cfg["read_len"], cfg["sigma"], cfg["min_read"], cfg["max_read"], 100 * cfg["mixed_frac"],
