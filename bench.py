@@ -4,11 +4,14 @@ A step is one batch of synthetic reads pushed through the hot path with the
 reference database resident in HBM: encode every read (kernel a), then
 exact cosine top-k against every reference (kernel b).  Prints one JSON line.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--config c2|c3]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config c1|c2|c3|c4|c5|aux]
                     [--form plain|tc] [--batch B] [--impl ours|reference]
 
 Workloads (seeded synthetic data standing in for real 16S data, none of
 which is available here):
+  c1  the reference's CPU-runnable case: 2,000 leaf references, D=8192, k=8, the
+      10,000 reads of 150 bp (1% substitutions) as one step, top-5; the result is
+      compared with the compiled reference's own answers for the same workload
   c2  plain GPU drop-in at scale: 50,000 leaf references of a 6-rank tree,
       D=8192, k=8, reads of 150 bp with 1% substitutions, top-5, NORM score
   c3  precision form: 200,000 leaf references, each the bundle of 8 noisy
@@ -41,6 +44,10 @@ for _p in (ROOT, PKG):
 import numpy as np  # noqa: E402
 
 CONFIGS = {
+    # the reference's CPU-runnable case: 2,000 leaves, 10,000 reads of 150 bp a step (the whole workload),
+    # checked against the compiled reference's own top-5 (tests/golden/c1_known_answer.json)
+    "c1": dict(n_leaves=2000, dim=8192, kmer=8, read_len=150, subst=0.01, topk=5, copies=0, bipolar=False,
+               tree_seed=1, read_seed=101, copy_seed=0, batch=10000, known_answer="c1_known_answer.json"),
     "c2": dict(n_leaves=50000, dim=8192, kmer=8, read_len=150, subst=0.01, topk=5, copies=0, bipolar=False,
                tree_seed=2, read_seed=102, copy_seed=0),
     "c3": dict(n_leaves=200000, dim=10240, kmer=10, read_len=250, subst=0.01, topk=5, copies=8, bipolar=True,
@@ -171,6 +178,21 @@ def build_database(H, ctx, cfg, dev):
     torch.cuda.synchronize()
     log("database: %d references x %d dims built in %.1f s" % (nr, dim, time.time() - t0))
     return tree, refs, rn, int(maxr.item())
+
+
+def known_answer(cfg, idx, score):
+    """The batch's top-k indices and float scores against the compiled reference's answers for the same
+    workload (sha256 of int32 / float32 little-endian arrays, as tests/golden/make_c1_golden.py stores them)."""
+    import hashlib
+    gold = json.load(open(os.path.join(ROOT, "tests", "golden", cfg["known_answer"])))
+    h = lambda a: hashlib.sha256(a.tobytes()).hexdigest()
+    n = gold["workload"]["n_reads"]
+    if idx.shape[0] != n:
+        return {"identical": None, "note": "the known answers cover exactly %d reads" % n}
+    i_ok = h(np.ascontiguousarray(idx, "<i4")) == gold["idx_sha256"]
+    s_ok = h(np.ascontiguousarray(score, "<f4")) == gold["score_sha256"]
+    return {"indices_identical": bool(i_ok), "float_scores_identical": bool(s_ok), "identical": bool(i_ok and s_ok),
+            "source": gold["source"]}
 
 
 def make_reads(H, tree, cfg, n, seed):
@@ -359,6 +381,9 @@ def run_ours(args, cfg):
     res["top1_accuracy"] = float((form.out[1][:B, 0].cpu().numpy() == reads.label[:B]).mean())
     res["gpu_first"] = tuple(x[:1024].cpu().numpy() for x in form.out)  # for the oracle's parity sample
     res["reads"] = reads
+    if cfg.get("known_answer"):
+        res["known_answer"] = {"form": form.name, "reads": B}
+        res["known_answer"].update(known_answer(cfg, form.out[1][:B].cpu().numpy(), form.out[0][:B].cpu().numpy()))
 
     # the plain drop-in on the same workload, for the tensor-core speed-up
     if args.form == "tc" and not args.no_plain:
@@ -384,6 +409,8 @@ def run_ours(args, cfg):
         tcf.run(d_buf, *batches[0])
         form.run(d_buf, *batches[0])
         torch.cuda.synchronize()
+        if cfg.get("known_answer"):
+            res["tc_known_answer"] = known_answer(cfg, tcf.out[1][:B].cpu().numpy(), tcf.out[0][:B].cpu().numpy())
         res["tc_form"] = dict(value=B / (tms / 1e3), ms=tms, search_ms=tsearch, limbs=tcf.db.limbs,
                               limb_bits=tcf.db.limb_bits,
                               labels_identical=bool(torch.equal(tcf.out[1], form.out[1])),
@@ -1160,7 +1187,7 @@ def main():
         return
     cfg = dict(CONFIGS[args.config])
     if not args.form:
-        args.form = {"c2": "plain", "c3": "tc", "c4": "pipe", "c5": "descent"}[args.config]
+        args.form = {"c1": "plain", "c2": "plain", "c3": "tc", "c4": "pipe", "c5": "descent"}[args.config]
     if args.refs:
         cfg["n_leaves"] = args.refs
     if args.topk:
@@ -1220,6 +1247,8 @@ def main():
         return
 
     import torch
+    if args.batch <= 0 and cfg.get("batch"):
+        args.batch = cfg["batch"]
     if args.batch <= 0:
         sms = torch.cuda.get_device_properties(0).multi_processor_count
         args.batch = 2 * sms * 128
@@ -1269,6 +1298,8 @@ def main():
     }
     if "top1_accuracy" in r:
         line["config"]["top1_accuracy"] = r["top1_accuracy"]  # top hit = the read's source leaf
+    if "known_answer" in r:
+        line["known_answer"] = r["known_answer"]
     if "tuned" in r:
         line["config"]["autotuned_schedule"] = r["tuned"]
         line["config"]["mean_read_len"] = r["mean_len"]
@@ -1284,6 +1315,8 @@ def main():
                            "scores_identical": t["scores_identical"],
                            "note": "the same count-valued reads as fp16 queries on the tensor cores, the "
                                    "database's limbs sized for the largest count (exact)"}
+        if "tc_known_answer" in r:
+            line["tc_form"]["known_answer"] = r["tc_known_answer"]
     if not args.no_cpu_baseline:
         v, threads, done, parity = cpu_baseline(cfg, r["refs_host"], r["reads"], r["gpu_first"])
         line["cpu_baseline"] = {"value": v, "unit": "reads/s", "cores": threads, "kind": "port",
