@@ -354,6 +354,10 @@ int hdc_context_option(hdc_context* ctx, int option, int value) {
                 return fail(HDC_ERR_INVALID, "option: wait limit must be 0 .. 4,000,000 thousand cycles");
             ctx->wait_cycles = (long long)value * 1000;
             return HDC_OK;
+        case HDC_GREEDY_FORM:
+            if (value < -1 || value > 1) return fail(HDC_ERR_INVALID, "option: greedy form must be -1, 0 or 1");
+            ctx->greedy_form = value;
+            return HDC_OK;
         case HDC_TEST_WITHHOLD_LOADS:
             if (value < 0 || value > 1) return fail(HDC_ERR_INVALID, "option: withhold must be 0 or 1");
             ctx->test_withhold_loads = value;

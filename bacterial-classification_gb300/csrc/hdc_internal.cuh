@@ -37,6 +37,7 @@ struct hdc_context {
     int tc_scatter = -1;            // tensor-core search: 1 scattered reference-tile order, 0 index order (-1: auto)
     int beam_grouped = -1;          // descent: 1 grouped by candidate node, 2 + tensor-core levels, 0 warp per read
     void* noalloc_scratch = nullptr;  // device address of hdc_search_plain_noalloc's fixed scratch (first call)
+    int greedy_form = -1;             // propagate-children selection: 1 scored (dim % 8 == 0), 0 sequential, -1 automatic
     int beam_one = -1;                // grouped descent: 1 every level in one cooperative launch, 0 a launch
                                       // sequence per level, -1 automatic (one launch where it fits)
     mutable int beam_one_fit = -1;    // the one-launch descent's CTAs all fit at once (-1: not asked yet)

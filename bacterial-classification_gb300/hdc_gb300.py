@@ -17,7 +17,7 @@ ERR = {1: "HDC_ERR_INVALID", 2: "HDC_ERR_RANGE", 3: "HDC_ERR_CUDA", 4: "HDC_ERR_
 SCORE_NORM, SCORE_COS, SCORE_DOT = 0, 1, 2
 TC_PREFETCH, TC_CLUSTER, TC_SHARE, BEAM_GROUPED, TC_SCATTER, TC_KBLOCK, TC_PAIR_MMA, TC_LANES = 1, 2, 3, 4, 5, 6, 7, 8
 OUT_I16, OUT_I32, OUT_BIPOLAR_BF16, OUT_BIPOLAR_I16, OUT_BIPOLAR_F16, OUT_BIPOLAR_I8, OUT_F16 = 0, 1, 2, 3, 4, 5, 6
-WAIT_LIMIT, TEST_WITHHOLD_LOADS, BEAM_ONE_LAUNCH = 9, 10, 11
+WAIT_LIMIT, TEST_WITHHOLD_LOADS, BEAM_ONE_LAUNCH, GREEDY_FORM = 9, 10, 11, 12
 OUT_SIGN_BITS = 7  # sign bits, int32 [n][dim / 32] (bit b of word w: element 32 w + b >= 0)
 
 # (name, restype, argtypes) of every exported entry point

@@ -1108,7 +1108,8 @@ def run_aux(args):
     sel, _ = sctx.propagate_greedy(hv, hn, gp, gi, rp, ri, 0.75)
     out["propagate_greedy"] = {"parents": len(groups), "candidates": int(cand_idx.size),
                                "selected": int(sel.sum().item()), "ms": ms,
-                               "bound": "latency: each parent's candidates are decided in order"}
+                               "form": "scored: pair scores in bulk (tiled), then each parent's decisions in "
+                                       "order from running maxima"}
     # identify: a leaf's similarity rows are its windows (135 of 150 bp, step 10); an internal
     # node's are the first 20 windows of its first descendant leaf
     row_off, node_rows = [], [0]

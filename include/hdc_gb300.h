@@ -322,6 +322,11 @@ int hdc_search_tc_last_shape(const hdc_context* ctx, int32_t shape[5]);
                               4,000,000, about 2 s at 2 GHz); a wait that gives up makes the
                               search return partial results and hdc_context_status report
                               100 + its code */
+#define HDC_GREEDY_FORM 12 /* hdc_propagate_greedy: 1 scores every pair a decision can need in
+                              bulk (tiled kernels), then decides each parent's candidates in order
+                              from running maxima; 0 one CTA per parent computing each decision's
+                              dots as it goes; -1 automatic (1 when dim % 8 == 0); results are
+                              identical */
 #define HDC_TEST_WITHHOLD_LOADS 10 /* tensor-core search, for tests of the bounded waits only: 1
                               makes the producer issue no operand loads, so the MMA issuer's
                               and the epilogue's waits run out (after HDC_WAIT_LIMIT) with

@@ -80,3 +80,49 @@ def test_bundle_tree_levels(hdc, orc, cuda):
         host = orc.bundle(host, ptr, idx)
         assert np.array_equal(level.cpu().numpy(), host)
         n = npar
+
+
+@pytest.mark.parametrize("dim,kmer", [(1024, 8), (2048, 10)])
+def test_greedy_scored_equals_sequential(hdc, cuda, dim, kmer):
+    """The scored form (pair scores in bulk, then the decisions in order from running
+    maxima) against the sequential form (each decision's dots computed as it is made):
+    identical decisions and best scores, for parents of 2,600 candidates (three blocks of
+    1,024), 1,100 candidates with existing sequences (their columns and the earlier
+    blocks' appended candidates in the fixed-column tiles), block-edge sizes 1,024 and
+    1,025, single candidates, an empty parent, and thresholds that select some, all
+    (2.0) or none (-2.0) of them."""
+    import torch
+    H = hdc
+    n_leaves = 2600
+    tree = H.synth_tree(77, n_leaves)
+    ctx = H.Context(dim, kmer, 150, 10)
+    hv = torch.empty((n_leaves, dim), dtype=torch.int16, device=cuda)
+    ctx.encode_segments(torch.from_numpy(tree.buf).to(cuda), torch.from_numpy(tree.off).to(cuda),
+                        torch.from_numpy(tree.len).to(cuda), hv, H.OUT_I16, tree.max_len())
+    norm2 = ctx.norms(hv)
+    groups = [list(range(n_leaves)), list(range(0, n_leaves, 2))[:1100], list(range(7)), list(range(40, 73)), [9],
+              [], list(range(1024)), list(range(500, 1525)), list(range(2599, 1500, -1))]
+    reps = [[], [5, 17, 901], [3], [], [1, 2], [4], [], [0, 1, 2, 3], []]
+    cand_ptr = np.zeros(len(groups) + 1, np.int64)
+    cand_ptr[1:] = np.cumsum([len(g) for g in groups])
+    rep_ptr = np.zeros(len(groups) + 1, np.int64)
+    rep_ptr[1:] = np.cumsum([len(r) for r in reps])
+    cand_idx = np.array([x for g in groups for x in g], np.int32)
+    rep_idx = np.array([x for r in reps for x in r], np.int32)
+    t = lambda a: torch.from_numpy(a).to(cuda)
+    for threshold in (0.75, 0.9, 2.0, -2.0):
+        out = []
+        for form in (0, 1):
+            ctx.option(H.GREEDY_FORM, form)
+            sel, best = ctx.propagate_greedy(hv, norm2, t(cand_ptr), t(cand_idx), t(rep_ptr), t(rep_idx), threshold)
+            torch.cuda.synchronize()
+            out.append((sel.cpu().numpy(), best.cpu().numpy()))
+        assert ctx.status() == 0
+        assert np.array_equal(out[0][0], out[1][0]), threshold
+        assert np.array_equal(out[0][1], out[1][1]), threshold
+        if threshold == 0.75:
+            assert 0 < out[0][0].sum() < len(cand_idx)
+        if threshold == 2.0:
+            assert out[0][0].all()
+        if threshold == -2.0:
+            assert not out[0][0].any()
