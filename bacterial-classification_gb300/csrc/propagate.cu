@@ -396,9 +396,11 @@ int propagate_scored(hdc_context* ctx, const int16_t* d_hv, const int64_t* d_nor
         if ((e = cudaGetLastError()) != cudaSuccess) st = cuda_fail(e, "propagate: launch");
         // the host copies of the tile lists must outlive their copies
         if (st == HDC_OK && (e = cudaStreamSynchronize(stream)) != cudaSuccess) st = cuda_fail(e, "propagate: block");
-        if (st == HDC_OK && b + 1 < max_blocks &&
-            (e = cudaMemcpy(na.data(), d_na, n_parents * 4, cudaMemcpyDeviceToHost)) != cudaSuccess)
-            st = cuda_fail(e, "propagate: appended counts");
+        if (st == HDC_OK && b + 1 < max_blocks) {  // the next block's fixed columns include these appends
+            e = cudaMemcpyAsync(na.data(), d_na, n_parents * 4, cudaMemcpyDeviceToHost, stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+            if (e != cudaSuccess) st = cuda_fail(e, "propagate: appended counts");
+        }
         cudaFreeAsync(tb, stream);
     }
     cudaFreeAsync(ws, stream);
