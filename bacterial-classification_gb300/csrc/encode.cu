@@ -376,21 +376,31 @@ __global__ void __launch_bounds__(kThreads) encode_kernel(const EncodeArgs a) {
     }
 }
 
+// The grid: every slab served by the same number of CTAs, all of them resident at once (one
+// wave).  Each warp takes a fixed share of the segments, so a CTA that had to wait for a free
+// SM would run its whole share after the others finished: the call would take two CTA times.
 template <int NP, int NH>
-int launch_np_nh(const EncodeArgs& a, int grid_x, int n_slabs, size_t smem, cudaStream_t stream) {
+int launch_np_nh(const hdc_context* ctx, const EncodeArgs& a, int n_slabs, size_t smem, cudaStream_t stream) {
     auto kern = encode_kernel<NP, NH>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_fail(e, "encode: cudaFuncSetAttribute");
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
+    if (e != cudaSuccess || per_sm < 1) return cuda_fail(e != cudaSuccess ? e : cudaErrorInvalidConfiguration,
+                                                         "encode: occupancy");
+    const int64_t fit = std::max<int64_t>(1, (int64_t)ctx->num_sms * per_sm / n_slabs);
+    const int64_t need = (a.n_segs + kWarps - 1) / kWarps;
+    const int grid_x = (int)std::min(fit, need);
     kern<<<dim3(grid_x, n_slabs), kThreads, smem, stream>>>(a);
     e = cudaGetLastError();
     return e == cudaSuccess ? HDC_OK : cuda_fail(e, "encode: launch");
 }
 
 template <int NP>
-int launch_np(const EncodeArgs& a, int nh, int grid_x, int n_slabs, size_t smem, cudaStream_t stream) {
-    if (nh <= 4) return launch_np_nh<NP, 4>(a, grid_x, n_slabs, smem, stream);
-    if (nh <= 8) return launch_np_nh<NP, 8>(a, grid_x, n_slabs, smem, stream);
-    return launch_np_nh<NP, 12>(a, grid_x, n_slabs, smem, stream);
+int launch_np(const hdc_context* ctx, const EncodeArgs& a, int nh, int n_slabs, size_t smem, cudaStream_t stream) {
+    if (nh <= 4) return launch_np_nh<NP, 4>(ctx, a, n_slabs, smem, stream);
+    if (nh <= 8) return launch_np_nh<NP, 8>(ctx, a, n_slabs, smem, stream);
+    return launch_np_nh<NP, 12>(ctx, a, n_slabs, smem, stream);
 }
 
 }  // namespace
@@ -496,17 +506,11 @@ int launch_encode(hdc_context* ctx, const char* d_bytes, const int64_t* d_seg_of
 
     const int n_slabs = (a.W32 + 31) / 32;
     const size_t smem = (size_t)a.table_rows * 32 * 4 + (size_t)kWarps * kChunk * 8;
-    // occupancy-sized grid: every SM busy, each slab served by the same number of CTAs
-    const int per_sm = std::max(1, std::min(8, (int)((227 * 1024) / (smem + 1024))));
-    const int64_t want = ((int64_t)ctx->num_sms * per_sm + n_slabs - 1) / n_slabs;
-    const int64_t need = (n_segs + kWarps - 1) / kWarps;
-    const int grid_x = (int)std::max<int64_t>(1, std::min<int64_t>(want, need));
-
     switch (np) {
-        case 1: return launch_np<1>(a, nh, grid_x, n_slabs, smem, stream);
-        case 2: return launch_np<2>(a, nh, grid_x, n_slabs, smem, stream);
-        case 3: return launch_np<3>(a, nh, grid_x, n_slabs, smem, stream);
-        default: return launch_np<4>(a, nh, grid_x, n_slabs, smem, stream);
+        case 1: return launch_np<1>(ctx, a, nh, n_slabs, smem, stream);
+        case 2: return launch_np<2>(ctx, a, nh, n_slabs, smem, stream);
+        case 3: return launch_np<3>(ctx, a, nh, n_slabs, smem, stream);
+        default: return launch_np<4>(ctx, a, nh, n_slabs, smem, stream);
     }
 }
 
