@@ -439,7 +439,9 @@ int hdc_identify(hdc_context* ctx, const int16_t* d_q, const int64_t* d_qnorm2, 
  * into d_out and d_name_off[j] / d_name_len[j] into d_in; *d_count (device
  * int64) = the number of kept records (may exceed max_records: then only the
  * first max_records are written).  Each record's sequence must be shorter than
- * 2^31 bytes.  Uses about 60 bytes of stream-ordered workspace per input byte. */
+ * 2^31 bytes.  Uses stream-ordered workspace of about 40 bytes per record and
+ * 40 per 8 KB of input, and synchronises the stream once (to size the
+ * record arrays). */
 int hdc_fasta_parse(hdc_context* ctx, const char* d_in, int64_t n, char* d_out, int64_t* d_seq_off,
                     int32_t* d_seq_len, int64_t* d_name_off, int32_t* d_name_len, int64_t max_records,
                     int64_t* d_count, void* stream);

@@ -64,3 +64,27 @@ def test_fasta_capacity(hdc, orc, cuda):
     ctx = hdc.Context(1024, 8, 150, 10)
     recs, c = _parse(hdc, ctx, data, cuda, max_records=20)
     assert c == 50 and recs == orc.fasta_records(data)[:20]
+
+
+def test_fasta_lines_across_tiles(hdc, orc, cuda):
+    """Lines longer than the parser's 8 KB tiles: text before the first header
+    over several tiles, a 20 KB header line, a 100 KB sequence line without
+    '\\n', CRLF lines, headers at tile edges and an input ending inside a
+    header."""
+    rng = random.Random(5)
+    seq = lambda n: "".join(rng.choice("ACGTN") for _ in range(n)).encode()
+    parts = [seq(30000), b"\n", seq(5000), b"\n>", b"h" * 20000, b"\n", seq(100000), b"\n"]
+    for i in range(200):  # short records of random sizes, some lines ending in CRLF
+        parts.append(b">r%d\n" % i)
+        parts.append(seq(rng.randint(0, 9000)) + (b"\r\n" if i % 3 == 0 else b"\n"))
+    data = b"".join(parts)
+    # headers placed exactly at multiples of 8 KB
+    edge = bytearray(b"A" * (8192 * 3 + 5))
+    for p in (8192 - 1, 2 * 8192 - 1):
+        edge[p] = ord("\n")
+        edge[p + 1] = ord(">")
+    data += bytes(edge) + b"\n>tail header without newline"
+    ctx = hdc.Context(1024, 8, 150, 10)
+    recs, c = _parse(hdc, ctx, data, cuda)
+    want = orc.fasta_records(data)
+    assert c == len(want) and recs == want
