@@ -35,25 +35,45 @@ constexpr int kIdWarps = 8;
 constexpr int kSimWarps = 8;
 
 // exact dot of an int16 row (global) with an int16 vector (shared or global),
-// one warp; dim % 8 == 0 and both 16-byte aligned
-__device__ __forceinline__ int64_t warp_dot_i16(const int16_t* __restrict__ q, const int16_t* __restrict__ v,
-                                                int dim) {
+// one warp; dim % 8 == 0 and both 16-byte aligned.  NARROW: every partial sum
+// fits int32, so the products are accumulated in int32 (two multiply-adds a
+// word instead of 64-bit additions).
+template <bool NARROW>
+__device__ __forceinline__ int64_t warp_dot_i16_t(const int16_t* __restrict__ q, const int16_t* __restrict__ v,
+                                                  int dim) {
     const int lane = threadIdx.x & 31;
     const uint4* q4 = reinterpret_cast<const uint4*>(q);
     const uint4* v4 = reinterpret_cast<const uint4*>(v);
     int64_t acc = 0;
+    int32_t acc32 = 0;
     for (int i = lane; i < dim / 8; i += 32) {
         const uint4 x = q4[i], y = __ldg(v4 + i);
         const uint32_t xs[4] = {x.x, x.y, x.z, x.w}, ys[4] = {y.x, y.y, y.z, y.w};
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            const int32_t p0 = (int32_t)(int16_t)(xs[u] & 0xffff) * (int32_t)(int16_t)(ys[u] & 0xffff);
-            const int32_t p1 = (int32_t)(int16_t)(xs[u] >> 16) * (int32_t)(int16_t)(ys[u] >> 16);
-            acc += (int64_t)p0 + (int64_t)p1;  // each product fits int32, their sum may not
+            const int32_t xl = (int32_t)(xs[u] << 16) >> 16, xh = (int32_t)xs[u] >> 16;
+            const int32_t yl = (int32_t)(ys[u] << 16) >> 16, yh = (int32_t)ys[u] >> 16;
+            if (NARROW) {
+                acc32 += xl * yl + xh * yh;
+            } else {
+                acc += (int64_t)(xl * yl) + (int64_t)(xh * yh);  // each product fits int32, their sum may not
+            }
         }
     }
+    if (NARROW) acc = acc32;
     for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     return acc;
+}
+
+// Cauchy-Schwarz bounds every partial sum of a dot (any subset of its products) by
+// sqrt(|q|^2 |r|^2): below 2^62 for the product of the squared norms, int32 never overflows.
+__device__ __forceinline__ bool dot_fits_i32(int64_t nq, int64_t nr) {
+    return nq <= 0 || nr <= 0 || nr < ((int64_t)1 << 62) / nq;
+}
+
+__device__ __forceinline__ int64_t warp_dot_i16(const int16_t* __restrict__ q, const int16_t* __restrict__ v, int dim,
+                                                int64_t nq, int64_t nr) {
+    return dot_fits_i32(nq, nr) ? warp_dot_i16_t<true>(q, v, dim) : warp_dot_i16_t<false>(q, v, dim);
 }
 
 struct Entry {
@@ -130,8 +150,9 @@ __global__ void __launch_bounds__(32 * kIdWarps) identify_kernel(const IdentifyA
                 const int64_t r0 = a.node_rows[node], r1 = a.node_rows[node + 1];
                 float best = -1.0f;  // identify starts every candidate at -1 (:127)
                 for (int64_t j = r0 + warp; j < r1; j += kIdWarps) {
-                    const int64_t dot = warp_dot_i16(qs, a.rows + j * a.dim, a.dim);
-                    best = fmaxf(best, exact_score(dot, qn, a.rn[j], a.mode));
+                    const int64_t rn = a.rn[j];
+                    const int64_t dot = warp_dot_i16(qs, a.rows + j * a.dim, a.dim, qn, rn);
+                    best = fmaxf(best, exact_score(dot, qn, rn, a.mode));
                 }
                 if (lane == 0) wbest[parity][warp] = best;
                 __syncthreads();
@@ -230,13 +251,14 @@ __global__ void __launch_bounds__(32 * kSimWarps) similarity_kernel(const Simila
     int32_t win = -1;
     if (a.ref_whole && a.ref_whole[ri] && r1 > r0) {
         // len <= L: the cosine of the two whole-sequence vectors, unclamped (:200-203)
-        best = exact_score(warp_dot_i16(q, a.rows + r0 * a.dim, a.dim), qn, a.rn[r0], a.mode);
+        best = exact_score(warp_dot_i16(q, a.rows + r0 * a.dim, a.dim, qn, a.rn[r0]), qn, a.rn[r0], a.mode);
         win = 0;
         r1 = r0;
     }
     for (int64_t j = r0; j < r1; ++j) {
-        const int64_t dot = warp_dot_i16(q, a.rows + j * a.dim, a.dim);
-        const float s = exact_score(dot, qn, a.rn[j], a.mode);
+        const int64_t rn = a.rn[j];
+        const int64_t dot = warp_dot_i16(q, a.rows + j * a.dim, a.dim, qn, rn);
+        const float s = exact_score(dot, qn, rn, a.mode);
         if (s > best) {  // strict: the first window reaching the maximum wins (:208-212)
             best = s;
             win = (int32_t)(j - r0);
