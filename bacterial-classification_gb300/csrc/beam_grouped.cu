@@ -409,61 +409,121 @@ __global__ void __launch_bounds__(kScoreThreads, ROWS16 ? kScoreBlocks16 : kScor
 
 // Per read: the best `beam` candidates, then the rule of the per-read kernel (stop below
 // the threshold with the best path, else keep the entries >= threshold, at most `beam`).
-__device__ void select_one(const GArgs& a, int L, int64_t r) {
-    if (a.done[r]) return;
-    uint64_t key[kMaxBeamG];
-    int32_t node[kMaxBeamG], slot[kMaxBeamG];
-    int n = 0;
-    for (int32_t p = a.off[r]; p < a.off[r + 1]; ++p) {
-        const uint64_t k = a.pair_key[p];
-        if (n < a.beam || k > key[n - 1]) {
-            int pos = n < a.beam ? n++ : a.beam - 1;
-            while (pos > 0 && key[pos - 1] < k) {
-                key[pos] = key[pos - 1];
-                node[pos] = node[pos - 1];
-                slot[pos] = slot[pos - 1];
-                --pos;
-            }
-            key[pos] = k;
-            node[pos] = a.pair_node[p];
-            slot[pos] = a.pair_slot[p];
-        }
-    }
-    int32_t np[kMaxBeamG][kMaxLevelsG];
-    float ns[kMaxBeamG][kMaxLevelsG];
-    for (int t = 0; t < n; ++t) {  // new beam rows from their parents' rows
-        for (int l = 0; l < L; ++l) {
-            np[t][l] = a.paths[state_at(r, slot[t], l)];
-            ns[t][l] = a.scores[state_at(r, slot[t], l)];
-        }
-        np[t][L] = node[t];
-        ns[t][L] = key_score(key[t]);
-    }
-    const bool stop = n == 0 || (double)key_score(key[0]) < a.threshold;
-    int keep = 0;
-    if (stop) {
-        a.out_depth[r] = n ? L + 1 : L;
-        keep = n ? 1 : 0;  // the best candidate's path is the answer
-        a.done[r] = 1;
-    } else {
-        while (keep < n && keep < a.beam && (double)key_score(key[keep]) >= a.threshold) ++keep;
-        a.nbeam[r] = keep;
-        if (L == a.levels - 1) {
-            a.out_depth[r] = a.levels;
-            a.done[r] = 1;
-        }
-    }
-    for (int t = 0; t < keep; ++t)
-        for (int l = 0; l <= L; ++l) {
-            a.paths[state_at(r, t, l)] = np[t][l];
-            a.scores[state_at(r, t, l)] = ns[t][l];
-        }
+// One warp per read, every lane calling with the same r.  The candidates are ordered by key
+// (descending), ties to the lower pair index (the order an insertion in pair order keeps);
+// round t takes the warp-wide first of those after round t - 1's pick, lane t keeps it.  The
+// keys of the first 128 pairs stay in registers (4 a lane), later ones are re-read each round.
+// The kept entries' paths are then copied lane-parallel: every old value is read before any
+// is written (a new entry's path comes from its parent's slot, possibly another entry's).
+constexpr int kSelCache = 4;
+
+__device__ __forceinline__ bool key_before(uint64_t k, int32_t p, uint64_t bk, int32_t bp) {
+    return k > bk || (k == bk && p < bp);
 }
 
+__device__ void select_warp(const GArgs& a, int L, int64_t r, int lane) {
+    if (a.done[r]) return;
+    const int32_t p0 = a.off[r], p1 = a.off[r + 1];
+    uint64_t ck[kSelCache];
+#pragma unroll
+    for (int i = 0; i < kSelCache; ++i) {
+        const int32_t p = p0 + lane + 32 * i;
+        ck[i] = p < p1 ? __ldcg(a.pair_key + p) : 0;  // from L2: written by other SMs in this kernel
+    }
+    const bool more = p1 - p0 > 32 * kSelCache;
+    uint64_t prev_k = 0, my_k = 0;
+    int32_t prev_p = -1, my_p = -1;
+    int n = 0;
+    for (int t = 0; t < a.beam; ++t) {
+        uint64_t bk = 0;
+        int32_t bp = INT32_MAX;  // nothing found: loses to every candidate
+        auto consider = [&](uint64_t k, int32_t p) {
+            if ((t == 0 || key_before(prev_k, prev_p, k, p)) && key_before(k, p, bk, bp)) {
+                bk = k;
+                bp = p;
+            }
+        };
+#pragma unroll
+        for (int i = 0; i < kSelCache; ++i)
+            if (p0 + lane + 32 * i < p1) consider(ck[i], p0 + lane + 32 * i);
+        if (more)
+            for (int32_t p = p0 + lane + 32 * kSelCache; p < p1; p += 32) consider(__ldcg(a.pair_key + p), p);
+        for (int o = 16; o; o >>= 1) {
+            const uint64_t ok = __shfl_xor_sync(0xffffffffu, bk, o);
+            const int32_t op = __shfl_xor_sync(0xffffffffu, bp, o);
+            if (key_before(ok, op, bk, bp)) {
+                bk = ok;
+                bp = op;
+            }
+        }
+        if (bp == INT32_MAX) break;  // no candidate left (the same on every lane)
+        if (lane == t) {
+            my_k = bk;
+            my_p = bp;
+        }
+        prev_k = bk;
+        prev_p = bp;
+        ++n;
+    }
+    const float my_s = key_score(my_k);
+    int32_t my_node = 0, my_slot = 0;
+    if (lane < n) {
+        my_node = a.pair_node[my_p];
+        my_slot = a.pair_slot[my_p];
+    }
+    const bool stop = n == 0 || (double)__shfl_sync(0xffffffffu, my_s, 0) < a.threshold;
+    int keep;
+    if (stop) {
+        keep = n ? 1 : 0;  // the best candidate's path is the answer
+    } else {
+        const uint32_t ok = __ballot_sync(0xffffffffu, lane < n && (double)my_s >= a.threshold);
+        keep = __ffs(~ok) - 1;  // the leading entries >= threshold (n <= 8: ~ok has a set bit)
+    }
+    if (lane == 0) {
+        if (stop) {
+            a.out_depth[r] = n ? L + 1 : L;
+            a.done[r] = 1;
+        } else {
+            a.nbeam[r] = keep;
+            if (L == a.levels - 1) {
+                a.out_depth[r] = a.levels;
+                a.done[r] = 1;
+            }
+        }
+    }
+    // entry t's levels 0..L: lanes i and i + 32 of the keep x (L + 1) values
+    int32_t vp[2];
+    float vs[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int i = lane + 32 * h, t = i / (L + 1), l = i - t * (L + 1);
+        const int src = t < kMaxBeamG ? t : 0;
+        const int32_t slot = __shfl_sync(0xffffffffu, my_slot, src);
+        const int32_t node = __shfl_sync(0xffffffffu, my_node, src);
+        const float sc = __shfl_sync(0xffffffffu, my_s, src);
+        vp[h] = node;
+        vs[h] = sc;
+        if (t < keep && l < L) {
+            vp[h] = a.paths[state_at(r, slot, l)];
+            vs[h] = a.scores[state_at(r, slot, l)];
+        }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int i = lane + 32 * h, t = i / (L + 1), l = i - t * (L + 1);
+        if (t < keep) {
+            a.paths[state_at(r, t, l)] = vp[h];
+            a.scores[state_at(r, t, l)] = vs[h];
+        }
+    }
+}
+
+// one warp per read
 __global__ void select_kernel(const GArgs a, int L) {
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (r >= a.nq) return;
-    select_one(a, L, r);
+    select_warp(a, L, r, threadIdx.x & 31);
 }
 
 __device__ __forceinline__ void output_one(const GArgs& a, int64_t r, int32_t* path, float* path_score,
@@ -483,6 +543,28 @@ __global__ void output_kernel(const GArgs a, int32_t* __restrict__ path, float* 
     output_one(a, r, path, path_score, depth);
 }
 
+// The last level scored apart from the one-launch descent, which stops once that level's
+// pairs are in node order: leaf_score_kernel scores them as score_kernel does (more warps per
+// SM than the cooperative launch holds), then select_output_kernel takes each read's final
+// beam and writes its output, one warp per read.  Neither runs when the descent gave up
+// (abort raised): its pair arrays are then incomplete.
+template <bool ROWS16>
+__global__ void __launch_bounds__(kScoreThreads, ROWS16 ? kScoreBlocks16 : kScoreBlocks)
+    leaf_score_kernel(const GArgs a, const int* __restrict__ abort) {
+    if (*abort) return;
+    score_pairs<ROWS16>(a, (((int64_t)blockIdx.x * blockDim.x) >> 5) + (threadIdx.x >> 5),
+                        ((int64_t)gridDim.x * blockDim.x) >> 5);
+}
+
+__global__ void select_output_kernel(const GArgs a, int L, int32_t* __restrict__ path, float* __restrict__ path_score,
+                                     int32_t* __restrict__ depth, const int* __restrict__ abort) {
+    const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (*abort || r >= a.nq) return;
+    select_warp(a, L, r, threadIdx.x & 31);
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) output_one(a, r, path, path_score, depth);
+}
+
 // ---------------------------------------------------------------- tensor-core scoring
 // Levels above the leaves score on the tensor cores, grouped by parent: the entries (read,
 // beam slot) whose beam row is node P are scored against P's children (a childless P
@@ -493,11 +575,13 @@ __global__ void output_kernel(const GArgs a, int32_t* __restrict__ path, float* 
 // prototype rows, split into three balanced base-2048 fp16 limbs, into 128-byte-swizzled
 // shared memory (the B operand); one thread issues M128 x N96 x K16 tcgen05 MMAs with A from
 // TMEM, the three limb tiles side by side, into one fp32 TMEM accumulator of 32 columns per
-// limb.  A in TMEM takes the signs' shared-memory stores and the MMAs' shared-memory reads of
-// A (32 KB of the ~60 KB of shared-memory traffic of a K block) off the shared memory.  Four epilogue
-// warps recombine the exact int64 dots and write the pair keys the select kernel reads.
-// Exact: a limb is at most 1024 in magnitude (the top one 512), so every partial sum is an
-// integer of magnitude <= dim * 1024 <= 2^24.  Level 0 is one parent (-1) whose children
+// limb.  An item whose children all have |v| <= 2^21 (known from their squared norms) takes
+// two limbs and N64 MMAs: a third less of the producers' conversions and stores.  A in TMEM
+// takes the signs' shared-memory stores and the MMAs' shared-memory reads of A (32 KB of the
+// ~60 KB of shared-memory traffic of a K block) off the shared memory.  Four epilogue warps
+// recombine the exact int64 dots and write the pair keys the select kernel reads.
+// Exact: a limb is at most 1024 in magnitude (the top one of three 512), so every partial sum
+// is an integer of magnitude <= dim * 1024 <= 2^24.  Level 0 is one parent (-1) whose children
 // are the roots and whose entries are all reads.
 constexpr int kTcE = 128;                                         // entries per item (TMEM lanes)
 constexpr int kTcC = 32;                                          // children per item (MMA N)
@@ -530,6 +614,7 @@ struct TcItems {
     int32_t* item_off;    // [n_nodes + 1]; item_off[n_nodes] = number of such items of the level
     int32_t* small;       // [n_nodes] 1: the parent shares an item (<= 64 entries, <= 16 children)
     int32_t* small_off;   // [n_nodes + 1]; small_off[n_nodes] = number of such parents
+    int32_t* fit2;        // [n_nodes] 1: every child of the parent fits two limbs (|v| <= 2^21)
     // item i: parent, first entry, first child (-1 parent: level 0); an item shared by two
     // parents (after the others) has item_e0 = -1, parent item_par and second parent item_j0 (or -1)
     int32_t* item_par;
@@ -585,11 +670,22 @@ __global__ void par_scatter_kernel(const GArgs a, TcItems t, int L) {
 // the same whatever its fill, and most parents of the lower levels are that small.
 constexpr int kTcHalfE = kTcE / 2, kTcHalfC = kTcC / 2;
 
+// A row fits two limbs when every element has |v| <= 2^21, and |v| <= sqrt(squared norm) for
+// each element: int16 rows always, int32 rows whose squared norm is at most 2^42.
+__device__ __forceinline__ bool row_fits2(const GArgs& a, int32_t c) {
+    return c >= a.n32 || a.pn[c] <= (int64_t(1) << 42);
+}
+
 __device__ __forceinline__ void item_count_one(const GArgs& a, const TcItems& t, int64_t P) {
     const int32_t m = t.par_cnt[P], nch = n_children(a, (int32_t)P);
     const bool small = m > 0 && m <= kTcHalfE && nch <= kTcHalfC;
     t.small[P] = small ? 1 : 0;
     t.item_cnt[P] = m && !small ? ((m + kTcE - 1) / kTcE) * ((nch + kTcC - 1) / kTcC) : 0;
+    if (m) {
+        bool two = true;
+        for (int32_t j = 0; two && j < nch; ++j) two = row_fits2(a, child_at(a, (int32_t)P, j));
+        t.fit2[P] = two ? 1 : 0;
+    }
 }
 
 __global__ void item_count_kernel(const GArgs a, TcItems t) {
@@ -665,6 +761,14 @@ __device__ __forceinline__ ItemRow item_row(const GArgs& a, const TcItems& t, in
     return x;
 }
 
+// Whether item `it` runs with two limbs (every child of its parents fits them; level 0's
+// roots always take three).
+__device__ __forceinline__ bool item_two(const TcItems& t, int32_t it) {
+    const int32_t p = t.item_par[it], e0 = t.item_e0[it], j0 = t.item_j0[it];
+    if (p < 0) return false;
+    return t.fit2[p] != 0 && (e0 >= 0 || j0 < 0 || t.fit2[j0] != 0);
+}
+
 __device__ __forceinline__ int32_t item_child(const GArgs& a, const TcItems& t, int32_t it, int js) {
     const int32_t p = t.item_par[it], e0 = t.item_e0[it], j0 = t.item_j0[it];
     if (e0 < 0) {
@@ -691,6 +795,12 @@ __device__ __forceinline__ void items_level0_range(const GArgs& a, const TcItems
 
 __global__ void items_level0_kernel(const GArgs a, TcItems t) {
     items_level0_range(a, t, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
+}
+
+// v = l0 + 2048 l1 with l0 in [-1024, 1023] and |l1| <= 1024, for |v| <= 2^21
+__device__ __forceinline__ void limbs2(int32_t v, int32_t& l0, int32_t& l1) {
+    l1 = (v >> 11) + (((v & 2047) + 1024) >> 11);  // floor((v + 1024) / 2048)
+    l0 = (int32_t)((uint32_t)v - ((uint32_t)l1 << 11));
 }
 
 // v = l0 + 2048 l1 + 2048^2 l2 with l0, l1 in [-1024, 1023] and |l2| <= 512, for every int32 v
@@ -807,6 +917,7 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
         bool ok = true;
         for (int32_t it = blockIdx.x; ok && it < n_items; it += gridDim.x, nbase += kblocks) {
             const int64_t rrow = item_row(a, t, it, tid).r;
+            const bool two = item_two(t, it);
             const uint2* bits_row = reinterpret_cast<const uint2*>(a.bits + (rrow >= 0 ? rrow : 0) * a.words);
             // the valid child slots: 0..n0-1 and, in a shared item, 16..16+n1-1
             const int32_t ip = t.item_par[it], ie0 = t.item_e0[it], ij0 = t.item_j0[it];
@@ -889,7 +1000,8 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
                         }
                         tc::tmem_st32(tmem + ((uint32_t)(warp & 3) << 21) + (uint32_t)(kTcACol + 32 * stage), col);
                     }
-                    // B: this thread's groups of 4 prototype values, each in three limbs (8 bytes per limb)
+                    // B: this thread's groups of 4 prototype values, each in two or three limbs (8
+                    // bytes per limb)
 #pragma unroll
                     for (int j = 0; j < 4; ++j) {
                         if (tid + kTcE * j >= ngroups) break;
@@ -901,16 +1013,21 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
                             x[2] = (int32_t)(pv[j].y << 16) >> 16;
                             x[3] = (int32_t)pv[j].y >> 16;
                         }
-#pragma unroll
-                        for (int e = 0; e < 4; ++e) limbs3(x[e], l0[e], l1[e], l2[e]);
                         const int js = gdst[j] >> 4, u = gdst[j] & 15;
                         const int off = (u & 1) * 8;
+                        if (two) {
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) limbs2(x[e], l0[e], l1[e]);
+                        } else {
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) limbs3(x[e], l0[e], l1[e], l2[e]);
+                            *reinterpret_cast<uint2*>(swz(st + 2 * kTcBBytes, js, u >> 1) + off) =
+                                make_uint2(half2_bits(l2[0], l2[1]), half2_bits(l2[2], l2[3]));
+                        }
                         *reinterpret_cast<uint2*>(swz(st, js, u >> 1) + off) =
                             make_uint2(half2_bits(l0[0], l0[1]), half2_bits(l0[2], l0[3]));
                         *reinterpret_cast<uint2*>(swz(st + kTcBBytes, js, u >> 1) + off) =
                             make_uint2(half2_bits(l1[0], l1[1]), half2_bits(l1[2], l1[3]));
-                        *reinterpret_cast<uint2*>(swz(st + 2 * kTcBBytes, js, u >> 1) + off) =
-                            make_uint2(half2_bits(l2[0], l2[1]), half2_bits(l2[2], l2[3]));
                     }
                     tc::tmem_st_wait();       // the A columns are written
                     tc::fence_before();       // ... before the arrive below (tcgen05 ordering)
@@ -934,6 +1051,7 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
             // this row's entry and its parent's columns (the same for the warp's 32 rows: a shared
             // item's halves are 64 rows)
             const ItemRow x = item_row(a, t, it, row);
+            const bool two = item_two(t, it);
             if (!tc::mbar_wait(&sm.accf_bar[acc], acc_phase, &sm.err, 12)) break;
             tc::fence_after();
             const uint32_t d = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * kTcAccCols);
@@ -943,7 +1061,12 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
                 uint32_t v0[16], v1[16], v2[16];
                 tc::tmem_ld16(d + h, v0);
                 tc::tmem_ld16(d + kTcC + h, v1);
-                tc::tmem_ld16(d + 2 * kTcC + h, v2);
+                if (two) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) v2[j] = 0;
+                } else {
+                    tc::tmem_ld16(d + 2 * kTcC + h, v2);
+                }
                 tc::tmem_ld_wait();
                 if (x.r < 0) continue;
 #pragma unroll
@@ -967,9 +1090,10 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
         }
     } else if (lane == 0) {
         // ------------------------------------------------ MMA issuer
-        // the three limb tiles of B are 96 consecutive rows of shared memory and their
-        // accumulators 96 consecutive columns: one N = 96 MMA covers all three
-        constexpr uint32_t IDESC = tc::idesc_f16_f32(kTcE, kTcLimbs * kTcC);
+        // the limb tiles of B are 64 or 96 consecutive rows of shared memory and their
+        // accumulators as many consecutive columns: one N = 64 or 96 MMA covers them all
+        constexpr uint32_t IDESC3 = tc::idesc_f16_f32(kTcE, kTcLimbs * kTcC);
+        constexpr uint32_t IDESC2 = tc::idesc_f16_f32(kTcE, 2 * kTcC);
         int& stage = run.stage;
         int& acc = run.acc;
         uint32_t& phase = run.phase;
@@ -979,6 +1103,7 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
             if (!tc::mbar_wait(&sm.acce_bar[acc], acc_phase ^ 1, &sm.err, 13)) break;
             tc::fence_after();
             const uint32_t d = tmem + (uint32_t)(acc * kTcAccCols);
+            const uint32_t IDESC = item_two(t, it) ? IDESC2 : IDESC3;
             for (int kb = 0; kb < kblocks; ++kb) {
                 if (!tc::mbar_wait(&sm.full_bar[stage], phase, &sm.err, 14)) {
                     ok = false;
@@ -1070,6 +1195,7 @@ struct OneArgs {
     float* out_score;
     int32_t* out_depth;
     unsigned long long* phase_ts;  // [kMaxPhaseTs] CTA 0's clock at the start and after every barrier
+    int leaf_apart;                // 1: stop at the last level's node-ordered pairs (scored by leaf_score_kernel)
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -1528,6 +1654,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs 
         if (b == 0 && tid == 0) atomicCAS(o.status, 0, kStatusChildCount);
     }
     __syncthreads();
+    bool apart_done = false;
     for (int L = 0; ok && L < a.levels; ++L) {
         const bool tcl = o.use_tc && L < a.levels - 1;
         // A: candidate counts of this CTA's reads and their sum; zero this level's node counters
@@ -1597,6 +1724,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs 
             // E: the pairs in node order
             scatter_range(a, gtid, gstride);
             if (!(ok = grid_barrier(o, sm, &ok_s, &n_ts))) break;
+            if (o.leaf_apart && L == a.levels - 1) {
+                // the last level is scored and selected by leaf_score_kernel and select_output_kernel
+                apart_done = true;
+                break;
+            }
             // F: the pairs scored on the CUDA cores: the leaf level's rows streamed through shared
             // memory, other levels (every level without the tensor cores) one warp per pair
             if (o.use_tc)
@@ -1612,10 +1744,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs 
             keys_from_parts(a, r0, r1);
             __syncthreads();
         }
-        for (int64_t r = r0 + tid; r < r1; r += nt) select_one(a, L, r);
+        for (int64_t r = r0 + (tid >> 5); r < r1; r += nt >> 5) select_warp(a, L, r, tid & 31);
         __syncthreads();
     }
-    if (ok)
+    if (ok && !apart_done)
         for (int64_t r = r0 + tid; r < r1; r += nt) output_one(a, r, o.out_path, o.out_score, o.out_depth);
     if (b == 0 && tid == 0) {
         if (n_ts < kMaxPhaseTs) o.phase_ts[n_ts++] = global_ns();
@@ -1751,6 +1883,7 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
             t.item_off = carve<int32_t>(cur, n_nodes + 1);
             t.small = carve<int32_t>(cur, n_nodes);
             t.small_off = carve<int32_t>(cur, n_nodes + 1);
+            t.fit2 = carve<int32_t>(cur, n_nodes);
             t.item_par = carve<int32_t>(cur, max_items);
             t.item_e0 = carve<int32_t>(cur, max_items);
             t.item_j0 = carve<int32_t>(cur, max_items);
@@ -1789,11 +1922,21 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
             }
         }
         o.phase_ts = ctx->d_phase_ts;
+        o.leaf_apart = ctx->beam_one != 1 ? 1 : 0;  // automatic: the last level in its own kernel
         e = cudaMemsetAsync(one_state, 0, 4 * sizeof(uint32_t), stream);
         void* args[] = {(void*)&a, (void*)&t, (void*)&o};
         if (e == cudaSuccess)
             e = cudaLaunchCooperativeKernel((const void*)descent_one_kernel, dim3((unsigned)ctx->num_sms),
                                             dim3(kTcThreads), args, kOneSmem, stream);
+        if (e == cudaSuccess && o.leaf_apart) {
+            if (n32 < n_nodes)
+                leaf_score_kernel<true><<<ctx->num_sms * kScoreBlocks16, kScoreThreads, 0, stream>>>(a, o.abort);
+            else
+                leaf_score_kernel<false><<<ctx->num_sms * kScoreBlocks, kScoreThreads, 0, stream>>>(a, o.abort);
+            select_output_kernel<<<(unsigned)((nq * 32 + 255) / 256), 256, 0, stream>>>(a, levels - 1, d_path,
+                                                                                      d_path_score, d_depth, o.abort);
+            e = cudaGetLastError();
+        }
         cudaFreeAsync(ws, stream);
         return e == cudaSuccess ? HDC_OK : cuda_fail(e, "beam: one-launch descent");
     }
@@ -1844,7 +1987,7 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
             else
                 score_kernel<false><<<ctx->num_sms * kScoreBlocks, kScoreThreads, 0, stream>>>(a);
         }
-        select_kernel<<<rb, 256, 0, stream>>>(a, L);
+        select_kernel<<<(unsigned)((nq * 32 + 255) / 256), 256, 0, stream>>>(a, L);
     }
     output_kernel<<<rb, 256, 0, stream>>>(a, d_path, d_path_score, d_depth);
     e = cudaGetLastError();

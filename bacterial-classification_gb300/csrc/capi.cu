@@ -346,7 +346,8 @@ int hdc_context_option(hdc_context* ctx, int option, int value) {
             ctx->beam_grouped = value;
             return HDC_OK;
         case HDC_BEAM_ONE_LAUNCH:
-            if (value < -1 || value > 1) return fail(HDC_ERR_INVALID, "option: one-launch descent must be -1, 0 or 1");
+            if (value < -1 || value > 2)
+                return fail(HDC_ERR_INVALID, "option: one-launch descent must be -1, 0, 1 or 2");
             ctx->beam_one = value;
             return HDC_OK;
         case HDC_WAIT_LIMIT:

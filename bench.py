@@ -581,8 +581,8 @@ def run_descent(args, cfg):
         torch.cuda.synchronize()
         beam_ms.append(ev[0].elapsed_time(ev[1]))
     path, score, depth = out["r"]
-    phases = descent_phases(ctx.beam_phase_times(), L, grouped_tc=args.beam_grouped in (-1, 2)) \
-        if split and args.beam_one != 0 else None
+    phases = descent_phases(ctx.beam_phase_times(), L, grouped_tc=args.beam_grouped in (-1, 2),
+                            apart=args.beam_one != 1) if split and args.beam_one != 0 else None
     depth_mean = float(depth.float().mean())
     last = 2 % n_pool  # out["r"] is from the last event-timed call, on dev_pool[2 % n_pool]
     leaf_acc = float((path[:, L - 1].cpu().numpy() == int(base[5]) + pool[last].label[:B]).mean())
@@ -630,8 +630,12 @@ def run_descent(args, cfg):
     # descent_tc_kernel.  One warp per read: one kernel.
     grouped = args.beam_grouped != 0 and dim % 1024 == 0 and dim <= 16384
     tc_levels = grouped and args.beam_grouped in (-1, 2)
-    if not grouped or args.beam_one != 0:  # one warp per read, or every level in one cooperative launch
+    if not grouped:  # one warp per read
         per_step = 2
+    elif args.beam_one == 1:  # every level in one cooperative launch
+        per_step = 2
+    elif args.beam_one != 0:  # the cooperative launch up to the leaf pairs, then leaf scoring and select (default)
+        per_step = 4
     elif tc_levels and L > 1:
         per_step = 1 + 3 + 6 * L + 2 + 14 * (L - 2) + 5
     else:
@@ -653,9 +657,12 @@ def run_descent(args, cfg):
     return res
 
 
-def descent_phases(ms, levels, grouped_tc=True):
+def descent_phases(ms, levels, grouped_tc=True, apart=False):
     """Per-level times (ms) of a one-launch descent from its phase clock: a level's
-    phases end at its scoring; the select of a level is counted with the next."""
+    phases end at its scoring; the select of a level is counted with the next.  With the
+    last level apart (the default) the cooperative launch ends at that level's
+    node-ordered pairs; leaf_score_kernel and select_output_kernel, timed with the
+    call, score them and take the final beams."""
     names = ["setup"]
     for L in range(levels):
         tcl = grouped_tc and L < levels - 1
@@ -663,9 +670,11 @@ def descent_phases(ms, levels, grouped_tc=True):
             names += ["count", "expand", "score_tc"]
         elif tcl:
             names += ["count", "expand", "parent_sums", "parent_scan", "scatter", "items", "score_tc"]
+        elif apart:
+            names += ["count", "expand", "node_sums", "node_scan", "scatter"]
         else:
             names += ["count", "expand", "node_sums", "node_scan", "scatter", "score_cuda"]
-    names += ["select_output"]
+    names += ["handoff" if apart else "select_output"]
     if len(ms) != len(names):
         return {"raw_ms": ms}
     out = {"setup": ms[0]}
@@ -673,13 +682,13 @@ def descent_phases(ms, levels, grouped_tc=True):
     i = 1
     for L in range(levels):
         tcl = grouped_tc and L < levels - 1
-        n = 3 if (tcl and L == 0) else 7 if tcl else 6
+        n = 3 if (tcl and L == 0) else 7 if tcl else (5 if apart else 6)
         for nm in names[i:i + n]:
             per_level[L][nm] = per_level[L].get(nm, 0.0) + ms[i]
             i += 1
     out["levels"] = [{k: round(v, 4) for k, v in d.items()} for d in per_level]
-    out["select_output"] = ms[-1]
-    out["total"] = sum(ms)
+    out[names[-1]] = ms[-1]
+    out["total_cooperative"] = sum(ms)
     return out
 
 
@@ -900,8 +909,12 @@ def descent_line(args, cfg, r, metric, workload):
                                "bound by their producers' conversions, the leaf level by HBM "
                                "(%d candidate rows per read)" % (
                                    "_split" if split else "",
-                                   "descent_one_kernel, every level in one cooperative launch" if args.beam_one != 0
-                                   else "kernels per level", r["proto_bytes"] / 1e9, cfg["levels"],
+                                   "descent_one_kernel, every level in one cooperative launch" if args.beam_one == 1
+                                   else "kernels per level" if args.beam_one == 0
+                                   else "descent_one_kernel, every level in one cooperative launch up to the "
+                                        "leaf pairs sorted by node, then leaf_score_kernel scoring them and "
+                                        "select_output_kernel taking the final beams", r["proto_bytes"] / 1e9,
+                                   cfg["levels"],
                                    r["rows_per_read"])},
         "propagate_bundle": {"kernel": "bundle_kernel (internal prototypes = int32 sums of children)",
                              "ms": bundle_ms, "gb_per_s": bundle_bytes / (bundle_ms / 1e3) / 1e9,
@@ -1172,7 +1185,8 @@ def main():
     ap.add_argument("--beam-grouped", type=int, default=-1,
                     help="descent: 1 reads grouped by candidate node, 0 one warp per read (-1: default)")
     ap.add_argument("--beam-one", type=int, default=-1,
-                    help="descent: 1 every level in one launch, 0 kernels per level (-1: default, one launch)")
+                    help="descent: 1 every level in one launch, 2 one launch up to the leaf pairs + a leaf kernel, "
+                         "0 kernels per level (-1: default, 2)")
     ap.add_argument("--score-mode", default="norm", choices=["norm", "cos", "dot"],
                     help="score of the top-k search (default the reference's NORM scale; the CPU legs need it)")
     ap.add_argument("--aux-scale", type=float, default=1.0,

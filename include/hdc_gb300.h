@@ -314,8 +314,11 @@ int hdc_search_tc_last_shape(const hdc_context* ctx, int32_t shape[5]);
                               automatic (2 when dim % 1024 == 0 and dim <= 16384, else 0) */
 #define HDC_BEAM_ONE_LAUNCH 11 /* grouped descent (HDC_BEAM_GROUPED 1 or 2): 1 runs every level
                               in one cooperative launch (one CTA per SM, the phases of a level
-                              separated by bounded grid-wide barriers), 0 a sequence of kernels
-                              per level, -1 automatic (one launch where all its CTAs fit);
+                              separated by bounded grid-wide barriers); 2 the same up to the
+                              last level's node-ordered pairs, which a second kernel scores
+                              (more warps per SM than the cooperative launch holds) and a third
+                              selects from (one warp per read); 0 a sequence of kernels per
+                              level; -1 automatic (2 where the cooperative CTAs all fit);
                               results are identical */
 #define HDC_WAIT_LIMIT 9   /* tensor-core search: its bounded device-side waits give up after
                               value x 1,000 SM cycles, 1 .. 4,000,000 (0: the default,

@@ -39,7 +39,7 @@ def _first_int16_node(proto):
 
 # grouped: 1 reads grouped by candidate node, 2 the same with the levels above the last on
 # the tensor cores, 0 one warp per read (identical results)
-@pytest.mark.parametrize("grouped,one", [(0, 0), (1, 0), (1, 1), (2, 0), (2, 1)])
+@pytest.mark.parametrize("grouped,one", [(0, 0), (1, 0), (1, 1), (1, 2), (2, 0), (2, 1), (2, 2)])
 @pytest.mark.parametrize("dim,kmer,n_leaves,beam,threshold,childless", [
     (1024, 10, 200, 5, 0.0, False), (2048, 12, 300, 3, 0.0, False), (1024, 8, 150, 5, 0.6, False),
     (2048, 10, 300, 5, -2.0, True), (1024, 10, 200, 8, float("-inf"), True)])
@@ -184,6 +184,89 @@ def test_beam_tensor_core_levels_wide_nodes_and_limbs(hdc, cuda):
         for x, y in zip(a, b_):
             assert np.array_equal(x, y)
 
+
+
+def test_beam_tensor_core_two_limb_items(hdc, cuda):
+    """Items whose children all have squared norms <= 2^42 (so every element
+    |v| <= 2^21) run with two fp16 limbs; the others with three.  Seven roots:
+    0-2 with 40 children each (items of their own), 3-6 with 10 children each
+    (two parents to a shared item when they have <= 64 entries, which reads
+    0-29 make them).  Children of roots 0, 3 and 5-6 fit two limbs, with rows
+    at the edge (one element +-2^21, norm exactly 2^42; all elements +-2^16);
+    roots 1 and 4 each have one child of norm 2^42 + 1; root 2's children
+    reach 2^26.  The tensor-core descent (every form) equals the CUDA-core
+    one, D = 1,024."""
+    import torch
+    H = hdc
+    g = np.random.default_rng(73)
+    dim, nq = 1024, 300
+    fan = [40, 40, 40, 10, 10, 10, 10]
+    n0, n1 = len(fan), sum(fan)
+    n2 = 2 * n1
+    ptr = np.zeros(n0 + n1 + n2 + 1, np.int64)
+    idx, first = [], [n0 + sum(fan[:r]) for r in range(n0)]
+    for r in range(n0):
+        idx += list(range(first[r], first[r] + fan[r]))
+        ptr[r + 1] = len(idx)
+    for v in range(n1):
+        idx += [n0 + n1 + 2 * v, n0 + n1 + 2 * v + 1]
+        ptr[n0 + v + 1] = len(idx)
+    ptr[n0 + n1 + 1:] = len(idx)
+    idx = np.array(idx, np.int32)
+    u = np.where(g.random(dim) < 0.5, -1, 1).astype(np.int64)
+    proto_h = np.zeros((n0 + n1 + n2, dim), np.int64)
+    for r in range(n0):
+        proto_h[r] = (1000 if r < 3 else -1000) * u + g.integers(-200, 201, dim)
+    e16 = 1 << 16
+    for r in range(n0):  # children leaning towards their root's reads (some pass threshold 0, some stop)
+        rows = slice(first[r], first[r] + fan[r])
+        h = (1 << 25) if r == 2 else e16 // 2
+        proto_h[rows] = (h if r < 3 else -h) * u + g.integers(-h, h + 1, (fan[r], dim))
+    c = first[0]
+    proto_h[c] = 0
+    proto_h[c, 0] = 1 << 21
+    proto_h[c + 1] = 0
+    proto_h[c + 1, 5] = -(1 << 21)
+    proto_h[c + 2, ::2], proto_h[c + 2, 1::2] = e16, -e16
+    proto_h[c + 3] = 0
+    proto_h[c + 3, 0], proto_h[c + 3, 1] = (1 << 21) - 1, 2047
+    for r in (1, 4):  # one child just over the bound: the parent's items take three limbs
+        c = first[r] + 1
+        proto_h[c] = 0
+        proto_h[c, 0], proto_h[c, 1] = 1 << 21, 1
+    proto_h[first[5]] = 0
+    proto_h[first[5], 3] = -(1 << 21)
+    proto_h[n0 + n1:] = g.integers(-30000, 30001, (n2, dim))
+    sq = (proto_h.astype(np.float64) ** 2).sum(axis=1)
+    assert sq[first[0]] == 2.0 ** 42 and sq[first[1] + 1] == 2.0 ** 42 + 1
+    flips = g.random((nq, dim)) < 0.2
+    q = np.where(flips, -u, u)
+    q[:30] = -q[:30]  # these reads follow roots 3-6 (few entries each: shared items)
+    proto = torch.from_numpy(proto_h.astype(np.int32)).to(cuda)
+    q8 = torch.from_numpy(q.astype(np.int8)).to(cuda)
+    ctx = H.Context(dim, 10, 250, 10)
+    qn, pn = ctx.norms(q8), ctx.norms(proto)
+    assert int(pn[first[0]]) == 1 << 42 and int(pn[first[4] + 1]) == (1 << 42) + 1
+    roots = torch.arange(0, n0, dtype=torch.int32, device=cuda)
+    d_ptr, d_idx = torch.from_numpy(ptr).to(cuda), torch.from_numpy(idx).to(cuda)
+    cases = [(levels, beam, threshold) for levels in (2, 3)
+             for beam, threshold in ((5, 0.0), (8, float("-inf")), (3, 0.0))]
+    forms = [(1, 0), (2, 0), (2, 1), (2, 2)]  # (HDC_BEAM_GROUPED, HDC_BEAM_ONE_LAUNCH)
+    out = {}
+    for grouped, one in forms:
+        ctx.option(H.BEAM_GROUPED, grouped)
+        ctx.option(H.BEAM_ONE_LAUNCH, one)
+        for case in cases:
+            res = ctx.beam_search(q8, qn, proto, pn, d_ptr, d_idx, roots, *case)
+            out[(grouped, one) + case] = [x.cpu().numpy() for x in res]
+    torch.cuda.synchronize()
+    assert ctx.status() == 0
+    for case in cases:
+        ref = out[(1, 0) + case]
+        assert (ref[2] == case[0]).any()  # some reads reach the last level
+        for form in forms[1:]:
+            for x, y in zip(ref, out[form + case]):
+                assert np.array_equal(x, y), (form, case)
 
 
 def test_beam_split_rows_equal_int32(hdc, cuda):
@@ -381,7 +464,9 @@ def test_beam_split_bit_reads_equal_int8_reads(hdc, cuda):
 
 def test_beam_one_launch_equals_level_kernels(hdc, cuda):
     """The one-launch descent (descent_one_kernel: every level in one cooperative
-    launch) against the same grouped descent run as kernels per level, on a
+    launch, and the same with the last level scored and selected by kernels of
+    their own) against the
+    same grouped descent run as kernels per level, on a
     20,000-leaf tree with 3,000 reads: identical paths, scores and depths for
     int32 rows and for split int16 rows with sign-bit reads, both grouped forms,
     thresholds 0 and -inf, 6 and 3 levels, a caller-given child count (equal,
@@ -433,11 +518,12 @@ def test_beam_one_launch_equals_level_kernels(hdc, cuda):
 
     ctx.option(H.BEAM_ONE_LAUNCH, 0)
     want = runs()
-    ctx.option(H.BEAM_ONE_LAUNCH, 1)
-    got = runs()
-    for w, g in zip(want, got):
-        for x, y in zip(w, g):
-            assert np.array_equal(x, y)
+    for one in (1, 2):  # every level in one launch; the same with the last level in the leaf kernel
+        ctx.option(H.BEAM_ONE_LAUNCH, one)
+        got = runs()
+        for w, g in zip(want, got):
+            for x, y in zip(w, g):
+                assert np.array_equal(x, y), one
     # a child count below the tree's: every read stops at depth 0 and the status reports it
     _, _, depth = ctx.beam_search_split(qbits, qn, p32, p16, pn, d_ptr, d_idx, roots, 6, 5, 0.0,
                                         max_children=maxc - 1)
