@@ -907,11 +907,15 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
         // ------------------------------------------------ producers: group g takes K blocks g, g + 2, ...
         // Row tid of A is this thread's entry.  The valid children's values of a K block are
         // groups of 4 (group 16 v + u: the item's v-th valid child, dims 4u..4u+3); group x
-        // goes to thread x mod 128, so the limb split is spread over the whole group.  Nothing
+        // goes to the thread with tb = x mod 128, so the limb split is spread over the whole
+        // group.  tb is tid rotated so that the groups past the first 128 (a warp that has any
+        // takes a second pass) fall to warp 1 or 6, not to the warps that share their SM
+        // sub-partition with the MMA issuer.  Nothing
         // is written for an unused row or child slot: an accumulator row or column depends only
         // on its own A row or B row, and the epilogue never reads those of unused ones.
         const int g = warp >> 2;
         const int tid = threadIdx.x & 127;
+        const int tb = (tid + (g ? 64 : 96)) & 127;
         const int ptid = threadIdx.x;  // 0..255: this thread's staging column
         int64_t& nbase = run.nbase;    // K blocks of the items before this one (the ring position)
         bool ok = true;
@@ -934,7 +938,7 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
             bool g16[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                const int x = tid + kTcE * i;
+                const int x = tb + kTcE * i;
                 gsrc[i] = reinterpret_cast<const char*>(a.proto);
                 gdst[i] = 0;
                 g16[i] = false;
@@ -959,7 +963,7 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
                         uint4* sb = staging + (size_t)slot * 5 * kTcProducers;
 #pragma unroll
                         for (int i = 0; i < 4; ++i)
-                            if (tid + kTcE * i < ngroups) {
+                            if (tb + kTcE * i < ngroups) {
                                 if (R16 && g16[i])
                                     cp_async8(sb + i * kTcProducers + ptid, gsrc[i] + kb * 128, 8);
                                 else
@@ -977,7 +981,7 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
                     const uint4* sb = staging + (size_t)slot * 5 * kTcProducers;
                     uint4 pv[4];
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) pv[j] = tid + kTcE * j < ngroups ? sb[j * kTcProducers + ptid] : make_uint4(0, 0, 0, 0);
+                    for (int j = 0; j < 4; ++j) pv[j] = tb + kTcE * j < ngroups ? sb[j * kTcProducers + ptid] : make_uint4(0, 0, 0, 0);
                     const uint2 w = rrow >= 0 ? *reinterpret_cast<const uint2*>(sb + 4 * kTcProducers + ptid) : make_uint2(0, 0);
                     issue(kb + 2 * kTcDepth, slot);  // the slot is free again: refill it kTcDepth blocks ahead
                     const int64_t n = nbase + kb;
@@ -1004,7 +1008,7 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
                     // bytes per limb)
 #pragma unroll
                     for (int j = 0; j < 4; ++j) {
-                        if (tid + kTcE * j >= ngroups) break;
+                        if (tb + kTcE * j >= ngroups) break;
                         int32_t l0[4], l1[4], l2[4];
                         int32_t x[4] = {(int32_t)pv[j].x, (int32_t)pv[j].y, (int32_t)pv[j].z, (int32_t)pv[j].w};
                         if (R16 && g16[j]) {  // four int16 values in the first 8 bytes
