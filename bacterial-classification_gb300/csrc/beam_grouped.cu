@@ -586,23 +586,39 @@ __global__ void select_output_kernel(const GArgs a, int L, int32_t* __restrict__
 constexpr int kTcE = 128;                                         // entries per item (TMEM lanes)
 constexpr int kTcC = 32;                                          // children per item (MMA N)
 constexpr int kTcLimbs = 3;
-constexpr int kTcStages = 4;  // even: each stage is always filled by the same producer group
-static_assert(kTcStages % 2 == 0, "producer groups alternate K blocks");
 // Each producer thread streams its own slice of a K block (16 prototype values, 64 bits of
 // its entry's read) with cp.async this many of its blocks ahead, into a private staging
 // area of shared memory ([slot][16-byte part][thread]: conflict-free), and converts it when
 // its copy group has landed.
 constexpr int kTcDepth = 4;
-constexpr int kTcProducers = 256;
-constexpr size_t kTcStageArea = (size_t)kTcDepth * 5 * kTcProducers * 16;  // 4 x 16 B values + 16 B bits
 constexpr int kTcAccCols = kTcLimbs * kTcC;                       // one accumulator set
 constexpr int kTcTmemCols = 512;                                  // two sets, then the A stages
 constexpr int kTcACol = 256;                                      // A of stage s: columns kTcACol + 32 s
-constexpr int kTcThreads = 416;                                   // warps 0-7 produce, 8-11 epilogue, 12 MMA
 constexpr int kTcBBytes = kTcC * 128;                             // per limb
 constexpr int kTcStageBytes = kTcLimbs * kTcBBytes;              // 12 KB of B (A is in TMEM)
-static_assert(kTcACol + 32 * kTcStages <= kTcTmemCols, "the A stages fit the TMEM allocation");
-constexpr size_t kTcSmem = (size_t)kTcStages * kTcStageBytes + kTcStageArea + 1024;
+constexpr int kTcMaxStages = 6;
+
+// The CTA of a tensor-core level with G producer groups of four warps (group g takes K blocks
+// g, g + G, ...): warps 0 .. 4G-1 produce, 4G .. 4G+3 run the epilogue, lane 0 of warp 4G+4
+// issues the MMAs.  A warp's registers come from its SM sub-partition's quarter of the file,
+// so 17 warps (G = 3: five on one sub-partition) get 96 registers a thread, 13 warps (G = 2)
+// 128: the level kernel takes three groups, the one-launch kernel, whose other phases need the
+// registers, two.
+template <int G>
+struct TcLayout {
+    static constexpr int kGroups = G;
+    static constexpr int kStages = 2 * G;  // two stages in flight per group
+    static constexpr int kProducers = 128 * G;
+    static constexpr size_t kStageArea = (size_t)kTcDepth * 5 * kProducers * 16;  // 4 x 16 B values + 16 B bits
+    static constexpr int kEpiWarp = 4 * G;
+    static constexpr int kMmaWarp = kEpiWarp + 4;
+    static constexpr int kThreads = 32 * (kMmaWarp + 1);
+    static constexpr size_t kSmem = (size_t)kStages * kTcStageBytes + kStageArea + 1024;
+    static_assert(kStages <= kTcMaxStages, "the barrier arrays hold every stage");
+    static_assert(kTcACol + 32 * kStages <= kTcTmemCols, "the A stages fit the TMEM allocation");
+};
+using TcLevel = TcLayout<3>;  // descent_tc_kernel: 544 threads
+using TcOne = TcLayout<2>;    // descent_one_kernel: 416 threads
 
 struct TcItems {
     int32_t* ent_read;    // [entries] grouped by parent
@@ -850,7 +866,7 @@ constexpr int kRowGroups = kRowConsumers / kQuarters;
 
 // Shared-memory state of the tensor-core scoring (one CTA per SM).
 struct TcShared {
-    uint64_t full_bar[kTcStages], empty_bar[kTcStages], accf_bar[2], acce_bar[2];
+    uint64_t full_bar[kTcMaxStages], empty_bar[kTcMaxStages], accf_bar[2], acce_bar[2];
     uint64_t drain_bar;  // the MMA issuer's last commit before TMEM is freed
     uint64_t row_full[kQuarters * kRowSlots], row_empty[kQuarters * kRowSlots];  // quarter q's ring: [q * kRowSlots, ..)
     uint32_t tmem_base;
@@ -867,11 +883,12 @@ struct TcRun {
 };
 
 // Barriers and the TMEM columns of the CTA (every thread calls it).
+template <class Lay>
 __device__ void tc_setup(TcShared& sm) {
     const int warp = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
         sm.err = 0;
-        for (int s = 0; s < kTcStages; ++s) {
+        for (int s = 0; s < Lay::kStages; ++s) {
             tc::mbar_init(&sm.full_bar[s], 4);  // one arrival per warp of the producer group
             tc::mbar_init(&sm.empty_bar[s], 1);
         }
@@ -886,7 +903,7 @@ __device__ void tc_setup(TcShared& sm) {
         }
         tc::fence_mbar_init();
     }
-    if (warp == 12) {
+    if (warp == Lay::kMmaWarp) {
         tc::tmem_alloc(&sm.tmem_base, kTcTmemCols);
         tc::tmem_relinquish();
     }
@@ -895,28 +912,29 @@ __device__ void tc_setup(TcShared& sm) {
     tc::fence_after();
 }
 
-// Scores the items of one level: warps 0-7 produce, 8-11 run the epilogue, lane 0 of warp 12
+// Scores the items of one level: warps 0-11 produce, 12-15 run the epilogue, lane 0 of warp 16
 // issues the MMAs.  Every thread of the CTA calls it; the items are blockIdx.x, + gridDim.x, ...
+template <class Lay>
 __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& run, uint8_t* ring, uint4* staging) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t tmem = sm.tmem_base;
     const int32_t n_items = t.item_off[a.n_nodes] + (t.small_off[a.n_nodes] + 1) / 2;
     const int kblocks = a.dim / 64;
 
-    if (warp < 8) {
-        // ------------------------------------------------ producers: group g takes K blocks g, g + 2, ...
+    if (warp < Lay::kEpiWarp) {
+        // ------------------------------------------------ producers: group g takes K blocks g, g + 3, ...
         // Row tid of A is this thread's entry.  The valid children's values of a K block are
         // groups of 4 (group 16 v + u: the item's v-th valid child, dims 4u..4u+3); group x
         // goes to the thread with tb = x mod 128, so the limb split is spread over the whole
         // group.  tb is tid rotated so that the groups past the first 128 (a warp that has any
-        // takes a second pass) fall to warp 1 or 6, not to the warps that share their SM
+        // takes a second pass) fall to warp 1, 6 or 11, not to the warps that share their SM
         // sub-partition with the MMA issuer.  Nothing
         // is written for an unused row or child slot: an accumulator row or column depends only
         // on its own A row or B row, and the epilogue never reads those of unused ones.
         const int g = warp >> 2;
         const int tid = threadIdx.x & 127;
-        const int tb = (tid + (g ? 64 : 96)) & 127;
-        const int ptid = threadIdx.x;  // 0..255: this thread's staging column
+        const int tb = (tid + 96 - 32 * g) & 127;
+        const int ptid = threadIdx.x;  // this thread's staging column
         int64_t& nbase = run.nbase;    // K blocks of the items before this one (the ring position)
         bool ok = true;
         for (int32_t it = blockIdx.x; ok && it < n_items; it += gridDim.x, nbase += kblocks) {
@@ -960,33 +978,33 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
                 constexpr bool R16 = decltype(rows16)::value;
                 auto issue = [&](int kb, int slot) {  // this thread's slices of K block kb, into staging slot `slot`
                     if (kb < kblocks) {
-                        uint4* sb = staging + (size_t)slot * 5 * kTcProducers;
+                        uint4* sb = staging + (size_t)slot * 5 * Lay::kProducers;
 #pragma unroll
                         for (int i = 0; i < 4; ++i)
                             if (tb + kTcE * i < ngroups) {
                                 if (R16 && g16[i])
-                                    cp_async8(sb + i * kTcProducers + ptid, gsrc[i] + kb * 128, 8);
+                                    cp_async8(sb + i * Lay::kProducers + ptid, gsrc[i] + kb * 128, 8);
                                 else
-                                    cp_async16(sb + i * kTcProducers + ptid, gsrc[i] + kb * 256, 16);
+                                    cp_async16(sb + i * Lay::kProducers + ptid, gsrc[i] + kb * 256, 16);
                             }
-                        if (rrow >= 0) cp_async8(sb + 4 * kTcProducers + ptid, bits_row + kb, 8);
+                        if (rrow >= 0) cp_async8(sb + 4 * Lay::kProducers + ptid, bits_row + kb, 8);
                     }
                     cp_async_commit();  // one group per call (possibly empty), so the wait below counts blocks
                 };
 #pragma unroll
-                for (int i = 0; i < kTcDepth; ++i) issue(g + 2 * i, i);
-                for (int kb = g, i = 0; kb < kblocks; kb += 2, ++i) {
+                for (int i = 0; i < kTcDepth; ++i) issue(g + Lay::kGroups * i, i);
+                for (int kb = g, i = 0; kb < kblocks; kb += Lay::kGroups, ++i) {
                     cp_async_wait<kTcDepth - 1>();  // this thread's copies of block kb have landed
                     const int slot = i % kTcDepth;
-                    const uint4* sb = staging + (size_t)slot * 5 * kTcProducers;
+                    const uint4* sb = staging + (size_t)slot * 5 * Lay::kProducers;
                     uint4 pv[4];
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) pv[j] = tb + kTcE * j < ngroups ? sb[j * kTcProducers + ptid] : make_uint4(0, 0, 0, 0);
-                    const uint2 w = rrow >= 0 ? *reinterpret_cast<const uint2*>(sb + 4 * kTcProducers + ptid) : make_uint2(0, 0);
-                    issue(kb + 2 * kTcDepth, slot);  // the slot is free again: refill it kTcDepth blocks ahead
+                    for (int j = 0; j < 4; ++j) pv[j] = tb + kTcE * j < ngroups ? sb[j * Lay::kProducers + ptid] : make_uint4(0, 0, 0, 0);
+                    const uint2 w = rrow >= 0 ? *reinterpret_cast<const uint2*>(sb + 4 * Lay::kProducers + ptid) : make_uint2(0, 0);
+                    issue(kb + Lay::kGroups * kTcDepth, slot);  // the slot is free again: refill it kTcDepth blocks ahead
                     const int64_t n = nbase + kb;
-                    const int stage = (int)(n % kTcStages);
-                    const uint32_t phase = (uint32_t)((n / kTcStages) & 1);
+                    const int stage = (int)(n % Lay::kStages);
+                    const uint32_t phase = (uint32_t)((n / Lay::kStages) & 1);
                     const bool got = tc::mbar_wait(&sm.empty_bar[stage], phase ^ 1, &sm.err, 11);
                     if (__any_sync(0xffffffffu, !got)) {
                         ok = false;
@@ -1046,7 +1064,7 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
                 body(std::false_type{});
         }
         cp_async_wait<0>();  // no copy may still be landing when the CTA leaves
-    } else if (warp < 12) {
+    } else if (warp < Lay::kMmaWarp) {
         // ------------------------------------------------ epilogue
         const int quarter = warp & 3, row = quarter * 32 + lane;
         int& acc = run.acc;
@@ -1121,7 +1139,7 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
                 for (int kk = 0; kk < 4; ++kk)
                     tc::mma_f16_ta(d, a_tm + 8 * kk, bdesc + 2 * kk, IDESC, (kb | kk) != 0 ? 1u : 0u);
                 tc::mma_commit(&sm.empty_bar[stage]);
-                if (++stage == kTcStages) {
+                if (++stage == Lay::kStages) {
                     stage = 0;
                     phase ^= 1;
                 }
@@ -1138,9 +1156,10 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
 
 // After the last scoring phase: wait (bounded) until every MMA this CTA issued has
 // completed, then free the TMEM columns and record a wait that gave up.
+template <class Lay>
 __device__ void tc_teardown(TcShared& sm, int* status) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (warp == 12 && lane == 0) {
+    if (warp == Lay::kMmaWarp && lane == 0) {
         tc::mma_commit(&sm.drain_bar);
         const long long c0 = clock64();
         while (!tc::mbar_try_wait(tc::smem_u32(&sm.drain_bar), 0) && clock64() - c0 < tc::kWaitCycles) {
@@ -1148,7 +1167,7 @@ __device__ void tc_teardown(TcShared& sm, int* status) {
     }
     tc::fence_before();
     __syncthreads();
-    if (warp == 12) {
+    if (warp == Lay::kMmaWarp) {
         tc::fence_after();
         tc::tmem_dealloc(sm.tmem_base, kTcTmemCols);
     }
@@ -1160,15 +1179,15 @@ __device__ __forceinline__ uint8_t* tc_ring(uint8_t* smem_raw) {
     return smem_raw + ((1024 - (raw_addr & 1023)) & 1023);
 }
 
-__global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a, const TcItems t) {
+__global__ void __launch_bounds__(TcLevel::kThreads, 1) descent_tc_kernel(const GArgs a, const TcItems t) {
     extern __shared__ uint8_t smem_raw[];
     __shared__ TcShared sm;
     uint8_t* ring = tc_ring(smem_raw);
-    uint4* staging = reinterpret_cast<uint4*>(ring + (size_t)kTcStages * kTcStageBytes);
-    tc_setup(sm);
+    uint4* staging = reinterpret_cast<uint4*>(ring + (size_t)TcLevel::kStages * kTcStageBytes);
+    tc_setup<TcLevel>(sm);
     TcRun run;
-    tc_phase(a, t, sm, run, ring, staging);
-    tc_teardown(sm, t.status);
+    tc_phase<TcLevel>(a, t, sm, run, ring, staging);
+    tc_teardown<TcLevel>(sm, t.status);
 }
 
 // ---------------------------------------------------------------- the whole descent in one launch
@@ -1180,10 +1199,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_tc_kernel(const GArgs a
 // scoring keeps its TMEM columns and mbarrier ring positions from one level to the next.
 
 constexpr int kCodeGridBarrier = 20;  // status 100 + this: a grid barrier gave up
-// Dynamic shared memory of the one-launch kernel: the tensor-core levels use the first kTcSmem
+// Dynamic shared memory of the one-launch kernel: the tensor-core levels use the first TcOne::kSmem
 // bytes; the streamed leaf level uses all of it (row slots + the consumers' bit buffers).
 constexpr size_t kOneSmem = 225 * 1024;
-static_assert(kOneSmem >= kTcSmem, "the one-launch kernel also runs the tensor-core levels");
+static_assert(kOneSmem >= TcOne::kSmem, "the one-launch kernel also runs the tensor-core levels");
 constexpr int kMaxPhaseTs = 64;       // phase timestamps kept of a launch (hdc_beam_phase_times)
 
 struct OneArgs {
@@ -1483,6 +1502,7 @@ __device__ void stream_phase(const GArgs& a, TcShared& sm, TcRun& run, uint8_t* 
     // into chunks of two consecutive pairs, chunk t going to group t % 3, so group g's k-th pair
     // is at position P0 + 2 g + 6 (k / 2) + k % 2; the two pairs of a chunk inside one node are
     // scored together from one read of the row.
+    if (warp > kRowConsumers) return;  // the CTA's warps past the consumers have no part here
     const int c = warp - 1, q = c % kQuarters, g = c / kQuarters;
     const int64_t P0 = a.node_off[n_lo], P1 = a.node_off[n_hi];
     const int64_t g0 = P0 + 2 * g;
@@ -1610,7 +1630,7 @@ __device__ void keys_from_parts(const GArgs& a, int64_t r0, int64_t r1) {
     }
 }
 
-__global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs a, const TcItems t, const OneArgs o) {
+__global__ void __launch_bounds__(TcOne::kThreads, 1) descent_one_kernel(const GArgs a, const TcItems t, const OneArgs o) {
     extern __shared__ uint8_t smem_raw[];
     __shared__ TcShared sm;
     __shared__ int32_t sh[32];
@@ -1621,9 +1641,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs 
         n_ts = 0;
         if (blockIdx.x == 0) o.phase_ts[n_ts++] = global_ns();
     }
-    uint4* staging = reinterpret_cast<uint4*>(ring + (size_t)kTcStages * kTcStageBytes);
+    uint4* staging = reinterpret_cast<uint4*>(ring + (size_t)TcOne::kStages * kTcStageBytes);
     if (o.use_tc) {
-        tc_setup(sm);
+        tc_setup<TcOne>(sm);
     } else {
         if (threadIdx.x == 0) sm.err = 0;
         __syncthreads();
@@ -1714,7 +1734,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs 
                 if (!(ok = grid_barrier(o, sm, &ok_s, &n_ts))) break;
             }
             // G: the level's pairs scored on the tensor cores
-            tc_phase(a, t, sm, run, ring, staging);
+            tc_phase<TcOne>(a, t, sm, run, ring, staging);
         } else {
             // C: pairs per node, summed per CTA
             sum = cta_sum(a.node_cnt, n0, n1, sh);
@@ -1758,7 +1778,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs 
         for (int i = n_ts; i < kMaxPhaseTs; ++i) o.phase_ts[i] = 0;
     }
     if (o.use_tc) {
-        tc_teardown(sm, o.status);
+        tc_teardown<TcOne>(sm, o.status);
     } else if (tid == 0 && sm.err) {
         atomicCAS(o.status, 0, 100 + sm.err);
     }
@@ -1767,13 +1787,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) descent_one_kernel(const GArgs 
 // The one-launch descent needs every CTA (one per SM) resident at once; checked once per
 // context, with the kernel's shared memory set.
 bool one_launch_fits(hdc_context* ctx) {
-    if (ctx->beam_one == 0) return false;
+    if (ctx->beam_one <= 0) return false;  // automatic: kernels per level (the fastest form here)
     if (ctx->beam_one_fit < 0) {
         int per_sm = 0;
         cudaError_t e = cudaFuncSetAttribute(descent_one_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)kOneSmem);
         if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, descent_one_kernel, kTcThreads, kOneSmem);
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, descent_one_kernel, TcOne::kThreads, kOneSmem);
         int coop = 0;
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device);
         cudaGetLastError();
@@ -1926,12 +1946,12 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
             }
         }
         o.phase_ts = ctx->d_phase_ts;
-        o.leaf_apart = ctx->beam_one != 1 ? 1 : 0;  // automatic: the last level in its own kernel
+        o.leaf_apart = ctx->beam_one == 2 ? 1 : 0;
         e = cudaMemsetAsync(one_state, 0, 4 * sizeof(uint32_t), stream);
         void* args[] = {(void*)&a, (void*)&t, (void*)&o};
         if (e == cudaSuccess)
             e = cudaLaunchCooperativeKernel((const void*)descent_one_kernel, dim3((unsigned)ctx->num_sms),
-                                            dim3(kTcThreads), args, kOneSmem, stream);
+                                            dim3(TcOne::kThreads), args, kOneSmem, stream);
         if (e == cudaSuccess && o.leaf_apart) {
             if (n32 < n_nodes)
                 leaf_score_kernel<true><<<ctx->num_sms * kScoreBlocks16, kScoreThreads, 0, stream>>>(a, o.abort);
@@ -1955,7 +1975,7 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
     const int work_grid = ctx->num_sms * 8;
     const unsigned nb = (unsigned)((n_nodes + 255) / 256);
     if (use_tc && (e = cudaFuncSetAttribute(descent_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)kTcSmem)) != cudaSuccess) {
+                                            (int)TcLevel::kSmem)) != cudaSuccess) {
         cudaFreeAsync(ws, stream);
         return cuda_fail(e, "beam: tensor-core scoring setup");
     }
@@ -1981,7 +2001,7 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
                 exclusive_scan(t.small, t.small_off, n_nodes, d_sums, stream);
                 item_write_kernel<<<nb, 256, 0, stream>>>(a, t);
             }
-            descent_tc_kernel<<<ctx->num_sms, kTcThreads, kTcSmem, stream>>>(a, t);
+            descent_tc_kernel<<<ctx->num_sms, TcLevel::kThreads, TcLevel::kSmem, stream>>>(a, t);
         } else {
             exclusive_scan(a.node_cnt, a.node_off, n_nodes, d_sums, stream);
             cudaMemcpyAsync(a.cursor, a.node_off, (size_t)n_nodes * 4, cudaMemcpyDeviceToDevice, stream);

@@ -634,7 +634,7 @@ def run_descent(args, cfg):
         per_step = 2
     elif args.beam_one == 1:  # every level in one cooperative launch
         per_step = 2
-    elif args.beam_one != 0:  # the cooperative launch up to the leaf pairs, then leaf scoring and select (default)
+    elif args.beam_one == 2:  # the cooperative launch up to the leaf pairs, then leaf scoring and select
         per_step = 4
     elif tc_levels and L > 1:
         per_step = 1 + 3 + 6 * L + 2 + 14 * (L - 2) + 5
@@ -1185,8 +1185,8 @@ def main():
     ap.add_argument("--beam-grouped", type=int, default=-1,
                     help="descent: 1 reads grouped by candidate node, 0 one warp per read (-1: default)")
     ap.add_argument("--beam-one", type=int, default=-1,
-                    help="descent: 1 every level in one launch, 2 one launch up to the leaf pairs + a leaf kernel, "
-                         "0 kernels per level (-1: default, 2)")
+                    help="descent: 1 every level in one launch, 2 one launch up to the leaf pairs + leaf kernels, "
+                         "0 kernels per level (-1: the library default, 0)")
     ap.add_argument("--score-mode", default="norm", choices=["norm", "cos", "dot"],
                     help="score of the top-k search (default the reference's NORM scale; the CPU legs need it)")
     ap.add_argument("--aux-scale", type=float, default=1.0,
@@ -1194,6 +1194,8 @@ def main():
     ap.add_argument("--proto-int32", action="store_true",
                     help="descent: every prototype row int32 (default: int16 rows from the first node whose rows fit)")
     args = ap.parse_args()
+    if args.beam_one < 0:  # the library's automatic descent form: kernels per level
+        args.beam_one = 0
     if args.warmup < 3:
         log("warmup raised to 3")
         args.warmup = 3

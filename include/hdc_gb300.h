@@ -318,8 +318,9 @@ int hdc_search_tc_last_shape(const hdc_context* ctx, int32_t shape[5]);
                               last level's node-ordered pairs, which a second kernel scores
                               (more warps per SM than the cooperative launch holds) and a third
                               selects from (one warp per read); 0 a sequence of kernels per
-                              level; -1 automatic (2 where the cooperative CTAs all fit);
-                              results are identical */
+                              level, whose tensor-core kernel has more producer warps than the
+                              cooperative CTA can hold (the fastest at D = 16,384); -1
+                              automatic (0); results are identical */
 #define HDC_WAIT_LIMIT 9   /* tensor-core search: its bounded device-side waits give up after
                               value x 1,000 SM cycles, 1 .. 4,000,000 (0: the default,
                               4,000,000, about 2 s at 2 GHz); a wait that gives up makes the
