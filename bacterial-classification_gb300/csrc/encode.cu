@@ -9,20 +9,24 @@
 // byte outside "ACGT"; src/HV.cpp:156-216 accumulates +1/-1 per bit).
 //
 // GB300 design
-//   * One warp owns 32 consecutive 32-bit words of the hypervector (a 1024-dim
-//     "slab"); lane l owns word l.  A CTA serves one slab for many segments,
-//     so the slab's lookup tables are built once per CTA and reused.
+//   * One warp owns 32 W consecutive 32-bit words of the hypervector (a
+//     1024 W-dim "slab"); lane l owns words W l .. W l + W - 1.  A CTA serves
+//     one slab for many segments, so the slab's lookup tables are built once
+//     per CTA and reused.  W = 2 where its table fits shared memory (every
+//     k <= 14): the per-position work (entry load, row addresses, k-mer
+//     staging) is then shared by two words.
 //   * The canonical k-mer's digits are split into parts of <= 4 digits.  For
 //     each part the CTA keeps in shared memory a table of all 4^len
 //     pre-rotated, pre-XORed binder fragments restricted to the slab; part 0
 //     also carries the all-ones start value.  A binder word is the XOR of
-//     one 128-byte table row per part (conflict-free: the 32 lanes read the
-//     32 words of one row).
-//   * Per chunk of 256 positions each lane computes 8 canonical k-mers with
-//     a rolling 2-bit code (revcomp = bitwise NOT of the little-endian code,
-//     forward = digit reversal), and writes one packed entry of table row
-//     offsets per position.  Invalid k-mers and the chunk tail point at an
-//     all-zero row, which contributes nothing.
+//     one 128 W-byte table row per part (conflict-free: the 32 lanes read the
+//     32 W words of one row).
+//   * Per chunk of kChunk positions each lane computes kChunk / 32 canonical
+//     k-mers with a rolling 2-bit code (revcomp = bitwise NOT of the
+//     little-endian code, forward = digit reversal), and writes one entry per
+//     position: the byte offsets of its table rows, so a row's address is one
+//     add.  Invalid k-mers and the chunk tail point at an all-zero row, which
+//     contributes nothing.
 //   * Bundling never unpacks bits: 16 binder words are reduced by a
 //     carry-save adder tree into bit-sliced counters (ones/twos/fours/eights
 //     plus NH higher planes), ~2 logic ops per word; counts are extracted
@@ -36,10 +40,12 @@
 namespace hdc {
 namespace {
 
-constexpr int kWarps = 8;
+constexpr int kWarps = 16;
 constexpr int kThreads = kWarps * 32;
-constexpr int kChunk = 256;  // positions per staged chunk: 8 per lane
+constexpr int kChunk = 64;  // positions per staged chunk
+constexpr int kPerLane = kChunk / 32;
 constexpr int kMaxParts = 4;
+constexpr size_t kMaxEncodeSmem = 227 * 1024;  // dynamic shared memory a CTA may opt into
 
 struct EncodeArgs {
     const uint32_t* base32;  // [4][W32], A,C,G,T
@@ -102,36 +108,167 @@ __device__ __forceinline__ uint32_t is_base(uint32_t c) {
     return (c == 'A') | (c == 'C') | (c == 'G') | (c == 'T');
 }
 
-template <int NP>
-__device__ __forceinline__ uint64_t pack_entry(const EncodeArgs& a, uint32_t canon) {
-    uint64_t e = 0;
+// A position's table rows, one per digit part, as byte offsets from the start of the table
+// (parts past NP and invalid k-mers point at the all-zero row).
+template <int NP, int W>
+__device__ __forceinline__ uint4 pack_entry(const EncodeArgs& a, uint32_t canon) {
+    constexpr uint32_t kRowBytes = 128u * W;
+    uint32_t f[kMaxParts];
 #pragma unroll
     for (int p = 0; p < kMaxParts; ++p) {
-        uint32_t row;
+        uint32_t row = (uint32_t)a.zero_row;
         if (p < NP) {
-            int len = a.part_len[p];
-            int shift = 2 * (a.k - a.part_first[p] - len);
-            uint32_t sub = (canon >> shift) & ((1u << (2 * len)) - 1u);
-            row = (uint32_t)a.part_row0[p] + sub;
-        } else {
-            row = (uint32_t)a.zero_row;
+            const int len = a.part_len[p];
+            const int shift = 2 * (a.k - a.part_first[p] - len);
+            row = (uint32_t)a.part_row0[p] + ((canon >> shift) & ((1u << (2 * len)) - 1u));
         }
-        e |= (uint64_t)(row * 32u) << (16 * p);
+        f[p] = row * kRowBytes;
     }
-    return e;
+    return make_uint4(f[0], f[1], f[2], f[3]);
 }
 
-template <int NP, int NH>
+// W consecutive words of a table row from shared memory (32-bit shared address)
+template <int W>
+__device__ __forceinline__ void lds_words(uint32_t addr, uint32_t (&v)[W]) {
+    if constexpr (W == 1) {
+        asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v[0]) : "r"(addr));
+    } else {
+        asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];" : "=r"(v[0]), "=r"(v[1]) : "r"(addr));
+    }
+}
+
+// One word of a segment's output from its bit-sliced counters (planes: ones, twos, fours,
+// eights, then hi[0 .. NH)); w32 is the word's index in the row.
+template <int NH>
+__device__ __forceinline__ void write_word(const EncodeArgs& a, int64_t seg, int w32, int nvalid, uint32_t ones,
+                                           uint32_t twos, uint32_t fours, uint32_t eights, const uint32_t (&hi)[NH]) {
+    if (a.out_kind == HDC_OUT_SIGN_BITS) {
+        // a row has ceil(dim / 32) words: a word that starts at or past dim writes nothing
+        // (the ring of 64-bit words can hold one more 32-bit word than that)
+        if (w32 * 32 >= a.dim) return;
+        // 2 count - nvalid >= 0, i.e. count >= ceil(nvalid / 2), compared plane by plane
+        // from the most significant: gt = lanes already above, eq = equal so far
+        const uint32_t thr = (uint32_t)(nvalid + 1) >> 1;
+        uint32_t gt = 0, eq = 0xffffffffu;
+        auto cmp = [&](uint32_t plane, int bit) {
+            if ((thr >> bit) & 1u) {
+                eq &= plane;
+            } else {
+                gt |= eq & plane;
+                eq &= ~plane;
+            }
+        };
+#pragma unroll
+        for (int h = NH - 1; h >= 0; --h) cmp(hi[h], 4 + h);
+        cmp(eights, 3);
+        cmp(fours, 2);
+        cmp(twos, 1);
+        cmp(ones, 0);
+        uint32_t bits = gt | eq;
+        const int nd = min(32, a.dim - w32 * 32);
+        if (nd < 32) bits &= (1u << nd) - 1u;
+        reinterpret_cast<uint32_t*>(a.out)[seg * a.out_stride + w32] = bits;
+        return;
+    }
+
+    // ---- counts -> output values, dims b and b+16 in 16-bit fields ----
+    uint32_t val[32];
+#pragma unroll
+    for (int b = 0; b < 16; ++b) {
+        const uint32_t M = 0x00010001u;
+        uint32_t v = ((ones >> b) & M) + (((twos >> b) & M) << 1) + (((fours >> b) & M) << 2) +
+                     (((eights >> b) & M) << 3);
+#pragma unroll
+        for (int h = 0; h < NH; ++h) v += ((hi[h] >> b) & M) << (4 + h);
+        val[b] = v & 0xffffu;
+        val[b + 16] = v >> 16;
+    }
+    const int dbase = w32 * 32;
+    const int nd = min(32, a.dim - dbase);
+    char* rowp = static_cast<char*>(a.out);
+    if (a.out_kind == HDC_OUT_I32) {
+        int32_t* o = reinterpret_cast<int32_t*>(rowp) + seg * a.out_stride + dbase;
+        if (nd == 32 && ((reinterpret_cast<uintptr_t>(o) & 15) == 0)) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                int4 v4;
+                v4.x = 2 * (int)val[4 * q + 0] - nvalid;
+                v4.y = 2 * (int)val[4 * q + 1] - nvalid;
+                v4.z = 2 * (int)val[4 * q + 2] - nvalid;
+                v4.w = 2 * (int)val[4 * q + 3] - nvalid;
+                reinterpret_cast<int4*>(o)[q] = v4;
+            }
+        } else {
+#pragma unroll
+            for (int b = 0; b < 32; ++b)
+                if (b < nd) o[b] = 2 * (int)val[b] - nvalid;
+        }
+    } else if (a.out_kind == HDC_OUT_BIPOLAR_I8) {
+        int8_t* o = reinterpret_cast<int8_t*>(rowp) + seg * a.out_stride + dbase;
+        uint32_t pk[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            pk[q] = 0;
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+                pk[q] |= (2 * (int)val[4 * q + t] - nvalid >= 0 ? 0x01u : 0xffu) << (8 * t);
+        }
+        if (nd == 32 && ((reinterpret_cast<uintptr_t>(o) & 15) == 0)) {
+            reinterpret_cast<uint4*>(o)[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            reinterpret_cast<uint4*>(o)[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+        } else {
+#pragma unroll
+            for (int b = 0; b < 32; ++b)
+                if (b < nd) o[b] = (int8_t)(pk[b >> 2] >> (8 * (b & 3)));
+        }
+    } else {
+        uint16_t* o = reinterpret_cast<uint16_t*>(rowp) + seg * a.out_stride + dbase;
+        uint32_t pk[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            uint32_t h2[2];
+#pragma unroll
+            for (int t = 0; t < 2; ++t) {
+                const int v = 2 * (int)val[2 * q + t] - nvalid;
+                if (a.out_kind == HDC_OUT_I16)
+                    h2[t] = (uint32_t)v & 0xffffu;
+                else if (a.out_kind == HDC_OUT_BIPOLAR_I16)
+                    h2[t] = v >= 0 ? 0x0001u : 0xffffu;
+                else if (a.out_kind == HDC_OUT_BIPOLAR_F16)
+                    h2[t] = v >= 0 ? 0x3c00u : 0xbc00u;  // fp16 +1 / -1
+                else if (a.out_kind == HDC_OUT_F16)
+                    h2[t] = __half_as_ushort(__int2half_rn(v));  // exact: |v| <= 2048
+                else
+                    h2[t] = v >= 0 ? 0x3f80u : 0xbf80u;  // bf16 +1 / -1
+            }
+            pk[q] = h2[0] | (h2[1] << 16);
+        }
+        if (nd == 32 && ((reinterpret_cast<uintptr_t>(o) & 15) == 0)) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                reinterpret_cast<uint4*>(o)[q] = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
+        } else {
+#pragma unroll
+            for (int b = 0; b < 32; ++b)
+                if (b < nd) o[b] = (uint16_t)(pk[b >> 1] >> (16 * (b & 1)));
+        }
+    }
+}
+
+// W: words a lane owns (a slab is 32 W words; W = 2 halves the per-position work of the
+// entries, addresses and k-mer staging per word, where the wider table fits shared memory)
+template <int NP, int NH, int W>
 __global__ void __launch_bounds__(kThreads) encode_kernel(const EncodeArgs a) {
     extern __shared__ __align__(16) uint32_t smem[];
-    uint32_t* table = smem;  // [table_rows][32]
-    uint64_t* lists = reinterpret_cast<uint64_t*>(smem + a.table_rows * 32);
+    constexpr int SW = 32 * W;  // words per slab
+    uint32_t* table = smem;     // [table_rows][SW]
+    uint4* lists = reinterpret_cast<uint4*>(smem + a.table_rows * SW);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int slab = blockIdx.y;
 
     // ---- lookup tables for this slab ----
-    for (int e = threadIdx.x; e < a.table_rows * 32; e += kThreads) {
-        const int row = e >> 5, w = slab * 32 + (e & 31);
+    for (int e = threadIdx.x; e < a.table_rows * SW; e += kThreads) {
+        const int row = e / SW, w = slab * SW + (e % SW);
         uint32_t v = 0;
         if (row < a.zero_row && w < a.W32) {
             int p = 0;
@@ -149,13 +286,14 @@ __global__ void __launch_bounds__(kThreads) encode_kernel(const EncodeArgs a) {
     }
     __syncthreads();
 
-    const uint32_t* trow = table + lane;
-    uint64_t* list = lists + warp * kChunk;
-    const uint64_t zero_entry = pack_entry<0>(a, 0);
+    // this lane's words of table row 0 (a row's W lane words are contiguous)
+    const uint32_t tbase = (uint32_t)__cvta_generic_to_shared(table) + 4u * W * lane;
+    uint4* list = lists + warp * kChunk;
+    const uint4 zero_entry = pack_entry<0, W>(a, 0);
     const int k = a.k;
     const uint32_t mask2k = k == 16 ? 0xffffffffu : ((1u << (2 * k)) - 1u);
     const int64_t gw = (int64_t)blockIdx.x * kWarps + warp, nw = (int64_t)gridDim.x * kWarps;
-    const int w32 = slab * 32 + lane;
+    const int w0 = slab * SW + W * lane;  // this lane's first word
 
     int64_t next = gw;
     if (a.queue) {
@@ -170,15 +308,19 @@ __global__ void __launch_bounds__(kThreads) encode_kernel(const EncodeArgs a) {
         get_segment(a, seg, start, len);
         const unsigned char* s = a.words ? nullptr : a.bytes + start;
         const int npos = len >= k ? len - k + 1 : 0;
-        uint32_t ones = 0, twos = 0, fours = 0, eights = 0;
-        uint32_t hi[NH];
+        uint32_t ones[W], twos[W], fours[W], eights[W];
+        uint32_t hi[W][NH];
 #pragma unroll
-        for (int h = 0; h < NH; ++h) hi[h] = 0;
+        for (int i = 0; i < W; ++i) {
+            ones[i] = twos[i] = fours[i] = eights[i] = 0;
+#pragma unroll
+            for (int h = 0; h < NH; ++h) hi[i][h] = 0;
+        }
         int nvalid = 0;
 
         for (int c0 = 0; c0 < npos; c0 += kChunk) {
-            // ---- stage 8 canonical k-mers per lane ----
-            const int p0 = c0 + lane * 8;
+            // ---- stage kPerLane canonical k-mers per lane ----
+            const int p0 = c0 + lane * kPerLane;
             uint32_t x = 0, m = 0;
             auto push = [&](int pos) {
                 uint32_t code, inv;
@@ -196,56 +338,75 @@ __global__ void __launch_bounds__(kThreads) encode_kernel(const EncodeArgs a) {
             };
             for (int j = 0; j < k - 1; ++j) push(p0 + j);
 #pragma unroll
-            for (int r = 0; r < 8; ++r) {
+            for (int r = 0; r < kPerLane; ++r) {
                 push(p0 + r + k - 1);
-                uint64_t e = zero_entry;
+                uint4 e = zero_entry;
                 if (p0 + r < npos && m == 0) {
                     uint32_t rc = ~x & mask2k;
                     uint32_t y = __brev(x) >> (32 - 2 * k);
                     uint32_t fw = ((y & 0x55555555u) << 1) | ((y >> 1) & 0x55555555u);
-                    e = pack_entry<NP>(a, fw < rc ? fw : rc);
+                    e = pack_entry<NP, W>(a, fw < rc ? fw : rc);
                     ++nvalid;
                 }
-                list[lane * 8 + r] = e;
+                list[lane * kPerLane + r] = e;
             }
             __syncwarp();
 
             // ---- bundle: binder words through a carry-save adder tree ----
             const int groups = (min(kChunk, npos - c0) + 15) >> 4;
             for (int g = 0; g < groups; ++g) {
-                uint32_t xw[16];
+                uint32_t xw[W][16];
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
-                    const uint64_t e = list[g * 16 + j];
-                    const uint32_t lo = (uint32_t)e, hw = (uint32_t)(e >> 32);
-                    uint32_t v = trow[lo & 0xffffu];
-                    if (NP > 1) v ^= trow[lo >> 16];
-                    if (NP > 2) v ^= trow[hw & 0xffffu];
-                    if (NP > 3) v ^= trow[hw >> 16];
-                    xw[j] = v;
-                }
-                uint32_t twosA, twosB, foursA, foursB, eightsA, eightsB, sixteens;
-                csa(twosA, ones, ones, xw[0], xw[1]);
-                csa(twosB, ones, ones, xw[2], xw[3]);
-                csa(foursA, twos, twos, twosA, twosB);
-                csa(twosA, ones, ones, xw[4], xw[5]);
-                csa(twosB, ones, ones, xw[6], xw[7]);
-                csa(foursB, twos, twos, twosA, twosB);
-                csa(eightsA, fours, fours, foursA, foursB);
-                csa(twosA, ones, ones, xw[8], xw[9]);
-                csa(twosB, ones, ones, xw[10], xw[11]);
-                csa(foursA, twos, twos, twosA, twosB);
-                csa(twosA, ones, ones, xw[12], xw[13]);
-                csa(twosB, ones, ones, xw[14], xw[15]);
-                csa(foursB, twos, twos, twosA, twosB);
-                csa(eightsB, fours, fours, foursA, foursB);
-                csa(sixteens, eights, eights, eightsA, eightsB);
-                uint32_t carry = sixteens;
+                    const uint4 e = list[g * 16 + j];
+                    uint32_t v[W];
+                    lds_words<W>(tbase + e.x, v);
+                    if (NP > 1) {
+                        uint32_t u[W];
+                        lds_words<W>(tbase + e.y, u);
 #pragma unroll
-                for (int h = 0; h < NH; ++h) {
-                    const uint32_t t = hi[h] & carry;
-                    hi[h] ^= carry;
-                    carry = t;
+                        for (int i = 0; i < W; ++i) v[i] ^= u[i];
+                    }
+                    if (NP > 2) {
+                        uint32_t u[W];
+                        lds_words<W>(tbase + e.z, u);
+#pragma unroll
+                        for (int i = 0; i < W; ++i) v[i] ^= u[i];
+                    }
+                    if (NP > 3) {
+                        uint32_t u[W];
+                        lds_words<W>(tbase + e.w, u);
+#pragma unroll
+                        for (int i = 0; i < W; ++i) v[i] ^= u[i];
+                    }
+#pragma unroll
+                    for (int i = 0; i < W; ++i) xw[i][j] = v[i];
+                }
+#pragma unroll
+                for (int i = 0; i < W; ++i) {
+                    uint32_t twosA, twosB, foursA, foursB, eightsA, eightsB, sixteens;
+                    csa(twosA, ones[i], ones[i], xw[i][0], xw[i][1]);
+                    csa(twosB, ones[i], ones[i], xw[i][2], xw[i][3]);
+                    csa(foursA, twos[i], twos[i], twosA, twosB);
+                    csa(twosA, ones[i], ones[i], xw[i][4], xw[i][5]);
+                    csa(twosB, ones[i], ones[i], xw[i][6], xw[i][7]);
+                    csa(foursB, twos[i], twos[i], twosA, twosB);
+                    csa(eightsA, fours[i], fours[i], foursA, foursB);
+                    csa(twosA, ones[i], ones[i], xw[i][8], xw[i][9]);
+                    csa(twosB, ones[i], ones[i], xw[i][10], xw[i][11]);
+                    csa(foursA, twos[i], twos[i], twosA, twosB);
+                    csa(twosA, ones[i], ones[i], xw[i][12], xw[i][13]);
+                    csa(twosB, ones[i], ones[i], xw[i][14], xw[i][15]);
+                    csa(foursB, twos[i], twos[i], twosA, twosB);
+                    csa(eightsB, fours[i], fours[i], foursA, foursB);
+                    csa(sixteens, eights[i], eights[i], eightsA, eightsB);
+                    uint32_t carry = sixteens;
+#pragma unroll
+                    for (int h = 0; h < NH; ++h) {
+                        const uint32_t t = hi[i][h] & carry;
+                        hi[i][h] ^= carry;
+                        carry = t;
+                    }
                 }
             }
             __syncwarp();
@@ -260,128 +421,18 @@ __global__ void __launch_bounds__(kThreads) encode_kernel(const EncodeArgs a) {
         } else {
             pos_q += nw;
         }
-        if (w32 >= a.W32) continue;
-
-        if (a.out_kind == HDC_OUT_SIGN_BITS) {
-            // a row has ceil(dim / 32) words: a lane whose word starts at or past dim writes nothing
-            // (the ring of 64-bit words can hold one more 32-bit word than that)
-            if (w32 * 32 >= a.dim) continue;
-            // 2 count - nvalid >= 0, i.e. count >= ceil(nvalid / 2), compared plane by plane
-            // from the most significant: gt = lanes already above, eq = equal so far
-            const uint32_t thr = (uint32_t)(nvalid + 1) >> 1;
-            uint32_t gt = 0, eq = 0xffffffffu;
-            auto cmp = [&](uint32_t plane, int bit) {
-                if ((thr >> bit) & 1u) {
-                    eq &= plane;
-                } else {
-                    gt |= eq & plane;
-                    eq &= ~plane;
-                }
-            };
 #pragma unroll
-            for (int h = NH - 1; h >= 0; --h) cmp(hi[h], 4 + h);
-            cmp(eights, 3);
-            cmp(fours, 2);
-            cmp(twos, 1);
-            cmp(ones, 0);
-            uint32_t bits = gt | eq;
-            const int nd = min(32, a.dim - w32 * 32);
-            if (nd < 32) bits &= (1u << nd) - 1u;
-            reinterpret_cast<uint32_t*>(a.out)[seg * a.out_stride + w32] = bits;
-            continue;
-        }
-
-        // ---- counts -> output values, dims b and b+16 in 16-bit fields ----
-        uint32_t val[32];
-#pragma unroll
-        for (int b = 0; b < 16; ++b) {
-            const uint32_t M = 0x00010001u;
-            uint32_t v = ((ones >> b) & M) + (((twos >> b) & M) << 1) + (((fours >> b) & M) << 2) +
-                         (((eights >> b) & M) << 3);
-#pragma unroll
-            for (int h = 0; h < NH; ++h) v += ((hi[h] >> b) & M) << (4 + h);
-            val[b] = v & 0xffffu;
-            val[b + 16] = v >> 16;
-        }
-        const int dbase = w32 * 32;
-        const int nd = min(32, a.dim - dbase);
-        char* rowp = static_cast<char*>(a.out);
-        if (a.out_kind == HDC_OUT_I32) {
-            int32_t* o = reinterpret_cast<int32_t*>(rowp) + seg * a.out_stride + dbase;
-            if (nd == 32 && ((reinterpret_cast<uintptr_t>(o) & 15) == 0)) {
-#pragma unroll
-                for (int q = 0; q < 8; ++q) {
-                    int4 v4;
-                    v4.x = 2 * (int)val[4 * q + 0] - nvalid;
-                    v4.y = 2 * (int)val[4 * q + 1] - nvalid;
-                    v4.z = 2 * (int)val[4 * q + 2] - nvalid;
-                    v4.w = 2 * (int)val[4 * q + 3] - nvalid;
-                    reinterpret_cast<int4*>(o)[q] = v4;
-                }
-            } else {
-#pragma unroll
-                for (int b = 0; b < 32; ++b)
-                    if (b < nd) o[b] = 2 * (int)val[b] - nvalid;
-            }
-        } else if (a.out_kind == HDC_OUT_BIPOLAR_I8) {
-            int8_t* o = reinterpret_cast<int8_t*>(rowp) + seg * a.out_stride + dbase;
-            uint32_t pk[8];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                pk[q] = 0;
-#pragma unroll
-                for (int t = 0; t < 4; ++t)
-                    pk[q] |= (2 * (int)val[4 * q + t] - nvalid >= 0 ? 0x01u : 0xffu) << (8 * t);
-            }
-            if (nd == 32 && ((reinterpret_cast<uintptr_t>(o) & 15) == 0)) {
-                reinterpret_cast<uint4*>(o)[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-                reinterpret_cast<uint4*>(o)[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
-            } else {
-#pragma unroll
-                for (int b = 0; b < 32; ++b)
-                    if (b < nd) o[b] = (int8_t)(pk[b >> 2] >> (8 * (b & 3)));
-            }
-        } else {
-            uint16_t* o = reinterpret_cast<uint16_t*>(rowp) + seg * a.out_stride + dbase;
-            uint32_t pk[16];
-#pragma unroll
-            for (int q = 0; q < 16; ++q) {
-                uint32_t h2[2];
-#pragma unroll
-                for (int t = 0; t < 2; ++t) {
-                    const int v = 2 * (int)val[2 * q + t] - nvalid;
-                    if (a.out_kind == HDC_OUT_I16)
-                        h2[t] = (uint32_t)v & 0xffffu;
-                    else if (a.out_kind == HDC_OUT_BIPOLAR_I16)
-                        h2[t] = v >= 0 ? 0x0001u : 0xffffu;
-                    else if (a.out_kind == HDC_OUT_BIPOLAR_F16)
-                        h2[t] = v >= 0 ? 0x3c00u : 0xbc00u;  // fp16 +1 / -1
-                    else if (a.out_kind == HDC_OUT_F16)
-                        h2[t] = __half_as_ushort(__int2half_rn(v));  // exact: |v| <= 2048
-                    else
-                        h2[t] = v >= 0 ? 0x3f80u : 0xbf80u;  // bf16 +1 / -1
-                }
-                pk[q] = h2[0] | (h2[1] << 16);
-            }
-            if (nd == 32 && ((reinterpret_cast<uintptr_t>(o) & 15) == 0)) {
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    reinterpret_cast<uint4*>(o)[q] = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
-            } else {
-#pragma unroll
-                for (int b = 0; b < 32; ++b)
-                    if (b < nd) o[b] = (uint16_t)(pk[b >> 1] >> (16 * (b & 1)));
-            }
-        }
+        for (int i = 0; i < W; ++i)
+            if (w0 + i < a.W32) write_word<NH>(a, seg, w0 + i, nvalid, ones[i], twos[i], fours[i], eights[i], hi[i]);
     }
 }
 
 // The grid: every slab served by the same number of CTAs, all of them resident at once (one
 // wave).  Each warp takes a fixed share of the segments, so a CTA that had to wait for a free
 // SM would run its whole share after the others finished: the call would take two CTA times.
-template <int NP, int NH>
+template <int NP, int NH, int W>
 int launch_np_nh(const hdc_context* ctx, const EncodeArgs& a, int n_slabs, size_t smem, cudaStream_t stream) {
-    auto kern = encode_kernel<NP, NH>;
+    auto kern = encode_kernel<NP, NH, W>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_fail(e, "encode: cudaFuncSetAttribute");
     int per_sm = 0;
@@ -396,15 +447,30 @@ int launch_np_nh(const hdc_context* ctx, const EncodeArgs& a, int n_slabs, size_
     return e == cudaSuccess ? HDC_OK : cuda_fail(e, "encode: launch");
 }
 
+// Shared memory of a CTA whose lanes own W words: the slab's table rows and the warps' lists
+size_t encode_smem(const EncodeArgs& a, int w) {
+    return (size_t)a.table_rows * 32 * w * 4 + (size_t)kWarps * kChunk * sizeof(uint4);
+}
+
+// Two words a lane where that table fits a CTA's shared memory, else one
 template <int NP>
-int launch_np(const hdc_context* ctx, const EncodeArgs& a, int nh, int n_slabs, size_t smem, cudaStream_t stream) {
-    if (nh <= 4) return launch_np_nh<NP, 4>(ctx, a, n_slabs, smem, stream);
-    if (nh <= 8) return launch_np_nh<NP, 8>(ctx, a, n_slabs, smem, stream);
-    return launch_np_nh<NP, 12>(ctx, a, n_slabs, smem, stream);
+int launch_np(const hdc_context* ctx, const EncodeArgs& a, int nh, cudaStream_t stream) {
+    const bool w2 = encode_smem(a, 2) <= kMaxEncodeSmem;
+    const int n_slabs = (a.W32 + 32 * (w2 ? 2 : 1) - 1) / (32 * (w2 ? 2 : 1));
+    const size_t smem = encode_smem(a, w2 ? 2 : 1);
+    if (w2) {
+        if (nh <= 4) return launch_np_nh<NP, 4, 2>(ctx, a, n_slabs, smem, stream);
+        if (nh <= 8) return launch_np_nh<NP, 8, 2>(ctx, a, n_slabs, smem, stream);
+        return launch_np_nh<NP, 12, 2>(ctx, a, n_slabs, smem, stream);
+    }
+    if (nh <= 4) return launch_np_nh<NP, 4, 1>(ctx, a, n_slabs, smem, stream);
+    if (nh <= 8) return launch_np_nh<NP, 8, 1>(ctx, a, n_slabs, smem, stream);
+    return launch_np_nh<NP, 12, 1>(ctx, a, n_slabs, smem, stream);
 }
 
 }  // namespace
 
+// the most slabs a call can have (one word a lane): the size of a work queue's counters
 int encode_slabs(const hdc_context* ctx) { return (ctx->words32 + 31) / 32; }
 
 namespace {
@@ -504,13 +570,11 @@ int launch_encode(hdc_context* ctx, const char* d_bytes, const int64_t* d_seg_of
     if (out_kind == HDC_OUT_F16 && max_nk > 2048)
         return fail(HDC_ERR_RANGE, "encode: fp16 counts are exact for segments of at most 2048 k-mers");
 
-    const int n_slabs = (a.W32 + 31) / 32;
-    const size_t smem = (size_t)a.table_rows * 32 * 4 + (size_t)kWarps * kChunk * 8;
     switch (np) {
-        case 1: return launch_np<1>(ctx, a, nh, n_slabs, smem, stream);
-        case 2: return launch_np<2>(ctx, a, nh, n_slabs, smem, stream);
-        case 3: return launch_np<3>(ctx, a, nh, n_slabs, smem, stream);
-        default: return launch_np<4>(ctx, a, nh, n_slabs, smem, stream);
+        case 1: return launch_np<1>(ctx, a, nh, stream);
+        case 2: return launch_np<2>(ctx, a, nh, stream);
+        case 3: return launch_np<3>(ctx, a, nh, stream);
+        default: return launch_np<4>(ctx, a, nh, stream);
     }
 }
 
