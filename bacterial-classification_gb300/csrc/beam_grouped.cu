@@ -543,28 +543,6 @@ __global__ void output_kernel(const GArgs a, int32_t* __restrict__ path, float* 
     output_one(a, r, path, path_score, depth);
 }
 
-// The last level scored apart from the one-launch descent, which stops once that level's
-// pairs are in node order: leaf_score_kernel scores them as score_kernel does (more warps per
-// SM than the cooperative launch holds), then select_output_kernel takes each read's final
-// beam and writes its output, one warp per read.  Neither runs when the descent gave up
-// (abort raised): its pair arrays are then incomplete.
-template <bool ROWS16>
-__global__ void __launch_bounds__(kScoreThreads, ROWS16 ? kScoreBlocks16 : kScoreBlocks)
-    leaf_score_kernel(const GArgs a, const int* __restrict__ abort) {
-    if (*abort) return;
-    score_pairs<ROWS16>(a, (((int64_t)blockIdx.x * blockDim.x) >> 5) + (threadIdx.x >> 5),
-                        ((int64_t)gridDim.x * blockDim.x) >> 5);
-}
-
-__global__ void select_output_kernel(const GArgs a, int L, int32_t* __restrict__ path, float* __restrict__ path_score,
-                                     int32_t* __restrict__ depth, const int* __restrict__ abort) {
-    const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (*abort || r >= a.nq) return;
-    select_warp(a, L, r, threadIdx.x & 31);
-    __syncwarp();
-    if ((threadIdx.x & 31) == 0) output_one(a, r, path, path_score, depth);
-}
-
 // ---------------------------------------------------------------- tensor-core scoring
 // Levels above the leaves score on the tensor cores, grouped by parent: the entries (read,
 // beam slot) whose beam row is node P are scored against P's children (a childless P
@@ -1218,7 +1196,7 @@ struct OneArgs {
     float* out_score;
     int32_t* out_depth;
     unsigned long long* phase_ts;  // [kMaxPhaseTs] CTA 0's clock at the start and after every barrier
-    int leaf_apart;                // 1: stop at the last level's node-ordered pairs (scored by leaf_score_kernel)
+    int leaf_apart;                // 1: stop at the last level's node-ordered pairs (scored by leaf_kernel)
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -1630,6 +1608,64 @@ __device__ void keys_from_parts(const GArgs& a, int64_t r0, int64_t r1) {
     }
 }
 
+// The last level scored apart from the one-launch descent, which stops once that level's
+// pairs are in node order (HDC_BEAM_ONE_LAUNCH 2): one more cooperative launch of score_kernel's
+// shape (more warps per SM than the descent's CTA holds) scores them, then, past a bounded grid
+// barrier, takes each read's final beam (one warp per read) and writes its output.  Selecting a
+// read's beam in the scoring phase, by whichever warp retired its last pair, cost 1.9 ms of a
+// 15 ms step (the count's atomics and the selects' dependent loads wait behind the level's row
+// traffic).  Nothing runs when the descent gave up (abort raised): its pair arrays are then
+// incomplete; a barrier that runs out of time raises it and reports status 120.
+struct LeafArgs {
+    int L;
+    int32_t* path;
+    float* path_score;
+    int32_t* depth;
+    unsigned* bar_count;  // the descent's grid barrier words, reused (both zero-based at rest)
+    unsigned* bar_gen;
+    int* abort;
+    int* status;
+};
+
+template <bool ROWS16>
+__global__ void __launch_bounds__(kScoreThreads, ROWS16 ? kScoreBlocks16 : kScoreBlocks)
+    leaf_kernel(const GArgs a, const LeafArgs l) {
+    __shared__ int ok_s;
+    if (ld_volatile(l.abort)) return;  // the same for every CTA: the descent finished before this launch
+    const int64_t w = (((int64_t)blockIdx.x * blockDim.x) >> 5) + (threadIdx.x >> 5);
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    score_pairs<ROWS16>(a, w, nw);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned g = ld_acquire_gpu(l.bar_gen);
+        if (atomicAdd(l.bar_count, 1u) == gridDim.x - 1) {
+            atomicExch(l.bar_count, 0u);
+            __threadfence();
+            st_release_gpu(l.bar_gen, g + 1);
+        } else {
+            const long long t0 = clock64();
+            while (ld_acquire_gpu(l.bar_gen) == g) {
+                if (ld_volatile(l.abort)) break;
+                if (clock64() - t0 > tc::kWaitCycles) {
+                    if (atomicExch(l.abort, 1) == 0) atomicCAS(l.status, 0, 100 + kCodeGridBarrier);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        ok_s = ld_volatile(l.abort) == 0;
+    }
+    __syncthreads();
+    if (!ok_s) return;
+    const int lane = threadIdx.x & 31;
+    for (int64_t r = w; r < a.nq; r += nw) {
+        select_warp(a, l.L, r, lane);
+        __syncwarp();
+        if (lane == 0) output_one(a, r, l.path, l.path_score, l.depth);
+    }
+}
+
 __global__ void __launch_bounds__(TcOne::kThreads, 1) descent_one_kernel(const GArgs a, const TcItems t, const OneArgs o) {
     extern __shared__ uint8_t smem_raw[];
     __shared__ TcShared sm;
@@ -1749,7 +1785,7 @@ __global__ void __launch_bounds__(TcOne::kThreads, 1) descent_one_kernel(const G
             scatter_range(a, gtid, gstride);
             if (!(ok = grid_barrier(o, sm, &ok_s, &n_ts))) break;
             if (o.leaf_apart && L == a.levels - 1) {
-                // the last level is scored and selected by leaf_score_kernel and select_output_kernel
+                // the last level is scored and selected by leaf_kernel
                 apart_done = true;
                 break;
             }
@@ -1787,7 +1823,7 @@ __global__ void __launch_bounds__(TcOne::kThreads, 1) descent_one_kernel(const G
 // The one-launch descent needs every CTA (one per SM) resident at once; checked once per
 // context, with the kernel's shared memory set.
 bool one_launch_fits(hdc_context* ctx) {
-    if (ctx->beam_one <= 0) return false;  // automatic: kernels per level (the fastest form here)
+    if (ctx->beam_one == 0) return false;
     if (ctx->beam_one_fit < 0) {
         int per_sm = 0;
         cudaError_t e = cudaFuncSetAttribute(descent_one_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1946,20 +1982,25 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
             }
         }
         o.phase_ts = ctx->d_phase_ts;
-        o.leaf_apart = ctx->beam_one == 2 ? 1 : 0;
+        o.leaf_apart = ctx->beam_one != 1 ? 1 : 0;  // automatic: the last level in a launch of its own
         e = cudaMemsetAsync(one_state, 0, 4 * sizeof(uint32_t), stream);
         void* args[] = {(void*)&a, (void*)&t, (void*)&o};
         if (e == cudaSuccess)
             e = cudaLaunchCooperativeKernel((const void*)descent_one_kernel, dim3((unsigned)ctx->num_sms),
                                             dim3(TcOne::kThreads), args, kOneSmem, stream);
         if (e == cudaSuccess && o.leaf_apart) {
-            if (n32 < n_nodes)
-                leaf_score_kernel<true><<<ctx->num_sms * kScoreBlocks16, kScoreThreads, 0, stream>>>(a, o.abort);
-            else
-                leaf_score_kernel<false><<<ctx->num_sms * kScoreBlocks, kScoreThreads, 0, stream>>>(a, o.abort);
-            select_output_kernel<<<(unsigned)((nq * 32 + 255) / 256), 256, 0, stream>>>(a, levels - 1, d_path,
-                                                                                      d_path_score, d_depth, o.abort);
-            e = cudaGetLastError();
+            LeafArgs l{levels - 1, d_path, d_path_score, d_depth, o.bar_count, o.bar_gen, o.abort, o.status};
+            void* largs[] = {(void*)&a, (void*)&l};
+            const bool r16 = n32 < n_nodes;
+            const void* kern = r16 ? (const void*)leaf_kernel<true> : (const void*)leaf_kernel<false>;
+            int per_sm = 0;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kScoreThreads, 0);
+            if (e == cudaSuccess) {
+                per_sm = std::min(per_sm, r16 ? kScoreBlocks16 : kScoreBlocks);
+                e = per_sm < 1 ? cudaErrorCooperativeLaunchTooLarge
+                               : cudaLaunchCooperativeKernel(kern, dim3((unsigned)(ctx->num_sms * per_sm)),
+                                                             dim3(kScoreThreads), largs, 0, stream);
+            }
         }
         cudaFreeAsync(ws, stream);
         return e == cudaSuccess ? HDC_OK : cuda_fail(e, "beam: one-launch descent");

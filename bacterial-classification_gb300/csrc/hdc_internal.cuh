@@ -39,8 +39,8 @@ struct hdc_context {
     void* noalloc_scratch = nullptr;  // device address of hdc_search_plain_noalloc's fixed scratch (first call)
     int greedy_form = -1;             // propagate-children selection: 1 scored (dim % 8 == 0), 0 sequential, -1 automatic
     int beam_one = -1;                // grouped descent: 1 every level in one cooperative launch, 2 the same
-                                      // with the last level in kernels of its own, 0 a launch
-                                      // sequence per level, -1 automatic (0)
+                                      // with the last level in a cooperative kernel of its own, 0 a
+                                      // launch sequence per level, -1 automatic (2 where it fits)
     mutable int beam_one_fit = -1;    // the one-launch descent's CTAs all fit at once (-1: not asked yet)
     unsigned long long* d_phase_ts = nullptr;  // phase clock of the last one-launch descent (diagnostic)
     long long wait_cycles = 0;        // tensor-core search: limit of its bounded waits in SM cycles (0: default)

@@ -586,6 +586,27 @@ def run_descent(args, cfg):
     depth_mean = float(depth.float().mean())
     last = 2 % n_pool  # out["r"] is from the last event-timed call, on dev_pool[2 % n_pool]
     leaf_acc = float((path[:, L - 1].cpu().numpy() == int(base[5]) + pool[last].label[:B]).mean())
+    # the same calls as kernels per level (HDC_BEAM_ONE_LAUNCH 0), timed beside the form above
+    alt = None
+    if split and args.beam_one != 0:
+        ref = [x.clone() for x in (path, score, depth)]
+        ctx.option(H.BEAM_ONE_LAUNCH, 0)
+        for i in range(args.warmup):
+            step(*dev_pool[i % n_pool])
+        torch.cuda.synchronize()
+        t0.record(stream)
+        for i in range(args.steps):
+            step(*dev_pool[i % n_pool])
+        t1.record(stream)
+        torch.cuda.synchronize()
+        alt_ms = t0.elapsed_time(t1) / args.steps
+        step(*dev_pool[last])
+        torch.cuda.synchronize()
+        same = all(torch.equal(x, y) for x, y in zip(ref, out["r"]))
+        alt = {"form": "kernels per level (HDC_BEAM_ONE_LAUNCH 0)", "value": B / (alt_ms / 1e3), "unit": "reads/s",
+               "ms_per_step": alt_ms, "gpu_launches_per_step": 1 + 3 + 6 * L + 2 + 14 * (L - 2) + 5,
+               "results_identical": same}
+        ctx.option(H.BEAM_ONE_LAUNCH, args.beam_one)
     # end to end: pinned host reads copied in, paths and scores copied back, every step
     h_pool = [(torch.from_numpy(r.buf).pin_memory(), torch.from_numpy(r.off).pin_memory(),
                torch.from_numpy(r.len).pin_memory()) for r in pool]
@@ -634,8 +655,8 @@ def run_descent(args, cfg):
         per_step = 2
     elif args.beam_one == 1:  # every level in one cooperative launch
         per_step = 2
-    elif args.beam_one == 2:  # the cooperative launch up to the leaf pairs, then leaf scoring and select
-        per_step = 4
+    elif args.beam_one == 2:  # the cooperative launch up to the leaf pairs, then a cooperative leaf kernel
+        per_step = 3
     elif tc_levels and L > 1:
         per_step = 1 + 3 + 6 * L + 2 + 14 * (L - 2) + 5
     else:
@@ -643,7 +664,7 @@ def run_descent(args, cfg):
     res = dict(ms=ms, e2e_ms=e2e_ms, search_ms=float(np.median(beam_ms)), clocks=clk.summary(),
                launches=per_step * args.steps, refs=int(base[-1]), h2d=io["h2d"], d2h=io["d2h"], tree=tree,
                bundle=bundle, depth_mean=depth_mean, rows_per_read=int(sum(cand)), leaf_accuracy=leaf_acc,
-               mean_len=float(np.mean(pool[0].len)), n_wide=n_wide, phases=phases,
+               mean_len=float(np.mean(pool[0].len)), n_wide=n_wide, phases=phases, alt=alt,
                proto_bytes=n_wide * dim * 4 + (n_nodes - n_wide) * dim * 2)
     if not args.no_cpu_baseline:
         # q8 and out["r"] hold the last step's batch and result
@@ -912,8 +933,8 @@ def descent_line(args, cfg, r, metric, workload):
                                    "descent_one_kernel, every level in one cooperative launch" if args.beam_one == 1
                                    else "kernels per level" if args.beam_one == 0
                                    else "descent_one_kernel, every level in one cooperative launch up to the "
-                                        "leaf pairs sorted by node, then leaf_score_kernel scoring them and "
-                                        "select_output_kernel taking the final beams", r["proto_bytes"] / 1e9,
+                                        "leaf pairs sorted by node, then leaf_kernel (cooperative) scoring them "
+                                        "and taking the final beams", r["proto_bytes"] / 1e9,
                                    cfg["levels"],
                                    r["rows_per_read"])},
         "propagate_bundle": {"kernel": "bundle_kernel (internal prototypes = int32 sums of children)",
@@ -922,6 +943,8 @@ def descent_line(args, cfg, r, metric, workload):
                              "per_rank": r["bundle"]},
         "clocks": r["clocks"], "gpu_launches": r["launches"],
     }
+    if r.get("alt"):
+        line["kernels_per_level_form"] = r["alt"]
     if r.get("phases"):
         line["descent_phases_ms"] = r["phases"]
     if "sample_identical" in r:
@@ -1185,8 +1208,8 @@ def main():
     ap.add_argument("--beam-grouped", type=int, default=-1,
                     help="descent: 1 reads grouped by candidate node, 0 one warp per read (-1: default)")
     ap.add_argument("--beam-one", type=int, default=-1,
-                    help="descent: 1 every level in one launch, 2 one launch up to the leaf pairs + leaf kernels, "
-                         "0 kernels per level (-1: the library default, 0)")
+                    help="descent: 1 every level in one launch, 2 one launch up to the leaf pairs + a leaf launch, "
+                         "0 kernels per level (-1: the library default, 2)")
     ap.add_argument("--score-mode", default="norm", choices=["norm", "cos", "dot"],
                     help="score of the top-k search (default the reference's NORM scale; the CPU legs need it)")
     ap.add_argument("--aux-scale", type=float, default=1.0,
@@ -1194,8 +1217,8 @@ def main():
     ap.add_argument("--proto-int32", action="store_true",
                     help="descent: every prototype row int32 (default: int16 rows from the first node whose rows fit)")
     args = ap.parse_args()
-    if args.beam_one < 0:  # the library's automatic descent form: kernels per level
-        args.beam_one = 0
+    if args.beam_one < 0:  # the library's automatic descent form: two cooperative launches
+        args.beam_one = 2
     if args.warmup < 3:
         log("warmup raised to 3")
         args.warmup = 3

@@ -315,12 +315,13 @@ int hdc_search_tc_last_shape(const hdc_context* ctx, int32_t shape[5]);
 #define HDC_BEAM_ONE_LAUNCH 11 /* grouped descent (HDC_BEAM_GROUPED 1 or 2): 1 runs every level
                               in one cooperative launch (one CTA per SM, the phases of a level
                               separated by bounded grid-wide barriers); 2 the same up to the
-                              last level's node-ordered pairs, which a second kernel scores
-                              (more warps per SM than the cooperative launch holds) and a third
-                              selects from (one warp per read); 0 a sequence of kernels per
-                              level, whose tensor-core kernel has more producer warps than the
-                              cooperative CTA can hold (the fastest at D = 16,384); -1
-                              automatic (0); results are identical */
+                              last level's node-ordered pairs, which a second cooperative launch
+                              scores (more warps per SM than the first holds) and, past a grid
+                              barrier, selects from (one warp per read): two launches a call;
+                              0 a sequence of kernels per level (about 100 a call), whose
+                              tensor-core kernel has more producer warps than the cooperative
+                              CTA can hold (3 % faster at D = 16,384); -1 automatic (2 where
+                              the cooperative CTAs fit, else 0); results are identical */
 #define HDC_WAIT_LIMIT 9   /* tensor-core search: its bounded device-side waits give up after
                               value x 1,000 SM cycles, 1 .. 4,000,000 (0: the default,
                               4,000,000, about 2 s at 2 GHz); a wait that gives up makes the
