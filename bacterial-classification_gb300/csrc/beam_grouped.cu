@@ -277,15 +277,25 @@ __global__ void scatter_kernel(const GArgs a) {
 __device__ __forceinline__ int32_t neg32(int32_t x) { return (int32_t)(0u - (uint32_t)x); }
 
 // Lane l's share of the dot of an int32 row: dims 128 j + 4 l .. + 3.
+constexpr int kRowPrefetch = 2;  // blocks of a row prefetched into L2 ahead of its loads
+
 __device__ __forceinline__ int64_t lane_dot32(const GArgs& a, int lane, int32_t node, int64_t r) {
     const int nsteps = a.dim / 128;  // a multiple of 8 (dim % 1024 == 0)
     const int sh = (lane & 7) * 4;
-    const int32_t* row = a.proto + (int64_t)node * a.dim + 4 * lane;
+    const int32_t* row0 = a.proto + (int64_t)node * a.dim;
+    const int32_t* row = row0 + 4 * lane;
     const uint32_t* qb = a.bits + r * a.words + (lane >> 3);
+    // lane 0 prefetches the row into L2 kRowPrefetch blocks of 4 steps (2 KB) ahead
+    const int nblk = nsteps / 4;
+    auto prefetch = [&](int q) {
+        if (lane == 0 && q < nblk) tc::prefetch_l2(row0 + (size_t)q * 512, 2048);
+    };
+    for (int q = 0; q < kRowPrefetch; ++q) prefetch(q);
     if (a.pn[node] < ((int64_t)1 << 44)) {
         // every |p| < 2^22, so a lane's (at most 512) terms sum below 2^31: int32 throughout
         int32_t acc32 = 0;
         for (int j = 0; j < nsteps; j += 4) {
+            prefetch(j / 4 + kRowPrefetch);
             int4 x[4];
             uint32_t w[4];
 #pragma unroll
@@ -304,6 +314,7 @@ __device__ __forceinline__ int64_t lane_dot32(const GArgs& a, int lane, int32_t 
     }
     int64_t acc = 0;
     for (int j = 0; j < nsteps; j += 4) {
+        prefetch(j / 4 + kRowPrefetch);
         int4 x[4];
         uint32_t w[4];
 #pragma unroll
@@ -329,17 +340,25 @@ __device__ __forceinline__ int signs4_bytes(uint32_t nib) {
 }
 
 // Lane l's share of the dot of an int16 row: dims 256 j + 8 l .. + 7 (one 16-byte load, one
-// byte of the read's bits), U loads in flight.  Each word holds two int16 values (the lower
+// byte of the read's bits), U loads in flight, and lane 0 prefetching the row into L2
+// kRowPrefetch blocks of U steps ahead (the loads of a block then find it there: 3.9 -> 3.55
+// ms for the c5 leaf level; 4 blocks ahead was slower).  Each word holds two int16 values (the lower
 // dim in the low half); dp2a multiplies them by two of the signed sign bytes and accumulates,
 // exactly.  |p| <= 2^15 and at most 512 terms a lane: int32 throughout.
 template <int U>
 __device__ __forceinline__ int64_t lane_dot16_u(const GArgs& a, int lane, int32_t node, int64_t r) {
     const int nsteps = a.dim / 256;  // a multiple of U
     const int sh = (lane & 3) * 8;
-    const int4* row = reinterpret_cast<const int4*>(a.proto16 + (node - a.n32) * a.dim) + lane;
+    const int16_t* row16 = a.proto16 + (node - a.n32) * a.dim;
+    const int4* row = reinterpret_cast<const int4*>(row16) + lane;
     const uint32_t* qb = a.bits + r * a.words + (lane >> 2);
+    constexpr uint32_t kBlk = U * 512;  // the warp's row bytes of one block of U steps
+    const int nblk = nsteps / U;
+    if (lane == 0)
+        for (int q = 0; q < kRowPrefetch && q < nblk; ++q) tc::prefetch_l2(row16 + (size_t)q * kBlk / 2, kBlk);
     int acc = 0;
     for (int j = 0; j < nsteps; j += U) {
+        if (lane == 0 && j / U + kRowPrefetch < nblk) tc::prefetch_l2(row16 + (size_t)(j / U + kRowPrefetch) * kBlk / 2, kBlk);
         int4 x[U];
         uint32_t w[U];
 #pragma unroll
@@ -1627,8 +1646,11 @@ struct LeafArgs {
     int* status;
 };
 
+// with int32 rows alone one CTA fewer per SM than score_kernel<false>: the select's registers
+constexpr int kLeafBlocks32 = kScoreBlocks - 2;
+
 template <bool ROWS16>
-__global__ void __launch_bounds__(kScoreThreads, ROWS16 ? kScoreBlocks16 : kScoreBlocks)
+__global__ void __launch_bounds__(kScoreThreads, ROWS16 ? kScoreBlocks16 : kLeafBlocks32)
     leaf_kernel(const GArgs a, const LeafArgs l) {
     __shared__ int ok_s;
     if (ld_volatile(l.abort)) return;  // the same for every CTA: the descent finished before this launch
@@ -1996,7 +2018,7 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
             int per_sm = 0;
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kScoreThreads, 0);
             if (e == cudaSuccess) {
-                per_sm = std::min(per_sm, r16 ? kScoreBlocks16 : kScoreBlocks);
+                per_sm = std::min(per_sm, r16 ? kScoreBlocks16 : kLeafBlocks32);
                 e = per_sm < 1 ? cudaErrorCooperativeLaunchTooLarge
                                : cudaLaunchCooperativeKernel(kern, dim3((unsigned)(ctx->num_sms * per_sm)),
                                                              dim3(kScoreThreads), largs, 0, stream);

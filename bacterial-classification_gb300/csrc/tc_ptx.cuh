@@ -100,6 +100,12 @@ __device__ __forceinline__ void tma_load_2d_hint(void* dst, const CUtensorMap* m
         : "memory");
 }
 
+// Bulk prefetch of `bytes` (a multiple of 16, 16-byte aligned) of global memory into L2: a
+// hint with no completion, issued by one thread for a whole block of a row.
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
 // 2-D TMA tile prefetch into L2 (no shared memory, no completion): brings a
 // tile toward the SM's L2 slice ahead of its load.
 __device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* map, int x, int y) {
