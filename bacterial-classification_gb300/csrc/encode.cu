@@ -40,7 +40,7 @@
 namespace hdc {
 namespace {
 
-constexpr int kWarps = 16;
+constexpr int kWarps = 24;
 constexpr int kThreads = kWarps * 32;
 constexpr int kChunk = 64;  // positions per staged chunk
 constexpr int kPerLane = kChunk / 32;
