@@ -428,28 +428,33 @@ __global__ void __launch_bounds__(kScoreThreads, ROWS16 ? kScoreBlocks16 : kScor
 
 // Per read: the best `beam` candidates, then the rule of the per-read kernel (stop below
 // the threshold with the best path, else keep the entries >= threshold, at most `beam`).
-// One warp per read, every lane calling with the same r.  The candidates are ordered by key
-// (descending), ties to the lower pair index (the order an insertion in pair order keeps);
-// round t takes the warp-wide first of those after round t - 1's pick, lane t keeps it.  The
-// keys of the first 128 pairs stay in registers (4 a lane), later ones are re-read each round.
-// The kept entries' paths are then copied lane-parallel: every old value is read before any
-// is written (a new entry's path comes from its parent's slot, possibly another entry's).
-constexpr int kSelCache = 4;
+// A group of G lanes per read (G = 8: four reads a warp at once, their dependent loads
+// overlapping), every lane of the group calling with the same r.  The candidates are ordered
+// by key (descending), ties to the lower pair index (the order an insertion in pair order
+// keeps); round t takes the group-wide first of those after round t - 1's pick, lane t keeps
+// it.  The keys of the first 8 G pairs stay in registers (8 a lane), later ones are re-read
+// each round.  The kept entries' paths are then copied lane-parallel: every old value is read
+// before any is written (a new entry's path comes from its parent's slot, possibly another
+// entry's).
+constexpr int kSelCache = 8;
 
 __device__ __forceinline__ bool key_before(uint64_t k, int32_t p, uint64_t bk, int32_t bp) {
     return k > bk || (k == bk && p < bp);
 }
 
-__device__ void select_warp(const GArgs& a, int L, int64_t r, int lane) {
+// lane: 0 .. G-1 within the group; gmask: the group's lanes in the warp
+template <int G>
+__device__ void select_group(const GArgs& a, int L, int64_t r, int lane, uint32_t gmask) {
+    static_assert(G >= kMaxBeamG && (G & (G - 1)) == 0 && G <= 32, "a lane per kept entry");
     if (a.done[r]) return;
     const int32_t p0 = a.off[r], p1 = a.off[r + 1];
     uint64_t ck[kSelCache];
 #pragma unroll
     for (int i = 0; i < kSelCache; ++i) {
-        const int32_t p = p0 + lane + 32 * i;
+        const int32_t p = p0 + lane + G * i;
         ck[i] = p < p1 ? __ldcg(a.pair_key + p) : 0;  // from L2: written by other SMs in this kernel
     }
-    const bool more = p1 - p0 > 32 * kSelCache;
+    const bool more = p1 - p0 > G * kSelCache;
     uint64_t prev_k = 0, my_k = 0;
     int32_t prev_p = -1, my_p = -1;
     int n = 0;
@@ -464,18 +469,19 @@ __device__ void select_warp(const GArgs& a, int L, int64_t r, int lane) {
         };
 #pragma unroll
         for (int i = 0; i < kSelCache; ++i)
-            if (p0 + lane + 32 * i < p1) consider(ck[i], p0 + lane + 32 * i);
+            if (p0 + lane + G * i < p1) consider(ck[i], p0 + lane + G * i);
         if (more)
-            for (int32_t p = p0 + lane + 32 * kSelCache; p < p1; p += 32) consider(__ldcg(a.pair_key + p), p);
-        for (int o = 16; o; o >>= 1) {
-            const uint64_t ok = __shfl_xor_sync(0xffffffffu, bk, o);
-            const int32_t op = __shfl_xor_sync(0xffffffffu, bp, o);
+            for (int32_t p = p0 + lane + G * kSelCache; p < p1; p += G) consider(__ldcg(a.pair_key + p), p);
+#pragma unroll
+        for (int o = G / 2; o; o >>= 1) {
+            const uint64_t ok = __shfl_xor_sync(gmask, bk, o, G);
+            const int32_t op = __shfl_xor_sync(gmask, bp, o, G);
             if (key_before(ok, op, bk, bp)) {
                 bk = ok;
                 bp = op;
             }
         }
-        if (bp == INT32_MAX) break;  // no candidate left (the same on every lane)
+        if (bp == INT32_MAX) break;  // no candidate left (the same on every lane of the group)
         if (lane == t) {
             my_k = bk;
             my_p = bp;
@@ -490,13 +496,14 @@ __device__ void select_warp(const GArgs& a, int L, int64_t r, int lane) {
         my_node = a.pair_node[my_p];
         my_slot = a.pair_slot[my_p];
     }
-    const bool stop = n == 0 || (double)__shfl_sync(0xffffffffu, my_s, 0) < a.threshold;
+    const bool stop = n == 0 || (double)__shfl_sync(gmask, my_s, 0, G) < a.threshold;
     int keep;
     if (stop) {
         keep = n ? 1 : 0;  // the best candidate's path is the answer
     } else {
-        const uint32_t ok = __ballot_sync(0xffffffffu, lane < n && (double)my_s >= a.threshold);
-        keep = __ffs(~ok) - 1;  // the leading entries >= threshold (n <= 8: ~ok has a set bit)
+        const uint32_t base = __ffs(gmask) - 1;
+        const uint32_t ok = (__ballot_sync(gmask, lane < n && (double)my_s >= a.threshold) & gmask) >> base;
+        keep = __ffs(~ok) - 1;  // the leading entries >= threshold (n <= 8 < G + 1: ~ok has a set bit)
     }
     if (lane == 0) {
         if (stop) {
@@ -510,16 +517,17 @@ __device__ void select_warp(const GArgs& a, int L, int64_t r, int lane) {
             }
         }
     }
-    // entry t's levels 0..L: lanes i and i + 32 of the keep x (L + 1) values
-    int32_t vp[2];
-    float vs[2];
+    // entry t's levels 0..L: lanes i, i + G, ... of the keep x (L + 1) values
+    constexpr int H = kMaxBeamG * kMaxLevelsG / G;
+    int32_t vp[H];
+    float vs[H];
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int i = lane + 32 * h, t = i / (L + 1), l = i - t * (L + 1);
+    for (int h = 0; h < H; ++h) {
+        const int i = lane + G * h, t = i / (L + 1), l = i - t * (L + 1);
         const int src = t < kMaxBeamG ? t : 0;
-        const int32_t slot = __shfl_sync(0xffffffffu, my_slot, src);
-        const int32_t node = __shfl_sync(0xffffffffu, my_node, src);
-        const float sc = __shfl_sync(0xffffffffu, my_s, src);
+        const int32_t slot = __shfl_sync(gmask, my_slot, src, G);
+        const int32_t node = __shfl_sync(gmask, my_node, src, G);
+        const float sc = __shfl_sync(gmask, my_s, src, G);
         vp[h] = node;
         vs[h] = sc;
         if (t < keep && l < L) {
@@ -527,10 +535,10 @@ __device__ void select_warp(const GArgs& a, int L, int64_t r, int lane) {
             vs[h] = a.scores[state_at(r, slot, l)];
         }
     }
-    __syncwarp();
+    __syncwarp(gmask);
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int i = lane + 32 * h, t = i / (L + 1), l = i - t * (L + 1);
+    for (int h = 0; h < H; ++h) {
+        const int i = lane + G * h, t = i / (L + 1), l = i - t * (L + 1);
         if (t < keep) {
             a.paths[state_at(r, t, l)] = vp[h];
             a.scores[state_at(r, t, l)] = vs[h];
@@ -538,11 +546,28 @@ __device__ void select_warp(const GArgs& a, int L, int64_t r, int lane) {
     }
 }
 
-// one warp per read
+constexpr int kSelLanes = 8;  // lanes per read in every select
+
+// The reads first, first + stride, ... of a warp's share: each group of kSelLanes lanes takes
+// every (32 / kSelLanes)-th of them.  `fin` (optional) runs on the group's lane 0 after a read's
+// beam is taken.
+template <class Fin>
+__device__ __forceinline__ void select_reads(const GArgs& a, int L, int64_t first, int64_t end, int64_t stride,
+                                             Fin fin) {
+    constexpr int kGroups = 32 / kSelLanes;
+    const int lane = threadIdx.x & 31, grp = lane / kSelLanes, gl = lane % kSelLanes;
+    const uint32_t gmask = ((1u << kSelLanes) - 1u) << (grp * kSelLanes);
+    for (int64_t r = first + grp * stride; r < end; r += kGroups * stride) {
+        select_group<kSelLanes>(a, L, r, gl, gmask);
+        __syncwarp(gmask);
+        if (gl == 0) fin(r);
+    }
+}
+
+// a group of kSelLanes lanes per read
 __global__ void select_kernel(const GArgs a, int L) {
-    const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (r >= a.nq) return;
-    select_warp(a, L, r, threadIdx.x & 31);
+    const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    select_reads(a, L, w, a.nq, ((int64_t)gridDim.x * blockDim.x) >> 5, [](int64_t) {});
 }
 
 __device__ __forceinline__ void output_one(const GArgs& a, int64_t r, int32_t* path, float* path_score,
@@ -1680,12 +1705,7 @@ __global__ void __launch_bounds__(kScoreThreads, ROWS16 ? kScoreBlocks16 : kLeaf
     }
     __syncthreads();
     if (!ok_s) return;
-    const int lane = threadIdx.x & 31;
-    for (int64_t r = w; r < a.nq; r += nw) {
-        select_warp(a, l.L, r, lane);
-        __syncwarp();
-        if (lane == 0) output_one(a, r, l.path, l.path_score, l.depth);
-    }
+    select_reads(a, l.L, w, a.nq, nw, [&](int64_t r) { output_one(a, r, l.path, l.path_score, l.depth); });
 }
 
 __global__ void __launch_bounds__(TcOne::kThreads, 1) descent_one_kernel(const GArgs a, const TcItems t, const OneArgs o) {
@@ -1826,7 +1846,7 @@ __global__ void __launch_bounds__(TcOne::kThreads, 1) descent_one_kernel(const G
             keys_from_parts(a, r0, r1);
             __syncthreads();
         }
-        for (int64_t r = r0 + (tid >> 5); r < r1; r += nt >> 5) select_warp(a, L, r, tid & 31);
+        select_reads(a, L, r0 + (tid >> 5), r1, nt >> 5, [](int64_t) {});
         __syncthreads();
     }
     if (ok && !apart_done)
@@ -2074,7 +2094,7 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
             else
                 score_kernel<false><<<ctx->num_sms * kScoreBlocks, kScoreThreads, 0, stream>>>(a);
         }
-        select_kernel<<<(unsigned)((nq * 32 + 255) / 256), 256, 0, stream>>>(a, L);
+        select_kernel<<<(unsigned)((nq * kSelLanes + 255) / 256), 256, 0, stream>>>(a, L);
     }
     output_kernel<<<rb, 256, 0, stream>>>(a, d_path, d_path_score, d_depth);
     e = cudaGetLastError();
