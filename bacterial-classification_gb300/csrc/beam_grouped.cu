@@ -228,29 +228,42 @@ __device__ __forceinline__ void put_pair(const GArgs& a, int32_t p, int64_t r, i
     if (count_nodes) atomicAdd(a.node_cnt + node, 1);
 }
 
-// the candidate pairs of read r at level L, from a.off[r] on
-__device__ void expand_one(const GArgs& a, int L, int64_t r, bool count_nodes) {
+// The pairs of beam entry b of read r (level 0: b = 0 writes the roots), at a.off[r] plus the
+// candidates of the entries before it: one thread per (read, entry), so the entries' dependent
+// loads (path, child range, children) run side by side.  With par_cnt set (a tensor-core level
+// above 0), the entry also counts itself to its parent.
+__device__ __forceinline__ void expand_entry(const GArgs& a, int L, int64_t r, int b, bool count_nodes,
+                                             int32_t* par_cnt) {
     if (a.done[r]) return;
-    int32_t p = a.off[r];
     if (L == 0) {
-        for (int i = 0; i < a.n_roots; ++i) put_pair(a, p++, r, a.roots[i], 0, count_nodes);
+        if (b == 0) {
+            int32_t p = a.off[r];
+            for (int i = 0; i < a.n_roots; ++i) put_pair(a, p++, r, a.roots[i], 0, count_nodes);
+        }
         return;
     }
-    for (int b = 0; b < a.nbeam[r]; ++b) {
-        const int32_t node = a.paths[state_at(r, b, L - 1)];
-        const int64_t c0 = a.child_ptr[node], c1 = a.child_ptr[node + 1];
-        if (c0 == c1) {
-            put_pair(a, p++, r, node, b, count_nodes);
-        } else {
-            for (int64_t c = c0; c < c1; ++c) put_pair(a, p++, r, a.child_idx[c], b, count_nodes);
-        }
+    const int nb = a.nbeam[r];
+    if (b >= nb) return;
+    int32_t p = a.off[r];
+    for (int e = 0; e < b; ++e) {
+        const int32_t prev = a.paths[state_at(r, e, L - 1)];
+        const int64_t k = a.child_ptr[prev + 1] - a.child_ptr[prev];
+        p += k ? (int32_t)k : 1;
+    }
+    const int32_t node = a.paths[state_at(r, b, L - 1)];
+    if (par_cnt) atomicAdd(par_cnt + node, 1);
+    const int64_t c0 = a.child_ptr[node], c1 = a.child_ptr[node + 1];
+    if (c0 == c1) {
+        put_pair(a, p, r, node, b, count_nodes);
+    } else {
+        for (int64_t c = c0; c < c1; ++c) put_pair(a, p++, r, a.child_idx[c], b, count_nodes);
     }
 }
 
 __global__ void expand_kernel(const GArgs a, int L, bool count_nodes) {
-    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= a.nq) return;
-    expand_one(a, L, r, count_nodes);
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nq * a.beam) return;
+    expand_entry(a, L, i / a.beam, (int)(i % a.beam), count_nodes, nullptr);
 }
 
 // pairs p = first, first + stride, ... to their node-ordered slots
@@ -719,9 +732,11 @@ __device__ __forceinline__ void item_count_one(const GArgs& a, const TcItems& t,
     const bool small = m > 0 && m <= kTcHalfE && nch <= kTcHalfC;
     t.small[P] = small ? 1 : 0;
     t.item_cnt[P] = m && !small ? ((m + kTcE - 1) / kTcE) * ((nch + kTcC - 1) / kTcC) : 0;
-    if (m) {
-        bool two = true;
-        for (int32_t j = 0; two && j < nch; ++j) two = row_fits2(a, child_at(a, (int32_t)P, j));
+    if (m) {  // the children's norms loaded independently (no early exit), four at a time
+        const int64_t c0 = a.child_ptr[P], c1 = a.child_ptr[P + 1];
+        bool two = c0 < c1 || row_fits2(a, (int32_t)P);
+#pragma unroll 4
+        for (int64_t c = c0; c < c1; ++c) two &= row_fits2(a, a.child_idx[c]);
         t.fit2[P] = two ? 1 : 0;
     }
 }
@@ -1773,10 +1788,8 @@ __global__ void __launch_bounds__(TcOne::kThreads, 1) descent_one_kernel(const G
         int32_t total = cta_scan(a.cnt, a.off, nullptr, r0, r1, base, sh);
         if (last_reads && tid == 0) a.off[a.nq] = total;
         __syncthreads();
-        for (int64_t r = r0 + tid; r < r1; r += nt) {
-            expand_one(a, L, r, !tcl);
-            if (tcl && L > 0) par_count_one(a, t, L, r);
-        }
+        for (int64_t i = r0 * a.beam + tid; i < r1 * a.beam; i += nt)
+            expand_entry(a, L, i / a.beam, (int)(i % a.beam), !tcl, tcl && L > 0 ? t.par_cnt : nullptr);
         if (tcl && L == 0) items_level0_range(a, t, gtid, gstride);
         if (!(ok = grid_barrier(o, sm, &ok_s, &n_ts))) break;
         if (tcl) {
@@ -2067,7 +2080,7 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
         count_kernel<<<rb, 256, 0, stream>>>(a, L);
         exclusive_scan(a.cnt, a.off, nq, d_sums, stream);
         if (!tc_level) cudaMemsetAsync(a.node_cnt, 0, (size_t)n_nodes * 4, stream);
-        expand_kernel<<<rb, 256, 0, stream>>>(a, L, !tc_level);
+        expand_kernel<<<(unsigned)((nq * beam + 255) / 256), 256, 0, stream>>>(a, L, !tc_level);
         if (tc_level) {
             // entries grouped by parent, then items of up to 128 entries x 32 children
             if (L == 0) {
