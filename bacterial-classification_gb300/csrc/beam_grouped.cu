@@ -218,6 +218,19 @@ __global__ void count_kernel(const GArgs a, int L) {
     a.cnt[r] = count_one(a, L, r);
 }
 
+// atomicAdd(ctr + node, 1) for the calling lanes, one atomic per distinct node of the warp
+// (the levels near the root have few nodes, each counted by most reads: the atomics on one
+// address serialise); returns the old value plus the lane's rank among its node's lanes.
+__device__ __forceinline__ int32_t warp_count(int32_t* ctr, int32_t node) {
+    const uint32_t active = __activemask();
+    const uint32_t peers = __match_any_sync(active, node);
+    const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+    int32_t base = 0;
+    if (lane == leader) base = atomicAdd(ctr + node, __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + __popc(peers & ((1u << lane) - 1u));
+}
+
 // count_nodes: the level is scored from node-sorted pairs (score_kernel), which need the
 // pairs per node; a tensor-core level groups the entries by parent instead
 __device__ __forceinline__ void put_pair(const GArgs& a, int32_t p, int64_t r, int32_t node, int slot,
@@ -251,7 +264,7 @@ __device__ __forceinline__ void expand_entry(const GArgs& a, int L, int64_t r, i
         p += k ? (int32_t)k : 1;
     }
     const int32_t node = a.paths[state_at(r, b, L - 1)];
-    if (par_cnt) atomicAdd(par_cnt + node, 1);
+    if (par_cnt) warp_count(par_cnt, node);
     const int64_t c0 = a.child_ptr[node], c1 = a.child_ptr[node + 1];
     if (c0 == c1) {
         put_pair(a, p, r, node, b, count_nodes);
@@ -703,7 +716,7 @@ __device__ __forceinline__ void par_scatter_one(const GArgs& a, const TcItems& t
     int32_t p = a.off[r];  // the candidates of beam slot b follow those of slots < b (expand_kernel)
     for (int b = 0; b < a.nbeam[r]; ++b) {
         const int32_t P = a.paths[state_at(r, b, L - 1)];
-        const int32_t pos = atomicAdd(t.par_cursor + P, 1);
+        const int32_t pos = warp_count(t.par_cursor, P);
         t.ent_read[pos] = (int32_t)r;
         t.ent_p0[pos] = p;
         p += n_children(a, P);
