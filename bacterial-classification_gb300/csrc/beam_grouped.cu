@@ -178,6 +178,7 @@ struct GArgs {
     int32_t* sorted;          // [P] pair indices ordered by node
     int64_t* part;            // [kQuarters][pstride] partial dots of a streamed level (one-launch form)
     int64_t pstride;
+    long long wait_cycles;    // limit of the descent's bounded waits (SM cycles)
 };
 
 // A caller-given largest child count below the tree's sizes the pair arrays too small: every
@@ -1055,7 +1056,7 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
                     const int64_t n = nbase + kb;
                     const int stage = (int)(n % Lay::kStages);
                     const uint32_t phase = (uint32_t)((n / Lay::kStages) & 1);
-                    const bool got = tc::mbar_wait(&sm.empty_bar[stage], phase ^ 1, &sm.err, 11);
+                    const bool got = tc::mbar_wait(&sm.empty_bar[stage], phase ^ 1, &sm.err, 11, a.wait_cycles);
                     if (__any_sync(0xffffffffu, !got)) {
                         ok = false;
                         break;
@@ -1124,7 +1125,7 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
             // item's halves are 64 rows)
             const ItemRow x = item_row(a, t, it, row);
             const bool two = item_two(t, it);
-            if (!tc::mbar_wait(&sm.accf_bar[acc], acc_phase, &sm.err, 12)) break;
+            if (!tc::mbar_wait(&sm.accf_bar[acc], acc_phase, &sm.err, 12, a.wait_cycles)) break;
             tc::fence_after();
             const uint32_t d = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * kTcAccCols);
             const int64_t qn = x.r >= 0 ? a.qn[x.r] : 0;
@@ -1172,12 +1173,12 @@ __device__ void tc_phase(const GArgs& a, const TcItems& t, TcShared& sm, TcRun& 
         uint32_t& acc_phase = run.acc_phase;
         bool ok = true;
         for (int32_t it = blockIdx.x; ok && it < n_items; it += gridDim.x) {
-            if (!tc::mbar_wait(&sm.acce_bar[acc], acc_phase ^ 1, &sm.err, 13)) break;
+            if (!tc::mbar_wait(&sm.acce_bar[acc], acc_phase ^ 1, &sm.err, 13, a.wait_cycles)) break;
             tc::fence_after();
             const uint32_t d = tmem + (uint32_t)(acc * kTcAccCols);
             const uint32_t IDESC = item_two(t, it) ? IDESC2 : IDESC3;
             for (int kb = 0; kb < kblocks; ++kb) {
-                if (!tc::mbar_wait(&sm.full_bar[stage], phase, &sm.err, 14)) {
+                if (!tc::mbar_wait(&sm.full_bar[stage], phase, &sm.err, 14, a.wait_cycles)) {
                     ok = false;
                     break;
                 }
@@ -1269,6 +1270,8 @@ struct OneArgs {
     int32_t* out_depth;
     unsigned long long* phase_ts;  // [kMaxPhaseTs] CTA 0's clock at the start and after every barrier
     int leaf_apart;                // 1: stop at the last level's node-ordered pairs (scored by leaf_kernel)
+    long long wait_cycles;         // limit of every bounded wait (SM cycles)
+    int late_cta;                  // test hook: CTA 0 reaches its first grid barrier 4 limits late
 };
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -1304,7 +1307,7 @@ __device__ bool grid_barrier(const OneArgs& o, const TcShared& sm, int* ok_s, in
             const long long t0 = clock64();
             while (ld_acquire_gpu(o.bar_gen) == g) {
                 if (ld_volatile(o.abort)) break;
-                if (clock64() - t0 > tc::kWaitCycles) {
+                if (clock64() - t0 > o.wait_cycles) {
                     if (atomicExch(o.abort, 1) == 0) atomicCAS(o.status, 0, 100 + kCodeGridBarrier);
                     break;
                 }
@@ -1516,7 +1519,7 @@ __device__ void stream_phase(const GArgs& a, TcShared& sm, TcRun& run, uint8_t* 
                                           : reinterpret_cast<const char*>(a.proto + n * a.dim);
                     for (int q = 0; q < kQuarters; ++q) {
                         const int b = q * kRowSlots + slot;
-                        if (!tc::mbar_wait(&sm.row_empty[b], parity ^ 1u, &sm.err, 15)) {
+                        if (!tc::mbar_wait(&sm.row_empty[b], parity ^ 1u, &sm.err, 15, a.wait_cycles)) {
                             ok = false;
                             break;
                         }
@@ -1614,7 +1617,7 @@ __device__ void stream_phase(const GArgs& a, TcShared& sm, TcRun& run, uint8_t* 
             if (ps == pe) continue;
             const int64_t n = nb + j;
             const int b = q * kRowSlots + slot;
-            if (!tc::mbar_wait(&sm.row_full[b], parity, &sm.err, 16)) {
+            if (!tc::mbar_wait(&sm.row_full[b], parity, &sm.err, 16, a.wait_cycles)) {
                 ok = false;
                 break;
             }
@@ -1722,7 +1725,7 @@ __global__ void __launch_bounds__(kScoreThreads, ROWS16 ? kScoreBlocks16 : kLeaf
             const long long t0 = clock64();
             while (ld_acquire_gpu(l.bar_gen) == g) {
                 if (ld_volatile(l.abort)) break;
-                if (clock64() - t0 > tc::kWaitCycles) {
+                if (clock64() - t0 > a.wait_cycles) {
                     if (atomicExch(l.abort, 1) == 0) atomicCAS(l.status, 0, 100 + kCodeGridBarrier);
                     break;
                 }
@@ -1776,6 +1779,10 @@ __global__ void __launch_bounds__(TcOne::kThreads, 1) descent_one_kernel(const G
         for (int64_t i = gtid; i < a.n_nodes; i += gstride) m = max(m, (int32_t)(a.child_ptr[i + 1] - a.child_ptr[i]));
         for (int off = 16; off; off >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, off));
         if ((tid & 31) == 0 && m) atomicMax(o.maxc, m);
+    }
+    if (o.late_cta && b == 0 && tid == 0) {  // test hook: the other CTAs' first wait runs out
+        const long long t0 = clock64();
+        while (clock64() - t0 < 4 * o.wait_cycles) __nanosleep(256);
     }
     bool ok = grid_barrier(o, sm, &ok_s, &n_ts);
     if (ok && o.maxc && ld_volatile(o.maxc) > o.given) {
@@ -1961,6 +1968,7 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
     a.child_ptr = d_child_ptr;
     a.child_idx = d_child_idx;
     a.roots = d_roots;
+    a.wait_cycles = ctx->wait_cycles > 0 ? ctx->wait_cycles : tc::kWaitCycles;
     const int64_t sums = std::max(scan_blocks_needed(nq), scan_blocks_needed(n_nodes));
     int32_t* d_sums = nullptr;
     int32_t* d_maxc_dev = nullptr;
@@ -2050,6 +2058,8 @@ int launch_beam_grouped(hdc_context* ctx, const int8_t* d_q, const uint32_t* d_q
             }
         }
         o.phase_ts = ctx->d_phase_ts;
+        o.wait_cycles = a.wait_cycles;
+        o.late_cta = ctx->test_withhold_loads == 2 ? 1 : 0;
         o.leaf_apart = ctx->beam_one != 1 ? 1 : 0;  // automatic: the last level in a launch of its own
         e = cudaMemsetAsync(one_state, 0, 4 * sizeof(uint32_t), stream);
         void* args[] = {(void*)&a, (void*)&t, (void*)&o};

@@ -360,7 +360,7 @@ int hdc_context_option(hdc_context* ctx, int option, int value) {
             ctx->greedy_form = value;
             return HDC_OK;
         case HDC_TEST_WITHHOLD_LOADS:
-            if (value < 0 || value > 1) return fail(HDC_ERR_INVALID, "option: withhold must be 0 or 1");
+            if (value < 0 || value > 2) return fail(HDC_ERR_INVALID, "option: withhold must be 0, 1 or 2");
             ctx->test_withhold_loads = value;
             return HDC_OK;
         default:

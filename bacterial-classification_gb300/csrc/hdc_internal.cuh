@@ -43,8 +43,10 @@ struct hdc_context {
                                       // launch sequence per level, -1 automatic (2 where it fits)
     mutable int beam_one_fit = -1;    // the one-launch descent's CTAs all fit at once (-1: not asked yet)
     unsigned long long* d_phase_ts = nullptr;  // phase clock of the last one-launch descent (diagnostic)
-    long long wait_cycles = 0;        // tensor-core search: limit of its bounded waits in SM cycles (0: default)
-    int test_withhold_loads = 0;      // tensor-core search: test hook, the producer issues no loads
+    long long wait_cycles = 0;        // tensor-core search and descent: limit of their bounded waits in SM
+                                      // cycles (0: default)
+    int test_withhold_loads = 0;      // test hook: 1 the search's producer issues no loads, 2 the cooperative
+                                      // descent's first CTA reaches its first grid barrier late
 };
 
 // A tensor-core reference database (hdc_refdb_create).

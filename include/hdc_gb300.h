@@ -322,20 +322,23 @@ int hdc_search_tc_last_shape(const hdc_context* ctx, int32_t shape[5]);
                               tensor-core kernel has more producer warps than the cooperative
                               CTA can hold (3 % faster at D = 16,384); -1 automatic (2 where
                               the cooperative CTAs fit, else 0); results are identical */
-#define HDC_WAIT_LIMIT 9   /* tensor-core search: its bounded device-side waits give up after
-                              value x 1,000 SM cycles, 1 .. 4,000,000 (0: the default,
-                              4,000,000, about 2 s at 2 GHz); a wait that gives up makes the
-                              search return partial results and hdc_context_status report
-                              100 + its code */
+#define HDC_WAIT_LIMIT 9   /* tensor-core search and grouped descent: their bounded device-side
+                              waits (pipeline mbarriers, grid barriers) give up after value x
+                              1,000 SM cycles, 1 .. 4,000,000 (0: the default, 4,000,000,
+                              about 2 s at 2 GHz); a wait that gives up makes the call return
+                              partial results and hdc_context_status report 100 + its code
+                              (120: a grid barrier of the cooperative descent) */
 #define HDC_GREEDY_FORM 12 /* hdc_propagate_greedy: 1 scores every pair a decision can need in
                               bulk (tiled kernels), then decides each parent's candidates in order
                               from running maxima; 0 one CTA per parent computing each decision's
                               dots as it goes; -1 automatic (1 when dim % 8 == 0); results are
                               identical */
-#define HDC_TEST_WITHHOLD_LOADS 10 /* tensor-core search, for tests of the bounded waits only: 1
-                              makes the producer issue no operand loads, so the MMA issuer's
-                              and the epilogue's waits run out (after HDC_WAIT_LIMIT) with
-                              nothing in flight and the search reports a timeout; 0 off */
+#define HDC_TEST_WITHHOLD_LOADS 10 /* for tests of the bounded waits only: 1 makes the
+                              tensor-core search's producer issue no operand loads, so the MMA
+                              issuer's and the epilogue's waits run out (after HDC_WAIT_LIMIT)
+                              with nothing in flight; 2 makes the cooperative descent's first
+                              CTA reach its first grid barrier four limits late, so the other
+                              CTAs' waits run out and every CTA leaves there; 0 off */
 int hdc_context_option(hdc_context* ctx, int option, int value);
 
 /* Hierarchical descent (config 5; targets/identify.cpp:89-202 with one

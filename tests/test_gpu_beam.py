@@ -531,3 +531,61 @@ def test_beam_one_launch_equals_level_kernels(hdc, cuda):
     assert (depth == 0).all()
     assert ctx.status() == 200
     assert ctx.status() == 0
+
+
+def test_beam_grid_barrier_wait_runs_out_and_context_recovers(hdc, cuda):
+    """A bounded grid-barrier wait of the cooperative descent that runs out,
+    without faulting anything: with HDC_TEST_WITHHOLD_LOADS 2 the first CTA
+    reaches its first grid barrier four wait limits late (HDC_WAIT_LIMIT), so
+    the other CTAs' waits give up and raise the abort word; every CTA leaves
+    at that barrier (no phase runs on incomplete data), the leaf launch does
+    nothing, TMEM is freed and the context status reports 120.  The next call
+    on the same context (hook off, default limit) equals the per-level
+    kernels, for both cooperative forms."""
+    import torch
+    H = hdc
+    dim, n_leaves, nq = 2048, 2000, 600
+    b, base, counts, ptr, idx = H.synth_tree_csr(n_leaves)
+    tree = H.synth_tree(31, n_leaves)
+    reads = H.synth_reads(32, tree, nq, 250, subst=0.01)
+    ctx = H.Context(dim, 12, 250, 10)
+    proto = torch.zeros((int(base[-1]), dim), dtype=torch.int32, device=cuda)
+    ctx.encode_segments(torch.from_numpy(tree.buf).to(cuda), torch.from_numpy(tree.off).to(cuda),
+                        torch.from_numpy(tree.len).to(cuda), proto[int(base[5]):], H.OUT_I32, tree.max_len())
+    d_idx = torch.from_numpy(idx).to(cuda)
+    for r in range(4, -1, -1):
+        lo, hi = int(base[r]), int(base[r + 1])
+        ctx.bundle(proto, torch.from_numpy(ptr[lo:hi + 1].copy()).to(cuda), d_idx, out=proto[lo:hi])
+    rb, ro, rl = (torch.from_numpy(x).to(cuda) for x in (reads.buf, reads.off, reads.len))
+    qbits = torch.empty((nq, dim // 32), dtype=torch.int32, device=cuda)
+    ctx.encode_segments(rb, ro, rl, qbits, H.OUT_SIGN_BITS, reads.max_len())
+    qn = torch.full((nq,), dim, dtype=torch.int64, device=cuda)
+    pn = ctx.norms(proto)
+    roots = torch.arange(0, counts[0], dtype=torch.int32, device=cuda)
+    d_ptr = torch.from_numpy(ptr).to(cuda)
+    n_wide = int(base[5])
+    p32, p16 = proto[:n_wide].contiguous(), proto[n_wide:].to(torch.int16)
+    maxc = int(np.diff(ptr).max())
+
+    def call():
+        res = ctx.beam_search_split(qbits, qn, p32, p16, pn, d_ptr, d_idx, roots, 6, 5, float("-inf"),
+                                    max_children=maxc)
+        torch.cuda.synchronize()
+        return [x.cpu().numpy() for x in res]
+
+    ctx.option(H.BEAM_GROUPED, 2)
+    ctx.option(H.BEAM_ONE_LAUNCH, 0)
+    want = call()
+    assert ctx.status() == 0
+    for one in (1, 2):
+        ctx.option(H.BEAM_ONE_LAUNCH, one)
+        ctx.option(H.WAIT_LIMIT, 1000)  # 10^6 SM cycles, about half a millisecond
+        ctx.option(H.TEST_WITHHOLD_LOADS, 2)
+        call()
+        assert ctx.status() == 120, one  # a grid barrier gave up
+        ctx.option(H.TEST_WITHHOLD_LOADS, 0)
+        ctx.option(H.WAIT_LIMIT, 0)
+        got = call()
+        assert ctx.status() == 0
+        for x, y in zip(want, got):
+            assert np.array_equal(x, y), one

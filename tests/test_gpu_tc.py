@@ -409,6 +409,7 @@ def test_tc_bounded_wait_runs_out_and_context_recovers(hdc, orc, cuda, cluster, 
 def test_wait_options_are_checked(hdc, cuda):
     H = hdc
     ctx = H.Context(1024, 10, 250, 10)
-    for opt, bad in ((H.WAIT_LIMIT, -1), (H.WAIT_LIMIT, 4000001), (H.TEST_WITHHOLD_LOADS, 2)):
+    for opt, bad in ((H.WAIT_LIMIT, -1), (H.WAIT_LIMIT, 4000001), (H.TEST_WITHHOLD_LOADS, 3),
+                     (H.TEST_WITHHOLD_LOADS, -1)):
         with pytest.raises(H.HDCError):
             ctx.option(opt, bad)
