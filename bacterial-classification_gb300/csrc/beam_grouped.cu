@@ -578,14 +578,14 @@ constexpr int kSelLanes = 8;  // lanes per read in every select
 // The reads first, first + stride, ... of a warp's share: each group of kSelLanes lanes takes
 // every (32 / kSelLanes)-th of them.  `fin` (optional) runs on the group's lane 0 after a read's
 // beam is taken.
-template <class Fin>
+template <int G = kSelLanes, class Fin>
 __device__ __forceinline__ void select_reads(const GArgs& a, int L, int64_t first, int64_t end, int64_t stride,
                                              Fin fin) {
-    constexpr int kGroups = 32 / kSelLanes;
-    const int lane = threadIdx.x & 31, grp = lane / kSelLanes, gl = lane % kSelLanes;
-    const uint32_t gmask = ((1u << kSelLanes) - 1u) << (grp * kSelLanes);
+    constexpr int kGroups = 32 / G;
+    const int lane = threadIdx.x & 31, grp = lane / G, gl = lane % G;
+    const uint32_t gmask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << (grp * G);
     for (int64_t r = first + grp * stride; r < end; r += kGroups * stride) {
-        select_group<kSelLanes>(a, L, r, gl, gmask);
+        select_group<G>(a, L, r, gl, gmask);
         __syncwarp(gmask);
         if (gl == 0) fin(r);
     }
@@ -1736,7 +1736,8 @@ __global__ void __launch_bounds__(kScoreThreads, ROWS16 ? kScoreBlocks16 : kLeaf
     }
     __syncthreads();
     if (!ok_s) return;
-    select_reads(a, l.L, w, a.nq, nw, [&](int64_t r) { output_one(a, r, l.path, l.path_score, l.depth); });
+    // 16 lanes a read here: the scoring phase's registers leave no room for 8 keys a lane
+    select_reads<16>(a, l.L, w, a.nq, nw, [&](int64_t r) { output_one(a, r, l.path, l.path_score, l.depth); });
 }
 
 __global__ void __launch_bounds__(TcOne::kThreads, 1) descent_one_kernel(const GArgs a, const TcItems t, const OneArgs o) {
