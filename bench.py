@@ -17,6 +17,14 @@ which is available here):
   c3  precision form: 200,000 leaf references, each the bundle of 8 noisy
       copies (1% substitutions) of its leaf, D=10240, k=10; reads of 250 bp
       with 1% substitutions, bipolar queries, top-5
+  c4  batching form: c3's database, reads of log-normal length (100-1600 bp),
+      20% with 6% substitutions and indels, top-10, CUDA-graph pipeline
+  c5  hierarchical descent: 500,000 leaves + every internal prototype of a
+      6-rank tree, D=16384, k=12, c4's reads, top-5 per rank root to leaf;
+      a step is the read encode and the descent (two cooperative launches by
+      default; --beam-one selects the other forms)
+  aux the kernels beside the hot path (FASTA ingest, packing, similarity,
+      identify, greedy selection), each timed once
 
 --impl reference times the reference CPU algorithm (the C restatement in
 oracle/, the reference's own sources being unavailable on the GPU host) on
@@ -59,7 +67,7 @@ CONFIGS = {
                mixed_frac=0.2, mixed_rate=0.06),
     # hierarchical descent: 500,000 leaves + internal prototypes (exact int32 sums of their
     # children, bottom-up over the 6 ranks), D=16,384, k=12; config-4 read distribution;
-    # beam 5 per rank, root to leaf (no early stop), in one launch per batch
+    # beam 5 per rank, root to leaf (no early stop), in two cooperative launches per batch
     "c5": dict(n_leaves=500000, dim=16384, kmer=12, read_len=250, subst=0.01, topk=5, copies=0, bipolar=True,
                tree_seed=5, read_seed=105, sigma=0.5, min_read=100, max_read=1600, mixed_frac=0.2,
                mixed_rate=0.06, beam=5, levels=6, threshold=float("-inf")),
@@ -508,7 +516,7 @@ def build_prototypes(H, ctx, cfg, dev):
 
 def run_descent(args, cfg):
     """Hierarchical descent: per step, encode a batch of reads to +1/-1 int8
-    and run the beam descent over the resident prototypes (one launch)."""
+    and run the beam descent over the resident prototypes."""
     import torch
     import hdc_gb300 as H
     dev = torch.device("cuda", 0)
