@@ -618,9 +618,10 @@ __global__ void output_kernel(const GArgs a, int32_t* __restrict__ path, float* 
 // Levels above the leaves score on the tensor cores, grouped by parent: the entries (read,
 // beam slot) whose beam row is node P are scored against P's children (a childless P
 // against itself) as one dense [entries] x [children] product.  A work item is up to 128
-// entries x 32 children of one parent.  Eight producer warps (two groups of four on alternate
-// K blocks) write the entries' +1/-1 signs (from the packed bits) as fp16 straight into TMEM
-// with tcgen05.st (the A operand: lane = entry, two signs a column), and the children's int32
+// entries x 32 children of one parent.  Producer warps, in groups of four taking every G-th K
+// block (TcLayout: three groups in the level kernel, two in the one-launch kernel), write the
+// entries' +1/-1 signs (from the packed bits) as fp16 straight into TMEM with tcgen05.st (the
+// A operand: lane = entry, two signs a column), and the children's int32
 // prototype rows, split into three balanced base-2048 fp16 limbs, into 128-byte-swizzled
 // shared memory (the B operand); one thread issues M128 x N96 x K16 tcgen05 MMAs with A from
 // TMEM, the three limb tiles side by side, into one fp32 TMEM accumulator of 32 columns per

@@ -690,8 +690,8 @@ def descent_phases(ms, levels, grouped_tc=True, apart=False):
     """Per-level times (ms) of a one-launch descent from its phase clock: a level's
     phases end at its scoring; the select of a level is counted with the next.  With the
     last level apart (the default) the cooperative launch ends at that level's
-    node-ordered pairs; leaf_score_kernel and select_output_kernel, timed with the
-    call, score them and take the final beams."""
+    node-ordered pairs; leaf_kernel, a second cooperative launch timed with the
+    call, scores them and takes the final beams."""
     names = ["setup"]
     for L in range(levels):
         tcl = grouped_tc and L < levels - 1
