@@ -36,6 +36,7 @@ constexpr int kKT = 32;        // dims per K tile
 constexpr int kThreadsP = 256;  // 16 x 16 threads
 constexpr int kBR = 128;        // references per CTA tile
 constexpr int kMaxK = 32;       // largest top-k
+constexpr int64_t kPlainWideTileRefs = 16384;  // int32 form: 4 x 8 register tiles from this many references on
 
 // ---------------------------------------------------------------- norms
 __device__ __forceinline__ int64_t as_i64(int8_t x) { return x; }
@@ -87,9 +88,12 @@ __device__ __forceinline__ int32_t fold_bits(float acc) { return __float_as_int(
 constexpr int32_t kMagicBits = 0x4B400000;
 
 template <int TQ, bool WIDE, bool VEC>
-// Two CTAs per SM for the int32 accumulators (4 queries x 8 references a thread, 127
+// Two CTAs per SM for the int32 accumulators with 4 queries x 8 references a thread (127
 // registers): more warps to hide the shared-memory loads than one CTA of 8 x 8 tiles at 248
-// registers (c2: 47,850 -> 49,543 reads/s); the int64 form keeps one (it would spill).
+// registers (c2, 50,000 references: 47,850 -> 49,543 reads/s).  Against few references the
+// 8 x 8 tiles stay faster (c1, 2,000 references: 841,788 against 584,322 reads/s): four
+// threads per query instead of two keep top-k lists whose inserts and merge then weigh more
+// than the dots.  The int64 form keeps one CTA (it would spill).
 __global__ void __launch_bounds__(kThreadsP, (TQ == 4 && !WIDE) ? 2 : 1) plain_kernel(const PlainArgs a) {
     constexpr int BQ = TQ * 16;          // queries per CTA tile
     constexpr int QLD = BQ + 4, RLD = kBR + 4;
@@ -424,7 +428,7 @@ int launch_search_plain(hdc_context* ctx, const int16_t* d_q, const int64_t* d_q
     const bool wide = prod * (int64_t)ctx->dim >= ((int64_t)1 << 31);
     const bool vec = (ctx->dim % 8 == 0) && ((reinterpret_cast<uintptr_t>(d_q) & 15) == 0) &&
                      ((reinterpret_cast<uintptr_t>(d_r) & 15) == 0);
-    const int tq = 4;
+    const int tq = wide || nr >= kPlainWideTileRefs ? 4 : 8;
     PlainArgs a{};
     a.q = d_q;
     a.qn = d_qn;
@@ -448,7 +452,8 @@ int launch_search_plain(hdc_context* ctx, const int16_t* d_q, const int64_t* d_q
     if (wide)
         st = vec ? launch_plain_t<4, true, true>(a, nq, stream) : launch_plain_t<4, true, false>(a, nq, stream);
     else
-        st = vec ? launch_plain_t<4, false, true>(a, nq, stream) : launch_plain_t<4, false, false>(a, nq, stream);
+        st = tq == 4 ? (vec ? launch_plain_t<4, false, true>(a, nq, stream) : launch_plain_t<4, false, false>(a, nq, stream))
+                     : (vec ? launch_plain_t<8, false, true>(a, nq, stream) : launch_plain_t<8, false, false>(a, nq, stream));
     if (st != HDC_OK) return st;
     return launch_merge(a.ws_key, a.ws_dot, a.n_splits, nq, k, d_qn, d_rn, nr, d_score, d_idx, d_cos, d_dot, stream);
 }
