@@ -36,7 +36,10 @@ constexpr int kKT = 32;        // dims per K tile
 constexpr int kThreadsP = 256;  // 16 x 16 threads
 constexpr int kBR = 128;        // references per CTA tile
 constexpr int kMaxK = 32;       // largest top-k
-constexpr int64_t kPlainWideTileRefs = 16384;  // int32 form: 4 x 8 register tiles from this many references on
+// int32 form: 4 x 8 register tiles where the fp32 partials are folded at least every 256 dims
+// (count-valued queries) and there are at least this many references
+constexpr int64_t kPlainWideTileRefs = 16384;
+constexpr int kPlainFoldTile = 64;
 
 // ---------------------------------------------------------------- norms
 __device__ __forceinline__ int64_t as_i64(int8_t x) { return x; }
@@ -90,10 +93,12 @@ constexpr int32_t kMagicBits = 0x4B400000;
 template <int TQ, bool WIDE, bool VEC>
 // Two CTAs per SM for the int32 accumulators with 4 queries x 8 references a thread (127
 // registers): more warps to hide the shared-memory loads than one CTA of 8 x 8 tiles at 248
-// registers (c2, 50,000 references: 47,850 -> 49,543 reads/s).  Against few references the
-// 8 x 8 tiles stay faster (c1, 2,000 references: 841,788 against 584,322 reads/s): four
-// threads per query instead of two keep top-k lists whose inserts and merge then weigh more
-// than the dots.  The int64 form keeps one CTA (it would spill).
+// registers, when the fp32 partials are folded often (c2, count-valued reads against 50,000
+// references: 47,850 -> 49,543 reads/s).  Otherwise the 8 x 8 tiles stay faster: with few
+// references (c1, 2,000: 841,788 against 584,322 reads/s) four threads per query keep top-k
+// lists whose inserts and merge weigh more than the dots, and with rare folds (c3's bipolar
+// queries: 8,497 against 6,760) the larger tiles' fewer shared-memory loads per FMA win.
+// The int64 form keeps one CTA (it would spill).
 __global__ void __launch_bounds__(kThreadsP, (TQ == 4 && !WIDE) ? 2 : 1) plain_kernel(const PlainArgs a) {
     constexpr int BQ = TQ * 16;          // queries per CTA tile
     constexpr int QLD = BQ + 4, RLD = kBR + 4;
@@ -428,7 +433,7 @@ int launch_search_plain(hdc_context* ctx, const int16_t* d_q, const int64_t* d_q
     const bool wide = prod * (int64_t)ctx->dim >= ((int64_t)1 << 31);
     const bool vec = (ctx->dim % 8 == 0) && ((reinterpret_cast<uintptr_t>(d_q) & 15) == 0) &&
                      ((reinterpret_cast<uintptr_t>(d_r) & 15) == 0);
-    const int tq = wide || nr >= kPlainWideTileRefs ? 4 : 8;
+    const int tq = wide || (fold_groups <= kPlainFoldTile && nr >= kPlainWideTileRefs) ? 4 : 8;
     PlainArgs a{};
     a.q = d_q;
     a.qn = d_qn;
