@@ -541,10 +541,12 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                             if (!__any_sync(0xffffffffu, pass)) continue;  // the common case: no lane
                             const double rsc = __shfl_sync(0xffffffffu, rs_lane, c);
                             if (!pass) continue;
+                            // each limb sum is an integer of magnitude <= 2^24: a 32-bit
+                            // conversion is exact and stays off the FP64 pipe
                             int64_t dot = 0;
 #pragma unroll
                             for (int l = 0; l < L; ++l)
-                                dot += (int64_t)__float2ll_rn(__uint_as_float(v[l][c])) * ((int64_t)1 << (a.limb_bits * l));
+                                dot += (int64_t)__float2int_rn(__uint_as_float(v[l][c])) * ((int64_t)1 << (a.limb_bits * l));
                             const int64_t gr = rbase + c;
                             const float s = exact_score_sqrt(dot, my_sq[m], rsc, a.mode);
                             const uint64_t key = make_key(s, (uint32_t)gr);

@@ -66,12 +66,16 @@ constexpr float kFilterMargin = 4e-6f;
 
 // The same score from sq = sqrt(nq) and sr = sqrt(nr), each already rounded to
 // double (0 for a zero norm): the identical sequence of IEEE operations, with
-// the two square roots computed once per query and per reference.
+// the two square roots computed once per query and per reference.  Two steps
+// leave the FP64 pipe with identical results: the zero tests read the bits (a
+// square root of a non-negative integer is +0 or positive), and NORM scales by 2
+// after the rounding to float, which commutes with it here (|c - 0.5| is 0 or at
+// least 2^-54, far from float's subnormals, and far below overflow).
 __device__ __forceinline__ float exact_score_sqrt(int64_t dot, double sq, double sr, int mode) {
     if (mode == HDC_SCORE_DOT) return __ll2float_rn(dot);
-    if (sq == 0.0 || sr == 0.0) return -1.0f;
+    if (__double_as_longlong(sq) == 0 || __double_as_longlong(sr) == 0) return -1.0f;
     const double c = __ddiv_rn((double)dot, __dmul_rn(sq, sr));
-    if (mode == HDC_SCORE_NORM) return __double2float_rn(__dmul_rn(2.0, __dadd_rn(c, -0.5)));
+    if (mode == HDC_SCORE_NORM) return 2.0f * __double2float_rn(__dadd_rn(c, -0.5));
     return __double2float_rn(c);
 }
 
