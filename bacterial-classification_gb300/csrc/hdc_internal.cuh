@@ -56,7 +56,7 @@ struct hdc_refdb {
     __half* d_limbs = nullptr;  // [L][r_pad][dim]
     int64_t* d_norm2 = nullptr; // [nr]
     float* d_rsq = nullptr;     // [nr]
-    double* d_sqrt = nullptr;   // [nr] sqrt(norm2) rounded to double (the exact score's factor)
+    double* d_sqrt = nullptr;   // [2][nr] sqrt(norm2) rounded to double (the exact score's factor), then its rounded reciprocal
     int32_t limb_max[4] = {0, 0, 0, 0};
     int limb_bits = 11;         // limbs are balanced base-2^limb_bits digits (the top one within the cap)
     int32_t max_abs = 0;

@@ -99,6 +99,7 @@ struct TcArgs {
     int64_t* ws_dot;
     int* status;          // device status word (0 = ok)
     const double* rs;     // [nr] sqrt(norm2) of the references
+    const double* ri;     // [nr] their rounded reciprocals (0 for a zero norm)
     // [S][nq] the orderable k-th best score of each reference lane's list (0: not full),
     // zeroed before the launch; null when the lanes do not exchange them
     uint32_t* lane_kth;
@@ -483,7 +484,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             const int qt = grp * a.G + gslot;  // past the last tile for a CTA without one: no live rows
             // this thread owns query row `row` of each M-block
             int64_t gq[MB];
-            double my_sq[MB];
+            double my_sq[MB], my_iq[MB];
             float my_rq[MB], thr[MB];
             uint32_t other_kth[MB], told[MB];  // best k-th of the other lanes; the value this lane last told
             bool live[MB];
@@ -494,6 +495,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 const int64_t qn = live[m] ? a.qn[gq[m]] : 0;
                 my_rq[m] = rsqrt_norm(qn);
                 my_sq[m] = __dsqrt_rn((double)qn);
+                my_iq[m] = qn ? __drcp_rn(my_sq[m]) : 0.0;
                 thr[m] = -INFINITY;
                 other_kth[m] = 0;
                 told[m] = 0;
@@ -526,6 +528,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         const bool in_lane = rbase + lane < a.nr;
                         const float rr_lane = in_lane ? __ldg(a.rr + rbase + lane) : 0.0f;
                         const double rs_lane = in_lane ? __ldg(a.rs + rbase + lane) : 0.0;
+                        const double ri_lane = in_lane ? __ldg(a.ri + rbase + lane) : 0.0;
 #pragma unroll
                         for (int c = 0; c < 32; ++c) {
                             const float rrc = __shfl_sync(0xffffffffu, rr_lane, c);
@@ -540,6 +543,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                             const bool pass = ap >= thr[m] && live[m] && rbase + c < a.nr;
                             if (!__any_sync(0xffffffffu, pass)) continue;  // the common case: no lane
                             const double rsc = __shfl_sync(0xffffffffu, rs_lane, c);
+                            const double ric = __shfl_sync(0xffffffffu, ri_lane, c);
                             if (!pass) continue;
                             // each limb sum is an integer of magnitude <= 2^24: a 32-bit
                             // conversion is exact and stays off the FP64 pipe
@@ -548,7 +552,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                             for (int l = 0; l < L; ++l)
                                 dot += (int64_t)__float2int_rn(__uint_as_float(v[l][c])) * ((int64_t)1 << (a.limb_bits * l));
                             const int64_t gr = rbase + c;
-                            const float s = exact_score_sqrt(dot, my_sq[m], rsc, a.mode);
+                            const float s = exact_score_recip(dot, my_sq[m], rsc, my_iq[m], ric, a.mode);
                             const uint64_t key = make_key(s, (uint32_t)gr);
                             // below another lane's k-th best: k better references already exist
                             if (key <= kth[m] || (uint32_t)(key >> 32) < other_kth[m]) continue;
@@ -664,7 +668,11 @@ __global__ void rsqrt_kernel(const int64_t* __restrict__ n2, int64_t n, float* _
 
 __global__ void sqrt_kernel(const int64_t* __restrict__ n2, int64_t n, double* __restrict__ out) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = __dsqrt_rn((double)n2[i]);
+    if (i < n) {
+        const double s = __dsqrt_rn((double)n2[i]);
+        out[i] = s;
+        out[n + i] = n2[i] ? __drcp_rn(s) : 0.0;
+    }
 }
 
 // cuTensorMapEncodeTiled resolved through the runtime, so the library does not
@@ -788,7 +796,7 @@ void refdb_destroy(hdc_refdb* db) {
 }
 
 int refdb_sqrt_table(hdc_refdb* db, cudaStream_t stream) {
-    cudaError_t e = cudaMalloc(&db->d_sqrt, (size_t)db->nr * sizeof(double));
+    cudaError_t e = cudaMalloc(&db->d_sqrt, 2 * (size_t)db->nr * sizeof(double));
     if (e != cudaSuccess) return cuda_fail(e, "refdb: allocation");
     sqrt_kernel<<<(unsigned)((db->nr + 255) / 256), 256, 0, stream>>>(db->d_norm2, db->nr, db->d_sqrt);
     e = cudaGetLastError();
@@ -1036,6 +1044,7 @@ static int search_part(hdc_context* ctx, const hdc_refdb* db, const __half* d_q,
         if (e != cudaSuccess) return cuda_fail(e, "tc search: clear lane thresholds");
     }
     a.rs = db->d_sqrt;
+    a.ri = db->d_sqrt + db->nr;
     a.limb_bits = db->limb_bits;
     a.limb_base = (float)(1 << db->limb_bits);
     a.status = d_status;

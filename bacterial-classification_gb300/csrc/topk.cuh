@@ -79,6 +79,43 @@ __device__ __forceinline__ float exact_score_sqrt(int64_t dot, double sq, double
     return __double2float_rn(c);
 }
 
+// True when the double t lies more than 2^-50 from every midpoint between two
+// adjacent floats, so that any value within 2^-50 of t rounds to the same float.
+// The midpoints of t's binade have the 29 low mantissa bits 1000...0; 2^-50 is
+// 2^(1025 - e) units of that binade (e the biased exponent).  Binades below
+// 2^-27 (and zero) are never "far": the margin would not fit in those bits.
+__device__ __forceinline__ bool far_from_float_midpoint(double t) {
+    const uint64_t b = (uint64_t)__double_as_longlong(t);
+    const int e = (int)((b >> 52) & 0x7ff);
+    const int64_t d = (int64_t)(b & 0x1fffffffull) - (int64_t)(1 << 28);
+    return e >= 998 && e <= 1024 && (d < 0 ? -d : d) > ((int64_t)1 << (1025 - e));
+}
+
+// exact_score_sqrt with the divide replaced by a reciprocal product and one
+// correction, given also iq = fl(1/sq) and ir = fl(1/sr) (0 for a zero norm).
+// y = fl(iq * ir) is within a few units in the last place of 1/p, p = fl(sq * sr),
+// so q0 = fl(dot * y) is too; the residual dot - q0 * p (one FMA) and
+// q1 = fl(q0 + residual * y) (the Newton correction of Markstein's division) put
+// q1 within one unit of fl(dot / p), i.e. within 2^-52 of the quotient the
+// reference rounds for |c| <= 1 (2^-51 with NORM's subtraction).  When the value
+// to be rounded to float lies more than 2^-50 from every float midpoint, its
+// rounding equals that of the reference's value; otherwise (a window of 2^-49
+// around each midpoint, rarely met) the exact sequence runs.
+__device__ __forceinline__ float exact_score_recip(int64_t dot, double sq, double sr, double iq, double ir,
+                                                   int mode) {
+    if (mode == HDC_SCORE_DOT) return __ll2float_rn(dot);
+    if (__double_as_longlong(sq) == 0 || __double_as_longlong(sr) == 0) return -1.0f;
+    const double x = (double)dot, p = __dmul_rn(sq, sr), y = __dmul_rn(iq, ir);
+    const double q0 = __dmul_rn(x, y);
+    const double q1 = __fma_rn(__fma_rn(-q0, p, x), y, q0);
+    const double t = mode == HDC_SCORE_NORM ? __dadd_rn(q1, -0.5) : q1;
+    if (far_from_float_midpoint(t)) {
+        const float f = __double2float_rn(t);
+        return mode == HDC_SCORE_NORM ? 2.0f * f : f;
+    }
+    return exact_score_sqrt(dot, sq, sr, mode);
+}
+
 __device__ __forceinline__ float approx_score(float dotf, float rq, float rr, int mode) {
     if (mode == HDC_SCORE_DOT) return dotf;
     const float c = dotf * rq * rr;  // rq/rr are 0 for zero norms

@@ -100,6 +100,59 @@ def test_tc_exact_worst_case_accumulators(hdc, orc, cuda):
     assert np.array_equal(d, od) and np.array_equal(i, oi)
 
 
+def _vector_with_sums(g, n, s1, s2):
+    """An integer vector of length n with sum s1 and sum of squares s2 exactly:
+    n - 3 random entries, then the last three from a perfect-square condition."""
+    import math
+    mean = s1 / n
+    sd = math.sqrt(s2 / n - mean * mean)
+    c = np.arange(-3 * int(sd), 3 * int(sd) + int(mean) + 1, dtype=np.int64)
+    for _ in range(200):
+        r = np.rint(g.normal(mean, sd, n - 3)).astype(np.int64)
+        u1 = s1 - int(r.sum()) - c
+        x = 2 * (s2 - int((r * r).sum()) - c * c) - u1 * u1
+        ok = x >= 0
+        s = np.floor(np.sqrt(np.where(ok, x, 0).astype(np.float64))).astype(np.int64)
+        for dd in (-1, 0, 1):
+            hit = ok & (s + dd >= 0) & ((s + dd) ** 2 == x) & (((u1 + s + dd) & 1) == 0)
+            if hit.any():
+                j = int(np.flatnonzero(hit)[0])
+                sq = int(s[j] + dd)
+                out = np.concatenate([r, [int(c[j]), (int(u1[j]) + sq) // 2, (int(u1[j]) - sq) // 2]])
+                assert int(out.sum()) == s1 and int((out * out).sum()) == s2
+                return out
+    raise RuntimeError("no vector with these sums")
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_tc_scores_at_float_midpoints(hdc, orc, cuda, mode):
+    """Cosines exactly on a midpoint between two floats, and their neighbours.
+
+    With an all-ones query of dim 4096 (sqrt(nq) = 64) and references of norm2
+    4^21 (sqrt = 2^21) the cosine is dot / 2^27 exactly, so dots can place it (or
+    NORM's c - 0.5) on a float midpoint, where the reference's rounding ties to
+    even and the search's reciprocal-product score must defer to the exact
+    divide; the neighbours (dot +- 2) take the fast path.  Negated queries give
+    the mirrored cosines."""
+    g = np.random.default_rng(21)
+    dim = 4096
+    mids = [2**26 + 4, 2**26 + 12, 3 * 2**25 + 2, 3 * 2**25 + 6, 2**25 - 2]
+    dots = mids + [x + d for x in mids for d in (-2, 2)]
+    refs = np.stack([_vector_with_sums(g, dim, x, 4**21) for x in dots]).astype(np.int32)
+    q = np.ones((2, dim), np.int8)
+    q[1] = -1
+    # the construction: COS 0.5 + 2^-25 ties down to 0.5, NORM 2 (0.25 + 2^-26) to 0.5
+    assert np.float32(mids[0] / 2.0**27) == np.float32(0.5)
+    assert np.float32(2 * (mids[2] / 2.0**27 - 0.5)) == np.float32(0.5)
+    ctx, db, tr, q16, qi, qn = _setup(hdc, cuda, refs, q, dim)
+    k = len(dots)
+    s, i, c, d = _run_tc(ctx, db, q16, qn, 1, k, mode)
+    os_, oi, oc, od = orc.topk(q.astype(np.int32), refs.astype(np.int32), k, mode)
+    assert np.array_equal(d, od) and np.array_equal(i, oi)
+    assert np.array_equal(s.view(np.uint32), os_.view(np.uint32))
+    assert np.array_equal(c, oc)
+
+
 def test_tc_rejects_inexact_range(hdc, cuda):
     import torch
     dim = 16384 + 64
