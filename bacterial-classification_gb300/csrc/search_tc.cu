@@ -529,6 +529,9 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                         const float rr_lane = in_lane ? __ldg(a.rr + rbase + lane) : 0.0f;
                         const double rs_lane = in_lane ? __ldg(a.rs + rbase + lane) : 0.0;
                         const double ri_lane = in_lane ? __ldg(a.ri + rbase + lane) : 0.0;
+                        // the fp32 filter over the chunk's 32 columns (unrolled, no slow path in
+                        // between, so the loop stays small in the instruction cache) ...
+                        uint32_t pm = 0;  // this lane's columns that pass
 #pragma unroll
                         for (int c = 0; c < 32; ++c) {
                             const float rrc = __shfl_sync(0xffffffffu, rr_lane, c);
@@ -540,25 +543,40 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                                 af = fmaf(__uint_as_float(v[l][c]), scale, af);
                             }
                             const float ap = approx_tc(af, my_rq[m], rrc, a.mode);
-                            const bool pass = ap >= thr[m] && live[m] && rbase + c < a.nr;
-                            if (!__any_sync(0xffffffffu, pass)) continue;  // the common case: no lane
+                            pm |= (uint32_t)(ap >= thr[m] && live[m] && rbase + c < a.nr) << c;
+                        }
+                        // ... then one copy of the exact path for each column any lane passed, its
+                        // limb sums read again from TMEM (the accumulator is held until the arrival
+                        // below).  The threshold of the chunk's later columns is the one of its
+                        // start: a few more candidates, all decided by the exact key.
+                        uint32_t wm = __reduce_or_sync(0xffffffffu, pm);
+                        while (wm) {
+                            const int c = __ffs(wm) - 1;
+                            wm &= wm - 1;
+                            uint32_t vc[L];
+#pragma unroll
+                            for (int l = 0; l < L; ++l) vc[l] = tc::tmem_ld1(d0 + (uint32_t)((m * L + l) * kBN + c0 + c));
+                            tc::tmem_ld_wait();
                             const double rsc = __shfl_sync(0xffffffffu, rs_lane, c);
                             const double ric = __shfl_sync(0xffffffffu, ri_lane, c);
-                            if (!pass) continue;
-                            // each limb sum is an integer of magnitude <= 2^24: a 32-bit
-                            // conversion is exact and stays off the FP64 pipe
-                            int64_t dot = 0;
+                            if ((pm >> c) & 1u) {
+                                // each limb sum is an integer of magnitude <= 2^24: a 32-bit
+                                // conversion is exact and stays off the FP64 pipe
+                                int64_t dot = 0;
 #pragma unroll
-                            for (int l = 0; l < L; ++l)
-                                dot += (int64_t)__float2int_rn(__uint_as_float(v[l][c])) * ((int64_t)1 << (a.limb_bits * l));
-                            const int64_t gr = rbase + c;
-                            const float s = exact_score_recip(dot, my_sq[m], rsc, my_iq[m], ric, a.mode);
-                            const uint64_t key = make_key(s, (uint32_t)gr);
-                            // below another lane's k-th best: k better references already exist
-                            if (key <= kth[m] || (uint32_t)(key >> 32) < other_kth[m]) continue;
-                            list_insert_strided(lk[m], ld[m], ls, k, key, dot);
-                            kth[m] = lk[m][(k - 1) * ls];
-                            if (kth[m] != 0) thr[m] = fmaxf(thr[m], filter_below(key_score(kth[m]), a.mode));
+                                for (int l = 0; l < L; ++l)
+                                    dot += (int64_t)__float2int_rn(__uint_as_float(vc[l])) * ((int64_t)1 << (a.limb_bits * l));
+                                const int64_t gr = rbase + c;
+                                const float s = exact_score_recip(dot, my_sq[m], rsc, my_iq[m], ric, a.mode);
+                                const uint64_t key = make_key(s, (uint32_t)gr);
+                                // below another lane's k-th best: k better references already exist
+                                if (key > kth[m] && (uint32_t)(key >> 32) >= other_kth[m]) {
+                                    list_insert_strided(lk[m], ld[m], ls, k, key, dot);
+                                    kth[m] = lk[m][(k - 1) * ls];
+                                    if (kth[m] != 0) thr[m] = fmaxf(thr[m], filter_below(key_score(kth[m]), a.mode));
+                                }
+                            }
+                            __syncwarp();  // converged for the next column's warp-wide TMEM load
                         }
                     }
                 }
