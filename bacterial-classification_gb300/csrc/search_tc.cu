@@ -126,6 +126,41 @@ __device__ __forceinline__ void list_insert_strided(uint64_t* keys, int64_t* dot
 // Filter threshold below a k-th best score sk: the fp32 estimate of any score
 // that can still beat sk is at least this (DOT estimates are within a
 // relative 4e-6 plus one unit).
+// Insert (key, dot) into a descending list of k <= KR keys held in registers
+// (keys[i] for i < k, 0 = empty), dropping the last entry, and return the new
+// last key.  The dots live in k slots at dots[slot * st]: nibble i of `slots` is
+// the slot of entry i, and the entry that drops out hands its slot to the new
+// dot.  Every index is a compile-time constant after unrolling, so the keys stay
+// in registers and an insertion costs one shared-memory store.
+template <int KR>
+__device__ __forceinline__ uint64_t reg_insert(uint64_t (&keys)[KR], uint64_t& slots, int k, uint64_t key, int64_t dot,
+                                               int64_t* dots, int st) {
+    static_assert(KR <= 16, "slots are nibbles of one word");
+    int pos = 0;
+#pragma unroll
+    for (int i = 0; i < KR - 1; ++i) pos += (i < k - 1 && keys[i] > key) ? 1 : 0;
+    // shift entries pos..k-2 down one place and put the key at pos, as masked selects
+    // (a plain "if (i == pos)" is folded back into a dynamic index, which would move
+    // the array to local memory)
+#pragma unroll
+    for (int i = KR - 1; i >= 0; --i) {
+        const uint64_t prev = i > 0 ? keys[i > 0 ? i - 1 : 0] : 0;
+        const uint64_t sh = 0ull - (uint64_t)(i > pos && i < k);
+        const uint64_t at = 0ull - (uint64_t)(i == pos);
+        keys[i] = (keys[i] & ~(sh | at)) | (prev & sh) | (key & at);
+    }
+    const uint64_t freed = (slots >> (4 * (k - 1))) & 15u;
+    const uint64_t below = (1ull << (4 * pos)) - 1;                        // nibbles 0..pos-1
+    const uint64_t thru = pos >= 15 ? ~0ull : (1ull << (4 * pos + 4)) - 1;  // nibbles 0..pos
+    const uint64_t upto = k >= 16 ? ~0ull : (1ull << (4 * k)) - 1;         // nibbles 0..k-1
+    slots = (slots & below) | (freed << (4 * pos)) | ((slots << 4) & upto & ~thru) | (slots & ~upto);
+    dots[(int)freed * st] = dot;
+    uint64_t last = 0;
+#pragma unroll
+    for (int i = 0; i < KR; ++i) last |= keys[i] & (0ull - (uint64_t)(i == k - 1));
+    return last;
+}
+
 __device__ __forceinline__ float filter_below(float sk, int mode) {
     return mode == HDC_SCORE_DOT ? sk - (fabsf(sk) * 4e-6f + 1.0f) : sk - kFilterMargin;
 }
@@ -144,7 +179,7 @@ __device__ __forceinline__ float approx_tc(float af, float rq, float rr, int mod
 // the same two query tiles on two neighbouring reference lanes: each query block
 // is loaded once, half by each pair, and multicast into both, which also keeps
 // the two lanes in step (a lane with fewer tiles runs empty ones at the end).
-template <int L, int kBN, int MB, int CL, bool SHARE_A, int BKT, bool PAIR_MMA>
+template <int L, int kBN, int MB, int CL, bool SHARE_A, int BKT, bool PAIR_MMA, int KR>
 __global__ void __launch_bounds__(kThreadsTC, 1)
     tc_search_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcArgs a) {
     using T = Tile<kBN, BKT>;
@@ -152,6 +187,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
     static_assert(!PAIR_MMA || (L == 2 && kBN == 128 && MB == 1 && (CL == 2 || CL == 4) && !SHARE_A),
                   "pair MMA shape");
     static_assert(CL <= 2 || PAIR_MMA, "clusters of 4 pair the MMA");
+    static_assert(KR == 0 || (KR == 16 && MB == 1), "register lists: one M-block, k <= 16");
     constexpr bool QUAD = PAIR_MMA && CL == 4;
     constexpr int LS = PAIR_MMA ? 1 : L;  // limb blocks this CTA stages
     constexpr int STAGES = tc_stages<kBN, BKT>(LS, MB);
@@ -479,6 +515,9 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
             }
         }
         uint64_t kth[MB];  // each list's k-th key (0 while it has fewer than k entries)
+        // KR > 0: the keys of the (single) list in registers, its dots in slots of ld[0]
+        uint64_t rkeys[KR > 0 ? KR : 1];
+        uint64_t rslots = 0;
         for (int grp = 0; ok && grp < a.n_groups; ++grp) {
             if (grp * a.G + lead_slot >= a.n_qtiles) continue;
             const int qt = grp * a.G + gslot;  // past the last tile for a CTA without one: no live rows
@@ -499,9 +538,15 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 thr[m] = -INFINITY;
                 other_kth[m] = 0;
                 told[m] = 0;
-                for (int i = 0; i < k; ++i) {
-                    lk[m][i * ls] = 0;
-                    ld[m][i * ls] = 0;
+                if constexpr (KR > 0) {
+#pragma unroll
+                    for (int i = 0; i < KR; ++i) rkeys[i] = 0;
+                    rslots = 0xfedcba9876543210ull;  // entry i in slot i
+                } else {
+                    for (int i = 0; i < k; ++i) {
+                        lk[m][i * ls] = 0;
+                        ld[m][i * ls] = 0;
+                    }
                 }
                 kth[m] = 0;
             }
@@ -571,8 +616,12 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                                 const uint64_t key = make_key(s, (uint32_t)gr);
                                 // below another lane's k-th best: k better references already exist
                                 if (key > kth[m] && (uint32_t)(key >> 32) >= other_kth[m]) {
-                                    list_insert_strided(lk[m], ld[m], ls, k, key, dot);
-                                    kth[m] = lk[m][(k - 1) * ls];
+                                    if constexpr (KR > 0) {
+                                        kth[m] = reg_insert<KR>(rkeys, rslots, k, key, dot, ld[m], ls);
+                                    } else {
+                                        list_insert_strided(lk[m], ld[m], ls, k, key, dot);
+                                        kth[m] = lk[m][(k - 1) * ls];
+                                    }
                                     if (kth[m] != 0) thr[m] = fmaxf(thr[m], filter_below(key_score(kth[m]), a.mode));
                                 }
                             }
@@ -624,9 +673,18 @@ __global__ void __launch_bounds__(kThreadsTC, 1)
                 if (!live[m]) continue;
                 uint64_t* ok_ = a.ws_key + ((int64_t)lane_j * a.nq + gq[m]) * k;
                 int64_t* od = a.ws_dot + ((int64_t)lane_j * a.nq + gq[m]) * k;
-                for (int i = 0; i < k; ++i) {
-                    ok_[i] = lk[m][i * ls];
-                    od[i] = ld[m][i * ls];
+                if constexpr (KR > 0) {
+#pragma unroll
+                    for (int i = 0; i < KR; ++i)
+                        if (i < k) {
+                            ok_[i] = rkeys[i];
+                            od[i] = rkeys[i] ? ld[m][(int)((rslots >> (4 * i)) & 15u) * ls] : 0;
+                        }
+                } else {
+                    for (int i = 0; i < k; ++i) {
+                        ok_[i] = lk[m][i * ls];
+                        od[i] = ld[m][i * ls];
+                    }
                 }
             }
         }
@@ -976,7 +1034,8 @@ constexpr int kNoClusterFit = -1;  // launch_tc_t: the clusters cannot all be re
 // shared memory (its mbarriers and flags)
 constexpr size_t kMaxDynSmem = 226 * 1024;
 
-template <int L, int N, int MB, int CL, bool SHARE_A = false, int BKT = Tile<N>::BK, bool PAIR_MMA = false>
+template <int L, int N, int MB, int CL, bool SHARE_A = false, int BKT = Tile<N>::BK, bool PAIR_MMA = false,
+          int KR = 0>
 static int launch_tc_t(const __half* d_q, const hdc_refdb* db, const TcArgs& a, int grid, cudaStream_t stream) {
     CUtensorMap tmA, tmB;
     // with CL CTAs sharing a block by multicast, each loads 1 / CL of its rows; with pair
@@ -992,7 +1051,7 @@ static int launch_tc_t(const __half* d_q, const hdc_refdb* db, const TcArgs& a, 
     TcArgs args = a;
     args.slist = ring + lists <= kMaxDynSmem ? 1 : 0;
     const size_t smem = ring + (args.slist ? lists : 0);
-    auto kern = tc_search_kernel<L, N, MB, CL, SHARE_A, BKT, PAIR_MMA>;
+    auto kern = tc_search_kernel<L, N, MB, CL, SHARE_A, BKT, PAIR_MMA, KR>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return cuda_fail(e, "tc search: cudaFuncSetAttribute");
     if constexpr (CL == 1) {
@@ -1075,6 +1134,10 @@ static int search_part(hdc_context* ctx, const hdc_refdb* db, const __half* d_q,
     int st;
     const int MB = tc_m_blocks(ctx, db);
     const bool pair_mma = CL == 2 && !share && tc_pair_mma(ctx, db);
+    // register-resident lists for 8 < k <= 16 (measured on 200,000 references of
+    // D = 10,240: top-10 194.9K -> 200.6K reads/s, top-5 219.2K -> 215.1K, so
+    // k <= 8 keeps the shared-memory lists)
+    const bool kreg = k > 8 && k <= 16;
     if (N == 256) {
         switch (db->L) {
             case 1: st = launch_tc_t<1, 256, 1, 1>(d_q, db, a, grid, stream); break;
@@ -1093,13 +1156,16 @@ static int search_part(hdc_context* ctx, const hdc_refdb* db, const __half* d_q,
             default: st = launch_tc_t<4, 128, 1, 2, true>(d_q, db, a, grid, stream); break;
         }
     } else if (CL == 4) {
-        st = launch_tc_t<2, 128, 1, 4, false, 64, true>(d_q, db, a, grid, stream);
+        st = kreg ? launch_tc_t<2, 128, 1, 4, false, 64, true, 16>(d_q, db, a, grid, stream)
+                     : launch_tc_t<2, 128, 1, 4, false, 64, true>(d_q, db, a, grid, stream);
         if (st == kNoClusterFit) {
             CL = 2;
-            st = launch_tc_t<2, 128, 1, 2, false, 64, true>(d_q, db, a, grid, stream);
+            st = kreg ? launch_tc_t<2, 128, 1, 2, false, 64, true, 16>(d_q, db, a, grid, stream)
+                         : launch_tc_t<2, 128, 1, 2, false, 64, true>(d_q, db, a, grid, stream);
         }
     } else if (CL == 2 && pair_mma) {
-        st = launch_tc_t<2, 128, 1, 2, false, 64, true>(d_q, db, a, grid, stream);
+        st = kreg ? launch_tc_t<2, 128, 1, 2, false, 64, true, 16>(d_q, db, a, grid, stream)
+                     : launch_tc_t<2, 128, 1, 2, false, 64, true>(d_q, db, a, grid, stream);
     } else if (CL == 2 && kb32) {
         switch (db->L) {
             case 1: st = launch_tc_t<1, 128, 1, 2, false, 32>(d_q, db, a, grid, stream); break;
@@ -1138,7 +1204,7 @@ static int search_part(hdc_context* ctx, const hdc_refdb* db, const __half* d_q,
 
 static int quad_clusters_fit(const hdc_context* ctx) {
     if (ctx->tc_quad_fit >= 0) return ctx->tc_quad_fit;
-    auto kern = tc_search_kernel<2, 128, 1, 4, false, 64, true>;
+    auto kern = tc_search_kernel<2, 128, 1, 4, false, 64, true, 0>;
     const size_t smem = (size_t)tc_stages<128, 64>(1, 1) * tc_stage_bytes<128, 64>(1, 1) + 1024;
     int fit = 0;
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess) {

@@ -328,12 +328,13 @@ _LANE_ORACLE = {}
 # so many references score close to a query's best) with duplicated rows
 # placed in other lanes' tiles (equal scores across lanes: ties go to the
 # lower index) checks that no reference of the final top-k is dropped.
-# Forms: multicast pairs, pair MMAs, and clusters of 4 (two pair MMAs on two
-# lanes sharing query blocks; 3 lanes round down to 2, and 94 reference tiles
-# over 4 lanes leave two lanes an empty last tile).
+# With pair MMAs, k = 9..16 keeps the lists' keys in registers (k = 9 and 16
+# are its bounds).  Forms: multicast pairs, pair MMAs, and clusters of 4 (two
+# pair MMAs on two lanes sharing query blocks; 3 lanes round down to 2, and 94
+# reference tiles over 4 lanes leave two lanes an empty last tile).
 @pytest.mark.parametrize("lanes", [2, 3, 4, 8])
 @pytest.mark.parametrize("pair,cluster", [(0, 2), (1, 2), (1, 4)])
-@pytest.mark.parametrize("k,mode", [(1, 0), (5, 0), (32, 0), (5, 2), (10, 1)])
+@pytest.mark.parametrize("k,mode", [(1, 0), (5, 0), (32, 0), (5, 2), (10, 1), (9, 0), (16, 0)])
 def test_tc_lane_exchange_vs_oracle(hdc, orc, cuda, lanes, pair, cluster, k, mode):
     import hdc_gb300
     g = np.random.default_rng(100 + k)
